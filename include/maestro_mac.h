@@ -1,0 +1,208 @@
+/*
+ * maestro_mac.h -- C ABI of the GB300 (sm_103a) MAC projection.
+ *
+ * Drop-in for MAESTRO's MAC projection hot path:
+ *   subroutine macproject(mla, umac, phi, rho, dx, the_bc_tower,
+ *                         macrhs, beta0_1d, beta0_1d_edge, beta0_cart_edge)
+ *       Source/macproject.f90:51-76
+ *   subroutine mac_multigrid(mla, rh, phi, fine_flx, solver_alpha, solver_beta, dx,
+ *                            the_bc_tower, bc_comp, stencil_order,
+ *                            rel_solver_eps, abs_solver_eps)
+ *       Source/mac_multigrid.f90:18-37 (forwards to FBoxLib ml_cc_solve, :56-67)
+ *   subroutine cell_to_edge(s0_cell, s0_edge)
+ *       Source/cell_to_edge.f90:14
+ *
+ * Plain pointers and sizes only.  Every entry point returns MAC_OK (0) or a negative MAC_ERR_*
+ * code (the reference aborts through bl_error instead, Source/macproject.f90:99-109).
+ * A context is single-threaded: one host thread and one CUDA stream at a time.
+ *
+ * Data layout at the boundary is FBoxLib's: one Fortran-ordered fab per box, indexed
+ * (lo-ng : hi+ng) per direction, edge (face) fabs one longer in their own direction, cell
+ * multi-component fabs (..., ncomp).  Box bounds are 0-based inclusive cell indices (lwb/upb).
+ * In 2-D the vertical direction is y, in 3-D it is z (MAESTRO planar geometry).
+ */
+#ifndef MAESTRO_MAC_H
+#define MAESTRO_MAC_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------------ */
+#define MAC_OK                 0
+#define MAC_ERR_INVALID       -1   /* bad argument: sizes, boxes, BCs, null pointers          */
+#define MAC_ERR_CUDA          -2   /* a CUDA runtime call failed                               */
+#define MAC_ERR_NOT_CONVERGED -3   /* max_vcycles reached above the tolerance                  */
+#define MAC_ERR_NONFINITE     -4   /* NaN/Inf met in the right-hand side or the residual       */
+#define MAC_ERR_ALLOC         -5   /* device memory allocation failed                          */
+#define MAC_ERR_UNSUPPORTED   -6   /* geometry the solver does not handle (see mac_strerror)   */
+#define MAC_ERR_BAD_DENSITY   -7   /* rho <= 0 or non-finite (face coefficients undefined)     */
+#define MAC_ERR_TOO_LARGE     -8   /* size above a fixed limit of the entry point              */
+
+/* ---- boundary codes: FBoxLib bc_module numbering of ell_bc_level_array(...,press_comp) ---- */
+#define MAC_BC_PER  -1   /* periodic                                       */
+#define MAC_BC_INT   0   /* interior (not a domain boundary; rejected here) */
+#define MAC_BC_DIR   1   /* homogeneous Dirichlet on phi (outlet)          */
+#define MAC_BC_NEU   2   /* homogeneous Neumann on phi (walls, inlet, symmetry) */
+
+/* ---- precision of the solve ---------------------------------------------------------------- */
+#define MAC_PREC_FP64   0   /* FP64 V-cycles: the plain drop-in                                */
+#define MAC_PREC_MIXED  1   /* FP32 V-cycles inside FP64 iterative refinement                  */
+
+/* ---- where the caller's pointers live ------------------------------------------------------ */
+#define MAC_PTR_HOST    0
+#define MAC_PTR_DEVICE  1
+
+typedef struct mac_ctx mac_ctx;
+
+/* Single-level geometry: the domain, its cell size, the elliptic BCs of press_comp and the boxes
+ * of the layout (ml_layout / boxarray of the one level). */
+typedef struct mac_geom {
+    int dm;                 /* 2 or 3                                                          */
+    int domain_lo[3];       /* problem domain, inclusive cell indices (entries >= dm ignored)  */
+    int domain_hi[3];
+    double dx[3];           /* cell size per direction                                         */
+    int bc_lo[3];           /* MAC_BC_* on the low side of each direction                       */
+    int bc_hi[3];           /* MAC_BC_* on the high side                                        */
+    int nboxes;
+    const int* box_lo;      /* [nboxes*3] inclusive lower cell index of each box (x fastest)   */
+    const int* box_hi;      /* [nboxes*3] inclusive upper cell index                            */
+} mac_geom;
+
+/* Solver options; mac_default_opts() fills MAESTRO's MAC settings. */
+typedef struct mac_opts {
+    int precision;          /* MAC_PREC_FP64 / MAC_PREC_MIXED                                  */
+    int use_alt_energy_fix; /* solver coefficient beta0^2/rho instead of beta0/rho
+                               (Source/macproject.f90:189-192; probin default .true.)          */
+    double rel_eps;         /* relative tolerance on ||f - L phi||_inf / ||f||_inf;
+                               default min(eps_mac * 10^(nlevs-1), eps_mac_max) = 1e-10
+                               (Source/macproject.f90:217, Source/mg_eps.f90:23-28)            */
+    double abs_eps;         /* absolute tolerance (<= 0: off; the reference passes -1)         */
+    int max_vcycles;        /* V-cycles (FP64) or refinement iterations (mixed) before
+                               MAC_ERR_NOT_CONVERGED                                           */
+    int nu1, nu2;           /* GS-RB sweeps down / up the V-cycle (FBoxLib defaults 2, 2)      */
+    int nub;                /* sweeps before and after the bottom solve (mg_bottom_nu = 10)    */
+    double bottom_eps;      /* bottom BiCGStab relative tolerance (eps_mac_bottom = 1e-3)      */
+    int bottom_max_iter;    /* bottom BiCGStab iteration limit                                 */
+    int max_levels;         /* 0: coarsen every box down to 2 cells per side (FBoxLib rule);
+                               > 0: cap on the number of MG levels                             */
+    int use_graph;          /* capture each V-cycle in a CUDA graph (1) or launch directly (0) */
+    int verbose;            /* 0 silent, 1 per-solve summary on stderr                         */
+} mac_opts;
+
+typedef struct mac_stats {
+    int status;             /* return code of the call                                         */
+    int vcycles;            /* V-cycles run (mixed: equal to refine_iters)                      */
+    int refine_iters;       /* FP64 refinement iterations (mixed precision), else 0            */
+    int nlevels;            /* MG levels used                                                  */
+    int bottom_iters;       /* BiCGStab iterations summed over the solve                        */
+    double fnorm;           /* ||f||_inf of the solver right-hand side (after mean removal)    */
+    double resid0;          /* initial ||f - L phi||_inf                                       */
+    double rel_resid;       /* final ||f - L phi||_inf / ||f||_inf, FP64                       */
+    int nhist;
+    double hist[64];        /* relative residual after every V-cycle / refinement iteration    */
+    double setup_ms;        /* device time: layout conversion + coefficients + RHS             */
+    double solve_ms;        /* device time: multigrid                                          */
+    double total_ms;        /* wall time of the call                                           */
+} mac_stats;
+
+/* Fill *o with MAESTRO's MAC-projection defaults (FP64, alt energy fix off, 1e-10, V(2,2),
+ * nub = 10, bottom 1e-3). */
+void mac_default_opts(mac_opts* o);
+
+/* Human-readable text of a status code (static storage). */
+const char* mac_strerror(int code);
+
+/* Library version string (static storage). */
+const char* mac_version(void);
+
+/* Create a solver context for one level geometry; device buffers are allocated here and reused
+ * by every call.  `cuda_stream` is a cudaStream_t (NULL: the legacy default stream). */
+int mac_ctx_create(mac_ctx** out, const mac_geom* g, const mac_opts* o, void* cuda_stream);
+int mac_ctx_destroy(mac_ctx* ctx);
+/* Replace the options of an existing context (precision, tolerances, sweeps). */
+int mac_ctx_set_opts(mac_ctx* ctx, const mac_opts* o);
+/* Number of MG levels and the cell counts of each (n[3*l + d]); returns the level count. */
+int mac_ctx_levels(const mac_ctx* ctx, int* n_out /* [3*32] or NULL */);
+
+/*
+ * MAC projection, the drop-in for macproject (Source/macproject.f90:51-328), single level,
+ * planar (beta0_1d) or no-beta0 form.
+ *   umac[d*nboxes + b] : edge fab of box b normal to direction d, ng_u ghosts   (in/out)
+ *   phi[b]             : cell fab, ng_phi ghosts; initial guess in, solution out (in/out)
+ *   rho[b]             : cell state fab with rho_ncomp components, ng_rho ghosts; component
+ *                        rho_comp (0-based) is the density (rho_comp in Source/variables.f90:105)
+ *   macrhs[b]          : cell fab, ng_rhs ghosts, or NULL (no source term)
+ *   beta0_1d           : nr = domain extent in the vertical direction, or NULL
+ *   beta0_1d_edge      : nr + 1 edge values, NULL iff beta0_1d is NULL
+ * `ptr_kind` says whether all of these live in host or device memory.  On return the valid
+ * faces of umac hold the projected velocity; same-level and periodic ghost faces are refilled
+ * from the valid region (multifab_fill_boundary, Source/macproject.f90:245-251); physical-
+ * boundary ghosts are left to the caller (multifab_physbc_edgevel).
+ */
+int mac_macproject(mac_ctx* ctx, int ptr_kind,
+                   double* const* umac, int ng_u,
+                   double* const* phi, int ng_phi,
+                   const double* const* rho, int ng_rho, int rho_ncomp, int rho_comp,
+                   const double* const* macrhs, int ng_rhs,
+                   const double* beta0_1d, const double* beta0_1d_edge,
+                   mac_stats* stats);
+
+/*
+ * Elliptic solve, the drop-in for mac_multigrid (Source/mac_multigrid.f90:18-67):
+ *   (alpha - div beta grad) phi = rh
+ * with face coefficients beta[d*nboxes + b] (edge fabs, ng_beta ghosts) and optional cell
+ * alpha[b] (NULL: alpha = 0, the MAC case).  phi is the initial guess in / solution out.
+ * fine_flx is not returned: on one level the face flux beta grad phi is formed by the caller
+ * from phi (mac_macproject does so internally).
+ */
+int mac_multigrid(mac_ctx* ctx, int ptr_kind,
+                  const double* const* rh, int ng_rh,
+                  double* const* phi, int ng_phi,
+                  const double* const* alpha, int ng_alpha,
+                  const double* const* beta, int ng_beta,
+                  mac_stats* stats);
+
+/*
+ * Whole-domain variant of mac_macproject for callers that keep one array per field on the
+ * device (natural layout, x fastest, no ghosts): ux (nx+1,ny,nz), uy (nx,ny+1,nz),
+ * uz (nx,ny,nz+1) (uz unused in 2-D), phi/rho/macrhs (nx,ny,nz), beta0 (nr), beta0_edge (nr+1).
+ * All pointers are device pointers; macrhs/beta0/beta0_edge may be NULL as above.
+ * Same arithmetic as mac_macproject.  No counterpart in the reference (its fields always come
+ * boxed); it is the device-resident form of Source/macproject.f90:51-328.
+ */
+int mac_macproject_dense(mac_ctx* ctx, double* ux, double* uy, double* uz, double* phi,
+                         const double* rho, const double* macrhs, const double* beta0,
+                         const double* beta0_edge, mac_stats* stats);
+
+/*
+ * Adjoint (reverse-mode derivative) of the whole-domain MAC projection; no counterpart in the
+ * reference.  Forward map (beta0 form, p = 1 + use_alt_energy_fix):
+ *   U_proj = U - c .* G phi,  A phi = f,  A = D diag(beta_f) G  (negated, alpha = 0),
+ *   beta_f = beta0_f^p * 2/(rho_L + rho_R),  c = beta_f / beta0_f,
+ *   f = macrhs - D(beta0_f U).
+ * Given the cotangent w = dL/dU_proj (face arrays like U), returns
+ *   dU     = dL/dU            (face arrays, natural layout, device)
+ *   drinv  = dL/d(1/rho)      (cells, device; may be NULL)
+ *   dbeta0 = dL/d(beta0_1d)   (nr cells, device; may be NULL) -- beta0_edge is taken as a
+ *            function of beta0 through cell_to_edge, so this includes the edge path
+ *   dmacrhs= dL/d(macrhs)     (cells, device; may be NULL)
+ * The adjoint solve reuses the forward V-cycle (A is self-adjoint).  U, rho, macrhs, beta0 are
+ * the forward inputs (U before projection).  phi_out (may be NULL) receives the forward phi.
+ */
+int mac_macproject_adjoint_dense(mac_ctx* ctx,
+                                 const double* ux, const double* uy, const double* uz,
+                                 const double* rho, const double* macrhs,
+                                 const double* beta0, const double* beta0_edge,
+                                 const double* wx, const double* wy, const double* wz,
+                                 double* dux, double* duy, double* duz,
+                                 double* drinv, double* dbeta0, double* dmacrhs,
+                                 double* phi_out, mac_stats* stats);
+
+/* beta0 cell -> edge values (Source/cell_to_edge.f90:14-70), host arrays, one level. */
+int mac_cell_to_edge(int nr, const double* s0_cell, double* s0_edge);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MAESTRO_MAC_H */

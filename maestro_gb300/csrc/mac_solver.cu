@@ -1,0 +1,767 @@
+// Context, V-cycle driver, mixed-precision refinement loop and the C ABI of the GB300 MAC
+// projection.
+//
+// Solve structure (FBoxLib ml_cc as used by Source/mac_multigrid.f90:56-67, Docs/mg/mg.tex:325-375):
+//   FP64  : repeat { V(nu1,nu2)-cycle on (phi, f); ||f - L phi||_inf } until
+//           ||r|| <= rel_eps ||f|| (or abs_eps), at most max_vcycles times.
+//   MIXED : r = f - L phi in FP64 (stored FP32); repeat { e = FP32 V-cycle on (e, r) from e = 0,
+//           FP64 bottom solve; phi += e in FP64; r = f - L phi in FP64 } until converged.
+// Every V-cycle (with its convergence residual) is captured once into a CUDA graph and replayed;
+// the host reads one 8-byte max-norm per cycle.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <chrono>
+#include <mutex>
+#include <string>
+
+#include "mac_internal.cuh"
+
+namespace mac {
+
+namespace {
+thread_local std::string g_last_cuda;
+constexpr int kBlk = 256;
+
+double bits_to_double(unsigned long long b) {
+    double d;
+    std::memcpy(&d, &b, sizeof(d));
+    return d;
+}
+
+}  // namespace
+
+void set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), "%s: %s (%s:%d)", cudaGetErrorString(e), what, file, line);
+    g_last_cuda = buf;
+}
+
+int alloc_device(mac_ctx* c, void** p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) return MAC_OK;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return MAC_ERR_ALLOC;
+    }
+    c->allocations.push_back(*p);
+    c->bytes_allocated += bytes;
+    return MAC_OK;
+}
+
+namespace {
+
+template <typename T>
+int alloc_arr(mac_ctx* c, T** p, size_t n) {
+    return alloc_device(c, reinterpret_cast<void**>(p), n * sizeof(T));
+}
+
+int alloc_level_fp32(mac_ctx* c, Level& L) {
+    if (L.a32.bx) return MAC_OK;
+    const size_t n = L.d.ncell;
+    int rc = 0;
+    rc |= alloc_arr(c, &L.a32.phi, n);
+    rc |= alloc_arr(c, &L.a32.f, n);
+    rc |= alloc_arr(c, &L.a32.bx, n);
+    rc |= alloc_arr(c, &L.a32.by, n);
+    rc |= alloc_arr(c, &L.a32.bz, n);
+    rc |= alloc_arr(c, &L.a32.diag, n);
+    rc |= alloc_arr(c, &L.a32.invdiag, n);
+    return rc ? MAC_ERR_ALLOC : MAC_OK;
+}
+
+BcDesc bc_desc(const mac_ctx* c) {
+    BcDesc b;
+    for (int d = 0; d < 3; ++d) {
+        b.lo[d] = c->bc_lo[d];
+        b.hi[d] = c->bc_hi[d];
+    }
+    return b;
+}
+
+// Host-side recursion issuing one V-cycle on levels l..L-1 (FP64 or FP32 arrays).
+template <typename T>
+LevelArrays<T>& arrays(Level& L);
+template <>
+LevelArrays<double>& arrays<double>(Level& L) { return L.a64; }
+template <>
+LevelArrays<float>& arrays<float>(Level& L) { return L.a32; }
+
+template <typename T>
+void vcycle(mac_ctx* c, int l) {
+    Level& L = c->lev[l];
+    LevelArrays<T>& a = arrays<T>(L);
+    const mac_opts& o = c->o;
+    if (l == c->nlevels - 1) {
+        launch_bottom<T>(L.d, L.a64, a.phi, a.f, c->bottom_scratch, c->singular, o.nub,
+                         o.bottom_eps, o.bottom_max_iter, c->red.counters, c->stream);
+        return;
+    }
+    for (int s = 0; s < o.nu1; ++s) {
+        launch_gsrb<T>(L.d, 0, a, c->stream);
+        launch_gsrb<T>(L.d, 1, a, c->stream);
+    }
+    Level& C = c->lev[l + 1];
+    LevelArrays<T>& ac = arrays<T>(C);
+    launch_resid_restrict<T>(L.d, C.d, a, ac.f, o.nu1 > 0, c->stream);
+    cudaMemsetAsync(ac.phi, 0, sizeof(T) * C.d.ncell, c->stream);
+    vcycle<T>(c, l + 1);
+    launch_prolong_add<T>(L.d, C.d, bc_desc(c), ac.phi, a.phi, c->stream);
+    for (int s = 0; s < o.nu2; ++s) {
+        launch_gsrb<T>(L.d, 0, a, c->stream);
+        launch_gsrb<T>(L.d, 1, a, c->stream);
+    }
+}
+
+// One iteration of the outer loop, ending with the max-norm of the fine residual in
+// red.maxbits and its copy in pinned host memory.
+void issue_iteration(mac_ctx* c, int prec) {
+    Level& F = c->lev[0];
+    cudaMemsetAsync(c->red.maxbits, 0, sizeof(unsigned long long), c->stream);
+    if (prec == MAC_PREC_FP64) {
+        vcycle<double>(c, 0);
+        launch_resid_norm<double>(F.d, F.a64, c->o.nu2 > 0, c->red.maxbits, c->stream);
+    } else {
+        cudaMemsetAsync(F.a32.phi, 0, sizeof(float) * F.d.ncell, c->stream);
+        vcycle<float>(c, 0);
+        launch_accumulate(F.d, F.a64.phi, F.a32.phi, c->stream);
+        launch_resid64_to32(F.d, F.a64, F.a32.f, c->red.maxbits, c->stream);
+    }
+    cudaMemcpyAsync(c->red.h_maxbits, c->red.maxbits, sizeof(unsigned long long),
+                    cudaMemcpyDeviceToHost, c->stream);
+}
+
+int get_iteration_exec(mac_ctx* c, int prec, cudaGraphExec_t* out) {
+    const int slot = prec == MAC_PREC_FP64 ? 0 : 1;
+    if (c->vc_exec[slot]) {
+        *out = c->vc_exec[slot];
+        return MAC_OK;
+    }
+    cudaGraph_t g = nullptr;
+    MAC_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    issue_iteration(c, prec);
+    MAC_CUDA_TRY(cudaStreamEndCapture(c->stream, &g));
+    cudaGraphExec_t ex = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    MAC_CUDA_TRY(e);
+    c->vc_exec[slot] = ex;
+    *out = ex;
+    return MAC_OK;
+}
+
+void drop_graphs(mac_ctx* c) {
+    for (int s = 0; s < 2; ++s)
+        if (c->vc_exec[s]) {
+            cudaGraphExecDestroy(c->vc_exec[s]);
+            c->vc_exec[s] = nullptr;
+        }
+}
+
+int run_iteration(mac_ctx* c, int prec, double* res_out) {
+    if (c->o.use_graph) {
+        cudaGraphExec_t ex;
+        int rc = get_iteration_exec(c, prec, &ex);
+        if (rc) return rc;
+        MAC_CUDA_TRY(cudaGraphLaunch(ex, c->stream));
+    } else {
+        issue_iteration(c, prec);
+        MAC_CUDA_TRY(cudaGetLastError());
+    }
+    MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    *res_out = bits_to_double(*c->red.h_maxbits);
+    return MAC_OK;
+}
+
+}  // namespace
+
+// Multigrid solve on level 0 with f, coefficients and phi (level-0 layout) already in place.
+// red.scalars[1] holds ||f||_inf (after mean removal).
+int run_solve(mac_ctx* c, mac_stats* st) {
+    const mac_opts& o = c->o;
+    Level& F = c->lev[0];
+    const int prec = o.precision;
+    if (prec == MAC_PREC_MIXED) {
+        for (int l = 0; l < c->nlevels; ++l) {
+            int rc = alloc_level_fp32(c, c->lev[l]);
+            if (rc) return rc;
+        }
+        int rc = setup_fp32_copies(c);
+        if (rc) return rc;
+    }
+    MAC_CUDA_TRY(cudaMemcpyAsync(c->red.h_scalars, c->red.scalars, 8 * sizeof(double),
+                                 cudaMemcpyDeviceToHost, c->stream));
+    MAC_CUDA_TRY(cudaMemcpyAsync(c->red.h_counters, c->red.counters, 4 * sizeof(int),
+                                 cudaMemcpyDeviceToHost, c->stream));
+    MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (c->red.h_counters[1]) return MAC_ERR_BAD_DENSITY;
+    const double fnorm = c->red.h_scalars[1];
+    st->fnorm = fnorm;
+    if (!std::isfinite(fnorm)) return MAC_ERR_NONFINITE;
+    MAC_CUDA_TRY(cudaMemsetAsync(c->red.counters, 0, sizeof(int), c->stream));
+    if (fnorm == 0.0) {
+        MAC_CUDA_TRY(cudaMemsetAsync(F.a64.phi, 0, sizeof(double) * F.d.ncell, c->stream));
+        st->rel_resid = 0.0;
+        return MAC_OK;
+    }
+    auto converged = [&](double r) {
+        return r <= o.rel_eps * fnorm || (o.abs_eps > 0.0 && r <= o.abs_eps);
+    };
+    // initial residual of the caller's guess (both colours)
+    MAC_CUDA_TRY(cudaMemsetAsync(c->red.maxbits, 0, sizeof(unsigned long long), c->stream));
+    if (prec == MAC_PREC_FP64)
+        launch_resid_norm<double>(F.d, F.a64, false, c->red.maxbits, c->stream);
+    else
+        launch_resid64_to32(F.d, F.a64, F.a32.f, c->red.maxbits, c->stream);
+    MAC_CUDA_TRY(cudaGetLastError());
+    MAC_CUDA_TRY(cudaMemcpyAsync(c->red.h_maxbits, c->red.maxbits, sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, c->stream));
+    MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    double res = bits_to_double(*c->red.h_maxbits);
+    st->resid0 = res;
+    if (!std::isfinite(res)) return MAC_ERR_NONFINITE;
+    int it = 0;
+    while (!converged(res) && it < o.max_vcycles) {
+        int rc = run_iteration(c, prec, &res);
+        if (rc) return rc;
+        ++it;
+        if (st->nhist < 64) st->hist[st->nhist++] = res / fnorm;
+        if (!std::isfinite(res)) {
+            st->vcycles = it;
+            st->rel_resid = res / fnorm;
+            return MAC_ERR_NONFINITE;
+        }
+    }
+    st->vcycles = it;
+    st->refine_iters = prec == MAC_PREC_MIXED ? it : 0;
+    st->rel_resid = res / fnorm;
+    MAC_CUDA_TRY(cudaMemcpyAsync(c->red.h_counters, c->red.counters, sizeof(int),
+                                 cudaMemcpyDeviceToHost, c->stream));
+    MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    st->bottom_iters = c->red.h_counters[0];
+    return converged(res) ? MAC_OK : MAC_ERR_NOT_CONVERGED;
+}
+
+}  // namespace mac
+
+using namespace mac;
+
+namespace {
+
+int nlevels_for(const mac_ctx* c) {
+    // FBoxLib rule: coarsen every box by 2 while all of its extents stay even and >= 2 after
+    // halving (Docs/mg/mg.tex:227-236).
+    int cmin = 1 << 30;
+    for (int b = 0; b < c->g.nboxes; ++b)
+        for (int d = 0; d < c->dm; ++d) {
+            int e = c->box_hi[3 * b + d] - c->box_lo[3 * b + d] + 1;
+            int k = 0;
+            while (e % 2 == 0 && e / 2 >= 2) {
+                e /= 2;
+                ++k;
+            }
+            cmin = std::min(cmin, k);
+        }
+    int nl = 1 + (cmin == (1 << 30) ? 0 : cmin);
+    if (c->o.max_levels > 0) nl = std::min(nl, c->o.max_levels);
+    return std::min(nl, kMaxLevels);
+}
+
+int validate_geom(const mac_geom* g) {
+    if (!g || (g->dm != 2 && g->dm != 3) || g->nboxes <= 0 || !g->box_lo || !g->box_hi)
+        return MAC_ERR_INVALID;
+    for (int d = 0; d < g->dm; ++d) {
+        if (g->domain_hi[d] < g->domain_lo[d] || !(g->dx[d] > 0.0)) return MAC_ERR_INVALID;
+        const int bl = g->bc_lo[d], bh = g->bc_hi[d];
+        if (bl != MAC_BC_PER && bl != MAC_BC_DIR && bl != MAC_BC_NEU) return MAC_ERR_INVALID;
+        if (bh != MAC_BC_PER && bh != MAC_BC_DIR && bh != MAC_BC_NEU) return MAC_ERR_INVALID;
+        if ((bl == MAC_BC_PER) != (bh == MAC_BC_PER)) return MAC_ERR_INVALID;
+    }
+    // boxes inside the domain and tiling it exactly (cell counts add up, no overlap by volume)
+    long long vol = 0, dom = 1;
+    for (int d = 0; d < g->dm; ++d) dom *= (long long)(g->domain_hi[d] - g->domain_lo[d] + 1);
+    for (int b = 0; b < g->nboxes; ++b) {
+        long long v = 1;
+        for (int d = 0; d < g->dm; ++d) {
+            const int lo = g->box_lo[3 * b + d], hi = g->box_hi[3 * b + d];
+            if (hi < lo || lo < g->domain_lo[d] || hi > g->domain_hi[d]) return MAC_ERR_INVALID;
+            v *= (long long)(hi - lo + 1);
+        }
+        vol += v;
+    }
+    if (vol != dom) return MAC_ERR_INVALID;
+    if (dom >= (1ll << 31) - 1) return MAC_ERR_UNSUPPORTED;
+    return MAC_OK;
+}
+
+int check_opts(const mac_opts* o) {
+    if (!o) return MAC_ERR_INVALID;
+    if (o->precision != MAC_PREC_FP64 && o->precision != MAC_PREC_MIXED) return MAC_ERR_INVALID;
+    if (o->nu1 < 0 || o->nu2 < 0 || o->nub < 0 || o->max_vcycles < 0 || o->bottom_max_iter < 0)
+        return MAC_ERR_INVALID;
+    if (!(o->rel_eps >= 0.0)) return MAC_ERR_INVALID;
+    return MAC_OK;
+}
+
+int ctx_alloc(mac_ctx* c) {
+    int rc = 0;
+    const size_t N = (size_t)c->n[0] * c->n[1] * c->n[2];
+    c->lev.assign(c->nlevels, Level());
+    int n[3] = {c->n[0], c->n[1], c->n[2]};
+    double h[3] = {c->dx[0], c->dx[1], c->dx[2]};
+    for (int l = 0; l < c->nlevels; ++l) {
+        Level& L = c->lev[l];
+        L.d.n0 = n[0];
+        L.d.n1 = n[1];
+        L.d.n2 = n[2];
+        L.d.ncell = n[0] * n[1] * n[2];
+        L.d.split = (l < c->nlevels - 1) ? 1 : 0;
+        L.d.hn0 = n[0] / 2;
+        L.d.half = L.d.ncell / 2;
+        L.d.rz = c->dm == 3 ? 2 : 1;
+        for (int d = 0; d < 3; ++d) L.h[d] = h[d];
+        if (L.d.split && (n[0] % 2 || n[1] % 2 || (c->dm == 3 && n[2] % 2))) return MAC_ERR_UNSUPPORTED;
+        const size_t nc = L.d.ncell;
+        rc |= alloc_arr(c, &L.a64.phi, nc);
+        rc |= alloc_arr(c, &L.a64.f, nc);
+        rc |= alloc_arr(c, &L.a64.bx, nc);
+        rc |= alloc_arr(c, &L.a64.by, nc);
+        rc |= alloc_arr(c, &L.a64.bz, nc);
+        rc |= alloc_arr(c, &L.a64.diag, nc);
+        rc |= alloc_arr(c, &L.a64.invdiag, nc);
+        for (int d = 0; d < c->dm; ++d)
+            for (int s = 0; s < 2; ++s) {
+                const int bc = s ? c->bc_hi[d] : c->bc_lo[d];
+                if (bc != MAC_BC_DIR) continue;
+                const int p0 = d == 0 ? 1 : 0, p1 = d == 2 ? 1 : 2;
+                rc |= alloc_arr(c, &L.wall[d][s], (size_t)n[p0] * n[p1]);
+            }
+        if (rc) return MAC_ERR_ALLOC;
+        if (l + 1 < c->nlevels) {
+            n[0] /= 2;
+            n[1] /= 2;
+            if (c->dm == 3) n[2] /= 2;
+            h[0] *= 2;
+            h[1] *= 2;
+            if (c->dm == 3) h[2] *= 2;
+        }
+    }
+    // z coefficients of a 2-D problem stay zero
+    if (c->dm == 2)
+        for (auto& L : c->lev) MAC_CUDA_TRY(cudaMemset(L.a64.bz, 0, sizeof(double) * L.d.ncell));
+    const Level& B = c->lev[c->nlevels - 1];
+    if (B.d.ncell > kBottomMaxCells) return MAC_ERR_UNSUPPORTED;
+    rc |= alloc_arr(c, &c->bottom_scratch, (size_t)9 * B.d.ncell);
+    for (int d = 0; d < c->dm; ++d) {
+        const size_t nf = (size_t)(c->n[0] + (d == 0)) * (c->n[1] + (d == 1)) * (c->n[2] + (d == 2));
+        rc |= alloc_arr(c, &c->u[d], nf);
+    }
+    rc |= alloc_arr(c, &c->rho, N);
+    rc |= alloc_arr(c, &c->rhs, N);
+    rc |= alloc_arr(c, &c->phin, N);
+    rc |= alloc_arr(c, &c->scratch, N);
+    const int nr = c->n[c->va];
+    rc |= alloc_arr(c, &c->beta0, (size_t)nr);
+    rc |= alloc_arr(c, &c->beta0e, (size_t)nr + 1);
+    const int nbp = ceil_div((long)N, kBlk);
+    c->red.nblocks_partial = nbp;
+    rc |= alloc_arr(c, &c->red.partial, (size_t)3 * nbp);
+    rc |= alloc_arr(c, &c->red.scalars, 8);
+    rc |= alloc_arr(c, &c->red.counters, 4);
+    rc |= alloc_arr(c, &c->red.maxbits, 1);
+    if (rc) return MAC_ERR_ALLOC;
+    MAC_CUDA_TRY(cudaMallocHost(&c->red.h_maxbits, sizeof(unsigned long long)));
+    MAC_CUDA_TRY(cudaMallocHost(&c->red.h_scalars, 8 * sizeof(double)));
+    MAC_CUDA_TRY(cudaMallocHost(&c->red.h_counters, 4 * sizeof(int)));
+    c->box_table_cap = 16 * c->g.nboxes;
+    MAC_CUDA_TRY(cudaMallocHost(&c->h_boxes, sizeof(BoxDesc) * c->box_table_cap));
+    rc |= alloc_arr(c, &c->d_boxes, (size_t)c->box_table_cap);
+    if (rc) return MAC_ERR_ALLOC;
+    for (int e = 0; e < 4; ++e) MAC_CUDA_TRY(cudaEventCreate(&c->ev[e]));
+    MAC_CUDA_TRY(cudaMemset(c->red.counters, 0, 4 * sizeof(int)));
+    return MAC_OK;
+}
+
+void ctx_free(mac_ctx* c) {
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    drop_graphs(c);
+    for (void* p : c->allocations) cudaFree(p);
+    c->allocations.clear();
+    if (c->staging) cudaFree(c->staging);
+    if (c->red.h_maxbits) cudaFreeHost(c->red.h_maxbits);
+    if (c->red.h_scalars) cudaFreeHost(c->red.h_scalars);
+    if (c->red.h_counters) cudaFreeHost(c->red.h_counters);
+    if (c->h_boxes) cudaFreeHost(c->h_boxes);
+    for (int e = 0; e < 4; ++e)
+        if (c->ev[e]) cudaEventDestroy(c->ev[e]);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    c->stream = nullptr;
+}
+
+// Copy a 1-D beta0 array (host or device) into the context.
+int load_beta0(mac_ctx* c, int ptr_kind, const double* b0, const double* b0e) {
+    const int nr = c->n[c->va];
+    const cudaMemcpyKind k = ptr_kind == MAC_PTR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    MAC_CUDA_TRY(cudaMemcpyAsync(c->beta0, b0, sizeof(double) * nr, k, c->stream));
+    MAC_CUDA_TRY(cudaMemcpyAsync(c->beta0e, b0e, sizeof(double) * (nr + 1), k, c->stream));
+    return MAC_OK;
+}
+
+// Per-call operator state: alpha on/off (Helmholtz) and whether the problem is singular.
+// CUDA graphs bake the singular flag into the bottom solve, so they are dropped on a change.
+int set_call_state(mac_ctx* c, bool with_alpha) {
+    for (auto& L : c->lev) {
+        if (with_alpha && !L.alpha_store) {
+            int rc = alloc_arr(c, &L.alpha_store, (size_t)L.d.ncell);
+            if (rc) return rc;
+        }
+        L.alpha = with_alpha ? L.alpha_store : nullptr;
+    }
+    const bool sing = c->geom_singular && !with_alpha;
+    if (sing != c->singular) drop_graphs(c);
+    c->singular = sing;
+    return MAC_OK;
+}
+
+// The projection on whole-domain device arrays already in c->u / c->rho / rhs / phin.
+int core_macproject(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats* st) {
+    Level& F = c->lev[0];
+    cudaEventRecord(c->ev[0], c->stream);
+    int rc = set_call_state(c, false);
+    if (rc) return rc;
+    rc = setup_fine_coefficients(c, have_beta0 ? c->beta0 : nullptr, have_beta0 ? c->beta0e : nullptr);
+    if (rc) return rc;
+    rc = setup_coarse_levels(c);
+    if (rc) return rc;
+    rc = setup_rhs(c, macrhs, have_beta0);
+    if (rc) return rc;
+    rc = natural_to_level0(c, c->phin, F.a64.phi);
+    if (rc) return rc;
+    cudaEventRecord(c->ev[1], c->stream);
+    const int solve_rc = run_solve(c, st);
+    if (solve_rc != MAC_OK && solve_rc != MAC_ERR_NOT_CONVERGED) return solve_rc;
+    cudaEventRecord(c->ev[2], c->stream);
+    rc = correct_velocity(c, have_beta0);
+    if (rc) return rc;
+    rc = level0_to_natural(c, F.a64.phi, c->phin);
+    if (rc) return rc;
+    cudaEventRecord(c->ev[3], c->stream);
+    MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    float a = 0.f, b = 0.f, cc = 0.f;
+    cudaEventElapsedTime(&a, c->ev[0], c->ev[1]);
+    cudaEventElapsedTime(&b, c->ev[1], c->ev[2]);
+    cudaEventElapsedTime(&cc, c->ev[2], c->ev[3]);
+    st->setup_ms = a + cc;
+    st->solve_ms = b;
+    return solve_rc;
+}
+
+void fill_common_stats(const mac_ctx* c, mac_stats* st) { st->nlevels = c->nlevels; }
+
+void report(const mac_ctx* c, const char* what, const mac_stats* st) {
+    if (c->o.verbose <= 0) return;
+    std::fprintf(stderr,
+                 "[maestro_mac] %s: status %d (%s) prec=%s levels=%d vcycles=%d rel_resid=%.3e "
+                 "setup=%.3f ms solve=%.3f ms total=%.3f ms\n",
+                 what, st->status, mac_strerror(st->status),
+                 c->o.precision == MAC_PREC_MIXED ? "mixed" : "fp64", st->nlevels, st->vcycles,
+                 st->rel_resid, st->setup_ms, st->solve_ms, st->total_ms);
+}
+
+}  // namespace
+
+extern "C" {
+
+void mac_default_opts(mac_opts* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->precision = MAC_PREC_FP64;
+    o->use_alt_energy_fix = 0;
+    o->rel_eps = 1e-10;   // min(eps_mac * 10^(nlevs-1), eps_mac_max), one AMR level
+    o->abs_eps = -1.0;
+    o->max_vcycles = 100;
+    o->nu1 = 2;
+    o->nu2 = 2;
+    o->nub = 10;
+    o->bottom_eps = 1e-3;
+    o->bottom_max_iter = 200;
+    o->max_levels = 0;
+    o->use_graph = 1;
+    o->verbose = 0;
+}
+
+const char* mac_strerror(int code) {
+    switch (code) {
+        case MAC_OK: return "ok";
+        case MAC_ERR_INVALID: return "invalid argument";
+        case MAC_ERR_CUDA: return g_last_cuda.empty() ? "CUDA error" : g_last_cuda.c_str();
+        case MAC_ERR_NOT_CONVERGED: return "multigrid did not reach the tolerance within max_vcycles";
+        case MAC_ERR_NONFINITE: return "non-finite value in the right-hand side or residual";
+        case MAC_ERR_ALLOC: return "device allocation failed";
+        case MAC_ERR_UNSUPPORTED:
+            return "unsupported geometry (every level but the coarsest needs even extents; the "
+                   "coarsest level must hold at most 65536 cells; at least two MG levels)";
+        case MAC_ERR_BAD_DENSITY: return "density <= 0 or non-finite";
+        case MAC_ERR_TOO_LARGE: return "size above the fixed limit of this entry point";
+        default: return "unknown status";
+    }
+}
+
+const char* mac_version(void) { return "maestro_gb300 mac 0.1 (sm_103a)"; }
+
+int mac_ctx_create(mac_ctx** out, const mac_geom* g, const mac_opts* o, void* cuda_stream) {
+    if (!out) return MAC_ERR_INVALID;
+    *out = nullptr;
+    int rc = validate_geom(g);
+    if (rc) return rc;
+    mac_opts oo;
+    if (o) {
+        oo = *o;
+    } else {
+        mac_default_opts(&oo);
+    }
+    rc = check_opts(&oo);
+    if (rc) return rc;
+    mac_ctx* c = new mac_ctx();
+    c->g = *g;
+    c->o = oo;
+    c->box_lo.assign(g->box_lo, g->box_lo + 3 * g->nboxes);
+    c->box_hi.assign(g->box_hi, g->box_hi + 3 * g->nboxes);
+    c->g.box_lo = c->box_lo.data();
+    c->g.box_hi = c->box_hi.data();
+    c->dm = g->dm;
+    for (int d = 0; d < 3; ++d) {
+        c->n[d] = d < g->dm ? g->domain_hi[d] - g->domain_lo[d] + 1 : 1;
+        c->bc_lo[d] = d < g->dm ? g->bc_lo[d] : MAC_BC_NEU;
+        c->bc_hi[d] = d < g->dm ? g->bc_hi[d] : MAC_BC_NEU;
+        c->dx[d] = d < g->dm ? g->dx[d] : 1.0;
+    }
+    c->va = g->dm - 1;
+    bool has_dir = false;
+    for (int d = 0; d < g->dm; ++d) has_dir = has_dir || c->bc_lo[d] == MAC_BC_DIR || c->bc_hi[d] == MAC_BC_DIR;
+    c->singular = !has_dir;
+    c->geom_singular = !has_dir;
+    c->stream = (cudaStream_t)cuda_stream;
+    if (!c->stream) {
+        // graph capture is not possible on the legacy NULL stream; a blocking stream keeps the
+        // legacy-stream ordering of the caller's work
+        if (cudaStreamCreate(&c->stream) != cudaSuccess) {
+            cudaGetLastError();
+            delete c;
+            return MAC_ERR_CUDA;
+        }
+        c->own_stream = true;
+    }
+    c->nlevels = nlevels_for(c);
+    if (c->nlevels < 2) {
+        if (c->own_stream) cudaStreamDestroy(c->stream);
+        delete c;
+        return MAC_ERR_UNSUPPORTED;
+    }
+    rc = ctx_alloc(c);
+    if (rc) {
+        ctx_free(c);
+        delete c;
+        return rc;
+    }
+    *out = c;
+    return MAC_OK;
+}
+
+int mac_ctx_destroy(mac_ctx* c) {
+    if (!c) return MAC_ERR_INVALID;
+    ctx_free(c);
+    delete c;
+    return MAC_OK;
+}
+
+int mac_ctx_set_opts(mac_ctx* c, const mac_opts* o) {
+    if (!c) return MAC_ERR_INVALID;
+    int rc = check_opts(o);
+    if (rc) return rc;
+    if (o->max_levels != c->o.max_levels) return MAC_ERR_INVALID;   // hierarchy is fixed
+    drop_graphs(c);
+    c->o = *o;
+    return MAC_OK;
+}
+
+int mac_ctx_levels(const mac_ctx* c, int* n_out) {
+    if (!c) return MAC_ERR_INVALID;
+    if (n_out)
+        for (int l = 0; l < c->nlevels; ++l) {
+            n_out[3 * l + 0] = c->lev[l].d.n0;
+            n_out[3 * l + 1] = c->lev[l].d.n1;
+            n_out[3 * l + 2] = c->lev[l].d.n2;
+        }
+    return c->nlevels;
+}
+
+int mac_macproject_dense(mac_ctx* c, double* ux, double* uy, double* uz, double* phi,
+                         const double* rho, const double* macrhs, const double* beta0,
+                         const double* beta0_edge, mac_stats* stats) {
+    mac_stats local;
+    mac_stats* st = stats ? stats : &local;
+    std::memset(st, 0, sizeof(*st));
+    if (!c || !ux || !uy || (c->dm == 3 && !uz) || !phi || !rho) return st->status = MAC_ERR_INVALID;
+    if ((beta0 == nullptr) != (beta0_edge == nullptr)) return st->status = MAC_ERR_INVALID;
+    const auto t0 = std::chrono::steady_clock::now();
+    fill_common_stats(c, st);
+    double* saved_u[3] = {c->u[0], c->u[1], c->u[2]};
+    double* saved_rho = c->rho;
+    double* saved_phin = c->phin;
+    c->u[0] = ux;
+    c->u[1] = uy;
+    c->u[2] = c->dm == 3 ? uz : nullptr;
+    c->rho = const_cast<double*>(rho);
+    c->phin = phi;
+    int rc = MAC_OK;
+    if (beta0) rc = load_beta0(c, MAC_PTR_DEVICE, beta0, beta0_edge);
+    if (!rc) rc = core_macproject(c, macrhs, beta0 != nullptr, st);
+    c->u[0] = saved_u[0];
+    c->u[1] = saved_u[1];
+    c->u[2] = saved_u[2];
+    c->rho = saved_rho;
+    c->phin = saved_phin;
+    st->status = rc;
+    st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    report(c, "macproject_dense", st);
+    return rc;
+}
+
+int mac_macproject(mac_ctx* c, int ptr_kind, double* const* umac, int ng_u, double* const* phi,
+                   int ng_phi, const double* const* rho, int ng_rho, int rho_ncomp, int rho_comp,
+                   const double* const* macrhs, int ng_rhs, const double* beta0_1d,
+                   const double* beta0_1d_edge, mac_stats* stats) {
+    mac_stats local;
+    mac_stats* st = stats ? stats : &local;
+    std::memset(st, 0, sizeof(*st));
+    if (!c || !umac || !phi || !rho) return st->status = MAC_ERR_INVALID;
+    if (ptr_kind != MAC_PTR_HOST && ptr_kind != MAC_PTR_DEVICE) return st->status = MAC_ERR_INVALID;
+    if (ng_u < 0 || ng_phi < 0 || ng_rho < 0 || ng_rhs < 0 || rho_ncomp < 1 || rho_comp < 0 ||
+        rho_comp >= rho_ncomp)
+        return st->status = MAC_ERR_INVALID;
+    if ((beta0_1d == nullptr) != (beta0_1d_edge == nullptr)) return st->status = MAC_ERR_INVALID;
+    const int nb = c->g.nboxes;
+    for (int b = 0; b < nb; ++b) {
+        if (!phi[b] || !rho[b] || (macrhs && !macrhs[b])) return st->status = MAC_ERR_INVALID;
+        for (int d = 0; d < c->dm; ++d)
+            if (!umac[d * nb + b]) return st->status = MAC_ERR_INVALID;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    fill_common_stats(c, st);
+    int rc = MAC_OK;
+    for (int d = 0; d < c->dm && !rc; ++d)
+        rc = gather_faces(c, ptr_kind, (const double* const*)(umac + d * nb), ng_u, d, c->u[d]);
+    if (!rc) rc = gather_cells(c, ptr_kind, rho, ng_rho, rho_ncomp, rho_comp, c->rho);
+    if (!rc && macrhs) rc = gather_cells(c, ptr_kind, macrhs, ng_rhs, 1, 0, c->rhs);
+    if (!rc) rc = gather_cells(c, ptr_kind, (const double* const*)phi, ng_phi, 1, 0, c->phin);
+    if (!rc && beta0_1d) rc = load_beta0(c, ptr_kind, beta0_1d, beta0_1d_edge);
+    int solve_rc = MAC_OK;
+    if (!rc) {
+        solve_rc = core_macproject(c, macrhs ? c->rhs : nullptr, beta0_1d != nullptr, st);
+        if (solve_rc != MAC_OK && solve_rc != MAC_ERR_NOT_CONVERGED) rc = solve_rc;
+    }
+    for (int d = 0; d < c->dm && !rc; ++d)
+        rc = scatter_faces(c, ptr_kind, umac + d * nb, ng_u, d, c->u[d]);
+    if (!rc) rc = scatter_cells(c, ptr_kind, phi, ng_phi, c->phin);
+    if (!rc) {
+        cudaError_t e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) {
+            set_last_cuda_error(e, "cudaStreamSynchronize", __FILE__, __LINE__);
+            rc = MAC_ERR_CUDA;
+        }
+    }
+    if (!rc) rc = solve_rc;
+    st->status = rc;
+    st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    report(c, "macproject", st);
+    return rc;
+}
+
+int mac_multigrid(mac_ctx* c, int ptr_kind, const double* const* rh, int ng_rh,
+                  double* const* phi, int ng_phi, const double* const* alpha, int ng_alpha,
+                  const double* const* beta, int ng_beta, mac_stats* stats) {
+    mac_stats local;
+    mac_stats* st = stats ? stats : &local;
+    std::memset(st, 0, sizeof(*st));
+    if (!c || !rh || !phi || !beta) return st->status = MAC_ERR_INVALID;
+    if (ptr_kind != MAC_PTR_HOST && ptr_kind != MAC_PTR_DEVICE) return st->status = MAC_ERR_INVALID;
+    if (ng_rh < 0 || ng_phi < 0 || ng_alpha < 0 || ng_beta < 0) return st->status = MAC_ERR_INVALID;
+    const int nb = c->g.nboxes;
+    for (int b = 0; b < nb; ++b) {
+        if (!rh[b] || !phi[b] || (alpha && !alpha[b])) return st->status = MAC_ERR_INVALID;
+        for (int d = 0; d < c->dm; ++d)
+            if (!beta[d * nb + b]) return st->status = MAC_ERR_INVALID;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    fill_common_stats(c, st);
+    Level& F = c->lev[0];
+    int rc = set_call_state(c, alpha != nullptr);
+    for (int d = 0; d < c->dm && !rc; ++d)
+        rc = gather_faces(c, ptr_kind, beta + d * nb, ng_beta, d, c->u[d]);
+    if (!rc) rc = gather_cells(c, ptr_kind, rh, ng_rh, 1, 0, c->rhs);
+    if (!rc && alpha) rc = gather_cells(c, ptr_kind, alpha, ng_alpha, 1, 0, c->scratch);
+    if (!rc) rc = gather_cells(c, ptr_kind, (const double* const*)phi, ng_phi, 1, 0, c->phin);
+    if (!rc) {
+        cudaEventRecord(c->ev[0], c->stream);
+        rc = setup_fine_from_faces(c, c->u[0], c->u[1], c->dm == 3 ? c->u[2] : nullptr,
+                                   alpha ? c->scratch : nullptr);
+    }
+    if (!rc) rc = setup_coarse_levels(c);
+    if (!rc) rc = setup_rhs_from(c, c->rhs);
+    if (!rc) rc = natural_to_level0(c, c->phin, F.a64.phi);
+    int solve_rc = MAC_OK;
+    if (!rc) {
+        cudaEventRecord(c->ev[1], c->stream);
+        solve_rc = run_solve(c, st);
+        if (solve_rc != MAC_OK && solve_rc != MAC_ERR_NOT_CONVERGED) rc = solve_rc;
+        cudaEventRecord(c->ev[2], c->stream);
+    }
+    if (!rc) rc = level0_to_natural(c, F.a64.phi, c->phin);
+    if (!rc) rc = scatter_cells(c, ptr_kind, phi, ng_phi, c->phin);
+    if (!rc) {
+        cudaError_t e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) {
+            set_last_cuda_error(e, "cudaStreamSynchronize", __FILE__, __LINE__);
+            rc = MAC_ERR_CUDA;
+        } else {
+            float a = 0.f, b = 0.f;
+            cudaEventElapsedTime(&a, c->ev[0], c->ev[1]);
+            cudaEventElapsedTime(&b, c->ev[1], c->ev[2]);
+            st->setup_ms = a;
+            st->solve_ms = b;
+        }
+    }
+    if (!rc) rc = solve_rc;
+    st->status = rc;
+    st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    report(c, "mac_multigrid", st);
+    return rc;
+}
+
+int mac_cell_to_edge(int nr, const double* s0_cell, double* s0_edge) {
+    if (nr < 1 || !s0_cell || !s0_edge) return MAC_ERR_INVALID;
+    for (int r = 0; r <= nr; ++r) {
+        if (r == 0) {
+            s0_edge[r] = s0_cell[0];
+        } else if (r == 1) {
+            s0_edge[r] = 0.5 * (s0_cell[0] + s0_cell[1 < nr ? 1 : 0]);
+        } else if (r == nr) {
+            s0_edge[r] = s0_cell[r - 1];
+        } else if (r == nr - 1) {
+            s0_edge[r] = 0.5 * (s0_cell[r] + s0_cell[r - 1]);
+        } else {
+            const double tmp = 7.0 / 12.0 * (s0_cell[r] + s0_cell[r - 1]) -
+                               1.0 / 12.0 * (s0_cell[r + 1] + s0_cell[r - 2]);
+            const double lo = s0_cell[r] < s0_cell[r - 1] ? s0_cell[r] : s0_cell[r - 1];
+            const double hi = s0_cell[r] < s0_cell[r - 1] ? s0_cell[r - 1] : s0_cell[r];
+            s0_edge[r] = tmp < lo ? lo : (tmp > hi ? hi : tmp);
+        }
+    }
+    return MAC_OK;
+}
+
+}  // extern "C"

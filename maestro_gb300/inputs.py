@@ -1,0 +1,221 @@
+"""Seeded synthetic inputs for the MAC projection: a stratified, planar atmosphere.
+
+No public dataset exists for this path; the workloads are the stratified-atmosphere cases of the
+MAC projection benchmark (2D 128^2, 3D 256^3 / 384^3 / 512^3 in 128^3 boxes), generated here:
+
+* domain [0,1]^dm, vertical direction = the last one (MAESTRO planar geometry), cell-centred
+  heights z_k = (k + 1/2) dz;
+* base density rho0(z) = 1e7 exp(-z / H), H a fraction of the domain height;
+* cell density rho = rho0 (1 + sigma N(0,1)) ("linear" noise) or rho0 exp(sigma N(0,1))
+  ("lognormal" noise);
+* beta0 = rho0^(1/1.4) at cell centres, beta0 at edges by the limited fourth-order rule of
+  Source/cell_to_edge.f90:14-70 (`cell_to_edge` below);
+* U_edge: a sum of random Fourier modes with |k| <= kmax, amplitude 1e6 cm/s; horizontal
+  directions periodic (e^{2 pi i k x}), vertical direction a slip wall: the wall-normal
+  component goes like sin(k pi z), the tangential ones like cos(k pi z), so U.n = 0 on the walls;
+  the field is divergent;
+* S - Sbar: Gaussian noise of amplitude 1e-3 s^-1 with the mean of every horizontal layer
+  removed, so macrhs = beta0 (S - Sbar) (Source/make_macrhs.f90:228-229) is compatible with the
+  singular periodic/Neumann problem;
+* w: N(0,1) face weights for the adjoint loss L = sum(w . U_proj).
+
+Arrays are float64, Fortran order, indexed like MAESTRO's fabs: cells (nx, ny[, nz]); faces with one
+extra entry along their own direction.
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+
+BC_PER, BC_INT, BC_DIR, BC_NEU = -1, 0, 1, 2
+
+
+def cell_to_edge(s0_cell: np.ndarray) -> np.ndarray:
+    """Edge values of a 1D base-state array (Source/cell_to_edge.f90:14-70, one level).
+
+    Copies at the two domain ends, arithmetic means one cell in, limited fourth-order
+    7/12 (a+b) - 1/12 (c+d) clipped to [min(a,b), max(a,b)] elsewhere.
+    """
+    c = np.asarray(s0_cell, dtype=np.float64)
+    nr = c.size
+    e = np.empty(nr + 1)
+    for r in range(nr + 1):
+        if r == 0:
+            e[r] = c[0]
+        elif r == 1:
+            e[r] = 0.5 * (c[0] + c[1])
+        elif r == nr:
+            e[r] = c[nr - 1]
+        elif r == nr - 1:
+            e[r] = 0.5 * (c[r] + c[r - 1])
+        else:
+            tmp = 7.0 / 12.0 * (c[r] + c[r - 1]) - 1.0 / 12.0 * (c[r + 1] + c[r - 2])
+            e[r] = min(max(tmp, min(c[r], c[r - 1])), max(c[r], c[r - 1]))
+    return e
+
+
+@dataclasses.dataclass
+class MacCase:
+    """One MAC-projection input set on the whole domain (single level)."""
+
+    name: str
+    dm: int
+    n: tuple
+    box: tuple                 # box extent (cells per direction); boxes tile the domain
+    dx: tuple
+    bc_lo: tuple
+    bc_hi: tuple
+    rho: np.ndarray
+    beta0: np.ndarray
+    beta0_edge: np.ndarray
+    umac: list
+    macrhs: np.ndarray
+    phi0: np.ndarray
+    w: list | None = None
+    seed: int = 0
+
+    @property
+    def ncell(self) -> int:
+        return int(np.prod(self.n))
+
+    def boxes(self):
+        """(lo, hi) inclusive cell bounds of every box, x fastest (FBoxLib box list order)."""
+        nb = [self.n[d] // self.box[d] for d in range(self.dm)]
+        out = []
+        for idx in np.ndindex(*reversed(nb)):
+            idx = tuple(reversed(idx))
+            lo = tuple(idx[d] * self.box[d] for d in range(self.dm))
+            hi = tuple(lo[d] + self.box[d] - 1 for d in range(self.dm))
+            out.append((lo, hi))
+        return out
+
+
+def _modes(kmax: int, dm: int):
+    """Integer wave vectors with |k| <= kmax: horizontal in [-kmax, kmax], vertical in [0, kmax]."""
+    ks = []
+    r = range(-kmax, kmax + 1)
+    if dm == 2:
+        for kx in r:
+            for kz in range(0, kmax + 1):
+                if kx * kx + kz * kz <= kmax * kmax and (kx, kz) != (0, 0):
+                    ks.append((kx, kz))
+    else:
+        for kx in r:
+            for ky in r:
+                for kz in range(0, kmax + 1):
+                    if kx * kx + ky * ky + kz * kz <= kmax * kmax and (kx, ky, kz) != (0, 0, 0):
+                        ks.append((kx, ky, kz))
+    return np.array(ks, dtype=np.int64)
+
+
+def _fourier_component(rng, n, dm, d, kmax, dtype=np.float64):
+    """Random real field on the faces normal to direction d (see module docstring)."""
+    modes = _modes(kmax, dm)
+    coef = rng.standard_normal(len(modes)) + 1j * rng.standard_normal(len(modes))
+    K = 2 * kmax + 1
+    kz_n = kmax + 1
+    if dm == 2:
+        C = np.zeros((K, kz_n), dtype=np.complex128)
+        C[modes[:, 0] + kmax, modes[:, 1]] = coef
+    else:
+        C = np.zeros((K, K, kz_n), dtype=np.complex128)
+        C[modes[:, 0] + kmax, modes[:, 1] + kmax, modes[:, 2]] = coef
+    shape = list(n)
+    shape[d] += 1
+    pos = []
+    for e in range(dm):
+        m = shape[e]
+        if e == d:
+            pos.append(np.arange(m) / n[e])            # faces
+        else:
+            pos.append((np.arange(m) + 0.5) / n[e])    # cell centres
+    kh = np.arange(-kmax, kmax + 1)
+    kv = np.arange(0, kmax + 1)
+    # vertical basis: sin for the wall-normal component, cos for the tangential ones
+    zv = pos[dm - 1]
+    Z = np.sin(np.pi * np.outer(kv, zv)) if d == dm - 1 else np.cos(np.pi * np.outer(kv, zv))
+    Ex = np.exp(2j * np.pi * np.outer(kh, pos[0]))           # (K, mx)
+    if dm == 2:
+        T = C @ Z                                            # (K, mz)
+        u = np.real(Ex.T @ T)                                # (mx, mz)
+    else:
+        Ey = np.exp(2j * np.pi * np.outer(kh, pos[1]))       # (K, my)
+        T1 = np.tensordot(C, Z, axes=([2], [0]))             # (K, K, mz)
+        T2 = np.tensordot(T1, Ey, axes=([1], [0]))           # (K, mz, my)
+        T2 = np.transpose(T2, (0, 2, 1)).reshape(K, -1)      # (K, my*mz)
+        u = np.real(Ex.T @ T2).reshape(shape[0], shape[1], shape[2], order="C")
+    u = np.asfortranarray(u.astype(dtype))
+    return u
+
+
+def make_case(name: str = "custom", dm: int = 3, n=(64, 64, 64), box=None, H_frac: float = 0.25,
+              noise: float = 0.01, noise_kind: str = "lognormal", kmax: int = 8, seed: int = 1234,
+              u_amp: float = 1e6, s_amp: float = 1e-3, with_w: bool = False) -> MacCase:
+    """Build a seeded stratified-atmosphere MAC case (see module docstring)."""
+    n = tuple(int(v) for v in n)
+    assert len(n) == dm
+    box = tuple(box) if box is not None else n
+    rng = np.random.default_rng(seed)
+    dx = tuple(1.0 / n[d] for d in range(dm))
+    nz = n[dm - 1]
+    z = (np.arange(nz) + 0.5) / nz
+    H = H_frac * 1.0
+    rho0 = 1e7 * np.exp(-z / H)
+    bshape = [1] * dm
+    bshape[dm - 1] = nz
+    rho0_b = rho0.reshape(bshape)
+    g = rng.standard_normal(n)
+    if noise_kind == "linear":
+        rho = rho0_b * (1.0 + noise * g)
+    else:
+        rho = rho0_b * np.exp(noise * g)
+    rho = np.asfortranarray(rho)
+    beta0 = rho0 ** (1.0 / 1.4)
+    beta0_edge = cell_to_edge(beta0)
+    umac = []
+    for d in range(dm):
+        u = _fourier_component(rng, n, dm, d, kmax)
+        m = np.max(np.abs(u))
+        umac.append(np.asfortranarray(u * (u_amp / m if m > 0 else 1.0)))
+    s = rng.standard_normal(n) * s_amp
+    axes = tuple(range(dm - 1))
+    s = s - s.mean(axis=axes, keepdims=True)
+    macrhs = np.asfortranarray(beta0.reshape(bshape) * s)
+    w = None
+    if with_w:
+        w = []
+        for d in range(dm):
+            shp = list(n)
+            shp[d] += 1
+            w.append(np.asfortranarray(rng.standard_normal(shp)))
+    bc_lo = tuple([BC_PER] * (dm - 1) + [BC_NEU])
+    bc_hi = tuple([BC_PER] * (dm - 1) + [BC_NEU])
+    return MacCase(name=name, dm=dm, n=n, box=box, dx=dx, bc_lo=bc_lo, bc_hi=bc_hi, rho=rho,
+                   beta0=beta0, beta0_edge=beta0_edge, umac=umac, macrhs=macrhs,
+                   phi0=np.zeros(n, order="F"), w=w, seed=seed)
+
+
+# The five MAC-projection workloads (sizes, boxes, stratification, noise, spectrum).
+CONFIGS = {
+    "2d_128": dict(dm=2, n=(128, 128), box=(128, 128), H_frac=0.25, noise=0.01,
+                   noise_kind="linear", kmax=8),
+    "3d_256": dict(dm=3, n=(256, 256, 256), box=(128, 128, 128), H_frac=0.25, noise=0.01,
+                   noise_kind="lognormal", kmax=16),
+    "3d_512_mixed": dict(dm=3, n=(512, 512, 512), box=(128, 128, 128), H_frac=0.15, noise=0.01,
+                         noise_kind="lognormal", kmax=32),
+    "3d_256_adjoint": dict(dm=3, n=(256, 256, 256), box=(128, 128, 128), H_frac=0.25,
+                           noise=0.01, noise_kind="lognormal", kmax=16, with_w=True),
+    "3d_384_stiff": dict(dm=3, n=(384, 384, 384), box=(128, 128, 128), H_frac=0.072,
+                         noise=0.05, noise_kind="lognormal", kmax=16),
+}
+
+
+def config_case(key: str, seed: int = 1234, scale: int = 1) -> MacCase:
+    """One of CONFIGS; `scale` > 1 divides every extent (and the box) by it for small tests."""
+    kw = dict(CONFIGS[key])
+    if scale > 1:
+        kw["n"] = tuple(v // scale for v in kw["n"])
+        kw["box"] = tuple(max(2, v // scale) for v in kw["box"])
+        kw["kmax"] = max(2, kw["kmax"] // scale)
+    return make_case(name=key, seed=seed, **kw)

@@ -1,0 +1,259 @@
+"""CPU oracle of the MAC projection -- TEST INFRASTRUCTURE ONLY.
+
+ctypes front end of ``mac_oracle.cpp``: an IEEE-FP64 C++/OpenMP restatement of MAESTRO's
+``macproject`` (Source/macproject.f90:51-328) and of the FBoxLib cell-centred multigrid that
+``mac_multigrid`` (Source/mac_multigrid.f90:18-67) calls.  Only ``tests/``,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may use this module, and only
+as the checker / the timed CPU reference.  The product library never imports it.
+
+Parity status: the reference (Fortran + the un-vendored FBoxLib) cannot be compiled here, so the
+oracle is pinned by (a) an MG-independent sparse direct solve of the same discrete system
+(scipy, tests/golden/make_golden.py) and (b) the known-answer behaviour of MAESTRO's own
+``test_projection`` unit test (Exec/UNIT_TESTS/test_projection/test_projection.f90:172-344,
+860-1050): a divergence-free field plus a discrete gradient projects back to the field.  No
+numeric golden outputs of the reference exist in its tree, so numerically the parity with the
+Fortran code itself is unpinned beyond those two anchors.
+
+Arrays are numpy float64 in Fortran order, indexed like the reference: cell arrays (nx, ny[, nz]),
+face arrays with one extra entry along their own direction.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libmac_oracle.so")
+
+# FBoxLib bc_module numbering, as stored in ell_bc_level_array(..., press_comp).
+BC_PER, BC_INT, BC_DIR, BC_NEU = -1, 0, 1, 2
+
+# Source/mg_eps.f90:23-28
+EPS_MAC, EPS_MAC_MAX, MAC_LEVEL_FACTOR, EPS_MAC_BOTTOM = 1e-10, 1e-8, 10.0, 1e-3
+
+
+class OrcOpts(ctypes.Structure):
+    _fields_ = [
+        ("dm", ctypes.c_int),
+        ("n", ctypes.c_int * 3),
+        ("dx", ctypes.c_double * 3),
+        ("bc_lo", ctypes.c_int * 3),
+        ("bc_hi", ctypes.c_int * 3),
+        ("nlevels", ctypes.c_int),
+        ("rel_eps", ctypes.c_double),
+        ("abs_eps", ctypes.c_double),
+        ("max_vcycles", ctypes.c_int),
+        ("nu1", ctypes.c_int),
+        ("nu2", ctypes.c_int),
+        ("nub", ctypes.c_int),
+        ("bottom_eps", ctypes.c_double),
+        ("bottom_max_iter", ctypes.c_int),
+        ("alt_energy_fix", ctypes.c_int),
+        ("nthreads", ctypes.c_int),
+    ]
+
+
+class OrcStats(ctypes.Structure):
+    _fields_ = [
+        ("status", ctypes.c_int),
+        ("vcycles", ctypes.c_int),
+        ("fnorm", ctypes.c_double),
+        ("resid0", ctypes.c_double),
+        ("rel_resid", ctypes.c_double),
+        ("nhist", ctypes.c_int),
+        ("hist", ctypes.c_double * 64),
+        ("bottom_iters", ctypes.c_int),
+    ]
+
+    def as_dict(self):
+        return {
+            "status": self.status,
+            "vcycles": self.vcycles,
+            "fnorm": self.fnorm,
+            "resid0": self.resid0,
+            "rel_resid": self.rel_resid,
+            "hist": [self.hist[i] for i in range(self.nhist)],
+            "bottom_iters": self.bottom_iters,
+        }
+
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile mac_oracle.cpp into oracle/_build/libmac_oracle.so (g++ + OpenMP)."""
+    if force or not os.path.exists(_LIB_PATH) or (
+        os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "mac_oracle.cpp"))
+    ):
+        subprocess.check_call(["make", "-s", "-C", _HERE], stdout=subprocess.DEVNULL)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        P = ctypes.POINTER
+        d = P(ctypes.c_double)
+        L.orc_macproject.argtypes = [P(OrcOpts), d, d, d, d, d, d, d, d, P(OrcStats)]
+        L.orc_macproject.restype = ctypes.c_int
+        L.orc_mac_multigrid.argtypes = [P(OrcOpts), d, d, d, d, d, d, P(OrcStats)]
+        L.orc_mac_multigrid.restype = ctypes.c_int
+        L.orc_apply_op.argtypes = [P(OrcOpts), d, d, d, d, d, d]
+        L.orc_apply_op.restype = None
+        L.orc_mac_coeffs.argtypes = [P(OrcOpts), d, d, d, d, d, d]
+        L.orc_mac_coeffs.restype = None
+        L.orc_cell_to_edge.argtypes = [ctypes.c_int, d, d]
+        L.orc_cell_to_edge.restype = None
+        L.orc_max_threads.argtypes = []
+        L.orc_max_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def max_threads() -> int:
+    return int(lib().orc_max_threads())
+
+
+def nlevels_for_boxes(box_extents, min_width: int = 2) -> int:
+    """MG depth when every box is coarsened by 2 down to `min_width` cells per side.
+
+    FBoxLib coarsens each box of the level while all of its extents stay even and at least
+    `min_width` after halving (Docs/mg/mg.tex:227-236: "coarsened as much as they can, down to
+    2^3 zones").  `box_extents` is an iterable of per-box extent tuples (cells per direction).
+    """
+    c = None
+    for ext in box_extents:
+        for e in ext:
+            k = 0
+            while e % 2 == 0 and e // 2 >= min_width:
+                e //= 2
+                k += 1
+            c = k if c is None else min(c, k)
+    return 1 + (c or 0)
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and (a.flags.f_contiguous or a.ndim == 1)
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _opts(shape, dx, bc_lo, bc_hi, nlevels, rel_eps, abs_eps, max_vcycles, nu1, nu2, nub,
+          bottom_eps, bottom_max_iter, alt_energy_fix, threads):
+    dm = len(shape)
+    o = OrcOpts()
+    o.dm = dm
+    n = list(shape) + [1] * (3 - dm)
+    for d in range(3):
+        o.n[d] = int(n[d])
+        o.dx[d] = float(dx[d]) if d < dm else 1.0
+        o.bc_lo[d] = int(bc_lo[d]) if d < dm else BC_NEU
+        o.bc_hi[d] = int(bc_hi[d]) if d < dm else BC_NEU
+    o.nlevels = int(nlevels)
+    o.rel_eps = rel_eps
+    o.abs_eps = abs_eps
+    o.max_vcycles = max_vcycles
+    o.nu1, o.nu2, o.nub = nu1, nu2, nub
+    o.bottom_eps = bottom_eps
+    o.bottom_max_iter = bottom_max_iter
+    o.alt_energy_fix = int(bool(alt_energy_fix))
+    o.nthreads = int(threads)
+    return o
+
+
+def _f64f(a):
+    return np.asfortranarray(np.asarray(a, dtype=np.float64))
+
+
+def macproject(umac, phi, rho, dx, bc_lo, bc_hi, macrhs=None, beta0=None, beta0_edge=None,
+               nlevels=None, rel_eps=EPS_MAC, abs_eps=-1.0, max_vcycles=100, nu1=2, nu2=2,
+               nub=10, bottom_eps=EPS_MAC_BOTTOM, bottom_max_iter=200, alt_energy_fix=False,
+               threads=0):
+    """Oracle MAC projection on the whole domain.  Returns (umac_new, phi_new, stats)."""
+    phi = _f64f(phi).copy(order="F")
+    rho = _f64f(rho)
+    shape = phi.shape
+    dm = len(shape)
+    u = [_f64f(x).copy(order="F") for x in umac]
+    for d in range(dm):
+        exp = list(shape)
+        exp[d] += 1
+        assert u[d].shape == tuple(exp), (d, u[d].shape, exp)
+    if nlevels is None:
+        nlevels = nlevels_for_boxes([shape])
+    o = _opts(shape, dx, bc_lo, bc_hi, nlevels, rel_eps, abs_eps, max_vcycles, nu1, nu2, nub,
+              bottom_eps, bottom_max_iter, alt_energy_fix, threads)
+    st = OrcStats()
+    rhs = _f64f(macrhs) if macrhs is not None else None
+    b0 = np.ascontiguousarray(beta0, dtype=np.float64) if beta0 is not None else None
+    b0e = np.ascontiguousarray(beta0_edge, dtype=np.float64) if beta0_edge is not None else None
+    uz = u[2] if dm == 3 else None
+    lib().orc_macproject(ctypes.byref(o), _ptr(u[0]), _ptr(u[1]), _ptr(uz), _ptr(phi), _ptr(rho),
+                         _ptr(rhs), _ptr(b0), _ptr(b0e), ctypes.byref(st))
+    return u, phi, st.as_dict()
+
+
+def mac_multigrid(rh, phi, beta, dx, bc_lo, bc_hi, alpha=None, nlevels=None, rel_eps=EPS_MAC,
+                  abs_eps=-1.0, max_vcycles=100, nu1=2, nu2=2, nub=10,
+                  bottom_eps=EPS_MAC_BOTTOM, bottom_max_iter=200, threads=0):
+    """Oracle of mac_multigrid: solve (alpha - div beta grad) phi = rh.  Returns (phi, stats)."""
+    rh = _f64f(rh)
+    phi = _f64f(phi).copy(order="F")
+    shape = rh.shape
+    dm = len(shape)
+    b = [_f64f(x) for x in beta]
+    if nlevels is None:
+        nlevels = nlevels_for_boxes([shape])
+    o = _opts(shape, dx, bc_lo, bc_hi, nlevels, rel_eps, abs_eps, max_vcycles, nu1, nu2, nub,
+              bottom_eps, bottom_max_iter, False, threads)
+    st = OrcStats()
+    al = _f64f(alpha) if alpha is not None else None
+    lib().orc_mac_multigrid(ctypes.byref(o), _ptr(rh), _ptr(phi), _ptr(b[0]), _ptr(b[1]),
+                            _ptr(b[2] if dm == 3 else None), _ptr(al), ctypes.byref(st))
+    return phi, st.as_dict()
+
+
+def apply_op(u, beta, dx, bc_lo, bc_hi, alpha=None):
+    """(alpha - div beta grad) u on one level (no MG)."""
+    u = _f64f(u)
+    shape = u.shape
+    dm = len(shape)
+    b = [_f64f(x) for x in beta]
+    o = _opts(shape, dx, bc_lo, bc_hi, 1, 0, 0, 0, 0, 0, 0, 0, 0, False, 0)
+    out = np.zeros(shape, order="F")
+    al = _f64f(alpha) if alpha is not None else None
+    lib().orc_apply_op(ctypes.byref(o), _ptr(u), _ptr(b[0]), _ptr(b[1]),
+                       _ptr(b[2] if dm == 3 else None), _ptr(al), _ptr(out))
+    return out
+
+
+def mac_coeffs(rho, dx, bc_lo, bc_hi, beta0=None, beta0_edge=None, alt_energy_fix=False):
+    """Face coefficients beta0^p * 2/(rho_L + rho_R) (mk_mac_coeffs + the beta0 multiply)."""
+    rho = _f64f(rho)
+    shape = rho.shape
+    dm = len(shape)
+    o = _opts(shape, dx, bc_lo, bc_hi, 1, 0, 0, 0, 0, 0, 0, 0, 0, alt_energy_fix, 0)
+    out = []
+    for d in range(dm):
+        s = list(shape)
+        s[d] += 1
+        out.append(np.zeros(s, order="F"))
+    b0 = np.ascontiguousarray(beta0, dtype=np.float64) if beta0 is not None else None
+    b0e = np.ascontiguousarray(beta0_edge, dtype=np.float64) if beta0_edge is not None else None
+    lib().orc_mac_coeffs(ctypes.byref(o), _ptr(rho), _ptr(b0), _ptr(b0e), _ptr(out[0]),
+                         _ptr(out[1]), _ptr(out[2] if dm == 3 else None))
+    return out
+
+
+def cell_to_edge(s0_cell):
+    """beta0 cell -> edge values, Source/cell_to_edge.f90:14-70 (one level)."""
+    c = np.ascontiguousarray(s0_cell, dtype=np.float64)
+    e = np.zeros(c.size + 1)
+    lib().orc_cell_to_edge(int(c.size), _ptr(c), _ptr(e))
+    return e

@@ -1,0 +1,83 @@
+"""C-ABI library checks that need no GPU: it loads, exports every symbol the header declares,
+rejects invalid arguments before touching the device, and its host-only routine matches the
+oracle."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle as O
+from maestro_gb300 import capi
+from maestro_gb300.build import build
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                      "maestro_mac.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build()
+    return capi.lib()
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(mac_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_and_binding_agree():
+    assert declared_functions() == sorted(capi.EXPORTED)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", capi.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    syms = {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+    for f in declared_functions():
+        assert f in syms, f
+        assert hasattr(lib, f)
+
+
+def test_strerror_and_defaults(lib):
+    for code in (0, -1, -2, -3, -4, -5, -6, -7, -8):
+        assert len(capi.strerror(code)) > 0
+    o = capi.default_opts()
+    # MAESTRO's MAC settings: eps_mac, V(2,2), mg_bottom_nu, eps_mac_bottom
+    assert o.rel_eps == 1e-10 and o.nu1 == 2 and o.nu2 == 2 and o.nub == 10
+    assert o.bottom_eps == 1e-3 and o.precision == capi.MAC_PREC_FP64 and o.abs_eps < 0
+
+
+def test_invalid_geometry_rejected_without_device(lib):
+    ctx = ctypes.c_void_p()
+    g = capi.MacGeom()
+    g.dm = 4
+    assert lib.mac_ctx_create(ctypes.byref(ctx), ctypes.byref(g), None, None) == capi.MAC_ERR_INVALID
+    # boxes that do not tile the domain
+    g.dm = 2
+    g.domain_hi[0] = 7
+    g.domain_hi[1] = 7
+    g.dx[0] = g.dx[1] = 1.0 / 8
+    g.bc_lo[0] = g.bc_hi[0] = capi.MAC_BC_PER
+    g.bc_lo[1] = g.bc_hi[1] = capi.MAC_BC_NEU
+    lo = (ctypes.c_int * 3)(0, 0, 0)
+    hi = (ctypes.c_int * 3)(3, 7, 0)
+    g.nboxes = 1
+    g.box_lo = ctypes.cast(lo, ctypes.POINTER(ctypes.c_int))
+    g.box_hi = ctypes.cast(hi, ctypes.POINTER(ctypes.c_int))
+    assert lib.mac_ctx_create(ctypes.byref(ctx), ctypes.byref(g), None, None) == capi.MAC_ERR_INVALID
+    # periodic on one side only
+    hi[0] = 7
+    g.bc_hi[0] = capi.MAC_BC_NEU
+    assert lib.mac_ctx_create(ctypes.byref(ctx), ctypes.byref(g), None, None) == capi.MAC_ERR_INVALID
+    assert lib.mac_ctx_destroy(None) == capi.MAC_ERR_INVALID
+    assert lib.mac_macproject_dense(None, *([None] * 8), None) == capi.MAC_ERR_INVALID
+
+
+def test_cell_to_edge_matches_oracle(lib):
+    from maestro_gb300.macproject import cell_to_edge
+    b = 1e7 ** (1 / 1.4) * np.exp(-np.linspace(0, 4, 64) / 1.4)
+    np.testing.assert_array_equal(cell_to_edge(b), O.cell_to_edge(b))

