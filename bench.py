@@ -1,0 +1,408 @@
+#!/usr/bin/env python
+"""MAC-projection benchmark on GB300: MAC solves/s at 256^3 to 1e-10 relative residual.
+
+One step = one complete MAC projection (Source/macproject.f90:51-328: beta0 scaling, RHS,
+face coefficients, multigrid to ||f - L phi|| <= 1e-10 ||f||, velocity correction) of the
+3-D 256^3 stratified-atmosphere workload (8 boxes of 128^3, periodic x/y, slip walls in z,
+rho0 = 1e7 exp(-z/H), H = 0.25, 1% lognormal density noise, |k| <= 16 velocity modes).
+Inputs are seeded synthetic data (no public dataset exists for this path).
+
+value  : mixed-precision solves/s (FP32 V-cycles inside FP64 iterative refinement), inputs
+         resident in HBM, CUDA events on the library's stream around K steps.
+fp64   : the plain FP64 solve timed the same way.
+e2e    : the same metric through the public C ABI (mac_macproject) with host (pinned) per-box
+         fabs: every step copies its inputs host->device and its result device->host.
+roofline: the finest-level red/black Gauss-Seidel sweeps of the mixed solve, timed live with
+         CUDA events recorded inside the V-cycle graph over the timed region.
+--impl reference: the CPU oracle (C++/OpenMP restatement of MAESTRO's FP64 solve; the Fortran
+         reference cannot be built here) on the host cores.
+
+Multi-GPU: the projection does not shard without a halo exchange; N ranks run N independent
+replicas (weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MAC solves/s at 256^3 to 1e-10 rel resid: mixed vs FP64 GPU; % HBM peak"
+UNIT = "solves/s"
+CONFIG_KEY = "3d_256"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default=CONFIG_KEY)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--seed", type=int, default=1234)
+    return ap.parse_args()
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---- clocks sampled during the timed region ---------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.path = None
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for ln in f:
+                p = [x.strip() for x in ln.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    smax.append(float(p[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, p[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---- reference arm: the CPU oracle ------------------------------------------------------------
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    import oracle as O
+    from maestro_gb300.inputs import CONFIGS, make_case
+    kw = dict(CONFIGS[args.config])
+    # bounded sample per step: the same stratified workload on one 128^3 box (1/8 of the cells,
+    # the same 7-level hierarchy), solves/s scaled to the 256^3 domain by the cell ratio
+    full = 1
+    for v in kw["n"]:
+        full *= v
+    kw["n"] = tuple(kw["box"])
+    sample_cells = 1
+    for v in kw["n"]:
+        sample_cells *= v
+    c = make_case(name=args.config + "_sample", seed=args.seed, **kw)
+    nlev = O.nlevels_for_boxes([c.box])
+    threads = O.max_threads()
+
+    def step():
+        t = time.perf_counter()
+        _, _, st = O.macproject(c.umac, c.phi0, c.rho, c.dx, c.bc_lo, c.bc_hi, macrhs=c.macrhs,
+                                beta0=c.beta0, beta0_edge=c.beta0_edge, nlevels=nlev)
+        assert st["status"] == 0 and st["rel_resid"] <= 1e-10
+        return time.perf_counter() - t
+
+    for _ in range(args.warmup):
+        step()
+    ts = [step() for _ in range(args.steps)]
+    secs = sum(ts)
+    value = args.steps / secs * (sample_cells / full)
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded stratified atmosphere)",
+        "config": {"workload": args.config, "n": list(CONFIGS[args.config]["n"]),
+                   "box": list(CONFIGS[args.config]["box"]), "rel_eps": 1e-10},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"per step one {kw['n'][0]}^3 solve of the same workload "
+                                   f"({sample_cells / full:.4g} of the cells), solves/s scaled "
+                                   f"by the cell ratio; C++/OpenMP FP64 restatement of MAESTRO's "
+                                   f"macproject + FBoxLib MG (Fortran reference unbuildable)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+    return 0
+
+
+# ---- our arm ----------------------------------------------------------------------------------
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import numpy as np
+    import torch
+
+    from maestro_gb300 import build as _build_mod  # noqa: F401
+    from maestro_gb300 import capi
+    from maestro_gb300.build import build
+    from maestro_gb300.inputs import config_case
+    from maestro_gb300.macproject import BcTower, Layout, MacProjector
+
+    build()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    c = config_case(args.config, seed=args.seed + rank)
+    N = c.ncell
+    stream = torch.cuda.current_stream(dev)
+    to_dev = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a).transpose())).to(dev)  # noqa: E731
+    u0 = [to_dev(a) for a in c.umac]
+    rho = to_dev(c.rho)
+    rhs = to_dev(c.macrhs)
+    b0 = torch.from_numpy(c.beta0).to(dev)
+    b0e = torch.from_numpy(c.beta0_edge).to(dev)
+    nsteps = args.steps + args.warmup
+    work_u = [[torch.empty_like(x) for x in u0] for _ in range(nsteps)]
+    work_phi = [torch.empty_like(rho) for _ in range(nsteps)]
+    lay = Layout.tiled(c.n, c.box)
+    bc = BcTower(c.bc_lo, c.bc_hi)
+
+    def reset_inputs():
+        for k in range(nsteps):
+            for d in range(c.dm):
+                work_u[k][d].copy_(u0[d])
+            work_phi[k].zero_()
+        torch.cuda.synchronize()
+
+    def timed_run(precision, timing):
+        P = MacProjector(lay, c.dx, bc, precision=precision, stream=stream.cuda_stream,
+                         timing=int(timing))
+        reset_inputs()
+        stats = []
+
+        def one(k):
+            u = work_u[k]
+            st = P.macproject_dense(u[0].data_ptr(), u[1].data_ptr(),
+                                    u[2].data_ptr() if c.dm == 3 else 0,
+                                    work_phi[k].data_ptr(), rho.data_ptr(), rhs.data_ptr(),
+                                    b0.data_ptr(), b0e.data_ptr(), strict=True)
+            return st
+
+        for k in range(args.warmup):
+            one(k)
+        barrier()
+        clocks = Clocks(local)
+        clocks.start()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(args.warmup, nsteps):
+            stats.append(one(k))
+        e1.record(stream)
+        barrier()
+        ck = clocks.stop()
+        ms = e0.elapsed_time(e1)
+        P.close()
+        return max_over_ranks(ms), stats, ck
+
+    ms_mixed, st_mixed, ck_mixed = timed_run("mixed", timing=True)
+    ms_fp64, st_fp64, ck_fp64 = timed_run("fp64", timing=True)
+    K = args.steps
+    value = world * K / (ms_mixed / 1e3)
+    fp64_value = world * K / (ms_fp64 / 1e3)
+
+    # error of the mixed result against the FP64 GPU solve of the same inputs (last step)
+    reset_inputs()
+    Pm = MacProjector(lay, c.dx, bc, precision="mixed", stream=stream.cuda_stream)
+    Pd = MacProjector(lay, c.dx, bc, precision="fp64", stream=stream.cuda_stream)
+    ua, pa = work_u[0], work_phi[0]
+    ub, pb = work_u[1], work_phi[1]
+    Pm.macproject_dense(ua[0].data_ptr(), ua[1].data_ptr(), ua[2].data_ptr(), pa.data_ptr(),
+                        rho.data_ptr(), rhs.data_ptr(), b0.data_ptr(), b0e.data_ptr())
+    Pd.macproject_dense(ub[0].data_ptr(), ub[1].data_ptr(), ub[2].data_ptr(), pb.data_ptr(),
+                        rho.data_ptr(), rhs.data_ptr(), b0.data_ptr(), b0e.data_ptr())
+    torch.cuda.synchronize()
+    da = pa - pa.mean()
+    db = pb - pb.mean()
+    phi_err = float((da - db).abs().max() / db.abs().max())
+    u_err = max(float((x - y).abs().max() / y.abs().max()) for x, y in zip(ua, ub))
+    Pm.close()
+    Pd.close()
+
+    # ---- roofline of the dominant kernel: finest-level GS-RB half sweeps (mixed, FP32) ------
+    hbm_peak, peak_kind = peaks()
+    kt_ms = sum(s["ktime_ms"][capi.KT_NAMES.index("smooth")] for s in st_mixed)
+    kt_n = sum(s["ktime_launches"][capi.KT_NAMES.index("smooth")] for s in st_mixed)
+    # algorithmic bytes per half-sweep launch: half of the fused red+black sweep's
+    # phi, f, beta_x, beta_y, beta_z read + phi write (6 words per cell), FP32 words
+    alg_bytes = 3 * 4 * N
+    avg_s = (kt_ms / kt_n) / 1e3 if kt_n else float("nan")
+    achieved = alg_bytes / avg_s / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            tj = json.load(f)
+        ent = tj.get("gsrb_fp32_fine")
+        if ent and ent.get("cells"):
+            traffic = ent["dram_bytes_per_launch"] * N / ent["cells"]
+    roofline = {"bound": "hbm", "kernel": "k_gsrb<float> finest level (one colour)",
+                "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": traffic,
+                "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_s * 1e3,
+                "peak_kind": peak_kind}
+    cls_ms = {nm: sum(s["ktime_ms"][i] for s in st_mixed) / K for i, nm in enumerate(capi.KT_NAMES)}
+
+    # ---- e2e through the public C ABI with pinned host fabs ---------------------------------
+    e2e = None
+    if not args.no_e2e:
+        per = [b == capi.MAC_BC_PER for b in c.bc_lo]
+
+        def pinned_like(a):
+            t = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+            v = t.numpy().reshape(a.shape, order="F")
+            v[...] = a
+            return t, v
+
+        def fab_set():
+            keep = []
+            fu = []
+            for d in range(c.dm):
+                lst = []
+                for f in lay.to_fabs(c.umac[d], ng=1, face_dir=d, periodic=per):
+                    t, v = pinned_like(f)
+                    keep.append(t)
+                    lst.append(v)
+                fu.append(lst)
+            fr, fp, fs = [], [], []
+            for f in lay.to_fabs(c.rho, ng=1, periodic=per):
+                t, v = pinned_like(f)
+                keep.append(t)
+                fr.append(v)
+            for f in lay.to_fabs(c.phi0, ng=1):
+                t, v = pinned_like(f)
+                keep.append(t)
+                fp.append(v)
+            for f in lay.to_fabs(c.macrhs, ng=0):
+                t, v = pinned_like(f)
+                keep.append(t)
+                fs.append(v)
+            return keep, fu, fr, fp, fs
+
+        E = args.e2e_steps
+        sets = [fab_set() for _ in range(E + 1)]
+        P = MacProjector(lay, c.dx, bc, precision="mixed", stream=stream.cuda_stream)
+        nbytes = lambda lst: sum(x.nbytes for x in lst)  # noqa: E731
+        s0 = sets[0]
+        u_bytes = sum(nbytes(s0[1][d]) for d in range(c.dm))
+        h2d = 2 * u_bytes + nbytes(s0[2]) + nbytes(s0[4]) + 2 * nbytes(s0[3]) + 8 * (2 * c.n[-1] + 1)
+        d2h = u_bytes + nbytes(s0[3])
+        P.macproject(s0[1], s0[3], s0[2], s0[4], c.beta0, c.beta0_edge, strict=True)  # warm-up
+        barrier()
+        t0 = time.perf_counter()
+        for k in range(1, E + 1):
+            s = sets[k]
+            P.macproject(s[1], s[3], s[2], s[4], c.beta0, c.beta0_edge, strict=True)
+        barrier()
+        secs = max_over_ranks(time.perf_counter() - t0)
+        P.close()
+        e2e = {"value": world * E / secs, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "steps": E, "api": "mac_macproject (MAC_PTR_HOST, "
+               "pinned per-box fabs, 8 boxes of 128^3 + 1 ghost)", "precision": "mixed"}
+
+    # ---- CPU baseline: one full solve of the workload by the oracle (rank 0, N = 1) ---------
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        import oracle as O
+        nlev = O.nlevels_for_boxes([c.box])
+        t0 = time.perf_counter()
+        _, _, sto = O.macproject(c.umac, c.phi0, c.rho, c.dx, c.bc_lo, c.bc_hi, macrhs=c.macrhs,
+                                 beta0=c.beta0, beta0_edge=c.beta0_edge, nlevels=nlev)
+        secs = time.perf_counter() - t0
+        cpu = {"value": 1.0 / secs, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+               "sample": f"one full {c.n[0]}^3 FP64 solve ({sto['vcycles']} V-cycles), "
+                         f"C++/OpenMP restatement of MAESTRO macproject + FBoxLib MG"}
+
+    launches = sum(s["launches"] for s in st_mixed)
+    rr = max(s["rel_resid"] for s in st_mixed)
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+        "warmup": args.warmup, "ms_per_step": ms_mixed / K, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 V-cycles + f64 refinement",
+        "data": "synthetic (seeded stratified atmosphere)",
+        "config": {"workload": args.config, "n": list(c.n), "box": list(c.box), "rel_eps": 1e-10,
+                   "precision": "mixed", "l2": "inputs larger than L2 (0.5 GB per step, "
+                   "a distinct copy per step)", "parallelism": f"replicas x{world}"},
+        "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": ms_fp64 / K,
+                 "vcycles": st_fp64[-1]["vcycles"], "rel_resid": st_fp64[-1]["rel_resid"]},
+        "mixed_over_fp64": value / fp64_value,
+        "mixed": {"refine_iters": st_mixed[-1]["refine_iters"], "rel_resid": rr,
+                  "phi_err_vs_fp64": phi_err, "u_err_vs_fp64": u_err,
+                  "ms_by_class": cls_ms},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": ck_mixed,
+        "clocks_fp64": ck_fp64,
+    }
+    if rank == 0:
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -88,7 +88,20 @@ typedef struct mac_opts {
                                > 0: cap on the number of MG levels                             */
     int use_graph;          /* capture each V-cycle in a CUDA graph (1) or launch directly (0) */
     int verbose;            /* 0 silent, 1 per-solve summary on stderr                         */
+    int timing;             /* 1: CUDA-event timing of the finest-level kernel classes into
+                               mac_stats.ktime_* (events recorded inside the V-cycle graph)    */
 } mac_opts;
+
+/* Kernel classes of mac_stats.ktime_* (finest level unless stated). */
+#define MAC_KT_SMOOTH    0   /* red/black Gauss-Seidel half sweeps                            */
+#define MAC_KT_RESTRICT  1   /* defect + restriction to level 1                               */
+#define MAC_KT_COARSE    2   /* everything on levels >= 1 incl. the bottom solve              */
+#define MAC_KT_PROLONG   3   /* prolongation from level 1                                     */
+#define MAC_KT_ACCUM     4   /* FP64 accumulation phi += e (mixed)                            */
+#define MAC_KT_RESID     5   /* convergence residual (FP64)                                   */
+#define MAC_KT_SETUP     6   /* coefficients, right-hand side, layout conversion              */
+#define MAC_KT_CORRECT   7   /* velocity correction + layout conversion                       */
+#define MAC_KT_NCLASS    8
 
 typedef struct mac_stats {
     int status;             /* return code of the call                                         */
@@ -104,6 +117,9 @@ typedef struct mac_stats {
     double setup_ms;        /* device time: layout conversion + coefficients + RHS             */
     double solve_ms;        /* device time: multigrid                                          */
     double total_ms;        /* wall time of the call                                           */
+    long long launches;     /* CUDA kernels this call launched (graph replays included)         */
+    double ktime_ms[8];     /* device time per MAC_KT_* class (opts.timing), summed            */
+    int ktime_launches[8];  /* kernel launches per class                                       */
 } mac_stats;
 
 /* Fill *o with MAESTRO's MAC-projection defaults (FP64, alt energy fix off, 1e-10, V(2,2),

@@ -24,6 +24,7 @@ MAC_ERR_TOO_LARGE = -8
 MAC_BC_PER, MAC_BC_INT, MAC_BC_DIR, MAC_BC_NEU = -1, 0, 1, 2
 MAC_PREC_FP64, MAC_PREC_MIXED = 0, 1
 MAC_PTR_HOST, MAC_PTR_DEVICE = 0, 1
+KT_NAMES = ("smooth", "restrict", "coarse", "prolong", "accum", "resid", "setup", "correct")
 
 # Every symbol include/maestro_mac.h declares.
 EXPORTED = (
@@ -62,6 +63,7 @@ class MacOpts(ctypes.Structure):
         ("max_levels", ctypes.c_int),
         ("use_graph", ctypes.c_int),
         ("verbose", ctypes.c_int),
+        ("timing", ctypes.c_int),
     ]
 
 
@@ -80,6 +82,9 @@ class MacStats(ctypes.Structure):
         ("setup_ms", ctypes.c_double),
         ("solve_ms", ctypes.c_double),
         ("total_ms", ctypes.c_double),
+        ("launches", ctypes.c_longlong),
+        ("ktime_ms", ctypes.c_double * 8),
+        ("ktime_launches", ctypes.c_int * 8),
     ]
 
     def as_dict(self):
@@ -96,6 +101,9 @@ class MacStats(ctypes.Structure):
             "setup_ms": self.setup_ms,
             "solve_ms": self.solve_ms,
             "total_ms": self.total_ms,
+            "launches": self.launches,
+            "ktime_ms": [self.ktime_ms[i] for i in range(8)],
+            "ktime_launches": [self.ktime_launches[i] for i in range(8)],
         }
 
 

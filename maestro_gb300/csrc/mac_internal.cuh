@@ -142,8 +142,13 @@ struct mac_ctx {
     mac::Reduce red;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
-    // CUDA graphs of one V-cycle (fp64 and fp32 inner)
+    // CUDA graphs of one V-cycle (fp64 and fp32 inner) and their kernel-node counts
     cudaGraphExec_t vc_exec[2] = {nullptr, nullptr};
+    long long graph_kernels[2] = {0, 0};
+    long long issued = 0;                         // kernels launched (host count)
+    cudaEvent_t tev[8] = {};                      // per-iteration timing events (opts.timing)
+    double ktime_ms[8] = {};
+    int ktime_launches[8] = {};
 
     size_t bytes_allocated = 0;
     std::vector<void*> allocations;

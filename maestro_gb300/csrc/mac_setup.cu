@@ -517,6 +517,7 @@ int setup_fine_coefficients(mac_ctx* c, const double* beta0, const double* beta0
         P, L.d, c->rho, beta0, beta0e, L.a64.bx, L.a64.by, L.a64.bz, L.wall[0][0], L.wall[0][1],
         L.wall[1][0], L.wall[1][1], L.wall[2][0], L.wall[2][1], c->red.counters + 1);
     MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
     DiagParams D;
     for (int d = 0; d < 3; ++d) {
         D.bc_lo[d] = c->bc_lo[d];
@@ -527,6 +528,7 @@ int setup_fine_coefficients(mac_ctx* c, const double* beta0, const double* beta0
     k_build_diag<<<ceil_div(L.d.ncell, kBlock), kBlock, 0, c->stream>>>(
         L.d, D, L.a64.bx, L.a64.by, L.a64.bz, L.alpha, L.a64.diag, L.a64.invdiag);
     MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
     return MAC_OK;
 }
 
@@ -537,6 +539,7 @@ int setup_coarse_levels(mac_ctx* c) {
         k_coarsen_coef<<<ceil_div(C.d.ncell, kBlock), kBlock, 0, c->stream>>>(
             F.d, C.d, F.a64.bx, F.a64.by, F.a64.bz, F.alpha, C.a64.bx, C.a64.by, C.a64.bz, C.alpha);
         MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
         for (int d = 0; d < 3; ++d)
             for (int s = 0; s < 2; ++s) {
                 if (!C.wall[d][s]) continue;
@@ -549,6 +552,7 @@ int setup_coarse_levels(mac_ctx* c) {
                 k_coarsen_wall<<<ceil_div((long)np0 * np1, kBlock), kBlock, 0, c->stream>>>(
                     np0, np1, r[p0], r[p1], fn[p0], F.wall[d][s], C.wall[d][s]);
                 MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
             }
         DiagParams D;
         for (int d = 0; d < 3; ++d) {
@@ -560,6 +564,7 @@ int setup_coarse_levels(mac_ctx* c) {
         k_build_diag<<<ceil_div(C.d.ncell, kBlock), kBlock, 0, c->stream>>>(
             C.d, D, C.a64.bx, C.a64.by, C.a64.bz, C.alpha, C.a64.diag, C.a64.invdiag);
         MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
     }
     return MAC_OK;
 }
@@ -574,6 +579,7 @@ int setup_fp32_copies(mac_ctx* c) {
         for (int a = 0; a < 5; ++a) {
             k_to_f32<<<ceil_div(n, kBlock), kBlock, 0, c->stream>>>(n, src[a], dst[a]);
             MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
         }
     }
     return MAC_OK;
@@ -593,12 +599,15 @@ int setup_rhs(mac_ctx* c, const double* macrhs, bool have_beta0) {
     k_rhs<<<nb, kBlock, 0, c->stream>>>(P, L.d, c->u[0], c->u[1], c->u[2], macrhs, c->beta0,
                                         c->beta0e, L.a64.f, c->red.partial);
     MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
     k_rhs_final<<<1, 1024, 0, c->stream>>>(nb, L.d.ncell, c->singular ? 1 : 0, c->red.partial,
                                            c->red.scalars);
     MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
     if (c->singular) {
         k_sub_mean<<<nb, kBlock, 0, c->stream>>>(L.d.ncell, L.a64.f, c->red.scalars);
         MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
     }
     return MAC_OK;
 }
@@ -620,6 +629,7 @@ int correct_velocity(mac_ctx* c, bool have_beta0) {
         k_correct<<<ceil_div(nf, kBlock), kBlock, 0, c->stream>>>(
             P, L.d, c->u[d], L.a64.phi, bd[d], L.wall[d][0], L.wall[d][1], c->beta0, c->beta0e);
         MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
     }
     return MAC_OK;
 }
@@ -628,6 +638,7 @@ int natural_to_level0(mac_ctx* c, const double* src, double* dst) {
     const Dims d = level0_dims(c);
     k_nat_to_l0<<<ceil_div(d.ncell, kBlock), kBlock, 0, c->stream>>>(d, src, dst);
     MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
     return MAC_OK;
 }
 
@@ -635,6 +646,7 @@ int level0_to_natural(mac_ctx* c, const double* src, double* dst) {
     const Dims d = level0_dims(c);
     k_l0_to_nat<<<ceil_div(d.ncell, kBlock), kBlock, 0, c->stream>>>(d, src, dst);
     MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
     return MAC_OK;
 }
 
@@ -758,6 +770,7 @@ int gather_common(mac_ctx* c, int ptr_kind, const double* const* fabs, int ng, i
     dim3 grid(64, c->g.nboxes);
     k_gather<<<grid, kBlock, 0, c->stream>>>(P, table, dst);
     MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
     if (ptr_kind == MAC_PTR_HOST) MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
     return MAC_OK;
 }
@@ -793,6 +806,7 @@ int scatter_common(mac_ctx* c, int ptr_kind, double* const* fabs, int ng, int di
     dim3 grid(64, c->g.nboxes);
     k_scatter<<<grid, kBlock, 0, c->stream>>>(P, table, src);
     MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
     if (ptr_kind == MAC_PTR_HOST) {
         for (int b = 0; b < c->g.nboxes; ++b) {
             size_t e = 1;
@@ -848,6 +862,7 @@ int setup_fine_from_faces(mac_ctx* c, const double* fx, const double* fy, const 
         L.a64.bz, L.wall[0][0], L.wall[0][1], L.wall[1][0], L.wall[1][1], L.wall[2][0],
         L.wall[2][1]);
     MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
     DiagParams D;
     for (int d = 0; d < 3; ++d) {
         D.bc_lo[d] = c->bc_lo[d];
@@ -859,6 +874,7 @@ int setup_fine_from_faces(mac_ctx* c, const double* fx, const double* fy, const 
         L.d, D, L.a64.bx, L.a64.by, L.a64.bz, alpha_nat ? L.alpha : nullptr, L.a64.diag,
         L.a64.invdiag);
     MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
     return MAC_OK;
 }
 
@@ -867,12 +883,15 @@ int setup_rhs_from(mac_ctx* c, const double* rh_nat) {
     const int nb = ceil_div(L.d.ncell, kBlock);
     k_load_rhs<<<nb, kBlock, 0, c->stream>>>(L.d, rh_nat, L.a64.f, c->red.partial);
     MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
     k_rhs_final<<<1, 1024, 0, c->stream>>>(nb, L.d.ncell, c->singular ? 1 : 0, c->red.partial,
                                            c->red.scalars);
     MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
     if (c->singular) {
         k_sub_mean<<<nb, kBlock, 0, c->stream>>>(L.d.ncell, L.a64.f, c->red.scalars);
         MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
     }
     return MAC_OK;
 }

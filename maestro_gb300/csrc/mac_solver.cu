@@ -95,43 +95,86 @@ void vcycle(mac_ctx* c, int l) {
     Level& L = c->lev[l];
     LevelArrays<T>& a = arrays<T>(L);
     const mac_opts& o = c->o;
+    const bool tm = o.timing && l == 0;
     if (l == c->nlevels - 1) {
         launch_bottom<T>(L.d, L.a64, a.phi, a.f, c->bottom_scratch, c->singular, o.nub,
                          o.bottom_eps, o.bottom_max_iter, c->red.counters, c->stream);
+        ++c->issued;
         return;
     }
+    if (tm) cudaEventRecordWithFlags(c->tev[0], c->stream, cudaEventRecordExternal);
     for (int s = 0; s < o.nu1; ++s) {
         launch_gsrb<T>(L.d, 0, a, c->stream);
         launch_gsrb<T>(L.d, 1, a, c->stream);
+        c->issued += 2;
     }
     Level& C = c->lev[l + 1];
     LevelArrays<T>& ac = arrays<T>(C);
+    if (tm) cudaEventRecordWithFlags(c->tev[1], c->stream, cudaEventRecordExternal);
     launch_resid_restrict<T>(L.d, C.d, a, ac.f, o.nu1 > 0, c->stream);
+    ++c->issued;
+    if (tm) cudaEventRecordWithFlags(c->tev[2], c->stream, cudaEventRecordExternal);
     cudaMemsetAsync(ac.phi, 0, sizeof(T) * C.d.ncell, c->stream);
     vcycle<T>(c, l + 1);
+    if (tm) cudaEventRecordWithFlags(c->tev[3], c->stream, cudaEventRecordExternal);
     launch_prolong_add<T>(L.d, C.d, bc_desc(c), ac.phi, a.phi, c->stream);
+    ++c->issued;
+    if (tm) cudaEventRecordWithFlags(c->tev[4], c->stream, cudaEventRecordExternal);
     for (int s = 0; s < o.nu2; ++s) {
         launch_gsrb<T>(L.d, 0, a, c->stream);
         launch_gsrb<T>(L.d, 1, a, c->stream);
+        c->issued += 2;
     }
+    if (tm) cudaEventRecordWithFlags(c->tev[5], c->stream, cudaEventRecordExternal);
 }
 
 // One iteration of the outer loop, ending with the max-norm of the fine residual in
 // red.maxbits and its copy in pinned host memory.
 void issue_iteration(mac_ctx* c, int prec) {
     Level& F = c->lev[0];
+    const bool tm = c->o.timing;
     cudaMemsetAsync(c->red.maxbits, 0, sizeof(unsigned long long), c->stream);
     if (prec == MAC_PREC_FP64) {
         vcycle<double>(c, 0);
+        if (tm) cudaEventRecordWithFlags(c->tev[6], c->stream, cudaEventRecordExternal);
         launch_resid_norm<double>(F.d, F.a64, c->o.nu2 > 0, c->red.maxbits, c->stream);
+        ++c->issued;
     } else {
         cudaMemsetAsync(F.a32.phi, 0, sizeof(float) * F.d.ncell, c->stream);
         vcycle<float>(c, 0);
         launch_accumulate(F.d, F.a64.phi, F.a32.phi, c->stream);
+        ++c->issued;
+        if (tm) cudaEventRecordWithFlags(c->tev[6], c->stream, cudaEventRecordExternal);
         launch_resid64_to32(F.d, F.a64, F.a32.f, c->red.maxbits, c->stream);
+        ++c->issued;
     }
+    if (tm) cudaEventRecordWithFlags(c->tev[7], c->stream, cudaEventRecordExternal);
     cudaMemcpyAsync(c->red.h_maxbits, c->red.maxbits, sizeof(unsigned long long),
                     cudaMemcpyDeviceToHost, c->stream);
+}
+
+// Accumulate the per-class device times of the iteration that just completed.
+void collect_timing(mac_ctx* c, int prec) {
+    if (!c->o.timing) return;
+    float t[7];
+    for (int e = 0; e < 7; ++e) {
+        t[e] = 0.f;
+        cudaEventElapsedTime(&t[e], c->tev[e], c->tev[e + 1]);
+    }
+    const mac_opts& o = c->o;
+    c->ktime_ms[MAC_KT_SMOOTH] += t[0] + t[4];
+    c->ktime_launches[MAC_KT_SMOOTH] += 2 * (o.nu1 + o.nu2);
+    c->ktime_ms[MAC_KT_RESTRICT] += t[1];
+    c->ktime_launches[MAC_KT_RESTRICT] += 1;
+    c->ktime_ms[MAC_KT_COARSE] += t[2];
+    c->ktime_ms[MAC_KT_PROLONG] += t[3];
+    c->ktime_launches[MAC_KT_PROLONG] += 1;
+    if (prec == MAC_PREC_MIXED) {
+        c->ktime_ms[MAC_KT_ACCUM] += t[5];
+        c->ktime_launches[MAC_KT_ACCUM] += 1;
+    }
+    c->ktime_ms[MAC_KT_RESID] += t[6];
+    c->ktime_launches[MAC_KT_RESID] += 1;
 }
 
 int get_iteration_exec(mac_ctx* c, int prec, cudaGraphExec_t* out) {
@@ -141,9 +184,12 @@ int get_iteration_exec(mac_ctx* c, int prec, cudaGraphExec_t* out) {
         return MAC_OK;
     }
     cudaGraph_t g = nullptr;
+    const long long before = c->issued;
     MAC_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     issue_iteration(c, prec);
     MAC_CUDA_TRY(cudaStreamEndCapture(c->stream, &g));
+    c->graph_kernels[slot] = c->issued - before;
+    c->issued = before;
     cudaGraphExec_t ex = nullptr;
     cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
     cudaGraphDestroy(g);
@@ -167,12 +213,14 @@ int run_iteration(mac_ctx* c, int prec, double* res_out) {
         int rc = get_iteration_exec(c, prec, &ex);
         if (rc) return rc;
         MAC_CUDA_TRY(cudaGraphLaunch(ex, c->stream));
+        c->issued += c->graph_kernels[prec == MAC_PREC_FP64 ? 0 : 1];
     } else {
         issue_iteration(c, prec);
         MAC_CUDA_TRY(cudaGetLastError());
     }
     MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
     *res_out = bits_to_double(*c->red.h_maxbits);
+    collect_timing(c, prec);
     return MAC_OK;
 }
 
@@ -216,6 +264,7 @@ int run_solve(mac_ctx* c, mac_stats* st) {
         launch_resid_norm<double>(F.d, F.a64, false, c->red.maxbits, c->stream);
     else
         launch_resid64_to32(F.d, F.a64, F.a32.f, c->red.maxbits, c->stream);
+    ++c->issued;
     MAC_CUDA_TRY(cudaGetLastError());
     MAC_CUDA_TRY(cudaMemcpyAsync(c->red.h_maxbits, c->red.maxbits, sizeof(unsigned long long),
                                  cudaMemcpyDeviceToHost, c->stream));
@@ -381,6 +430,7 @@ int ctx_alloc(mac_ctx* c) {
     rc |= alloc_arr(c, &c->d_boxes, (size_t)c->box_table_cap);
     if (rc) return MAC_ERR_ALLOC;
     for (int e = 0; e < 4; ++e) MAC_CUDA_TRY(cudaEventCreate(&c->ev[e]));
+    for (int e = 0; e < 8; ++e) MAC_CUDA_TRY(cudaEventCreate(&c->tev[e]));
     MAC_CUDA_TRY(cudaMemset(c->red.counters, 0, 4 * sizeof(int)));
     return MAC_OK;
 }
@@ -397,6 +447,8 @@ void ctx_free(mac_ctx* c) {
     if (c->h_boxes) cudaFreeHost(c->h_boxes);
     for (int e = 0; e < 4; ++e)
         if (c->ev[e]) cudaEventDestroy(c->ev[e]);
+    for (int e = 0; e < 8; ++e)
+        if (c->tev[e]) cudaEventDestroy(c->tev[e]);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     c->stream = nullptr;
 }
@@ -441,13 +493,17 @@ int core_macproject(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats
     rc = natural_to_level0(c, c->phin, F.a64.phi);
     if (rc) return rc;
     cudaEventRecord(c->ev[1], c->stream);
+    const long long setup_kernels = c->issued;
     const int solve_rc = run_solve(c, st);
     if (solve_rc != MAC_OK && solve_rc != MAC_ERR_NOT_CONVERGED) return solve_rc;
     cudaEventRecord(c->ev[2], c->stream);
+    const long long before_corr = c->issued;
     rc = correct_velocity(c, have_beta0);
     if (rc) return rc;
     rc = level0_to_natural(c, F.a64.phi, c->phin);
     if (rc) return rc;
+    c->ktime_launches[MAC_KT_CORRECT] += (int)(c->issued - before_corr);
+    c->ktime_launches[MAC_KT_SETUP] += (int)setup_kernels;
     cudaEventRecord(c->ev[3], c->stream);
     MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
     float a = 0.f, b = 0.f, cc = 0.f;
@@ -456,10 +512,27 @@ int core_macproject(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats
     cudaEventElapsedTime(&cc, c->ev[2], c->ev[3]);
     st->setup_ms = a + cc;
     st->solve_ms = b;
+    c->ktime_ms[MAC_KT_SETUP] += a;
+    c->ktime_ms[MAC_KT_CORRECT] += cc;
     return solve_rc;
 }
 
-void fill_common_stats(const mac_ctx* c, mac_stats* st) { st->nlevels = c->nlevels; }
+void fill_common_stats(mac_ctx* c, mac_stats* st) {
+    st->nlevels = c->nlevels;
+    c->issued = 0;
+    for (int k = 0; k < MAC_KT_NCLASS; ++k) {
+        c->ktime_ms[k] = 0.0;
+        c->ktime_launches[k] = 0;
+    }
+}
+
+void finish_stats(mac_ctx* c, mac_stats* st) {
+    st->launches = c->issued;
+    for (int k = 0; k < MAC_KT_NCLASS; ++k) {
+        st->ktime_ms[k] = c->ktime_ms[k];
+        st->ktime_launches[k] = c->ktime_launches[k];
+    }
+}
 
 void report(const mac_ctx* c, const char* what, const mac_stats* st) {
     if (c->o.verbose <= 0) return;
@@ -627,6 +700,7 @@ int mac_macproject_dense(mac_ctx* c, double* ux, double* uy, double* uz, double*
     c->phin = saved_phin;
     st->status = rc;
     st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    finish_stats(c, st);
     report(c, "macproject_dense", st);
     return rc;
 }
@@ -677,6 +751,7 @@ int mac_macproject(mac_ctx* c, int ptr_kind, double* const* umac, int ng_u, doub
     if (!rc) rc = solve_rc;
     st->status = rc;
     st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    finish_stats(c, st);
     report(c, "macproject", st);
     return rc;
 }
@@ -738,6 +813,7 @@ int mac_multigrid(mac_ctx* c, int ptr_kind, const double* const* rh, int ng_rh,
     if (!rc) rc = solve_rc;
     st->status = rc;
     st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    finish_stats(c, st);
     report(c, "mac_multigrid", st);
     return rc;
 }

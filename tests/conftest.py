@@ -16,7 +16,7 @@ def pytest_configure(config):
 @pytest.fixture(scope="session")
 def cuda_lib():
     """The built CUDA library; GPU tests fail (not skip) when it is missing."""
-    from maestro_gb300 import build as _b
     from maestro_gb300 import capi
-    _b.build()
+    from maestro_gb300.build import build
+    build()
     return capi.lib()
