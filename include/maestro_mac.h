@@ -215,6 +215,34 @@ int mac_macproject_adjoint_dense(mac_ctx* ctx,
                                  double* drinv, double* dbeta0, double* dmacrhs,
                                  double* phi_out, mac_stats* stats);
 
+/* ---- allocation-free small solve ----------------------------------------------------------- */
+#define MAC_NOALLOC_MAX_CELLS 4096   /* largest level mac_solve_small_noalloc accepts (cells)  */
+
+/*
+ * (alpha - div beta grad) phi = rh on one small single-box level, allocating no device memory.
+ * No counterpart in the reference.
+ * For callers that cannot allocate on the GPU -- a host code whose device memory belongs to its
+ * own pool allocator, a loop held to a fixed memory budget, or a call site where cudaMalloc is
+ * forbidden or too slow.  The caller passes device pointers to its inputs and output (natural
+ * layout, x fastest): rh and phi (n[0]*n[1]*n[2]; phi = initial guess in, solution out),
+ * beta_x/y/z face coefficients ((n[d]+1) along d; beta_z unused in 2-D), alpha (cells, or NULL
+ * for the MAC case).  Same operator and boundary handling as mac_multigrid; solved by the
+ * single-CTA BiCGStab of the multigrid's coarsest level, run to
+ * ||rh - L phi||_inf <= rel_eps ||rh||_inf (mean of rh removed when the problem is singular)
+ * within max_iter iterations (else MAC_ERR_NOT_CONVERGED).
+ * Limits: at most MAC_NOALLOC_MAX_CELLS cells (else MAC_ERR_TOO_LARGE).  Its work storage is one
+ * fixed array of 14*MAC_NOALLOC_MAX_CELLS doubles that every GPU loading the library holds until
+ * the process exits.  All calls share that array and it keeps the last call's contents; calls
+ * that overlap on the GPU (other streams or host threads) race -- serialise them.  The first call
+ * on a device looks up the array's address with that device current; make it before any stream
+ * capture.  Blocks the host until the solve has finished (it reads the result back).
+ */
+int mac_solve_small_noalloc(int dm, const int* n, const double* dx, const int* bc_lo,
+                            const int* bc_hi, const double* rh, double* phi,
+                            const double* beta_x, const double* beta_y, const double* beta_z,
+                            const double* alpha, double rel_eps, int max_iter,
+                            void* cuda_stream, mac_stats* stats);
+
 /* beta0 cell -> edge values (Source/cell_to_edge.f90:14-70), host arrays, one level. */
 int mac_cell_to_edge(int nr, const double* s0_cell, double* s0_edge);
 

@@ -31,7 +31,9 @@ EXPORTED = (
     "mac_default_opts", "mac_strerror", "mac_version", "mac_ctx_create", "mac_ctx_destroy",
     "mac_ctx_set_opts", "mac_ctx_levels", "mac_macproject", "mac_multigrid",
     "mac_macproject_dense", "mac_macproject_adjoint_dense", "mac_cell_to_edge",
+    "mac_solve_small_noalloc",
 )
+MAC_NOALLOC_MAX_CELLS = 4096
 
 
 class MacGeom(ctypes.Structure):
@@ -159,6 +161,10 @@ def lib():
     L.mac_macproject_adjoint_dense.restype = ctypes.c_int
     L.mac_cell_to_edge.argtypes = [ctypes.c_int, dp, dp]
     L.mac_cell_to_edge.restype = ctypes.c_int
+    ip = P(ctypes.c_int)
+    L.mac_solve_small_noalloc.argtypes = [ctypes.c_int, ip, dp, ip, ip, vp, vp, vp, vp, vp, vp,
+                                          ctypes.c_double, ctypes.c_int, vp, P(MacStats)]
+    L.mac_solve_small_noalloc.restype = ctypes.c_int
     _lib = L
     return L
 
