@@ -54,6 +54,12 @@ struct Dims {
     int rz;           // coarsening ratio in z to the next level (1 in 2-D)
 };
 
+// Index of cell (i, j, k) of a level in its storage layout.
+__host__ __device__ __forceinline__ int level_index(const Dims& d, int i, int j, int k) {
+    if (d.split) return ((i + j + k) & 1) * d.half + (j + d.n1 * k) * d.hn0 + (i >> 1);
+    return i + d.n0 * (j + d.n1 * k);
+}
+
 // Boundary description for the prolongation ghosts (per direction, low/high).
 struct BcDesc {
     int lo[3];
@@ -201,6 +207,13 @@ int scatter_faces(mac_ctx* c, int ptr_kind, double* const* fabs, int ng, int dir
 
 // ---- solver (mac_solver.cu) -----------------------------------------------------------------
 int run_solve(mac_ctx* c, mac_stats* st);
+// Forward projection on the whole-domain arrays already in c->u / c->rho / c->phin; leaves the
+// level-0 coefficients and phi (level-0 layout) in place.
+int forward_projection(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats* st);
+int set_call_state(mac_ctx* c, bool with_alpha);
+int load_beta0(mac_ctx* c, int ptr_kind, const double* b0, const double* b0e);
+void begin_call_stats(mac_ctx* c, mac_stats* st);
+void end_call_stats(mac_ctx* c, mac_stats* st);
 int alloc_device(mac_ctx* c, void** p, size_t bytes);
 
 inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }

@@ -20,10 +20,7 @@ namespace {
 
 constexpr int kBlock = 256;
 
-__device__ __forceinline__ int lidx(const Dims& d, int i, int j, int k) {
-    if (d.split) return ((i + j + k) & 1) * d.half + (j + d.n1 * k) * d.hn0 + (i >> 1);
-    return i + d.n0 * (j + d.n1 * k);
-}
+__device__ __forceinline__ int lidx(const Dims& d, int i, int j, int k) { return level_index(d, i, j, k); }
 
 struct FineParams {
     int n[3];

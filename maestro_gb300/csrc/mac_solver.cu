@@ -454,7 +454,7 @@ void ctx_free(mac_ctx* c) {
 }
 
 // Copy a 1-D beta0 array (host or device) into the context.
-int load_beta0(mac_ctx* c, int ptr_kind, const double* b0, const double* b0e) {
+int load_beta0_impl(mac_ctx* c, int ptr_kind, const double* b0, const double* b0e) {
     const int nr = c->n[c->va];
     const cudaMemcpyKind k = ptr_kind == MAC_PTR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     MAC_CUDA_TRY(cudaMemcpyAsync(c->beta0, b0, sizeof(double) * nr, k, c->stream));
@@ -464,7 +464,7 @@ int load_beta0(mac_ctx* c, int ptr_kind, const double* b0, const double* b0e) {
 
 // Per-call operator state: alpha on/off (Helmholtz) and whether the problem is singular.
 // CUDA graphs bake the singular flag into the bottom solve, so they are dropped on a change.
-int set_call_state(mac_ctx* c, bool with_alpha) {
+int set_call_state_impl(mac_ctx* c, bool with_alpha) {
     for (auto& L : c->lev) {
         if (with_alpha && !L.alpha_store) {
             int rc = alloc_arr(c, &L.alpha_store, (size_t)L.d.ncell);
@@ -482,7 +482,7 @@ int set_call_state(mac_ctx* c, bool with_alpha) {
 int core_macproject(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats* st) {
     Level& F = c->lev[0];
     cudaEventRecord(c->ev[0], c->stream);
-    int rc = set_call_state(c, false);
+    int rc = set_call_state_impl(c, false);
     if (rc) return rc;
     rc = setup_fine_coefficients(c, have_beta0 ? c->beta0 : nullptr, have_beta0 ? c->beta0e : nullptr);
     if (rc) return rc;
@@ -545,6 +545,18 @@ void report(const mac_ctx* c, const char* what, const mac_stats* st) {
 }
 
 }  // namespace
+
+namespace mac {
+int forward_projection(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats* st) {
+    return core_macproject(c, macrhs, have_beta0, st);
+}
+int set_call_state(mac_ctx* c, bool with_alpha) { return set_call_state_impl(c, with_alpha); }
+int load_beta0(mac_ctx* c, int ptr_kind, const double* b0, const double* b0e) {
+    return load_beta0_impl(c, ptr_kind, b0, b0e);
+}
+void begin_call_stats(mac_ctx* c, mac_stats* st) { fill_common_stats(c, st); }
+void end_call_stats(mac_ctx* c, mac_stats* st) { finish_stats(c, st); }
+}  // namespace mac
 
 extern "C" {
 
@@ -691,7 +703,7 @@ int mac_macproject_dense(mac_ctx* c, double* ux, double* uy, double* uz, double*
     c->rho = const_cast<double*>(rho);
     c->phin = phi;
     int rc = MAC_OK;
-    if (beta0) rc = load_beta0(c, MAC_PTR_DEVICE, beta0, beta0_edge);
+    if (beta0) rc = load_beta0_impl(c, MAC_PTR_DEVICE, beta0, beta0_edge);
     if (!rc) rc = core_macproject(c, macrhs, beta0 != nullptr, st);
     c->u[0] = saved_u[0];
     c->u[1] = saved_u[1];
@@ -732,7 +744,7 @@ int mac_macproject(mac_ctx* c, int ptr_kind, double* const* umac, int ng_u, doub
     if (!rc) rc = gather_cells(c, ptr_kind, rho, ng_rho, rho_ncomp, rho_comp, c->rho);
     if (!rc && macrhs) rc = gather_cells(c, ptr_kind, macrhs, ng_rhs, 1, 0, c->rhs);
     if (!rc) rc = gather_cells(c, ptr_kind, (const double* const*)phi, ng_phi, 1, 0, c->phin);
-    if (!rc && beta0_1d) rc = load_beta0(c, ptr_kind, beta0_1d, beta0_1d_edge);
+    if (!rc && beta0_1d) rc = load_beta0_impl(c, ptr_kind, beta0_1d, beta0_1d_edge);
     int solve_rc = MAC_OK;
     if (!rc) {
         solve_rc = core_macproject(c, macrhs ? c->rhs : nullptr, beta0_1d != nullptr, st);
@@ -774,7 +786,7 @@ int mac_multigrid(mac_ctx* c, int ptr_kind, const double* const* rh, int ng_rh,
     const auto t0 = std::chrono::steady_clock::now();
     fill_common_stats(c, st);
     Level& F = c->lev[0];
-    int rc = set_call_state(c, alpha != nullptr);
+    int rc = set_call_state_impl(c, alpha != nullptr);
     for (int d = 0; d < c->dm && !rc; ++d)
         rc = gather_faces(c, ptr_kind, beta + d * nb, ng_beta, d, c->u[d]);
     if (!rc) rc = gather_cells(c, ptr_kind, rh, ng_rh, 1, 0, c->rhs);
