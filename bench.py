@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--seed", type=int, default=1234)
+    ap.add_argument("--inner", type=int, default=3,
+                    help="mixed precision: FP32 V-cycles per FP64 refinement step")
     return ap.parse_args()
 
 
@@ -227,7 +229,7 @@ def main():
 
     def timed_run(precision, timing):
         P = MacProjector(lay, c.dx, bc, precision=precision, stream=stream.cuda_stream,
-                         timing=int(timing))
+                         timing=int(timing), inner_vcycles=args.inner)
         reset_inputs()
         stats = []
 
@@ -264,7 +266,8 @@ def main():
 
     # error of the mixed result against the FP64 GPU solve of the same inputs (last step)
     reset_inputs()
-    Pm = MacProjector(lay, c.dx, bc, precision="mixed", stream=stream.cuda_stream)
+    Pm = MacProjector(lay, c.dx, bc, precision="mixed", stream=stream.cuda_stream,
+                      inner_vcycles=args.inner)
     Pd = MacProjector(lay, c.dx, bc, precision="fp64", stream=stream.cuda_stream)
     ua, pa = work_u[0], work_phi[0]
     ub, pb = work_u[1], work_phi[1]
@@ -342,7 +345,8 @@ def main():
 
         E = args.e2e_steps
         sets = [fab_set() for _ in range(E + 1)]
-        P = MacProjector(lay, c.dx, bc, precision="mixed", stream=stream.cuda_stream)
+        P = MacProjector(lay, c.dx, bc, precision="mixed", stream=stream.cuda_stream,
+                         inner_vcycles=args.inner)
         nbytes = lambda lst: sum(x.nbytes for x in lst)  # noqa: E731
         s0 = sets[0]
         u_bytes = sum(nbytes(s0[1][d]) for d in range(c.dm))
@@ -387,7 +391,8 @@ def main():
         "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": ms_fp64 / K,
                  "vcycles": st_fp64[-1]["vcycles"], "rel_resid": st_fp64[-1]["rel_resid"]},
         "mixed_over_fp64": value / fp64_value,
-        "mixed": {"refine_iters": st_mixed[-1]["refine_iters"], "rel_resid": rr,
+        "mixed": {"refine_iters": st_mixed[-1]["refine_iters"], "inner_vcycles": args.inner,
+                  "vcycles": st_mixed[-1]["refine_iters"] * args.inner, "rel_resid": rr,
                   "phi_err_vs_fp64": phi_err, "u_err_vs_fp64": u_err,
                   "ms_by_class": cls_ms},
         "roofline": roofline,

@@ -90,6 +90,10 @@ typedef struct mac_opts {
     int verbose;            /* 0 silent, 1 per-solve summary on stderr                         */
     int timing;             /* 1: CUDA-event timing of the finest-level kernel classes into
                                mac_stats.ktime_* (events recorded inside the V-cycle graph)    */
+    int inner_vcycles;      /* mixed precision: FP32 V-cycles per FP64 refinement step (>= 1;
+                               default 3); the FP64 residual is formed once per step           */
+    int coarse_tail;        /* 1 (default): the levels small enough for shared memory and the
+                               bottom solve run as one single-CTA kernel (same arithmetic)     */
 } mac_opts;
 
 /* Kernel classes of mac_stats.ktime_* (finest level unless stated). */

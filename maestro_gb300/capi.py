@@ -66,6 +66,8 @@ class MacOpts(ctypes.Structure):
         ("use_graph", ctypes.c_int),
         ("verbose", ctypes.c_int),
         ("timing", ctypes.c_int),
+        ("inner_vcycles", ctypes.c_int),
+        ("coarse_tail", ctypes.c_int),
     ]
 
 

@@ -24,6 +24,7 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <cstring>
 #include <vector>
 
 #include "maestro_mac.h"
@@ -59,6 +60,47 @@ __host__ __device__ __forceinline__ int level_index(const Dims& d, int i, int j,
     if (d.split) return ((i + j + k) & 1) * d.half + (j + d.n1 * k) * d.hn0 + (i >> 1);
     return i + d.n0 * (j + d.n1 * k);
 }
+
+// 1/x in FP64 without the division instruction sequence: the hardware reciprocal estimate
+// (rcp.approx.ftz.f64, on the special-function unit) refined by one third-order Newton step
+// y <- y0 + y0 (e + e^2), e = 1 - x y0, which cubes the estimate's relative error, so the result
+// is within rounding of 1/x.  Zero, subnormal, huge or non-finite inputs (tested on the exponent
+// bits: no FP64 instruction) use the IEEE division.
+__device__ __forceinline__ double recip_nr(double x) {
+    const unsigned ex = (unsigned)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7FFu;
+    if (ex < 64u || ex > 1980u) return 1.0 / x;
+    double y0;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y0) : "d"(x));
+    const double e = fma(-x, y0, 1.0);
+    return fma(y0, fma(e, e, e), y0);
+}
+
+// Order-preserving map of a double onto unsigned 64-bit integers (max/min on the integer pipe;
+// NaN maps above +inf / below -inf depending on its sign bit).
+__device__ __forceinline__ unsigned long long ordered_bits(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
+}
+__host__ __device__ inline double from_ordered_bits(unsigned long long u) {
+    const unsigned long long b = (u >> 63) ? (u & 0x7FFFFFFFFFFFFFFFULL) : ~u;
+    double d;
+    memcpy(&d, &b, sizeof(d));
+    return d;
+}
+
+// Positive, finite double (integer test on the bit pattern: no FP64 instructions).
+__device__ __forceinline__ bool positive_finite(double v) {
+    const long long b = __double_as_longlong(v);
+    return b > 0 && b < 0x7FF0000000000000LL;
+}
+
+// Per-layer factor tables (k_beta0_tables), nr+1 entries each, vertical index r:
+enum {
+    kTabFac0 = 0,   // beta0_f^p * 2 / h_d^2 of the low face along d (3 tables: d = 0, 1, 2)
+    kTabG0 = 3,     // beta0_f / dx_d (3 tables): divergence of beta0 U
+    kTabK0 = 6,     // h_d / beta0_f (3 tables): correction U -= beta' K (phi_hi - phi_lo)
+    kTabCount = 9
+};
 
 // Boundary description for the prolongation ghosts (per direction, low/high).
 struct BcDesc {
@@ -134,6 +176,8 @@ struct mac_ctx {
     double* phin = nullptr;                       // phi natural
     double* beta0 = nullptr;                      // [nr]
     double* beta0e = nullptr;                     // [nr+1]
+    // per vertical index r: the kTab* factor tables, (nr+1) doubles each
+    double* b0tab = nullptr;
     double* scratch = nullptr;                    // generic FP64 scratch (ncell)
     // caller-layout staging
     double* staging = nullptr;
@@ -152,7 +196,16 @@ struct mac_ctx {
     cudaGraphExec_t vc_exec[2] = {nullptr, nullptr};
     long long graph_kernels[2] = {0, 0};
     long long issued = 0;                         // kernels launched (host count)
-    cudaEvent_t tev[8] = {};                      // per-iteration timing events (opts.timing)
+    cudaEvent_t tev[4][8] = {};                   // timing events of up to 4 V-cycles per iteration
+    cudaEvent_t tail[3] = {};                     // before/after accumulation, after the residual
+    int vtimer = 0;                               // inner V-cycle being issued (timing slot)
+    // finest level of the mixed solve: FP32 density (level-0 layout) and the per-layer FP32 face
+    // factors of OtfParams (kOtfTables tables of nr+1), for coefficients computed on the fly
+    float* rho32 = nullptr;
+    float* fac32 = nullptr;
+    bool otf = false;                             // finest-level FP32 kernels use rho32
+    int tail_start[2] = {-1, -1};                 // first tail level (FP64, FP32); -1: none
+    size_t tail_smem[2] = {0, 0};
     double ktime_ms[8] = {};
     int ktime_launches[8] = {};
 
@@ -177,10 +230,61 @@ void launch_resid_norm(const Dims& d, const LevelArrays<T>& a, bool red_only,
 void launch_resid64_to32(const Dims& d, const LevelArrays<double>& a, float* r32,
                          unsigned long long* maxbits, cudaStream_t s);
 void launch_accumulate(const Dims& d, double* phi, const float* e, cudaStream_t s);
+// Finest-level FP32 kernels with face coefficients computed from rho32 (mixed precision).
+// Per-layer FP32 face factors beta0_f^p * 2 / h_d^2 (tables of nr+1 floats, vertical index r):
+//   0: x faces; 1: y faces (3-D: horizontal; 2-D: unused); 2: low vertical face of layer r,
+//   3: high vertical face of layer r -- both zero where the face is a non-periodic wall;
+//   4: Dirichlet diagonal term of layer r (wall factor of the vertical walls touching it).
+constexpr int kOtfTables = 5;
+struct OtfParams {
+    int n[3];
+    int per[3];
+    int dlo[3], dhi[3];   // Dirichlet flags
+    int has_dir;          // any Dirichlet face
+    int va;
+    int dm;
+    const float* fac;     // kOtfTables tables of (n[va] + 1)
+    const float* rho;     // level-0 layout
+};
+void launch_gsrb_otf(const Dims& d, const OtfParams& P, int colour, float* e, const float* r,
+                     cudaStream_t s);
+void launch_resid_restrict_otf(const Dims& fine, const Dims& coarse, const OtfParams& P,
+                               const float* e, const float* r, float* fc, bool red_only,
+                               cudaStream_t s);
+
 template <typename Tio>
 void launch_bottom(const Dims& d, const LevelArrays<double>& a64, Tio* x, const Tio* f,
                    double* scratch, bool singular, int nub, double eps, int max_iter,
                    int* iter_counter, cudaStream_t s);
+
+int prepare_kernels();
+
+// ---- single-CTA tail V-cycle (mac_tail.cu) --------------------------------------------------
+constexpr int kTailMaxLevels = 8;
+constexpr int kTailSmemMax = 200 * 1024;
+template <typename T>
+struct TailParams {
+    int nlev;                             // tail levels above the bottom
+    Dims lev[kTailMaxLevels];             // their dimensions (checkerboard-split in global memory)
+    const T* bx[kTailMaxLevels];
+    const T* by[kTailMaxLevels];
+    const T* bz[kTailMaxLevels];
+    const T* dg[kTailMaxLevels];
+    const T* idg[kTailMaxLevels];
+    Dims bottom;                          // bottom level (natural layout, FP64 operator)
+    const double *bbx, *bby, *bbz, *bdg, *bidg;
+    const T* f0;                          // right-hand side of the first tail level
+    T* e0;                                // its correction (output)
+    BcDesc bc;
+    int nu1, nu2, nub, singular, bottom_max_iter;
+    double bottom_eps;
+    int* iters;
+};
+template <typename T>
+size_t tail_smem_bytes(const Dims* lev, int nl, const Dims& bottom);
+template <typename T>
+void launch_tail(const TailParams<T>& P, size_t smem, cudaStream_t s);
+int prepare_tail_kernels();
 
 // ---- setup kernels (mac_setup.cu) -----------------------------------------------------------
 int setup_fine_coefficients(mac_ctx* c, const double* beta0, const double* beta0e);
@@ -217,5 +321,30 @@ void end_call_stats(mac_ctx* c, mac_stats* st);
 int alloc_device(mac_ctx* c, void** p, size_t bytes);
 
 inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
+
+// 3-D launch over an (nx, ny, nz) index space (x fastest): 128-thread blocks of (bx, 128/bx)
+// with bx the smallest power of two >= nx in [32, 128]; z = blockIdx.z.  Kernels recover their
+// indices without integer division.
+struct Grid3 {
+    dim3 grid, block;
+};
+inline Grid3 grid3(int nx, int ny, int nz) {
+    int bx = 32;
+    while (bx < nx && bx < 128) bx <<= 1;
+    const int by = 128 / bx;
+    Grid3 g;
+    g.block = dim3(bx, by, 1);
+    g.grid = dim3(ceil_div(nx, bx), ceil_div(ny, by), nz);
+    return g;
+}
+
+// Launch grid of the right-hand-side kernel (each block covers kRhsPlanes planes); its block
+// count sizes the partial-sum buffer.
+constexpr int kRhsPlanes = 16;
+inline Grid3 rhs_grid(const int* n) {
+    Grid3 g = grid3(n[0], n[1], 1);
+    g.grid.z = ceil_div(n[2], kRhsPlanes);
+    return g;
+}
 
 }  // namespace mac

@@ -5,6 +5,7 @@
 // (:196-211 smoothers, :221-259 bottom solvers, :325-375 V-cycle flow); the level layout and
 // the boundary trick are described in mac_internal.cuh.
 #include "mac_internal.cuh"
+#include "mac_bottom.cuh"
 
 namespace mac {
 
@@ -66,11 +67,12 @@ __device__ __forceinline__ unsigned long long block_max_u64(unsigned long long v
         unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
         v = w > v ? w : v;
     }
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    const int lane = tid & 31, wid = tid >> 5;
     if (lane == 0) sm[wid] = v;
     __syncthreads();
     if (wid == 0) {
-        v = (lane < (int)(blockDim.x >> 5)) ? sm[lane] : 0ull;
+        v = (lane < (int)((blockDim.x * blockDim.y) >> 5)) ? sm[lane] : 0ull;
         for (int o = 16; o > 0; o >>= 1) {
             unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
             v = w > v ? w : v;
@@ -86,12 +88,11 @@ k_gsrb(Dims d, int colour, T* __restrict__ us, const T* __restrict__ uo, const T
        const T* __restrict__ bxs, const T* __restrict__ bys, const T* __restrict__ bzs,
        const T* __restrict__ bxo, const T* __restrict__ byo, const T* __restrict__ bzo,
        const T* __restrict__ ids) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= d.half) return;
-    const int h = q % d.hn0;
-    const int row = q / d.hn0;
-    const int j = row % d.n1;
-    const int k = row / d.n1;
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (h >= d.hn0 || j >= d.n1) return;
+    const int q = (j + d.n1 * k) * d.hn0 + h;
     Nbr nb;
     split_nbrs(d, colour, h, j, k, nb);
     T acc = arms<T>(fs[q], q, nb, uo, bxs, bys, bzs, bxo, byo, bzo);
@@ -104,12 +105,10 @@ __global__ void __launch_bounds__(kBlock)
 k_resid_restrict(Dims F, Dims C, const T* __restrict__ u, const T* __restrict__ f,
                  const T* __restrict__ bx, const T* __restrict__ by, const T* __restrict__ bz,
                  const T* __restrict__ dg, T* __restrict__ fc) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= C.ncell) return;
-    const int I = q % C.n0;
-    const int row = q / C.n0;
-    const int J = row % C.n1;
-    const int K = row / C.n1;
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    const int K = blockIdx.z;
+    if (I >= C.n0 || J >= C.n1) return;
     T sum = T(0);
     for (int b = 0; b < F.rz; ++b) {
 #pragma unroll
@@ -138,68 +137,94 @@ k_resid_restrict(Dims F, Dims C, const T* __restrict__ u, const T* __restrict__ 
 }
 
 // ---- prolongation: u_fine += (bi/tri)linear interpolation of the coarse correction ----------
-__device__ __forceinline__ int ghost_fix(int q, int n, int blo, int bhi, float& sgn) {
-    if (q < 0) {
-        if (blo == MAC_BC_PER) return n - 1;
-        sgn = (blo == MAC_BC_DIR) ? -1.f : 1.f;
-        return 0;
+// Trilinear (bilinear in 2-D) cell-centred interpolation of the coarse correction, added to the
+// 2^dm children of each coarse cell: one thread per coarse cell reads its 3x3x3 coarse
+// neighbourhood (ghosts: periodic wrap, even/odd reflection for Neumann/Dirichlet, folded into
+// the weights as signs) and interpolates separably, z then y then x, with weights 3/4 and 1/4.
+template <typename T>
+__device__ __forceinline__ void coarse_nb(int q, int n, int blo, int bhi, int& qm, int& qp, T& wm,
+                                          T& wp) {
+    wm = T(0.25);
+    wp = T(0.25);
+    if (q > 0) {
+        qm = q - 1;
+    } else if (blo == MAC_BC_PER) {
+        qm = n - 1;
+    } else {
+        qm = 0;
+        if (blo == MAC_BC_DIR) wm = T(-0.25);
     }
-    if (q >= n) {
-        if (bhi == MAC_BC_PER) return 0;
-        sgn = (bhi == MAC_BC_DIR) ? -1.f : 1.f;
-        return n - 1;
+    if (q < n - 1) {
+        qp = q + 1;
+    } else if (bhi == MAC_BC_PER) {
+        qp = 0;
+    } else {
+        qp = n - 1;
+        if (bhi == MAC_BC_DIR) wp = T(-0.25);
     }
-    return q;
 }
 
-template <typename T>
+template <typename T, bool Z2>
 __global__ void __launch_bounds__(kBlock)
 k_prolong_add(Dims F, Dims C, BcDesc bc, const T* __restrict__ ec, T* __restrict__ u) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= F.half) return;
-    const int h = q % F.hn0;
-    const int row = q / F.hn0;
-    const int j = row % F.n1;
-    const int k = row / F.n1;
-    const int I = h;
-    const int J = j >> 1;
-    const int oj = (j & 1) ? 1 : -1;
-    int K, ok;
-    if (F.rz == 2) {
-        K = k >> 1;
-        ok = (k & 1) ? 1 : -1;
-    } else {
-        K = k;
-        ok = 0;
-    }
-    float sJ = 1.f, sK = 1.f, sIm = 1.f, sIp = 1.f;
-    const int J2 = ghost_fix(J + oj, C.n1, bc.lo[1], bc.hi[1], sJ);
-    const int K2 = ok ? ghost_fix(K + ok, C.n2, bc.lo[2], bc.hi[2], sK) : K;
-    const int Im = ghost_fix(I - 1, C.n0, bc.lo[0], bc.hi[0], sIm);
-    const int Ip = ghost_fix(I + 1, C.n0, bc.lo[0], bc.hi[0], sIp);
-    const T wz0 = ok ? T(0.75) : T(1), wz1 = ok ? T(0.25) : T(0);
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    const int K = blockIdx.z;
+    if (I >= C.n0 || J >= C.n1) return;
+    int xs[3], ys[3], zs[3];
+    T wxm, wxp, wym, wyp, wzm = T(0), wzp = T(0);
+    xs[1] = I;
+    ys[1] = J;
+    zs[1] = K;
+    coarse_nb<T>(I, C.n0, bc.lo[0], bc.hi[0], xs[0], xs[2], wxm, wxp);
+    coarse_nb<T>(J, C.n1, bc.lo[1], bc.hi[1], ys[0], ys[2], wym, wyp);
+    if (Z2) coarse_nb<T>(K, C.n2, bc.lo[2], bc.hi[2], zs[0], zs[2], wzm, wzp);
     auto cval = [&](int X, int Y, int Z) -> T {
-        int ci;
-        if (C.split)
-            ci = ((X + Y + Z) & 1) * C.half + (Y + C.n1 * Z) * C.hn0 + (X >> 1);
-        else
-            ci = X + C.n0 * (Y + C.n1 * Z);
-        return ec[ci];
+        if (C.split) return ec[((X + Y + Z) & 1) * C.half + (Y + C.n1 * Z) * C.hn0 + (X >> 1)];
+        return ec[X + C.n0 * (Y + C.n1 * Z)];
     };
-    auto col = [&](int X) -> T {
-        T a = T(0.75) * cval(X, J, K) + T(0.25) * (T)sJ * cval(X, J2, K);
-        T v = wz0 * a;
-        if (ok) {
-            T b = T(0.75) * cval(X, J, K2) + T(0.25) * (T)sJ * cval(X, J2, K2);
-            v += wz1 * (T)sK * b;
+    // Yv[x][yc][zc]: value interpolated in z and y, still at coarse x-column x
+    T Yv[3][2][2];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int X = xs[a];
+        T Zv[3][2];   // [y][zc]
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            const int Y = ys[b];
+            const T c0 = cval(X, Y, K);
+            if (Z2) {
+                const T t = T(0.75) * c0;
+                Zv[b][0] = fmaT(wzm, cval(X, Y, zs[0]), t);
+                Zv[b][1] = fmaT(wzp, cval(X, Y, zs[2]), t);
+            } else {
+                Zv[b][0] = c0;
+                Zv[b][1] = c0;
+            }
         }
-        return v;
-    };
-    const T vI = col(I), vm = col(Im), vp = col(Ip);
-    const int cA = (j + k) & 1;   // colour of fine cell 2h
-    const int idx = row * F.hn0 + h;
-    u[cA * F.half + idx] += T(0.75) * vI + T(0.25) * (T)sIm * vm;
-    u[(cA ^ 1) * F.half + idx] += T(0.75) * vI + T(0.25) * (T)sIp * vp;
+#pragma unroll
+        for (int zc = 0; zc < 2; ++zc) {
+            const T t = T(0.75) * Zv[1][zc];
+            Yv[a][0][zc] = fmaT(wym, Zv[0][zc], t);
+            Yv[a][1][zc] = fmaT(wyp, Zv[2][zc], t);
+        }
+    }
+    const int hn0 = F.hn0, n1 = F.n1;
+#pragma unroll
+    for (int zc = 0; zc < (Z2 ? 2 : 1); ++zc) {
+#pragma unroll
+        for (int yc = 0; yc < 2; ++yc) {
+            const T t = T(0.75) * Yv[1][yc][zc];
+            const T v0 = fmaT(wxm, Yv[0][yc][zc], t);
+            const T v1 = fmaT(wxp, Yv[2][yc][zc], t);
+            const int j = 2 * J + yc;
+            const int k = Z2 ? 2 * K + zc : K;
+            const int base = (j + n1 * k) * hn0 + I;
+            const int c0 = (yc + zc) & 1;   // colour of child 2I (2I+2J+2K is even)
+            u[c0 * F.half + base] += v0;
+            u[(c0 ^ 1) * F.half + base] += v1;
+        }
+    }
 }
 
 // ---- residual max-norm (FP64 accumulation of |r|) ---------------------------------------------
@@ -208,13 +233,12 @@ __global__ void __launch_bounds__(kBlock)
 k_resid_norm(Dims F, const T* __restrict__ u, const T* __restrict__ f, const T* __restrict__ bx,
              const T* __restrict__ by, const T* __restrict__ bz, const T* __restrict__ dg,
              unsigned long long* __restrict__ maxbits) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
     unsigned long long m = 0ull;
-    if (q < F.half) {
-        const int h = q % F.hn0;
-        const int row = q / F.hn0;
-        const int j = row % F.n1;
-        const int k = row / F.n1;
+    if (h < F.hn0 && j < F.n1) {
+        const int q = (j + F.n1 * k) * F.hn0 + h;
 #pragma unroll
         for (int colour = 0; colour < (RED_ONLY ? 1 : 2); ++colour) {
             const int off = colour * F.half, oth = (colour ^ 1) * F.half;
@@ -228,7 +252,7 @@ k_resid_norm(Dims F, const T* __restrict__ u, const T* __restrict__ f, const T* 
         }
     }
     m = block_max_u64(m);
-    if (threadIdx.x == 0 && m) atomicMax(maxbits, m);
+    if (threadIdx.x == 0 && threadIdx.y == 0 && m) atomicMax(maxbits, m);
 }
 
 // FP64 residual of the whole fine level, stored as FP32 (the refinement right-hand side).
@@ -237,13 +261,12 @@ k_resid64_to32(Dims F, const double* __restrict__ u, const double* __restrict__ 
                const double* __restrict__ bx, const double* __restrict__ by,
                const double* __restrict__ bz, const double* __restrict__ dg,
                float* __restrict__ r32, unsigned long long* __restrict__ maxbits) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
     unsigned long long m = 0ull;
-    if (q < F.half) {
-        const int h = q % F.hn0;
-        const int row = q / F.hn0;
-        const int j = row % F.n1;
-        const int k = row / F.n1;
+    if (h < F.hn0 && j < F.n1) {
+        const int q = (j + F.n1 * k) * F.hn0 + h;
 #pragma unroll
         for (int colour = 0; colour < 2; ++colour) {
             const int off = colour * F.half, oth = (colour ^ 1) * F.half;
@@ -258,7 +281,7 @@ k_resid64_to32(Dims F, const double* __restrict__ u, const double* __restrict__ 
         }
     }
     m = block_max_u64(m);
-    if (threadIdx.x == 0 && m) atomicMax(maxbits, m);
+    if (threadIdx.x == 0 && threadIdx.y == 0 && m) atomicMax(maxbits, m);
 }
 
 __global__ void __launch_bounds__(kBlock)
@@ -267,175 +290,52 @@ k_accumulate(int n, double* __restrict__ u, const float* __restrict__ e) {
     if (q < n) u[q] += (double)e[q];
 }
 
-// ---- single-CTA FP64 bottom solver (natural layout) -----------------------------------------
+// ---- single-CTA FP64 bottom solver (natural layout): device code in mac_bottom.cuh -------------
 constexpr int kBottomThreads = 1024;
+constexpr int kBottomSmemCells = 1024;   // 14 doubles per cell: 114,688 B of shared memory
 
-struct BotView {
-    int n0, n1, n2, N;
-    const double *bx, *by, *bz, *dg, *idg;
-};
-
-__device__ __forceinline__ double bot_arms(const BotView& v, const double* __restrict__ x, int c) {
-    const int i = c % v.n0;
-    const int row = c / v.n0;
-    const int j = row % v.n1;
-    const int k = row / v.n1;
-    const int im = i == 0 ? v.n0 - 1 : i - 1, ip = i == v.n0 - 1 ? 0 : i + 1;
-    const int jm = j == 0 ? v.n1 - 1 : j - 1, jp = j == v.n1 - 1 ? 0 : j + 1;
-    const int km = k == 0 ? v.n2 - 1 : k - 1, kp = k == v.n2 - 1 ? 0 : k + 1;
-    const int cxp = ip + v.n0 * (j + v.n1 * k), cxm = im + v.n0 * (j + v.n1 * k);
-    const int cyp = i + v.n0 * (jp + v.n1 * k), cym = i + v.n0 * (jm + v.n1 * k);
-    const int czp = i + v.n0 * (j + v.n1 * kp), czm = i + v.n0 * (j + v.n1 * km);
-    double s = v.bx[c] * x[cxm];
-    s = fma(v.bx[cxp], x[cxp], s);
-    s = fma(v.by[c], x[cym], s);
-    s = fma(v.by[cyp], x[cyp], s);
-    s = fma(v.bz[c], x[czm], s);
-    s = fma(v.bz[czp], x[czp], s);
-    return s;
-}
-
-__device__ double bot_sum(double v, double* sm) {
-    // deterministic tree reduction over the CTA
-    const int t = threadIdx.x;
-    sm[t] = v;
-    __syncthreads();
-    for (int o = kBottomThreads / 2; o > 0; o >>= 1) {
-        if (t < o) sm[t] += sm[t + o];
-        __syncthreads();
-    }
-    const double r = sm[0];
-    __syncthreads();
-    return r;
-}
-
-__device__ double bot_max(double v, double* sm) {
-    const int t = threadIdx.x;
-    sm[t] = v;
-    __syncthreads();
-    for (int o = kBottomThreads / 2; o > 0; o >>= 1) {
-        if (t < o) sm[t] = fmax(sm[t], sm[t + o]);
-        __syncthreads();
-    }
-    const double r = sm[0];
-    __syncthreads();
-    return r;
-}
-
-__device__ void bot_gsrb(const BotView& v, double* x, const double* f) {
-    for (int colour = 0; colour < 2; ++colour) {
-        for (int c = threadIdx.x; c < v.N; c += kBottomThreads) {
-            const int i = c % v.n0, row = c / v.n0, j = row % v.n1, k = row / v.n1;
-            if (((i + j + k) & 1) != colour) continue;
-            x[c] = (f[c] + bot_arms(v, x, c)) * v.idg[c];
-        }
-        __syncthreads();
-    }
-}
-
-__device__ void bot_apply(const BotView& v, const double* x, double* y) {
-    for (int c = threadIdx.x; c < v.N; c += kBottomThreads) y[c] = v.dg[c] * x[c] - bot_arms(v, x, c);
-    __syncthreads();
-}
-
-template <typename Tio>
+// SMEM: the five operator arrays and the nine work vectors live in dynamic shared memory
+// (levels of up to kBottomSmemCells cells, 128 threads), else in global scratch (1024 threads).
+template <typename Tio, bool SMEM>
 __global__ void __launch_bounds__(kBottomThreads)
-k_bottom(BotView v, Tio* __restrict__ xio, const Tio* __restrict__ fio, double* __restrict__ scr,
+k_bottom(BotView vin, Tio* __restrict__ xio, const Tio* __restrict__ fio, double* __restrict__ gscr,
          int singular, int nub, double eps, int max_iter, int* __restrict__ iters) {
-    __shared__ double sm[kBottomThreads];
-    const int N = v.N;
+    __shared__ double sm[33];
+    extern __shared__ double dsm[];
+    const int N = vin.N;
+    BotView v = vin;
+    double* scr = gscr;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    if (SMEM) {
+        double* ops = dsm;
+        for (int c = tid; c < N; c += nt) {
+            ops[c] = vin.bx[c];
+            ops[N + c] = vin.by[c];
+            ops[2 * N + c] = vin.bz[c];
+            ops[3 * N + c] = vin.dg[c];
+            ops[4 * N + c] = vin.idg[c];
+        }
+        v.bx = ops;
+        v.by = ops + N;
+        v.bz = ops + 2 * N;
+        v.dg = ops + 3 * N;
+        v.idg = ops + 4 * N;
+        scr = dsm + 5 * N;
+    }
     double* x = scr;
     double* f = scr + N;
-    double* r = scr + 2 * N;
-    double* rh = scr + 3 * N;
-    double* p = scr + 4 * N;
-    double* vv = scr + 5 * N;
-    double* s = scr + 6 * N;
-    double* t = scr + 7 * N;
-    double* y = scr + 8 * N;
-    const int tid = threadIdx.x;
-    double loc = 0.0;
-    for (int c = tid; c < N; c += kBottomThreads) {
+    for (int c = tid; c < N; c += nt) {
         x[c] = (double)xio[c];
         f[c] = (double)fio[c];
-        loc += f[c];
     }
-    const double mean = bot_sum(loc, sm) / N;
-    if (singular)
-        for (int c = tid; c < N; c += kBottomThreads) f[c] -= mean;
     __syncthreads();
-    for (int it = 0; it < nub; ++it) bot_gsrb(v, x, f);
-
-    // r = f - A x
-    bot_apply(v, x, t);
-    loc = 0.0;
-    for (int c = tid; c < N; c += kBottomThreads) {
-        r[c] = f[c] - t[c];
-        rh[c] = r[c];
-        p[c] = 0.0;
-        vv[c] = 0.0;
-        loc = fmax(loc, fabs(r[c]));
-    }
-    const double r0 = bot_max(loc, sm);
-    int count = 0;
-    if (r0 > 0.0) {
-        const double tol = eps * r0;
-        double rho_old = 1.0, alpha = 1.0, omega = 1.0;
-        for (int it = 0; it < max_iter; ++it) {
-            ++count;
-            loc = 0.0;
-            for (int c = tid; c < N; c += kBottomThreads) loc += rh[c] * r[c];
-            const double rho = bot_sum(loc, sm);
-            if (rho == 0.0) break;
-            const double beta = (rho / rho_old) * (alpha / omega);
-            for (int c = tid; c < N; c += kBottomThreads) {
-                p[c] = r[c] + beta * (p[c] - omega * vv[c]);
-                y[c] = p[c] * v.idg[c];
-            }
-            __syncthreads();
-            bot_apply(v, y, vv);
-            loc = 0.0;
-            for (int c = tid; c < N; c += kBottomThreads) loc += rh[c] * vv[c];
-            const double rv = bot_sum(loc, sm);
-            if (rv == 0.0) break;
-            alpha = rho / rv;
-            loc = 0.0;
-            for (int c = tid; c < N; c += kBottomThreads) {
-                s[c] = r[c] - alpha * vv[c];
-                loc = fmax(loc, fabs(s[c]));
-            }
-            const double sn = bot_max(loc, sm);
-            if (sn <= tol) {
-                for (int c = tid; c < N; c += kBottomThreads) x[c] += alpha * y[c];
-                __syncthreads();
-                break;
-            }
-            // y now holds p/diag; keep it for the x update, use r as temporary for s/diag
-            for (int c = tid; c < N; c += kBottomThreads) x[c] += alpha * y[c];
-            for (int c = tid; c < N; c += kBottomThreads) y[c] = s[c] * v.idg[c];
-            __syncthreads();
-            bot_apply(v, y, t);
-            double l1 = 0.0, l2 = 0.0;
-            for (int c = tid; c < N; c += kBottomThreads) {
-                l1 += t[c] * s[c];
-                l2 += t[c] * t[c];
-            }
-            const double ts = bot_sum(l1, sm);
-            const double tt = bot_sum(l2, sm);
-            omega = tt > 0.0 ? ts / tt : 0.0;
-            loc = 0.0;
-            for (int c = tid; c < N; c += kBottomThreads) {
-                x[c] += omega * y[c];
-                r[c] = s[c] - omega * t[c];
-                loc = fmax(loc, fabs(r[c]));
-            }
-            const double rn = bot_max(loc, sm);
-            if (rn <= tol || omega == 0.0) break;
-            rho_old = rho;
-        }
-    }
-    for (int it = 0; it < nub; ++it) bot_gsrb(v, x, f);
-    for (int c = tid; c < N; c += kBottomThreads) xio[c] = (Tio)x[c];
+    int count;
+    if (SMEM)
+        count = bottom_body<Sync128<false>>(v, x, f, scr + 2 * N, sm, singular, nub, eps, max_iter);
+    else
+        count = bottom_body<CtaSync>(v, x, f, scr + 2 * N, sm, singular, nub, eps, max_iter);
+    __syncthreads();
+    for (int c = tid; c < N; c += nt) xio[c] = (Tio)x[c];
     if (tid == 0 && iters) atomicAdd(iters, count);
 }
 
@@ -445,7 +345,8 @@ k_bottom(BotView v, Tio* __restrict__ xio, const Tio* __restrict__ fio, double* 
 template <typename T>
 void launch_gsrb(const Dims& d, int colour, LevelArrays<T>& a, cudaStream_t s) {
     const int own = colour * d.half, oth = (colour ^ 1) * d.half;
-    k_gsrb<T><<<ceil_div(d.half, kBlock), kBlock, 0, s>>>(
+    const Grid3 g = grid3(d.hn0, d.n1, d.n2);
+    k_gsrb<T><<<g.grid, g.block, 0, s>>>(
         d, colour, a.phi + own, a.phi + oth, a.f + own, a.bx + own, a.by + own, a.bz + own,
         a.bx + oth, a.by + oth, a.bz + oth, a.invdiag + own);
 }
@@ -453,36 +354,41 @@ void launch_gsrb(const Dims& d, int colour, LevelArrays<T>& a, cudaStream_t s) {
 template <typename T>
 void launch_resid_restrict(const Dims& fine, const Dims& coarse, const LevelArrays<T>& a, T* fc,
                            bool red_only, cudaStream_t s) {
-    const int nb = ceil_div(coarse.ncell, kBlock);
+    const Grid3 g = grid3(coarse.n0, coarse.n1, coarse.n2);
     if (red_only)
-        k_resid_restrict<T, true><<<nb, kBlock, 0, s>>>(fine, coarse, a.phi, a.f, a.bx, a.by, a.bz,
-                                                        a.diag, fc);
+        k_resid_restrict<T, true><<<g.grid, g.block, 0, s>>>(fine, coarse, a.phi, a.f, a.bx, a.by,
+                                                             a.bz, a.diag, fc);
     else
-        k_resid_restrict<T, false><<<nb, kBlock, 0, s>>>(fine, coarse, a.phi, a.f, a.bx, a.by,
-                                                         a.bz, a.diag, fc);
+        k_resid_restrict<T, false><<<g.grid, g.block, 0, s>>>(fine, coarse, a.phi, a.f, a.bx, a.by,
+                                                              a.bz, a.diag, fc);
 }
 
 template <typename T>
 void launch_prolong_add(const Dims& fine, const Dims& coarse, const BcDesc& bc, const T* ec,
                         T* phi_fine, cudaStream_t s) {
-    k_prolong_add<T><<<ceil_div(fine.half, kBlock), kBlock, 0, s>>>(fine, coarse, bc, ec, phi_fine);
+    const Grid3 g = grid3(coarse.n0, coarse.n1, coarse.n2);
+    if (fine.rz == 2)
+        k_prolong_add<T, true><<<g.grid, g.block, 0, s>>>(fine, coarse, bc, ec, phi_fine);
+    else
+        k_prolong_add<T, false><<<g.grid, g.block, 0, s>>>(fine, coarse, bc, ec, phi_fine);
 }
 
 template <typename T>
 void launch_resid_norm(const Dims& d, const LevelArrays<T>& a, bool red_only,
                        unsigned long long* maxbits, cudaStream_t s) {
-    const int nb = ceil_div(d.half, kBlock);
+    const Grid3 g = grid3(d.hn0, d.n1, d.n2);
     if (red_only)
-        k_resid_norm<T, true><<<nb, kBlock, 0, s>>>(d, a.phi, a.f, a.bx, a.by, a.bz, a.diag, maxbits);
+        k_resid_norm<T, true><<<g.grid, g.block, 0, s>>>(d, a.phi, a.f, a.bx, a.by, a.bz, a.diag,
+                                                         maxbits);
     else
-        k_resid_norm<T, false><<<nb, kBlock, 0, s>>>(d, a.phi, a.f, a.bx, a.by, a.bz, a.diag,
-                                                     maxbits);
+        k_resid_norm<T, false><<<g.grid, g.block, 0, s>>>(d, a.phi, a.f, a.bx, a.by, a.bz, a.diag,
+                                                          maxbits);
 }
 
 void launch_resid64_to32(const Dims& d, const LevelArrays<double>& a, float* r32,
                          unsigned long long* maxbits, cudaStream_t s) {
-    k_resid64_to32<<<ceil_div(d.half, kBlock), kBlock, 0, s>>>(d, a.phi, a.f, a.bx, a.by, a.bz,
-                                                               a.diag, r32, maxbits);
+    const Grid3 g = grid3(d.hn0, d.n1, d.n2);
+    k_resid64_to32<<<g.grid, g.block, 0, s>>>(d, a.phi, a.f, a.bx, a.by, a.bz, a.diag, r32, maxbits);
 }
 
 void launch_accumulate(const Dims& d, double* phi, const float* e, cudaStream_t s) {
@@ -503,8 +409,27 @@ void launch_bottom(const Dims& d, const LevelArrays<double>& a64, Tio* x, const 
     v.bz = a64.bz;
     v.dg = a64.diag;
     v.idg = a64.invdiag;
-    k_bottom<Tio><<<1, kBottomThreads, 0, s>>>(v, x, f, scratch, singular ? 1 : 0, nub, eps,
-                                               max_iter, iter_counter);
+    // small levels: 128 threads, operator and vectors in shared memory; large: one 1024-thread
+    // CTA on global scratch
+    const size_t smem = (size_t)14 * d.ncell * sizeof(double);
+    if (d.ncell <= kBottomSmemCells)
+        k_bottom<Tio, true><<<1, 128, smem, s>>>(v, x, f, scratch, singular ? 1 : 0, nub, eps,
+                                                 max_iter, iter_counter);
+    else
+        k_bottom<Tio, false><<<1, kBottomThreads, 0, s>>>(v, x, f, scratch, singular ? 1 : 0, nub,
+                                                          eps, max_iter, iter_counter);
+}
+
+// Opt the shared-memory bottom solver into more than 48 KB of dynamic shared memory (called once
+// per context, outside any stream capture).
+int prepare_kernels() {
+    const int bytes = 14 * kBottomSmemCells * (int)sizeof(double);
+    if (cudaFuncSetAttribute(k_bottom<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess ||
+        cudaFuncSetAttribute(k_bottom<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return MAC_ERR_CUDA;
+    }
+    return MAC_OK;
 }
 
 template void launch_gsrb<double>(const Dims&, int, LevelArrays<double>&, cudaStream_t);

@@ -31,72 +31,117 @@ struct FineParams {
     double ih2[3];
 };
 
-__device__ __forceinline__ double beta0_pow(double b, int p) { return p == 2 ? b * b : b; }
+
+// Per-layer factor tables (see kTab* in mac_internal.cuh), one thread per vertical index r.
+// beta0 on the low face of a cell in layer r: beta0[r] for the horizontal directions,
+// beta0_edge[r] for the vertical one (mult_edge_by_1d_coeff, Source/macproject.f90:577-609).
+__global__ void k_beta0_tables(int nr, int va, int p, const double* __restrict__ b0,
+                               const double* __restrict__ b0e, double3 h, double* __restrict__ tab,
+                               float* __restrict__ fac32, int vper, int vdlo, int vdhi) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r > nr) return;
+    const double hh[3] = {h.x, h.y, h.z};
+    const int st = nr + 1;
+    const double bc = p ? b0[r < nr ? r : nr - 1] : 1.0;
+    const double be = p ? b0e[r] : 1.0;
+    for (int d = 0; d < 3; ++d) {
+        const double b = d == va ? be : bc;
+        const double bp = p == 2 ? b * b : (p == 1 ? b : 1.0);
+        tab[(kTabFac0 + d) * st + r] = bp * 2.0 / (hh[d] * hh[d]);
+        tab[(kTabG0 + d) * st + r] = b / hh[d];
+        tab[(kTabK0 + d) * st + r] = hh[d] / b;
+    }
+    // FP32 tables of the on-the-fly finest-level kernels (OtfParams)
+    const double hv = hh[va];
+    const double bcp = p == 2 ? bc * bc : (p == 1 ? bc : 1.0);
+    fac32[0 * st + r] = (float)(bcp * 2.0 / (hh[0] * hh[0]));
+    fac32[1 * st + r] = (float)(bcp * 2.0 / (hh[1] * hh[1]));
+    if (r < nr) {
+        const double bl = p ? b0e[r] : 1.0, bh = p ? b0e[r + 1] : 1.0;
+        const double fl = (p == 2 ? bl * bl : (p == 1 ? bl : 1.0)) * 2.0 / (hv * hv);
+        const double fh = (p == 2 ? bh * bh : (p == 1 ? bh : 1.0)) * 2.0 / (hv * hv);
+        const bool wl = r == 0 && !vper, wh = r == nr - 1 && !vper;
+        fac32[2 * st + r] = wl ? 0.f : (float)fl;
+        fac32[3 * st + r] = wh ? 0.f : (float)fh;
+        // Dirichlet wall: 2 beta'_wall = 2 fac/(2 rho) = fac / rho, here the fac part
+        fac32[4 * st + r] = (float)((wl && vdlo ? fl : 0.0) + (wh && vdhi ? fh : 0.0));
+    } else {
+        fac32[2 * st + r] = 0.f;
+        fac32[3 * st + r] = 0.f;
+        fac32[4 * st + r] = 0.f;
+    }
+}
 
 // beta' on the low faces of every fine cell, Dirichlet wall planes, density check.
+// beta'_d = fac_d[layer] / (rho_a + rho_b)  (= beta0^p 2/(rho_a + rho_b) / h_d^2)
+__device__ __forceinline__ void fine_face(const FineParams& P, int dd, int cd, int nd, int q,
+                                          int stride, double rc, const double* __restrict__ rho,
+                                          double fac, double fhi, double* out, int li,
+                                          double* wl, double* wh, int plane) {
+    double v = 0.0;
+    const bool per = P.bc_lo[dd] == MAC_BC_PER;
+    if (cd > 0)
+        v = fac * recip_nr(rc + rho[q - stride]);
+    else if (per)
+        v = fac * recip_nr(rc + rho[q + (nd - 1) * stride]);
+    out[li] = v;
+    if (cd == 0 && P.bc_lo[dd] == MAC_BC_DIR) wl[plane] = fac * recip_nr(rc + rc);
+    if (cd == nd - 1 && P.bc_hi[dd] == MAC_BC_DIR) wh[plane] = fhi * recip_nr(rc + rc);
+}
+
 __global__ void __launch_bounds__(kBlock)
-k_fine_coef(FineParams P, Dims d, const double* __restrict__ rho, const double* __restrict__ b0,
-            const double* __restrict__ b0e, double* __restrict__ bx, double* __restrict__ by,
-            double* __restrict__ bz, double* __restrict__ wlo0, double* __restrict__ whi0,
-            double* __restrict__ wlo1, double* __restrict__ whi1, double* __restrict__ wlo2,
-            double* __restrict__ whi2, int* __restrict__ err) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= d.ncell) return;
-    const int i = q % P.n[0];
-    const int row = q / P.n[0];
-    const int j = row % P.n[1];
-    const int k = row / P.n[1];
-    const int c[3] = {i, j, k};
+k_fine_coef(FineParams P, Dims d, const double* __restrict__ rho, const double* __restrict__ tab,
+            double* __restrict__ bx, double* __restrict__ by, double* __restrict__ bz,
+            double* __restrict__ wlo0, double* __restrict__ whi0, double* __restrict__ wlo1,
+            double* __restrict__ whi1, double* __restrict__ wlo2, double* __restrict__ whi2,
+            int* __restrict__ err, float* __restrict__ rho32) {
+    const int n0 = P.n[0], n1 = P.n[1], n2 = P.n[2];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= n0 || j >= n1) return;
+    const int q = i + n0 * (j + n1 * k);
     const double rc = rho[q];
-    if (!(rc > 0.0) || !isfinite(rc)) atomicOr(err, 1);
+    if (!positive_finite(rc)) atomicOr(err, 1);
     const int li = lidx(d, i, j, k);
-    double* out[3] = {bx, by, bz};
-    double* wl[3] = {wlo0, wlo1, wlo2};
-    double* wh[3] = {whi0, whi1, whi2};
-    const int r = c[P.va];
-#pragma unroll
-    for (int dd = 0; dd < 3; ++dd) {
-        if (!P.active[dd]) {
-            out[dd][li] = 0.0;
-            continue;
-        }
-        const double bcell = P.p ? beta0_pow(b0[r], P.p) : 1.0;
-        const double blo = P.p ? (dd == P.va ? beta0_pow(b0e[r], P.p) : bcell) : 1.0;
-        double v = 0.0;
-        if (c[dd] > 0 || P.bc_lo[dd] == MAC_BC_PER) {
-            int nb[3] = {i, j, k};
-            nb[dd] = c[dd] > 0 ? c[dd] - 1 : P.n[dd] - 1;
-            const double rn = rho[nb[0] + P.n[0] * (nb[1] + P.n[1] * nb[2])];
-            v = blo * (2.0 / (rc + rn)) * P.ih2[dd];
-        }
-        out[dd][li] = v;
-        const int plane = dd == 0 ? (j + P.n[1] * k) : dd == 1 ? (i + P.n[0] * k) : (i + P.n[0] * j);
-        if (c[dd] == 0 && P.bc_lo[dd] == MAC_BC_DIR)
-            wl[dd][plane] = blo * (2.0 / (rc + rc)) * P.ih2[dd];
-        if (c[dd] == P.n[dd] - 1 && P.bc_hi[dd] == MAC_BC_DIR) {
-            const double bhi = P.p ? (dd == P.va ? beta0_pow(b0e[r + 1], P.p) : bcell) : 1.0;
-            wh[dd][plane] = bhi * (2.0 / (rc + rc)) * P.ih2[dd];
-        }
-    }
+    if (rho32) rho32[li] = (float)rc;
+    const bool v2 = P.va == 2;
+    const int r = v2 ? k : j;                       // vertical index (3-D: z, 2-D: y)
+    const int st = (v2 ? n2 : n1) + 1;
+    const double* f0 = tab + kTabFac0 * st;
+    const double* f1 = tab + (kTabFac0 + 1) * st;
+    const double* f2 = tab + (kTabFac0 + 2) * st;
+    // x: horizontal
+    fine_face(P, 0, i, n0, q, 1, rc, rho, f0[r], f0[r], bx, li, wlo0, whi0, j + n1 * k);
+    // y: horizontal in 3-D, vertical in 2-D
+    fine_face(P, 1, j, n1, q, n0, rc, rho, f1[r], v2 ? f1[r] : f1[r + 1], by, li, wlo1, whi1,
+              i + n0 * k);
+    // z: vertical in 3-D, absent in 2-D
+    if (P.active[2])
+        fine_face(P, 2, k, n2, q, n0 * n1, rc, rho, f2[r], f2[r + 1], bz, li, wlo2, whi2,
+                  i + n0 * j);
+    else
+        bz[li] = 0.0;
 }
 
 struct DiagParams {
     int bc_lo[3], bc_hi[3];
+    int any_dir;
     const double* wl[3];
     const double* wh[3];
 };
 
-// diag = alpha + sum of the six face coefficients (+ 2 beta'_wall on Dirichlet faces).
+// diag = alpha + sum of the six face coefficients (+ 2 beta'_wall on Dirichlet faces); optional
+// 1/diag in FP64 and FP32 copies of diag and 1/diag (mixed precision).
 __global__ void __launch_bounds__(kBlock)
 k_build_diag(Dims d, DiagParams P, const double* __restrict__ bx, const double* __restrict__ by,
              const double* __restrict__ bz, const double* __restrict__ alpha,
-             double* __restrict__ dg, double* __restrict__ idg) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= d.ncell) return;
-    const int i = q % d.n0;
-    const int row = q / d.n0;
-    const int j = row % d.n1;
-    const int k = row / d.n1;
+             double* __restrict__ dg, double* __restrict__ idg, float* __restrict__ dg32,
+             float* __restrict__ idg32) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= d.n0 || j >= d.n1) return;
     const int me = lidx(d, i, j, k);
     const int ip = i == d.n0 - 1 ? 0 : i + 1;
     const int jp = j == d.n1 - 1 ? 0 : j + 1;
@@ -105,16 +150,21 @@ k_build_diag(Dims d, DiagParams P, const double* __restrict__ bx, const double* 
     s += bx[me] + bx[lidx(d, ip, j, k)];
     s += by[me] + by[lidx(d, i, jp, k)];
     s += bz[me] + bz[lidx(d, i, j, kp)];
-    const int c[3] = {i, j, k};
-    const int n[3] = {d.n0, d.n1, d.n2};
-#pragma unroll
-    for (int dd = 0; dd < 3; ++dd) {
-        const int plane = dd == 0 ? (j + d.n1 * k) : dd == 1 ? (i + d.n0 * k) : (i + d.n0 * j);
-        if (c[dd] == 0 && P.bc_lo[dd] == MAC_BC_DIR && P.wl[dd]) s += 2.0 * P.wl[dd][plane];
-        if (c[dd] == n[dd] - 1 && P.bc_hi[dd] == MAC_BC_DIR && P.wh[dd]) s += 2.0 * P.wh[dd][plane];
+    if (P.any_dir) {
+        if (i == 0 && P.bc_lo[0] == MAC_BC_DIR) s += 2.0 * P.wl[0][j + d.n1 * k];
+        if (i == d.n0 - 1 && P.bc_hi[0] == MAC_BC_DIR) s += 2.0 * P.wh[0][j + d.n1 * k];
+        if (j == 0 && P.bc_lo[1] == MAC_BC_DIR) s += 2.0 * P.wl[1][i + d.n0 * k];
+        if (j == d.n1 - 1 && P.bc_hi[1] == MAC_BC_DIR) s += 2.0 * P.wh[1][i + d.n0 * k];
+        if (k == 0 && P.bc_lo[2] == MAC_BC_DIR) s += 2.0 * P.wl[2][i + d.n0 * j];
+        if (k == d.n2 - 1 && P.bc_hi[2] == MAC_BC_DIR) s += 2.0 * P.wh[2][i + d.n0 * j];
     }
     dg[me] = s;
-    idg[me] = 1.0 / s;
+    if (idg) idg[me] = recip_nr(s);
+    if (dg32) {
+        const float sf = (float)s;
+        dg32[me] = sf;
+        idg32[me] = 1.0f / sf;
+    }
 }
 
 // Coarse low-face coefficients: mean of the fine low faces tiling the coarse face, / 4 for h^2.
@@ -122,13 +172,12 @@ __global__ void __launch_bounds__(kBlock)
 k_coarsen_coef(Dims F, Dims C, const double* __restrict__ fbx, const double* __restrict__ fby,
                const double* __restrict__ fbz, const double* __restrict__ falpha,
                double* __restrict__ cbx, double* __restrict__ cby, double* __restrict__ cbz,
-               double* __restrict__ calpha) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= C.ncell) return;
-    const int I = q % C.n0;
-    const int row = q / C.n0;
-    const int J = row % C.n1;
-    const int K = row / C.n1;
+               double* __restrict__ calpha, float* __restrict__ cbx32, float* __restrict__ cby32,
+               float* __restrict__ cbz32) {
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    const int K = blockIdx.z;
+    if (I >= C.n0 || J >= C.n1) return;
     const int rz = F.rz;
     double sx = 0.0, sy = 0.0, sz = 0.0;
     for (int b = 0; b < rz; ++b)
@@ -140,15 +189,22 @@ k_coarsen_coef(Dims F, Dims C, const double* __restrict__ fbx, const double* __r
         for (int b = 0; b < 2; ++b)
             for (int a = 0; a < 2; ++a) sz += fbz[lidx(F, 2 * I + a, 2 * J + b, 2 * K)];
     const int me = lidx(C, I, J, K);
-    cbx[me] = 0.25 * sx / (2 * rz);
-    cby[me] = 0.25 * sy / (2 * rz);
-    cbz[me] = rz == 2 ? 0.25 * sz / 4 : 0.0;
+    const double w = rz == 2 ? 0.0625 : 0.125;   // 1/4 (h^2) times the mean over 2*rz faces
+    const double vx = w * sx, vy = w * sy, vz = rz == 2 ? 0.0625 * sz : 0.0;
+    cbx[me] = vx;
+    cby[me] = vy;
+    cbz[me] = vz;
+    if (cbx32) {
+        cbx32[me] = (float)vx;
+        cby32[me] = (float)vy;
+        cbz32[me] = (float)vz;
+    }
     if (falpha) {
         double sa = 0.0;
         for (int b = 0; b < rz; ++b)
             for (int a1 = 0; a1 < 2; ++a1)
                 for (int a0 = 0; a0 < 2; ++a0) sa += falpha[lidx(F, 2 * I + a0, 2 * J + a1, rz * K + b)];
-        calpha[me] = sa / (4 * rz);
+        calpha[me] = sa * (rz == 2 ? 0.125 : 0.25);
     }
 }
 
@@ -161,7 +217,7 @@ __global__ void k_coarsen_wall(int np0, int np1, int r0, int r1, int fp0,
     double s = 0.0;
     for (int b = 0; b < r1; ++b)
         for (int a = 0; a < r0; ++a) s += fw[(r0 * P0 + a) + fp0 * (r1 * P1 + b)];
-    cw[q] = 0.25 * s / (r0 * r1);
+    cw[q] = 0.25 * s * (r0 * r1 == 4 ? 0.25 : (r0 * r1 == 2 ? 0.5 : 1.0));
 }
 
 __global__ void k_to_f32(int n, const double* __restrict__ a, float* __restrict__ b) {
@@ -172,105 +228,134 @@ __global__ void k_to_f32(int n, const double* __restrict__ a, float* __restrict_
 struct RhsParams {
     int n[3];
     int dm, va, have_beta0;
-    double dx[3];
+    double idx[3];   // 1/dx
 };
 
-// f = -(div(beta0 U) - macrhs) in the level-0 layout, with per-block (sum, max, min).
+// f = -(div(beta0 U) - macrhs) (FROM_RH: f = rh, already a natural cell array) in the level-0
+// layout, with per-block partials: FP64 sum (fixed order) and max/min of f as ordered bit
+// patterns (integer pipe).  U is scaled by beta0 face by face as mult_edge_by_1d_coeff does (x/y
+// faces by beta0(k), the vertical faces by beta0_edge(k)) before the differences.  Each block
+// covers a (bx x by) tile of rows over kRhsPlanes planes so the partials stay few.
+template <int DM, bool FROM_RH>
 __global__ void __launch_bounds__(kBlock)
 k_rhs(RhsParams P, Dims d, const double* __restrict__ ux, const double* __restrict__ uy,
       const double* __restrict__ uz, const double* __restrict__ macrhs,
-      const double* __restrict__ b0, const double* __restrict__ b0e, double* __restrict__ f,
-      double* __restrict__ partial) {
-    __shared__ double ssum[kBlock], smax[kBlock], smin[kBlock];
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    double v = 0.0, vmax = -INFINITY, vmin = INFINITY;
-    if (q < d.ncell) {
-        const int i = q % P.n[0];
-        const int row = q / P.n[0];
-        const int j = row % P.n[1];
-        const int k = row / P.n[1];
-        const int c[3] = {i, j, k};
-        const double* u[3] = {ux, uy, uz};
-        double dv = 0.0;
-        for (int dd = 0; dd < P.dm; ++dd) {
-            const int m0 = P.n[0] + (dd == 0), m1 = P.n[1] + (dd == 1);
-            const int flo = i + m0 * (j + m1 * k);
-            const int stride = dd == 0 ? 1 : dd == 1 ? m0 : m0 * m1;
-            double ulo = u[dd][flo], uhi = u[dd][flo + stride];
-            if (P.have_beta0) {
-                const int r = c[P.va];
-                if (dd == P.va) {
-                    ulo = ulo * b0e[r];
-                    uhi = uhi * b0e[r + 1];
+      const double* __restrict__ tab, double* __restrict__ f, double* __restrict__ partial) {
+    __shared__ double ssum[8];
+    __shared__ unsigned long long smax[8], smin[8];
+    const int n0 = P.n[0], n1 = P.n[1], n2 = P.n[2];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k0 = blockIdx.z * kRhsPlanes;
+    double sum = 0.0;
+    unsigned long long mx = 0ull, mn = ~0ull;
+    if (i < n0 && j < n1) {
+        const int st = P.n[DM - 1] + 1;
+        for (int k = k0; k < k0 + kRhsPlanes && k < n2; ++k) {
+            const int q = i + n0 * (j + n1 * k);
+            double v;
+            if (FROM_RH) {
+                v = macrhs[q];
+            } else {
+                const int r = DM == 3 ? k : j;
+                const int fx = i + (n0 + 1) * (j + n1 * k);
+                const int fy = i + n0 * (j + (n1 + 1) * k);
+                // div(beta0 U) with beta0/dx folded into per-layer factors
+                double dv = (ux[fx + 1] - ux[fx]) * tab[kTabG0 * st + r];
+                if (DM == 3) {
+                    dv = fma(uy[fy + n0] - uy[fy], tab[(kTabG0 + 1) * st + r], dv);
+                    const double* g = tab + (kTabG0 + 2) * st;
+                    dv = fma(uz[q + n0 * n1], g[r + 1], dv);
+                    dv = fma(-uz[q], g[r], dv);
                 } else {
-                    ulo = ulo * b0[r];
-                    uhi = uhi * b0[r];
+                    const double* g = tab + (kTabG0 + 1) * st;
+                    dv = fma(uy[fy + n0], g[r + 1], dv);
+                    dv = fma(-uy[fy], g[r], dv);
                 }
+                v = macrhs ? macrhs[q] - dv : -dv;
             }
-            dv += (uhi - ulo) / P.dx[dd];
+            f[lidx(d, i, j, k)] = v;
+            sum += v;
+            const unsigned long long o = ordered_bits(v);
+            mx = o > mx ? o : mx;
+            mn = o < mn ? o : mn;
         }
-        if (macrhs) dv = dv - macrhs[q];
-        v = -dv;
-        f[lidx(d, i, j, k)] = v;
-        vmax = v;
-        vmin = v;
     }
-    const int t = threadIdx.x;
-    ssum[t] = v;
-    smax[t] = vmax;
-    smin[t] = vmin;
+    for (int o = 16; o > 0; o >>= 1) {
+        sum += __shfl_down_sync(0xffffffffu, sum, o);
+        const unsigned long long a = __shfl_down_sync(0xffffffffu, mx, o);
+        const unsigned long long b = __shfl_down_sync(0xffffffffu, mn, o);
+        mx = a > mx ? a : mx;
+        mn = b < mn ? b : mn;
+    }
+    const int t = threadIdx.x + blockDim.x * threadIdx.y;
+    const int lane = t & 31, wid = t >> 5, nw = (blockDim.x * blockDim.y) >> 5;
+    if (lane == 0) {
+        ssum[wid] = sum;
+        smax[wid] = mx;
+        smin[wid] = mn;
+    }
     __syncthreads();
-    for (int o = kBlock / 2; o > 0; o >>= 1) {
-        if (t < o) {
-            ssum[t] += ssum[t + o];
-            smax[t] = fmax(smax[t], smax[t + o]);
-            smin[t] = fmin(smin[t], smin[t + o]);
-            if (isnan(smax[t + o]) || isnan(smax[t])) smax[t] = NAN;
-        }
-        __syncthreads();
-    }
     if (t == 0) {
-        partial[3 * blockIdx.x + 0] = ssum[0];
-        partial[3 * blockIdx.x + 1] = smax[0];
-        partial[3 * blockIdx.x + 2] = smin[0];
+        double s = 0.0;
+        unsigned long long a = 0ull, b = ~0ull;
+        for (int w = 0; w < nw; ++w) {
+            s += ssum[w];
+            a = smax[w] > a ? smax[w] : a;
+            b = smin[w] < b ? smin[w] : b;
+        }
+        const int blk = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+        partial[3 * blk + 0] = s;
+        partial[3 * blk + 1] = __longlong_as_double((long long)a);
+        partial[3 * blk + 2] = __longlong_as_double((long long)b);
     }
 }
 
-// Deterministic final reduction of the k_rhs partials: mean and ||f - mean||_inf.
+// Deterministic final reduction of the k_rhs partials: mean (singular problems) and
+// ||f - mean||_inf; NaN if anything is not finite.
 __global__ void k_rhs_final(int nblocks, int ncell, int singular, const double* __restrict__ partial,
                             double* __restrict__ scalars) {
-    __shared__ double ssum[1024], smax[1024], smin[1024];
-    const int t = threadIdx.x;
-    double s = 0.0, mx = -INFINITY, mn = INFINITY;
-    bool nan = false;
-    for (int b = t; b < nblocks; b += blockDim.x) {
+    __shared__ double ssum[32];
+    __shared__ unsigned long long smax[32], smin[32];
+    double s = 0.0;
+    unsigned long long mx = 0ull, mn = ~0ull;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
         s += partial[3 * b];
-        const double a = partial[3 * b + 1], c = partial[3 * b + 2];
-        nan = nan || isnan(a) || isnan(c) || isnan(partial[3 * b]);
-        mx = fmax(mx, a);
-        mn = fmin(mn, c);
+        const unsigned long long a = (unsigned long long)__double_as_longlong(partial[3 * b + 1]);
+        const unsigned long long c = (unsigned long long)__double_as_longlong(partial[3 * b + 2]);
+        mx = a > mx ? a : mx;
+        mn = c < mn ? c : mn;
     }
-    ssum[t] = s;
-    smax[t] = nan ? NAN : mx;
-    smin[t] = mn;
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_down_sync(0xffffffffu, s, o);
+        const unsigned long long a = __shfl_down_sync(0xffffffffu, mx, o);
+        const unsigned long long c = __shfl_down_sync(0xffffffffu, mn, o);
+        mx = a > mx ? a : mx;
+        mn = c < mn ? c : mn;
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        ssum[wid] = s;
+        smax[wid] = mx;
+        smin[wid] = mn;
+    }
     __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (t < o) {
-            ssum[t] += ssum[t + o];
-            const bool n2 = isnan(smax[t]) || isnan(smax[t + o]);
-            smax[t] = n2 ? NAN : fmax(smax[t], smax[t + o]);
-            smin[t] = fmin(smin[t], smin[t + o]);
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        unsigned long long a = 0ull, c = ~0ull;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            t += ssum[w];
+            a = smax[w] > a ? smax[w] : a;
+            c = smin[w] < c ? smin[w] : c;
         }
-        __syncthreads();
-    }
-    if (t == 0) {
-        const double mean = singular ? ssum[0] / ncell : 0.0;
+        const double vmax = from_ordered_bits(a), vmin = from_ordered_bits(c);
+        const double mean = singular ? t / ncell : 0.0;
         scalars[0] = mean;
-        scalars[1] = fmax(smax[0] - mean, mean - smin[0]);
-        if (isnan(smax[0]) || !isfinite(ssum[0])) scalars[1] = NAN;
-        scalars[2] = ssum[0];
-        scalars[3] = smax[0];
-        scalars[4] = smin[0];
+        scalars[1] = fmax(vmax - mean, mean - vmin);
+        if (!isfinite(t) || !isfinite(vmax) || !isfinite(vmin)) scalars[1] = NAN;
+        scalars[2] = t;
+        scalars[3] = vmax;
+        scalars[4] = vmin;
     }
 }
 
@@ -283,79 +368,68 @@ struct CorrParams {
     int n[3];
     int dir, va, have_beta0;
     int bc_lo, bc_hi;
-    double dx;
+    double idx;  // 1/dx
     double h2;   // h_dir^2 (beta = beta' * h2)
 };
 
-// U = (beta0 U - beta_f G phi) / beta0 on every face normal to P.dir (natural face layout).
+// U = (beta0 U - beta_f G phi) / beta0 = U - beta' (h / beta0) (phi_hi - phi_lo) on every face
+// normal to P.dir (natural face layout); beta' = beta_f / h^2 is the stored coefficient, h/beta0 a
+// per-layer factor.  Neumann walls keep U; Dirichlet walls use the ghost -phi_boundary.
 __global__ void __launch_bounds__(kBlock)
 k_correct(CorrParams P, Dims d, double* __restrict__ u, const double* __restrict__ phi,
           const double* __restrict__ bd, const double* __restrict__ wlo,
-          const double* __restrict__ whi, const double* __restrict__ b0,
-          const double* __restrict__ b0e) {
-    const int m0 = P.n[0] + (P.dir == 0), m1 = P.n[1] + (P.dir == 1), m2 = P.n[2] + (P.dir == 2);
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= m0 * m1 * m2) return;
-    const int i = q % m0;
-    const int row = q / m0;
-    const int j = row % m1;
-    const int k = row / m1;
-    int c[3] = {i, j, k};
+          const double* __restrict__ whi, const double* __restrict__ tab) {
     const int dir = P.dir;
-    const int nd = P.n[dir];
-    const int qd = c[dir];
-    double bb = 1.0;
-    if (P.have_beta0) {
-        const int r = c[P.va];
-        bb = (dir == P.va) ? b0e[r] : b0[r];
-    }
-    double x = u[q];
-    if (P.have_beta0) x = x * bb;
-    double beta = 0.0, g = 0.0;
+    const int m0 = P.n[0] + (dir == 0), m1 = P.n[1] + (dir == 1);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= m0 || j >= m1) return;
+    const int q = i + m0 * (j + m1 * k);
+    const int qd = dir == 0 ? i : (dir == 1 ? j : k);
+    const int nd = dir == 0 ? P.n[0] : (dir == 1 ? P.n[1] : P.n[2]);
+    const bool v2 = P.va == 2;
+    const int r = v2 ? k : j;
+    const int st = (v2 ? P.n[2] : P.n[1]) + 1;
+    const double kap = tab[(kTabK0 + dir) * st + r];
     const int plane = dir == 0 ? (j + P.n[1] * k) : dir == 1 ? (i + P.n[0] * k) : (i + P.n[0] * j);
+    // cells on the low (a) and high (b) side of the face, periodic wrap at the boundary faces
+    const int di = dir == 0, dj = dir == 1, dk = dir == 2;
+    double beta = 0.0, dphi = 0.0;
     if (qd > 0 && qd < nd) {
-        int lo[3] = {c[0], c[1], c[2]};
-        lo[dir] -= 1;
-        const int chi = lidx(d, c[0], c[1], c[2]);
-        beta = bd[chi] * P.h2;
-        g = (phi[chi] - phi[lidx(d, lo[0], lo[1], lo[2])]) / P.dx;
+        const int chi = lidx(d, i, j, k);
+        beta = bd[chi];
+        dphi = phi[chi] - phi[lidx(d, i - di, j - dj, k - dk)];
     } else if ((qd == 0 && P.bc_lo == MAC_BC_PER) || (qd == nd && P.bc_hi == MAC_BC_PER)) {
-        int hi[3] = {c[0], c[1], c[2]}, lo[3] = {c[0], c[1], c[2]};
-        hi[dir] = 0;
-        lo[dir] = nd - 1;
-        const int chi = lidx(d, hi[0], hi[1], hi[2]);
-        beta = bd[chi] * P.h2;
-        g = (phi[chi] - phi[lidx(d, lo[0], lo[1], lo[2])]) / P.dx;
+        const int chi = lidx(d, di ? 0 : i, dj ? 0 : j, dk ? 0 : k);
+        beta = bd[chi];
+        dphi = phi[chi] - phi[lidx(d, di ? nd - 1 : i, dj ? nd - 1 : j, dk ? nd - 1 : k)];
     } else if (qd == 0) {
         if (P.bc_lo == MAC_BC_DIR) {
-            beta = wlo[plane] * P.h2;
-            g = 2.0 * phi[lidx(d, c[0], c[1], c[2])] / P.dx;
+            beta = wlo[plane];
+            dphi = 2.0 * phi[lidx(d, i, j, k)];
         }
-    } else {
-        if (P.bc_hi == MAC_BC_DIR) {
-            int lo[3] = {c[0], c[1], c[2]};
-            lo[dir] -= 1;
-            beta = whi[plane] * P.h2;
-            g = -2.0 * phi[lidx(d, lo[0], lo[1], lo[2])] / P.dx;
-        }
+    } else if (P.bc_hi == MAC_BC_DIR) {
+        beta = whi[plane];
+        dphi = -2.0 * phi[lidx(d, i - di, j - dj, k - dk)];
     }
-    x = x - beta * g;
-    if (P.have_beta0) x = x / bb;
-    u[q] = x;
+    if (beta != 0.0) u[q] = fma(-(beta * kap), dphi, u[q]);
 }
 
 __global__ void k_nat_to_l0(Dims d, const double* __restrict__ src, double* __restrict__ dst) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= d.ncell) return;
-    const int i = q % d.n0, row = q / d.n0, j = row % d.n1, k = row / d.n1;
-    dst[lidx(d, i, j, k)] = src[q];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= d.n0 || j >= d.n1) return;
+    dst[lidx(d, i, j, k)] = src[i + d.n0 * (j + d.n1 * k)];
 }
 
 __global__ void k_l0_to_nat(Dims d, const double* __restrict__ src, double* __restrict__ dst) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= d.ncell) return;
-    const int i = q % d.n0, row = q / d.n0, j = row % d.n1, k = row / d.n1;
-    dst[q] = src[lidx(d, i, j, k)];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= d.n0 || j >= d.n1) return;
+    dst[i + d.n0 * (j + d.n1 * k)] = src[lidx(d, i, j, k)];
 }
 
 // ---- caller box layout <-> whole-domain natural arrays --------------------------------------
@@ -426,12 +500,11 @@ k_fine_coef_faces(FineParams P, Dims d, const double* __restrict__ fx,
                   double* __restrict__ bx, double* __restrict__ by, double* __restrict__ bz,
                   double* __restrict__ wlo0, double* __restrict__ whi0, double* __restrict__ wlo1,
                   double* __restrict__ whi1, double* __restrict__ wlo2, double* __restrict__ whi2) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= d.ncell) return;
-    const int i = q % P.n[0];
-    const int row = q / P.n[0];
-    const int j = row % P.n[1];
-    const int k = row / P.n[1];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= P.n[0] || j >= P.n[1]) return;
+    const int q = i + P.n[0] * (j + P.n[1] * k);
     const int c[3] = {i, j, k};
     const int li = lidx(d, i, j, k);
     const double* fin[3] = {fx, fy, fz};
@@ -457,46 +530,45 @@ k_fine_coef_faces(FineParams P, Dims d, const double* __restrict__ fx,
     }
 }
 
-// f <- rh (natural) in the level-0 layout, with the per-block (sum, max, min) of k_rhs.
-__global__ void __launch_bounds__(kBlock)
-k_load_rhs(Dims d, const double* __restrict__ rh, double* __restrict__ f,
-           double* __restrict__ partial) {
-    __shared__ double ssum[kBlock], smax[kBlock], smin[kBlock];
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    double v = 0.0, vmax = -INFINITY, vmin = INFINITY;
-    if (q < d.ncell) {
-        const int i = q % d.n0, row = q / d.n0, j = row % d.n1, k = row / d.n1;
-        v = rh[q];
-        f[lidx(d, i, j, k)] = v;
-        vmax = v;
-        vmin = v;
-    }
-    const int t = threadIdx.x;
-    ssum[t] = v;
-    smax[t] = vmax;
-    smin[t] = vmin;
-    __syncthreads();
-    for (int o = kBlock / 2; o > 0; o >>= 1) {
-        if (t < o) {
-            ssum[t] += ssum[t + o];
-            const bool n2 = isnan(smax[t]) || isnan(smax[t + o]);
-            smax[t] = n2 ? NAN : fmax(smax[t], smax[t + o]);
-            smin[t] = fmin(smin[t], smin[t + o]);
-        }
-        __syncthreads();
-    }
-    if (t == 0) {
-        partial[3 * blockIdx.x + 0] = ssum[0];
-        partial[3 * blockIdx.x + 1] = smax[0];
-        partial[3 * blockIdx.x + 2] = smin[0];
-    }
-}
-
 Dims level0_dims(const mac_ctx* c) { return c->lev[0].d; }
 
 }  // namespace
 
 // ------------------------------------------------------------------------------------------
+namespace {
+
+DiagParams diag_params(const mac_ctx* c, const Level& L) {
+    DiagParams D;
+    D.any_dir = 0;
+    for (int d = 0; d < 3; ++d) {
+        D.bc_lo[d] = c->bc_lo[d];
+        D.bc_hi[d] = c->bc_hi[d];
+        D.wl[d] = L.wall[d][0];
+        D.wh[d] = L.wall[d][1];
+        D.any_dir |= (c->bc_lo[d] == MAC_BC_DIR || c->bc_hi[d] == MAC_BC_DIR) ? 1 : 0;
+    }
+    return D;
+}
+
+bool mixed(const mac_ctx* c) { return c->o.precision == MAC_PREC_MIXED; }
+
+// diag (+ 1/diag in FP64 where an FP64 smoother or the bottom solve reads it, + FP32 copies
+// for the mixed-precision inner cycle) of level l.
+int build_diag(mac_ctx* c, int l, bool fp32) {
+    Level& L = c->lev[l];
+    const bool need_inv64 = !mixed(c) || l == c->nlevels - 1;
+    const Grid3 g = grid3(L.d.n0, L.d.n1, L.d.n2);
+    k_build_diag<<<g.grid, g.block, 0, c->stream>>>(
+        L.d, diag_params(c, L), L.a64.bx, L.a64.by, L.a64.bz, L.alpha, L.a64.diag,
+        need_inv64 ? L.a64.invdiag : nullptr, fp32 ? L.a32.diag : nullptr,
+        fp32 ? L.a32.invdiag : nullptr);
+    MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
+    return MAC_OK;
+}
+
+}  // namespace
+
 int setup_fine_coefficients(mac_ctx* c, const double* beta0, const double* beta0e) {
     Level& L = c->lev[0];
     FineParams P;
@@ -510,33 +582,34 @@ int setup_fine_coefficients(mac_ctx* c, const double* beta0, const double* beta0
     P.va = c->va;
     P.p = beta0 ? (c->o.use_alt_energy_fix ? 2 : 1) : 0;
     MAC_CUDA_TRY(cudaMemsetAsync(c->red.counters, 0, 4 * sizeof(int), c->stream));
-    k_fine_coef<<<ceil_div(L.d.ncell, kBlock), kBlock, 0, c->stream>>>(
-        P, L.d, c->rho, beta0, beta0e, L.a64.bx, L.a64.by, L.a64.bz, L.wall[0][0], L.wall[0][1],
-        L.wall[1][0], L.wall[1][1], L.wall[2][0], L.wall[2][1], c->red.counters + 1);
+    const int nr = c->n[c->va];
+    k_beta0_tables<<<ceil_div(nr + 1, 128), 128, 0, c->stream>>>(
+        nr, c->va, P.p, beta0, beta0e, make_double3(L.h[0], L.h[1], L.h[2]), c->b0tab, c->fac32,
+        c->bc_lo[c->va] == MAC_BC_PER ? 1 : 0, c->bc_lo[c->va] == MAC_BC_DIR ? 1 : 0,
+        c->bc_hi[c->va] == MAC_BC_DIR ? 1 : 0);
     MAC_CUDA_TRY(cudaGetLastError());
     ++c->issued;
-    DiagParams D;
-    for (int d = 0; d < 3; ++d) {
-        D.bc_lo[d] = c->bc_lo[d];
-        D.bc_hi[d] = c->bc_hi[d];
-        D.wl[d] = L.wall[d][0];
-        D.wh[d] = L.wall[d][1];
-    }
-    k_build_diag<<<ceil_div(L.d.ncell, kBlock), kBlock, 0, c->stream>>>(
-        L.d, D, L.a64.bx, L.a64.by, L.a64.bz, L.alpha, L.a64.diag, L.a64.invdiag);
+    const Grid3 g = grid3(L.d.n0, L.d.n1, L.d.n2);
+    k_fine_coef<<<g.grid, g.block, 0, c->stream>>>(
+        P, L.d, c->rho, c->b0tab, L.a64.bx, L.a64.by, L.a64.bz, L.wall[0][0], L.wall[0][1],
+        L.wall[1][0], L.wall[1][1], L.wall[2][0], L.wall[2][1], c->red.counters + 1,
+        c->otf ? c->rho32 : nullptr);
     MAC_CUDA_TRY(cudaGetLastError());
     ++c->issued;
-    return MAC_OK;
+    return build_diag(c, 0, mixed(c) && !c->otf);
 }
 
 int setup_coarse_levels(mac_ctx* c) {
+    const bool fp32 = mixed(c);
     for (int l = 1; l < c->nlevels; ++l) {
         Level& F = c->lev[l - 1];
         Level& C = c->lev[l];
-        k_coarsen_coef<<<ceil_div(C.d.ncell, kBlock), kBlock, 0, c->stream>>>(
-            F.d, C.d, F.a64.bx, F.a64.by, F.a64.bz, F.alpha, C.a64.bx, C.a64.by, C.a64.bz, C.alpha);
+        const Grid3 g = grid3(C.d.n0, C.d.n1, C.d.n2);
+        k_coarsen_coef<<<g.grid, g.block, 0, c->stream>>>(
+            F.d, C.d, F.a64.bx, F.a64.by, F.a64.bz, F.alpha, C.a64.bx, C.a64.by, C.a64.bz, C.alpha,
+            fp32 ? C.a32.bx : nullptr, fp32 ? C.a32.by : nullptr, fp32 ? C.a32.bz : nullptr);
         MAC_CUDA_TRY(cudaGetLastError());
-    ++c->issued;
+        ++c->issued;
         for (int d = 0; d < 3; ++d)
             for (int s = 0; s < 2; ++s) {
                 if (!C.wall[d][s]) continue;
@@ -549,52 +622,60 @@ int setup_coarse_levels(mac_ctx* c) {
                 k_coarsen_wall<<<ceil_div((long)np0 * np1, kBlock), kBlock, 0, c->stream>>>(
                     np0, np1, r[p0], r[p1], fn[p0], F.wall[d][s], C.wall[d][s]);
                 MAC_CUDA_TRY(cudaGetLastError());
-    ++c->issued;
+                ++c->issued;
             }
-        DiagParams D;
-        for (int d = 0; d < 3; ++d) {
-            D.bc_lo[d] = c->bc_lo[d];
-            D.bc_hi[d] = c->bc_hi[d];
-            D.wl[d] = C.wall[d][0];
-            D.wh[d] = C.wall[d][1];
-        }
-        k_build_diag<<<ceil_div(C.d.ncell, kBlock), kBlock, 0, c->stream>>>(
-            C.d, D, C.a64.bx, C.a64.by, C.a64.bz, C.alpha, C.a64.diag, C.a64.invdiag);
-        MAC_CUDA_TRY(cudaGetLastError());
-    ++c->issued;
+        int rc = build_diag(c, l, fp32);
+        if (rc) return rc;
     }
     return MAC_OK;
 }
 
+// FP32 copies of the finest level's operator for the mixed-precision inner cycle when its
+// coefficients are not computed on the fly (mac_multigrid: face coefficients given).
 int setup_fp32_copies(mac_ctx* c) {
-    for (int l = 0; l < c->nlevels; ++l) {
-        Level& L = c->lev[l];
-        if (!L.a32.bx) continue;
-        const int n = L.d.ncell;
-        const double* src[5] = {L.a64.bx, L.a64.by, L.a64.bz, L.a64.diag, L.a64.invdiag};
-        float* dst[5] = {L.a32.bx, L.a32.by, L.a32.bz, L.a32.diag, L.a32.invdiag};
-        for (int a = 0; a < 5; ++a) {
-            k_to_f32<<<ceil_div(n, kBlock), kBlock, 0, c->stream>>>(n, src[a], dst[a]);
-            MAC_CUDA_TRY(cudaGetLastError());
-    ++c->issued;
-        }
+    if (c->otf) return MAC_OK;
+    Level& L = c->lev[0];
+    const int n = L.d.ncell;
+    const double* src[3] = {L.a64.bx, L.a64.by, L.a64.bz};
+    float* dst[3] = {L.a32.bx, L.a32.by, L.a32.bz};
+    for (int a = 0; a < 3; ++a) {
+        k_to_f32<<<ceil_div(n, kBlock), kBlock, 0, c->stream>>>(n, src[a], dst[a]);
+        MAC_CUDA_TRY(cudaGetLastError());
+        ++c->issued;
     }
     return MAC_OK;
 }
 
-int setup_rhs(mac_ctx* c, const double* macrhs, bool have_beta0) {
+namespace {
+
+int launch_rhs(mac_ctx* c, const double* macrhs, bool from_rh) {
     Level& L = c->lev[0];
     RhsParams P;
     for (int d = 0; d < 3; ++d) {
         P.n[d] = c->n[d];
-        P.dx[d] = c->dx[d];
+        P.idx[d] = 1.0 / c->dx[d];
     }
     P.dm = c->dm;
     P.va = c->va;
-    P.have_beta0 = have_beta0 ? 1 : 0;
-    const int nb = ceil_div(L.d.ncell, kBlock);
-    k_rhs<<<nb, kBlock, 0, c->stream>>>(P, L.d, c->u[0], c->u[1], c->u[2], macrhs, c->beta0,
-                                        c->beta0e, L.a64.f, c->red.partial);
+    P.have_beta0 = 1;
+    const Grid3 g = rhs_grid(c->n);
+    const int nb = (int)(g.grid.x * g.grid.y * g.grid.z);
+    if (nb > c->red.nblocks_partial) return MAC_ERR_INVALID;   // buffer sized by rhs_grid
+    if (c->dm == 3) {
+        if (from_rh)
+            k_rhs<3, true><<<g.grid, g.block, 0, c->stream>>>(P, L.d, nullptr, nullptr, nullptr, macrhs,
+                                                              c->b0tab, L.a64.f, c->red.partial);
+        else
+            k_rhs<3, false><<<g.grid, g.block, 0, c->stream>>>(P, L.d, c->u[0], c->u[1], c->u[2], macrhs,
+                                                               c->b0tab, L.a64.f, c->red.partial);
+    } else {
+        if (from_rh)
+            k_rhs<2, true><<<g.grid, g.block, 0, c->stream>>>(P, L.d, nullptr, nullptr, nullptr, macrhs,
+                                                              c->b0tab, L.a64.f, c->red.partial);
+        else
+            k_rhs<2, false><<<g.grid, g.block, 0, c->stream>>>(P, L.d, c->u[0], c->u[1], nullptr, macrhs,
+                                                               c->b0tab, L.a64.f, c->red.partial);
+    }
     MAC_CUDA_TRY(cudaGetLastError());
     ++c->issued;
     k_rhs_final<<<1, 1024, 0, c->stream>>>(nb, L.d.ncell, c->singular ? 1 : 0, c->red.partial,
@@ -602,11 +683,19 @@ int setup_rhs(mac_ctx* c, const double* macrhs, bool have_beta0) {
     MAC_CUDA_TRY(cudaGetLastError());
     ++c->issued;
     if (c->singular) {
-        k_sub_mean<<<nb, kBlock, 0, c->stream>>>(L.d.ncell, L.a64.f, c->red.scalars);
+        k_sub_mean<<<ceil_div(L.d.ncell, kBlock), kBlock, 0, c->stream>>>(L.d.ncell, L.a64.f,
+                                                                         c->red.scalars);
         MAC_CUDA_TRY(cudaGetLastError());
-    ++c->issued;
+        ++c->issued;
     }
     return MAC_OK;
+}
+
+}  // namespace
+
+int setup_rhs(mac_ctx* c, const double* macrhs, bool have_beta0) {
+    (void)have_beta0;   // the factor tables hold beta0 = 1 when there is none
+    return launch_rhs(c, macrhs, false);
 }
 
 int correct_velocity(mac_ctx* c, bool have_beta0) {
@@ -620,20 +709,21 @@ int correct_velocity(mac_ctx* c, bool have_beta0) {
         P.have_beta0 = have_beta0 ? 1 : 0;
         P.bc_lo = c->bc_lo[d];
         P.bc_hi = c->bc_hi[d];
-        P.dx = c->dx[d];
+        P.idx = 1.0 / c->dx[d];
         P.h2 = c->dx[d] * c->dx[d];
-        const long nf = (long)(c->n[0] + (d == 0)) * (c->n[1] + (d == 1)) * (c->n[2] + (d == 2));
-        k_correct<<<ceil_div(nf, kBlock), kBlock, 0, c->stream>>>(
-            P, L.d, c->u[d], L.a64.phi, bd[d], L.wall[d][0], L.wall[d][1], c->beta0, c->beta0e);
+        const Grid3 g = grid3(c->n[0] + (d == 0), c->n[1] + (d == 1), c->n[2] + (d == 2));
+        k_correct<<<g.grid, g.block, 0, c->stream>>>(P, L.d, c->u[d], L.a64.phi, bd[d],
+                                                     L.wall[d][0], L.wall[d][1], c->b0tab);
         MAC_CUDA_TRY(cudaGetLastError());
-    ++c->issued;
+        ++c->issued;
     }
     return MAC_OK;
 }
 
 int natural_to_level0(mac_ctx* c, const double* src, double* dst) {
     const Dims d = level0_dims(c);
-    k_nat_to_l0<<<ceil_div(d.ncell, kBlock), kBlock, 0, c->stream>>>(d, src, dst);
+    const Grid3 g = grid3(d.n0, d.n1, d.n2);
+    k_nat_to_l0<<<g.grid, g.block, 0, c->stream>>>(d, src, dst);
     MAC_CUDA_TRY(cudaGetLastError());
     ++c->issued;
     return MAC_OK;
@@ -641,7 +731,8 @@ int natural_to_level0(mac_ctx* c, const double* src, double* dst) {
 
 int level0_to_natural(mac_ctx* c, const double* src, double* dst) {
     const Dims d = level0_dims(c);
-    k_l0_to_nat<<<ceil_div(d.ncell, kBlock), kBlock, 0, c->stream>>>(d, src, dst);
+    const Grid3 g = grid3(d.n0, d.n1, d.n2);
+    k_l0_to_nat<<<g.grid, g.block, 0, c->stream>>>(d, src, dst);
     MAC_CUDA_TRY(cudaGetLastError());
     ++c->issued;
     return MAC_OK;
@@ -854,43 +945,16 @@ int setup_fine_from_faces(mac_ctx* c, const double* fx, const double* fy, const 
     P.va = c->va;
     P.p = 0;
     MAC_CUDA_TRY(cudaMemsetAsync(c->red.counters, 0, 4 * sizeof(int), c->stream));
-    k_fine_coef_faces<<<ceil_div(L.d.ncell, kBlock), kBlock, 0, c->stream>>>(
+    const Grid3 g = grid3(L.d.n0, L.d.n1, L.d.n2);
+    k_fine_coef_faces<<<g.grid, g.block, 0, c->stream>>>(
         P, L.d, fx, fy, fz, alpha_nat, alpha_nat ? L.alpha : nullptr, L.a64.bx, L.a64.by,
         L.a64.bz, L.wall[0][0], L.wall[0][1], L.wall[1][0], L.wall[1][1], L.wall[2][0],
         L.wall[2][1]);
     MAC_CUDA_TRY(cudaGetLastError());
     ++c->issued;
-    DiagParams D;
-    for (int d = 0; d < 3; ++d) {
-        D.bc_lo[d] = c->bc_lo[d];
-        D.bc_hi[d] = c->bc_hi[d];
-        D.wl[d] = L.wall[d][0];
-        D.wh[d] = L.wall[d][1];
-    }
-    k_build_diag<<<ceil_div(L.d.ncell, kBlock), kBlock, 0, c->stream>>>(
-        L.d, D, L.a64.bx, L.a64.by, L.a64.bz, alpha_nat ? L.alpha : nullptr, L.a64.diag,
-        L.a64.invdiag);
-    MAC_CUDA_TRY(cudaGetLastError());
-    ++c->issued;
-    return MAC_OK;
+    return build_diag(c, 0, mixed(c));
 }
 
-int setup_rhs_from(mac_ctx* c, const double* rh_nat) {
-    Level& L = c->lev[0];
-    const int nb = ceil_div(L.d.ncell, kBlock);
-    k_load_rhs<<<nb, kBlock, 0, c->stream>>>(L.d, rh_nat, L.a64.f, c->red.partial);
-    MAC_CUDA_TRY(cudaGetLastError());
-    ++c->issued;
-    k_rhs_final<<<1, 1024, 0, c->stream>>>(nb, L.d.ncell, c->singular ? 1 : 0, c->red.partial,
-                                           c->red.scalars);
-    MAC_CUDA_TRY(cudaGetLastError());
-    ++c->issued;
-    if (c->singular) {
-        k_sub_mean<<<nb, kBlock, 0, c->stream>>>(L.d.ncell, L.a64.f, c->red.scalars);
-        MAC_CUDA_TRY(cudaGetLastError());
-    ++c->issued;
-    }
-    return MAC_OK;
-}
+int setup_rhs_from(mac_ctx* c, const double* rh_nat) { return launch_rhs(c, rh_nat, true); }
 
 }  // namespace mac

@@ -15,6 +15,7 @@
 #include <chrono>
 #include <mutex>
 #include <string>
+#include <type_traits>
 
 #include "mac_internal.cuh"
 
@@ -22,7 +23,6 @@ namespace mac {
 
 namespace {
 thread_local std::string g_last_cuda;
-constexpr int kBlk = 256;
 
 double bits_to_double(unsigned long long b) {
     double d;
@@ -90,42 +90,112 @@ LevelArrays<double>& arrays<double>(Level& L) { return L.a64; }
 template <>
 LevelArrays<float>& arrays<float>(Level& L) { return L.a32; }
 
+OtfParams otf_params(const mac_ctx* c) {
+    OtfParams P;
+    for (int d = 0; d < 3; ++d) {
+        P.n[d] = c->n[d];
+        P.per[d] = (d < c->dm && c->bc_lo[d] == MAC_BC_PER) ? 1 : 0;
+        P.dlo[d] = (d < c->dm && c->bc_lo[d] == MAC_BC_DIR) ? 1 : 0;
+        P.dhi[d] = (d < c->dm && c->bc_hi[d] == MAC_BC_DIR) ? 1 : 0;
+    }
+    P.has_dir = 0;
+    for (int d = 0; d < 3; ++d) P.has_dir |= P.dlo[d] | P.dhi[d];
+    P.va = c->va;
+    P.dm = c->dm;
+    P.fac = c->fac32;
+    P.rho = c->rho32;
+    return P;
+}
+
+inline void mark(mac_ctx* c, bool on, int slot) {
+    if (on && c->vtimer < 4)
+        cudaEventRecordWithFlags(c->tev[c->vtimer][slot], c->stream, cudaEventRecordExternal);
+}
+
 template <typename T>
 void vcycle(mac_ctx* c, int l) {
     Level& L = c->lev[l];
     LevelArrays<T>& a = arrays<T>(L);
     const mac_opts& o = c->o;
     const bool tm = o.timing && l == 0;
+    const bool otf = std::is_same<T, float>::value && l == 0 && c->otf;
     if (l == c->nlevels - 1) {
         launch_bottom<T>(L.d, L.a64, a.phi, a.f, c->bottom_scratch, c->singular, o.nub,
                          o.bottom_eps, o.bottom_max_iter, c->red.counters, c->stream);
         ++c->issued;
         return;
     }
-    if (tm) cudaEventRecordWithFlags(c->tev[0], c->stream, cudaEventRecordExternal);
-    for (int s = 0; s < o.nu1; ++s) {
-        launch_gsrb<T>(L.d, 0, a, c->stream);
-        launch_gsrb<T>(L.d, 1, a, c->stream);
-        c->issued += 2;
+    const int tslot = std::is_same<T, float>::value ? 1 : 0;
+    if (o.coarse_tail && l == c->tail_start[tslot]) {
+        TailParams<T> tp;
+        tp.nlev = c->nlevels - 1 - l;
+        for (int q = 0; q < tp.nlev; ++q) {
+            Level& Lq = c->lev[l + q];
+            LevelArrays<T>& aq = arrays<T>(Lq);
+            tp.lev[q] = Lq.d;
+            tp.bx[q] = aq.bx;
+            tp.by[q] = aq.by;
+            tp.bz[q] = aq.bz;
+            tp.dg[q] = aq.diag;
+            tp.idg[q] = aq.invdiag;
+        }
+        Level& B = c->lev[c->nlevels - 1];
+        tp.bottom = B.d;
+        tp.bbx = B.a64.bx;
+        tp.bby = B.a64.by;
+        tp.bbz = B.a64.bz;
+        tp.bdg = B.a64.diag;
+        tp.bidg = B.a64.invdiag;
+        tp.f0 = a.f;
+        tp.e0 = a.phi;
+        tp.bc = bc_desc(c);
+        tp.nu1 = o.nu1;
+        tp.nu2 = o.nu2;
+        tp.nub = o.nub;
+        tp.singular = c->singular ? 1 : 0;
+        tp.bottom_max_iter = o.bottom_max_iter;
+        tp.bottom_eps = o.bottom_eps;
+        tp.iters = c->red.counters;
+        launch_tail<T>(tp, c->tail_smem[tslot], c->stream);
+        ++c->issued;
+        return;
     }
+    const OtfParams P = otf ? otf_params(c) : OtfParams{};
+    auto sweep = [&]() {
+        for (int colour = 0; colour < 2; ++colour) {
+            if (otf)
+                launch_gsrb_otf(L.d, P, colour, reinterpret_cast<float*>(a.phi),
+                                reinterpret_cast<const float*>(a.f), c->stream);
+            else
+                launch_gsrb<T>(L.d, colour, a, c->stream);
+        }
+        c->issued += 2;
+    };
+    mark(c, tm, 0);
+    for (int s = 0; s < o.nu1; ++s) sweep();
     Level& C = c->lev[l + 1];
     LevelArrays<T>& ac = arrays<T>(C);
-    if (tm) cudaEventRecordWithFlags(c->tev[1], c->stream, cudaEventRecordExternal);
-    launch_resid_restrict<T>(L.d, C.d, a, ac.f, o.nu1 > 0, c->stream);
+    mark(c, tm, 1);
+    if (otf)
+        launch_resid_restrict_otf(L.d, C.d, P, reinterpret_cast<const float*>(a.phi),
+                                  reinterpret_cast<const float*>(a.f),
+                                  reinterpret_cast<float*>(ac.f), o.nu1 > 0, c->stream);
+    else
+        launch_resid_restrict<T>(L.d, C.d, a, ac.f, o.nu1 > 0, c->stream);
     ++c->issued;
-    if (tm) cudaEventRecordWithFlags(c->tev[2], c->stream, cudaEventRecordExternal);
+    mark(c, tm, 2);
     cudaMemsetAsync(ac.phi, 0, sizeof(T) * C.d.ncell, c->stream);
     vcycle<T>(c, l + 1);
-    if (tm) cudaEventRecordWithFlags(c->tev[3], c->stream, cudaEventRecordExternal);
+    mark(c, tm, 3);
     launch_prolong_add<T>(L.d, C.d, bc_desc(c), ac.phi, a.phi, c->stream);
     ++c->issued;
-    if (tm) cudaEventRecordWithFlags(c->tev[4], c->stream, cudaEventRecordExternal);
-    for (int s = 0; s < o.nu2; ++s) {
-        launch_gsrb<T>(L.d, 0, a, c->stream);
-        launch_gsrb<T>(L.d, 1, a, c->stream);
-        c->issued += 2;
-    }
-    if (tm) cudaEventRecordWithFlags(c->tev[5], c->stream, cudaEventRecordExternal);
+    mark(c, tm, 4);
+    for (int s = 0; s < o.nu2; ++s) sweep();
+    mark(c, tm, 5);
+}
+
+int inner_cycles(const mac_ctx* c, int prec) {
+    return prec == MAC_PREC_FP64 ? 1 : (c->o.inner_vcycles > 1 ? c->o.inner_vcycles : 1);
 }
 
 // One iteration of the outer loop, ending with the max-norm of the fine residual in
@@ -135,20 +205,27 @@ void issue_iteration(mac_ctx* c, int prec) {
     const bool tm = c->o.timing;
     cudaMemsetAsync(c->red.maxbits, 0, sizeof(unsigned long long), c->stream);
     if (prec == MAC_PREC_FP64) {
+        c->vtimer = 0;
         vcycle<double>(c, 0);
-        if (tm) cudaEventRecordWithFlags(c->tev[6], c->stream, cudaEventRecordExternal);
+        if (tm) cudaEventRecordWithFlags(c->tail[0], c->stream, cudaEventRecordExternal);
+        if (tm) cudaEventRecordWithFlags(c->tail[1], c->stream, cudaEventRecordExternal);
         launch_resid_norm<double>(F.d, F.a64, c->o.nu2 > 0, c->red.maxbits, c->stream);
         ++c->issued;
     } else {
         cudaMemsetAsync(F.a32.phi, 0, sizeof(float) * F.d.ncell, c->stream);
-        vcycle<float>(c, 0);
+        const int nv = inner_cycles(c, prec);
+        for (int v = 0; v < nv; ++v) {
+            c->vtimer = v;
+            vcycle<float>(c, 0);
+        }
+        if (tm) cudaEventRecordWithFlags(c->tail[0], c->stream, cudaEventRecordExternal);
         launch_accumulate(F.d, F.a64.phi, F.a32.phi, c->stream);
         ++c->issued;
-        if (tm) cudaEventRecordWithFlags(c->tev[6], c->stream, cudaEventRecordExternal);
+        if (tm) cudaEventRecordWithFlags(c->tail[1], c->stream, cudaEventRecordExternal);
         launch_resid64_to32(F.d, F.a64, F.a32.f, c->red.maxbits, c->stream);
         ++c->issued;
     }
-    if (tm) cudaEventRecordWithFlags(c->tev[7], c->stream, cudaEventRecordExternal);
+    if (tm) cudaEventRecordWithFlags(c->tail[2], c->stream, cudaEventRecordExternal);
     cudaMemcpyAsync(c->red.h_maxbits, c->red.maxbits, sizeof(unsigned long long),
                     cudaMemcpyDeviceToHost, c->stream);
 }
@@ -156,24 +233,30 @@ void issue_iteration(mac_ctx* c, int prec) {
 // Accumulate the per-class device times of the iteration that just completed.
 void collect_timing(mac_ctx* c, int prec) {
     if (!c->o.timing) return;
-    float t[7];
-    for (int e = 0; e < 7; ++e) {
-        t[e] = 0.f;
-        cudaEventElapsedTime(&t[e], c->tev[e], c->tev[e + 1]);
-    }
     const mac_opts& o = c->o;
-    c->ktime_ms[MAC_KT_SMOOTH] += t[0] + t[4];
-    c->ktime_launches[MAC_KT_SMOOTH] += 2 * (o.nu1 + o.nu2);
-    c->ktime_ms[MAC_KT_RESTRICT] += t[1];
-    c->ktime_launches[MAC_KT_RESTRICT] += 1;
-    c->ktime_ms[MAC_KT_COARSE] += t[2];
-    c->ktime_ms[MAC_KT_PROLONG] += t[3];
-    c->ktime_launches[MAC_KT_PROLONG] += 1;
+    const int nv = inner_cycles(c, prec);
+    for (int v = 0; v < nv && v < 4; ++v) {
+        float t[5];
+        for (int e = 0; e < 5; ++e) {
+            t[e] = 0.f;
+            cudaEventElapsedTime(&t[e], c->tev[v][e], c->tev[v][e + 1]);
+        }
+        c->ktime_ms[MAC_KT_SMOOTH] += t[0] + t[4];
+        c->ktime_launches[MAC_KT_SMOOTH] += 2 * (o.nu1 + o.nu2);
+        c->ktime_ms[MAC_KT_RESTRICT] += t[1];
+        c->ktime_launches[MAC_KT_RESTRICT] += 1;
+        c->ktime_ms[MAC_KT_COARSE] += t[2];
+        c->ktime_ms[MAC_KT_PROLONG] += t[3];
+        c->ktime_launches[MAC_KT_PROLONG] += 1;
+    }
+    float ta = 0.f, tr = 0.f;
+    cudaEventElapsedTime(&ta, c->tail[0], c->tail[1]);
+    cudaEventElapsedTime(&tr, c->tail[1], c->tail[2]);
     if (prec == MAC_PREC_MIXED) {
-        c->ktime_ms[MAC_KT_ACCUM] += t[5];
+        c->ktime_ms[MAC_KT_ACCUM] += ta;
         c->ktime_launches[MAC_KT_ACCUM] += 1;
     }
-    c->ktime_ms[MAC_KT_RESID] += t[6];
+    c->ktime_ms[MAC_KT_RESID] += tr;
     c->ktime_launches[MAC_KT_RESID] += 1;
 }
 
@@ -233,10 +316,6 @@ int run_solve(mac_ctx* c, mac_stats* st) {
     Level& F = c->lev[0];
     const int prec = o.precision;
     if (prec == MAC_PREC_MIXED) {
-        for (int l = 0; l < c->nlevels; ++l) {
-            int rc = alloc_level_fp32(c, c->lev[l]);
-            if (rc) return rc;
-        }
         int rc = setup_fp32_copies(c);
         if (rc) return rc;
     }
@@ -398,11 +477,37 @@ int ctx_alloc(mac_ctx* c) {
             if (c->dm == 3) h[2] *= 2;
         }
     }
+    // FP32 copies for the mixed-precision inner cycle (precision can change per call)
+    for (auto& L : c->lev) {
+        rc = alloc_level_fp32(c, L);
+        if (rc) return rc;
+    }
     // z coefficients of a 2-D problem stay zero
     if (c->dm == 2)
-        for (auto& L : c->lev) MAC_CUDA_TRY(cudaMemset(L.a64.bz, 0, sizeof(double) * L.d.ncell));
+        for (auto& L : c->lev) {
+            MAC_CUDA_TRY(cudaMemset(L.a64.bz, 0, sizeof(double) * L.d.ncell));
+            MAC_CUDA_TRY(cudaMemset(L.a32.bz, 0, sizeof(float) * L.d.ncell));
+        }
     const Level& B = c->lev[c->nlevels - 1];
     if (B.d.ncell > kBottomMaxCells) return MAC_ERR_UNSUPPORTED;
+    // single-CTA tail plans: from the first level >= 1 that is small enough (FP32 <= 4096 cells,
+    // FP64 <= 512: one SM's FP64 rate) and whose tail fits in shared memory
+    for (int slot = 0; slot < 2; ++slot) {
+        const int limit = slot ? 4096 : 512;
+        c->tail_start[slot] = -1;
+        if (B.d.ncell > 4096) continue;
+        for (int l = 1; l < c->nlevels - 1; ++l) {
+            if (c->lev[l].d.ncell > limit || c->nlevels - 1 - l > kTailMaxLevels) continue;
+            Dims ds[kTailMaxLevels];
+            for (int q = 0; q < c->nlevels - 1 - l; ++q) ds[q] = c->lev[l + q].d;
+            const size_t bytes = slot ? tail_smem_bytes<float>(ds, c->nlevels - 1 - l, B.d)
+                                      : tail_smem_bytes<double>(ds, c->nlevels - 1 - l, B.d);
+            if (bytes > (size_t)kTailSmemMax) continue;
+            c->tail_start[slot] = l;
+            c->tail_smem[slot] = bytes;
+            break;
+        }
+    }
     rc |= alloc_arr(c, &c->bottom_scratch, (size_t)9 * B.d.ncell);
     for (int d = 0; d < c->dm; ++d) {
         const size_t nf = (size_t)(c->n[0] + (d == 0)) * (c->n[1] + (d == 1)) * (c->n[2] + (d == 2));
@@ -415,7 +520,11 @@ int ctx_alloc(mac_ctx* c) {
     const int nr = c->n[c->va];
     rc |= alloc_arr(c, &c->beta0, (size_t)nr);
     rc |= alloc_arr(c, &c->beta0e, (size_t)nr + 1);
-    const int nbp = ceil_div((long)N, kBlk);
+    rc |= alloc_arr(c, &c->b0tab, (size_t)kTabCount * (nr + 1));
+    rc |= alloc_arr(c, &c->fac32, (size_t)kOtfTables * (nr + 1));
+    rc |= alloc_arr(c, &c->rho32, N);
+    const Grid3 rg = rhs_grid(c->n);
+    const int nbp = (int)(rg.grid.x * rg.grid.y * rg.grid.z);
     c->red.nblocks_partial = nbp;
     rc |= alloc_arr(c, &c->red.partial, (size_t)3 * nbp);
     rc |= alloc_arr(c, &c->red.scalars, 8);
@@ -430,7 +539,9 @@ int ctx_alloc(mac_ctx* c) {
     rc |= alloc_arr(c, &c->d_boxes, (size_t)c->box_table_cap);
     if (rc) return MAC_ERR_ALLOC;
     for (int e = 0; e < 4; ++e) MAC_CUDA_TRY(cudaEventCreate(&c->ev[e]));
-    for (int e = 0; e < 8; ++e) MAC_CUDA_TRY(cudaEventCreate(&c->tev[e]));
+    for (int v = 0; v < 4; ++v)
+        for (int e = 0; e < 8; ++e) MAC_CUDA_TRY(cudaEventCreate(&c->tev[v][e]));
+    for (int e = 0; e < 3; ++e) MAC_CUDA_TRY(cudaEventCreate(&c->tail[e]));
     MAC_CUDA_TRY(cudaMemset(c->red.counters, 0, 4 * sizeof(int)));
     return MAC_OK;
 }
@@ -447,8 +558,11 @@ void ctx_free(mac_ctx* c) {
     if (c->h_boxes) cudaFreeHost(c->h_boxes);
     for (int e = 0; e < 4; ++e)
         if (c->ev[e]) cudaEventDestroy(c->ev[e]);
-    for (int e = 0; e < 8; ++e)
-        if (c->tev[e]) cudaEventDestroy(c->tev[e]);
+    for (int v = 0; v < 4; ++v)
+        for (int e = 0; e < 8; ++e)
+            if (c->tev[v][e]) cudaEventDestroy(c->tev[v][e]);
+    for (int e = 0; e < 3; ++e)
+        if (c->tail[e]) cudaEventDestroy(c->tail[e]);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     c->stream = nullptr;
 }
@@ -464,6 +578,12 @@ int load_beta0_impl(mac_ctx* c, int ptr_kind, const double* b0, const double* b0
 
 // Per-call operator state: alpha on/off (Helmholtz) and whether the problem is singular.
 // CUDA graphs bake the singular flag into the bottom solve, so they are dropped on a change.
+int set_otf(mac_ctx* c, bool on) {
+    if (on != c->otf) drop_graphs(c);
+    c->otf = on;
+    return MAC_OK;
+}
+
 int set_call_state_impl(mac_ctx* c, bool with_alpha) {
     for (auto& L : c->lev) {
         if (with_alpha && !L.alpha_store) {
@@ -484,6 +604,7 @@ int core_macproject(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats
     cudaEventRecord(c->ev[0], c->stream);
     int rc = set_call_state_impl(c, false);
     if (rc) return rc;
+    set_otf(c, c->o.precision == MAC_PREC_MIXED);
     rc = setup_fine_coefficients(c, have_beta0 ? c->beta0 : nullptr, have_beta0 ? c->beta0e : nullptr);
     if (rc) return rc;
     rc = setup_coarse_levels(c);
@@ -576,6 +697,9 @@ void mac_default_opts(mac_opts* o) {
     o->max_levels = 0;
     o->use_graph = 1;
     o->verbose = 0;
+    o->timing = 0;
+    o->inner_vcycles = 3;
+    o->coarse_tail = 1;
 }
 
 const char* mac_strerror(int code) {
@@ -646,7 +770,9 @@ int mac_ctx_create(mac_ctx** out, const mac_geom* g, const mac_opts* o, void* cu
         delete c;
         return MAC_ERR_UNSUPPORTED;
     }
-    rc = ctx_alloc(c);
+    rc = prepare_kernels();
+    if (!rc) rc = prepare_tail_kernels();
+    if (!rc) rc = ctx_alloc(c);
     if (rc) {
         ctx_free(c);
         delete c;
@@ -787,6 +913,7 @@ int mac_multigrid(mac_ctx* c, int ptr_kind, const double* const* rh, int ng_rh,
     fill_common_stats(c, st);
     Level& F = c->lev[0];
     int rc = set_call_state_impl(c, alpha != nullptr);
+    set_otf(c, false);
     for (int d = 0; d < c->dm && !rc; ++d)
         rc = gather_faces(c, ptr_kind, beta + d * nb, ng_beta, d, c->u[d]);
     if (!rc) rc = gather_cells(c, ptr_kind, rh, ng_rh, 1, 0, c->rhs);

@@ -1,0 +1,329 @@
+// Single-CTA "tail" of the V-cycle: every level from the first one small enough to live in
+// shared memory down to the bottom solve runs inside one kernel, so the smallest levels no
+// longer pay one kernel launch per half-sweep.  The arithmetic is the multi-kernel V-cycle's,
+// operation for operation (same fused-multiply-add order per cell, same child order in the
+// restriction, same separable trilinear prolongation, the same single-warp bottom solve), so the
+// result is bitwise the same; only the data lives in shared memory in natural layout.
+#include "mac_internal.cuh"
+#include "mac_bottom.cuh"
+
+namespace mac {
+namespace {
+
+constexpr int kTailThreads = 1024;
+
+__device__ __forceinline__ double fmaT2(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fmaT2(float a, float b, float c) { return fmaf(a, b, c); }
+
+template <typename T>
+struct TailLevel {
+    int n0, n1, n2, N, rz;
+    T *e, *f, *bx, *by, *bz, *dg, *idg;   // shared memory, natural layout
+};
+
+__device__ __forceinline__ void decode(int c, int n0, int n1, int& i, int& j, int& k) {
+    i = c % n0;
+    const int row = c / n0;
+    j = row % n1;
+    k = row / n1;
+}
+
+template <typename T>
+__device__ __forceinline__ T arms_nat(T acc, const TailLevel<T>& L, const T* __restrict__ u, int i,
+                                      int j, int k, int c) {
+    const int im = i == 0 ? L.n0 - 1 : i - 1, ip = i == L.n0 - 1 ? 0 : i + 1;
+    const int jm = j == 0 ? L.n1 - 1 : j - 1, jp = j == L.n1 - 1 ? 0 : j + 1;
+    const int km = k == 0 ? L.n2 - 1 : k - 1, kp = k == L.n2 - 1 ? 0 : k + 1;
+    const int cxm = im + L.n0 * (j + L.n1 * k), cxp = ip + L.n0 * (j + L.n1 * k);
+    const int cym = i + L.n0 * (jm + L.n1 * k), cyp = i + L.n0 * (jp + L.n1 * k);
+    const int czm = i + L.n0 * (j + L.n1 * km), czp = i + L.n0 * (j + L.n1 * kp);
+    acc = fmaT2(L.bx[c], u[cxm], acc);
+    acc = fmaT2(L.bx[cxp], u[cxp], acc);
+    acc = fmaT2(L.by[c], u[cym], acc);
+    acc = fmaT2(L.by[cyp], u[cyp], acc);
+    acc = fmaT2(L.bz[c], u[czm], acc);
+    acc = fmaT2(L.bz[czp], u[czp], acc);
+    return acc;
+}
+
+// Thread layout over an (nx, rows) index space: tx strides x, ty strides the rows (row =
+// j + n1 k, decoded incrementally), so no per-cell integer division.
+struct Lanes {
+    int tx, ty, TX, RY;
+};
+__device__ __forceinline__ Lanes lanes(int nx) {
+    Lanes q;
+    q.TX = nx < 32 ? nx : 32;
+    q.tx = threadIdx.x % q.TX;
+    q.ty = threadIdx.x / q.TX;
+    q.RY = blockDim.x / q.TX;
+    return q;
+}
+
+template <typename T>
+__device__ void tail_sweep(const TailLevel<T>& L) {
+    const int hn0 = L.n0 >> 1, rows = L.n1 * L.n2;
+    const Lanes q = lanes(hn0);
+    for (int colour = 0; colour < 2; ++colour) {
+        if (q.ty < q.RY) {
+            int j = q.ty % L.n1, k = q.ty / L.n1;
+            const int dj = q.RY % L.n1, dk = q.RY / L.n1;
+            for (int row = q.ty; row < rows; row += q.RY) {
+                const int s = (colour + j + k) & 1;
+                for (int h = q.tx; h < hn0; h += q.TX) {
+                    const int i = 2 * h + s;
+                    const int c = i + L.n0 * row;
+                    const T acc = arms_nat<T>(L.f[c], L, L.e, i, j, k, c);
+                    L.e[c] = acc * L.idg[c];
+                }
+                j += dj;
+                k += dk;
+                if (j >= L.n1) {
+                    j -= L.n1;
+                    ++k;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// defect of level F restricted into out[coarse natural index] (as T, then converted to To)
+template <typename T, typename To>
+__device__ void tail_restrict(const TailLevel<T>& F, int cn0, int cn1, int cn2, To* out,
+                              bool red_only) {
+    const Lanes ln = lanes(cn0);
+    const int rows = cn1 * cn2;
+    for (int crow = ln.ty; ln.ty < ln.RY && crow < rows; crow += ln.RY)
+    for (int I = ln.tx; I < cn0; I += ln.TX) {
+        const int J = crow % cn1, K = crow / cn1;
+        const int q = I + cn0 * crow;
+        T sum = T(0);
+        for (int b = 0; b < F.rz; ++b) {
+            for (int a = 0; a < 2; ++a) {
+                const int j = 2 * J + a;
+                const int k = F.rz == 2 ? 2 * K + b : K;
+                for (int colour = 0; colour < (red_only ? 1 : 2); ++colour) {
+                    const int i = 2 * I + ((colour + j + k) & 1);
+                    const int c = i + F.n0 * (j + F.n1 * k);
+                    T r = fmaT2(-F.dg[c], F.e[c], F.f[c]);
+                    r = arms_nat<T>(r, F, F.e, i, j, k, c);
+                    sum += r;
+                }
+            }
+        }
+        out[q] = (To)(sum * (T)(1.0 / (4 * F.rz)));
+    }
+    __syncthreads();
+}
+
+template <typename T>
+__device__ __forceinline__ void nb_w(int q, int n, int blo, int bhi, int& qm, int& qp, T& wm, T& wp) {
+    wm = T(0.25);
+    wp = T(0.25);
+    if (q > 0) qm = q - 1;
+    else if (blo == MAC_BC_PER) qm = n - 1;
+    else {
+        qm = 0;
+        if (blo == MAC_BC_DIR) wm = T(-0.25);
+    }
+    if (q < n - 1) qp = q + 1;
+    else if (bhi == MAC_BC_PER) qp = 0;
+    else {
+        qp = n - 1;
+        if (bhi == MAC_BC_DIR) wp = T(-0.25);
+    }
+}
+
+// e_fine += trilinear interpolation of the coarse correction ec (natural, cn0 x cn1 x cn2)
+template <typename T>
+__device__ void tail_prolong(const TailLevel<T>& F, const T* ec, int cn0, int cn1, int cn2,
+                             const BcDesc& bc) {
+    const bool z2 = F.rz == 2;
+    const Lanes ln = lanes(cn0);
+    const int rows = cn1 * cn2;
+    for (int crow = ln.ty; ln.ty < ln.RY && crow < rows; crow += ln.RY)
+    for (int I = ln.tx; I < cn0; I += ln.TX) {
+        const int J = crow % cn1, K = crow / cn1;
+        int xs[3], ys[3], zs[3];
+        T wxm, wxp, wym, wyp, wzm = T(0), wzp = T(0);
+        xs[1] = I;
+        ys[1] = J;
+        zs[1] = K;
+        nb_w<T>(I, cn0, bc.lo[0], bc.hi[0], xs[0], xs[2], wxm, wxp);
+        nb_w<T>(J, cn1, bc.lo[1], bc.hi[1], ys[0], ys[2], wym, wyp);
+        if (z2) nb_w<T>(K, cn2, bc.lo[2], bc.hi[2], zs[0], zs[2], wzm, wzp);
+        T Yv[3][2][2];
+        for (int a = 0; a < 3; ++a) {
+            const int X = xs[a];
+            T Zv[3][2];
+            for (int b = 0; b < 3; ++b) {
+                const int Y = ys[b];
+                const T c0 = ec[X + cn0 * (Y + cn1 * K)];
+                if (z2) {
+                    const T t = T(0.75) * c0;
+                    Zv[b][0] = fmaT2(wzm, ec[X + cn0 * (Y + cn1 * zs[0])], t);
+                    Zv[b][1] = fmaT2(wzp, ec[X + cn0 * (Y + cn1 * zs[2])], t);
+                } else {
+                    Zv[b][0] = c0;
+                    Zv[b][1] = c0;
+                }
+            }
+            for (int zc = 0; zc < 2; ++zc) {
+                const T t = T(0.75) * Zv[1][zc];
+                Yv[a][0][zc] = fmaT2(wym, Zv[0][zc], t);
+                Yv[a][1][zc] = fmaT2(wyp, Zv[2][zc], t);
+            }
+        }
+        for (int zc = 0; zc < (z2 ? 2 : 1); ++zc) {
+            for (int yc = 0; yc < 2; ++yc) {
+                const T t = T(0.75) * Yv[1][yc][zc];
+                const T v0 = fmaT2(wxm, Yv[0][yc][zc], t);
+                const T v1 = fmaT2(wxp, Yv[2][yc][zc], t);
+                const int j = 2 * J + yc;
+                const int k = z2 ? 2 * K + zc : K;
+                const int base = F.n0 * (j + F.n1 * k) + 2 * I;
+                F.e[base] += v0;
+                F.e[base + 1] += v1;
+            }
+        }
+    }
+    __syncthreads();
+}
+
+}  // namespace
+
+template <typename T>
+__global__ void __launch_bounds__(kTailThreads)
+k_tail(TailParams<T> P) {
+    extern __shared__ __align__(16) unsigned char tail_smem[];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int nl = P.nlev;   // non-bottom tail levels
+    TailLevel<T> L[kTailMaxLevels];
+    // carve shared memory: per non-bottom level 7 arrays of T, then the bottom's 14 N doubles
+    size_t off = 0;
+    for (int l = 0; l < nl; ++l) {
+        const int N = P.lev[l].ncell;
+        T* base = reinterpret_cast<T*>(tail_smem + off);
+        L[l].n0 = P.lev[l].n0;
+        L[l].n1 = P.lev[l].n1;
+        L[l].n2 = P.lev[l].n2;
+        L[l].N = N;
+        L[l].rz = P.lev[l].rz;
+        L[l].e = base;
+        L[l].f = base + N;
+        L[l].bx = base + 2 * N;
+        L[l].by = base + 3 * N;
+        L[l].bz = base + 4 * N;
+        L[l].dg = base + 5 * N;
+        L[l].idg = base + 6 * N;
+        off += ((size_t)7 * N * sizeof(T) + 15) & ~(size_t)15;
+    }
+    double* bsm = reinterpret_cast<double*>(tail_smem + off);
+    const Dims BD = P.bottom;
+    const int NB = BD.ncell;
+    // load the operators (split layout in global memory -> natural in shared memory)
+    for (int l = 0; l < nl; ++l) {
+        const Dims& D = P.lev[l];
+        for (int c = tid; c < L[l].N; c += nt) {
+            int i, j, k;
+            decode(c, D.n0, D.n1, i, j, k);
+            const int g = level_index(D, i, j, k);
+            L[l].bx[c] = P.bx[l][g];
+            L[l].by[c] = P.by[l][g];
+            L[l].bz[c] = P.bz[l][g];
+            L[l].dg[c] = P.dg[l][g];
+            L[l].idg[c] = P.idg[l][g];
+            L[l].e[c] = T(0);
+            if (l == 0) L[l].f[c] = P.f0[g];
+        }
+    }
+    BotView v;
+    v.n0 = BD.n0;
+    v.n1 = BD.n1;
+    v.n2 = BD.n2;
+    v.N = NB;
+    double* ops = bsm;
+    for (int c = tid; c < NB; c += nt) {
+        ops[c] = P.bbx[c];
+        ops[NB + c] = P.bby[c];
+        ops[2 * NB + c] = P.bbz[c];
+        ops[3 * NB + c] = P.bdg[c];
+        ops[4 * NB + c] = P.bidg[c];
+    }
+    v.bx = ops;
+    v.by = ops + NB;
+    v.bz = ops + 2 * NB;
+    v.dg = ops + 3 * NB;
+    v.idg = ops + 4 * NB;
+    double* xb = bsm + 5 * NB;
+    double* fb = bsm + 6 * NB;
+    double* wb = bsm + 7 * NB;
+    __syncthreads();
+    // down the V
+    for (int l = 0; l < nl; ++l) {
+        for (int s = 0; s < P.nu1; ++s) tail_sweep<T>(L[l]);
+        if (l + 1 < nl) {
+            tail_restrict<T, T>(L[l], L[l + 1].n0, L[l + 1].n1, L[l + 1].n2, L[l + 1].f, P.nu1 > 0);
+        } else {
+            tail_restrict<T, double>(L[l], BD.n0, BD.n1, BD.n2, fb, P.nu1 > 0);
+        }
+    }
+    // bottom: one warp, FP64 (input rhs rounded through T as in the multi-kernel path)
+    for (int c = tid; c < NB; c += nt) xb[c] = 0.0;
+    __syncthreads();
+    int count = 0;
+    __shared__ double sm_red[33];
+    if (tid < 128)
+        count = bottom_body<Sync128<true>>(v, xb, fb, wb, sm_red, P.singular, P.nub, P.bottom_eps,
+                                           P.bottom_max_iter);
+    __syncthreads();
+    // the bottom solution is handed up as T, like the multi-kernel path's bottom output
+    T* eb = reinterpret_cast<T*>(wb);
+    for (int c = tid; c < NB; c += nt) eb[c] = (T)xb[c];
+    __syncthreads();
+    // up the V
+    for (int l = nl - 1; l >= 0; --l) {
+        if (l + 1 < nl)
+            tail_prolong<T>(L[l], L[l + 1].e, L[l + 1].n0, L[l + 1].n1, L[l + 1].n2, P.bc);
+        else
+            tail_prolong<T>(L[l], eb, BD.n0, BD.n1, BD.n2, P.bc);
+        for (int s = 0; s < P.nu2; ++s) tail_sweep<T>(L[l]);
+    }
+    // hand the correction of the first tail level back (its split layout)
+    const Dims& D0 = P.lev[0];
+    for (int c = tid; c < L[0].N; c += nt) {
+        int i, j, k;
+        decode(c, D0.n0, D0.n1, i, j, k);
+        P.e0[level_index(D0, i, j, k)] = L[0].e[c];
+    }
+    if (tid == 0 && P.iters) atomicAdd(P.iters, count);
+}
+
+template <typename T>
+size_t tail_smem_bytes(const Dims* lev, int nl, const Dims& bottom) {
+    size_t off = 0;
+    for (int l = 0; l < nl; ++l) off += ((size_t)7 * lev[l].ncell * sizeof(T) + 15) & ~(size_t)15;
+    return off + (size_t)14 * bottom.ncell * sizeof(double);
+}
+
+template <typename T>
+void launch_tail(const TailParams<T>& P, size_t smem, cudaStream_t s) {
+    k_tail<T><<<1, kTailThreads, smem, s>>>(P);
+}
+
+int prepare_tail_kernels() {
+    if (cudaFuncSetAttribute(k_tail<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmemMax) != cudaSuccess ||
+        cudaFuncSetAttribute(k_tail<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmemMax) != cudaSuccess) {
+        cudaGetLastError();
+        return MAC_ERR_CUDA;
+    }
+    return MAC_OK;
+}
+
+template size_t tail_smem_bytes<float>(const Dims*, int, const Dims&);
+template size_t tail_smem_bytes<double>(const Dims*, int, const Dims&);
+template void launch_tail<float>(const TailParams<float>&, size_t, cudaStream_t);
+template void launch_tail<double>(const TailParams<double>&, size_t, cudaStream_t);
+
+}  // namespace mac

@@ -144,6 +144,27 @@ def test_tight_tolerance_agreement(cuda_lib, precision):
     assert u_rel_err(u, u_o) <= 1e-11
 
 
+@pytest.mark.parametrize("name", ["strat64_b32", "stiff48_b16"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_coarse_tail_is_bitwise_identical(cuda_lib, name, precision):
+    # the single-CTA tail of the V-cycle runs the same arithmetic as the per-level kernels
+    c = build3d(name)
+    u1, phi1, st1 = gpu_project(c, precision, coarse_tail=1)
+    u0, phi0, st0 = gpu_project(c, precision, coarse_tail=0)
+    np.testing.assert_array_equal(phi1, phi0)
+    for a, b in zip(u1, u0):
+        np.testing.assert_array_equal(a, b)
+    assert st1["vcycles"] == st0["vcycles"] and st1["launches"] <= st0["launches"]
+
+
+def test_coarse_tail_2d(cuda_lib):
+    from maestro_gb300.inputs import config_case
+    c = config_case("2d_128", seed=7)
+    u1, phi1, st1 = gpu_project(c, "mixed", coarse_tail=1)
+    u0, phi0, st0 = gpu_project(c, "mixed", coarse_tail=0)
+    np.testing.assert_array_equal(phi1, phi0)
+
+
 def test_alt_energy_fix_3d(cuda_lib):
     c = build3d("contrast32_b16")
     u_o, phi_o, _ = oracle_project(c, alt=True)
@@ -168,7 +189,20 @@ def test_no_beta0_no_rhs_unit_test_form(cuda_lib):
     assert u_rel_err(ub, uo) <= 1e-9
 
 
-def test_mac_multigrid_helmholtz_matches_oracle(cuda_lib):
+@pytest.mark.parametrize("inner", [1, 2, 3])
+def test_mixed_inner_vcycles(cuda_lib, inner):
+    # mixed precision with 1, 2 or 3 FP32 V-cycles per FP64 refinement step
+    c = build3d("stiff48_b16")
+    u_o, phi_o, st_o = oracle_project(c)
+    u, phi, st = gpu_project(c, "mixed", inner_vcycles=inner)
+    assert st["status"] == 0 and st["rel_resid"] <= 1e-10
+    assert true_rel_resid(c, phi) <= 1.5e-10
+    assert phi_rel_err(phi, phi_o) <= 1e-8 and u_rel_err(u, u_o) <= 1e-8
+    assert st["refine_iters"] * inner >= st_o["vcycles"] - 1
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_mac_multigrid_helmholtz_matches_oracle(cuda_lib, precision):
     # thermal-diffusion form: (alpha - div beta grad) phi = rh with alpha = rho != 0
     c = make_case(dm=3, n=(32, 32, 32), box=(16, 16, 16), kmax=4, seed=31)
     beta = O.mac_coeffs(c.rho, c.dx, c.bc_lo, c.bc_hi, c.beta0, c.beta0_edge)
@@ -178,7 +212,7 @@ def test_mac_multigrid_helmholtz_matches_oracle(cuda_lib):
                                   alpha=alpha, nlevels=O.nlevels_for_boxes([c.box]))
     lay = Layout.tiled(c.n, c.box)
     per = [b == BC_PER for b in c.bc_lo]
-    P = MacProjector(lay, c.dx, BcTower(c.bc_lo, c.bc_hi))
+    P = MacProjector(lay, c.dx, BcTower(c.bc_lo, c.bc_hi), precision=precision)
     try:
         fphi = lay.to_fabs(np.zeros(c.n), ng=1)
         st = P.mac_multigrid(lay.to_fabs(rh, ng=0),
@@ -190,7 +224,7 @@ def test_mac_multigrid_helmholtz_matches_oracle(cuda_lib):
         P.close()
     phi = lay.from_fabs(fphi, ng=1)
     assert st["status"] == 0 and st["rel_resid"] <= 1e-10
-    assert rel_err(phi, phi_o) <= 1e-9
+    assert rel_err(phi, phi_o) <= (1e-9 if precision == "fp64" else 1e-8)
 
 
 def test_repeat_calls_bitwise_identical(cuda_lib):
