@@ -50,8 +50,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--seed", type=int, default=1234)
-    ap.add_argument("--inner", type=int, default=3,
-                    help="mixed precision: FP32 V-cycles per FP64 refinement step")
+    ap.add_argument("--inner", type=int, default=4,
+                    help="mixed precision: most FP32 V-cycles per FP64 refinement step")
+    ap.add_argument("--fixed-inner", action="store_true",
+                    help="mixed precision: always --inner V-cycles per step (no adaptive count)")
     return ap.parse_args()
 
 
@@ -229,7 +231,7 @@ def main():
 
     def timed_run(precision, timing):
         P = MacProjector(lay, c.dx, bc, precision=precision, stream=stream.cuda_stream,
-                         timing=int(timing), inner_vcycles=args.inner)
+                         timing=int(timing), inner_vcycles=args.inner, adaptive_inner=int(not args.fixed_inner))
         reset_inputs()
         stats = []
 
@@ -267,7 +269,7 @@ def main():
     # error of the mixed result against the FP64 GPU solve of the same inputs (last step)
     reset_inputs()
     Pm = MacProjector(lay, c.dx, bc, precision="mixed", stream=stream.cuda_stream,
-                      inner_vcycles=args.inner)
+                      inner_vcycles=args.inner, adaptive_inner=int(not args.fixed_inner))
     Pd = MacProjector(lay, c.dx, bc, precision="fp64", stream=stream.cuda_stream)
     ua, pa = work_u[0], work_phi[0]
     ub, pb = work_u[1], work_phi[1]
@@ -346,7 +348,7 @@ def main():
         E = args.e2e_steps
         sets = [fab_set() for _ in range(E + 1)]
         P = MacProjector(lay, c.dx, bc, precision="mixed", stream=stream.cuda_stream,
-                         inner_vcycles=args.inner)
+                         inner_vcycles=args.inner, adaptive_inner=int(not args.fixed_inner))
         nbytes = lambda lst: sum(x.nbytes for x in lst)  # noqa: E731
         s0 = sets[0]
         u_bytes = sum(nbytes(s0[1][d]) for d in range(c.dm))
@@ -392,7 +394,8 @@ def main():
                  "vcycles": st_fp64[-1]["vcycles"], "rel_resid": st_fp64[-1]["rel_resid"]},
         "mixed_over_fp64": value / fp64_value,
         "mixed": {"refine_iters": st_mixed[-1]["refine_iters"], "inner_vcycles": args.inner,
-                  "vcycles": st_mixed[-1]["refine_iters"] * args.inner, "rel_resid": rr,
+                  "adaptive_inner": not args.fixed_inner,
+                  "vcycles": st_mixed[-1]["vcycles"], "rel_resid": rr,
                   "phi_err_vs_fp64": phi_err, "u_err_vs_fp64": u_err,
                   "ms_by_class": cls_ms},
         "roofline": roofline,

@@ -91,9 +91,14 @@ typedef struct mac_opts {
     int timing;             /* 1: CUDA-event timing of the finest-level kernel classes into
                                mac_stats.ktime_* (events recorded inside the V-cycle graph)    */
     int inner_vcycles;      /* mixed precision: FP32 V-cycles per FP64 refinement step (>= 1;
-                               default 3); the FP64 residual is formed once per step           */
+                               default 4; the most per step when adaptive_inner is on); the
+                               FP64 residual is formed once per step                          */
     int coarse_tail;        /* 1 (default): the levels small enough for shared memory and the
                                bottom solve run as one single-CTA kernel (same arithmetic)     */
+    int adaptive_inner;     /* mixed precision, 1 (default): after each step the next step runs
+                               only as many inner V-cycles (<= inner_vcycles) as the contraction
+                               just observed predicts the tolerance needs; 0: always
+                               inner_vcycles                                                   */
 } mac_opts;
 
 /* Kernel classes of mac_stats.ktime_* (finest level unless stated). */
@@ -109,7 +114,7 @@ typedef struct mac_opts {
 
 typedef struct mac_stats {
     int status;             /* return code of the call                                         */
-    int vcycles;            /* V-cycles run (mixed: equal to refine_iters)                      */
+    int vcycles;            /* V-cycles run (mixed: FP32 V-cycles summed over the steps)       */
     int refine_iters;       /* FP64 refinement iterations (mixed precision), else 0            */
     int nlevels;            /* MG levels used                                                  */
     int bottom_iters;       /* BiCGStab iterations summed over the solve                        */

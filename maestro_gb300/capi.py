@@ -68,6 +68,7 @@ class MacOpts(ctypes.Structure):
         ("timing", ctypes.c_int),
         ("inner_vcycles", ctypes.c_int),
         ("coarse_tail", ctypes.c_int),
+        ("adaptive_inner", ctypes.c_int),
     ]
 
 

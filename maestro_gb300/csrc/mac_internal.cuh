@@ -153,6 +153,8 @@ struct BoxDesc {   // one fab of the caller's layout (device copy of the table)
 
 }  // namespace mac
 
+constexpr int kInnerGraphs = 8;   // mixed-precision steps of up to 8 inner V-cycles are graphed
+
 struct mac_ctx {
     mac_geom g{};
     mac_opts o{};
@@ -192,9 +194,11 @@ struct mac_ctx {
     mac::Reduce red;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
-    // CUDA graphs of one V-cycle (fp64 and fp32 inner) and their kernel-node counts
-    cudaGraphExec_t vc_exec[2] = {nullptr, nullptr};
-    long long graph_kernels[2] = {0, 0};
+    // CUDA graphs of one outer iteration and their kernel-node counts: slot 0 the FP64 V-cycle,
+    // slot v (1..kInnerGraphs) a mixed-precision step with v inner FP32 V-cycles
+    cudaGraphExec_t vc_exec[kInnerGraphs + 1] = {};
+    long long graph_kernels[kInnerGraphs + 1] = {};
+    int cur_inner = 1;   // inner V-cycles of the next mixed-precision refinement step
     long long issued = 0;                         // kernels launched (host count)
     cudaEvent_t tev[4][8] = {};                   // timing events of up to 4 V-cycles per iteration
     cudaEvent_t tail[3] = {};                     // before/after accumulation, after the residual

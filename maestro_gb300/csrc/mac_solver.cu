@@ -8,6 +8,7 @@
 //           FP64 bottom solve; phi += e in FP64; r = f - L phi in FP64 } until converged.
 // Every V-cycle (with its convergence residual) is captured once into a CUDA graph and replayed;
 // the host reads one 8-byte max-norm per cycle.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -195,7 +196,11 @@ void vcycle(mac_ctx* c, int l) {
 }
 
 int inner_cycles(const mac_ctx* c, int prec) {
-    return prec == MAC_PREC_FP64 ? 1 : (c->o.inner_vcycles > 1 ? c->o.inner_vcycles : 1);
+    return prec == MAC_PREC_FP64 ? 1 : (c->cur_inner > 1 ? c->cur_inner : 1);
+}
+
+int graph_slot(const mac_ctx* c, int prec) {
+    return prec == MAC_PREC_FP64 ? 0 : inner_cycles(c, prec);
 }
 
 // One iteration of the outer loop, ending with the max-norm of the fine residual in
@@ -261,7 +266,7 @@ void collect_timing(mac_ctx* c, int prec) {
 }
 
 int get_iteration_exec(mac_ctx* c, int prec, cudaGraphExec_t* out) {
-    const int slot = prec == MAC_PREC_FP64 ? 0 : 1;
+    const int slot = graph_slot(c, prec);
     if (c->vc_exec[slot]) {
         *out = c->vc_exec[slot];
         return MAC_OK;
@@ -283,7 +288,7 @@ int get_iteration_exec(mac_ctx* c, int prec, cudaGraphExec_t* out) {
 }
 
 void drop_graphs(mac_ctx* c) {
-    for (int s = 0; s < 2; ++s)
+    for (int s = 0; s <= kInnerGraphs; ++s)
         if (c->vc_exec[s]) {
             cudaGraphExecDestroy(c->vc_exec[s]);
             c->vc_exec[s] = nullptr;
@@ -291,12 +296,12 @@ void drop_graphs(mac_ctx* c) {
 }
 
 int run_iteration(mac_ctx* c, int prec, double* res_out) {
-    if (c->o.use_graph) {
+    if (c->o.use_graph && graph_slot(c, prec) <= kInnerGraphs) {
         cudaGraphExec_t ex;
         int rc = get_iteration_exec(c, prec, &ex);
         if (rc) return rc;
         MAC_CUDA_TRY(cudaGraphLaunch(ex, c->stream));
-        c->issued += c->graph_kernels[prec == MAC_PREC_FP64 ? 0 : 1];
+        c->issued += c->graph_kernels[graph_slot(c, prec)];
     } else {
         issue_iteration(c, prec);
         MAC_CUDA_TRY(cudaGetLastError());
@@ -308,6 +313,19 @@ int run_iteration(mac_ctx* c, int prec, double* res_out) {
 }
 
 }  // namespace
+
+// Inner V-cycles of the next mixed-precision refinement step: the per-V-cycle contraction seen
+// in the step just run, r_new / r_old = rate^nv, taken a little pessimistically (rate^0.85),
+// predicts how many V-cycles reach the target; at least 1, at most inner_max.
+int next_inner(double r_old, double r_new, int nv, double target, int inner_max) {
+    if (!(r_new > 0.0) || !(r_old > 0.0) || r_new >= r_old || target <= 0.0) return inner_max;
+    const double log_rate = 0.85 * std::log(r_new / r_old) / nv;   // < 0
+    const double need = std::log(target / r_new);                  // < 0 when not converged
+    if (need >= 0.0) return 1;
+    const double m = std::ceil(need / log_rate - 1e-9);
+    if (!(m < inner_max)) return inner_max;
+    return m < 1.0 ? 1 : (int)m;
+}
 
 // Multigrid solve on level 0 with f, coefficients and phi (level-0 layout) already in place.
 // red.scalars[1] holds ||f||_inf (after mean removal).
@@ -351,19 +369,27 @@ int run_solve(mac_ctx* c, mac_stats* st) {
     double res = bits_to_double(*c->red.h_maxbits);
     st->resid0 = res;
     if (!std::isfinite(res)) return MAC_ERR_NONFINITE;
-    int it = 0;
+    int it = 0, nv_total = 0;
+    const int inner_max = o.inner_vcycles > 1 ? o.inner_vcycles : 1;
+    const double target = std::max(o.rel_eps * fnorm, o.abs_eps > 0.0 ? o.abs_eps : 0.0);
+    c->cur_inner = inner_max;
     while (!converged(res) && it < o.max_vcycles) {
+        const double res_prev = res;
+        const int nv = inner_cycles(c, prec);
         int rc = run_iteration(c, prec, &res);
         if (rc) return rc;
         ++it;
+        nv_total += nv;
         if (st->nhist < 64) st->hist[st->nhist++] = res / fnorm;
         if (!std::isfinite(res)) {
-            st->vcycles = it;
+            st->vcycles = nv_total;
             st->rel_resid = res / fnorm;
             return MAC_ERR_NONFINITE;
         }
+        if (prec == MAC_PREC_MIXED && o.adaptive_inner)
+            c->cur_inner = next_inner(res_prev, res, nv, target, inner_max);
     }
-    st->vcycles = it;
+    st->vcycles = nv_total;
     st->refine_iters = prec == MAC_PREC_MIXED ? it : 0;
     st->rel_resid = res / fnorm;
     MAC_CUDA_TRY(cudaMemcpyAsync(c->red.h_counters, c->red.counters, sizeof(int),
@@ -698,8 +724,9 @@ void mac_default_opts(mac_opts* o) {
     o->use_graph = 1;
     o->verbose = 0;
     o->timing = 0;
-    o->inner_vcycles = 3;
+    o->inner_vcycles = 4;
     o->coarse_tail = 1;
+    o->adaptive_inner = 1;
 }
 
 const char* mac_strerror(int code) {

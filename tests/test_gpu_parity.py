@@ -189,16 +189,21 @@ def test_no_beta0_no_rhs_unit_test_form(cuda_lib):
     assert u_rel_err(ub, uo) <= 1e-9
 
 
-@pytest.mark.parametrize("inner", [1, 2, 3])
-def test_mixed_inner_vcycles(cuda_lib, inner):
-    # mixed precision with 1, 2 or 3 FP32 V-cycles per FP64 refinement step
+@pytest.mark.parametrize("adaptive", [0, 1])
+@pytest.mark.parametrize("inner", [1, 2, 3, 4, 6])
+def test_mixed_inner_vcycles(cuda_lib, inner, adaptive):
+    # mixed precision with up to 1..6 FP32 V-cycles per FP64 refinement step, fixed or adaptive
     c = build3d("stiff48_b16")
     u_o, phi_o, st_o = oracle_project(c)
-    u, phi, st = gpu_project(c, "mixed", inner_vcycles=inner)
+    u, phi, st = gpu_project(c, "mixed", inner_vcycles=inner, adaptive_inner=adaptive)
     assert st["status"] == 0 and st["rel_resid"] <= 1e-10
     assert true_rel_resid(c, phi) <= 1.5e-10
     assert phi_rel_err(phi, phi_o) <= 1e-8 and u_rel_err(u, u_o) <= 1e-8
-    assert st["refine_iters"] * inner >= st_o["vcycles"] - 1
+    assert st["vcycles"] >= st_o["vcycles"] - 1
+    if adaptive:
+        assert st["refine_iters"] <= st["vcycles"] <= st["refine_iters"] * inner
+    else:
+        assert st["vcycles"] == st["refine_iters"] * inner
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
