@@ -38,6 +38,7 @@ extern "C" {
 #define MAC_ERR_UNSUPPORTED   -6   /* geometry the solver does not handle (see mac_strerror)   */
 #define MAC_ERR_BAD_DENSITY   -7   /* rho <= 0 or non-finite (face coefficients undefined)     */
 #define MAC_ERR_TOO_LARGE     -8   /* size above a fixed limit of the entry point              */
+#define MAC_ERR_DEVICE_TIMEOUT -9  /* a kernel's bounded wait for its own async copies expired  */
 
 /* ---- boundary codes: FBoxLib bc_module numbering of ell_bc_level_array(...,press_comp) ---- */
 #define MAC_BC_PER  -1   /* periodic                                       */

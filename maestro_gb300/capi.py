@@ -20,6 +20,7 @@ MAC_ERR_ALLOC = -5
 MAC_ERR_UNSUPPORTED = -6
 MAC_ERR_BAD_DENSITY = -7
 MAC_ERR_TOO_LARGE = -8
+MAC_ERR_DEVICE_TIMEOUT = -9
 
 MAC_BC_PER, MAC_BC_INT, MAC_BC_DIR, MAC_BC_NEU = -1, 0, 1, 2
 MAC_PREC_FP64, MAC_PREC_MIXED = 0, 1

@@ -151,6 +151,31 @@ struct BoxDesc {   // one fab of the caller's layout (device copy of the table)
     int comp_off;  // offset of the component inside the fab, in elements
 };
 
+// Finest-level FP32 kernels with face coefficients computed from rho32 (mixed precision).
+// Per-layer FP32 face factors beta0_f^p * 2 / h_d^2 (tables of nr+1 floats, vertical index r):
+//   0: x faces; 1: y faces (3-D: horizontal; 2-D: unused); 2: low vertical face of layer r,
+//   3: high vertical face of layer r -- both zero where the face is a non-periodic wall;
+//   4: Dirichlet diagonal term of layer r (wall factor of the vertical walls touching it).
+constexpr int kOtfTables = 5;
+struct OtfParams {
+    int n[3];
+    int per[3];
+    int dlo[3], dhi[3];   // Dirichlet flags
+    int has_dir;          // any Dirichlet face
+    int va;
+    int dm;
+    const float* fac;     // kOtfTables tables of (n[va] + 1)
+    const float* rho;     // level-0 layout
+    // staged 3-D half-sweep (rows of whole colour-half planes copied to shared memory by bulk
+    // async copies); ty == 0: not applicable, the per-cell kernel runs instead
+    int ty;               // rows of a tile
+    int zc, nz;           // planes per block, blocks along z
+    int smem;             // dynamic shared memory bytes
+    int* err;             // device flag: a bounded wait on a copy gave up
+};
+// Tile plan of the staged half-sweep for the finest level (OtfParams.ty/zc/nz/smem).
+void plan_otf_tile(const Dims& d, int dm, int sms, OtfParams& P);
+
 }  // namespace mac
 
 constexpr int kInnerGraphs = 8;   // mixed-precision steps of up to 8 inner V-cycles are graphed
@@ -199,6 +224,8 @@ struct mac_ctx {
     cudaGraphExec_t vc_exec[kInnerGraphs + 1] = {};
     long long graph_kernels[kInnerGraphs + 1] = {};
     int cur_inner = 1;   // inner V-cycles of the next mixed-precision refinement step
+    int sms = 0;         // SM count of the device
+    mac::OtfParams otf_tile;  // tile plan of the staged finest-level half-sweep (ty/zc/nz/smem)
     long long issued = 0;                         // kernels launched (host count)
     cudaEvent_t tev[4][8] = {};                   // timing events of up to 4 V-cycles per iteration
     cudaEvent_t tail[3] = {};                     // before/after accumulation, after the residual
@@ -234,22 +261,7 @@ void launch_resid_norm(const Dims& d, const LevelArrays<T>& a, bool red_only,
 void launch_resid64_to32(const Dims& d, const LevelArrays<double>& a, float* r32,
                          unsigned long long* maxbits, cudaStream_t s);
 void launch_accumulate(const Dims& d, double* phi, const float* e, cudaStream_t s);
-// Finest-level FP32 kernels with face coefficients computed from rho32 (mixed precision).
-// Per-layer FP32 face factors beta0_f^p * 2 / h_d^2 (tables of nr+1 floats, vertical index r):
-//   0: x faces; 1: y faces (3-D: horizontal; 2-D: unused); 2: low vertical face of layer r,
-//   3: high vertical face of layer r -- both zero where the face is a non-periodic wall;
-//   4: Dirichlet diagonal term of layer r (wall factor of the vertical walls touching it).
-constexpr int kOtfTables = 5;
-struct OtfParams {
-    int n[3];
-    int per[3];
-    int dlo[3], dhi[3];   // Dirichlet flags
-    int has_dir;          // any Dirichlet face
-    int va;
-    int dm;
-    const float* fac;     // kOtfTables tables of (n[va] + 1)
-    const float* rho;     // level-0 layout
-};
+
 void launch_gsrb_otf(const Dims& d, const OtfParams& P, int colour, float* e, const float* r,
                      cudaStream_t s);
 void launch_resid_restrict_otf(const Dims& fine, const Dims& coarse, const OtfParams& P,

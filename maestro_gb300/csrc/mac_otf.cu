@@ -7,6 +7,9 @@
 // inner (FP32) V-cycle uses these; the FP64 refinement residual keeps the stored FP64 operator.
 #include "mac_internal.cuh"
 
+#include <algorithm>
+#include <mutex>
+
 namespace mac {
 namespace {
 
@@ -118,6 +121,292 @@ k_gsrb_otf(Dims d, OtfParams P, int colour, float* __restrict__ es, const float*
     es[q] = acc * rcp_approx(diag);
 }
 
+// ---- staged 3-D half-sweep -------------------------------------------------------------------
+// A block owns a tile of all hn0 colour-half columns x ty rows and marches through zc planes.
+// Per plane, one thread issues bulk async copies (cp.async.bulk, completion counted on an
+// mbarrier) of the other colour's e and rho on rows j0-1 .. j0+ty (wrapped) and the own colour's
+// r and rho on rows j0 .. j0+ty-1 into a ring of kStages shared-memory stages, up to
+// kStages - 1 planes ahead of the plane being updated.  Per plane, thread 0 waits on the
+// mbarrier of the next plane and one block barrier publishes it to the other threads (they do
+// not poll) and frees the stage read last for the next copy.  Each thread updates 4 consecutive
+// own cells of one row (float4 reads of the stage); the other colour's centre row of planes
+// k-1 / k / k+1 is carried in registers.  Arithmetic per cell is that of otf_cell, in the same
+// order (the x-parity and the Dirichlet terms resolved at compile time).  Every wait is bounded
+// (about one second of %globaltimer); on expiry the block records the failure in P.err, waits
+// (bounded) for the copies it issued and leaves.  4 ring stages at 256^3 (ty = 8): 72 KB of
+// shared memory and 80 registers a thread, 3 blocks per SM.
+constexpr int kStages = 4;          // planes in the shared-memory ring
+constexpr int kCellsPerThread = 4;  // consecutive colour-half columns (one float4) per thread
+constexpr unsigned long long kWaitNs = 1000000000ull;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,
+                                         uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(dst), "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Wait for phase `parity` of the mbarrier; false after about kWaitNs without completion.
+__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (unsigned n = 1;; ++n) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((n & 63u) == 0 && global_ns() - t0 > kWaitNs) return false;
+    }
+}
+
+template <int V>
+struct FV {
+    float v[V];
+};
+template <int V>
+__device__ __forceinline__ FV<V> ldv(const float* p) {
+    FV<V> r;
+    if constexpr (V == 4) {
+        const float4 t = *reinterpret_cast<const float4*>(p);
+        r.v[0] = t.x; r.v[1] = t.y; r.v[2] = t.z; r.v[3] = t.w;
+    } else {
+        const float2 t = *reinterpret_cast<const float2*>(p);
+        r.v[0] = t.x; r.v[1] = t.y;
+    }
+    return r;
+}
+template <int V>
+__device__ __forceinline__ void stv(float* p, const float* v) {
+    if constexpr (V == 4)
+        *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    else
+        *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+}
+
+// Updates V consecutive own cells of one row (colour-half columns c0 .. c0+V-1) whose x-parity
+// is SP (i = 2 (c0 + m) + SP); ex/rx = the other colour's value at the column just outside the
+// group on the side SP selects (c0 - 1 for SP = 0, c0 + V for SP = 1).  fxl0 / fxhV: x factors
+// of the group's outer low / high faces (zero on a non-periodic wall); wx0 / wxV / wmid: the
+// Dirichlet diagonal factors of the first, last and inner cells (DIR only).
+template <int V, int SP, bool DIR>
+__device__ __forceinline__ void update_group(float ex, float rx, const FV<V>& Ec, const FV<V>& Rc,
+                                             const FV<V>& Eb, const FV<V>& Rb, const FV<V>& Ea,
+                                             const FV<V>& Ra, const FV<V>& Eym, const FV<V>& Rym,
+                                             const FV<V>& Eyp, const FV<V>& Ryp, const FV<V>& Fo,
+                                             const FV<V>& Ro, float fx, float fxl0, float fxhV,
+                                             float fyl, float fyh, float fzl, float fzh,
+                                             float wx0, float wxV, float wmid, float* out) {
+#pragma unroll
+    for (int m = 0; m < V; ++m) {
+        const float rc = Ro.v[m];
+        float el, rl, eh, rh, fl, fh;
+        if (SP == 0) {
+            el = m == 0 ? ex : Ec.v[m - 1];
+            rl = m == 0 ? rx : Rc.v[m - 1];
+            eh = Ec.v[m];
+            rh = Rc.v[m];
+            fl = m == 0 ? fxl0 : fx;
+            fh = fx;
+        } else {
+            el = Ec.v[m];
+            rl = Rc.v[m];
+            eh = m == V - 1 ? ex : Ec.v[m + 1];
+            rh = m == V - 1 ? rx : Rc.v[m + 1];
+            fl = fx;
+            fh = m == V - 1 ? fxhV : fx;
+        }
+        float acc = Fo.v[m];
+        float b = fl * rcp_approx(rc + rl);
+        acc = fmaf(b, el, acc);
+        float dg = b;
+        b = fh * rcp_approx(rc + rh);
+        acc = fmaf(b, eh, acc);
+        dg += b;
+        b = fyl * rcp_approx(rc + Rym.v[m]);
+        acc = fmaf(b, Eym.v[m], acc);
+        dg += b;
+        b = fyh * rcp_approx(rc + Ryp.v[m]);
+        acc = fmaf(b, Eyp.v[m], acc);
+        dg += b;
+        b = fzl * rcp_approx(rc + Rb.v[m]);
+        acc = fmaf(b, Eb.v[m], acc);
+        dg += b;
+        b = fzh * rcp_approx(rc + Ra.v[m]);
+        acc = fmaf(b, Ea.v[m], acc);
+        dg += b;
+        if (DIR) {
+            const float w = (SP == 0 && m == 0) ? wx0 : (SP == 1 && m == V - 1) ? wxV : wmid;
+            dg += w * rcp_approx(rc);
+        }
+        out[m] = acc * rcp_approx(dg);
+    }
+}
+
+template <bool DIR>
+__global__ void __launch_bounds__(256)
+k_gsrb_otf_staged(Dims d, OtfParams P, int colour, float* __restrict__ es,
+                  const float* __restrict__ eo, const float* __restrict__ rs,
+                  const float* __restrict__ rhos, const float* __restrict__ rhoo) {
+    constexpr int V = kCellsPerThread;
+    extern __shared__ __align__(128) float sm[];
+    __shared__ int abort_flag;
+    const int hn0 = d.hn0, n1 = d.n1, n2 = d.n2, TY = P.ty;
+    const int oth = (TY + 2) * hn0;    // floats of one other-colour array in a stage
+    const int own = TY * hn0;          // floats of one own-colour array in a stage
+    const int stage = 2 * oth + 2 * own;
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(sm + kStages * stage);
+    const int j0 = blockIdx.x * TY;
+    const int k0 = blockIdx.y * P.zc;
+    const int kend = min(k0 + P.zc, n2);
+    const int nq = kend - k0 + 2;      // planes k0-1 .. kend, local index q = p - (k0 - 1)
+    const long plane = (long)n1 * hn0;
+    const int t = threadIdx.x;
+    if (t == 0) {
+        for (int q = 0; q < kStages; ++q) mbar_init(smem_addr(&bars[q]), 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    // thread 0: copy plane q into stage q % kStages
+    auto issue = [&](int q) {
+        const int sidx = q % kStages;
+        int p = k0 - 1 + q;
+        p += (p < 0) ? n2 : 0;
+        p -= (p >= n2) ? n2 : 0;
+        float* st = sm + sidx * stage;
+        const uint32_t bar = smem_addr(&bars[sidx]);
+        mbar_expect_tx(bar, (uint32_t)stage * 4u);
+        const long pb = (long)p * plane;
+        int slot = 0;
+        while (slot < TY + 2) {
+            int row = j0 - 1 + slot;
+            row += (row < 0) ? n1 : 0;
+            row -= (row >= n1) ? n1 : 0;
+            const int len = min(TY + 2 - slot, n1 - row);
+            const uint32_t bytes = (uint32_t)(len * hn0) * 4u;
+            bulk_g2s(smem_addr(st + slot * hn0), eo + pb + (long)row * hn0, bytes, bar);
+            bulk_g2s(smem_addr(st + oth + slot * hn0), rhoo + pb + (long)row * hn0, bytes, bar);
+            slot += len;
+        }
+        bulk_g2s(smem_addr(st + 2 * oth), rs + pb + (long)j0 * hn0, (uint32_t)own * 4u, bar);
+        bulk_g2s(smem_addr(st + 2 * oth + own), rhos + pb + (long)j0 * hn0, (uint32_t)own * 4u,
+                 bar);
+    };
+    int issued = 0;      // planes issued so far (thread 0)
+    int confirmed = 0;   // planes whose copies thread 0 has seen complete
+    if (t == 0) {
+        for (; issued < min(kStages, nq); ++issued) issue(issued);
+    }
+    // thread 0 waits for plane q; the __syncthreads that follows every call publishes the
+    // stage (and a failed wait) to the other threads, which do not poll the barrier
+    auto wait_plane = [&](int q) {
+        if (t != 0 || abort_flag) return;
+        if (mbar_wait(smem_addr(&bars[q % kStages]), (uint32_t)((q / kStages) & 1))) {
+            confirmed = q + 1;
+        } else {
+            abort_flag = 1;
+            atomicExch(P.err, 1);
+        }
+    };
+
+    // this thread's V cells: row r of the tile, columns c0 .. c0+V-1
+    const int idx = V * t;
+    const int r = idx / hn0, c0 = idx - r * hn0;
+    const int j = j0 + r;
+    const int cm = (c0 == 0) ? hn0 - 1 : c0 - 1;          // column left of the group (wrapped)
+    const int cp = (c0 + V == hn0) ? 0 : c0 + V;          // column right of the group
+    const bool jl = j > 0 || P.per[1], jh = j < n1 - 1 || P.per[1];
+    // non-periodic x walls: the low face of i = 0 (c0 == 0, m == 0, s == 0) and the high face of
+    // i = n0 - 1 (c0 + V == hn0, m == V - 1, s == 1)
+    const bool wlo = !P.per[0] && c0 == 0, whi = !P.per[0] && c0 + V == hn0;
+    // Dirichlet walls touching the group: x low (first cell, s = 0), x high (last cell, s = 1),
+    // y (every cell of the row)
+    const bool dxl = P.dlo[0] && c0 == 0, dxh = P.dhi[0] && c0 + V == hn0;
+    const bool dy = (j == 0 && P.dlo[1]) || (j == n1 - 1 && P.dhi[1]);
+    const int st_n = n2 + 1;
+    const int ctr = (r + 1) * hn0 + c0;                    // centre row in an other-colour array
+
+    wait_plane(0);
+    wait_plane(1);
+    __syncthreads();
+    FV<V> Eb = ldv<V>(sm + ctr), Rb = ldv<V>(sm + oth + ctr);
+    FV<V> Ec = ldv<V>(sm + stage + ctr), Rc = ldv<V>(sm + stage + oth + ctr);
+    for (int k = k0; k < kend; ++k) {
+        const int q = k - k0 + 1;
+        wait_plane(q + 1);
+        // every thread is done with stage (q - 1) % kStages: refill it with plane q - 1 + kStages
+        __syncthreads();
+        if (abort_flag) break;
+        if (t == 0 && issued < nq) issue(issued++);
+        const float* sc = sm + (q % kStages) * stage;
+        const float* su = sm + ((q + 1) % kStages) * stage;
+        const FV<V> Ea = ldv<V>(su + ctr), Ra = ldv<V>(su + oth + ctr);
+        const int s = (colour + j + k) & 1;
+        const int cx = s ? cp : cm;
+        const float ex = sc[(r + 1) * hn0 + cx], rx = sc[oth + (r + 1) * hn0 + cx];
+        const FV<V> Eym = ldv<V>(sc + r * hn0 + c0), Rym = ldv<V>(sc + oth + r * hn0 + c0);
+        const FV<V> Eyp = ldv<V>(sc + (r + 2) * hn0 + c0), Ryp = ldv<V>(sc + oth + (r + 2) * hn0 + c0);
+        const FV<V> Fo = ldv<V>(sc + 2 * oth + r * hn0 + c0);
+        const FV<V> Ro = ldv<V>(sc + 2 * oth + own + r * hn0 + c0);
+        const float fx = P.fac[k], fy = P.fac[st_n + k];
+        const float fyl = jl ? fy : 0.f, fyh = jh ? fy : 0.f;
+        const float fzl = P.fac[2 * st_n + k], fzh = P.fac[3 * st_n + k];
+        const float fxl0 = wlo ? 0.f : fx, fxhV = whi ? 0.f : fx;
+        float out[V];
+        if (DIR) {
+            const float wmid = P.fac[4 * st_n + k] + (dy ? fy : 0.f);
+            const float wx0 = wmid + (dxl ? fx : 0.f), wxV = wmid + (dxh ? fx : 0.f);
+            if (s)
+                update_group<V, 1, true>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp, Ryp, Fo,
+                                         Ro, fx, fxl0, fxhV, fyl, fyh, fzl, fzh, wx0, wxV, wmid,
+                                         out);
+            else
+                update_group<V, 0, true>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp, Ryp, Fo,
+                                         Ro, fx, fxl0, fxhV, fyl, fyh, fzl, fzh, wx0, wxV, wmid,
+                                         out);
+        } else if (s) {
+            update_group<V, 1, false>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp, Ryp, Fo, Ro,
+                                      fx, fxl0, fxhV, fyl, fyh, fzl, fzh, 0.f, 0.f, 0.f, out);
+        } else {
+            update_group<V, 0, false>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp, Ryp, Fo, Ro,
+                                      fx, fxl0, fxhV, fyl, fyh, fzl, fzh, 0.f, 0.f, 0.f, out);
+        }
+        stv<V>(es + (long)k * plane + (long)j * hn0 + c0, out);
+        Eb = Ec;
+        Rb = Rc;
+        Ec = Ea;
+        Rc = Ra;
+    }
+    if (t == 0 && confirmed < issued) {
+        // a wait gave up: leave no copy in flight into this block's shared memory (bounded)
+        for (int q = confirmed; q < issued; ++q)
+            mbar_wait(smem_addr(&bars[q % kStages]), (uint32_t)((q / kStages) & 1));
+    }
+}
+
 template <int DM, bool RED_ONLY>
 __global__ void __launch_bounds__(kB)
 k_resid_restrict_otf(Dims F, Dims C, OtfParams P, const float* __restrict__ e,
@@ -161,12 +450,71 @@ void launch_gsrb_otf(const Dims& d, const OtfParams& P, int colour, float* e, co
                      cudaStream_t s) {
     const int own = colour * d.half, oth = (colour ^ 1) * d.half;
     const Grid3 g = grid3(d.hn0, d.n1, d.n2);
-    if (P.dm == 3)
+    if (P.dm == 3 && P.ty > 0) {
+        const dim3 grid(d.n1 / P.ty, P.nz);
+        const int nt = P.ty * d.hn0 / kCellsPerThread;
+        if (P.has_dir)
+            k_gsrb_otf_staged<true><<<grid, nt, P.smem, s>>>(d, P, colour, e + own, e + oth,
+                                                             r + own, P.rho + own, P.rho + oth);
+        else
+            k_gsrb_otf_staged<false><<<grid, nt, P.smem, s>>>(d, P, colour, e + own, e + oth,
+                                                              r + own, P.rho + own, P.rho + oth);
+    }
+    else if (P.dm == 3)
         k_gsrb_otf<3><<<g.grid, g.block, 0, s>>>(d, P, colour, e + own, e + oth, r + own,
                                                  P.rho + own, P.rho + oth);
     else
         k_gsrb_otf<2><<<g.grid, g.block, 0, s>>>(d, P, colour, e + own, e + oth, r + own,
                                                  P.rho + own, P.rho + oth);
+}
+
+// Tile plan of the staged half-sweep: ty = the largest power of two with ty * hn0 <= 1024 cells
+// that divides n1 (one float4 group of 4 cells per thread, at most 256 threads); whole rows of
+// 16-byte multiples (hn0 % 4 == 0); chunks of planes so that the blocks fill the resident slots
+// of every SM once.  Sets ty = 0 where the staged kernel does not apply.
+void plan_otf_tile(const Dims& d, int dm, int sms, OtfParams& P) {
+    static std::mutex mu;
+    static int smem_set = 0;
+    P.ty = P.zc = P.nz = P.smem = 0;
+    if (dm != 3 || !d.split || d.hn0 % 4 || d.hn0 > 1024 || d.n2 < 2) return;
+    int ty = 1;
+    while (2 * ty * d.hn0 <= 1024 && d.n1 % (2 * ty) == 0) ty *= 2;
+    const int nt = ty * d.hn0 / kCellsPerThread;
+    if (nt < 32 || nt % 32) return;
+    const int stage = (4 * ty + 4) * d.hn0;
+    const int smem = kStages * stage * 4 + kStages * 8;
+    if (smem > 200 * 1024) return;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (smem > smem_set) {
+            if (cudaFuncSetAttribute(k_gsrb_otf_staged<false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_gsrb_otf_staged<true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+                    cudaSuccess) {
+                cudaGetLastError();
+                return;
+            }
+            smem_set = smem;
+        }
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gsrb_otf_staged<false>, nt,
+                                                      smem) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return;
+    }
+    const long tiles = d.n1 / ty;
+    long chunks = ((long)sms * per_sm) / tiles;
+    if (chunks < 1) chunks = 1;
+    int zc = ceil_div(d.n2, (int)std::min<long>(chunks, d.n2));
+    if (zc < 4) zc = std::min(4, d.n2);
+    P.ty = ty;
+    P.zc = zc;
+    P.nz = ceil_div(d.n2, zc);
+    P.smem = smem;
 }
 
 void launch_resid_restrict_otf(const Dims& fine, const Dims& coarse, const OtfParams& P,

@@ -105,6 +105,11 @@ OtfParams otf_params(const mac_ctx* c) {
     P.dm = c->dm;
     P.fac = c->fac32;
     P.rho = c->rho32;
+    P.ty = c->otf_tile.ty;
+    P.zc = c->otf_tile.zc;
+    P.nz = c->otf_tile.nz;
+    P.smem = c->otf_tile.smem;
+    P.err = c->red.counters + 2;
     return P;
 }
 
@@ -392,10 +397,11 @@ int run_solve(mac_ctx* c, mac_stats* st) {
     st->vcycles = nv_total;
     st->refine_iters = prec == MAC_PREC_MIXED ? it : 0;
     st->rel_resid = res / fnorm;
-    MAC_CUDA_TRY(cudaMemcpyAsync(c->red.h_counters, c->red.counters, sizeof(int),
+    MAC_CUDA_TRY(cudaMemcpyAsync(c->red.h_counters, c->red.counters, 3 * sizeof(int),
                                  cudaMemcpyDeviceToHost, c->stream));
     MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
     st->bottom_iters = c->red.h_counters[0];
+    if (c->red.h_counters[2]) return MAC_ERR_DEVICE_TIMEOUT;
     return converged(res) ? MAC_OK : MAC_ERR_NOT_CONVERGED;
 }
 
@@ -557,6 +563,12 @@ int ctx_alloc(mac_ctx* c) {
     rc |= alloc_arr(c, &c->red.counters, 4);
     rc |= alloc_arr(c, &c->red.maxbits, 1);
     if (rc) return MAC_ERR_ALLOC;
+    {
+        int dev = 0;
+        MAC_CUDA_TRY(cudaGetDevice(&dev));
+        MAC_CUDA_TRY(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev));
+        plan_otf_tile(c->lev[0].d, c->dm, c->sms, c->otf_tile);
+    }
     MAC_CUDA_TRY(cudaMallocHost(&c->red.h_maxbits, sizeof(unsigned long long)));
     MAC_CUDA_TRY(cudaMallocHost(&c->red.h_scalars, 8 * sizeof(double)));
     MAC_CUDA_TRY(cudaMallocHost(&c->red.h_counters, 4 * sizeof(int)));
@@ -742,6 +754,8 @@ const char* mac_strerror(int code) {
                    "coarsest level must hold at most 65536 cells; at least two MG levels)";
         case MAC_ERR_BAD_DENSITY: return "density <= 0 or non-finite";
         case MAC_ERR_TOO_LARGE: return "size above the fixed limit of this entry point";
+        case MAC_ERR_DEVICE_TIMEOUT:
+            return "a kernel gave up waiting (about 1 s) for its own asynchronous copies";
         default: return "unknown status";
     }
 }
