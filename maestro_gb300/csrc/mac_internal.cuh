@@ -33,6 +33,7 @@ namespace mac {
 
 constexpr int kMaxLevels = 32;
 constexpr int kBottomMaxCells = 65536;   // single-CTA bottom solver limit
+constexpr int kBotScrPerCell = 18;       // bottom solver scratch: 14 doubles + 7 ints per cell
 
 #define MAC_CUDA_TRY(expr)                                   \
     do {                                                     \

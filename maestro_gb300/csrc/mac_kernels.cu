@@ -292,7 +292,7 @@ k_accumulate(int n, double* __restrict__ u, const float* __restrict__ e) {
 
 // ---- single-CTA FP64 bottom solver (natural layout): device code in mac_bottom.cuh -------------
 constexpr int kBottomThreads = 1024;
-constexpr int kBottomSmemCells = 1024;   // 14 doubles per cell: 114,688 B of shared memory
+constexpr int kBottomSmemCells = 1024;   // 7 + kBotScrPerCell doubles per cell: 204,800 B
 
 // SMEM: the five operator arrays and the nine work vectors live in dynamic shared memory
 // (levels of up to kBottomSmemCells cells, 128 threads), else in global scratch (1024 threads).
@@ -411,7 +411,7 @@ void launch_bottom(const Dims& d, const LevelArrays<double>& a64, Tio* x, const 
     v.idg = a64.invdiag;
     // small levels: 128 threads, operator and vectors in shared memory; large: one 1024-thread
     // CTA on global scratch
-    const size_t smem = (size_t)14 * d.ncell * sizeof(double);
+    const size_t smem = (size_t)(7 + kBotScrPerCell) * d.ncell * sizeof(double);
     if (d.ncell <= kBottomSmemCells)
         k_bottom<Tio, true><<<1, 128, smem, s>>>(v, x, f, scratch, singular ? 1 : 0, nub, eps,
                                                  max_iter, iter_counter);
@@ -423,7 +423,7 @@ void launch_bottom(const Dims& d, const LevelArrays<double>& a64, Tio* x, const 
 // Opt the shared-memory bottom solver into more than 48 KB of dynamic shared memory (called once
 // per context, outside any stream capture).
 int prepare_kernels() {
-    const int bytes = 14 * kBottomSmemCells * (int)sizeof(double);
+    const int bytes = (7 + kBotScrPerCell) * kBottomSmemCells * (int)sizeof(double);
     if (cudaFuncSetAttribute(k_bottom<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess ||
         cudaFuncSetAttribute(k_bottom<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) {
         cudaGetLastError();

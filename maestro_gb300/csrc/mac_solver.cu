@@ -540,7 +540,7 @@ int ctx_alloc(mac_ctx* c) {
             break;
         }
     }
-    rc |= alloc_arr(c, &c->bottom_scratch, (size_t)9 * B.d.ncell);
+    rc |= alloc_arr(c, &c->bottom_scratch, (size_t)(2 + kBotScrPerCell) * B.d.ncell);
     for (int d = 0; d < c->dm; ++d) {
         const size_t nf = (size_t)(c->n[0] + (d == 0)) * (c->n[1] + (d == 1)) * (c->n[2] + (d == 2));
         rc |= alloc_arr(c, &c->u[d], nf);

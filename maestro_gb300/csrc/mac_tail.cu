@@ -61,7 +61,7 @@ __device__ __forceinline__ Lanes lanes(int nx) {
 }
 
 template <typename T>
-__device__ void tail_sweep(const TailLevel<T>& L) {
+__device__ __noinline__ void tail_sweep(const TailLevel<T>& L) {
     const int hn0 = L.n0 >> 1, rows = L.n1 * L.n2;
     const Lanes q = lanes(hn0);
     for (int colour = 0; colour < 2; ++colour) {
@@ -90,7 +90,7 @@ __device__ void tail_sweep(const TailLevel<T>& L) {
 
 // defect of level F restricted into out[coarse natural index] (as T, then converted to To)
 template <typename T, typename To>
-__device__ void tail_restrict(const TailLevel<T>& F, int cn0, int cn1, int cn2, To* out,
+__device__ __noinline__ void tail_restrict(const TailLevel<T>& F, int cn0, int cn1, int cn2, To* out,
                               bool red_only) {
     const Lanes ln = lanes(cn0);
     const int rows = cn1 * cn2;
@@ -137,7 +137,7 @@ __device__ __forceinline__ void nb_w(int q, int n, int blo, int bhi, int& qm, in
 
 // e_fine += trilinear interpolation of the coarse correction ec (natural, cn0 x cn1 x cn2)
 template <typename T>
-__device__ void tail_prolong(const TailLevel<T>& F, const T* ec, int cn0, int cn1, int cn2,
+__device__ __noinline__ void tail_prolong(const TailLevel<T>& F, const T* ec, int cn0, int cn1, int cn2,
                              const BcDesc& bc) {
     const bool z2 = F.rz == 2;
     const Lanes ln = lanes(cn0);
@@ -191,6 +191,44 @@ __device__ void tail_prolong(const TailLevel<T>& F, const T* ec, int cn0, int cn
     __syncthreads();
 }
 
+// Asynchronous 4/8-byte global -> shared copy (cp.async); completed by cp_async_wait().
+template <typename T>
+__device__ __forceinline__ void cp_async(T* dst, const T* src) {
+    static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4 or 8 bytes");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(
+                     (unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src), "n"(sizeof(T))
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_all;" ::: "memory");
+}
+
+// Visit every cell of a checkerboard-split level once: fn(g, c) with g the split-layout
+// (global) index and c the natural (shared-memory) index; rows decoded incrementally, no
+// per-cell integer division.
+template <class Fn>
+__device__ __forceinline__ void for_split_cells(const Dims& D, Fn fn) {
+    const Lanes q = lanes(D.hn0);
+    if (q.ty >= q.RY) return;
+    const int rows = D.n1 * D.n2;
+    int j = q.ty % D.n1, k = q.ty / D.n1;
+    const int dj = q.RY % D.n1, dk = q.RY / D.n1;
+    for (int row = q.ty; row < rows; row += q.RY) {
+        for (int colour = 0; colour < 2; ++colour) {
+            const int s = (colour + j + k) & 1;
+            for (int h = q.tx; h < D.hn0; h += q.TX)
+                fn(colour * D.half + row * D.hn0 + h, 2 * h + s + D.n0 * row);
+        }
+        j += dj;
+        k += dk;
+        if (j >= D.n1) {
+            j -= D.n1;
+            ++k;
+        }
+    }
+}
+
 }  // namespace
 
 template <typename T>
@@ -200,7 +238,8 @@ k_tail(TailParams<T> P) {
     const int tid = threadIdx.x, nt = blockDim.x;
     const int nl = P.nlev;   // non-bottom tail levels
     TailLevel<T> L[kTailMaxLevels];
-    // carve shared memory: per non-bottom level 7 arrays of T, then the bottom's 14 N doubles
+    // carve shared memory: per non-bottom level 7 arrays of T, then the bottom's operator (5 N),
+    // x, f and scratch (kBotScrPerCell N) doubles
     size_t off = 0;
     for (int l = 0; l < nl; ++l) {
         const int N = P.lev[l].ncell;
@@ -224,19 +263,18 @@ k_tail(TailParams<T> P) {
     const int NB = BD.ncell;
     // load the operators (split layout in global memory -> natural in shared memory)
     for (int l = 0; l < nl; ++l) {
-        const Dims& D = P.lev[l];
-        for (int c = tid; c < L[l].N; c += nt) {
-            int i, j, k;
-            decode(c, D.n0, D.n1, i, j, k);
-            const int g = level_index(D, i, j, k);
-            L[l].bx[c] = P.bx[l][g];
-            L[l].by[c] = P.by[l][g];
-            L[l].bz[c] = P.bz[l][g];
-            L[l].dg[c] = P.dg[l][g];
-            L[l].idg[c] = P.idg[l][g];
-            L[l].e[c] = T(0);
-            if (l == 0) L[l].f[c] = P.f0[g];
-        }
+        const TailLevel<T>& Ll = L[l];
+        const T *gbx = P.bx[l], *gby = P.by[l], *gbz = P.bz[l], *gdg = P.dg[l], *gidg = P.idg[l];
+        const T* gf = l == 0 ? P.f0 : nullptr;
+        for_split_cells(P.lev[l], [&](int g, int c) {
+            cp_async(Ll.bx + c, gbx + g);
+            cp_async(Ll.by + c, gby + g);
+            cp_async(Ll.bz + c, gbz + g);
+            cp_async(Ll.dg + c, gdg + g);
+            cp_async(Ll.idg + c, gidg + g);
+            if (gf) cp_async(Ll.f + c, gf + g);
+            Ll.e[c] = T(0);
+        });
     }
     BotView v;
     v.n0 = BD.n0;
@@ -245,12 +283,13 @@ k_tail(TailParams<T> P) {
     v.N = NB;
     double* ops = bsm;
     for (int c = tid; c < NB; c += nt) {
-        ops[c] = P.bbx[c];
-        ops[NB + c] = P.bby[c];
-        ops[2 * NB + c] = P.bbz[c];
-        ops[3 * NB + c] = P.bdg[c];
-        ops[4 * NB + c] = P.bidg[c];
+        cp_async(ops + c, P.bbx + c);
+        cp_async(ops + NB + c, P.bby + c);
+        cp_async(ops + 2 * NB + c, P.bbz + c);
+        cp_async(ops + 3 * NB + c, P.bdg + c);
+        cp_async(ops + 4 * NB + c, P.bidg + c);
     }
+    cp_async_wait();
     v.bx = ops;
     v.by = ops + NB;
     v.bz = ops + 2 * NB;
@@ -291,11 +330,10 @@ k_tail(TailParams<T> P) {
         for (int s = 0; s < P.nu2; ++s) tail_sweep<T>(L[l]);
     }
     // hand the correction of the first tail level back (its split layout)
-    const Dims& D0 = P.lev[0];
-    for (int c = tid; c < L[0].N; c += nt) {
-        int i, j, k;
-        decode(c, D0.n0, D0.n1, i, j, k);
-        P.e0[level_index(D0, i, j, k)] = L[0].e[c];
+    {
+        const T* e = L[0].e;
+        T* ge = P.e0;
+        for_split_cells(P.lev[0], [&](int g, int c) { ge[g] = e[c]; });
     }
     if (tid == 0 && P.iters) atomicAdd(P.iters, count);
 }
@@ -304,7 +342,7 @@ template <typename T>
 size_t tail_smem_bytes(const Dims* lev, int nl, const Dims& bottom) {
     size_t off = 0;
     for (int l = 0; l < nl; ++l) off += ((size_t)7 * lev[l].ncell * sizeof(T) + 15) & ~(size_t)15;
-    return off + (size_t)14 * bottom.ncell * sizeof(double);
+    return off + (size_t)(7 + kBotScrPerCell) * bottom.ncell * sizeof(double);
 }
 
 template <typename T>
