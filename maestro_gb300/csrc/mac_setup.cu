@@ -11,6 +11,7 @@
 //   245-251  multifab_fill_boundary                     -> k_scatter_faces (ghost faces)
 #include <cstdio>
 #include <cstring>
+#include <vector>
 
 #include "mac_internal.cuh"
 
@@ -441,54 +442,98 @@ struct GatherParams {
 };
 
 // Whole-domain array <- valid region of every box.  Faces: each box writes lo..hi along dir,
-// and hi+1 only at the domain's high end.
-__global__ void k_gather(GatherParams P, const BoxDesc* __restrict__ boxes, double* __restrict__ dst) {
-    const BoxDesc B = boxes[blockIdx.y];
+// and hi+1 only at the domain's high end.  One warp per x-row of a box (rows = (j, k) pairs),
+// lanes striding x with four loads in flight, so that fabs read over the host link (page-locked
+// host memory) keep enough requests outstanding.  Block (32, kRowsPerBlock), grid (row blocks,
+// boxes).
+constexpr int kRowsPerBlock = 8;
+
+__global__ void __launch_bounds__(32 * kRowsPerBlock)
+k_gather(GatherParams P, const BoxDesc* __restrict__ boxes, double* __restrict__ dst) {
+    const BoxDesc& B = boxes[blockIdx.y];
     const int e0 = B.hi[0] - B.lo[0] + 1 + (P.dir == 0);
     const int e1 = B.hi[1] - B.lo[1] + 1 + (P.dir == 1);
     const int e2 = B.hi[2] - B.lo[2] + 1 + (P.dir == 2);
+    const int row = blockIdx.x * kRowsPerBlock + threadIdx.y;
+    if (row >= e1 * e2) return;
+    const int b = row % e1, c = row / e1;
+    const int gj = B.lo[1] + b, gk = B.lo[2] + c;
+    if (P.dir == 1 && b == e1 - 1 && gj != P.n[1]) return;   // the next box's low face
+    if (P.dir == 2 && c == e2 - 1 && gk != P.n[2]) return;
+    const int ev = (P.dir == 0 && B.hi[0] + 1 != P.n[0]) ? e0 - 1 : e0;
     const int m0 = P.n[0] + (P.dir == 0), m1 = P.n[1] + (P.dir == 1);
-    const int total = e0 * e1 * e2;
     const int g0 = B.ng, g1 = B.ng, g2 = P.dm == 3 ? B.ng : 0;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
-        const int a = t % e0, row = t / e0, b = row % e1, c = row / e1;
-        const int gi = B.lo[0] + a, gj = B.lo[1] + b, gk = B.lo[2] + c;
-        if (P.dir >= 0) {
-            const int gc[3] = {gi, gj, gk};
-            const int hi = (P.dir == 0 ? B.hi[0] : P.dir == 1 ? B.hi[1] : B.hi[2]);
-            if (gc[P.dir] == hi + 1 && hi + 1 != P.n[P.dir]) continue;
-        }
-        const long src = (long)(a + g0) + (long)B.ext[0] * ((b + g1) + (long)B.ext[1] * (c + g2));
-        dst[gi + (long)m0 * (gj + (long)m1 * gk)] = B.ptr[B.comp_off + src];
+    const double* s =
+        B.ptr + B.comp_off + g0 + (long)B.ext[0] * ((b + g1) + (long)B.ext[1] * (c + g2));
+    double* d = dst + B.lo[0] + (long)m0 * (gj + (long)m1 * gk);
+    for (int a0 = threadIdx.x; a0 < ev; a0 += 128) {
+        double v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = a0 + 32 * q < ev ? s[a0 + 32 * q] : 0.0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (a0 + 32 * q < ev) d[a0 + 32 * q] = v[q];
     }
 }
 
 // Every entry of every fab (valid + ghosts) <- whole-domain array, periodic wrap; ghosts outside
-// a non-periodic domain boundary are left untouched.
-__global__ void k_scatter(GatherParams P, const BoxDesc* __restrict__ boxes,
-                          const double* __restrict__ src) {
-    const BoxDesc B = boxes[blockIdx.y];
-    double* dst = const_cast<double*>(B.ptr);
-    const int total = B.ext[0] * B.ext[1] * B.ext[2];
-    const int m0 = P.n[0] + (P.dir == 0), m1 = P.n[1] + (P.dir == 1);
+// a non-periodic domain boundary are left untouched.  One warp per fab row, as k_gather.
+__global__ void __launch_bounds__(32 * kRowsPerBlock)
+k_scatter(GatherParams P, const BoxDesc* __restrict__ boxes, const double* __restrict__ src) {
+    const BoxDesc& B = boxes[blockIdx.y];
+    const int row = blockIdx.x * kRowsPerBlock + threadIdx.y;
+    if (row >= B.ext[1] * B.ext[2]) return;
+    const int b = row % B.ext[1], c = row / B.ext[1];
     const int g[3] = {B.ng, B.ng, P.dm == 3 ? B.ng : 0};
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
-        const int a = t % B.ext[0], row = t / B.ext[0], b = row % B.ext[1], c = row / B.ext[1];
-        int gc[3] = {B.lo[0] - g[0] + a, B.lo[1] - g[1] + b, B.lo[2] - g[2] + c};
-        bool ok = true;
-        for (int dd = 0; dd < 3; ++dd) {
-            const int lim = P.n[dd] + (P.dir == dd ? 1 : 0);
-            if (gc[dd] < 0 || gc[dd] >= lim) {
-                if (!P.bc_per[dd]) {
-                    ok = false;
-                    break;
-                }
-                gc[dd] = (gc[dd] % P.n[dd] + P.n[dd]) % P.n[dd];
-            }
+    int gc[3] = {0, B.lo[1] - g[1] + b, B.lo[2] - g[2] + c};
+    for (int dd = 1; dd < 3; ++dd) {
+        const int lim = P.n[dd] + (P.dir == dd ? 1 : 0);
+        if (gc[dd] < 0 || gc[dd] >= lim) {
+            if (!P.bc_per[dd]) return;
+            gc[dd] = (gc[dd] % P.n[dd] + P.n[dd]) % P.n[dd];
         }
-        if (!ok) continue;
-        dst[t] = src[gc[0] + (long)m0 * (gc[1] + (long)m1 * gc[2])];
     }
+    const int m0 = P.n[0] + (P.dir == 0), m1 = P.n[1] + (P.dir == 1);
+    const int lim0 = m0, x0 = B.lo[0] - g[0];
+    const double* s = src + (long)m0 * (gc[1] + (long)m1 * gc[2]);
+    double* d = const_cast<double*>(B.ptr) + (long)B.ext[0] * (b + (long)B.ext[1] * c);
+    const int e0 = B.ext[0];
+    for (int a0 = threadIdx.x; a0 < e0; a0 += 128) {
+        double v[4];
+        bool ok[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int a = a0 + 32 * q;
+            int gi = x0 + a;
+            ok[q] = a < e0;
+            if (gi < 0 || gi >= lim0) {
+                if (P.bc_per[0])
+                    gi = (gi % P.n[0] + P.n[0]) % P.n[0];
+                else
+                    ok[q] = false;
+            }
+            v[q] = ok[q] ? s[gi] : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (ok[q]) d[a0 + 32 * q] = v[q];
+    }
+}
+
+// Launch grid of k_gather / k_scatter: enough row blocks for the largest box.
+dim3 box_rows_grid(const mac_ctx* c, int dir, int ng, bool with_ghosts) {
+    long rows = 1;
+    for (int b = 0; b < c->g.nboxes; ++b) {
+        long r = 1;
+        for (int d = 1; d < 3; ++d) {
+            const int g = (d < c->dm && with_ghosts) ? ng : 0;
+            const int lo = d < c->dm ? c->box_lo[3 * b + d] : 0;
+            const int hi = d < c->dm ? c->box_hi[3 * b + d] : 0;
+            r *= (long)(hi - lo + 1 + (dir == d ? 1 : 0) + 2 * g);
+        }
+        rows = r > rows ? r : rows;
+    }
+    return dim3((unsigned)ceil_div((int)rows, kRowsPerBlock), (unsigned)c->g.nboxes);
 }
 
 // beta' from caller-supplied face coefficients (natural face layout), Dirichlet wall planes,
@@ -828,8 +873,41 @@ GatherParams gparams(const mac_ctx* c, int dir) {
     return P;
 }
 
+// Host fabs in page-locked (pinned or registered) memory have a device address: the gather and
+// scatter kernels then read and write them in place over the host link, with no staging copy.
+// Returns true (and the device addresses) when every fab of the list is such memory.
+bool host_fabs_mapped(const mac_ctx* c, const double* const* fabs, std::vector<double*>* dev) {
+    const int nb = c->g.nboxes;
+    dev->assign(nb, nullptr);
+    for (int b = 0; b < nb; ++b) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, fabs[b]) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return false;
+        (*dev)[b] = static_cast<double*>(a.devicePointer);
+    }
+    return true;
+}
+
 int gather_common(mac_ctx* c, int ptr_kind, const double* const* fabs, int ng, int ncomp, int comp,
                   int dir, double* dst) {
+    std::vector<double*> mapped;
+    if (ptr_kind == MAC_PTR_HOST && host_fabs_mapped(c, fabs, &mapped)) {
+        BoxDesc* table = nullptr;
+        size_t tot = 0;
+        std::vector<size_t> offs;
+        int rc = fill_boxes(c, dir, ng, ncomp, comp, mapped.data(), MAC_PTR_DEVICE, false, &table,
+                            &tot, &offs);
+        if (rc) return rc;
+        const GatherParams P = gparams(c, dir);
+        k_gather<<<box_rows_grid(c, dir, ng, false), dim3(32, kRowsPerBlock), 0, c->stream>>>(
+            P, table, dst);
+        MAC_CUDA_TRY(cudaGetLastError());
+        ++c->issued;
+        return MAC_OK;
+    }
     if (ptr_kind == MAC_PTR_HOST) {
         int rc = ensure_staging(c, host_staging_need(c, dir, ng));
         if (rc) return rc;
@@ -855,8 +933,8 @@ int gather_common(mac_ctx* c, int ptr_kind, const double* const* fabs, int ng, i
         }
     }
     const GatherParams P = gparams(c, dir);
-    dim3 grid(64, c->g.nboxes);
-    k_gather<<<grid, kBlock, 0, c->stream>>>(P, table, dst);
+    k_gather<<<box_rows_grid(c, dir, ng, false), dim3(32, kRowsPerBlock), 0, c->stream>>>(P, table,
+                                                                                          dst);
     MAC_CUDA_TRY(cudaGetLastError());
     ++c->issued;
     if (ptr_kind == MAC_PTR_HOST) MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -865,6 +943,22 @@ int gather_common(mac_ctx* c, int ptr_kind, const double* const* fabs, int ng, i
 
 int scatter_common(mac_ctx* c, int ptr_kind, double* const* fabs, int ng, int dir,
                    const double* src) {
+    std::vector<double*> mapped;
+    if (ptr_kind == MAC_PTR_HOST && host_fabs_mapped(c, (const double* const*)fabs, &mapped)) {
+        // written in place: the entries the kernel leaves alone keep their host values
+        BoxDesc* table = nullptr;
+        size_t tot = 0;
+        std::vector<size_t> offs;
+        int rc = fill_boxes(c, dir, ng, 1, 0, (const double* const*)mapped.data(), MAC_PTR_DEVICE,
+                            false, &table, &tot, &offs);
+        if (rc) return rc;
+        const GatherParams P = gparams(c, dir);
+        k_scatter<<<box_rows_grid(c, dir, ng, true), dim3(32, kRowsPerBlock), 0, c->stream>>>(
+            P, table, src);
+        MAC_CUDA_TRY(cudaGetLastError());
+        ++c->issued;
+        return MAC_OK;
+    }
     if (ptr_kind == MAC_PTR_HOST) {
         int rc = ensure_staging(c, host_staging_need(c, dir, ng));
         if (rc) return rc;
@@ -891,8 +985,8 @@ int scatter_common(mac_ctx* c, int ptr_kind, double* const* fabs, int ng, int di
         }
     }
     const GatherParams P = gparams(c, dir);
-    dim3 grid(64, c->g.nboxes);
-    k_scatter<<<grid, kBlock, 0, c->stream>>>(P, table, src);
+    k_scatter<<<box_rows_grid(c, dir, ng, true), dim3(32, kRowsPerBlock), 0, c->stream>>>(P, table,
+                                                                                           src);
     MAC_CUDA_TRY(cudaGetLastError());
     ++c->issued;
     if (ptr_kind == MAC_PTR_HOST) {
