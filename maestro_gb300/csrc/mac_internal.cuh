@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstring>
+#include <functional>
 #include <vector>
 
 #include "maestro_mac.h"
@@ -207,9 +208,14 @@ struct mac_ctx {
     // per vertical index r: the kTab* factor tables, (nr+1) doubles each
     double* b0tab = nullptr;
     double* scratch = nullptr;                    // generic FP64 scratch (ncell)
-    // caller-layout staging
+    // caller-layout staging (host-pointer calls): one region per array of a call, filled and
+    // drained by the copy engines on the transfer stream
     double* staging = nullptr;
     size_t staging_elems = 0;
+    size_t staging_cursor = 0;
+    cudaStream_t xfer = nullptr;               // host <-> device copies of host-pointer calls
+    cudaEvent_t xev[16] = {};                  // cross-stream ordering events (ring)
+    int xev_next = 0;
     mac::BoxDesc* d_boxes = nullptr;
     mac::BoxDesc* h_boxes = nullptr;              // pinned
     int box_table_cap = 0;
@@ -309,7 +315,10 @@ int setup_coarse_levels(mac_ctx* c);
 int setup_fp32_copies(mac_ctx* c);
 int setup_rhs(mac_ctx* c, const double* macrhs, bool have_beta0);
 int finish_rhs_stats(mac_ctx* c, double* fnorm_out, bool* finite_out);
-int correct_velocity(mac_ctx* c, bool have_beta0);
+// after_dir (optional) runs after the direction's correction kernel is queued (host-pointer
+// calls start that direction's copy-back there).
+int correct_velocity(mac_ctx* c, bool have_beta0,
+                     const std::function<int(int)>* after_dir = nullptr);
 int setup_fine_from_faces(mac_ctx* c, const double* fx, const double* fy, const double* fz,
                           const double* alpha_nat);
 int setup_rhs_from(mac_ctx* c, const double* rh_nat);
@@ -318,6 +327,21 @@ int level0_to_natural(mac_ctx* c, const double* src, double* dst);
 int check_density(mac_ctx* c, bool* ok);
 
 // caller box layout
+// Gather split in two: gather_begin issues the host -> device copies of the fabs (transfer
+// stream, host pointers only); gather_end orders the main stream after them and launches the
+// gather kernel.  Work that does not need the array can be issued in between.
+struct PendingGather {
+    int ptr_kind = 0, ng = 0, ncomp = 1, comp = 0, dir = -1;
+    const double* const* fabs = nullptr;
+    double* dst = nullptr;
+    double* region = nullptr;   // staging region (host pointers)
+    cudaEvent_t ev = nullptr;
+};
+int staging_reserve(mac_ctx* c, size_t total_elems);
+size_t host_fab_elems(const mac_ctx* c, int dir, int ng);
+int gather_begin(mac_ctx* c, int ptr_kind, const double* const* fabs, int ng, int ncomp, int comp,
+                 int dir, double* dst, PendingGather* pg);
+int gather_end(mac_ctx* c, const PendingGather& pg);
 int gather_cells(mac_ctx* c, int ptr_kind, const double* const* fabs, int ng, int ncomp, int comp,
                  double* dst);
 int gather_faces(mac_ctx* c, int ptr_kind, const double* const* fabs, int ng, int dir,
@@ -340,13 +364,13 @@ int alloc_device(mac_ctx* c, void** p, size_t bytes);
 inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
 
 // 3-D launch over an (nx, ny, nz) index space (x fastest): 128-thread blocks of (bx, 128/bx)
-// with bx the smallest power of two >= nx in [32, 128]; z = blockIdx.z.  Kernels recover their
+// with bx the smallest power of two >= nx, at most 128; z = blockIdx.z.  Kernels recover their
 // indices without integer division.
 struct Grid3 {
     dim3 grid, block;
 };
 inline Grid3 grid3(int nx, int ny, int nz) {
-    int bx = 32;
+    int bx = 1;   // narrow rows share a warp (bx < 32), so no lane idles on small levels
     while (bx < nx && bx < 128) bx <<= 1;
     const int by = 128 / bx;
     Grid3 g;

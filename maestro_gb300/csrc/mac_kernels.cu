@@ -4,6 +4,8 @@
 // Arithmetic follows the FBoxLib cell-centred MG as described in MAESTRO's Docs/mg/mg.tex
 // (:196-211 smoothers, :221-259 bottom solvers, :325-375 V-cycle flow); the level layout and
 // the boundary trick are described in mac_internal.cuh.
+#include <type_traits>
+
 #include "mac_internal.cuh"
 #include "mac_bottom.cuh"
 
@@ -97,6 +99,73 @@ k_gsrb(Dims d, int colour, T* __restrict__ us, const T* __restrict__ uo, const T
     split_nbrs(d, colour, h, j, k, nb);
     T acc = arms<T>(fs[q], q, nb, uo, bxs, bys, bzs, bxo, byo, bzo);
     us[q] = acc * ids[q];
+}
+
+// Red/black half-sweep on a checkerboard-split FP32 level with 4 consecutive colour-half cells
+// (h0 .. h0+3 of one row) per thread: every operand is a float4 load except the other colour's
+// value (and x coefficient) one column outside the group.  Same per-cell arithmetic as k_gsrb.
+// Requires hn0 % 4 == 0.
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ float f4(const float4& v, int m) {
+    return m == 0 ? v.x : m == 1 ? v.y : m == 2 ? v.z : v.w;
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_gsrb4(Dims d, int colour, float* __restrict__ us, const float* __restrict__ uo,
+        const float* __restrict__ fs, const float* __restrict__ bxs, const float* __restrict__ bys,
+        const float* __restrict__ bzs, const float* __restrict__ bxo,
+        const float* __restrict__ byo, const float* __restrict__ bzo,
+        const float* __restrict__ ids) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    const int h0 = 4 * t;
+    if (h0 >= d.hn0 || j >= d.n1) return;
+    const int s = (colour + j + k) & 1;
+    const int jm = (j == 0) ? d.n1 - 1 : j - 1;
+    const int jp = (j == d.n1 - 1) ? 0 : j + 1;
+    const int km = (k == 0) ? d.n2 - 1 : k - 1;
+    const int kp = (k == d.n2 - 1) ? 0 : k + 1;
+    const int row = (j + d.n1 * k) * d.hn0;
+    const int q = row + h0;
+    // column just outside the group on the side the parity needs (wrapped within the row)
+    const int hx = s ? (h0 + 4 == d.hn0 ? 0 : h0 + 4) : (h0 == 0 ? d.hn0 - 1 : h0 - 1);
+    const float4 f = ld4(fs + q), bx = ld4(bxs + q), by = ld4(bys + q), bz = ld4(bzs + q);
+    const float4 id = ld4(ids + q);
+    const float4 uc = ld4(uo + q);
+    const float ux = uo[row + hx];
+    const float4 bxn = ld4(bxo + q);
+    const float bxx = bxo[row + hx];
+    const float4 uym = ld4(uo + (jm + d.n1 * k) * d.hn0 + h0);
+    const int qyp = (jp + d.n1 * k) * d.hn0 + h0;
+    const float4 uyp = ld4(uo + qyp), byp = ld4(byo + qyp);
+    const float4 uzm = ld4(uo + (j + d.n1 * km) * d.hn0 + h0);
+    const int qzp = (j + d.n1 * kp) * d.hn0 + h0;
+    const float4 uzp = ld4(uo + qzp), bzp = ld4(bzo + qzp);
+    float out[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        // x-neighbours of cell i = 2 (h0 + m) + s: other-colour columns h-1+s (low), h+s (high)
+        float ul, uh, bh;
+        if (s) {
+            ul = f4(uc, m);
+            uh = m == 3 ? ux : f4(uc, m + 1);
+            bh = m == 3 ? bxx : f4(bxn, m + 1);
+        } else {
+            ul = m == 0 ? ux : f4(uc, m - 1);
+            uh = f4(uc, m);
+            bh = f4(bxn, m);
+        }
+        float acc = f4(f, m);
+        acc = fmaf(f4(bx, m), ul, acc);
+        acc = fmaf(bh, uh, acc);
+        acc = fmaf(f4(by, m), f4(uym, m), acc);
+        acc = fmaf(f4(byp, m), f4(uyp, m), acc);
+        acc = fmaf(f4(bz, m), f4(uzm, m), acc);
+        acc = fmaf(f4(bzp, m), f4(uzp, m), acc);
+        out[m] = acc * f4(id, m);
+    }
+    *reinterpret_cast<float4*>(us + q) = make_float4(out[0], out[1], out[2], out[3]);
 }
 
 // ---- defect r = f - L u on the children of each coarse cell, averaged into the coarse rhs ---
@@ -345,6 +414,16 @@ k_bottom(BotView vin, Tio* __restrict__ xio, const Tio* __restrict__ fio, double
 template <typename T>
 void launch_gsrb(const Dims& d, int colour, LevelArrays<T>& a, cudaStream_t s) {
     const int own = colour * d.half, oth = (colour ^ 1) * d.half;
+    if constexpr (std::is_same<T, float>::value) {
+        // four cells a thread pays off on large levels; small ones want more threads in flight
+        if (d.hn0 % 4 == 0 && d.half >= (1 << 19)) {
+            const Grid3 g4 = grid3(d.hn0 / 4, d.n1, d.n2);
+            k_gsrb4<<<g4.grid, g4.block, 0, s>>>(
+                d, colour, a.phi + own, a.phi + oth, a.f + own, a.bx + own, a.by + own,
+                a.bz + own, a.bx + oth, a.by + oth, a.bz + oth, a.invdiag + own);
+            return;
+        }
+    }
     const Grid3 g = grid3(d.hn0, d.n1, d.n2);
     k_gsrb<T><<<g.grid, g.block, 0, s>>>(
         d, colour, a.phi + own, a.phi + oth, a.f + own, a.bx + own, a.by + own, a.bz + own,

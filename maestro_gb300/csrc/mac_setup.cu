@@ -9,8 +9,10 @@
 //   229      mkumac                                     -> k_correct    (908-975)
 //   232-236  divide out beta0                           -> fused into k_correct
 //   245-251  multifab_fill_boundary                     -> k_scatter_faces (ghost faces)
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <vector>
 
 #include "mac_internal.cuh"
@@ -743,7 +745,7 @@ int setup_rhs(mac_ctx* c, const double* macrhs, bool have_beta0) {
     return launch_rhs(c, macrhs, false);
 }
 
-int correct_velocity(mac_ctx* c, bool have_beta0) {
+int correct_velocity(mac_ctx* c, bool have_beta0, const std::function<int(int)>* after_dir) {
     Level& L = c->lev[0];
     const double* bd[3] = {L.a64.bx, L.a64.by, L.a64.bz};
     for (int d = 0; d < c->dm; ++d) {
@@ -761,6 +763,10 @@ int correct_velocity(mac_ctx* c, bool have_beta0) {
                                                      L.wall[d][0], L.wall[d][1], c->b0tab);
         MAC_CUDA_TRY(cudaGetLastError());
         ++c->issued;
+        if (after_dir) {
+            int rc = (*after_dir)(d);
+            if (rc) return rc;
+        }
     }
     return MAC_OK;
 }
@@ -787,6 +793,15 @@ int level0_to_natural(mac_ctx* c, const double* src, double* dst) {
 namespace {
 
 constexpr int kBoxSlots = 16;
+
+constexpr int kBoxChunk = 64;   // 64 descriptors fit the 4 KB kernel-parameter space
+struct BoxChunk {
+    int n;
+    BoxDesc b[kBoxChunk];
+};
+__global__ void k_put_boxes(BoxChunk ch, BoxDesc* __restrict__ dst) {
+    for (int q = threadIdx.x; q < ch.n; q += blockDim.x) dst[q] = ch.b[q];
+}
 
 struct SlotCursor {
     int next = 0;
@@ -826,7 +841,15 @@ int fill_boxes(mac_ctx* c, int dir, int ng, int ncomp, int comp, const double* c
     }
     *total_elems = off;
     BoxDesc* d = c->d_boxes + (size_t)slot * nb;
-    MAC_CUDA_TRY(cudaMemcpyAsync(d, h, sizeof(BoxDesc) * nb, cudaMemcpyHostToDevice, c->stream));
+    // uploaded as kernel parameters, not by a copy: a host -> device copy on the main stream would
+    // queue on the copy engine behind the transfer stream's bulk input copies
+    for (int b0 = 0; b0 < nb; b0 += kBoxChunk) {
+        BoxChunk ch;
+        ch.n = std::min(kBoxChunk, nb - b0);
+        for (int q = 0; q < ch.n; ++q) ch.b[q] = h[b0 + q];
+        k_put_boxes<<<1, 32, 0, c->stream>>>(ch, d + b0);
+        MAC_CUDA_TRY(cudaGetLastError());
+    }
     *dev_table = d;
     return MAC_OK;
 }
@@ -835,6 +858,7 @@ int ensure_staging(mac_ctx* c, size_t elems) {
     if (elems <= c->staging_elems) return MAC_OK;
     if (c->staging) {
         MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        if (c->xfer) MAC_CUDA_TRY(cudaStreamSynchronize(c->xfer));
         cudaFree(c->staging);
         c->staging = nullptr;
     }
@@ -845,21 +869,6 @@ int ensure_staging(mac_ctx* c, size_t elems) {
     }
     c->staging_elems = elems;
     return MAC_OK;
-}
-
-size_t host_staging_need(const mac_ctx* c, int dir, int ng) {
-    size_t tot = 0;
-    for (int b = 0; b < c->g.nboxes; ++b) {
-        size_t e = 1;
-        for (int d = 0; d < 3; ++d) {
-            const int g = d < c->dm ? ng : 0;
-            const int lo = d < c->dm ? c->box_lo[3 * b + d] : 0;
-            const int hi = d < c->dm ? c->box_hi[3 * b + d] : 0;
-            e *= (size_t)(hi - lo + 1 + (dir == d ? 1 : 0) + 2 * g);
-        }
-        tot += e;
-    }
-    return tot;
 }
 
 GatherParams gparams(const mac_ctx* c, int dir) {
@@ -873,135 +882,200 @@ GatherParams gparams(const mac_ctx* c, int dir) {
     return P;
 }
 
-// Host fabs in page-locked (pinned or registered) memory have a device address: the gather and
-// scatter kernels then read and write them in place over the host link, with no staging copy.
-// Returns true (and the device addresses) when every fab of the list is such memory.
-bool host_fabs_mapped(const mac_ctx* c, const double* const* fabs, std::vector<double*>* dev) {
-    const int nb = c->g.nboxes;
-    dev->assign(nb, nullptr);
-    for (int b = 0; b < nb; ++b) {
-        cudaPointerAttributes a;
-        if (cudaPointerGetAttributes(&a, fabs[b]) != cudaSuccess) {
-            cudaGetLastError();
-            return false;
-        }
-        if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return false;
-        (*dev)[b] = static_cast<double*>(a.devicePointer);
+// Elements of one box's fab (one component) in element offset order of the fab list.
+size_t fab_elems(const mac_ctx* c, int b, int dir, int ng) {
+    size_t e = 1;
+    for (int d = 0; d < 3; ++d) {
+        const int g = d < c->dm ? ng : 0;
+        const int lo = d < c->dm ? c->box_lo[3 * b + d] : 0;
+        const int hi = d < c->dm ? c->box_hi[3 * b + d] : 0;
+        e *= (size_t)(hi - lo + 1 + (dir == d ? 1 : 0) + 2 * g);
     }
-    return true;
+    return e;
 }
 
-int gather_common(mac_ctx* c, int ptr_kind, const double* const* fabs, int ng, int ncomp, int comp,
-                  int dir, double* dst) {
-    std::vector<double*> mapped;
-    if (ptr_kind == MAC_PTR_HOST && host_fabs_mapped(c, fabs, &mapped)) {
-        BoxDesc* table = nullptr;
-        size_t tot = 0;
-        std::vector<size_t> offs;
-        int rc = fill_boxes(c, dir, ng, ncomp, comp, mapped.data(), MAC_PTR_DEVICE, false, &table,
-                            &tot, &offs);
-        if (rc) return rc;
-        const GatherParams P = gparams(c, dir);
-        k_gather<<<box_rows_grid(c, dir, ng, false), dim3(32, kRowsPerBlock), 0, c->stream>>>(
-            P, table, dst);
-        MAC_CUDA_TRY(cudaGetLastError());
-        ++c->issued;
-        return MAC_OK;
-    }
-    if (ptr_kind == MAC_PTR_HOST) {
-        int rc = ensure_staging(c, host_staging_need(c, dir, ng));
-        if (rc) return rc;
-    }
-    BoxDesc* table = nullptr;
-    size_t tot = 0;
-    std::vector<size_t> offs;
-    int rc = fill_boxes(c, dir, ng, ncomp, comp, fabs, ptr_kind, true, &table, &tot, &offs);
-    if (rc) return rc;
-    if (ptr_kind == MAC_PTR_HOST) {
-        for (int b = 0; b < c->g.nboxes; ++b) {
-            const BoxDesc& B = c->h_boxes[0];
-            (void)B;
-            size_t e = 1;
-            for (int d = 0; d < 3; ++d) {
-                const int g = d < c->dm ? ng : 0;
-                const int lo = d < c->dm ? c->box_lo[3 * b + d] : 0;
-                const int hi = d < c->dm ? c->box_hi[3 * b + d] : 0;
-                e *= (size_t)(hi - lo + 1 + (dir == d ? 1 : 0) + 2 * g);
-            }
-            MAC_CUDA_TRY(cudaMemcpyAsync(c->staging + offs[b], fabs[b] + e * comp, e * sizeof(double),
-                                         cudaMemcpyHostToDevice, c->stream));
+cudaEvent_t next_event(mac_ctx* c) {
+    cudaEvent_t e = c->xev[c->xev_next];
+    c->xev_next = (c->xev_next + 1) % (int)(sizeof(c->xev) / sizeof(c->xev[0]));
+    return e;
+}
+
+double* staging_take(mac_ctx* c, size_t elems) {
+    if (c->staging_cursor + elems > c->staging_elems) return nullptr;
+    double* p = c->staging + c->staging_cursor;
+    c->staging_cursor += elems;
+    return p;
+}
+
+// Region of a fab that k_scatter writes, per direction as [lo, hi] in fab-local indices: every
+// entry whose global index lies in the domain, or in a periodic direction.
+void written_region(const mac_ctx* c, int b, int dir, int ng, int lo[3], int hi[3], int ext[3]) {
+    for (int d = 0; d < 3; ++d) {
+        if (d >= c->dm) {
+            lo[d] = hi[d] = 0;
+            ext[d] = 1;
+            continue;
         }
+        const int blo = c->box_lo[3 * b + d] - c->g.domain_lo[d];
+        const int bhi = c->box_hi[3 * b + d] - c->g.domain_lo[d];
+        ext[d] = bhi - blo + 1 + (dir == d ? 1 : 0) + 2 * ng;
+        const bool per = c->bc_lo[d] == MAC_BC_PER;
+        const int lim = c->n[d] + (dir == d ? 1 : 0);
+        const int g0 = blo - ng;   // global index of fab entry 0
+        lo[d] = per ? 0 : std::max(0, -g0);
+        hi[d] = per ? ext[d] - 1 : std::min(ext[d] - 1, lim - 1 - g0);
     }
-    const GatherParams P = gparams(c, dir);
-    k_gather<<<box_rows_grid(c, dir, ng, false), dim3(32, kRowsPerBlock), 0, c->stream>>>(P, table,
-                                                                                          dst);
-    MAC_CUDA_TRY(cudaGetLastError());
-    ++c->issued;
-    if (ptr_kind == MAC_PTR_HOST) MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+}
+
+}  // namespace
+
+size_t host_fab_elems(const mac_ctx* c, int dir, int ng) {
+    size_t tot = 0;
+    for (int b = 0; b < c->g.nboxes; ++b) tot += fab_elems(c, b, dir, ng);
+    return tot;
+}
+
+// Make room for the staging regions of one host-pointer call and start carving at offset 0.
+int staging_reserve(mac_ctx* c, size_t total_elems) {
+    int rc = ensure_staging(c, total_elems);
+    if (rc) return rc;
+    c->staging_cursor = 0;
     return MAC_OK;
 }
 
-int scatter_common(mac_ctx* c, int ptr_kind, double* const* fabs, int ng, int dir,
-                   const double* src) {
-    std::vector<double*> mapped;
-    if (ptr_kind == MAC_PTR_HOST && host_fabs_mapped(c, (const double* const*)fabs, &mapped)) {
-        // written in place: the entries the kernel leaves alone keep their host values
-        BoxDesc* table = nullptr;
-        size_t tot = 0;
-        std::vector<size_t> offs;
-        int rc = fill_boxes(c, dir, ng, 1, 0, (const double* const*)mapped.data(), MAC_PTR_DEVICE,
-                            false, &table, &tot, &offs);
+int gather_begin(mac_ctx* c, int ptr_kind, const double* const* fabs, int ng, int ncomp, int comp,
+                 int dir, double* dst, PendingGather* pg) {
+    pg->ptr_kind = ptr_kind;
+    pg->fabs = fabs;
+    pg->ng = ng;
+    pg->ncomp = ncomp;
+    pg->comp = comp;
+    pg->dir = dir;
+    pg->dst = dst;
+    pg->region = nullptr;
+    pg->ev = nullptr;
+    if (ptr_kind != MAC_PTR_HOST) return MAC_OK;
+    const size_t need = host_fab_elems(c, dir, ng);
+    if (c->staging_cursor + need > c->staging_elems) {
+        // a call that did not reserve (or an unplanned array): grow after the pending work
+        MAC_CUDA_TRY(cudaStreamSynchronize(c->xfer));
+        MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        int rc = ensure_staging(c, need);
         if (rc) return rc;
-        const GatherParams P = gparams(c, dir);
-        k_scatter<<<box_rows_grid(c, dir, ng, true), dim3(32, kRowsPerBlock), 0, c->stream>>>(
-            P, table, src);
-        MAC_CUDA_TRY(cudaGetLastError());
-        ++c->issued;
-        return MAC_OK;
+        c->staging_cursor = 0;
     }
-    if (ptr_kind == MAC_PTR_HOST) {
-        int rc = ensure_staging(c, host_staging_need(c, dir, ng));
-        if (rc) return rc;
+    pg->region = staging_take(c, need);
+    size_t off = 0;
+    for (int b = 0; b < c->g.nboxes; ++b) {
+        const size_t e = fab_elems(c, b, dir, ng);
+        MAC_CUDA_TRY(cudaMemcpyAsync(pg->region + off, fabs[b] + e * comp, e * sizeof(double),
+                                     cudaMemcpyHostToDevice, c->xfer));
+        off += e;
     }
+    pg->ev = next_event(c);
+    MAC_CUDA_TRY(cudaEventRecord(pg->ev, c->xfer));
+    return MAC_OK;
+}
+
+int gather_end(mac_ctx* c, const PendingGather& pg) {
     BoxDesc* table = nullptr;
     size_t tot = 0;
     std::vector<size_t> offs;
-    int rc = fill_boxes(c, dir, ng, 1, 0, (const double* const*)fabs, ptr_kind, true, &table, &tot,
-                        &offs);
-    if (rc) return rc;
-    if (ptr_kind == MAC_PTR_HOST) {
-        // the kernel writes every fab entry it can; copy the current host contents first so the
-        // entries it leaves alone (physical-boundary ghosts) survive the round trip
+    int rc;
+    if (pg.ptr_kind == MAC_PTR_HOST) {
+        MAC_CUDA_TRY(cudaStreamWaitEvent(c->stream, pg.ev, 0));
+        // the staged copy holds one component per fab, contiguous in box order
+        std::vector<const double*> ptrs(c->g.nboxes);
+        size_t off = 0;
         for (int b = 0; b < c->g.nboxes; ++b) {
-            size_t e = 1;
-            for (int d = 0; d < 3; ++d) {
-                const int g = d < c->dm ? ng : 0;
-                const int lo = d < c->dm ? c->box_lo[3 * b + d] : 0;
-                const int hi = d < c->dm ? c->box_hi[3 * b + d] : 0;
-                e *= (size_t)(hi - lo + 1 + (dir == d ? 1 : 0) + 2 * g);
-            }
-            MAC_CUDA_TRY(cudaMemcpyAsync(c->staging + offs[b], fabs[b], e * sizeof(double),
-                                         cudaMemcpyHostToDevice, c->stream));
+            ptrs[b] = pg.region + off;
+            off += fab_elems(c, b, pg.dir, pg.ng);
         }
+        rc = fill_boxes(c, pg.dir, pg.ng, 1, 0, ptrs.data(), MAC_PTR_DEVICE, false, &table, &tot,
+                        &offs);
+    } else {
+        rc = fill_boxes(c, pg.dir, pg.ng, pg.ncomp, pg.comp, pg.fabs, MAC_PTR_DEVICE, false, &table,
+                        &tot, &offs);
     }
+    if (rc) return rc;
+    const GatherParams P = gparams(c, pg.dir);
+    k_gather<<<box_rows_grid(c, pg.dir, pg.ng, false), dim3(32, kRowsPerBlock), 0, c->stream>>>(
+        P, table, pg.dst);
+    MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
+    return MAC_OK;
+}
+
+namespace {
+
+int gather_common(mac_ctx* c, int ptr_kind, const double* const* fabs, int ng, int ncomp, int comp,
+                  int dir, double* dst) {
+    PendingGather pg;
+    int rc = gather_begin(c, ptr_kind, fabs, ng, ncomp, comp, dir, dst, &pg);
+    return rc ? rc : gather_end(c, pg);
+}
+
+// Whole-domain array -> every fab.  Host pointers: the kernel fills a staging copy of the fabs on
+// the main stream and the copy engines bring back, per fab, only the region the kernel wrote, so
+// the host entries it leaves alone (ghosts outside non-periodic walls) keep their values.  The
+// copies complete on the transfer stream; the caller synchronises it before returning.
+int scatter_common(mac_ctx* c, int ptr_kind, double* const* fabs, int ng, int dir,
+                   const double* src) {
+    BoxDesc* table = nullptr;
+    size_t tot = 0;
+    std::vector<size_t> offs;
+    double* region = nullptr;
+    std::vector<const double*> ptrs(c->g.nboxes);
+    if (ptr_kind == MAC_PTR_HOST) {
+        const size_t need = host_fab_elems(c, dir, ng);
+        if (c->staging_cursor + need > c->staging_elems) {
+            MAC_CUDA_TRY(cudaStreamSynchronize(c->xfer));
+            MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+            int rc = ensure_staging(c, need);
+            if (rc) return rc;
+            c->staging_cursor = 0;
+        }
+        region = staging_take(c, need);
+        size_t off = 0;
+        for (int b = 0; b < c->g.nboxes; ++b) {
+            ptrs[b] = region + off;
+            off += fab_elems(c, b, dir, ng);
+        }
+    } else {
+        for (int b = 0; b < c->g.nboxes; ++b) ptrs[b] = fabs[b];
+    }
+    int rc = fill_boxes(c, dir, ng, 1, 0, ptrs.data(), MAC_PTR_DEVICE, false, &table, &tot, &offs);
+    if (rc) return rc;
     const GatherParams P = gparams(c, dir);
     k_scatter<<<box_rows_grid(c, dir, ng, true), dim3(32, kRowsPerBlock), 0, c->stream>>>(P, table,
                                                                                            src);
     MAC_CUDA_TRY(cudaGetLastError());
     ++c->issued;
-    if (ptr_kind == MAC_PTR_HOST) {
-        for (int b = 0; b < c->g.nboxes; ++b) {
-            size_t e = 1;
-            for (int d = 0; d < 3; ++d) {
-                const int g = d < c->dm ? ng : 0;
-                const int lo = d < c->dm ? c->box_lo[3 * b + d] : 0;
-                const int hi = d < c->dm ? c->box_hi[3 * b + d] : 0;
-                e *= (size_t)(hi - lo + 1 + (dir == d ? 1 : 0) + 2 * g);
-            }
-            MAC_CUDA_TRY(cudaMemcpyAsync(fabs[b], c->staging + offs[b], e * sizeof(double),
-                                         cudaMemcpyDeviceToHost, c->stream));
+    if (ptr_kind != MAC_PTR_HOST) return MAC_OK;
+    cudaEvent_t ev = next_event(c);
+    MAC_CUDA_TRY(cudaEventRecord(ev, c->stream));
+    MAC_CUDA_TRY(cudaStreamWaitEvent(c->xfer, ev, 0));
+    for (int b = 0; b < c->g.nboxes; ++b) {
+        int lo[3], hi[3], ext[3];
+        written_region(c, b, dir, ng, lo, hi, ext);
+        double* sdev = const_cast<double*>(ptrs[b]);
+        if (lo[0] == 0 && hi[0] == ext[0] - 1 && lo[1] == 0 && hi[1] == ext[1] - 1) {
+            // whole rows and planes: one linear copy of planes lo[2] .. hi[2]
+            const size_t plane = (size_t)ext[0] * ext[1];
+            MAC_CUDA_TRY(cudaMemcpyAsync(fabs[b] + plane * lo[2], sdev + plane * lo[2],
+                                         plane * (hi[2] - lo[2] + 1) * sizeof(double),
+                                         cudaMemcpyDeviceToHost, c->xfer));
+        } else {
+            cudaMemcpy3DParms p = {};
+            p.srcPtr = make_cudaPitchedPtr(sdev, ext[0] * sizeof(double), ext[0], ext[1]);
+            p.dstPtr = make_cudaPitchedPtr(fabs[b], ext[0] * sizeof(double), ext[0], ext[1]);
+            p.srcPos = make_cudaPos(lo[0] * sizeof(double), lo[1], lo[2]);
+            p.dstPos = p.srcPos;
+            p.extent = make_cudaExtent((hi[0] - lo[0] + 1) * sizeof(double), hi[1] - lo[1] + 1,
+                                       hi[2] - lo[2] + 1);
+            p.kind = cudaMemcpyDeviceToHost;
+            MAC_CUDA_TRY(cudaMemcpy3DAsync(&p, c->xfer));
         }
-        MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
     }
     return MAC_OK;
 }

@@ -14,6 +14,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <chrono>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <type_traits>
@@ -581,11 +582,15 @@ int ctx_alloc(mac_ctx* c) {
         for (int e = 0; e < 8; ++e) MAC_CUDA_TRY(cudaEventCreate(&c->tev[v][e]));
     for (int e = 0; e < 3; ++e) MAC_CUDA_TRY(cudaEventCreate(&c->tail[e]));
     MAC_CUDA_TRY(cudaMemset(c->red.counters, 0, 4 * sizeof(int)));
+    // copy-engine stream of host-pointer calls (independent of the legacy stream) and its events
+    MAC_CUDA_TRY(cudaStreamCreateWithFlags(&c->xfer, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : c->xev) MAC_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     return MAC_OK;
 }
 
 void ctx_free(mac_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->xfer) cudaStreamSynchronize(c->xfer);
     drop_graphs(c);
     for (void* p : c->allocations) cudaFree(p);
     c->allocations.clear();
@@ -601,6 +606,13 @@ void ctx_free(mac_ctx* c) {
             if (c->tev[v][e]) cudaEventDestroy(c->tev[v][e]);
     for (int e = 0; e < 3; ++e)
         if (c->tail[e]) cudaEventDestroy(c->tail[e]);
+    for (cudaEvent_t& e : c->xev)
+        if (e) {
+            cudaEventDestroy(e);
+            e = nullptr;
+        }
+    if (c->xfer) cudaStreamDestroy(c->xfer);
+    c->xfer = nullptr;
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     c->stream = nullptr;
 }
@@ -637,7 +649,11 @@ int set_call_state_impl(mac_ctx* c, bool with_alpha) {
 }
 
 // The projection on whole-domain device arrays already in c->u / c->rho / rhs / phin.
-int core_macproject(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats* st) {
+int core_macproject(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats* st,
+                    const std::function<int()>* before_rhs = nullptr,
+                    const std::function<int()>* before_phi = nullptr,
+                    const std::function<int()>* after_phi = nullptr,
+                    const std::function<int(int)>* after_dir = nullptr) {
     Level& F = c->lev[0];
     cudaEventRecord(c->ev[0], c->stream);
     int rc = set_call_state_impl(c, false);
@@ -647,8 +663,10 @@ int core_macproject(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats
     if (rc) return rc;
     rc = setup_coarse_levels(c);
     if (rc) return rc;
+    if (before_rhs && (rc = (*before_rhs)())) return rc;
     rc = setup_rhs(c, macrhs, have_beta0);
     if (rc) return rc;
+    if (before_phi && (rc = (*before_phi)())) return rc;
     rc = natural_to_level0(c, c->phin, F.a64.phi);
     if (rc) return rc;
     cudaEventRecord(c->ev[1], c->stream);
@@ -657,9 +675,10 @@ int core_macproject(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats
     if (solve_rc != MAC_OK && solve_rc != MAC_ERR_NOT_CONVERGED) return solve_rc;
     cudaEventRecord(c->ev[2], c->stream);
     const long long before_corr = c->issued;
-    rc = correct_velocity(c, have_beta0);
-    if (rc) return rc;
     rc = level0_to_natural(c, F.a64.phi, c->phin);
+    if (rc) return rc;
+    if (after_phi && (rc = (*after_phi)())) return rc;
+    rc = correct_velocity(c, have_beta0, after_dir);
     if (rc) return rc;
     c->ktime_launches[MAC_KT_CORRECT] += (int)(c->issued - before_corr);
     c->ktime_launches[MAC_KT_SETUP] += (int)setup_kernels;
@@ -906,23 +925,52 @@ int mac_macproject(mac_ctx* c, int ptr_kind, double* const* umac, int ng_u, doub
     const auto t0 = std::chrono::steady_clock::now();
     fill_common_stats(c, st);
     int rc = MAC_OK;
-    for (int d = 0; d < c->dm && !rc; ++d)
-        rc = gather_faces(c, ptr_kind, (const double* const*)(umac + d * nb), ng_u, d, c->u[d]);
-    if (!rc) rc = gather_cells(c, ptr_kind, rho, ng_rho, rho_ncomp, rho_comp, c->rho);
-    if (!rc && macrhs) rc = gather_cells(c, ptr_kind, macrhs, ng_rhs, 1, 0, c->rhs);
-    if (!rc) rc = gather_cells(c, ptr_kind, (const double* const*)phi, ng_phi, 1, 0, c->phin);
+    if (ptr_kind == MAC_PTR_HOST) {
+        size_t need = host_fab_elems(c, -1, ng_rho) + host_fab_elems(c, -1, ng_phi);
+        for (int d = 0; d < c->dm; ++d) need += host_fab_elems(c, d, ng_u);
+        if (macrhs) need += host_fab_elems(c, -1, ng_rhs);
+        rc = staging_reserve(c, need);
+    }
+    // Host pointers: every input's copy is queued on the copy engines at once, in the order the
+    // setup consumes them (rho, velocities, rhs, phi); each gather kernel waits only for its own
+    // array, so the coefficient setup runs while the later arrays are still in flight.
+    PendingGather g_rho, g_u[3], g_rhs, g_phi;
+    // beta0 first: its small copy must not queue behind the bulk inputs on the copy engine
     if (!rc && beta0_1d) rc = load_beta0_impl(c, ptr_kind, beta0_1d, beta0_1d_edge);
+    if (!rc) rc = gather_begin(c, ptr_kind, rho, ng_rho, rho_ncomp, rho_comp, -1, c->rho, &g_rho);
+    for (int d = 0; d < c->dm && !rc; ++d)
+        rc = gather_begin(c, ptr_kind, (const double* const*)(umac + d * nb), ng_u, 1, 0, d, c->u[d],
+                          &g_u[d]);
+    if (!rc && macrhs) rc = gather_begin(c, ptr_kind, macrhs, ng_rhs, 1, 0, -1, c->rhs, &g_rhs);
+    if (!rc) rc = gather_begin(c, ptr_kind, (const double* const*)phi, ng_phi, 1, 0, -1, c->phin,
+                               &g_phi);
+    if (!rc) rc = gather_end(c, g_rho);
+    const std::function<int()> before_rhs = [&]() {
+        for (int d = 0; d < c->dm; ++d) {
+            int r = gather_end(c, g_u[d]);
+            if (r) return r;
+        }
+        return macrhs ? gather_end(c, g_rhs) : MAC_OK;
+    };
+    const std::function<int()> before_phi = [&]() { return gather_end(c, g_phi); };
+    // outputs go back as soon as each is final: phi before the velocity correction, each
+    // velocity component right after its correction kernel
+    const std::function<int()> after_phi = [&]() {
+        return scatter_cells(c, ptr_kind, phi, ng_phi, c->phin);
+    };
+    const std::function<int(int)> after_dir = [&](int d) {
+        return scatter_faces(c, ptr_kind, umac + d * nb, ng_u, d, c->u[d]);
+    };
     int solve_rc = MAC_OK;
     if (!rc) {
-        solve_rc = core_macproject(c, macrhs ? c->rhs : nullptr, beta0_1d != nullptr, st);
+        solve_rc = core_macproject(c, macrhs ? c->rhs : nullptr, beta0_1d != nullptr, st,
+                                   &before_rhs, &before_phi, &after_phi, &after_dir);
         if (solve_rc != MAC_OK && solve_rc != MAC_ERR_NOT_CONVERGED) rc = solve_rc;
     }
-    for (int d = 0; d < c->dm && !rc; ++d)
-        rc = scatter_faces(c, ptr_kind, umac + d * nb, ng_u, d, c->u[d]);
-    if (!rc) rc = scatter_cells(c, ptr_kind, phi, ng_phi, c->phin);
-    if (!rc) {
-        cudaError_t e = cudaStreamSynchronize(c->stream);
-        if (e != cudaSuccess) {
+    {
+        cudaError_t e = cudaStreamSynchronize(c->xfer);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess && !rc) {
             set_last_cuda_error(e, "cudaStreamSynchronize", __FILE__, __LINE__);
             rc = MAC_ERR_CUDA;
         }
@@ -955,6 +1003,12 @@ int mac_multigrid(mac_ctx* c, int ptr_kind, const double* const* rh, int ng_rh,
     Level& F = c->lev[0];
     int rc = set_call_state_impl(c, alpha != nullptr);
     set_otf(c, false);
+    if (!rc && ptr_kind == MAC_PTR_HOST) {
+        size_t need = host_fab_elems(c, -1, ng_rh) + host_fab_elems(c, -1, ng_phi);
+        for (int d = 0; d < c->dm; ++d) need += host_fab_elems(c, d, ng_beta);
+        if (alpha) need += host_fab_elems(c, -1, ng_alpha);
+        rc = staging_reserve(c, need);
+    }
     for (int d = 0; d < c->dm && !rc; ++d)
         rc = gather_faces(c, ptr_kind, beta + d * nb, ng_beta, d, c->u[d]);
     if (!rc) rc = gather_cells(c, ptr_kind, rh, ng_rh, 1, 0, c->rhs);
@@ -978,7 +1032,8 @@ int mac_multigrid(mac_ctx* c, int ptr_kind, const double* const* rh, int ng_rh,
     if (!rc) rc = level0_to_natural(c, F.a64.phi, c->phin);
     if (!rc) rc = scatter_cells(c, ptr_kind, phi, ng_phi, c->phin);
     if (!rc) {
-        cudaError_t e = cudaStreamSynchronize(c->stream);
+        cudaError_t e = cudaStreamSynchronize(c->xfer);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
         if (e != cudaSuccess) {
             set_last_cuda_error(e, "cudaStreamSynchronize", __FILE__, __LINE__);
             rc = MAC_ERR_CUDA;
