@@ -289,9 +289,10 @@ def main():
     hbm_peak, peak_kind = peaks()
     kt_ms = sum(s["ktime_ms"][capi.KT_NAMES.index("smooth")] for s in st_mixed)
     kt_n = sum(s["ktime_launches"][capi.KT_NAMES.index("smooth")] for s in st_mixed)
-    # algorithmic bytes per half-sweep launch: half of the fused red+black sweep's
-    # phi, f, beta_x, beta_y, beta_z read + phi write (6 words per cell), FP32 words
-    alg_bytes = 3 * 4 * N
+    # algorithmic bytes per half-sweep launch of the on-the-fly design (per cell of the level):
+    # the other colour's e (2 B) and both colours' rho (4 B) read, the own colour's f read (2 B)
+    # and e write (2 B) = 10 B; coefficients are formed from rho in registers, none is stored
+    alg_bytes = 10 * N
     avg_s = (kt_ms / kt_n) / 1e3 if kt_n else float("nan")
     achieved = alg_bytes / avg_s / 1e9
     traffic = None
@@ -299,10 +300,12 @@ def main():
     if os.path.exists(tp):
         with open(tp) as f:
             tj = json.load(f)
-        ent = tj.get("gsrb_fp32_fine")
+        ent = tj.get("gsrb_otf_staged_fine")
         if ent and ent.get("cells"):
             traffic = ent["dram_bytes_per_launch"] * N / ent["cells"]
-    roofline = {"bound": "hbm", "kernel": "k_gsrb<float> finest level (one colour)",
+    roofline = {"bound": "hbm",
+                "kernel": "k_gsrb_otf_staged (finest level, one colour half-sweep, FP32, "
+                          "coefficients from rho on the fly)",
                 "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "traffic": traffic,
                 "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_s * 1e3,
