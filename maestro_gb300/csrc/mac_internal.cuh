@@ -261,7 +261,7 @@ void launch_resid_restrict(const Dims& fine, const Dims& coarse, const LevelArra
                            T* fc, bool red_only, cudaStream_t s);
 template <typename T>
 void launch_prolong_add(const Dims& fine, const Dims& coarse, const BcDesc& bc, const T* ec,
-                        T* phi_fine, cudaStream_t s);
+                        T* phi_fine, bool black_only, cudaStream_t s);
 template <typename T>
 void launch_resid_norm(const Dims& d, const LevelArrays<T>& a, bool red_only,
                        unsigned long long* maxbits, cudaStream_t s);

@@ -233,7 +233,10 @@ __device__ __forceinline__ void coarse_nb(int q, int n, int blo, int bhi, int& q
     }
 }
 
-template <typename T, bool Z2>
+// BLACK_ONLY: add the correction to colour-1 cells only.  When post-smoothing follows, its first
+// half-sweep overwrites every colour-0 cell without reading it (a red/black update reads only the
+// other colour), so the colour-0 corrections would never be used: half the read-modify-write.
+template <typename T, bool Z2, bool BLACK_ONLY>
 __global__ void __launch_bounds__(kBlock)
 k_prolong_add(Dims F, Dims C, BcDesc bc, const T* __restrict__ ec, T* __restrict__ u) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
@@ -284,14 +287,20 @@ k_prolong_add(Dims F, Dims C, BcDesc bc, const T* __restrict__ ec, T* __restrict
 #pragma unroll
         for (int yc = 0; yc < 2; ++yc) {
             const T t = T(0.75) * Yv[1][yc][zc];
-            const T v0 = fmaT(wxm, Yv[0][yc][zc], t);
-            const T v1 = fmaT(wxp, Yv[2][yc][zc], t);
             const int j = 2 * J + yc;
             const int k = Z2 ? 2 * K + zc : K;
             const int base = (j + n1 * k) * hn0 + I;
             const int c0 = (yc + zc) & 1;   // colour of child 2I (2I+2J+2K is even)
-            u[c0 * F.half + base] += v0;
-            u[(c0 ^ 1) * F.half + base] += v1;
+            if (BLACK_ONLY) {
+                // the colour-1 child: 2I when c0 == 1, else 2I+1
+                const T v = c0 ? fmaT(wxm, Yv[0][yc][zc], t) : fmaT(wxp, Yv[2][yc][zc], t);
+                u[F.half + base] += v;
+            } else {
+                const T v0 = fmaT(wxm, Yv[0][yc][zc], t);
+                const T v1 = fmaT(wxp, Yv[2][yc][zc], t);
+                u[c0 * F.half + base] += v0;
+                u[(c0 ^ 1) * F.half + base] += v1;
+            }
         }
     }
 }
@@ -444,12 +453,20 @@ void launch_resid_restrict(const Dims& fine, const Dims& coarse, const LevelArra
 
 template <typename T>
 void launch_prolong_add(const Dims& fine, const Dims& coarse, const BcDesc& bc, const T* ec,
-                        T* phi_fine, cudaStream_t s) {
+                        T* phi_fine, bool black_only, cudaStream_t s) {
     const Grid3 g = grid3(coarse.n0, coarse.n1, coarse.n2);
-    if (fine.rz == 2)
-        k_prolong_add<T, true><<<g.grid, g.block, 0, s>>>(fine, coarse, bc, ec, phi_fine);
-    else
-        k_prolong_add<T, false><<<g.grid, g.block, 0, s>>>(fine, coarse, bc, ec, phi_fine);
+    if (fine.rz == 2) {
+        if (black_only)
+            k_prolong_add<T, true, true><<<g.grid, g.block, 0, s>>>(fine, coarse, bc, ec, phi_fine);
+        else
+            k_prolong_add<T, true, false><<<g.grid, g.block, 0, s>>>(fine, coarse, bc, ec, phi_fine);
+    } else {
+        if (black_only)
+            k_prolong_add<T, false, true><<<g.grid, g.block, 0, s>>>(fine, coarse, bc, ec, phi_fine);
+        else
+            k_prolong_add<T, false, false><<<g.grid, g.block, 0, s>>>(fine, coarse, bc, ec,
+                                                                      phi_fine);
+    }
 }
 
 template <typename T>
@@ -518,9 +535,9 @@ template void launch_resid_restrict<double>(const Dims&, const Dims&, const Leve
 template void launch_resid_restrict<float>(const Dims&, const Dims&, const LevelArrays<float>&,
                                            float*, bool, cudaStream_t);
 template void launch_prolong_add<double>(const Dims&, const Dims&, const BcDesc&, const double*,
-                                         double*, cudaStream_t);
+                                         double*, bool, cudaStream_t);
 template void launch_prolong_add<float>(const Dims&, const Dims&, const BcDesc&, const float*,
-                                        float*, cudaStream_t);
+                                         float*, bool, cudaStream_t);
 template void launch_resid_norm<double>(const Dims&, const LevelArrays<double>&, bool,
                                         unsigned long long*, cudaStream_t);
 template void launch_resid_norm<float>(const Dims&, const LevelArrays<float>&, bool,

@@ -194,7 +194,8 @@ void vcycle(mac_ctx* c, int l) {
     cudaMemsetAsync(ac.phi, 0, sizeof(T) * C.d.ncell, c->stream);
     vcycle<T>(c, l + 1);
     mark(c, tm, 3);
-    launch_prolong_add<T>(L.d, C.d, bc_desc(c), ac.phi, a.phi, c->stream);
+    // with post-smoothing, only colour-1 cells need the correction (see k_prolong_add)
+    launch_prolong_add<T>(L.d, C.d, bc_desc(c), ac.phi, a.phi, o.nu2 > 0, c->stream);
     ++c->issued;
     mark(c, tm, 4);
     for (int s = 0; s < o.nu2; ++s) sweep();

@@ -136,9 +136,10 @@ __device__ __forceinline__ void nb_w(int q, int n, int blo, int bhi, int& qm, in
 }
 
 // e_fine += trilinear interpolation of the coarse correction ec (natural, cn0 x cn1 x cn2)
+// black_only: colour-1 children only (post-smoothing follows; see k_prolong_add)
 template <typename T>
 __device__ __noinline__ void tail_prolong(const TailLevel<T>& F, const T* ec, int cn0, int cn1, int cn2,
-                             const BcDesc& bc) {
+                             const BcDesc& bc, bool black_only) {
     const bool z2 = F.rz == 2;
     const Lanes ln = lanes(cn0);
     const int rows = cn1 * cn2;
@@ -178,13 +179,12 @@ __device__ __noinline__ void tail_prolong(const TailLevel<T>& F, const T* ec, in
         for (int zc = 0; zc < (z2 ? 2 : 1); ++zc) {
             for (int yc = 0; yc < 2; ++yc) {
                 const T t = T(0.75) * Yv[1][yc][zc];
-                const T v0 = fmaT2(wxm, Yv[0][yc][zc], t);
-                const T v1 = fmaT2(wxp, Yv[2][yc][zc], t);
                 const int j = 2 * J + yc;
                 const int k = z2 ? 2 * K + zc : K;
                 const int base = F.n0 * (j + F.n1 * k) + 2 * I;
-                F.e[base] += v0;
-                F.e[base + 1] += v1;
+                const int c0 = (yc + zc) & 1;   // colour of child 2I
+                if (!black_only || c0) F.e[base] += fmaT2(wxm, Yv[0][yc][zc], t);
+                if (!black_only || !c0) F.e[base + 1] += fmaT2(wxp, Yv[2][yc][zc], t);
             }
         }
     }
@@ -324,9 +324,10 @@ k_tail(TailParams<T> P) {
     // up the V
     for (int l = nl - 1; l >= 0; --l) {
         if (l + 1 < nl)
-            tail_prolong<T>(L[l], L[l + 1].e, L[l + 1].n0, L[l + 1].n1, L[l + 1].n2, P.bc);
+            tail_prolong<T>(L[l], L[l + 1].e, L[l + 1].n0, L[l + 1].n1, L[l + 1].n2, P.bc,
+                            P.nu2 > 0);
         else
-            tail_prolong<T>(L[l], eb, BD.n0, BD.n1, BD.n2, P.bc);
+            tail_prolong<T>(L[l], eb, BD.n0, BD.n1, BD.n2, P.bc, P.nu2 > 0);
         for (int s = 0; s < P.nu2; ++s) tail_sweep<T>(L[l]);
     }
     // hand the correction of the first tail level back (its split layout)
