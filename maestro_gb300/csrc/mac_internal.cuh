@@ -26,6 +26,7 @@
 #include <cstdint>
 #include <cstring>
 #include <functional>
+#include <utility>
 #include <vector>
 
 #include "maestro_mac.h"
@@ -258,7 +259,7 @@ template <typename T>
 void launch_gsrb(const Dims& d, int colour, LevelArrays<T>& a, cudaStream_t s);
 template <typename T>
 void launch_resid_restrict(const Dims& fine, const Dims& coarse, const LevelArrays<T>& a,
-                           T* fc, bool red_only, cudaStream_t s);
+                           T* fc, T* ec, bool red_only, cudaStream_t s);
 template <typename T>
 void launch_prolong_add(const Dims& fine, const Dims& coarse, const BcDesc& bc, const T* ec,
                         T* phi_fine, bool black_only, cudaStream_t s);
@@ -272,8 +273,8 @@ void launch_accumulate(const Dims& d, double* phi, const float* e, cudaStream_t 
 void launch_gsrb_otf(const Dims& d, const OtfParams& P, int colour, float* e, const float* r,
                      cudaStream_t s);
 void launch_resid_restrict_otf(const Dims& fine, const Dims& coarse, const OtfParams& P,
-                               const float* e, const float* r, float* fc, bool red_only,
-                               cudaStream_t s);
+                               const float* e, const float* r, float* fc, float* ec,
+                               bool red_only, cudaStream_t s);
 
 template <typename Tio>
 void launch_bottom(const Dims& d, const LevelArrays<double>& a64, Tio* x, const Tio* f,
@@ -362,6 +363,19 @@ void end_call_stats(mac_ctx* c, mac_stats* st);
 int alloc_device(mac_ctx* c, void** p, size_t bytes);
 
 inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
+
+// Kernel launch through cudaLaunchKernelEx with no attributes (the same as <<<>>>), so launch sites
+// read alike whatever the argument count.
+template <typename... KArgs, typename... Args>
+inline void launch_plain(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                         cudaStream_t s, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 // 3-D launch over an (nx, ny, nz) index space (x fastest): 128-thread blocks of (bx, 128/bx)
 // with bx the smallest power of two >= nx, at most 128; z = blockIdx.z.  Kernels recover their

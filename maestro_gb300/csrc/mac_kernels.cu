@@ -173,7 +173,7 @@ template <typename T, bool RED_ONLY>
 __global__ void __launch_bounds__(kBlock)
 k_resid_restrict(Dims F, Dims C, const T* __restrict__ u, const T* __restrict__ f,
                  const T* __restrict__ bx, const T* __restrict__ by, const T* __restrict__ bz,
-                 const T* __restrict__ dg, T* __restrict__ fc) {
+                 const T* __restrict__ dg, T* __restrict__ fc, T* __restrict__ ec) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
     const int K = blockIdx.z;
@@ -203,6 +203,7 @@ k_resid_restrict(Dims F, Dims C, const T* __restrict__ u, const T* __restrict__ 
     else
         ci = I + C.n0 * (J + C.n1 * K);
     fc[ci] = sum * (T)(1.0 / (4 * F.rz));
+    ec[ci] = T(0);   // the coarse correction starts from zero (no separate memset in the chain)
 }
 
 // ---- prolongation: u_fine += (bi/tri)linear interpolation of the coarse correction ----------
@@ -427,28 +428,34 @@ void launch_gsrb(const Dims& d, int colour, LevelArrays<T>& a, cudaStream_t s) {
         // four cells a thread pays off on large levels; small ones want more threads in flight
         if (d.hn0 % 4 == 0 && d.half >= (1 << 19)) {
             const Grid3 g4 = grid3(d.hn0 / 4, d.n1, d.n2);
-            k_gsrb4<<<g4.grid, g4.block, 0, s>>>(
-                d, colour, a.phi + own, a.phi + oth, a.f + own, a.bx + own, a.by + own,
-                a.bz + own, a.bx + oth, a.by + oth, a.bz + oth, a.invdiag + own);
+            launch_plain(k_gsrb4, g4.grid, g4.block, 0, s, d, colour, a.phi + own,
+                       (const float*)(a.phi + oth), (const float*)(a.f + own),
+                       (const float*)(a.bx + own), (const float*)(a.by + own),
+                       (const float*)(a.bz + own), (const float*)(a.bx + oth),
+                       (const float*)(a.by + oth), (const float*)(a.bz + oth),
+                       (const float*)(a.invdiag + own));
             return;
         }
     }
     const Grid3 g = grid3(d.hn0, d.n1, d.n2);
-    k_gsrb<T><<<g.grid, g.block, 0, s>>>(
-        d, colour, a.phi + own, a.phi + oth, a.f + own, a.bx + own, a.by + own, a.bz + own,
-        a.bx + oth, a.by + oth, a.bz + oth, a.invdiag + own);
+    launch_plain(k_gsrb<T>, g.grid, g.block, 0, s, d, colour, a.phi + own, (const T*)(a.phi + oth),
+               (const T*)(a.f + own), (const T*)(a.bx + own), (const T*)(a.by + own),
+               (const T*)(a.bz + own), (const T*)(a.bx + oth), (const T*)(a.by + oth),
+               (const T*)(a.bz + oth), (const T*)(a.invdiag + own));
 }
 
 template <typename T>
 void launch_resid_restrict(const Dims& fine, const Dims& coarse, const LevelArrays<T>& a, T* fc,
-                           bool red_only, cudaStream_t s) {
+                           T* ec, bool red_only, cudaStream_t s) {
     const Grid3 g = grid3(coarse.n0, coarse.n1, coarse.n2);
     if (red_only)
-        k_resid_restrict<T, true><<<g.grid, g.block, 0, s>>>(fine, coarse, a.phi, a.f, a.bx, a.by,
-                                                             a.bz, a.diag, fc);
+        launch_plain(k_resid_restrict<T, true>, g.grid, g.block, 0, s, fine, coarse,
+                   (const T*)a.phi, (const T*)a.f, (const T*)a.bx, (const T*)a.by, (const T*)a.bz,
+                   (const T*)a.diag, fc, ec);
     else
-        k_resid_restrict<T, false><<<g.grid, g.block, 0, s>>>(fine, coarse, a.phi, a.f, a.bx, a.by,
-                                                              a.bz, a.diag, fc);
+        launch_plain(k_resid_restrict<T, false>, g.grid, g.block, 0, s, fine, coarse,
+                   (const T*)a.phi, (const T*)a.f, (const T*)a.bx, (const T*)a.by, (const T*)a.bz,
+                   (const T*)a.diag, fc, ec);
 }
 
 template <typename T>
@@ -457,15 +464,18 @@ void launch_prolong_add(const Dims& fine, const Dims& coarse, const BcDesc& bc, 
     const Grid3 g = grid3(coarse.n0, coarse.n1, coarse.n2);
     if (fine.rz == 2) {
         if (black_only)
-            k_prolong_add<T, true, true><<<g.grid, g.block, 0, s>>>(fine, coarse, bc, ec, phi_fine);
+            launch_plain(k_prolong_add<T, true, true>, g.grid, g.block, 0, s, fine, coarse, bc, ec,
+                       phi_fine);
         else
-            k_prolong_add<T, true, false><<<g.grid, g.block, 0, s>>>(fine, coarse, bc, ec, phi_fine);
+            launch_plain(k_prolong_add<T, true, false>, g.grid, g.block, 0, s, fine, coarse, bc, ec,
+                       phi_fine);
     } else {
         if (black_only)
-            k_prolong_add<T, false, true><<<g.grid, g.block, 0, s>>>(fine, coarse, bc, ec, phi_fine);
+            launch_plain(k_prolong_add<T, false, true>, g.grid, g.block, 0, s, fine, coarse, bc, ec,
+                       phi_fine);
         else
-            k_prolong_add<T, false, false><<<g.grid, g.block, 0, s>>>(fine, coarse, bc, ec,
-                                                                      phi_fine);
+            launch_plain(k_prolong_add<T, false, false>, g.grid, g.block, 0, s, fine, coarse, bc, ec,
+                       phi_fine);
     }
 }
 
@@ -474,21 +484,25 @@ void launch_resid_norm(const Dims& d, const LevelArrays<T>& a, bool red_only,
                        unsigned long long* maxbits, cudaStream_t s) {
     const Grid3 g = grid3(d.hn0, d.n1, d.n2);
     if (red_only)
-        k_resid_norm<T, true><<<g.grid, g.block, 0, s>>>(d, a.phi, a.f, a.bx, a.by, a.bz, a.diag,
-                                                         maxbits);
+        launch_plain(k_resid_norm<T, true>, g.grid, g.block, 0, s, d, (const T*)a.phi,
+                   (const T*)a.f, (const T*)a.bx, (const T*)a.by, (const T*)a.bz,
+                   (const T*)a.diag, maxbits);
     else
-        k_resid_norm<T, false><<<g.grid, g.block, 0, s>>>(d, a.phi, a.f, a.bx, a.by, a.bz, a.diag,
-                                                          maxbits);
+        launch_plain(k_resid_norm<T, false>, g.grid, g.block, 0, s, d, (const T*)a.phi,
+                   (const T*)a.f, (const T*)a.bx, (const T*)a.by, (const T*)a.bz,
+                   (const T*)a.diag, maxbits);
 }
 
 void launch_resid64_to32(const Dims& d, const LevelArrays<double>& a, float* r32,
                          unsigned long long* maxbits, cudaStream_t s) {
     const Grid3 g = grid3(d.hn0, d.n1, d.n2);
-    k_resid64_to32<<<g.grid, g.block, 0, s>>>(d, a.phi, a.f, a.bx, a.by, a.bz, a.diag, r32, maxbits);
+    launch_plain(k_resid64_to32, g.grid, g.block, 0, s, d, (const double*)a.phi,
+               (const double*)a.f, (const double*)a.bx, (const double*)a.by, (const double*)a.bz,
+               (const double*)a.diag, r32, maxbits);
 }
 
 void launch_accumulate(const Dims& d, double* phi, const float* e, cudaStream_t s) {
-    k_accumulate<<<ceil_div(d.ncell, kBlock), kBlock, 0, s>>>(d.ncell, phi, e);
+    launch_plain(k_accumulate, dim3(ceil_div(d.ncell, kBlock)), dim3(kBlock), 0, s, d.ncell, phi, e);
 }
 
 template <typename Tio>
@@ -509,11 +523,11 @@ void launch_bottom(const Dims& d, const LevelArrays<double>& a64, Tio* x, const 
     // CTA on global scratch
     const size_t smem = (size_t)(7 + kBotScrPerCell) * d.ncell * sizeof(double);
     if (d.ncell <= kBottomSmemCells)
-        k_bottom<Tio, true><<<1, 128, smem, s>>>(v, x, f, scratch, singular ? 1 : 0, nub, eps,
-                                                 max_iter, iter_counter);
+        launch_plain(k_bottom<Tio, true>, dim3(1), dim3(128), smem, s, v, x, f, scratch,
+                   singular ? 1 : 0, nub, eps, max_iter, iter_counter);
     else
-        k_bottom<Tio, false><<<1, kBottomThreads, 0, s>>>(v, x, f, scratch, singular ? 1 : 0, nub,
-                                                          eps, max_iter, iter_counter);
+        launch_plain(k_bottom<Tio, false>, dim3(1), dim3(kBottomThreads), 0, s, v, x, f, scratch,
+                   singular ? 1 : 0, nub, eps, max_iter, iter_counter);
 }
 
 // Opt the shared-memory bottom solver into more than 48 KB of dynamic shared memory (called once
@@ -531,9 +545,9 @@ int prepare_kernels() {
 template void launch_gsrb<double>(const Dims&, int, LevelArrays<double>&, cudaStream_t);
 template void launch_gsrb<float>(const Dims&, int, LevelArrays<float>&, cudaStream_t);
 template void launch_resid_restrict<double>(const Dims&, const Dims&, const LevelArrays<double>&,
-                                            double*, bool, cudaStream_t);
+                                            double*, double*, bool, cudaStream_t);
 template void launch_resid_restrict<float>(const Dims&, const Dims&, const LevelArrays<float>&,
-                                           float*, bool, cudaStream_t);
+                                            float*, float*, bool, cudaStream_t);
 template void launch_prolong_add<double>(const Dims&, const Dims&, const BcDesc&, const double*,
                                          double*, bool, cudaStream_t);
 template void launch_prolong_add<float>(const Dims&, const Dims&, const BcDesc&, const float*,

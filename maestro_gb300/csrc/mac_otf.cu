@@ -413,7 +413,7 @@ k_gsrb_otf_staged(Dims d, OtfParams P, int colour, float* __restrict__ es,
 template <int DM, bool RED_ONLY>
 __global__ void __launch_bounds__(kB)
 k_resid_restrict_otf(Dims F, Dims C, OtfParams P, const float* __restrict__ e,
-                     const float* __restrict__ r, float* __restrict__ fc) {
+                     const float* __restrict__ r, float* __restrict__ fc, float* __restrict__ ec) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
     const int K = blockIdx.z;
@@ -445,6 +445,7 @@ k_resid_restrict_otf(Dims F, Dims C, OtfParams P, const float* __restrict__ e,
     else
         ci = I + C.n0 * (J + C.n1 * K);
     fc[ci] = sum * (DM == 3 ? 0.125f : 0.25f);
+    ec[ci] = 0.f;   // the coarse correction starts from zero (no separate memset in the chain)
 }
 
 }  // namespace
@@ -457,18 +458,18 @@ void launch_gsrb_otf(const Dims& d, const OtfParams& P, int colour, float* e, co
         const dim3 grid(d.n1 / P.ty, P.nz);
         const int nt = P.ty * d.hn0 / kCellsPerThread;
         if (P.has_dir)
-            k_gsrb_otf_staged<true><<<grid, nt, P.smem, s>>>(d, P, colour, e + own, e + oth,
-                                                             r + own, P.rho + own, P.rho + oth);
+            launch_plain(k_gsrb_otf_staged<true>, grid, dim3(nt), (size_t)P.smem, s, d, P, colour,
+                       e + own, (const float*)(e + oth), r + own, P.rho + own, P.rho + oth);
         else
-            k_gsrb_otf_staged<false><<<grid, nt, P.smem, s>>>(d, P, colour, e + own, e + oth,
-                                                              r + own, P.rho + own, P.rho + oth);
+            launch_plain(k_gsrb_otf_staged<false>, grid, dim3(nt), (size_t)P.smem, s, d, P, colour,
+                       e + own, (const float*)(e + oth), r + own, P.rho + own, P.rho + oth);
     }
     else if (P.dm == 3)
-        k_gsrb_otf<3><<<g.grid, g.block, 0, s>>>(d, P, colour, e + own, e + oth, r + own,
-                                                 P.rho + own, P.rho + oth);
+        launch_plain(k_gsrb_otf<3>, g.grid, g.block, 0, s, d, P, colour, e + own,
+                   (const float*)(e + oth), r + own, P.rho + own, P.rho + oth);
     else
-        k_gsrb_otf<2><<<g.grid, g.block, 0, s>>>(d, P, colour, e + own, e + oth, r + own,
-                                                 P.rho + own, P.rho + oth);
+        launch_plain(k_gsrb_otf<2>, g.grid, g.block, 0, s, d, P, colour, e + own,
+                   (const float*)(e + oth), r + own, P.rho + own, P.rho + oth);
 }
 
 // Tile plan of the staged half-sweep: ty = the largest power of two with ty * hn0 <= 1024 cells
@@ -521,19 +522,23 @@ void plan_otf_tile(const Dims& d, int dm, int sms, OtfParams& P) {
 }
 
 void launch_resid_restrict_otf(const Dims& fine, const Dims& coarse, const OtfParams& P,
-                               const float* e, const float* r, float* fc, bool red_only,
-                               cudaStream_t s) {
+                               const float* e, const float* r, float* fc, float* ec,
+                               bool red_only, cudaStream_t s) {
     const Grid3 g = grid3(coarse.n0, coarse.n1, coarse.n2);
     if (P.dm == 3) {
         if (red_only)
-            k_resid_restrict_otf<3, true><<<g.grid, g.block, 0, s>>>(fine, coarse, P, e, r, fc);
+            launch_plain(k_resid_restrict_otf<3, true>, g.grid, g.block, 0, s, fine, coarse, P, e, r,
+                       fc, ec);
         else
-            k_resid_restrict_otf<3, false><<<g.grid, g.block, 0, s>>>(fine, coarse, P, e, r, fc);
+            launch_plain(k_resid_restrict_otf<3, false>, g.grid, g.block, 0, s, fine, coarse, P, e,
+                       r, fc, ec);
     } else {
         if (red_only)
-            k_resid_restrict_otf<2, true><<<g.grid, g.block, 0, s>>>(fine, coarse, P, e, r, fc);
+            launch_plain(k_resid_restrict_otf<2, true>, g.grid, g.block, 0, s, fine, coarse, P, e, r,
+                       fc, ec);
         else
-            k_resid_restrict_otf<2, false><<<g.grid, g.block, 0, s>>>(fine, coarse, P, e, r, fc);
+            launch_plain(k_resid_restrict_otf<2, false>, g.grid, g.block, 0, s, fine, coarse, P, e,
+                       r, fc, ec);
     }
 }
 

@@ -186,12 +186,12 @@ void vcycle(mac_ctx* c, int l) {
     if (otf)
         launch_resid_restrict_otf(L.d, C.d, P, reinterpret_cast<const float*>(a.phi),
                                   reinterpret_cast<const float*>(a.f),
-                                  reinterpret_cast<float*>(ac.f), o.nu1 > 0, c->stream);
+                                  reinterpret_cast<float*>(ac.f), reinterpret_cast<float*>(ac.phi),
+                                  o.nu1 > 0, c->stream);
     else
-        launch_resid_restrict<T>(L.d, C.d, a, ac.f, o.nu1 > 0, c->stream);
+        launch_resid_restrict<T>(L.d, C.d, a, ac.f, ac.phi, o.nu1 > 0, c->stream);
     ++c->issued;
-    mark(c, tm, 2);
-    cudaMemsetAsync(ac.phi, 0, sizeof(T) * C.d.ncell, c->stream);
+    mark(c, tm, 2);   // (the restriction also zeroed the coarse correction ac.phi)
     vcycle<T>(c, l + 1);
     mark(c, tm, 3);
     // with post-smoothing, only colour-1 cells need the correction (see k_prolong_add)

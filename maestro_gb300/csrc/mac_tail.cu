@@ -348,7 +348,7 @@ size_t tail_smem_bytes(const Dims* lev, int nl, const Dims& bottom) {
 
 template <typename T>
 void launch_tail(const TailParams<T>& P, size_t smem, cudaStream_t s) {
-    k_tail<T><<<1, kTailThreads, smem, s>>>(P);
+    launch_plain(k_tail<T>, dim3(1), dim3(kTailThreads), smem, s, P);
 }
 
 int prepare_tail_kernels() {
