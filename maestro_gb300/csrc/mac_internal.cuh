@@ -364,16 +364,29 @@ int alloc_device(mac_ctx* c, void** p, size_t bytes);
 
 inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
 
-// Kernel launch through cudaLaunchKernelEx with no attributes (the same as <<<>>>), so launch sites
-// read alike whatever the argument count.
+// ---- kernel launch of the V-cycle chain ---------------------------------------------------------
+// The kernels of one outer iteration form a chain on one stream.  They are launched with
+// programmatic stream serialisation: a kernel's grid is scheduled while its predecessor drains.
+// Every chain kernel starts with pdl_wait() (returns once the predecessor has completed and its
+// writes are visible; no global access comes before it) followed by pdl_trigger() (lets the next
+// kernel be scheduled).  Both are no-ops for a kernel launched without the attribute.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
 template <typename... KArgs, typename... Args>
-inline void launch_plain(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+inline void launch_chain(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
                          cudaStream_t s, Args&&... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
     cfg.blockDim = block;
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
     cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
 }
 

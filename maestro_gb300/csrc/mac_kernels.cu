@@ -90,6 +90,8 @@ k_gsrb(Dims d, int colour, T* __restrict__ us, const T* __restrict__ uo, const T
        const T* __restrict__ bxs, const T* __restrict__ bys, const T* __restrict__ bzs,
        const T* __restrict__ bxo, const T* __restrict__ byo, const T* __restrict__ bzo,
        const T* __restrict__ ids) {
+    pdl_wait();
+    pdl_trigger();
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
@@ -116,6 +118,8 @@ k_gsrb4(Dims d, int colour, float* __restrict__ us, const float* __restrict__ uo
         const float* __restrict__ bzs, const float* __restrict__ bxo,
         const float* __restrict__ byo, const float* __restrict__ bzo,
         const float* __restrict__ ids) {
+    pdl_wait();
+    pdl_trigger();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
@@ -174,6 +178,8 @@ __global__ void __launch_bounds__(kBlock)
 k_resid_restrict(Dims F, Dims C, const T* __restrict__ u, const T* __restrict__ f,
                  const T* __restrict__ bx, const T* __restrict__ by, const T* __restrict__ bz,
                  const T* __restrict__ dg, T* __restrict__ fc, T* __restrict__ ec) {
+    pdl_wait();
+    pdl_trigger();
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
     const int K = blockIdx.z;
@@ -240,6 +246,8 @@ __device__ __forceinline__ void coarse_nb(int q, int n, int blo, int bhi, int& q
 template <typename T, bool Z2, bool BLACK_ONLY>
 __global__ void __launch_bounds__(kBlock)
 k_prolong_add(Dims F, Dims C, BcDesc bc, const T* __restrict__ ec, T* __restrict__ u) {
+    pdl_wait();
+    pdl_trigger();
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
     const int K = blockIdx.z;
@@ -312,6 +320,8 @@ __global__ void __launch_bounds__(kBlock)
 k_resid_norm(Dims F, const T* __restrict__ u, const T* __restrict__ f, const T* __restrict__ bx,
              const T* __restrict__ by, const T* __restrict__ bz, const T* __restrict__ dg,
              unsigned long long* __restrict__ maxbits) {
+    pdl_wait();
+    pdl_trigger();
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
@@ -340,6 +350,8 @@ k_resid64_to32(Dims F, const double* __restrict__ u, const double* __restrict__ 
                const double* __restrict__ bx, const double* __restrict__ by,
                const double* __restrict__ bz, const double* __restrict__ dg,
                float* __restrict__ r32, unsigned long long* __restrict__ maxbits) {
+    pdl_wait();
+    pdl_trigger();
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
@@ -365,6 +377,8 @@ k_resid64_to32(Dims F, const double* __restrict__ u, const double* __restrict__ 
 
 __global__ void __launch_bounds__(kBlock)
 k_accumulate(int n, double* __restrict__ u, const float* __restrict__ e) {
+    pdl_wait();
+    pdl_trigger();
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q < n) u[q] += (double)e[q];
 }
@@ -379,6 +393,8 @@ template <typename Tio, bool SMEM>
 __global__ void __launch_bounds__(kBottomThreads)
 k_bottom(BotView vin, Tio* __restrict__ xio, const Tio* __restrict__ fio, double* __restrict__ gscr,
          int singular, int nub, double eps, int max_iter, int* __restrict__ iters) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double sm[33];
     extern __shared__ double dsm[];
     const int N = vin.N;
@@ -428,7 +444,7 @@ void launch_gsrb(const Dims& d, int colour, LevelArrays<T>& a, cudaStream_t s) {
         // four cells a thread pays off on large levels; small ones want more threads in flight
         if (d.hn0 % 4 == 0 && d.half >= (1 << 19)) {
             const Grid3 g4 = grid3(d.hn0 / 4, d.n1, d.n2);
-            launch_plain(k_gsrb4, g4.grid, g4.block, 0, s, d, colour, a.phi + own,
+            launch_chain(k_gsrb4, g4.grid, g4.block, 0, s, d, colour, a.phi + own,
                        (const float*)(a.phi + oth), (const float*)(a.f + own),
                        (const float*)(a.bx + own), (const float*)(a.by + own),
                        (const float*)(a.bz + own), (const float*)(a.bx + oth),
@@ -438,7 +454,7 @@ void launch_gsrb(const Dims& d, int colour, LevelArrays<T>& a, cudaStream_t s) {
         }
     }
     const Grid3 g = grid3(d.hn0, d.n1, d.n2);
-    launch_plain(k_gsrb<T>, g.grid, g.block, 0, s, d, colour, a.phi + own, (const T*)(a.phi + oth),
+    launch_chain(k_gsrb<T>, g.grid, g.block, 0, s, d, colour, a.phi + own, (const T*)(a.phi + oth),
                (const T*)(a.f + own), (const T*)(a.bx + own), (const T*)(a.by + own),
                (const T*)(a.bz + own), (const T*)(a.bx + oth), (const T*)(a.by + oth),
                (const T*)(a.bz + oth), (const T*)(a.invdiag + own));
@@ -449,11 +465,11 @@ void launch_resid_restrict(const Dims& fine, const Dims& coarse, const LevelArra
                            T* ec, bool red_only, cudaStream_t s) {
     const Grid3 g = grid3(coarse.n0, coarse.n1, coarse.n2);
     if (red_only)
-        launch_plain(k_resid_restrict<T, true>, g.grid, g.block, 0, s, fine, coarse,
+        launch_chain(k_resid_restrict<T, true>, g.grid, g.block, 0, s, fine, coarse,
                    (const T*)a.phi, (const T*)a.f, (const T*)a.bx, (const T*)a.by, (const T*)a.bz,
                    (const T*)a.diag, fc, ec);
     else
-        launch_plain(k_resid_restrict<T, false>, g.grid, g.block, 0, s, fine, coarse,
+        launch_chain(k_resid_restrict<T, false>, g.grid, g.block, 0, s, fine, coarse,
                    (const T*)a.phi, (const T*)a.f, (const T*)a.bx, (const T*)a.by, (const T*)a.bz,
                    (const T*)a.diag, fc, ec);
 }
@@ -464,17 +480,17 @@ void launch_prolong_add(const Dims& fine, const Dims& coarse, const BcDesc& bc, 
     const Grid3 g = grid3(coarse.n0, coarse.n1, coarse.n2);
     if (fine.rz == 2) {
         if (black_only)
-            launch_plain(k_prolong_add<T, true, true>, g.grid, g.block, 0, s, fine, coarse, bc, ec,
+            launch_chain(k_prolong_add<T, true, true>, g.grid, g.block, 0, s, fine, coarse, bc, ec,
                        phi_fine);
         else
-            launch_plain(k_prolong_add<T, true, false>, g.grid, g.block, 0, s, fine, coarse, bc, ec,
+            launch_chain(k_prolong_add<T, true, false>, g.grid, g.block, 0, s, fine, coarse, bc, ec,
                        phi_fine);
     } else {
         if (black_only)
-            launch_plain(k_prolong_add<T, false, true>, g.grid, g.block, 0, s, fine, coarse, bc, ec,
+            launch_chain(k_prolong_add<T, false, true>, g.grid, g.block, 0, s, fine, coarse, bc, ec,
                        phi_fine);
         else
-            launch_plain(k_prolong_add<T, false, false>, g.grid, g.block, 0, s, fine, coarse, bc, ec,
+            launch_chain(k_prolong_add<T, false, false>, g.grid, g.block, 0, s, fine, coarse, bc, ec,
                        phi_fine);
     }
 }
@@ -484,11 +500,11 @@ void launch_resid_norm(const Dims& d, const LevelArrays<T>& a, bool red_only,
                        unsigned long long* maxbits, cudaStream_t s) {
     const Grid3 g = grid3(d.hn0, d.n1, d.n2);
     if (red_only)
-        launch_plain(k_resid_norm<T, true>, g.grid, g.block, 0, s, d, (const T*)a.phi,
+        launch_chain(k_resid_norm<T, true>, g.grid, g.block, 0, s, d, (const T*)a.phi,
                    (const T*)a.f, (const T*)a.bx, (const T*)a.by, (const T*)a.bz,
                    (const T*)a.diag, maxbits);
     else
-        launch_plain(k_resid_norm<T, false>, g.grid, g.block, 0, s, d, (const T*)a.phi,
+        launch_chain(k_resid_norm<T, false>, g.grid, g.block, 0, s, d, (const T*)a.phi,
                    (const T*)a.f, (const T*)a.bx, (const T*)a.by, (const T*)a.bz,
                    (const T*)a.diag, maxbits);
 }
@@ -496,13 +512,13 @@ void launch_resid_norm(const Dims& d, const LevelArrays<T>& a, bool red_only,
 void launch_resid64_to32(const Dims& d, const LevelArrays<double>& a, float* r32,
                          unsigned long long* maxbits, cudaStream_t s) {
     const Grid3 g = grid3(d.hn0, d.n1, d.n2);
-    launch_plain(k_resid64_to32, g.grid, g.block, 0, s, d, (const double*)a.phi,
+    launch_chain(k_resid64_to32, g.grid, g.block, 0, s, d, (const double*)a.phi,
                (const double*)a.f, (const double*)a.bx, (const double*)a.by, (const double*)a.bz,
                (const double*)a.diag, r32, maxbits);
 }
 
 void launch_accumulate(const Dims& d, double* phi, const float* e, cudaStream_t s) {
-    launch_plain(k_accumulate, dim3(ceil_div(d.ncell, kBlock)), dim3(kBlock), 0, s, d.ncell, phi, e);
+    launch_chain(k_accumulate, dim3(ceil_div(d.ncell, kBlock)), dim3(kBlock), 0, s, d.ncell, phi, e);
 }
 
 template <typename Tio>
@@ -523,10 +539,10 @@ void launch_bottom(const Dims& d, const LevelArrays<double>& a64, Tio* x, const 
     // CTA on global scratch
     const size_t smem = (size_t)(7 + kBotScrPerCell) * d.ncell * sizeof(double);
     if (d.ncell <= kBottomSmemCells)
-        launch_plain(k_bottom<Tio, true>, dim3(1), dim3(128), smem, s, v, x, f, scratch,
+        launch_chain(k_bottom<Tio, true>, dim3(1), dim3(128), smem, s, v, x, f, scratch,
                    singular ? 1 : 0, nub, eps, max_iter, iter_counter);
     else
-        launch_plain(k_bottom<Tio, false>, dim3(1), dim3(kBottomThreads), 0, s, v, x, f, scratch,
+        launch_chain(k_bottom<Tio, false>, dim3(1), dim3(kBottomThreads), 0, s, v, x, f, scratch,
                    singular ? 1 : 0, nub, eps, max_iter, iter_counter);
 }
 

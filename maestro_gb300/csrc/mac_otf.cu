@@ -108,6 +108,8 @@ __global__ void __launch_bounds__(kB)
 k_gsrb_otf(Dims d, OtfParams P, int colour, float* __restrict__ es, const float* __restrict__ eo,
            const float* __restrict__ rs, const float* __restrict__ rhos,
            const float* __restrict__ rhoo) {
+    pdl_wait();
+    pdl_trigger();
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
@@ -292,6 +294,8 @@ k_gsrb_otf_staged(Dims d, OtfParams P, int colour, float* __restrict__ es,
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
+    pdl_wait();
+    pdl_trigger();
 
     // thread 0: copy plane q into stage q % kStages
     auto issue = [&](int q) {
@@ -414,6 +418,8 @@ template <int DM, bool RED_ONLY>
 __global__ void __launch_bounds__(kB)
 k_resid_restrict_otf(Dims F, Dims C, OtfParams P, const float* __restrict__ e,
                      const float* __restrict__ r, float* __restrict__ fc, float* __restrict__ ec) {
+    pdl_wait();
+    pdl_trigger();
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
     const int K = blockIdx.z;
@@ -458,17 +464,17 @@ void launch_gsrb_otf(const Dims& d, const OtfParams& P, int colour, float* e, co
         const dim3 grid(d.n1 / P.ty, P.nz);
         const int nt = P.ty * d.hn0 / kCellsPerThread;
         if (P.has_dir)
-            launch_plain(k_gsrb_otf_staged<true>, grid, dim3(nt), (size_t)P.smem, s, d, P, colour,
+            launch_chain(k_gsrb_otf_staged<true>, grid, dim3(nt), (size_t)P.smem, s, d, P, colour,
                        e + own, (const float*)(e + oth), r + own, P.rho + own, P.rho + oth);
         else
-            launch_plain(k_gsrb_otf_staged<false>, grid, dim3(nt), (size_t)P.smem, s, d, P, colour,
+            launch_chain(k_gsrb_otf_staged<false>, grid, dim3(nt), (size_t)P.smem, s, d, P, colour,
                        e + own, (const float*)(e + oth), r + own, P.rho + own, P.rho + oth);
     }
     else if (P.dm == 3)
-        launch_plain(k_gsrb_otf<3>, g.grid, g.block, 0, s, d, P, colour, e + own,
+        launch_chain(k_gsrb_otf<3>, g.grid, g.block, 0, s, d, P, colour, e + own,
                    (const float*)(e + oth), r + own, P.rho + own, P.rho + oth);
     else
-        launch_plain(k_gsrb_otf<2>, g.grid, g.block, 0, s, d, P, colour, e + own,
+        launch_chain(k_gsrb_otf<2>, g.grid, g.block, 0, s, d, P, colour, e + own,
                    (const float*)(e + oth), r + own, P.rho + own, P.rho + oth);
 }
 
@@ -527,17 +533,17 @@ void launch_resid_restrict_otf(const Dims& fine, const Dims& coarse, const OtfPa
     const Grid3 g = grid3(coarse.n0, coarse.n1, coarse.n2);
     if (P.dm == 3) {
         if (red_only)
-            launch_plain(k_resid_restrict_otf<3, true>, g.grid, g.block, 0, s, fine, coarse, P, e, r,
+            launch_chain(k_resid_restrict_otf<3, true>, g.grid, g.block, 0, s, fine, coarse, P, e, r,
                        fc, ec);
         else
-            launch_plain(k_resid_restrict_otf<3, false>, g.grid, g.block, 0, s, fine, coarse, P, e,
+            launch_chain(k_resid_restrict_otf<3, false>, g.grid, g.block, 0, s, fine, coarse, P, e,
                        r, fc, ec);
     } else {
         if (red_only)
-            launch_plain(k_resid_restrict_otf<2, true>, g.grid, g.block, 0, s, fine, coarse, P, e, r,
+            launch_chain(k_resid_restrict_otf<2, true>, g.grid, g.block, 0, s, fine, coarse, P, e, r,
                        fc, ec);
         else
-            launch_plain(k_resid_restrict_otf<2, false>, g.grid, g.block, 0, s, fine, coarse, P, e,
+            launch_chain(k_resid_restrict_otf<2, false>, g.grid, g.block, 0, s, fine, coarse, P, e,
                        r, fc, ec);
     }
 }

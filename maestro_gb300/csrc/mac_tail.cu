@@ -236,6 +236,8 @@ __global__ void __launch_bounds__(kTailThreads)
 k_tail(TailParams<T> P) {
     extern __shared__ __align__(16) unsigned char tail_smem[];
     const int tid = threadIdx.x, nt = blockDim.x;
+    pdl_wait();
+    pdl_trigger();
     const int nl = P.nlev;   // non-bottom tail levels
     TailLevel<T> L[kTailMaxLevels];
     // carve shared memory: per non-bottom level 7 arrays of T, then the bottom's operator (5 N),
@@ -348,7 +350,7 @@ size_t tail_smem_bytes(const Dims* lev, int nl, const Dims& bottom) {
 
 template <typename T>
 void launch_tail(const TailParams<T>& P, size_t smem, cudaStream_t s) {
-    launch_plain(k_tail<T>, dim3(1), dim3(kTailThreads), smem, s, P);
+    launch_chain(k_tail<T>, dim3(1), dim3(kTailThreads), smem, s, P);
 }
 
 int prepare_tail_kernels() {
