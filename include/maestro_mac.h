@@ -256,6 +256,41 @@ int mac_solve_small_noalloc(int dm, const int* n, const double* dx, const int* b
 /* beta0 cell -> edge values (Source/cell_to_edge.f90:14-70), host arrays, one level. */
 int mac_cell_to_edge(int nr, const double* s0_cell, double* s0_edge);
 
+/* ---- producers of the projection's inputs (planar geometry) ----------------------------------
+ * mac_make_macrhs replaces make_macrhs (Source/make_macrhs.f90:28-107; 2-D :135-178, 3-D
+ * :184-240) for one level:
+ *   macrhs = beta0(r) (S_cc - Sbar(r) + delta_gamma1_term)             r = vertical index
+ *   if dpdt_factor > 0: delta_chi = 0 first when is_predictor; below the base cutoff
+ *   (r < base_cutoff_density_coord) delta_chi += dpdt_factor delta_p_term / (dt gamma1bar(r)
+ *   p0(r)) and macrhs += beta0(r) delta_chi.
+ * Per-box fabs (host or device pointers, one component each); Sbar, beta0, gamma1bar, p0 are the
+ * 1-D base state (nr values, same pointer kind).  gamma1bar, p0, delta_p_term and delta_chi may be
+ * NULL when dpdt_factor <= 0.  Difference from the reference: ghost cells of macrhs and
+ * delta_chi are filled from their valid images (periodic / neighbouring boxes) instead of being
+ * left untouched; ghosts outside non-periodic walls are left untouched. */
+int mac_make_macrhs(mac_ctx* ctx, int ptr_kind, double* const* macrhs, int ng_rh,
+                    const double* const* S_cc, int ng_sr, const double* const* delta_gamma1_term,
+                    int ng_dg, const double* Sbar, const double* beta0, const double* gamma1bar,
+                    const double* p0, const double* const* delta_p_term, int ng_dp,
+                    double* const* delta_chi, int ng_d, double dt, double dpdt_factor,
+                    int base_cutoff_density_coord, int is_predictor);
+
+/* Whole-domain device form of mac_make_macrhs (natural layout (nx,ny[,nz]) arrays, device 1-D
+ * base state); no reference counterpart (device-resident drivers). */
+int mac_make_macrhs_dense(mac_ctx* ctx, double* macrhs, const double* S_cc,
+                          const double* delta_gamma1_term, const double* Sbar,
+                          const double* beta0, const double* gamma1bar, const double* p0,
+                          const double* delta_p_term, double* delta_chi, double dt,
+                          double dpdt_factor, int base_cutoff_density_coord, int is_predictor);
+
+/* mac_make_at_halftime replaces make_at_halftime (Source/make_at_halftime.f90:82-130) for one
+ * level: half(out_comp) = (sold(in_comp) + snew(in_comp)) / 2 on valid cells; ghost cells are
+ * filled from their valid images (the reference's ml_restrict_and_fill).  half fabs have one
+ * component (half_ncomp = 1, out_comp = 0); sold/snew have s_ncomp components. */
+int mac_make_at_halftime(mac_ctx* ctx, int ptr_kind, double* const* half, int ng_half,
+                         int out_comp, int half_ncomp, const double* const* sold, int ng_old,
+                         const double* const* snew, int ng_new, int in_comp, int s_ncomp);
+
 #ifdef __cplusplus
 }
 #endif

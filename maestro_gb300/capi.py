@@ -32,7 +32,7 @@ EXPORTED = (
     "mac_default_opts", "mac_strerror", "mac_version", "mac_ctx_create", "mac_ctx_destroy",
     "mac_ctx_set_opts", "mac_ctx_levels", "mac_macproject", "mac_multigrid",
     "mac_macproject_dense", "mac_macproject_adjoint_dense", "mac_cell_to_edge",
-    "mac_solve_small_noalloc",
+    "mac_solve_small_noalloc", "mac_make_macrhs", "mac_make_macrhs_dense", "mac_make_at_halftime",
 )
 MAC_NOALLOC_MAX_CELLS = 4096
 
@@ -169,6 +169,14 @@ def lib():
     L.mac_solve_small_noalloc.argtypes = [ctypes.c_int, ip, dp, ip, ip, vp, vp, vp, vp, vp, vp,
                                           ctypes.c_double, ctypes.c_int, vp, P(MacStats)]
     L.mac_solve_small_noalloc.restype = ctypes.c_int
+    ci, cd = ctypes.c_int, ctypes.c_double
+    L.mac_make_macrhs.argtypes = [vp, ci, dpp, ci, dpp, ci, dpp, ci, dp, dp, dp, dp, dpp, ci, dpp,
+                                  ci, cd, cd, ci, ci]
+    L.mac_make_macrhs.restype = ci
+    L.mac_make_macrhs_dense.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, cd, cd, ci, ci]
+    L.mac_make_macrhs_dense.restype = ci
+    L.mac_make_at_halftime.argtypes = [vp, ci, dpp, ci, ci, ci, dpp, ci, dpp, ci, ci, ci]
+    L.mac_make_at_halftime.restype = ci
     _lib = L
     return L
 

@@ -209,6 +209,7 @@ struct mac_ctx {
     // per vertical index r: the kTab* factor tables, (nr+1) doubles each
     double* b0tab = nullptr;
     double* scratch = nullptr;                    // generic FP64 scratch (ncell)
+    double* base1d = nullptr;                     // 4 x (nr + 1) base-state values
     // caller-layout staging (host-pointer calls): one region per array of a call, filled and
     // drained by the copy engines on the transfer stream
     double* staging = nullptr;

@@ -551,6 +551,7 @@ int ctx_alloc(mac_ctx* c) {
     rc |= alloc_arr(c, &c->rhs, N);
     rc |= alloc_arr(c, &c->phin, N);
     rc |= alloc_arr(c, &c->scratch, N);
+    rc |= alloc_arr(c, &c->base1d, (size_t)4 * (c->n[c->va] + 1));
     const int nr = c->n[c->va];
     rc |= alloc_arr(c, &c->beta0, (size_t)nr);
     rc |= alloc_arr(c, &c->beta0e, (size_t)nr + 1);

@@ -217,6 +217,34 @@ class MacProjector:
         self._check(rc, "mac_multigrid", st, strict)
         return st.as_dict()
 
+    def make_macrhs(self, macrhs, S_cc, delta_gamma1_term, Sbar, beta0, gamma1bar=None, p0=None,
+                    delta_p_term=None, delta_chi=None, dt=0.0, dpdt_factor=0.0,
+                    base_cutoff_density_coord=None, is_predictor=True, ng_rh=0, ng_sr=0, ng_dg=0,
+                    ng_dp=0, ng_d=0):
+        """Per-box make_macrhs (Source/make_macrhs.f90:28-240, planar); fills macrhs (and updates
+        delta_chi) in place.  base_cutoff_density_coord defaults to the vertical extent."""
+        nr = self.layout.n[-1]
+        cut = nr if base_cutoff_density_coord is None else int(base_cutoff_density_coord)
+        chi = dpdt_factor > 0.0
+        rc = capi.lib().mac_make_macrhs(
+            self.ctx, capi.MAC_PTR_HOST, _ptr_array(macrhs), ng_rh, _ptr_array(S_cc), ng_sr,
+            _ptr_array(delta_gamma1_term), ng_dg, _dptr(Sbar), _dptr(beta0),
+            _dptr(gamma1bar) if chi else None, _dptr(p0) if chi else None,
+            _ptr_array(delta_p_term) if chi else None, ng_dp,
+            _ptr_array(delta_chi) if chi else None, ng_d, float(dt), float(dpdt_factor), cut,
+            int(bool(is_predictor)))
+        if rc != capi.MAC_OK:
+            raise MacError(rc, "mac_make_macrhs")
+
+    def make_at_halftime(self, half, sold, snew, in_comp=0, s_ncomp=1, ng_half=1, ng_old=1,
+                         ng_new=1):
+        """Per-box make_at_halftime (Source/make_at_halftime.f90:82-130); fills half in place."""
+        rc = capi.lib().mac_make_at_halftime(
+            self.ctx, capi.MAC_PTR_HOST, _ptr_array(half), ng_half, 0, 1, _ptr_array(sold), ng_old,
+            _ptr_array(snew), ng_new, int(in_comp), int(s_ncomp))
+        if rc != capi.MAC_OK:
+            raise MacError(rc, "mac_make_at_halftime")
+
     def macproject_dense(self, ux, uy, uz, phi, rho, macrhs=None, beta0=None, beta0_edge=None,
                          strict=False):
         """Whole-domain variant on device pointers (ints, e.g. torch tensor data_ptr())."""

@@ -257,3 +257,36 @@ def cell_to_edge(s0_cell):
     e = np.zeros(c.size + 1)
     lib().orc_cell_to_edge(int(c.size), _ptr(c), _ptr(e))
     return e
+
+
+def make_macrhs(S_cc, delta_gamma1_term, Sbar, beta0, gamma1bar=None, p0=None, delta_p_term=None,
+                delta_chi=None, dt=0.0, dpdt_factor=0.0, base_cutoff_density_coord=None,
+                is_predictor=True):
+    """Planar make_macrhs on whole-domain arrays (numpy restatement).
+
+    Source/make_macrhs.f90:135-178 (2-D) and :184-240 (3-D): rhs = beta0(r) (S_cc - Sbar(r) +
+    delta_gamma1_term), r the vertical (last) index; with dpdt_factor > 0, delta_chi is zeroed on
+    a predictor call and, for r < base_cutoff_density_coord, delta_chi += dpdt_factor delta_p_term
+    / (dt gamma1bar(r) p0(r)) and rhs += beta0(r) delta_chi.  Returns (rhs, delta_chi)."""
+    S = np.asarray(S_cc, dtype=np.float64)
+    shp = [1] * S.ndim
+    shp[-1] = -1
+    col = lambda v: np.asarray(v, dtype=np.float64).reshape(shp)  # noqa: E731
+    rhs = col(beta0) * (S - col(Sbar) + np.asarray(delta_gamma1_term, dtype=np.float64))
+    chi = None if delta_chi is None else np.array(delta_chi, dtype=np.float64, order="F")
+    if dpdt_factor > 0.0:
+        nr = S.shape[-1]
+        cut = nr if base_cutoff_density_coord is None else int(base_cutoff_density_coord)
+        if is_predictor:
+            chi[...] = 0.0
+        below = (np.arange(nr) < cut).reshape(shp)
+        inc = dpdt_factor * np.asarray(delta_p_term, dtype=np.float64) / (
+            dt * col(gamma1bar) * col(p0))
+        chi = np.where(below, chi + inc, chi)
+        rhs = np.where(below, rhs + col(beta0) * chi, rhs)
+    return np.asfortranarray(rhs), (None if chi is None else np.asfortranarray(chi))
+
+
+def make_at_halftime(sold, snew):
+    """Source/make_at_halftime.f90:134-190: half = (old + new) / 2 cell by cell."""
+    return 0.5 * (np.asarray(sold, dtype=np.float64) + np.asarray(snew, dtype=np.float64))
