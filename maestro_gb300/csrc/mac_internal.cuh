@@ -174,6 +174,7 @@ struct OtfParams {
     int ty;               // rows of a tile
     int zc, nz;           // planes per block, blocks along z
     int smem;             // dynamic shared memory bytes
+    int rty, rzc, rnz, rsmem;   // the same for the staged defect + restriction (rty == 0: none)
     int* err;             // device flag: a bounded wait on a copy gave up
 };
 // Tile plan of the staged half-sweep for the finest level (OtfParams.ty/zc/nz/smem).

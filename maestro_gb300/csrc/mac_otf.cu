@@ -138,6 +138,7 @@ k_gsrb_otf(Dims d, OtfParams P, int colour, float* __restrict__ es, const float*
 // (bounded) for the copies it issued and leaves.  4 ring stages at 256^3 (ty = 8): 72 KB of
 // shared memory and 80 registers a thread, 3 blocks per SM.
 constexpr int kStages = 4;          // planes in the shared-memory ring
+constexpr int kRStages = 3;         // the same for the staged restriction (one more array a plane)
 constexpr int kCellsPerThread = 4;  // consecutive colour-half columns (one float4) per thread
 constexpr unsigned long long kWaitNs = 1000000000ull;
 
@@ -215,14 +216,15 @@ __device__ __forceinline__ void stv(float* p, const float* v) {
 // group on the side SP selects (c0 - 1 for SP = 0, c0 + V for SP = 1).  fxl0 / fxhV: x factors
 // of the group's outer low / high faces (zero on a non-periodic wall); wx0 / wxV / wmid: the
 // Dirichlet diagonal factors of the first, last and inner cells (DIR only).
-template <int V, int SP, bool DIR>
+template <int V, int SP, bool DIR, bool RES = false>
 __device__ __forceinline__ void update_group(float ex, float rx, const FV<V>& Ec, const FV<V>& Rc,
                                              const FV<V>& Eb, const FV<V>& Rb, const FV<V>& Ea,
                                              const FV<V>& Ra, const FV<V>& Eym, const FV<V>& Rym,
                                              const FV<V>& Eyp, const FV<V>& Ryp, const FV<V>& Fo,
                                              const FV<V>& Ro, float fx, float fxl0, float fxhV,
                                              float fyl, float fyh, float fzl, float fzh,
-                                             float wx0, float wxV, float wmid, float* out) {
+                                             float wx0, float wxV, float wmid, float* out,
+                                             const float* eown = nullptr) {
 #pragma unroll
     for (int m = 0; m < V; ++m) {
         const float rc = Ro.v[m];
@@ -265,7 +267,8 @@ __device__ __forceinline__ void update_group(float ex, float rx, const FV<V>& Ec
             const float w = (SP == 0 && m == 0) ? wx0 : (SP == 1 && m == V - 1) ? wxV : wmid;
             dg += w * rcp_approx(rc);
         }
-        out[m] = acc * rcp_approx(dg);
+        // RES: the defect f - L e of the own cell instead of its Gauss-Seidel update
+        out[m] = RES ? fmaf(-dg, eown[m], acc) : acc * rcp_approx(dg);
     }
 }
 
@@ -414,6 +417,179 @@ k_gsrb_otf_staged(Dims d, OtfParams P, int colour, float* __restrict__ es,
     }
 }
 
+// Defect of the colour-0 cells of the finest FP32 level (after a colour-1 half-sweep the
+// colour-1 defect vanishes) restricted into the coarse right-hand side, staged like
+// k_gsrb_otf_staged: a block owns all colour-half columns of P.rty rows and marches through an
+// even number of planes; the stage adds the own colour's e rows to the half-sweep's stage.  A
+// thread forms the defects of its 4 cells (columns c0 .. c0+3 = coarse columns I), sums the two
+// planes of a coarse plane in registers and the two rows of a coarse row through shared memory,
+// then writes the 4 coarse values (two float2 per colour half of the coarse level) and zeroes the
+// coarse correction there.  Same per-cell arithmetic as k_resid_restrict_otf; the eight children
+// are summed as (plane pair per row) then (row pair).
+template <bool DIR>
+__global__ void __launch_bounds__(256)
+k_resid_restrict_staged(Dims d, Dims C, OtfParams P, const float* __restrict__ eo,
+                        const float* __restrict__ eown, const float* __restrict__ rs,
+                        const float* __restrict__ rhos, const float* __restrict__ rhoo,
+                        float* __restrict__ fc, float* __restrict__ ec) {
+    constexpr int V = kCellsPerThread;
+    constexpr int colour = 0;
+    extern __shared__ __align__(128) float sm[];
+    __shared__ int abort_flag;
+    __shared__ __align__(16) float comb[256 * V];
+    const int hn0 = d.hn0, n1 = d.n1, n2 = d.n2, TY = P.rty;
+    const int oth = (TY + 2) * hn0;
+    const int own = TY * hn0;
+    const int stage = 2 * oth + 3 * own;
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(sm + kRStages * stage);
+    const int j0 = blockIdx.x * TY;
+    const int k0 = blockIdx.y * P.rzc;
+    const int kend = min(k0 + P.rzc, n2);
+    const int nq = kend - k0 + 2;
+    const long plane = (long)n1 * hn0;
+    const int t = threadIdx.x;
+    if (t == 0) {
+        for (int q = 0; q < kRStages; ++q) mbar_init(smem_addr(&bars[q]), 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    pdl_wait();
+    pdl_trigger();
+
+    auto issue = [&](int q) {
+        const int sidx = q % kRStages;
+        int p = k0 - 1 + q;
+        p += (p < 0) ? n2 : 0;
+        p -= (p >= n2) ? n2 : 0;
+        float* st = sm + sidx * stage;
+        const uint32_t bar = smem_addr(&bars[sidx]);
+        mbar_expect_tx(bar, (uint32_t)stage * 4u);
+        const long pb = (long)p * plane;
+        int slot = 0;
+        while (slot < TY + 2) {
+            int row = j0 - 1 + slot;
+            row += (row < 0) ? n1 : 0;
+            row -= (row >= n1) ? n1 : 0;
+            const int len = min(TY + 2 - slot, n1 - row);
+            const uint32_t bytes = (uint32_t)(len * hn0) * 4u;
+            bulk_g2s(smem_addr(st + slot * hn0), eo + pb + (long)row * hn0, bytes, bar);
+            bulk_g2s(smem_addr(st + oth + slot * hn0), rhoo + pb + (long)row * hn0, bytes, bar);
+            slot += len;
+        }
+        const uint32_t ob = (uint32_t)own * 4u;
+        bulk_g2s(smem_addr(st + 2 * oth), rs + pb + (long)j0 * hn0, ob, bar);
+        bulk_g2s(smem_addr(st + 2 * oth + own), rhos + pb + (long)j0 * hn0, ob, bar);
+        bulk_g2s(smem_addr(st + 2 * oth + 2 * own), eown + pb + (long)j0 * hn0, ob, bar);
+    };
+    int issued = 0, confirmed = 0;
+    if (t == 0) {
+        for (; issued < min(kRStages, nq); ++issued) issue(issued);
+    }
+    auto wait_plane = [&](int q) {
+        if (t != 0 || abort_flag) return;
+        if (mbar_wait(smem_addr(&bars[q % kRStages]), (uint32_t)((q / kRStages) & 1))) {
+            confirmed = q + 1;
+        } else {
+            abort_flag = 1;
+            atomicExch(P.err, 1);
+        }
+    };
+
+    const int idx = V * t;
+    const int r = idx / hn0, c0 = idx - r * hn0;
+    const int j = j0 + r;
+    const int cm = (c0 == 0) ? hn0 - 1 : c0 - 1;
+    const int cp = (c0 + V == hn0) ? 0 : c0 + V;
+    const bool jl = j > 0 || P.per[1], jh = j < n1 - 1 || P.per[1];
+    const bool wlo = !P.per[0] && c0 == 0, whi = !P.per[0] && c0 + V == hn0;
+    const bool dxl = P.dlo[0] && c0 == 0, dxh = P.dhi[0] && c0 + V == hn0;
+    const bool dy = (j == 0 && P.dlo[1]) || (j == n1 - 1 && P.dhi[1]);
+    const int st_n = n2 + 1;
+    const int ctr = (r + 1) * hn0 + c0;
+
+    wait_plane(0);
+    wait_plane(1);
+    __syncthreads();
+    FV<V> Eb = ldv<V>(sm + ctr), Rb = ldv<V>(sm + oth + ctr);
+    FV<V> Ec = ldv<V>(sm + stage + ctr), Rc = ldv<V>(sm + stage + oth + ctr);
+    float racc[V];
+    for (int k = k0; k < kend; ++k) {
+        const int q = k - k0 + 1;
+        wait_plane(q + 1);
+        __syncthreads();
+        if (abort_flag) break;
+        if (t == 0 && issued < nq) issue(issued++);
+        const float* sc = sm + (q % kRStages) * stage;
+        const float* su = sm + ((q + 1) % kRStages) * stage;
+        const FV<V> Ea = ldv<V>(su + ctr), Ra = ldv<V>(su + oth + ctr);
+        const int s = (colour + j + k) & 1;
+        const int cx = s ? cp : cm;
+        const float ex = sc[(r + 1) * hn0 + cx], rx = sc[oth + (r + 1) * hn0 + cx];
+        const FV<V> Eym = ldv<V>(sc + r * hn0 + c0), Rym = ldv<V>(sc + oth + r * hn0 + c0);
+        const FV<V> Eyp = ldv<V>(sc + (r + 2) * hn0 + c0);
+        const FV<V> Ryp = ldv<V>(sc + oth + (r + 2) * hn0 + c0);
+        const FV<V> Fo = ldv<V>(sc + 2 * oth + r * hn0 + c0);
+        const FV<V> Ro = ldv<V>(sc + 2 * oth + own + r * hn0 + c0);
+        const FV<V> Eown = ldv<V>(sc + 2 * oth + 2 * own + r * hn0 + c0);
+        const float fx = P.fac[k], fy = P.fac[st_n + k];
+        const float fyl = jl ? fy : 0.f, fyh = jh ? fy : 0.f;
+        const float fzl = P.fac[2 * st_n + k], fzh = P.fac[3 * st_n + k];
+        const float fxl0 = wlo ? 0.f : fx, fxhV = whi ? 0.f : fx;
+        float res[V];
+        if (DIR) {
+            const float wmid = P.fac[4 * st_n + k] + (dy ? fy : 0.f);
+            const float wx0 = wmid + (dxl ? fx : 0.f), wxV = wmid + (dxh ? fx : 0.f);
+            if (s)
+                update_group<V, 1, true, true>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp, Ryp,
+                                               Fo, Ro, fx, fxl0, fxhV, fyl, fyh, fzl, fzh, wx0,
+                                               wxV, wmid, res, Eown.v);
+            else
+                update_group<V, 0, true, true>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp, Ryp,
+                                               Fo, Ro, fx, fxl0, fxhV, fyl, fyh, fzl, fzh, wx0,
+                                               wxV, wmid, res, Eown.v);
+        } else if (s) {
+            update_group<V, 1, false, true>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp, Ryp, Fo,
+                                            Ro, fx, fxl0, fxhV, fyl, fyh, fzl, fzh, 0.f, 0.f, 0.f,
+                                            res, Eown.v);
+        } else {
+            update_group<V, 0, false, true>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp, Ryp, Fo,
+                                            Ro, fx, fxl0, fxhV, fyl, fyh, fzl, fzh, 0.f, 0.f, 0.f,
+                                            res, Eown.v);
+        }
+        if ((k & 1) == 0) {
+#pragma unroll
+            for (int m = 0; m < V; ++m) racc[m] = res[m];
+        } else {
+#pragma unroll
+            for (int m = 0; m < V; ++m) racc[m] += res[m];
+            // rows 2J (even r) and 2J+1 (odd r) of coarse row J: the odd row hands its sums over
+            if (r & 1) *reinterpret_cast<float4*>(comb + V * t) = make_float4(racc[0], racc[1], racc[2], racc[3]);
+            __syncthreads();
+            if (!(r & 1)) {
+                const float4 o = *reinterpret_cast<const float4*>(comb + V * (t + hn0 / V));
+                const float v0 = (racc[0] + o.x) * 0.125f, v1 = (racc[1] + o.y) * 0.125f;
+                const float v2 = (racc[2] + o.z) * 0.125f, v3 = (racc[3] + o.w) * 0.125f;
+                const int J = j >> 1, K = k >> 1;
+                const int pc = (c0 + J + K) & 1;   // coarse colour of I = c0 (and c0 + 2)
+                const long base = (long)(J + C.n1 * K) * C.hn0 + (c0 >> 1);
+                *reinterpret_cast<float2*>(fc + pc * C.half + base) = make_float2(v0, v2);
+                *reinterpret_cast<float2*>(fc + (pc ^ 1) * C.half + base) = make_float2(v1, v3);
+                *reinterpret_cast<float2*>(ec + pc * C.half + base) = make_float2(0.f, 0.f);
+                *reinterpret_cast<float2*>(ec + (pc ^ 1) * C.half + base) = make_float2(0.f, 0.f);
+            }
+        }
+        Eb = Ec;
+        Rb = Rc;
+        Ec = Ea;
+        Rc = Ra;
+    }
+    if (t == 0 && confirmed < issued) {
+        for (int q = confirmed; q < issued; ++q)
+            mbar_wait(smem_addr(&bars[q % kRStages]), (uint32_t)((q / kRStages) & 1));
+    }
+}
+
 template <int DM, bool RED_ONLY>
 __global__ void __launch_bounds__(kB)
 k_resid_restrict_otf(Dims F, Dims C, OtfParams P, const float* __restrict__ e,
@@ -486,6 +662,7 @@ void plan_otf_tile(const Dims& d, int dm, int sms, OtfParams& P) {
     static std::mutex mu;
     static int smem_set = 0;
     P.ty = P.zc = P.nz = P.smem = 0;
+    P.rty = P.rzc = P.rnz = P.rsmem = 0;
     if (dm != 3 || !d.split || d.hn0 % 4 || d.hn0 > 1024 || d.n2 < 2) return;
     int ty = 1;
     while (2 * ty * d.hn0 <= 1024 && d.n1 % (2 * ty) == 0) ty *= 2;
@@ -525,11 +702,62 @@ void plan_otf_tile(const Dims& d, int dm, int sms, OtfParams& P) {
     P.zc = zc;
     P.nz = ceil_div(d.n2, zc);
     P.smem = smem;
+    // staged defect + restriction: the same tiles, one more own-colour array in the stage, plane
+    // chunks of even length (a coarse plane is two fine planes)
+    static int rsmem_set = 0;
+    const int rstage = (2 * (ty + 2) + 3 * ty) * d.hn0;
+    const int rsmem = kRStages * rstage * 4 + kRStages * 8;
+    if (ty % 2 || d.n2 % 2 || rsmem > 200 * 1024) return;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (rsmem > rsmem_set) {
+            if (cudaFuncSetAttribute(k_resid_restrict_staged<false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, rsmem) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_resid_restrict_staged<true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, rsmem) !=
+                    cudaSuccess) {
+                cudaGetLastError();
+                return;
+            }
+            rsmem_set = rsmem;
+        }
+    }
+    int rper_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rper_sm, k_resid_restrict_staged<false>,
+                                                      nt, rsmem) != cudaSuccess ||
+        rper_sm < 1) {
+        cudaGetLastError();
+        return;
+    }
+    long rchunks = ((long)sms * rper_sm) / tiles;
+    if (rchunks < 1) rchunks = 1;
+    int rzc = ceil_div(d.n2, (int)std::min<long>(rchunks, d.n2 / 2));
+    rzc += rzc & 1;
+    if (rzc < 4) rzc = std::min(4, d.n2);
+    P.rty = ty;
+    P.rzc = rzc;
+    P.rnz = ceil_div(d.n2, rzc);
+    P.rsmem = rsmem;
 }
 
 void launch_resid_restrict_otf(const Dims& fine, const Dims& coarse, const OtfParams& P,
                                const float* e, const float* r, float* fc, float* ec,
                                bool red_only, cudaStream_t s) {
+    if (P.dm == 3 && P.rty > 0 && red_only && coarse.split) {
+        // colour 0 is "own": its e, f and rho; colour 1 the other colour's e and rho
+        const dim3 grid(fine.n1 / P.rty, P.rnz);
+        const int nt = P.rty * fine.hn0 / kCellsPerThread;
+        const float* eo = e + fine.half;
+        const float* rhoo = P.rho + fine.half;
+        if (P.has_dir)
+            launch_chain(k_resid_restrict_staged<true>, grid, dim3(nt), (size_t)P.rsmem, s, fine,
+                         coarse, P, eo, e, r, (const float*)P.rho, rhoo, fc, ec);
+        else
+            launch_chain(k_resid_restrict_staged<false>, grid, dim3(nt), (size_t)P.rsmem, s, fine,
+                         coarse, P, eo, e, r, (const float*)P.rho, rhoo, fc, ec);
+        return;
+    }
     const Grid3 g = grid3(coarse.n0, coarse.n1, coarse.n2);
     if (P.dm == 3) {
         if (red_only)

@@ -110,6 +110,10 @@ OtfParams otf_params(const mac_ctx* c) {
     P.zc = c->otf_tile.zc;
     P.nz = c->otf_tile.nz;
     P.smem = c->otf_tile.smem;
+    P.rty = c->otf_tile.rty;
+    P.rzc = c->otf_tile.rzc;
+    P.rnz = c->otf_tile.rnz;
+    P.rsmem = c->otf_tile.rsmem;
     P.err = c->red.counters + 2;
     return P;
 }
