@@ -78,6 +78,36 @@ __device__ __forceinline__ double recip_nr(double x) {
     return fma(y0, fma(e, e, e), y0);
 }
 
+// FP64 <-> FP32 conversions on the integer pipe.  On GB300 a conversion instruction between FP64
+// and FP32 occupies the scarce FP64 pipe like an FMA; in the FP64-bound kernels (the refinement
+// residual, the accumulation, the coefficient setup) these bit-level versions keep it free.
+// Results equal the hardware conversions (round to nearest even); operands outside the normal
+// FP32 range (zero excepted), infinities and NaNs take the hardware path.
+__device__ __forceinline__ float to_float_rn(double x) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const unsigned e = (unsigned)(u >> 52) & 0x7FFu;
+    if (e >= 897u && e <= 1150u) {   // normal FP32 exponents 1 .. 254
+        const unsigned long long m = u & 0xFFFFFFFFFFFFFull;
+        const unsigned rem = (unsigned)(m & 0x1FFFFFFFull);   // the 29 dropped bits
+        unsigned r = ((unsigned)(u >> 63) << 31) | ((e - 896u) << 23) | (unsigned)(m >> 29);
+        r += (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) ? 1u : 0u;
+        return __uint_as_float(r);
+    }
+    return __double2float_rn(x);
+}
+__device__ __forceinline__ double to_double(float f) {
+    const unsigned v = __float_as_uint(f);
+    const unsigned e = (v >> 23) & 0xFFu;
+    if (e - 1u < 254u) {   // normal
+        const unsigned long long d = ((unsigned long long)(v >> 31) << 63) |
+                                     ((unsigned long long)(e + 896u) << 52) |
+                                     ((unsigned long long)(v & 0x7FFFFFu) << 29);
+        return __longlong_as_double((long long)d);
+    }
+    if ((v & 0x7FFFFFFFu) == 0u) return __longlong_as_double((long long)((unsigned long long)(v >> 31) << 63));
+    return (double)f;
+}
+
 // Order-preserving map of a double onto unsigned 64-bit integers (max/min on the integer pipe;
 // NaN maps above +inf / below -inf depending on its sign bit).
 __device__ __forceinline__ unsigned long long ordered_bits(double v) {

@@ -366,7 +366,7 @@ k_resid64_to32(Dims F, const double* __restrict__ u, const double* __restrict__ 
             double r = fma(-dg[off + q], u[off + q], f[off + q]);
             r = arms<double>(r, q, nb, u + oth, bx + off, by + off, bz + off, bx + oth, by + oth,
                              bz + oth);
-            r32[off + q] = (float)r;
+            r32[off + q] = to_float_rn(r);
             const unsigned long long b = abs_bits(r);
             m = b > m ? b : m;
         }

@@ -107,7 +107,7 @@ k_fine_coef(FineParams P, Dims d, const double* __restrict__ rho, const double* 
     const double rc = rho[q];
     if (!positive_finite(rc)) atomicOr(err, 1);
     const int li = lidx(d, i, j, k);
-    if (rho32) rho32[li] = (float)rc;
+    if (rho32) rho32[li] = to_float_rn(rc);
     const bool v2 = P.va == 2;
     const int r = v2 ? k : j;                       // vertical index (3-D: z, 2-D: y)
     const int st = (v2 ? n2 : n1) + 1;
