@@ -1,0 +1,121 @@
+"""The workload configurations at their full sizes, through size-independent properties (the CPU
+oracle is too slow at these sizes; its parity with the GPU path is established on the smaller
+cases of test_gpu_parity.py / test_gpu_adjoint.py):
+
+* 512^3 mixed precision (64 boxes of 128^3, ~1e3 density contrast) and the 384^3 stiff stress
+  case (27 boxes, ~1e6 contrast, 5% noise): the mixed-precision and the FP64 GPU solves both
+  reach 1e-10 relative residual and agree to 1e-9 (phi with its mean removed, U);
+* 256^3 adjoint (the loss L = sum(w . U_proj)): the adjoint gradients with respect to U_edge and
+  1/rho match central finite differences of the forward FP64 solve along seeded random
+  directions, to 1e-6 relative.
+"""
+import numpy as np
+import pytest
+
+from maestro_gb300.inputs import cell_to_edge, config_case
+from maestro_gb300.macproject import BcTower, Layout, MacProjector
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return pytest.importorskip("torch")
+
+
+def _dev_case(torch, c):
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a).transpose())).to(dev)  # noqa: E731
+    return t, dev
+
+
+def _solve(torch, c, precision, rel_eps=1e-10, u_in=None, rho_in=None):
+    t, dev = _dev_case(torch, c)
+    u = [t(a) for a in (u_in if u_in is not None else c.umac)]
+    phi = t(c.phi0)
+    rho = t(rho_in if rho_in is not None else c.rho)
+    rhs = t(c.macrhs)
+    b0 = torch.from_numpy(np.ascontiguousarray(c.beta0)).to(dev)
+    b0e = torch.from_numpy(np.ascontiguousarray(c.beta0_edge)).to(dev)
+    lay = Layout.tiled(c.n, c.box)
+    P = MacProjector(lay, c.dx, BcTower(c.bc_lo, c.bc_hi), precision=precision, rel_eps=rel_eps,
+                     stream=torch.cuda.current_stream().cuda_stream)
+    try:
+        st = P.macproject_dense(u[0].data_ptr(), u[1].data_ptr(), u[2].data_ptr(),
+                                phi.data_ptr(), rho.data_ptr(), rhs.data_ptr(), b0.data_ptr(),
+                                b0e.data_ptr(), strict=True)
+    finally:
+        P.close()
+    torch.cuda.synchronize()
+    return u, phi, st
+
+
+@pytest.mark.parametrize("key", ["3d_512_mixed", "3d_384_stiff"])
+def test_large_configs_mixed_matches_fp64(cuda_lib, torch, key):
+    c = config_case(key, seed=17)
+    u64, p64, st64 = _solve(torch, c, "fp64")
+    u32, p32, st32 = _solve(torch, c, "mixed")
+    assert st64["status"] == 0 and st64["rel_resid"] <= 1e-10
+    assert st32["status"] == 0 and st32["rel_resid"] <= 1e-10
+    assert st32["refine_iters"] <= 6
+    scale = lambda x: float(x.abs().max())  # noqa: E731
+    p64, p32 = p64 - p64.mean(), p32 - p32.mean()
+    assert float((p32 - p64).abs().max()) <= 1e-9 * scale(p64)
+    for a, b in zip(u32, u64):
+        assert float((a - b).abs().max()) <= 1e-9 * scale(b)
+
+
+def test_adjoint_256_matches_finite_differences(cuda_lib, torch):
+    c = config_case("3d_256_adjoint", seed=5)
+    t, dev = _dev_case(torch, c)
+    lay = Layout.tiled(c.n, c.box)
+    P = MacProjector(lay, c.dx, BcTower(c.bc_lo, c.bc_hi), precision="fp64", rel_eps=1e-13,
+                     stream=torch.cuda.current_stream().cuda_stream)
+    try:
+        u = [t(a) for a in c.umac]
+        w = [t(a) for a in c.w]
+        du = [torch.zeros_like(x) for x in u]
+        rho = t(c.rho)
+        rhs = t(c.macrhs)
+        b0 = torch.from_numpy(c.beta0).to(dev)
+        b0e = torch.from_numpy(c.beta0_edge).to(dev)
+        drinv = torch.zeros_like(rho)
+        dmac = torch.zeros_like(rho)
+        phi = torch.zeros_like(rho)
+        db0 = torch.zeros_like(b0)
+        st = P.adjoint_dense([x.data_ptr() for x in u], rho.data_ptr(), rhs.data_ptr(),
+                             b0.data_ptr(), b0e.data_ptr(), [x.data_ptr() for x in w],
+                             [x.data_ptr() for x in du], drinv.data_ptr(), db0.data_ptr(),
+                             dmac.data_ptr(), phi.data_ptr())
+        torch.cuda.synchronize()
+        assert st["status"] == 0
+    finally:
+        P.close()
+    back = lambda x: np.asfortranarray(x.cpu().numpy().transpose())  # noqa: E731
+    gu = [back(x) for x in du]
+    grinv = back(drinv)
+
+    def loss(umac, rho_):
+        uo, _, s = _solve(torch, c, "fp64", rel_eps=1e-13, u_in=umac, rho_in=rho_)
+        assert s["status"] == 0
+        return sum(float(np.sum(back(uo[d]) * c.w[d])) for d in range(3))
+
+    rng = np.random.default_rng(8)
+    umax = max(float(np.abs(a).max()) for a in c.umac)
+    for _ in range(2):
+        v = [rng.standard_normal(a.shape) for a in c.umac]
+        h = 1e-6 * umax
+        lp = loss([a + h * b for a, b in zip(c.umac, v)], c.rho)
+        lm = loss([a - h * b for a, b in zip(c.umac, v)], c.rho)
+        fd = (lp - lm) / (2 * h)
+        an = sum(float(np.sum(g * b)) for g, b in zip(gu, v))
+        assert abs(fd - an) <= 1e-6 * max(abs(fd), abs(an))
+    rinv = 1.0 / c.rho
+    for _ in range(2):
+        v = rng.standard_normal(c.rho.shape)
+        h = 1e-6
+        lp = loss(c.umac, 1.0 / (rinv * (1.0 + h * v)))
+        lm = loss(c.umac, 1.0 / (rinv * (1.0 - h * v)))
+        fd = (lp - lm) / (2 * h)
+        an = float(np.sum(grinv * rinv * v))
+        assert abs(fd - an) <= 1e-6 * max(abs(fd), abs(an))
