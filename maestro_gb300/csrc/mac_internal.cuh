@@ -346,15 +346,18 @@ int prepare_tail_kernels();
 int setup_fine_coefficients(mac_ctx* c, const double* beta0, const double* beta0e);
 int setup_coarse_levels(mac_ctx* c);
 int setup_fp32_copies(mac_ctx* c);
-int setup_rhs(mac_ctx* c, const double* macrhs, bool have_beta0);
+// phi_nat (optional): the initial guess in natural layout, moved into the level-0 phi in the same pass
+int setup_rhs(mac_ctx* c, const double* macrhs, bool have_beta0, const double* phi_nat = nullptr);
 int finish_rhs_stats(mac_ctx* c, double* fnorm_out, bool* finite_out);
 // after_dir (optional) runs after the direction's correction kernel is queued (host-pointer
-// calls start that direction's copy-back there).
+// calls start that direction's copy-back there); phi_nat_out (optional) receives phi in natural
+// layout from the x-direction pass.
 int correct_velocity(mac_ctx* c, bool have_beta0,
-                     const std::function<int(int)>* after_dir = nullptr);
+                     const std::function<int(int)>* after_dir = nullptr,
+                     double* phi_nat_out = nullptr);
 int setup_fine_from_faces(mac_ctx* c, const double* fx, const double* fy, const double* fz,
                           const double* alpha_nat);
-int setup_rhs_from(mac_ctx* c, const double* rh_nat);
+int setup_rhs_from(mac_ctx* c, const double* rh_nat, const double* phi_nat = nullptr);
 int natural_to_level0(mac_ctx* c, const double* src, double* dst);
 int level0_to_natural(mac_ctx* c, const double* src, double* dst);
 int check_density(mac_ctx* c, bool* ok);

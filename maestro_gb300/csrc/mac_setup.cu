@@ -243,7 +243,8 @@ template <int DM, bool FROM_RH>
 __global__ void __launch_bounds__(kBlock)
 k_rhs(RhsParams P, Dims d, const double* __restrict__ ux, const double* __restrict__ uy,
       const double* __restrict__ uz, const double* __restrict__ macrhs,
-      const double* __restrict__ tab, double* __restrict__ f, double* __restrict__ partial) {
+      const double* __restrict__ tab, double* __restrict__ f, double* __restrict__ partial,
+      const double* __restrict__ phi_nat, double* __restrict__ phi_l0) {
     __shared__ double ssum[8];
     __shared__ unsigned long long smax[8], smin[8];
     const int n0 = P.n[0], n1 = P.n[1], n2 = P.n[2];
@@ -277,7 +278,11 @@ k_rhs(RhsParams P, Dims d, const double* __restrict__ ux, const double* __restri
                 }
                 v = macrhs ? macrhs[q] - dv : -dv;
             }
-            f[lidx(d, i, j, k)] = v;
+            const int li = lidx(d, i, j, k);
+            f[li] = v;
+            // the initial guess moves to the level-0 layout in the same pass (this kernel is
+            // bound by the FP64 pipe, the copy rides along in its memory slack)
+            if (phi_nat) phi_l0[li] = phi_nat[q];
             sum += v;
             const unsigned long long o = ordered_bits(v);
             mx = o > mx ? o : mx;
@@ -381,7 +386,8 @@ struct CorrParams {
 __global__ void __launch_bounds__(kBlock)
 k_correct(CorrParams P, Dims d, double* __restrict__ u, const double* __restrict__ phi,
           const double* __restrict__ bd, const double* __restrict__ wlo,
-          const double* __restrict__ whi, const double* __restrict__ tab) {
+          const double* __restrict__ whi, const double* __restrict__ tab,
+          double* __restrict__ phi_nat) {
     const int dir = P.dir;
     const int m0 = P.n[0] + (dir == 0), m1 = P.n[1] + (dir == 1);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -419,6 +425,9 @@ k_correct(CorrParams P, Dims d, double* __restrict__ u, const double* __restrict
     // beta == 0 (a wall face without Dirichlet) leaves the face alone; tested on the bit pattern
     // so that no FP64 comparison occupies the FP64 pipe
     if ((unsigned long long)__double_as_longlong(beta) << 1) u[q] = fma(-(beta * kap), dphi, u[q]);
+    // the x-direction pass also returns phi to the natural layout (one cell per x face but the
+    // last; this kernel is bound by the FP64 pipe, the copy rides along)
+    if (phi_nat && i < P.n[0]) phi_nat[i + P.n[0] * (j + P.n[1] * k)] = phi[lidx(d, i, j, k)];
 }
 
 __global__ void k_nat_to_l0(Dims d, const double* __restrict__ src, double* __restrict__ dst) {
@@ -697,7 +706,7 @@ int setup_fp32_copies(mac_ctx* c) {
 
 namespace {
 
-int launch_rhs(mac_ctx* c, const double* macrhs, bool from_rh) {
+int launch_rhs(mac_ctx* c, const double* macrhs, bool from_rh, const double* phi_nat) {
     Level& L = c->lev[0];
     RhsParams P;
     for (int d = 0; d < 3; ++d) {
@@ -713,17 +722,17 @@ int launch_rhs(mac_ctx* c, const double* macrhs, bool from_rh) {
     if (c->dm == 3) {
         if (from_rh)
             k_rhs<3, true><<<g.grid, g.block, 0, c->stream>>>(P, L.d, nullptr, nullptr, nullptr, macrhs,
-                                                              c->b0tab, L.a64.f, c->red.partial);
+                                                              c->b0tab, L.a64.f, c->red.partial, phi_nat, L.a64.phi);
         else
             k_rhs<3, false><<<g.grid, g.block, 0, c->stream>>>(P, L.d, c->u[0], c->u[1], c->u[2], macrhs,
-                                                               c->b0tab, L.a64.f, c->red.partial);
+                                                               c->b0tab, L.a64.f, c->red.partial, phi_nat, L.a64.phi);
     } else {
         if (from_rh)
             k_rhs<2, true><<<g.grid, g.block, 0, c->stream>>>(P, L.d, nullptr, nullptr, nullptr, macrhs,
-                                                              c->b0tab, L.a64.f, c->red.partial);
+                                                              c->b0tab, L.a64.f, c->red.partial, phi_nat, L.a64.phi);
         else
             k_rhs<2, false><<<g.grid, g.block, 0, c->stream>>>(P, L.d, c->u[0], c->u[1], nullptr, macrhs,
-                                                               c->b0tab, L.a64.f, c->red.partial);
+                                                               c->b0tab, L.a64.f, c->red.partial, phi_nat, L.a64.phi);
     }
     MAC_CUDA_TRY(cudaGetLastError());
     ++c->issued;
@@ -742,12 +751,13 @@ int launch_rhs(mac_ctx* c, const double* macrhs, bool from_rh) {
 
 }  // namespace
 
-int setup_rhs(mac_ctx* c, const double* macrhs, bool have_beta0) {
+int setup_rhs(mac_ctx* c, const double* macrhs, bool have_beta0, const double* phi_nat) {
     (void)have_beta0;   // the factor tables hold beta0 = 1 when there is none
-    return launch_rhs(c, macrhs, false);
+    return launch_rhs(c, macrhs, false, phi_nat);
 }
 
-int correct_velocity(mac_ctx* c, bool have_beta0, const std::function<int(int)>* after_dir) {
+int correct_velocity(mac_ctx* c, bool have_beta0, const std::function<int(int)>* after_dir,
+                     double* phi_nat_out) {
     Level& L = c->lev[0];
     const double* bd[3] = {L.a64.bx, L.a64.by, L.a64.bz};
     for (int d = 0; d < c->dm; ++d) {
@@ -762,7 +772,8 @@ int correct_velocity(mac_ctx* c, bool have_beta0, const std::function<int(int)>*
         P.h2 = c->dx[d] * c->dx[d];
         const Grid3 g = grid3(c->n[0] + (d == 0), c->n[1] + (d == 1), c->n[2] + (d == 2));
         k_correct<<<g.grid, g.block, 0, c->stream>>>(P, L.d, c->u[d], L.a64.phi, bd[d],
-                                                     L.wall[d][0], L.wall[d][1], c->b0tab);
+                                                     L.wall[d][0], L.wall[d][1], c->b0tab,
+                                                     d == 0 ? phi_nat_out : nullptr);
         MAC_CUDA_TRY(cudaGetLastError());
         ++c->issued;
         if (after_dir) {
@@ -1125,6 +1136,8 @@ int setup_fine_from_faces(mac_ctx* c, const double* fx, const double* fy, const 
     return build_diag(c, 0, mixed(c));
 }
 
-int setup_rhs_from(mac_ctx* c, const double* rh_nat) { return launch_rhs(c, rh_nat, true); }
+int setup_rhs_from(mac_ctx* c, const double* rh_nat, const double* phi_nat) {
+    return launch_rhs(c, rh_nat, true, phi_nat);
+}
 
 }  // namespace mac

@@ -670,10 +670,8 @@ int core_macproject(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats
     rc = setup_coarse_levels(c);
     if (rc) return rc;
     if (before_rhs && (rc = (*before_rhs)())) return rc;
-    rc = setup_rhs(c, macrhs, have_beta0);
-    if (rc) return rc;
     if (before_phi && (rc = (*before_phi)())) return rc;
-    rc = natural_to_level0(c, c->phin, F.a64.phi);
+    rc = setup_rhs(c, macrhs, have_beta0, c->phin);   // also moves phi into the level-0 layout
     if (rc) return rc;
     cudaEventRecord(c->ev[1], c->stream);
     const long long setup_kernels = c->issued;
@@ -681,10 +679,15 @@ int core_macproject(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats
     if (solve_rc != MAC_OK && solve_rc != MAC_ERR_NOT_CONVERGED) return solve_rc;
     cudaEventRecord(c->ev[2], c->stream);
     const long long before_corr = c->issued;
-    rc = level0_to_natural(c, F.a64.phi, c->phin);
-    if (rc) return rc;
-    if (after_phi && (rc = (*after_phi)())) return rc;
-    rc = correct_velocity(c, have_beta0, after_dir);
+    // the x-direction correction also returns phi to the natural layout; phi's copy-back (host
+    // pointers) starts right after it
+    const std::function<int(int)> dir_hook = [&](int d) {
+        int r = MAC_OK;
+        if (d == 0 && after_phi) r = (*after_phi)();
+        if (!r && after_dir) r = (*after_dir)(d);
+        return r;
+    };
+    rc = correct_velocity(c, have_beta0, &dir_hook, c->phin);
     if (rc) return rc;
     c->ktime_launches[MAC_KT_CORRECT] += (int)(c->issued - before_corr);
     c->ktime_launches[MAC_KT_SETUP] += (int)setup_kernels;
@@ -1026,8 +1029,7 @@ int mac_multigrid(mac_ctx* c, int ptr_kind, const double* const* rh, int ng_rh,
                                    alpha ? c->scratch : nullptr);
     }
     if (!rc) rc = setup_coarse_levels(c);
-    if (!rc) rc = setup_rhs_from(c, c->rhs);
-    if (!rc) rc = natural_to_level0(c, c->phin, F.a64.phi);
+    if (!rc) rc = setup_rhs_from(c, c->rhs, c->phin);   // also moves phi into the level-0 layout
     int solve_rc = MAC_OK;
     if (!rc) {
         cudaEventRecord(c->ev[1], c->stream);
