@@ -67,7 +67,49 @@ def peaks():
 
 
 # ---- clocks sampled during the timed region ---------------------------------------------------
+class _Nvml:
+    """Read-only NVML queries through ctypes (SM clock, its maximum, clock event reasons)."""
+    SM = 1
+    BITS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown",
+            0x4: "sw_power_cap"}
+
+    def __init__(self, torch_index):
+        import ctypes
+        self.c = ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.lib = lib
+        self.h = ctypes.c_void_p()
+        ok = False
+        try:
+            import torch
+            uuid = getattr(torch.cuda.get_device_properties(torch_index), "uuid", None)
+            if uuid is not None:
+                ok = lib.nvmlDeviceGetHandleByUUID(("GPU-" + str(uuid)).encode(),
+                                                   ctypes.byref(self.h)) == 0
+        except Exception:
+            ok = False
+        if not ok and lib.nvmlDeviceGetHandleByIndex_v2(torch_index, ctypes.byref(self.h)) != 0:
+            raise RuntimeError("no NVML handle")
+        self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        v = ctypes.c_uint()
+        self.max_sm = float(v.value) if lib.nvmlDeviceGetMaxClockInfo(
+            self.h, self.SM, ctypes.byref(v)) == 0 else None
+
+    def sample(self):
+        c = self.c
+        v, r = c.c_uint(), c.c_ulonglong()
+        sm = float(v.value) if self.lib.nvmlDeviceGetClockInfo(self.h, self.SM, c.byref(v)) == 0 \
+            else None
+        bits = r.value if self.reasons_fn(self.h, c.byref(r)) == 0 else 0
+        return sm, {nm for b, nm in self.BITS.items() if bits & b}
+
+
 class Clocks:
+    """SM clocks and clock event reasons sampled while the timed region runs: NVML polled from a
+    thread every 5 ms (read-only queries), else nvidia-smi at its 200 ms period."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -76,8 +118,29 @@ class Clocks:
         self.proc = None
         self.path = None
         self.gpu = gpu_index
+        self.nvml = None
+        self.thread = None
+        try:
+            self.nvml = _Nvml(gpu_index)
+        except Exception:
+            self.nvml = None
 
     def start(self):
+        if self.nvml is not None:
+            import threading
+            self.sm, self.reasons = [], set()
+            self.halt = threading.Event()
+
+            def run():
+                while not self.halt.is_set():
+                    sm, rs = self.nvml.sample()
+                    if sm is not None:
+                        self.sm.append(sm)
+                    self.reasons |= rs
+                    self.halt.wait(0.005)
+            self.thread = threading.Thread(target=run, daemon=True)
+            self.thread.start()
+            return
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
@@ -90,6 +153,13 @@ class Clocks:
             self.proc = None
 
     def stop(self):
+        if self.thread is not None:
+            self.halt.set()
+            self.thread.join()
+            sm = self.sm
+            return {"sm_mhz": statistics.median(sm) if sm else None,
+                    "sm_max_mhz": self.nvml.max_sm, "reasons": sorted(self.reasons),
+                    "samples": len(sm), "source": "nvml"}
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
         self.proc.terminate()
@@ -116,7 +186,7 @@ class Clocks:
         os.unlink(self.path)
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi"}
 
 
 # ---- reference arm: the CPU oracle ------------------------------------------------------------
@@ -374,6 +444,8 @@ def main():
             P.macproject(s[1], s[3], s[2], s[4], c.beta0, c.beta0_edge, strict=True)
             refill(s)
         step_s = []
+        ck_e2e = Clocks(local)
+        ck_e2e.start()
         for k in range(E):
             s = sets[(k + 1) % 2]
             barrier()
@@ -382,6 +454,7 @@ def main():
             barrier()
             step_s.append(time.perf_counter() - t0)
             refill(s)
+        ck_e2e = ck_e2e.stop()
         secs = max_over_ranks(sum(step_s))
         P.close()
         e2e = {"value": world * E / secs, "unit": UNIT, "h2d_bytes_per_step": h2d,
@@ -390,7 +463,7 @@ def main():
                "api": "mac_macproject (MAC_PTR_HOST; page-locked per-box fabs, 8 boxes of 128^3 "
                       "+ 1 ghost, copied by the copy engines on a transfer stream overlapped "
                       "with the setup and the copy-back)",
-               "precision": "mixed"}
+               "precision": "mixed", "clocks": ck_e2e}
 
     # ---- CPU baseline: one full solve of the workload by the oracle (rank 0, N = 1) ---------
     cpu = None

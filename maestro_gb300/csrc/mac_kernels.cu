@@ -59,6 +59,10 @@ __device__ __forceinline__ T arms(T acc, int me, const Nbr& nb, const T* __restr
     return acc;
 }
 
+__device__ __forceinline__ unsigned long long dbits(double v) {
+    return (unsigned long long)__double_as_longlong(v);
+}
+
 __device__ __forceinline__ unsigned long long abs_bits(double v) {
     return (unsigned long long)__double_as_longlong(fabs(v));
 }
@@ -344,7 +348,10 @@ k_resid_norm(Dims F, const T* __restrict__ u, const T* __restrict__ f, const T* 
     if (threadIdx.x == 0 && threadIdx.y == 0 && m) atomicMax(maxbits, m);
 }
 
-// FP64 residual of the whole fine level, stored as FP32 (the refinement right-hand side).
+// FP64 residual of the whole fine level, stored as FP32 (the refinement right-hand side).  Where
+// phi is +0 on a cell and its six neighbours (the usual zero initial guess) the residual is f
+// itself, except that -0 becomes +0 as (-0) + (+0) does in the FMA chain: that branch issues no
+// FP64 instruction and reads no coefficient, with bitwise the chain's result.
 __global__ void __launch_bounds__(kBlock)
 k_resid64_to32(Dims F, const double* __restrict__ u, const double* __restrict__ f,
                const double* __restrict__ bx, const double* __restrict__ by,
@@ -363,9 +370,26 @@ k_resid64_to32(Dims F, const double* __restrict__ u, const double* __restrict__ 
             const int off = colour * F.half, oth = (colour ^ 1) * F.half;
             Nbr nb;
             split_nbrs(F, colour, h, j, k, nb);
-            double r = fma(-dg[off + q], u[off + q], f[off + q]);
-            r = arms<double>(r, q, nb, u + oth, bx + off, by + off, bz + off, bx + oth, by + oth,
-                             bz + oth);
+            const double* uo = u + oth;
+            const double uc = u[off + q];
+            const double v0 = uo[nb.xm], v1 = uo[nb.xp], v2 = uo[nb.ym], v3 = uo[nb.yp],
+                         v4 = uo[nb.zm], v5 = uo[nb.zp];
+            const unsigned long long any =
+                dbits(uc) | dbits(v0) | dbits(v1) | dbits(v2) | dbits(v3) | dbits(v4) | dbits(v5);
+            double r;
+            if (any == 0ull) {
+                const unsigned long long fb = dbits(f[off + q]);
+                r = __longlong_as_double((long long)(fb == 0x8000000000000000ull ? 0ull : fb));
+            } else {
+                // the FMA order of arms(): x-, x+, y-, y+, z-, z+
+                r = fma(-dg[off + q], uc, f[off + q]);
+                r = fma(bx[off + q], v0, r);
+                r = fma(bx[oth + nb.xp], v1, r);
+                r = fma(by[off + q], v2, r);
+                r = fma(by[oth + nb.yp], v3, r);
+                r = fma(bz[off + q], v4, r);
+                r = fma(bz[oth + nb.zp], v5, r);
+            }
             r32[off + q] = to_float_rn(r);
             const unsigned long long b = abs_bits(r);
             m = b > m ? b : m;

@@ -236,8 +236,6 @@ __global__ void __launch_bounds__(kTailThreads)
 k_tail(TailParams<T> P) {
     extern __shared__ __align__(16) unsigned char tail_smem[];
     const int tid = threadIdx.x, nt = blockDim.x;
-    pdl_wait();
-    pdl_trigger();
     const int nl = P.nlev;   // non-bottom tail levels
     TailLevel<T> L[kTailMaxLevels];
     // carve shared memory: per non-bottom level 7 arrays of T, then the bottom's operator (5 N),
@@ -263,18 +261,19 @@ k_tail(TailParams<T> P) {
     double* bsm = reinterpret_cast<double*>(tail_smem + off);
     const Dims BD = P.bottom;
     const int NB = BD.ncell;
-    // load the operators (split layout in global memory -> natural in shared memory)
+    // load the operators (split layout in global memory -> natural in shared memory).  They are
+    // built before the solve starts (and the host waits for that), so their copies are issued
+    // before the wait on the preceding kernel and overlap its last part; only the restricted
+    // defect f0 comes from that kernel.
     for (int l = 0; l < nl; ++l) {
         const TailLevel<T>& Ll = L[l];
         const T *gbx = P.bx[l], *gby = P.by[l], *gbz = P.bz[l], *gdg = P.dg[l], *gidg = P.idg[l];
-        const T* gf = l == 0 ? P.f0 : nullptr;
         for_split_cells(P.lev[l], [&](int g, int c) {
             cp_async(Ll.bx + c, gbx + g);
             cp_async(Ll.by + c, gby + g);
             cp_async(Ll.bz + c, gbz + g);
             cp_async(Ll.dg + c, gdg + g);
             cp_async(Ll.idg + c, gidg + g);
-            if (gf) cp_async(Ll.f + c, gf + g);
             Ll.e[c] = T(0);
         });
     }
@@ -290,6 +289,13 @@ k_tail(TailParams<T> P) {
         cp_async(ops + 2 * NB + c, P.bbz + c);
         cp_async(ops + 3 * NB + c, P.bdg + c);
         cp_async(ops + 4 * NB + c, P.bidg + c);
+    }
+    pdl_wait();
+    pdl_trigger();
+    {
+        const T* gf = P.f0;
+        T* sf = L[0].f;
+        for_split_cells(P.lev[0], [&](int g, int c) { cp_async(sf + c, gf + g); });
     }
     cp_async_wait();
     v.bx = ops;
