@@ -109,12 +109,15 @@ class _Nvml:
 
 class Clocks:
     """SM clocks and clock event reasons sampled while the timed region runs: NVML polled from a
-    thread every 5 ms (read-only queries), else nvidia-smi at its 200 ms period."""
+    thread (read-only queries; every 5 ms by default, every 100 ms around the end-to-end calls,
+    whose host-side API calls a tighter poll was seen to delay), else nvidia-smi at its 200 ms
+    period."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, period_s=0.005):
+        self.period = period_s
         self.proc = None
         self.path = None
         self.gpu = gpu_index
@@ -137,7 +140,7 @@ class Clocks:
                     if sm is not None:
                         self.sm.append(sm)
                     self.reasons |= rs
-                    self.halt.wait(0.005)
+                    self.halt.wait(self.period)
             self.thread = threading.Thread(target=run, daemon=True)
             self.thread.start()
             return
@@ -444,7 +447,7 @@ def main():
             P.macproject(s[1], s[3], s[2], s[4], c.beta0, c.beta0_edge, strict=True)
             refill(s)
         step_s = []
-        ck_e2e = Clocks(local)
+        ck_e2e = Clocks(local, period_s=0.1)
         ck_e2e.start()
         for k in range(E):
             s = sets[(k + 1) % 2]

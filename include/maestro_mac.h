@@ -100,6 +100,13 @@ typedef struct mac_opts {
                                only as many inner V-cycles (<= inner_vcycles) as the contraction
                                just observed predicts the tolerance needs; 0: always
                                inner_vcycles                                                   */
+    int inner_krylov;       /* mixed precision with nu2 > 0: 1 = the inner FP32 V-cycles of a
+                               step precondition a flexible conjugate-gradient iteration (one
+                               previous direction kept; each V-cycle starts from zero on the
+                               current FP32 residual): fewer V-cycles, but at the same residual
+                               tolerance the projected velocity can be further from the
+                               converged one; 0 (default) = plain V-cycles, the reference's
+                               iteration                                                       */
 } mac_opts;
 
 /* Kernel classes of mac_stats.ktime_* (finest level unless stated). */
@@ -107,7 +114,7 @@ typedef struct mac_opts {
 #define MAC_KT_RESTRICT  1   /* defect + restriction to level 1                               */
 #define MAC_KT_COARSE    2   /* everything on levels >= 1 incl. the bottom solve              */
 #define MAC_KT_PROLONG   3   /* prolongation from level 1                                     */
-#define MAC_KT_ACCUM     4   /* FP64 accumulation phi += e (mixed)                            */
+#define MAC_KT_ACCUM     4   /* FP64 accumulation phi += e and the inner Krylov steps (mixed) */
 #define MAC_KT_RESID     5   /* convergence residual (FP64)                                   */
 #define MAC_KT_SETUP     6   /* coefficients, right-hand side, layout conversion              */
 #define MAC_KT_CORRECT   7   /* velocity correction + layout conversion                       */

@@ -70,6 +70,7 @@ class MacOpts(ctypes.Structure):
         ("inner_vcycles", ctypes.c_int),
         ("coarse_tail", ctypes.c_int),
         ("adaptive_inner", ctypes.c_int),
+        ("inner_krylov", ctypes.c_int),
     ]
 
 

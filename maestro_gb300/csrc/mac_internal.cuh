@@ -210,6 +210,19 @@ struct OtfParams {
 // Tile plan of the staged half-sweep for the finest level (OtfParams.ty/zc/nz/smem).
 void plan_otf_tile(const Dims& d, int dm, int sms, OtfParams& P);
 
+// Flexible-CG vectors of the mixed-precision inner solve (level-0 layout, FP32): search
+// direction p, q = L p, accumulated correction x, the colour-0 half of w = L z; the inner-product
+// partials, [0] alpha [1] beta [2] (p, q) of the last step, and the finished-block counter.
+struct KrylovBufs {
+    float* p = nullptr;
+    float* q = nullptr;
+    float* x = nullptr;
+    float* w0 = nullptr;
+    double* partial = nullptr;
+    double* scalars = nullptr;
+    unsigned* count = nullptr;
+};
+
 }  // namespace mac
 
 constexpr int kInnerGraphs = 8;   // mixed-precision steps of up to 8 inner V-cycles are graphed
@@ -275,6 +288,7 @@ struct mac_ctx {
     float* rho32 = nullptr;
     float* fac32 = nullptr;
     bool otf = false;                             // finest-level FP32 kernels use rho32
+    mac::KrylovBufs kry;                          // flexible-CG vectors (allocated on first use)
     int tail_start[2] = {-1, -1};                 // first tail level (FP64, FP32); -1: none
     size_t tail_smem[2] = {0, 0};
     double ktime_ms[8] = {};
@@ -298,9 +312,21 @@ void launch_prolong_add(const Dims& fine, const Dims& coarse, const BcDesc& bc, 
 template <typename T>
 void launch_resid_norm(const Dims& d, const LevelArrays<T>& a, bool red_only,
                        unsigned long long* maxbits, cudaStream_t s);
+// r32 = f - L phi (FP64 arithmetic, FP32 result) and its max-norm; e32 (optional) is zeroed in
+// the same pass (the next inner solve starts from e = 0)
 void launch_resid64_to32(const Dims& d, const LevelArrays<double>& a, float* r32,
-                         unsigned long long* maxbits, cudaStream_t s);
+                         unsigned long long* maxbits, cudaStream_t s, float* e32 = nullptr);
 void launch_accumulate(const Dims& d, double* phi, const float* e, cudaStream_t s);
+
+// flexible CG around the FP32 V-cycle (mac_krylov.cu); A.phi = z (the V-cycle output), A.f = r
+int krylov_partials(const Dims& d);
+void launch_fcg_dots(const Dims& d, int dm, bool otf, const OtfParams& P,
+                     const LevelArrays<float>& A, const KrylovBufs& K, bool first, bool store_w,
+                     cudaStream_t s);
+void launch_fcg_update(const Dims& d, const LevelArrays<float>& A, const KrylovBufs& K,
+                       bool first, cudaStream_t s);
+void launch_fcg_final(const Dims& d, double* phi, const LevelArrays<float>& A,
+                      const KrylovBufs& K, bool first, cudaStream_t s);
 
 void launch_gsrb_otf(const Dims& d, const OtfParams& P, int colour, float* e, const float* r,
                      cudaStream_t s);

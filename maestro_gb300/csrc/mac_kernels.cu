@@ -356,7 +356,8 @@ __global__ void __launch_bounds__(kBlock)
 k_resid64_to32(Dims F, const double* __restrict__ u, const double* __restrict__ f,
                const double* __restrict__ bx, const double* __restrict__ by,
                const double* __restrict__ bz, const double* __restrict__ dg,
-               float* __restrict__ r32, unsigned long long* __restrict__ maxbits) {
+               float* __restrict__ r32, unsigned long long* __restrict__ maxbits,
+               float* __restrict__ e32) {
     pdl_wait();
     pdl_trigger();
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
@@ -391,6 +392,7 @@ k_resid64_to32(Dims F, const double* __restrict__ u, const double* __restrict__ 
                 r = fma(bz[oth + nb.zp], v5, r);
             }
             r32[off + q] = to_float_rn(r);
+            if (e32) e32[off + q] = 0.f;
             const unsigned long long b = abs_bits(r);
             m = b > m ? b : m;
         }
@@ -534,11 +536,11 @@ void launch_resid_norm(const Dims& d, const LevelArrays<T>& a, bool red_only,
 }
 
 void launch_resid64_to32(const Dims& d, const LevelArrays<double>& a, float* r32,
-                         unsigned long long* maxbits, cudaStream_t s) {
+                         unsigned long long* maxbits, cudaStream_t s, float* e32) {
     const Grid3 g = grid3(d.hn0, d.n1, d.n2);
     launch_chain(k_resid64_to32, g.grid, g.block, 0, s, d, (const double*)a.phi,
                (const double*)a.f, (const double*)a.bx, (const double*)a.by, (const double*)a.bz,
-               (const double*)a.diag, r32, maxbits);
+               (const double*)a.diag, r32, maxbits, e32);
 }
 
 void launch_accumulate(const Dims& d, double* phi, const float* e, cudaStream_t s) {

@@ -4,8 +4,9 @@
 // Solve structure (FBoxLib ml_cc as used by Source/mac_multigrid.f90:56-67, Docs/mg/mg.tex:325-375):
 //   FP64  : repeat { V(nu1,nu2)-cycle on (phi, f); ||f - L phi||_inf } until
 //           ||r|| <= rel_eps ||f|| (or abs_eps), at most max_vcycles times.
-//   MIXED : r = f - L phi in FP64 (stored FP32); repeat { e = FP32 V-cycle on (e, r) from e = 0,
-//           FP64 bottom solve; phi += e in FP64; r = f - L phi in FP64 } until converged.
+//   MIXED : r = f - L phi in FP64 (stored FP32); repeat { e = FP32 V-cycles on (e, r) from e = 0
+//           (with an FP64 bottom solve), combined by flexible CG (inner_krylov) or applied one
+//           after the other; phi += e in FP64; r = f - L phi in FP64 } until converged.
 // Every V-cycle (with its convergence residual) is captured once into a CUDA graph and replayed;
 // the host reads one 8-byte max-norm per cycle.
 #include <algorithm>
@@ -206,6 +207,34 @@ void vcycle(mac_ctx* c, int l) {
     mark(c, tm, 5);
 }
 
+// Flexible CG around the inner V-cycles: mixed precision with post-smoothing (after its last
+// colour-1 half-sweep the V-cycle output satisfies L z = r on colour 1, which the Krylov kernels
+// use).
+bool use_krylov(const mac_ctx* c, int prec) {
+    return prec == MAC_PREC_MIXED && c->o.inner_krylov && c->o.nu2 > 0;
+}
+
+int ensure_krylov(mac_ctx* c) {
+    KrylovBufs& K = c->kry;
+    if (K.p) return MAC_OK;
+    const Dims& d = c->lev[0].d;
+    int rc = 0;
+    rc |= alloc_arr(c, &K.p, (size_t)d.ncell);
+    rc |= alloc_arr(c, &K.q, (size_t)d.ncell);
+    rc |= alloc_arr(c, &K.x, (size_t)d.ncell);
+    rc |= alloc_arr(c, &K.w0, (size_t)d.half);
+    rc |= alloc_arr(c, &K.partial, (size_t)krylov_partials(d));
+    rc |= alloc_arr(c, &K.scalars, 4);
+    rc |= alloc_arr(c, &K.count, 1);
+    if (rc) {
+        K = KrylovBufs();
+        return MAC_ERR_ALLOC;
+    }
+    MAC_CUDA_TRY(cudaMemset(K.count, 0, sizeof(unsigned)));
+    MAC_CUDA_TRY(cudaMemset(K.scalars, 0, 4 * sizeof(double)));
+    return MAC_OK;
+}
+
 int inner_cycles(const mac_ctx* c, int prec) {
     return prec == MAC_PREC_FP64 ? 1 : (c->cur_inner > 1 ? c->cur_inner : 1);
 }
@@ -228,17 +257,35 @@ void issue_iteration(mac_ctx* c, int prec) {
         launch_resid_norm<double>(F.d, F.a64, c->o.nu2 > 0, c->red.maxbits, c->stream);
         ++c->issued;
     } else {
-        cudaMemsetAsync(F.a32.phi, 0, sizeof(float) * F.d.ncell, c->stream);
+        // e (F.a32.phi) enters at zero: the residual kernel that formed this step's right-hand
+        // side cleared it
         const int nv = inner_cycles(c, prec);
-        for (int v = 0; v < nv; ++v) {
-            c->vtimer = v;
-            vcycle<float>(c, 0);
+        if (use_krylov(c, prec)) {
+            const OtfParams P = c->otf ? otf_params(c) : OtfParams{};
+            for (int v = 0; v < nv; ++v) {
+                c->vtimer = v;
+                vcycle<float>(c, 0);
+                const bool last = v + 1 == nv;
+                launch_fcg_dots(F.d, c->dm, c->otf, P, F.a32, c->kry, v == 0, !last, c->stream);
+                if (!last)
+                    launch_fcg_update(F.d, F.a32, c->kry, v == 0, c->stream);
+                else
+                    launch_fcg_final(F.d, F.a64.phi, F.a32, c->kry, v == 0, c->stream);
+                c->issued += 2;
+                mark(c, tm, 6);
+            }
+            if (tm) cudaEventRecordWithFlags(c->tail[0], c->stream, cudaEventRecordExternal);
+        } else {
+            for (int v = 0; v < nv; ++v) {
+                c->vtimer = v;
+                vcycle<float>(c, 0);
+            }
+            if (tm) cudaEventRecordWithFlags(c->tail[0], c->stream, cudaEventRecordExternal);
+            launch_accumulate(F.d, F.a64.phi, F.a32.phi, c->stream);
+            ++c->issued;
         }
-        if (tm) cudaEventRecordWithFlags(c->tail[0], c->stream, cudaEventRecordExternal);
-        launch_accumulate(F.d, F.a64.phi, F.a32.phi, c->stream);
-        ++c->issued;
         if (tm) cudaEventRecordWithFlags(c->tail[1], c->stream, cudaEventRecordExternal);
-        launch_resid64_to32(F.d, F.a64, F.a32.f, c->red.maxbits, c->stream);
+        launch_resid64_to32(F.d, F.a64, F.a32.f, c->red.maxbits, c->stream, F.a32.phi);
         ++c->issued;
     }
     if (tm) cudaEventRecordWithFlags(c->tail[2], c->stream, cudaEventRecordExternal);
@@ -264,11 +311,17 @@ void collect_timing(mac_ctx* c, int prec) {
         c->ktime_ms[MAC_KT_COARSE] += t[2];
         c->ktime_ms[MAC_KT_PROLONG] += t[3];
         c->ktime_launches[MAC_KT_PROLONG] += 1;
+        if (use_krylov(c, prec)) {
+            float tk = 0.f;
+            cudaEventElapsedTime(&tk, c->tev[v][5], c->tev[v][6]);
+            c->ktime_ms[MAC_KT_ACCUM] += tk;
+            c->ktime_launches[MAC_KT_ACCUM] += 2;
+        }
     }
     float ta = 0.f, tr = 0.f;
     cudaEventElapsedTime(&ta, c->tail[0], c->tail[1]);
     cudaEventElapsedTime(&tr, c->tail[1], c->tail[2]);
-    if (prec == MAC_PREC_MIXED) {
+    if (prec == MAC_PREC_MIXED && !use_krylov(c, prec)) {
         c->ktime_ms[MAC_KT_ACCUM] += ta;
         c->ktime_launches[MAC_KT_ACCUM] += 1;
     }
@@ -347,6 +400,7 @@ int run_solve(mac_ctx* c, mac_stats* st) {
     if (prec == MAC_PREC_MIXED) {
         int rc = setup_fp32_copies(c);
         if (rc) return rc;
+        if (use_krylov(c, prec) && (rc = ensure_krylov(c))) return rc;
     }
     MAC_CUDA_TRY(cudaMemcpyAsync(c->red.h_scalars, c->red.scalars, 8 * sizeof(double),
                                  cudaMemcpyDeviceToHost, c->stream));
@@ -371,7 +425,7 @@ int run_solve(mac_ctx* c, mac_stats* st) {
     if (prec == MAC_PREC_FP64)
         launch_resid_norm<double>(F.d, F.a64, false, c->red.maxbits, c->stream);
     else
-        launch_resid64_to32(F.d, F.a64, F.a32.f, c->red.maxbits, c->stream);
+        launch_resid64_to32(F.d, F.a64, F.a32.f, c->red.maxbits, c->stream, F.a32.phi);
     ++c->issued;
     MAC_CUDA_TRY(cudaGetLastError());
     MAC_CUDA_TRY(cudaMemcpyAsync(c->red.h_maxbits, c->red.maxbits, sizeof(unsigned long long),
@@ -767,6 +821,7 @@ void mac_default_opts(mac_opts* o) {
     o->inner_vcycles = 4;
     o->coarse_tail = 1;
     o->adaptive_inner = 1;
+    o->inner_krylov = 0;
 }
 
 const char* mac_strerror(int code) {
