@@ -167,7 +167,8 @@ struct Level {
 struct Reduce {
     unsigned long long* maxbits = nullptr;  // running max of |r| as IEEE bits (non-negative)
     double* partial = nullptr;              // per-block partials (sum, max, min)
-    double* scalars = nullptr;              // [0] mean, [1] fnorm, [2] sum, [3] max, [4] min
+    double* scalars = nullptr;              // [0] mean, [1] fnorm, [2] sum, [3] max, [4] min,
+                                            // [5] OR of the guess's bits (0: phi = +0)
     int* counters = nullptr;                // [0] bottom iterations
     unsigned long long* h_maxbits = nullptr;
     double* h_scalars = nullptr;
@@ -289,6 +290,7 @@ struct mac_ctx {
     float* fac32 = nullptr;
     bool otf = false;                             // finest-level FP32 kernels use rho32
     mac::KrylovBufs kry;                          // flexible-CG vectors (allocated on first use)
+    bool mean_pending = false;                    // f still holds the mean (singular problem)
     int tail_start[2] = {-1, -1};                 // first tail level (FP64, FP32); -1: none
     size_t tail_smem[2] = {0, 0};
     double ktime_ms[8] = {};
@@ -316,6 +318,9 @@ void launch_resid_norm(const Dims& d, const LevelArrays<T>& a, bool red_only,
 // the same pass (the next inner solve starts from e = 0)
 void launch_resid64_to32(const Dims& d, const LevelArrays<double>& a, float* r32,
                          unsigned long long* maxbits, cudaStream_t s, float* e32 = nullptr);
+// the initial residual of a zero guess: f -= mean (mean non-null), r32 = f, e32 = 0, max |f|
+void launch_first_resid_zero(const Dims& d, double* f, const double* mean, float* r32,
+                             float* e32, unsigned long long* maxbits, cudaStream_t s);
 void launch_accumulate(const Dims& d, double* phi, const float* e, cudaStream_t s);
 
 // flexible CG around the FP32 V-cycle (mac_krylov.cu); A.phi = z (the V-cycle output), A.f = r
@@ -375,6 +380,8 @@ int setup_fp32_copies(mac_ctx* c);
 // phi_nat (optional): the initial guess in natural layout, moved into the level-0 phi in the same pass
 int setup_rhs(mac_ctx* c, const double* macrhs, bool have_beta0, const double* phi_nat = nullptr);
 int finish_rhs_stats(mac_ctx* c, double* fnorm_out, bool* finite_out);
+// f -= mean on level 0 (red.scalars[0]); the solve issues it for singular problems
+void launch_sub_mean(mac_ctx* c);
 // after_dir (optional) runs after the direction's correction kernel is queued (host-pointer
 // calls start that direction's copy-back there); phi_nat_out (optional) receives phi in natural
 // layout from the x-direction pass.
@@ -470,6 +477,7 @@ inline Grid3 grid3(int nx, int ny, int nz) {
 // Launch grid of the right-hand-side kernel (each block covers kRhsPlanes planes); its block
 // count sizes the partial-sum buffer.
 constexpr int kRhsPlanes = 16;
+constexpr int kRhsPartials = 4;   // per block: sum, max, min of f; OR of the guess's bits
 inline Grid3 rhs_grid(const int* n) {
     Grid3 g = grid3(n[0], n[1], 1);
     g.grid.z = ceil_div(n[2], kRhsPlanes);

@@ -401,12 +401,60 @@ k_resid64_to32(Dims F, const double* __restrict__ u, const double* __restrict__ 
     if (threadIdx.x == 0 && threadIdx.y == 0 && m) atomicMax(maxbits, m);
 }
 
+// phi += e, four cells a thread (n % 4 == 0; the level-0 arrays always qualify), else one.
+template <int V>
 __global__ void __launch_bounds__(kBlock)
 k_accumulate(int n, double* __restrict__ u, const float* __restrict__ e) {
     pdl_wait();
     pdl_trigger();
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < n) u[q] += (double)e[q];
+    const int q = (blockIdx.x * blockDim.x + threadIdx.x) * V;
+    if (q >= n) return;
+    if (V == 4) {
+        const float4 ev = *reinterpret_cast<const float4*>(e + q);
+        double2 a = *reinterpret_cast<const double2*>(u + q);
+        double2 b = *reinterpret_cast<const double2*>(u + q + 2);
+        a.x += (double)ev.x;
+        a.y += (double)ev.y;
+        b.x += (double)ev.z;
+        b.y += (double)ev.w;
+        *reinterpret_cast<double2*>(u + q) = a;
+        *reinterpret_cast<double2*>(u + q + 2) = b;
+    } else {
+        u[q] += (double)e[q];
+    }
+}
+
+// Initial residual of a guess that is +0 everywhere: r = f (the FMA chain of k_resid64_to32
+// gives f with -0 turned into +0), after f -= mean for a singular problem (the subtraction that
+// would otherwise be its own pass).  Two cells a thread.
+__global__ void __launch_bounds__(kBlock)
+k_first_resid_zero(int n, double* __restrict__ f, const double* __restrict__ mean,
+                   float* __restrict__ r32, float* __restrict__ e32,
+                   unsigned long long* __restrict__ maxbits) {
+    pdl_wait();
+    pdl_trigger();
+    const int q = (blockIdx.x * blockDim.x + threadIdx.x) * 2;
+    unsigned long long m = 0ull;
+    if (q < n) {
+        double2 v = *reinterpret_cast<const double2*>(f + q);
+        if (mean) {
+            const double mu = *mean;
+            v.x -= mu;
+            v.y -= mu;
+            *reinterpret_cast<double2*>(f + q) = v;
+        }
+        unsigned long long b0 = dbits(v.x), b1 = dbits(v.y);
+        b0 = b0 == 0x8000000000000000ull ? 0ull : b0;
+        b1 = b1 == 0x8000000000000000ull ? 0ull : b1;
+        const double r0 = __longlong_as_double((long long)b0);
+        const double r1 = __longlong_as_double((long long)b1);
+        *reinterpret_cast<float2*>(r32 + q) = make_float2(to_float_rn(r0), to_float_rn(r1));
+        *reinterpret_cast<float2*>(e32 + q) = make_float2(0.f, 0.f);
+        const unsigned long long a0 = abs_bits(r0), a1 = abs_bits(r1);
+        m = a0 > a1 ? a0 : a1;
+    }
+    m = block_max_u64(m);
+    if (threadIdx.x == 0 && m) atomicMax(maxbits, m);
 }
 
 // ---- single-CTA FP64 bottom solver (natural layout): device code in mac_bottom.cuh -------------
@@ -544,7 +592,18 @@ void launch_resid64_to32(const Dims& d, const LevelArrays<double>& a, float* r32
 }
 
 void launch_accumulate(const Dims& d, double* phi, const float* e, cudaStream_t s) {
-    launch_chain(k_accumulate, dim3(ceil_div(d.ncell, kBlock)), dim3(kBlock), 0, s, d.ncell, phi, e);
+    if (d.ncell % 4 == 0)
+        launch_chain(k_accumulate<4>, dim3(ceil_div(d.ncell / 4, kBlock)), dim3(kBlock), 0, s,
+                     d.ncell, phi, e);
+    else
+        launch_chain(k_accumulate<1>, dim3(ceil_div(d.ncell, kBlock)), dim3(kBlock), 0, s,
+                     d.ncell, phi, e);
+}
+
+void launch_first_resid_zero(const Dims& d, double* f, const double* mean, float* r32,
+                             float* e32, unsigned long long* maxbits, cudaStream_t s) {
+    launch_chain(k_first_resid_zero, dim3(ceil_div(d.ncell / 2, kBlock)), dim3(kBlock), 0, s,
+                 d.ncell, f, mean, r32, e32, maxbits);
 }
 
 template <typename Tio>

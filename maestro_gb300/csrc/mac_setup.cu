@@ -246,13 +246,15 @@ k_rhs(RhsParams P, Dims d, const double* __restrict__ ux, const double* __restri
       const double* __restrict__ tab, double* __restrict__ f, double* __restrict__ partial,
       const double* __restrict__ phi_nat, double* __restrict__ phi_l0) {
     __shared__ double ssum[8];
-    __shared__ unsigned long long smax[8], smin[8];
+    __shared__ unsigned long long smax[8], smin[8], sor[8];
     const int n0 = P.n[0], n1 = P.n[1], n2 = P.n[2];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k0 = blockIdx.z * kRhsPlanes;
     double sum = 0.0;
     unsigned long long mx = 0ull, mn = ~0ull;
+    // OR of the guess's bit patterns: 0 when phi is +0 everywhere (no guess given: unknown)
+    unsigned long long por = phi_nat ? 0ull : ~0ull;
     if (i < n0 && j < n1) {
         const int st = P.n[DM - 1] + 1;
         for (int k = k0; k < k0 + kRhsPlanes && k < n2; ++k) {
@@ -282,7 +284,11 @@ k_rhs(RhsParams P, Dims d, const double* __restrict__ ux, const double* __restri
             f[li] = v;
             // the initial guess moves to the level-0 layout in the same pass (this kernel is
             // bound by the FP64 pipe, the copy rides along in its memory slack)
-            if (phi_nat) phi_l0[li] = phi_nat[q];
+            if (phi_nat) {
+                const double g = phi_nat[q];
+                phi_l0[li] = g;
+                por |= (unsigned long long)__double_as_longlong(g);
+            }
             sum += v;
             const unsigned long long o = ordered_bits(v);
             mx = o > mx ? o : mx;
@@ -295,6 +301,7 @@ k_rhs(RhsParams P, Dims d, const double* __restrict__ ux, const double* __restri
         const unsigned long long b = __shfl_down_sync(0xffffffffu, mn, o);
         mx = a > mx ? a : mx;
         mn = b < mn ? b : mn;
+        por |= __shfl_down_sync(0xffffffffu, por, o);
     }
     const int t = threadIdx.x + blockDim.x * threadIdx.y;
     const int lane = t & 31, wid = t >> 5, nw = (blockDim.x * blockDim.y) >> 5;
@@ -302,37 +309,42 @@ k_rhs(RhsParams P, Dims d, const double* __restrict__ ux, const double* __restri
         ssum[wid] = sum;
         smax[wid] = mx;
         smin[wid] = mn;
+        sor[wid] = por;
     }
     __syncthreads();
     if (t == 0) {
         double s = 0.0;
-        unsigned long long a = 0ull, b = ~0ull;
+        unsigned long long a = 0ull, b = ~0ull, o = 0ull;
         for (int w = 0; w < nw; ++w) {
             s += ssum[w];
             a = smax[w] > a ? smax[w] : a;
             b = smin[w] < b ? smin[w] : b;
+            o |= sor[w];
         }
         const int blk = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-        partial[3 * blk + 0] = s;
-        partial[3 * blk + 1] = __longlong_as_double((long long)a);
-        partial[3 * blk + 2] = __longlong_as_double((long long)b);
+        partial[kRhsPartials * blk + 0] = s;
+        partial[kRhsPartials * blk + 1] = __longlong_as_double((long long)a);
+        partial[kRhsPartials * blk + 2] = __longlong_as_double((long long)b);
+        partial[kRhsPartials * blk + 3] = __longlong_as_double((long long)o);
     }
 }
 
 // Deterministic final reduction of the k_rhs partials: mean (singular problems) and
-// ||f - mean||_inf; NaN if anything is not finite.
+// ||f - mean||_inf; NaN if anything is not finite; [5] the OR of the guess's bit patterns.
 __global__ void k_rhs_final(int nblocks, int ncell, int singular, const double* __restrict__ partial,
                             double* __restrict__ scalars) {
     __shared__ double ssum[32];
-    __shared__ unsigned long long smax[32], smin[32];
+    __shared__ unsigned long long smax[32], smin[32], sor[32];
     double s = 0.0;
-    unsigned long long mx = 0ull, mn = ~0ull;
+    unsigned long long mx = 0ull, mn = ~0ull, por = 0ull;
     for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
-        s += partial[3 * b];
-        const unsigned long long a = (unsigned long long)__double_as_longlong(partial[3 * b + 1]);
-        const unsigned long long c = (unsigned long long)__double_as_longlong(partial[3 * b + 2]);
+        const double* pb = partial + kRhsPartials * b;
+        s += pb[0];
+        const unsigned long long a = (unsigned long long)__double_as_longlong(pb[1]);
+        const unsigned long long c = (unsigned long long)__double_as_longlong(pb[2]);
         mx = a > mx ? a : mx;
         mn = c < mn ? c : mn;
+        por |= (unsigned long long)__double_as_longlong(pb[3]);
     }
     for (int o = 16; o > 0; o >>= 1) {
         s += __shfl_down_sync(0xffffffffu, s, o);
@@ -340,22 +352,26 @@ __global__ void k_rhs_final(int nblocks, int ncell, int singular, const double* 
         const unsigned long long c = __shfl_down_sync(0xffffffffu, mn, o);
         mx = a > mx ? a : mx;
         mn = c < mn ? c : mn;
+        por |= __shfl_down_sync(0xffffffffu, por, o);
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0) {
         ssum[wid] = s;
         smax[wid] = mx;
         smin[wid] = mn;
+        sor[wid] = por;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         double t = 0.0;
-        unsigned long long a = 0ull, c = ~0ull;
+        unsigned long long a = 0ull, c = ~0ull, o = 0ull;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
             t += ssum[w];
             a = smax[w] > a ? smax[w] : a;
             c = smin[w] < c ? smin[w] : c;
+            o |= sor[w];
         }
+        scalars[5] = __longlong_as_double((long long)o);
         const double vmax = from_ordered_bits(a), vmin = from_ordered_bits(c);
         const double mean = singular ? t / ncell : 0.0;
         scalars[0] = mean;
@@ -740,16 +756,18 @@ int launch_rhs(mac_ctx* c, const double* macrhs, bool from_rh, const double* phi
                                            c->red.scalars);
     MAC_CUDA_TRY(cudaGetLastError());
     ++c->issued;
-    if (c->singular) {
-        k_sub_mean<<<ceil_div(L.d.ncell, kBlock), kBlock, 0, c->stream>>>(L.d.ncell, L.a64.f,
-                                                                         c->red.scalars);
-        MAC_CUDA_TRY(cudaGetLastError());
-        ++c->issued;
-    }
+    // the mean of a singular problem comes off f in the solve's first pass over f (run_solve)
+    c->mean_pending = c->singular;
     return MAC_OK;
 }
 
 }  // namespace
+
+void launch_sub_mean(mac_ctx* c) {
+    Level& L = c->lev[0];
+    k_sub_mean<<<ceil_div(L.d.ncell, kBlock), kBlock, 0, c->stream>>>(L.d.ncell, L.a64.f,
+                                                                     c->red.scalars);
+}
 
 int setup_rhs(mac_ctx* c, const double* macrhs, bool have_beta0, const double* phi_nat) {
     (void)have_beta0;   // the factor tables hold beta0 = 1 when there is none

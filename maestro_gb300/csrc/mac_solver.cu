@@ -412,6 +412,8 @@ int run_solve(mac_ctx* c, mac_stats* st) {
     st->fnorm = fnorm;
     if (!std::isfinite(fnorm)) return MAC_ERR_NONFINITE;
     MAC_CUDA_TRY(cudaMemsetAsync(c->red.counters, 0, sizeof(int), c->stream));
+    const bool mean_pending = c->mean_pending;
+    c->mean_pending = false;
     if (fnorm == 0.0) {
         MAC_CUDA_TRY(cudaMemsetAsync(F.a64.phi, 0, sizeof(double) * F.d.ncell, c->stream));
         st->rel_resid = 0.0;
@@ -420,18 +422,42 @@ int run_solve(mac_ctx* c, mac_stats* st) {
     auto converged = [&](double r) {
         return r <= o.rel_eps * fnorm || (o.abs_eps > 0.0 && r <= o.abs_eps);
     };
-    // initial residual of the caller's guess (both colours)
+    // initial residual of the caller's guess (both colours); f loses its mean (singular problem)
+    // on the way.  A guess that is +0 everywhere (the usual zero start) leaves r = f - mean, whose
+    // max-norm fnorm already is.
+    unsigned long long guess_bits;
+    std::memcpy(&guess_bits, &c->red.h_scalars[5], sizeof(guess_bits));
+    const bool zero_guess = guess_bits == 0ull;
+    double res;
     MAC_CUDA_TRY(cudaMemsetAsync(c->red.maxbits, 0, sizeof(unsigned long long), c->stream));
-    if (prec == MAC_PREC_FP64)
-        launch_resid_norm<double>(F.d, F.a64, false, c->red.maxbits, c->stream);
-    else
-        launch_resid64_to32(F.d, F.a64, F.a32.f, c->red.maxbits, c->stream, F.a32.phi);
-    ++c->issued;
+    if (prec == MAC_PREC_MIXED && zero_guess) {
+        launch_first_resid_zero(F.d, F.a64.f, mean_pending ? c->red.scalars : nullptr, F.a32.f,
+                                F.a32.phi, c->red.maxbits, c->stream);
+        ++c->issued;
+    } else {
+        if (mean_pending) {
+            launch_sub_mean(c);
+            ++c->issued;
+        }
+        if (prec == MAC_PREC_FP64) {
+            if (!zero_guess) {
+                launch_resid_norm<double>(F.d, F.a64, false, c->red.maxbits, c->stream);
+                ++c->issued;
+            }
+        } else {
+            launch_resid64_to32(F.d, F.a64, F.a32.f, c->red.maxbits, c->stream, F.a32.phi);
+            ++c->issued;
+        }
+    }
     MAC_CUDA_TRY(cudaGetLastError());
-    MAC_CUDA_TRY(cudaMemcpyAsync(c->red.h_maxbits, c->red.maxbits, sizeof(unsigned long long),
-                                 cudaMemcpyDeviceToHost, c->stream));
-    MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
-    double res = bits_to_double(*c->red.h_maxbits);
+    if (prec == MAC_PREC_FP64 && zero_guess) {
+        res = fnorm;   // max |f - mean| (rounding is monotone: equal to the cell-wise maximum)
+    } else {
+        MAC_CUDA_TRY(cudaMemcpyAsync(c->red.h_maxbits, c->red.maxbits, sizeof(unsigned long long),
+                                     cudaMemcpyDeviceToHost, c->stream));
+        MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        res = bits_to_double(*c->red.h_maxbits);
+    }
     st->resid0 = res;
     if (!std::isfinite(res)) return MAC_ERR_NONFINITE;
     int it = 0, nv_total = 0;
@@ -619,7 +645,7 @@ int ctx_alloc(mac_ctx* c) {
     const Grid3 rg = rhs_grid(c->n);
     const int nbp = (int)(rg.grid.x * rg.grid.y * rg.grid.z);
     c->red.nblocks_partial = nbp;
-    rc |= alloc_arr(c, &c->red.partial, (size_t)3 * nbp);
+    rc |= alloc_arr(c, &c->red.partial, (size_t)kRhsPartials * nbp);
     rc |= alloc_arr(c, &c->red.scalars, 8);
     rc |= alloc_arr(c, &c->red.counters, 4);
     rc |= alloc_arr(c, &c->red.maxbits, 1);
