@@ -446,16 +446,17 @@ def main():
         for s in sets:   # warm-up: one call on each page-locked set (first use maps the pages)
             P.macproject(s[1], s[3], s[2], s[4], c.beta0, c.beta0_edge, strict=True)
             refill(s)
-        step_s = []
+        step_s, dev_ms = [], []
         ck_e2e = Clocks(local, period_s=0.1)
         ck_e2e.start()
         for k in range(E):
             s = sets[(k + 1) % 2]
             barrier()
             t0 = time.perf_counter()
-            P.macproject(s[1], s[3], s[2], s[4], c.beta0, c.beta0_edge, strict=True)
+            st = P.macproject(s[1], s[3], s[2], s[4], c.beta0, c.beta0_edge, strict=True)
             barrier()
             step_s.append(time.perf_counter() - t0)
+            dev_ms.append(round(st["setup_ms"] + st["solve_ms"], 3))
             refill(s)
         ck_e2e = ck_e2e.stop()
         secs = max_over_ranks(sum(step_s))
@@ -463,6 +464,7 @@ def main():
         e2e = {"value": world * E / secs, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "steps": E,
                "ms_per_step": [round(x * 1e3, 3) for x in step_s],
+               "device_ms_per_step": dev_ms,
                "api": "mac_macproject (MAC_PTR_HOST; page-locked per-box fabs, 8 boxes of 128^3 "
                       "+ 1 ghost, copied by the copy engines on a transfer stream overlapped "
                       "with the setup and the copy-back)",
@@ -496,6 +498,8 @@ def main():
         "mixed_over_fp64": value / fp64_value,
         "mixed": {"refine_iters": st_mixed[-1]["refine_iters"], "inner_vcycles": args.inner,
                   "adaptive_inner": not args.fixed_inner,
+                  "inner_cycle": "V(%d,%d)" % (capi.default_opts().inner_nu1,
+                                               capi.default_opts().inner_nu2),
                   "vcycles": st_mixed[-1]["vcycles"], "rel_resid": rr,
                   "phi_err_vs_fp64": phi_err, "u_err_vs_fp64": u_err,
                   "ms_by_class": cls_ms},

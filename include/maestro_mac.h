@@ -107,6 +107,10 @@ typedef struct mac_opts {
                                tolerance the projected velocity can be further from the
                                converged one; 0 (default) = plain V-cycles, the reference's
                                iteration                                                       */
+    int inner_nu1, inner_nu2; /* mixed precision: GS-RB sweeps down / up the inner FP32
+                               V-cycles (default 2 / 1: at 256^3 one V-cycle more than with
+                               2 / 2, each a sixth cheaper; -1: nu1 / nu2); the FP64 V-cycle
+                               always uses nu1 / nu2                                           */
 } mac_opts;
 
 /* Kernel classes of mac_stats.ktime_* (finest level unless stated). */

@@ -71,6 +71,8 @@ class MacOpts(ctypes.Structure):
         ("coarse_tail", ctypes.c_int),
         ("adaptive_inner", ctypes.c_int),
         ("inner_krylov", ctypes.c_int),
+        ("inner_nu1", ctypes.c_int),
+        ("inner_nu2", ctypes.c_int),
     ]
 
 

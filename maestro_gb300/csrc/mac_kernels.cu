@@ -255,7 +255,8 @@ k_prolong_add(Dims F, Dims C, BcDesc bc, const T* __restrict__ ec, T* __restrict
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
     const int K = blockIdx.z;
-    if (I >= C.n0 || J >= C.n1) return;
+    // every lane stays to the shuffles below; lanes outside the level compute nothing
+    const bool valid = I < C.n0 && J < C.n1;
     int xs[3], ys[3], zs[3];
     T wxm, wxp, wym, wyp, wzm = T(0), wzp = T(0);
     xs[1] = I;
@@ -268,20 +269,17 @@ k_prolong_add(Dims F, Dims C, BcDesc bc, const T* __restrict__ ec, T* __restrict
         if (C.split) return ec[((X + Y + Z) & 1) * C.half + (Y + C.n1 * Z) * C.hn0 + (X >> 1)];
         return ec[X + C.n0 * (Y + C.n1 * Z)];
     };
-    // Yv[x][yc][zc]: value interpolated in z and y, still at coarse x-column x
-    T Yv[3][2][2];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const int X = xs[a];
+    // Y[yc][zc]: the coarse column X interpolated in z, then y (9 coarse values)
+    auto column = [&](int X, T (&Y)[2][2]) {
         T Zv[3][2];   // [y][zc]
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
-            const int Y = ys[b];
-            const T c0 = cval(X, Y, K);
+            const int Yi = ys[b];
+            const T c0 = cval(X, Yi, K);
             if (Z2) {
                 const T t = T(0.75) * c0;
-                Zv[b][0] = fmaT(wzm, cval(X, Y, zs[0]), t);
-                Zv[b][1] = fmaT(wzp, cval(X, Y, zs[2]), t);
+                Zv[b][0] = fmaT(wzm, cval(X, Yi, zs[0]), t);
+                Zv[b][1] = fmaT(wzp, cval(X, Yi, zs[2]), t);
             } else {
                 Zv[b][0] = c0;
                 Zv[b][1] = c0;
@@ -290,8 +288,45 @@ k_prolong_add(Dims F, Dims C, BcDesc bc, const T* __restrict__ ec, T* __restrict
 #pragma unroll
         for (int zc = 0; zc < 2; ++zc) {
             const T t = T(0.75) * Zv[1][zc];
-            Yv[a][0][zc] = fmaT(wym, Zv[0][zc], t);
-            Yv[a][1][zc] = fmaT(wyp, Zv[2][zc], t);
+            Y[0][zc] = fmaT(wym, Zv[0][zc], t);
+            Y[1][zc] = fmaT(wyp, Zv[2][zc], t);
+        }
+    };
+    // Yv[a]: columns I-1, I, I+1.  The own column is computed here; the neighbouring ones come
+    // from the lanes that computed them (same row, adjacent x) where those exist, else they are
+    // computed again (warp edges, periodic wrap) or are the own column (walls).  The arithmetic
+    // per column is the same whichever lane does it.
+    T Yv[3][2][2];
+    if (valid) column(I, Yv[1]);
+    else Yv[1][0][0] = Yv[1][0][1] = Yv[1][1][0] = Yv[1][1][1] = T(0);
+    T lft[2][2], rgt[2][2];
+#pragma unroll
+    for (int yc = 0; yc < 2; ++yc)
+#pragma unroll
+        for (int zc = 0; zc < 2; ++zc) {
+            lft[yc][zc] = __shfl_up_sync(0xffffffffu, Yv[1][yc][zc], 1);
+            rgt[yc][zc] = __shfl_down_sync(0xffffffffu, Yv[1][yc][zc], 1);
+        }
+    if (!valid) return;
+    const int lane = (threadIdx.x + blockDim.x * threadIdx.y) & 31;
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+        const int a = side ? 2 : 0;
+        const int X = xs[a];
+        const bool from_lane = side ? (X == I + 1 && lane < 31 && threadIdx.x + 1 < blockDim.x)
+                                    : (X == I - 1 && lane > 0 && threadIdx.x > 0);
+        if (from_lane) {
+#pragma unroll
+            for (int yc = 0; yc < 2; ++yc)
+#pragma unroll
+                for (int zc = 0; zc < 2; ++zc) Yv[a][yc][zc] = side ? rgt[yc][zc] : lft[yc][zc];
+        } else if (X == I) {
+#pragma unroll
+            for (int yc = 0; yc < 2; ++yc)
+#pragma unroll
+                for (int zc = 0; zc < 2; ++zc) Yv[a][yc][zc] = Yv[1][yc][zc];
+        } else {
+            column(X, Yv[a]);
         }
     }
     const int hn0 = F.hn0, n1 = F.n1;

@@ -124,6 +124,15 @@ inline void mark(mac_ctx* c, bool on, int slot) {
         cudaEventRecordWithFlags(c->tev[c->vtimer][slot], c->stream, cudaEventRecordExternal);
 }
 
+// GS-RB sweeps down / up a V-cycle: the FP32 (inner, mixed-precision) V-cycle may use its own
+// counts (inner_nu1/inner_nu2 >= 0), the FP64 V-cycle always uses nu1/nu2.
+int sweeps_down(const mac_ctx* c, bool fp32) {
+    return fp32 && c->o.inner_nu1 >= 0 ? c->o.inner_nu1 : c->o.nu1;
+}
+int sweeps_up(const mac_ctx* c, bool fp32) {
+    return fp32 && c->o.inner_nu2 >= 0 ? c->o.inner_nu2 : c->o.nu2;
+}
+
 template <typename T>
 void vcycle(mac_ctx* c, int l) {
     Level& L = c->lev[l];
@@ -131,6 +140,8 @@ void vcycle(mac_ctx* c, int l) {
     const mac_opts& o = c->o;
     const bool tm = o.timing && l == 0;
     const bool otf = std::is_same<T, float>::value && l == 0 && c->otf;
+    const int nu1 = sweeps_down(c, std::is_same<T, float>::value);
+    const int nu2 = sweeps_up(c, std::is_same<T, float>::value);
     if (l == c->nlevels - 1) {
         launch_bottom<T>(L.d, L.a64, a.phi, a.f, c->bottom_scratch, c->singular, o.nub,
                          o.bottom_eps, o.bottom_max_iter, c->red.counters, c->stream);
@@ -161,8 +172,8 @@ void vcycle(mac_ctx* c, int l) {
         tp.f0 = a.f;
         tp.e0 = a.phi;
         tp.bc = bc_desc(c);
-        tp.nu1 = o.nu1;
-        tp.nu2 = o.nu2;
+        tp.nu1 = nu1;
+        tp.nu2 = nu2;
         tp.nub = o.nub;
         tp.singular = c->singular ? 1 : 0;
         tp.bottom_max_iter = o.bottom_max_iter;
@@ -184,7 +195,7 @@ void vcycle(mac_ctx* c, int l) {
         c->issued += 2;
     };
     mark(c, tm, 0);
-    for (int s = 0; s < o.nu1; ++s) sweep();
+    for (int s = 0; s < nu1; ++s) sweep();
     Level& C = c->lev[l + 1];
     LevelArrays<T>& ac = arrays<T>(C);
     mark(c, tm, 1);
@@ -192,18 +203,18 @@ void vcycle(mac_ctx* c, int l) {
         launch_resid_restrict_otf(L.d, C.d, P, reinterpret_cast<const float*>(a.phi),
                                   reinterpret_cast<const float*>(a.f),
                                   reinterpret_cast<float*>(ac.f), reinterpret_cast<float*>(ac.phi),
-                                  o.nu1 > 0, c->stream);
+                                  nu1 > 0, c->stream);
     else
-        launch_resid_restrict<T>(L.d, C.d, a, ac.f, ac.phi, o.nu1 > 0, c->stream);
+        launch_resid_restrict<T>(L.d, C.d, a, ac.f, ac.phi, nu1 > 0, c->stream);
     ++c->issued;
     mark(c, tm, 2);   // (the restriction also zeroed the coarse correction ac.phi)
     vcycle<T>(c, l + 1);
     mark(c, tm, 3);
     // with post-smoothing, only colour-1 cells need the correction (see k_prolong_add)
-    launch_prolong_add<T>(L.d, C.d, bc_desc(c), ac.phi, a.phi, o.nu2 > 0, c->stream);
+    launch_prolong_add<T>(L.d, C.d, bc_desc(c), ac.phi, a.phi, nu2 > 0, c->stream);
     ++c->issued;
     mark(c, tm, 4);
-    for (int s = 0; s < o.nu2; ++s) sweep();
+    for (int s = 0; s < nu2; ++s) sweep();
     mark(c, tm, 5);
 }
 
@@ -211,7 +222,7 @@ void vcycle(mac_ctx* c, int l) {
 // colour-1 half-sweep the V-cycle output satisfies L z = r on colour 1, which the Krylov kernels
 // use).
 bool use_krylov(const mac_ctx* c, int prec) {
-    return prec == MAC_PREC_MIXED && c->o.inner_krylov && c->o.nu2 > 0;
+    return prec == MAC_PREC_MIXED && c->o.inner_krylov && sweeps_up(c, true) > 0;
 }
 
 int ensure_krylov(mac_ctx* c) {
@@ -305,7 +316,8 @@ void collect_timing(mac_ctx* c, int prec) {
             cudaEventElapsedTime(&t[e], c->tev[v][e], c->tev[v][e + 1]);
         }
         c->ktime_ms[MAC_KT_SMOOTH] += t[0] + t[4];
-        c->ktime_launches[MAC_KT_SMOOTH] += 2 * (o.nu1 + o.nu2);
+        c->ktime_launches[MAC_KT_SMOOTH] +=
+            2 * (sweeps_down(c, prec == MAC_PREC_MIXED) + sweeps_up(c, prec == MAC_PREC_MIXED));
         c->ktime_ms[MAC_KT_RESTRICT] += t[1];
         c->ktime_launches[MAC_KT_RESTRICT] += 1;
         c->ktime_ms[MAC_KT_COARSE] += t[2];
@@ -548,6 +560,7 @@ int check_opts(const mac_opts* o) {
     if (o->precision != MAC_PREC_FP64 && o->precision != MAC_PREC_MIXED) return MAC_ERR_INVALID;
     if (o->nu1 < 0 || o->nu2 < 0 || o->nub < 0 || o->max_vcycles < 0 || o->bottom_max_iter < 0)
         return MAC_ERR_INVALID;
+    if (o->inner_nu1 < -1 || o->inner_nu2 < -1) return MAC_ERR_INVALID;
     if (!(o->rel_eps >= 0.0)) return MAC_ERR_INVALID;
     return MAC_OK;
 }
@@ -848,6 +861,8 @@ void mac_default_opts(mac_opts* o) {
     o->coarse_tail = 1;
     o->adaptive_inner = 1;
     o->inner_krylov = 0;
+    o->inner_nu1 = 2;
+    o->inner_nu2 = 1;
 }
 
 const char* mac_strerror(int code) {
