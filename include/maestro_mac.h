@@ -111,6 +111,9 @@ typedef struct mac_opts {
                                V-cycles (default 2 / 1: at 256^3 one V-cycle more than with
                                2 / 2, each a sixth cheaper; -1: nu1 / nu2); the FP64 V-cycle
                                always uses nu1 / nu2                                           */
+    int inner_exact_bottom; /* mixed precision, 1 (default): the inner V-cycles solve a bottom of
+                               at most 64 cells exactly, by its dense FP64 (pseudo-)inverse
+                               formed once per solve; 0: FP64 BiCGStab as the FP64 V-cycle     */
 } mac_opts;
 
 /* Kernel classes of mac_stats.ktime_* (finest level unless stated). */

@@ -73,6 +73,7 @@ class MacOpts(ctypes.Structure):
         ("inner_krylov", ctypes.c_int),
         ("inner_nu1", ctypes.c_int),
         ("inner_nu2", ctypes.c_int),
+        ("inner_exact_bottom", ctypes.c_int),
     ]
 
 

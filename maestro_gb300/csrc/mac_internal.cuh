@@ -291,6 +291,10 @@ struct mac_ctx {
     bool otf = false;                             // finest-level FP32 kernels use rho32
     mac::KrylovBufs kry;                          // flexible-CG vectors (allocated on first use)
     bool mean_pending = false;                    // f still holds the mean (singular problem)
+    double* bot_inv = nullptr;                    // dense bottom (pseudo-)inverse (small bottoms)
+    cudaStream_t aux = nullptr;                   // side stream of the bottom inverse
+    cudaEvent_t aux_ev[2] = {nullptr, nullptr};   // [0] operators ready, [1] inverse done
+    bool inv_pending = false;                     // the main stream still has to wait on aux_ev[1]
     int tail_start[2] = {-1, -1};                 // first tail level (FP64, FP32); -1: none
     size_t tail_smem[2] = {0, 0};
     double ktime_ms[8] = {};
@@ -366,16 +370,26 @@ struct TailParams {
     int nu1, nu2, nub, singular, bottom_max_iter;
     double bottom_eps;
     int* iters;
+    const double* binv;                   // dense (pseudo-)inverse of the bottom; null: BiCGStab
 };
 template <typename T>
 size_t tail_smem_bytes(const Dims* lev, int nl, const Dims& bottom);
 template <typename T>
 void launch_tail(const TailParams<T>& P, size_t smem, cudaStream_t s);
 int prepare_tail_kernels();
+// exact bottom solve of the FP32 V-cycle: bottoms of at most kDenseBottomMax cells, row r of the
+// inverse applied by kDenseSeg lanes of a warp
+constexpr int kDenseBottomMax = 64;
+constexpr int kDenseSeg = 16;
+void launch_bottom_inverse(const Dims& d, const double* bx, const double* by, const double* bz,
+                           const double* dg, bool singular, double* out, cudaStream_t s);
 
 // ---- setup kernels (mac_setup.cu) -----------------------------------------------------------
 int setup_fine_coefficients(mac_ctx* c, const double* beta0, const double* beta0e);
 int setup_coarse_levels(mac_ctx* c);
+// the exact bottom's (pseudo-)inverse, on the side stream once the bottom operator is built
+// (no-op unless the FP32 V-cycle uses it); run_solve orders the V-cycles after it
+int issue_bottom_inverse(mac_ctx* c);
 int setup_fp32_copies(mac_ctx* c);
 // phi_nat (optional): the initial guess in natural layout, moved into the level-0 phi in the same pass
 int setup_rhs(mac_ctx* c, const double* macrhs, bool have_beta0, const double* phi_nat = nullptr);

@@ -701,7 +701,7 @@ int setup_coarse_levels(mac_ctx* c) {
         int rc = build_diag(c, l, fp32);
         if (rc) return rc;
     }
-    return MAC_OK;
+    return issue_bottom_inverse(c);
 }
 
 // FP32 copies of the finest level's operator for the mixed-precision inner cycle when its

@@ -124,6 +124,12 @@ inline void mark(mac_ctx* c, bool on, int slot) {
         cudaEventRecordWithFlags(c->tev[c->vtimer][slot], c->stream, cudaEventRecordExternal);
 }
 
+// The FP32 V-cycle's bottom solved exactly by the dense (pseudo-)inverse (small bottoms, run
+// through the tail kernel); the FP64 V-cycle keeps BiCGStab.
+bool exact_bottom(const mac_ctx* c) {
+    return c->o.inner_exact_bottom && c->o.coarse_tail && c->bot_inv != nullptr;
+}
+
 // GS-RB sweeps down / up a V-cycle: the FP32 (inner, mixed-precision) V-cycle may use its own
 // counts (inner_nu1/inner_nu2 >= 0), the FP64 V-cycle always uses nu1/nu2.
 int sweeps_down(const mac_ctx* c, bool fp32) {
@@ -179,6 +185,7 @@ void vcycle(mac_ctx* c, int l) {
         tp.bottom_max_iter = o.bottom_max_iter;
         tp.bottom_eps = o.bottom_eps;
         tp.iters = c->red.counters;
+        tp.binv = std::is_same<T, float>::value && exact_bottom(c) ? c->bot_inv : nullptr;
         launch_tail<T>(tp, c->tail_smem[tslot], c->stream);
         ++c->issued;
         return;
@@ -413,6 +420,14 @@ int run_solve(mac_ctx* c, mac_stats* st) {
         int rc = setup_fp32_copies(c);
         if (rc) return rc;
         if (use_krylov(c, prec) && (rc = ensure_krylov(c))) return rc;
+        if (exact_bottom(c)) {
+            if (!c->inv_pending) {   // (a caller that built the levels some other way)
+                int rc2 = issue_bottom_inverse(c);
+                if (rc2) return rc2;
+            }
+            MAC_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->aux_ev[1], 0));
+            c->inv_pending = false;
+        }
     }
     MAC_CUDA_TRY(cudaMemcpyAsync(c->red.h_scalars, c->red.scalars, 8 * sizeof(double),
                                  cudaMemcpyDeviceToHost, c->stream));
@@ -640,6 +655,8 @@ int ctx_alloc(mac_ctx* c) {
         }
     }
     rc |= alloc_arr(c, &c->bottom_scratch, (size_t)(2 + kBotScrPerCell) * B.d.ncell);
+    if (c->tail_start[1] >= 0 && B.d.ncell <= kDenseBottomMax)
+        rc |= alloc_arr(c, &c->bot_inv, (size_t)B.d.ncell * B.d.ncell);
     for (int d = 0; d < c->dm; ++d) {
         const size_t nf = (size_t)(c->n[0] + (d == 0)) * (c->n[1] + (d == 1)) * (c->n[2] + (d == 2));
         rc |= alloc_arr(c, &c->u[d], nf);
@@ -683,6 +700,8 @@ int ctx_alloc(mac_ctx* c) {
     MAC_CUDA_TRY(cudaMemset(c->red.counters, 0, 4 * sizeof(int)));
     // copy-engine stream of host-pointer calls (independent of the legacy stream) and its events
     MAC_CUDA_TRY(cudaStreamCreateWithFlags(&c->xfer, cudaStreamNonBlocking));
+    MAC_CUDA_TRY(cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : c->aux_ev) MAC_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     for (cudaEvent_t& e : c->xev) MAC_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     return MAC_OK;
 }
@@ -690,6 +709,7 @@ int ctx_alloc(mac_ctx* c) {
 void ctx_free(mac_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->xfer) cudaStreamSynchronize(c->xfer);
+    if (c->aux) cudaStreamSynchronize(c->aux);
     drop_graphs(c);
     for (void* p : c->allocations) cudaFree(p);
     c->allocations.clear();
@@ -712,6 +732,13 @@ void ctx_free(mac_ctx* c) {
         }
     if (c->xfer) cudaStreamDestroy(c->xfer);
     c->xfer = nullptr;
+    for (cudaEvent_t& e : c->aux_ev)
+        if (e) {
+            cudaEventDestroy(e);
+            e = nullptr;
+        }
+    if (c->aux) cudaStreamDestroy(c->aux);
+    c->aux = nullptr;
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     c->stream = nullptr;
 }
@@ -831,6 +858,24 @@ int forward_projection(mac_ctx* c, const double* macrhs, bool have_beta0, mac_st
     return core_macproject(c, macrhs, have_beta0, st);
 }
 int set_call_state(mac_ctx* c, bool with_alpha) { return set_call_state_impl(c, with_alpha); }
+
+int issue_bottom_inverse(mac_ctx* c) {
+    // an inverse issued by a call that stopped before its solve may still read the operator the
+    // main stream is about to rebuild
+    if (c->inv_pending) MAC_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->aux_ev[1], 0));
+    c->inv_pending = false;
+    if (c->o.precision != MAC_PREC_MIXED || !exact_bottom(c)) return MAC_OK;
+    const Level& B = c->lev[c->nlevels - 1];
+    MAC_CUDA_TRY(cudaEventRecord(c->aux_ev[0], c->stream));
+    MAC_CUDA_TRY(cudaStreamWaitEvent(c->aux, c->aux_ev[0], 0));
+    launch_bottom_inverse(B.d, B.a64.bx, B.a64.by, B.a64.bz, B.a64.diag, c->singular, c->bot_inv,
+                          c->aux);
+    MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
+    MAC_CUDA_TRY(cudaEventRecord(c->aux_ev[1], c->aux));
+    c->inv_pending = true;
+    return MAC_OK;
+}
 int load_beta0(mac_ctx* c, int ptr_kind, const double* b0, const double* b0e) {
     return load_beta0_impl(c, ptr_kind, b0, b0e);
 }
@@ -863,6 +908,7 @@ void mac_default_opts(mac_opts* o) {
     o->inner_krylov = 0;
     o->inner_nu1 = 2;
     o->inner_nu2 = 1;
+    o->inner_exact_bottom = 1;
 }
 
 const char* mac_strerror(int code) {

@@ -316,14 +316,38 @@ k_tail(TailParams<T> P) {
             tail_restrict<T, double>(L[l], BD.n0, BD.n1, BD.n2, fb, P.nu1 > 0);
         }
     }
-    // bottom: one warp, FP64 (input rhs rounded through T as in the multi-kernel path)
-    for (int c = tid; c < NB; c += nt) xb[c] = 0.0;
-    __syncthreads();
+    // bottom, FP64 (input rhs rounded through T as in the multi-kernel path)
     int count = 0;
     __shared__ double sm_red[33];
-    if (tid < 128)
-        count = bottom_body<Sync128<true>>(v, xb, fb, wb, sm_red, P.singular, P.nub, P.bottom_eps,
-                                           P.bottom_max_iter);
+    if (P.binv) {
+        // exact solve by the precomputed (pseudo-)inverse: x = B^-1 (f - mean f) (the mean comes
+        // off for a singular operator, whose constant mode B^-1 only scales)
+        if (P.singular) {
+            if (tid < 32) {
+                double s = 0.0;
+                for (int c = tid; c < NB; c += 32) s += fb[c];
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                if (tid == 0) sm_red[32] = s / NB;
+            }
+            __syncthreads();
+            const double mean = sm_red[32];
+            for (int c = tid; c < NB; c += nt) fb[c] -= mean;
+            __syncthreads();
+        }
+        // row r of B^-1 by kDenseSeg lanes of one warp (NB <= kDenseBottomMax: one pass)
+        const int r = tid / kDenseSeg, sg = tid % kDenseSeg;
+        double acc = 0.0;
+        if (r < NB)
+            for (int c = sg; c < NB; c += kDenseSeg) acc = fma(__ldg(P.binv + (size_t)r * NB + c), fb[c], acc);
+        for (int o = kDenseSeg / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (r < NB && sg == 0) xb[r] = acc;
+    } else {
+        for (int c = tid; c < NB; c += nt) xb[c] = 0.0;
+        __syncthreads();
+        if (tid < 128)
+            count = bottom_body<Sync128<true>>(v, xb, fb, wb, sm_red, P.singular, P.nub,
+                                               P.bottom_eps, P.bottom_max_iter);
+    }
     __syncthreads();
     // the bottom solution is handed up as T, like the multi-kernel path's bottom output
     T* eb = reinterpret_cast<T*>(wb);
@@ -345,6 +369,99 @@ k_tail(TailParams<T> P) {
         for_split_cells(P.lev[0], [&](int g, int c) { ge[g] = e[c]; });
     }
     if (tid == 0 && P.iters) atomicAdd(P.iters, count);
+}
+
+// (Pseudo-)inverse of the bottom operator for the exact bottom solve of the FP32 V-cycle: the
+// dense N x N matrix of A x = diag x - sum_n a_n x_n (N <= kDenseBottomMax, natural layout; a
+// periodic arm that wraps onto the same neighbour twice adds up), plus sigma 1 1^T with sigma =
+// mean(diag) / N when A is singular (constant null space: B^-1 f = A^+ f for f of zero mean).
+// B is symmetric positive definite, so it is inverted by the symmetric sweep operator (Gauss-
+// Jordan elimination without pivoting that keeps the matrix symmetric; after sweeping every
+// pivot the matrix holds -B^-1), updating only the upper triangle: N (N + 1) / 2 FMAs a pivot,
+// each thread owning fixed elements of the packed triangle so that warps stay full (GB300 issues
+// FP64 instructions per warp, whatever the number of active lanes).  FP64, shared memory, one
+// CTA, once per solve (on a side stream, overlapping the right-hand-side setup).
+constexpr int kInvPerThread = (kDenseBottomMax * (kDenseBottomMax + 1) / 2 + kTailThreads - 1) / kTailThreads;
+
+__global__ void __launch_bounds__(kTailThreads)
+k_bottom_inverse(Dims D, const double* __restrict__ bx, const double* __restrict__ by,
+                 const double* __restrict__ bz, const double* __restrict__ dg, int singular,
+                 double* __restrict__ out) {
+    __shared__ double M[kDenseBottomMax * kDenseBottomMax];
+    __shared__ double row[kDenseBottomMax], sk[kDenseBottomMax];
+    __shared__ double sdiag, sip;
+    const int N = D.ncell, tid = threadIdx.x, nt = blockDim.x;
+    if (tid < 32) {
+        double s = 0.0;
+        for (int c = tid; c < N; c += 32) s += dg[c];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (tid == 0) sdiag = singular ? s / ((double)N * N) : 0.0;
+    }
+    __syncthreads();
+    for (int q = tid; q < N * N; q += nt) M[q] = sdiag;
+    __syncthreads();
+    // row c by thread c (its six arms load in parallel with the other rows')
+    if (tid < N) {
+        const int c = tid;
+        const int i = c % D.n0, rw = c / D.n0, j = rw % D.n1, k = rw / D.n1;
+        const int im = i == 0 ? D.n0 - 1 : i - 1, ip = i == D.n0 - 1 ? 0 : i + 1;
+        const int jm = j == 0 ? D.n1 - 1 : j - 1, jp = j == D.n1 - 1 ? 0 : j + 1;
+        const int km = k == 0 ? D.n2 - 1 : k - 1, kp = k == D.n2 - 1 ? 0 : k + 1;
+        const int nbr[6] = {im + D.n0 * (j + D.n1 * k), ip + D.n0 * (j + D.n1 * k),
+                            i + D.n0 * (jm + D.n1 * k), i + D.n0 * (jp + D.n1 * k),
+                            i + D.n0 * (j + D.n1 * km), i + D.n0 * (j + D.n1 * kp)};
+        const double a[6] = {bx[c], bx[nbr[1]], by[c], by[nbr[3]], bz[c], bz[nbr[5]]};
+        M[c * N + c] += dg[c];
+        for (int n = 0; n < 6; ++n) M[c * N + nbr[n]] -= a[n];
+    }
+    // the upper-triangle elements (i <= j) this thread updates: packed indices tid + m nt
+    int ei[kInvPerThread], ej[kInvPerThread];
+    const int npk = N * (N + 1) / 2;
+#pragma unroll
+    for (int m = 0; m < kInvPerThread; ++m) {
+        int p = tid + m * nt, i = 0;
+        ei[m] = -1;
+        ej[m] = 0;
+        if (p < npk) {
+            while (p >= N - i) {
+                p -= N - i;
+                ++i;
+            }
+            ei[m] = i;
+            ej[m] = i + p;
+        }
+    }
+    __syncthreads();
+    for (int k = 0; k < N; ++k) {
+        // row k of the symmetric matrix (upper-triangle storage) and the pivot's reciprocal
+        if (tid < N) row[tid] = tid < k ? M[tid * N + k] : M[k * N + tid];
+        if (tid == 0) sip = recip_nr(M[k * N + k]);
+        __syncthreads();
+        if (tid < N) sk[tid] = row[tid] * sip;
+        __syncthreads();
+#pragma unroll
+        for (int m = 0; m < kInvPerThread; ++m) {
+            const int i = ei[m], j = ej[m];
+            if (i < 0) continue;
+            double& v = M[i * N + j];
+            if (i == k)
+                v = j == k ? -sip : sk[j];
+            else if (j == k)
+                v = sk[i];
+            else
+                v = fma(-row[i], sk[j], v);
+        }
+        __syncthreads();
+    }
+    for (int q = tid; q < N * N; q += nt) {
+        const int i = q / N, j = q - i * N;
+        out[q] = -(i <= j ? M[i * N + j] : M[j * N + i]);
+    }
+}
+
+void launch_bottom_inverse(const Dims& d, const double* bx, const double* by, const double* bz,
+                           const double* dg, bool singular, double* out, cudaStream_t s) {
+    k_bottom_inverse<<<1, kTailThreads, 0, s>>>(d, bx, by, bz, dg, singular ? 1 : 0, out);
 }
 
 template <typename T>

@@ -149,10 +149,11 @@ def test_tight_tolerance_agreement(cuda_lib, precision):
 @pytest.mark.parametrize("name", ["strat64_b32", "stiff48_b16"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_coarse_tail_is_bitwise_identical(cuda_lib, name, precision):
-    # the single-CTA tail of the V-cycle runs the same arithmetic as the per-level kernels
+    # the single-CTA tail of the V-cycle runs the same arithmetic as the per-level kernels (with
+    # the same bottom solver: the exact dense bottom of the inner V-cycles exists only in the tail)
     c = build3d(name)
-    u1, phi1, st1 = gpu_project(c, precision, coarse_tail=1)
-    u0, phi0, st0 = gpu_project(c, precision, coarse_tail=0)
+    u1, phi1, st1 = gpu_project(c, precision, coarse_tail=1, inner_exact_bottom=0)
+    u0, phi0, st0 = gpu_project(c, precision, coarse_tail=0, inner_exact_bottom=0)
     np.testing.assert_array_equal(phi1, phi0)
     for a, b in zip(u1, u0):
         np.testing.assert_array_equal(a, b)
@@ -162,8 +163,8 @@ def test_coarse_tail_is_bitwise_identical(cuda_lib, name, precision):
 def test_coarse_tail_2d(cuda_lib):
     from maestro_gb300.inputs import config_case
     c = config_case("2d_128", seed=7)
-    u1, phi1, st1 = gpu_project(c, "mixed", coarse_tail=1)
-    u0, phi0, st0 = gpu_project(c, "mixed", coarse_tail=0)
+    u1, phi1, st1 = gpu_project(c, "mixed", coarse_tail=1, inner_exact_bottom=0)
+    u0, phi0, st0 = gpu_project(c, "mixed", coarse_tail=0, inner_exact_bottom=0)
     np.testing.assert_array_equal(phi1, phi0)
 
 
@@ -351,3 +352,19 @@ def test_full_size_256_mixed_matches_fp64(cuda_lib):
     assert float((p32 - p64).abs().max()) <= 1e-9 * scale(p64)
     for a, b in zip(u32, u64):
         assert float((a - b).abs().max()) <= 1e-9 * scale(b)
+
+
+@pytest.mark.parametrize("exact", [0, 1])
+@pytest.mark.parametrize("name", ["strat64_b32", "outlet32_b16", "walls32x16x32"])
+def test_mixed_exact_bottom(cuda_lib, name, exact):
+    # the inner V-cycles' bottom (<= 64 cells) solved by its dense FP64 (pseudo-)inverse, or by
+    # BiCGStab as in the FP64 V-cycle: both reach the tolerance and match the oracle
+    c = build3d(name)
+    singular = all(b != BC_DIR for b in c.bc_lo + c.bc_hi)
+    u_o, phi_o, st_o = oracle_project(c)
+    u, phi, st = gpu_project(c, "mixed", inner_exact_bottom=exact)
+    assert st["status"] == 0 and st["rel_resid"] <= 1e-10
+    assert true_rel_resid(c, phi) <= 1.5e-10
+    assert phi_rel_err(phi, phi_o, singular) <= 1e-8
+    assert u_rel_err(u, u_o) <= 1e-8
+    assert (st["bottom_iters"] == 0) == bool(exact)
