@@ -296,6 +296,26 @@ k_prolong_add(Dims F, Dims C, BcDesc bc, const T* __restrict__ ec, T* __restrict
     // from the lanes that computed them (same row, adjacent x) where those exist, else they are
     // computed again (warp edges, periodic wrap) or are the own column (walls).  The arithmetic
     // per column is the same whichever lane does it.
+    // the fine values to update are loaded first: their DRAM latency overlaps the coarse loads
+    // and the interpolation instead of following them
+    const int hn0 = F.hn0, n1 = F.n1;
+    constexpr int kNz = Z2 ? 2 : 1;
+    T fold[kNz][2][2];
+    if (valid) {
+#pragma unroll
+        for (int zc = 0; zc < kNz; ++zc)
+#pragma unroll
+            for (int yc = 0; yc < 2; ++yc) {
+                const int base = (2 * J + yc + n1 * (Z2 ? 2 * K + zc : K)) * hn0 + I;
+                const int c0 = (yc + zc) & 1;
+                if (BLACK_ONLY) {
+                    fold[zc][yc][0] = u[F.half + base];
+                } else {
+                    fold[zc][yc][0] = u[c0 * F.half + base];
+                    fold[zc][yc][1] = u[(c0 ^ 1) * F.half + base];
+                }
+            }
+    }
     T Yv[3][2][2];
     if (valid) column(I, Yv[1]);
     else Yv[1][0][0] = Yv[1][0][1] = Yv[1][1][0] = Yv[1][1][1] = T(0);
@@ -329,9 +349,8 @@ k_prolong_add(Dims F, Dims C, BcDesc bc, const T* __restrict__ ec, T* __restrict
             column(X, Yv[a]);
         }
     }
-    const int hn0 = F.hn0, n1 = F.n1;
 #pragma unroll
-    for (int zc = 0; zc < (Z2 ? 2 : 1); ++zc) {
+    for (int zc = 0; zc < kNz; ++zc) {
 #pragma unroll
         for (int yc = 0; yc < 2; ++yc) {
             const T t = T(0.75) * Yv[1][yc][zc];
@@ -342,12 +361,115 @@ k_prolong_add(Dims F, Dims C, BcDesc bc, const T* __restrict__ ec, T* __restrict
             if (BLACK_ONLY) {
                 // the colour-1 child: 2I when c0 == 1, else 2I+1
                 const T v = c0 ? fmaT(wxm, Yv[0][yc][zc], t) : fmaT(wxp, Yv[2][yc][zc], t);
-                u[F.half + base] += v;
+                u[F.half + base] = fold[zc][yc][0] + v;
             } else {
                 const T v0 = fmaT(wxm, Yv[0][yc][zc], t);
                 const T v1 = fmaT(wxp, Yv[2][yc][zc], t);
-                u[c0 * F.half + base] += v0;
-                u[(c0 ^ 1) * F.half + base] += v1;
+                u[c0 * F.half + base] = fold[zc][yc][0] + v0;
+                u[(c0 ^ 1) * F.half + base] = fold[zc][yc][1] + v1;
+            }
+        }
+    }
+}
+
+// 3-D prolongation marching up z: a thread owns coarse column (I, J) for a chunk of planes and
+// keeps the three coarse planes K-1, K, K+1 of its column's rows J-1, J, J+1 in registers (three
+// loads a plane); the x-neighbour columns come from the adjacent lanes.  Each warp covers 30
+// columns: lanes 0 and 31 only compute the columns left and right of them (periodic wrap or, at a
+// wall, the edge column itself, which is what the wall reflection uses).  The arithmetic per
+// fine cell is k_prolong_add's, operation for operation.
+template <typename T, bool BLACK_ONLY>
+__global__ void __launch_bounds__(kBlock)
+k_prolong_z(Dims F, Dims C, BcDesc bc, const T* __restrict__ ec, T* __restrict__ u, int kc) {
+    pdl_wait();
+    pdl_trigger();
+    const int lane = threadIdx.x & 31;
+    const int warp = (threadIdx.x >> 5) + (blockDim.x >> 5) * blockIdx.x;
+    const int I = warp * 30 + lane - 1;
+    const int J = blockIdx.y;
+    const int K0 = blockIdx.z * kc;
+    const int K1 = min(K0 + kc, C.n2);
+    // the column this lane computes: its own, or the wrapped / clamped one beyond the ends
+    const int X = I < 0 ? (bc.lo[0] == MAC_BC_PER ? C.n0 - 1 : 0)
+                        : (I >= C.n0 ? (bc.hi[0] == MAC_BC_PER ? 0 : C.n0 - 1) : I);
+    const bool out = lane >= 1 && lane <= 30 && I < C.n0;
+    int ys[3];
+    T wym, wyp, wxm = T(0), wxp = T(0);
+    ys[1] = J;
+    coarse_nb<T>(J, C.n1, bc.lo[1], bc.hi[1], ys[0], ys[2], wym, wyp);
+    if (out) {
+        int xm, xp;
+        coarse_nb<T>(I, C.n0, bc.lo[0], bc.hi[0], xm, xp, wxm, wxp);
+    }
+    auto cval = [&](int Y, int Z) -> T {
+        if (C.split) return ec[((X + Y + Z) & 1) * C.half + (Y + C.n1 * Z) * C.hn0 + (X >> 1)];
+        return ec[X + C.n0 * (Y + C.n1 * Z)];
+    };
+    // planes K-1 (cm), K (c0), K+1 (cp) of rows ys[0..2], as coarse_nb indexes them (wrap or
+    // clamp; the wall weight carries the sign)
+    int zm, zp;
+    T wzm, wzp;
+    coarse_nb<T>(K0, C.n2, bc.lo[2], bc.hi[2], zm, zp, wzm, wzp);
+    T cm[3], c0[3], cp[3];
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+        cm[b] = cval(ys[b], zm);
+        c0[b] = cval(ys[b], K0);
+        cp[b] = cval(ys[b], zp);
+    }
+    const int hn0 = F.hn0, n1 = F.n1;
+#pragma unroll 2
+    for (int K = K0; K < K1; ++K) {
+        if (K > K0) {
+            coarse_nb<T>(K, C.n2, bc.lo[2], bc.hi[2], zm, zp, wzm, wzp);
+            // the window moves up one plane: K-1 <- K, K <- K+1, K+1 loaded (at a wall K-1 or
+            // K+1 is plane K itself, which coarse_nb's index already says)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                const T nk = cp[b];
+                cm[b] = zm == K - 1 ? c0[b] : cval(ys[b], zm);
+                c0[b] = nk;
+                cp[b] = cval(ys[b], zp);
+            }
+        }
+        T Zv[3][2];
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            const T t = T(0.75) * c0[b];
+            Zv[b][0] = fmaT(wzm, cm[b], t);
+            Zv[b][1] = fmaT(wzp, cp[b], t);
+        }
+        T Yc[2][2], lft[2][2], rgt[2][2];
+#pragma unroll
+        for (int zc = 0; zc < 2; ++zc) {
+            const T t = T(0.75) * Zv[1][zc];
+            Yc[0][zc] = fmaT(wym, Zv[0][zc], t);
+            Yc[1][zc] = fmaT(wyp, Zv[2][zc], t);
+        }
+#pragma unroll
+        for (int yc = 0; yc < 2; ++yc)
+#pragma unroll
+            for (int zc = 0; zc < 2; ++zc) {
+                lft[yc][zc] = __shfl_up_sync(0xffffffffu, Yc[yc][zc], 1);
+                rgt[yc][zc] = __shfl_down_sync(0xffffffffu, Yc[yc][zc], 1);
+            }
+        if (!out) continue;
+#pragma unroll
+        for (int zc = 0; zc < 2; ++zc) {
+#pragma unroll
+            for (int yc = 0; yc < 2; ++yc) {
+                const T t = T(0.75) * Yc[yc][zc];
+                const int base = (2 * J + yc + n1 * (2 * K + zc)) * hn0 + I;
+                const int cc = (yc + zc) & 1;   // colour of child 2I
+                if (BLACK_ONLY) {
+                    const T v = cc ? fmaT(wxm, lft[yc][zc], t) : fmaT(wxp, rgt[yc][zc], t);
+                    u[F.half + base] += v;
+                } else {
+                    const T v0 = fmaT(wxm, lft[yc][zc], t);
+                    const T v1 = fmaT(wxp, rgt[yc][zc], t);
+                    u[cc * F.half + base] += v0;
+                    u[(cc ^ 1) * F.half + base] += v1;
+                }
             }
         }
     }
@@ -587,7 +709,25 @@ template <typename T>
 void launch_prolong_add(const Dims& fine, const Dims& coarse, const BcDesc& bc, const T* ec,
                         T* phi_fine, bool black_only, cudaStream_t s) {
     const Grid3 g = grid3(coarse.n0, coarse.n1, coarse.n2);
-    if (fine.rz == 2) {
+    if (std::is_same<T, double>::value && fine.rz == 2 && fine.split &&
+        fine.ncell >= (1 << 22)) {
+        // z-marching kernel for large FP64 levels (measured: FP64 solve +2.4% at 256^3; the FP32
+        // level-0 prolongation stays faster with one thread per coarse cell): warps of 30
+        // columns, up to 8 warps a block along x; planes per thread as many as still leave ~48
+        // warps per SM of GB300's 152 (the window's start costs three plane loads, a step one)
+        const int warps = ceil_div(coarse.n0, 30);
+        const int wpb = warps < 8 ? warps : 8;
+        const long cols = (long)warps * coarse.n1;
+        int kc = 16;
+        while (kc > 2 && cols * ceil_div(coarse.n2, kc) < 152L * 48) kc >>= 1;
+        const dim3 grid(ceil_div(warps, wpb), coarse.n1, ceil_div(coarse.n2, kc));
+        if (black_only)
+            launch_chain(k_prolong_z<T, true>, grid, dim3(32 * wpb), 0, s, fine, coarse, bc, ec,
+                         phi_fine, kc);
+        else
+            launch_chain(k_prolong_z<T, false>, grid, dim3(32 * wpb), 0, s, fine, coarse, bc, ec,
+                         phi_fine, kc);
+    } else if (fine.rz == 2) {
         if (black_only)
             launch_chain(k_prolong_add<T, true, true>, g.grid, g.block, 0, s, fine, coarse, bc, ec,
                        phi_fine);
