@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--seed", type=int, default=1234)
-    ap.add_argument("--inner", type=int, default=4,
+    ap.add_argument("--inner", type=int, default=None,
                     help="mixed precision: most FP32 V-cycles per FP64 refinement step")
     ap.add_argument("--fixed-inner", action="store_true",
                     help="mixed precision: always --inner V-cycles per step (no adaptive count)")
@@ -260,6 +260,13 @@ def main():
     from maestro_gb300.inputs import config_case
     from maestro_gb300.macproject import BcTower, Layout, MacProjector
 
+    # inner-solve options: the library's defaults unless given
+    inner_opts = {}
+    if args.inner:
+        inner_opts["inner_vcycles"] = args.inner
+    if args.fixed_inner:
+        inner_opts["adaptive_inner"] = 0
+
     build()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
@@ -304,7 +311,7 @@ def main():
 
     def timed_run(precision, timing):
         P = MacProjector(lay, c.dx, bc, precision=precision, stream=stream.cuda_stream,
-                         timing=int(timing), inner_vcycles=args.inner, adaptive_inner=int(not args.fixed_inner))
+                         timing=int(timing), **inner_opts)
         reset_inputs()
         stats = []
 
@@ -342,7 +349,7 @@ def main():
     # error of the mixed result against the FP64 GPU solve of the same inputs (last step)
     reset_inputs()
     Pm = MacProjector(lay, c.dx, bc, precision="mixed", stream=stream.cuda_stream,
-                      inner_vcycles=args.inner, adaptive_inner=int(not args.fixed_inner))
+                      **inner_opts)
     Pd = MacProjector(lay, c.dx, bc, precision="fp64", stream=stream.cuda_stream)
     ua, pa = work_u[0], work_phi[0]
     ub, pb = work_u[1], work_phi[1]
@@ -427,7 +434,7 @@ def main():
         sets = [fab_set() for _ in range(2)]
         pristine = fab_set()
         P = MacProjector(lay, c.dx, bc, precision="mixed", stream=stream.cuda_stream,
-                         inner_vcycles=args.inner, adaptive_inner=int(not args.fixed_inner))
+                         **inner_opts)
         nbytes = lambda lst: sum(x.nbytes for x in lst)  # noqa: E731
         s0 = sets[0]
         u_bytes = sum(nbytes(s0[1][d]) for d in range(c.dm))
@@ -496,7 +503,9 @@ def main():
         "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": ms_fp64 / K,
                  "vcycles": st_fp64[-1]["vcycles"], "rel_resid": st_fp64[-1]["rel_resid"]},
         "mixed_over_fp64": value / fp64_value,
-        "mixed": {"refine_iters": st_mixed[-1]["refine_iters"], "inner_vcycles": args.inner,
+        "mixed": {"refine_iters": st_mixed[-1]["refine_iters"],
+                  "inner_vcycles": args.inner or capi.default_opts().inner_vcycles,
+                  "inner_omega": capi.default_opts().inner_omega,
                   "adaptive_inner": not args.fixed_inner,
                   "inner_cycle": "V(%d,%d)" % (capi.default_opts().inner_nu1,
                                                capi.default_opts().inner_nu2),

@@ -92,7 +92,7 @@ typedef struct mac_opts {
     int timing;             /* 1: CUDA-event timing of the finest-level kernel classes into
                                mac_stats.ktime_* (events recorded inside the V-cycle graph)    */
     int inner_vcycles;      /* mixed precision: FP32 V-cycles per FP64 refinement step (>= 1;
-                               default 4; the most per step when adaptive_inner is on); the
+                               default 3; the most per step when adaptive_inner is on); the
                                FP64 residual is formed once per step                          */
     int coarse_tail;        /* 1 (default): the levels small enough for shared memory and the
                                bottom solve run as one single-CTA kernel (same arithmetic)     */
@@ -114,6 +114,9 @@ typedef struct mac_opts {
     int inner_exact_bottom; /* mixed precision, 1 (default): the inner V-cycles solve a bottom of
                                at most 64 cells exactly, by its dense FP64 (pseudo-)inverse
                                formed once per solve; 0: FP64 BiCGStab as the FP64 V-cycle     */
+    double inner_omega;     /* mixed precision: relaxation weight of the inner V-cycles'
+                               red/black half-sweeps, 0 < omega < 2 (default 1.25; 1:
+                               Gauss-Seidel)                                                   */
 } mac_opts;
 
 /* Kernel classes of mac_stats.ktime_* (finest level unless stated). */

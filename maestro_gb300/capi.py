@@ -74,6 +74,7 @@ class MacOpts(ctypes.Structure):
         ("inner_nu1", ctypes.c_int),
         ("inner_nu2", ctypes.c_int),
         ("inner_exact_bottom", ctypes.c_int),
+        ("inner_omega", ctypes.c_double),
     ]
 
 

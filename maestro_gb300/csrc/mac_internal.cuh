@@ -207,6 +207,7 @@ struct OtfParams {
     int smem;             // dynamic shared memory bytes
     int rty, rzc, rnz, rsmem;   // the same for the staged defect + restriction (rty == 0: none)
     int* err;             // device flag: a bounded wait on a copy gave up
+    float omega;          // relaxation weight of the half-sweeps (1: Gauss-Seidel)
 };
 // Tile plan of the staged half-sweep for the finest level (OtfParams.ty/zc/nz/smem).
 void plan_otf_tile(const Dims& d, int dm, int sms, OtfParams& P);
@@ -307,8 +308,9 @@ struct mac_ctx {
 namespace mac {
 
 // ---- kernels / launchers (mac_kernels.cu) -------------------------------------------------
+// omega != 1: over-relaxed update e = e_old + omega (e_GS - e_old)
 template <typename T>
-void launch_gsrb(const Dims& d, int colour, LevelArrays<T>& a, cudaStream_t s);
+void launch_gsrb(const Dims& d, int colour, LevelArrays<T>& a, cudaStream_t s, T omega = T(1));
 template <typename T>
 void launch_resid_restrict(const Dims& fine, const Dims& coarse, const LevelArrays<T>& a,
                            T* fc, T* ec, bool red_only, cudaStream_t s);
@@ -371,6 +373,7 @@ struct TailParams {
     double bottom_eps;
     int* iters;
     const double* binv;                   // dense (pseudo-)inverse of the bottom; null: BiCGStab
+    T omega;                              // relaxation weight of the half-sweeps (1: Gauss-Seidel)
 };
 template <typename T>
 size_t tail_smem_bytes(const Dims* lev, int nl, const Dims& bottom);

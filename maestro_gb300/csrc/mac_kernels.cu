@@ -88,12 +88,12 @@ __device__ __forceinline__ unsigned long long block_max_u64(unsigned long long v
 }
 
 // ---- red/black Gauss-Seidel half sweep (one colour) -----------------------------------------
-template <typename T>
+template <typename T, bool SOR>
 __global__ void __launch_bounds__(kBlock)
 k_gsrb(Dims d, int colour, T* __restrict__ us, const T* __restrict__ uo, const T* __restrict__ fs,
        const T* __restrict__ bxs, const T* __restrict__ bys, const T* __restrict__ bzs,
        const T* __restrict__ bxo, const T* __restrict__ byo, const T* __restrict__ bzo,
-       const T* __restrict__ ids) {
+       const T* __restrict__ ids, T omega) {
     pdl_wait();
     pdl_trigger();
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
@@ -104,7 +104,12 @@ k_gsrb(Dims d, int colour, T* __restrict__ us, const T* __restrict__ uo, const T
     Nbr nb;
     split_nbrs(d, colour, h, j, k, nb);
     T acc = arms<T>(fs[q], q, nb, uo, bxs, bys, bzs, bxo, byo, bzo);
-    us[q] = acc * ids[q];
+    if (SOR) {
+        const T old = us[q];
+        us[q] = fmaT(omega, acc * ids[q] - old, old);
+    } else {
+        us[q] = acc * ids[q];
+    }
 }
 
 // Red/black half-sweep on a checkerboard-split FP32 level with 4 consecutive colour-half cells
@@ -116,12 +121,13 @@ __device__ __forceinline__ float f4(const float4& v, int m) {
     return m == 0 ? v.x : m == 1 ? v.y : m == 2 ? v.z : v.w;
 }
 
+template <bool SOR>
 __global__ void __launch_bounds__(kBlock)
 k_gsrb4(Dims d, int colour, float* __restrict__ us, const float* __restrict__ uo,
         const float* __restrict__ fs, const float* __restrict__ bxs, const float* __restrict__ bys,
         const float* __restrict__ bzs, const float* __restrict__ bxo,
         const float* __restrict__ byo, const float* __restrict__ bzo,
-        const float* __restrict__ ids) {
+        const float* __restrict__ ids, float omega) {
     pdl_wait();
     pdl_trigger();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -172,6 +178,11 @@ k_gsrb4(Dims d, int colour, float* __restrict__ us, const float* __restrict__ uo
         acc = fmaf(f4(bz, m), f4(uzm, m), acc);
         acc = fmaf(f4(bzp, m), f4(uzp, m), acc);
         out[m] = acc * f4(id, m);
+    }
+    if (SOR) {
+        const float4 o = ld4(us + q);
+#pragma unroll
+        for (int m = 0; m < 4; ++m) out[m] = fmaf(omega, out[m] - f4(o, m), f4(o, m));
     }
     *reinterpret_cast<float4*>(us + q) = make_float4(out[0], out[1], out[2], out[3]);
 }
@@ -669,26 +680,29 @@ k_bottom(BotView vin, Tio* __restrict__ xio, const Tio* __restrict__ fio, double
 
 // ---- launchers ------------------------------------------------------------------------------
 template <typename T>
-void launch_gsrb(const Dims& d, int colour, LevelArrays<T>& a, cudaStream_t s) {
+void launch_gsrb(const Dims& d, int colour, LevelArrays<T>& a, cudaStream_t s, T omega) {
     const int own = colour * d.half, oth = (colour ^ 1) * d.half;
+    const bool sor = omega != T(1);
     if constexpr (std::is_same<T, float>::value) {
         // four cells a thread pays off on large levels; small ones want more threads in flight
         if (d.hn0 % 4 == 0 && d.half >= (1 << 19)) {
             const Grid3 g4 = grid3(d.hn0 / 4, d.n1, d.n2);
-            launch_chain(k_gsrb4, g4.grid, g4.block, 0, s, d, colour, a.phi + own,
+            auto kern = sor ? k_gsrb4<true> : k_gsrb4<false>;
+            launch_chain(kern, g4.grid, g4.block, 0, s, d, colour, a.phi + own,
                        (const float*)(a.phi + oth), (const float*)(a.f + own),
                        (const float*)(a.bx + own), (const float*)(a.by + own),
                        (const float*)(a.bz + own), (const float*)(a.bx + oth),
                        (const float*)(a.by + oth), (const float*)(a.bz + oth),
-                       (const float*)(a.invdiag + own));
+                       (const float*)(a.invdiag + own), omega);
             return;
         }
     }
     const Grid3 g = grid3(d.hn0, d.n1, d.n2);
-    launch_chain(k_gsrb<T>, g.grid, g.block, 0, s, d, colour, a.phi + own, (const T*)(a.phi + oth),
+    auto kern = sor ? k_gsrb<T, true> : k_gsrb<T, false>;
+    launch_chain(kern, g.grid, g.block, 0, s, d, colour, a.phi + own, (const T*)(a.phi + oth),
                (const T*)(a.f + own), (const T*)(a.bx + own), (const T*)(a.by + own),
                (const T*)(a.bz + own), (const T*)(a.bx + oth), (const T*)(a.by + oth),
-               (const T*)(a.bz + oth), (const T*)(a.invdiag + own));
+               (const T*)(a.bz + oth), (const T*)(a.invdiag + own), omega);
 }
 
 template <typename T>
@@ -818,8 +832,8 @@ int prepare_kernels() {
     return MAC_OK;
 }
 
-template void launch_gsrb<double>(const Dims&, int, LevelArrays<double>&, cudaStream_t);
-template void launch_gsrb<float>(const Dims&, int, LevelArrays<float>&, cudaStream_t);
+template void launch_gsrb<double>(const Dims&, int, LevelArrays<double>&, cudaStream_t, double);
+template void launch_gsrb<float>(const Dims&, int, LevelArrays<float>&, cudaStream_t, float);
 template void launch_resid_restrict<double>(const Dims&, const Dims&, const LevelArrays<double>&,
                                             double*, double*, bool, cudaStream_t);
 template void launch_resid_restrict<float>(const Dims&, const Dims&, const LevelArrays<float>&,

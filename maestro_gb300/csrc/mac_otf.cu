@@ -16,7 +16,7 @@ namespace {
 
 constexpr int kB = 256;
 
-template <int DM>
+template <int DM, bool SOR>
 __global__ void __launch_bounds__(kB)
 k_gsrb_otf(Dims d, OtfParams P, int colour, float* __restrict__ es, const float* __restrict__ eo,
            const float* __restrict__ rs, const float* __restrict__ rhos,
@@ -33,7 +33,12 @@ k_gsrb_otf(Dims d, OtfParams P, int colour, float* __restrict__ es, const float*
     nbrs(d, colour, h, j, k, nb);
     float acc = rs[q], diag;
     otf_cell<DM>(P, nb, i, j, k, rhos[q], rhoo, eo, acc, diag);
-    es[q] = acc * rcp_approx(diag);
+    if (SOR) {
+        const float old = es[q];
+        es[q] = fmaf(P.omega, acc * rcp_approx(diag) - old, old);
+    } else {
+        es[q] = acc * rcp_approx(diag);
+    }
 }
 
 // ---- staged 3-D half-sweep -------------------------------------------------------------------
@@ -185,8 +190,8 @@ __device__ __forceinline__ void update_group(float ex, float rx, const FV<V>& Ec
     }
 }
 
-template <bool DIR>
-__global__ void __launch_bounds__(256)
+template <bool DIR, bool SOR>
+__global__ void __launch_bounds__(256, 3)
 k_gsrb_otf_staged(Dims d, OtfParams P, int colour, float* __restrict__ es,
                   const float* __restrict__ eo, const float* __restrict__ rs,
                   const float* __restrict__ rhos, const float* __restrict__ rhoo) {
@@ -279,6 +284,9 @@ k_gsrb_otf_staged(Dims d, OtfParams P, int colour, float* __restrict__ es,
     FV<V> Ec = ldv<V>(sm + stage + ctr), Rc = ldv<V>(sm + stage + oth + ctr);
     for (int k = k0; k < kend; ++k) {
         const int q = k - k0 + 1;
+        // SOR: the own cells' old values, loaded before the wait so that their latency overlaps it
+        FV<V> Eold;
+        if (SOR) Eold = ldv<V>(es + (long)k * plane + (long)j * hn0 + c0);
         wait_plane(q + 1);
         // every thread is done with stage (q - 1) % kStages: refill it with plane q - 1 + kStages
         __syncthreads();
@@ -316,6 +324,10 @@ k_gsrb_otf_staged(Dims d, OtfParams P, int colour, float* __restrict__ es,
         } else {
             update_group<V, 0, false>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp, Ryp, Fo, Ro,
                                       fx, fxl0, fxhV, fyl, fyh, fzl, fzh, 0.f, 0.f, 0.f, out);
+        }
+        if (SOR) {
+#pragma unroll
+            for (int m = 0; m < V; ++m) out[m] = fmaf(P.omega, out[m] - Eold.v[m], Eold.v[m]);
         }
         stv<V>(es + (long)k * plane + (long)j * hn0 + c0, out);
         Eb = Ec;
@@ -549,22 +561,23 @@ void launch_gsrb_otf(const Dims& d, const OtfParams& P, int colour, float* e, co
                      cudaStream_t s) {
     const int own = colour * d.half, oth = (colour ^ 1) * d.half;
     const Grid3 g = grid3(d.hn0, d.n1, d.n2);
+    const bool sor = P.omega != 1.f;
     if (P.dm == 3 && P.ty > 0) {
         const dim3 grid(d.n1 / P.ty, P.nz);
         const int nt = P.ty * d.hn0 / kCellsPerThread;
-        if (P.has_dir)
-            launch_chain(k_gsrb_otf_staged<true>, grid, dim3(nt), (size_t)P.smem, s, d, P, colour,
-                       e + own, (const float*)(e + oth), r + own, P.rho + own, P.rho + oth);
-        else
-            launch_chain(k_gsrb_otf_staged<false>, grid, dim3(nt), (size_t)P.smem, s, d, P, colour,
-                       e + own, (const float*)(e + oth), r + own, P.rho + own, P.rho + oth);
+        auto kern = P.has_dir ? (sor ? k_gsrb_otf_staged<true, true> : k_gsrb_otf_staged<true, false>)
+                              : (sor ? k_gsrb_otf_staged<false, true> : k_gsrb_otf_staged<false, false>);
+        launch_chain(kern, grid, dim3(nt), (size_t)P.smem, s, d, P, colour, e + own,
+                     (const float*)(e + oth), r + own, P.rho + own, P.rho + oth);
+    } else if (P.dm == 3) {
+        auto kern = sor ? k_gsrb_otf<3, true> : k_gsrb_otf<3, false>;
+        launch_chain(kern, g.grid, g.block, 0, s, d, P, colour, e + own, (const float*)(e + oth),
+                     r + own, P.rho + own, P.rho + oth);
+    } else {
+        auto kern = sor ? k_gsrb_otf<2, true> : k_gsrb_otf<2, false>;
+        launch_chain(kern, g.grid, g.block, 0, s, d, P, colour, e + own, (const float*)(e + oth),
+                     r + own, P.rho + own, P.rho + oth);
     }
-    else if (P.dm == 3)
-        launch_chain(k_gsrb_otf<3>, g.grid, g.block, 0, s, d, P, colour, e + own,
-                   (const float*)(e + oth), r + own, P.rho + own, P.rho + oth);
-    else
-        launch_chain(k_gsrb_otf<2>, g.grid, g.block, 0, s, d, P, colour, e + own,
-                   (const float*)(e + oth), r + own, P.rho + own, P.rho + oth);
 }
 
 // Tile plan of the staged half-sweep: ty = the largest power of two with ty * hn0 <= 1024 cells
@@ -587,10 +600,16 @@ void plan_otf_tile(const Dims& d, int dm, int sms, OtfParams& P) {
     {
         std::lock_guard<std::mutex> lk(mu);
         if (smem > smem_set) {
-            if (cudaFuncSetAttribute(k_gsrb_otf_staged<false>,
+            if (cudaFuncSetAttribute(k_gsrb_otf_staged<false, false>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
                     cudaSuccess ||
-                cudaFuncSetAttribute(k_gsrb_otf_staged<true>,
+                cudaFuncSetAttribute(k_gsrb_otf_staged<true, false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_gsrb_otf_staged<false, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_gsrb_otf_staged<true, true>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
                     cudaSuccess) {
                 cudaGetLastError();
@@ -600,7 +619,7 @@ void plan_otf_tile(const Dims& d, int dm, int sms, OtfParams& P) {
         }
     }
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gsrb_otf_staged<false>, nt,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gsrb_otf_staged<false, false>, nt,
                                                       smem) != cudaSuccess ||
         per_sm < 1) {
         cudaGetLastError();

@@ -116,6 +116,7 @@ OtfParams otf_params(const mac_ctx* c) {
     P.rnz = c->otf_tile.rnz;
     P.rsmem = c->otf_tile.rsmem;
     P.err = c->red.counters + 2;
+    P.omega = (float)c->o.inner_omega;
     return P;
 }
 
@@ -148,6 +149,10 @@ void vcycle(mac_ctx* c, int l) {
     const bool otf = std::is_same<T, float>::value && l == 0 && c->otf;
     const int nu1 = sweeps_down(c, std::is_same<T, float>::value);
     const int nu2 = sweeps_up(c, std::is_same<T, float>::value);
+    // over-relaxation (FP32 V-cycle only); the red-only defect and the black-only prolongation
+    // rest on plain Gauss-Seidel half-sweeps
+    const T omega = std::is_same<T, float>::value ? T(c->o.inner_omega) : T(1);
+    const bool gs = omega == T(1);
     if (l == c->nlevels - 1) {
         launch_bottom<T>(L.d, L.a64, a.phi, a.f, c->bottom_scratch, c->singular, o.nub,
                          o.bottom_eps, o.bottom_max_iter, c->red.counters, c->stream);
@@ -186,6 +191,7 @@ void vcycle(mac_ctx* c, int l) {
         tp.bottom_eps = o.bottom_eps;
         tp.iters = c->red.counters;
         tp.binv = std::is_same<T, float>::value && exact_bottom(c) ? c->bot_inv : nullptr;
+        tp.omega = omega;
         launch_tail<T>(tp, c->tail_smem[tslot], c->stream);
         ++c->issued;
         return;
@@ -197,7 +203,7 @@ void vcycle(mac_ctx* c, int l) {
                 launch_gsrb_otf(L.d, P, colour, reinterpret_cast<float*>(a.phi),
                                 reinterpret_cast<const float*>(a.f), c->stream);
             else
-                launch_gsrb<T>(L.d, colour, a, c->stream);
+                launch_gsrb<T>(L.d, colour, a, c->stream, omega);
         }
         c->issued += 2;
     };
@@ -210,15 +216,15 @@ void vcycle(mac_ctx* c, int l) {
         launch_resid_restrict_otf(L.d, C.d, P, reinterpret_cast<const float*>(a.phi),
                                   reinterpret_cast<const float*>(a.f),
                                   reinterpret_cast<float*>(ac.f), reinterpret_cast<float*>(ac.phi),
-                                  nu1 > 0, c->stream);
+                                  gs && nu1 > 0, c->stream);
     else
-        launch_resid_restrict<T>(L.d, C.d, a, ac.f, ac.phi, nu1 > 0, c->stream);
+        launch_resid_restrict<T>(L.d, C.d, a, ac.f, ac.phi, gs && nu1 > 0, c->stream);
     ++c->issued;
     mark(c, tm, 2);   // (the restriction also zeroed the coarse correction ac.phi)
     vcycle<T>(c, l + 1);
     mark(c, tm, 3);
     // with post-smoothing, only colour-1 cells need the correction (see k_prolong_add)
-    launch_prolong_add<T>(L.d, C.d, bc_desc(c), ac.phi, a.phi, nu2 > 0, c->stream);
+    launch_prolong_add<T>(L.d, C.d, bc_desc(c), ac.phi, a.phi, gs && nu2 > 0, c->stream);
     ++c->issued;
     mark(c, tm, 4);
     for (int s = 0; s < nu2; ++s) sweep();
@@ -229,7 +235,8 @@ void vcycle(mac_ctx* c, int l) {
 // colour-1 half-sweep the V-cycle output satisfies L z = r on colour 1, which the Krylov kernels
 // use).
 bool use_krylov(const mac_ctx* c, int prec) {
-    return prec == MAC_PREC_MIXED && c->o.inner_krylov && sweeps_up(c, true) > 0;
+    return prec == MAC_PREC_MIXED && c->o.inner_krylov && sweeps_up(c, true) > 0 &&
+           c->o.inner_omega == 1.0;
 }
 
 int ensure_krylov(mac_ctx* c) {
@@ -576,6 +583,7 @@ int check_opts(const mac_opts* o) {
     if (o->nu1 < 0 || o->nu2 < 0 || o->nub < 0 || o->max_vcycles < 0 || o->bottom_max_iter < 0)
         return MAC_ERR_INVALID;
     if (o->inner_nu1 < -1 || o->inner_nu2 < -1) return MAC_ERR_INVALID;
+    if (!(o->inner_omega > 0.0 && o->inner_omega < 2.0)) return MAC_ERR_INVALID;
     if (!(o->rel_eps >= 0.0)) return MAC_ERR_INVALID;
     return MAC_OK;
 }
@@ -902,13 +910,14 @@ void mac_default_opts(mac_opts* o) {
     o->use_graph = 1;
     o->verbose = 0;
     o->timing = 0;
-    o->inner_vcycles = 4;
+    o->inner_vcycles = 3;
     o->coarse_tail = 1;
     o->adaptive_inner = 1;
     o->inner_krylov = 0;
     o->inner_nu1 = 2;
     o->inner_nu2 = 1;
     o->inner_exact_bottom = 1;
+    o->inner_omega = 1.25;
 }
 
 const char* mac_strerror(int code) {

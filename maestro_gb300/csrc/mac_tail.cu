@@ -61,7 +61,7 @@ __device__ __forceinline__ Lanes lanes(int nx) {
 }
 
 template <typename T>
-__device__ __noinline__ void tail_sweep(const TailLevel<T>& L) {
+__device__ __noinline__ void tail_sweep(const TailLevel<T>& L, T omega) {
     const int hn0 = L.n0 >> 1, rows = L.n1 * L.n2;
     const Lanes q = lanes(hn0);
     for (int colour = 0; colour < 2; ++colour) {
@@ -74,7 +74,10 @@ __device__ __noinline__ void tail_sweep(const TailLevel<T>& L) {
                     const int i = 2 * h + s;
                     const int c = i + L.n0 * row;
                     const T acc = arms_nat<T>(L.f[c], L, L.e, i, j, k, c);
-                    L.e[c] = acc * L.idg[c];
+                    if (omega != T(1))
+                        L.e[c] = fmaT2(omega, acc * L.idg[c] - L.e[c], L.e[c]);
+                    else
+                        L.e[c] = acc * L.idg[c];
                 }
                 j += dj;
                 k += dk;
@@ -309,11 +312,14 @@ k_tail(TailParams<T> P) {
     __syncthreads();
     // down the V
     for (int l = 0; l < nl; ++l) {
-        for (int s = 0; s < P.nu1; ++s) tail_sweep<T>(L[l]);
+        for (int s = 0; s < P.nu1; ++s) tail_sweep<T>(L[l], P.omega);
+        // red-only defect / black-only prolongation rest on plain Gauss-Seidel half-sweeps
+        const bool gs = P.omega == T(1);
         if (l + 1 < nl) {
-            tail_restrict<T, T>(L[l], L[l + 1].n0, L[l + 1].n1, L[l + 1].n2, L[l + 1].f, P.nu1 > 0);
+            tail_restrict<T, T>(L[l], L[l + 1].n0, L[l + 1].n1, L[l + 1].n2, L[l + 1].f,
+                                gs && P.nu1 > 0);
         } else {
-            tail_restrict<T, double>(L[l], BD.n0, BD.n1, BD.n2, fb, P.nu1 > 0);
+            tail_restrict<T, double>(L[l], BD.n0, BD.n1, BD.n2, fb, gs && P.nu1 > 0);
         }
     }
     // bottom, FP64 (input rhs rounded through T as in the multi-kernel path)
@@ -355,12 +361,13 @@ k_tail(TailParams<T> P) {
     __syncthreads();
     // up the V
     for (int l = nl - 1; l >= 0; --l) {
+        const bool gs = P.omega == T(1);
         if (l + 1 < nl)
             tail_prolong<T>(L[l], L[l + 1].e, L[l + 1].n0, L[l + 1].n1, L[l + 1].n2, P.bc,
-                            P.nu2 > 0);
+                            gs && P.nu2 > 0);
         else
-            tail_prolong<T>(L[l], eb, BD.n0, BD.n1, BD.n2, P.bc, P.nu2 > 0);
-        for (int s = 0; s < P.nu2; ++s) tail_sweep<T>(L[l]);
+            tail_prolong<T>(L[l], eb, BD.n0, BD.n1, BD.n2, P.bc, gs && P.nu2 > 0);
+        for (int s = 0; s < P.nu2; ++s) tail_sweep<T>(L[l], P.omega);
     }
     // hand the correction of the first tail level back (its split layout)
     {

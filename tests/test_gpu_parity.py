@@ -198,24 +198,25 @@ def _stiff48_oracle():
     return oracle_project(c), oracle_project(c, rel_eps=1e-14)
 
 
-@pytest.mark.parametrize("nu", [(2, 1), (2, 2)])
+@pytest.mark.parametrize("cycle", [(2, 1, 1.25), (2, 2, 1.0)], ids=["V21sor", "V22gs"])
 @pytest.mark.parametrize("adaptive", [0, 1])
 @pytest.mark.parametrize("inner", [1, 2, 3, 4, 6])
-def test_mixed_inner_vcycles(cuda_lib, inner, adaptive, nu):
-    # mixed precision with up to 1..6 FP32 V-cycles per FP64 refinement step, fixed or adaptive,
-    # inner V(2,1) (the default) or V(2,2).  On this stiff case (density contrast ~1e6) the
-    # oracle's own velocities at the 1e-10 tolerance are ~8e-9 from the converged solution
-    # (rel_eps 1e-14): agreement with the oracle is checked at 2e-8, closeness to the converged
-    # solution at 1.5e-8.
+def test_mixed_inner_vcycles(cuda_lib, inner, adaptive, cycle):
+    # mixed precision with up to 1..6 FP32 V-cycles per FP64 refinement step, fixed or adaptive;
+    # inner V(2,1) with over-relaxed half-sweeps (the default) or plain Gauss-Seidel V(2,2) (the
+    # reference's cycle).  On this stiff case (density contrast ~1e6) the oracle's own
+    # velocities at the 1e-10 tolerance are ~8e-9 from the converged solution (rel_eps 1e-14):
+    # agreement with the oracle is checked at 2e-8, closeness to the converged solution at
+    # 1.5e-8.
     c = build3d("stiff48_b16")
     (u_o, phi_o, st_o), (u_x, phi_x, _) = _stiff48_oracle()
     u, phi, st = gpu_project(c, "mixed", inner_vcycles=inner, adaptive_inner=adaptive,
-                             inner_nu1=nu[0], inner_nu2=nu[1])
+                             inner_nu1=cycle[0], inner_nu2=cycle[1], inner_omega=cycle[2])
     assert st["status"] == 0 and st["rel_resid"] <= 1e-10
     assert true_rel_resid(c, phi) <= 1.5e-10
     assert phi_rel_err(phi, phi_o) <= 1e-8 and u_rel_err(u, u_o) <= 2e-8
     assert phi_rel_err(phi, phi_x) <= 1e-8 and u_rel_err(u, u_x) <= 1.5e-8
-    assert st["vcycles"] >= st_o["vcycles"] - 1
+    assert st["vcycles"] <= 2 * st_o["vcycles"] + 2
     if adaptive:
         assert st["refine_iters"] <= st["vcycles"] <= st["refine_iters"] * inner
     else:
