@@ -12,7 +12,7 @@ value  : mixed-precision solves/s (FP32 V-cycles inside FP64 iterative refinemen
 fp64   : the plain FP64 solve timed the same way.
 e2e    : the same metric through the public C ABI (mac_macproject) with host (pinned) per-box
          fabs: every step copies its inputs host->device and its result device->host.
-roofline: the finest-level red/black Gauss-Seidel sweeps of the mixed solve, timed live with
+roofline: the finest-level red/black half-sweeps of the mixed solve, timed live with
          CUDA events recorded inside the V-cycle graph over the timed region.
 --impl reference: the CPU oracle (C++/OpenMP restatement of MAESTRO's FP64 solve; the Fortran
          reference cannot be built here) on the host cores.
@@ -371,8 +371,11 @@ def main():
     kt_n = sum(s["ktime_launches"][capi.KT_NAMES.index("smooth")] for s in st_mixed)
     # algorithmic bytes per half-sweep launch of the on-the-fly design (per cell of the level):
     # the other colour's e (2 B) and both colours' rho (4 B) read, the own colour's f read (2 B)
-    # and e write (2 B) = 10 B; coefficients are formed from rho in registers, none is stored
-    alg_bytes = 10 * N
+    # and e write (2 B) = 10 B; the over-relaxed half-sweep (inner_omega != 1) also reads the own
+    # colour's old e (2 B) = 12 B; coefficients are formed from rho in registers, none is stored
+    omega = capi.default_opts().inner_omega
+    sor = omega != 1.0
+    alg_bytes = (12 if sor else 10) * N
     avg_s = (kt_ms / kt_n) / 1e3 if kt_n else float("nan")
     achieved = alg_bytes / avg_s / 1e9
     traffic = None
@@ -380,12 +383,13 @@ def main():
     if os.path.exists(tp):
         with open(tp) as f:
             tj = json.load(f)
-        ent = tj.get("gsrb_otf_staged_fine")
+        ent = tj.get("gsrb_otf_staged_sor_fine" if sor else "gsrb_otf_staged_fine")
         if ent and ent.get("cells"):
             traffic = ent["dram_bytes_per_launch"] * N / ent["cells"]
     roofline = {"bound": "hbm",
                 "kernel": "k_gsrb_otf_staged (finest level, one colour half-sweep, FP32, "
-                          "coefficients from rho on the fly)",
+                          "coefficients from rho on the fly%s)" % (
+                              ", over-relaxed omega=%.2f" % omega if sor else ""),
                 "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "traffic": traffic,
                 "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_s * 1e3,

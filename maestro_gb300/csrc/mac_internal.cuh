@@ -292,6 +292,7 @@ struct mac_ctx {
     bool otf = false;                             // finest-level FP32 kernels use rho32
     mac::KrylovBufs kry;                          // flexible-CG vectors (allocated on first use)
     bool mean_pending = false;                    // f still holds the mean (singular problem)
+    float* def_b = nullptr;                       // colour-1 defects of the finest FP32 level
     double* bot_inv = nullptr;                    // dense bottom (pseudo-)inverse (small bottoms)
     cudaStream_t aux = nullptr;                   // side stream of the bottom inverse
     cudaEvent_t aux_ev[2] = {nullptr, nullptr};   // [0] operators ready, [1] inverse done
@@ -339,11 +340,17 @@ void launch_fcg_update(const Dims& d, const LevelArrays<float>& A, const KrylovB
 void launch_fcg_final(const Dims& d, double* phi, const LevelArrays<float>& A,
                       const KrylovBufs& K, bool first, cudaStream_t s);
 
+// dout (optional, over-relaxed staged half-sweeps only): the updated cells' defects f - L e,
+// colour-half indexing; launch_gsrb_otf returns without writing it where it does not apply
 void launch_gsrb_otf(const Dims& d, const OtfParams& P, int colour, float* e, const float* r,
-                     cudaStream_t s);
+                     cudaStream_t s, float* dout = nullptr);
+// blk (optional): colour-1 defects written by the preceding over-relaxed colour-1 half-sweep;
+// with red_only false the staged kernel then forms only the colour-0 defects and adds them
 void launch_resid_restrict_otf(const Dims& fine, const Dims& coarse, const OtfParams& P,
                                const float* e, const float* r, float* fc, float* ec,
-                               bool red_only, cudaStream_t s);
+                               bool red_only, cudaStream_t s, const float* blk = nullptr);
+// whether the staged half-sweep and defect kernels run on this level (then dout/blk apply)
+inline bool otf_staged(const OtfParams& P) { return P.dm == 3 && P.ty > 0 && P.rty > 0; }
 
 template <typename Tio>
 void launch_bottom(const Dims& d, const LevelArrays<double>& a64, Tio* x, const Tio* f,

@@ -134,7 +134,7 @@ __device__ __forceinline__ void stv(float* p, const float* v) {
 // group on the side SP selects (c0 - 1 for SP = 0, c0 + V for SP = 1).  fxl0 / fxhV: x factors
 // of the group's outer low / high faces (zero on a non-periodic wall); wx0 / wxV / wmid: the
 // Dirichlet diagonal factors of the first, last and inner cells (DIR only).
-template <int V, int SP, bool DIR, bool RES = false>
+template <int V, int SP, bool DIR, bool RES = false, bool KEEP = false>
 __device__ __forceinline__ void update_group(float ex, float rx, const FV<V>& Ec, const FV<V>& Rc,
                                              const FV<V>& Eb, const FV<V>& Rb, const FV<V>& Ea,
                                              const FV<V>& Ra, const FV<V>& Eym, const FV<V>& Rym,
@@ -142,7 +142,8 @@ __device__ __forceinline__ void update_group(float ex, float rx, const FV<V>& Ec
                                              const FV<V>& Ro, float fx, float fxl0, float fxhV,
                                              float fyl, float fyh, float fzl, float fzh,
                                              float wx0, float wxV, float wmid, float* out,
-                                             const float* eown = nullptr) {
+                                             const float* eown = nullptr, float* accv = nullptr,
+                                             float* dgv = nullptr) {
 #pragma unroll
     for (int m = 0; m < V; ++m) {
         const float rc = Ro.v[m];
@@ -185,16 +186,24 @@ __device__ __forceinline__ void update_group(float ex, float rx, const FV<V>& Ec
             const float w = (SP == 0 && m == 0) ? wx0 : (SP == 1 && m == V - 1) ? wxV : wmid;
             dg += w * rcp_approx(rc);
         }
-        // RES: the defect f - L e of the own cell instead of its Gauss-Seidel update
+        // RES: the defect f - L e of the own cell instead of its Gauss-Seidel update; KEEP: also
+        // hand back f + sum(arms) and the diagonal (the defect after an over-relaxed update)
         out[m] = RES ? fmaf(-dg, eown[m], acc) : acc * rcp_approx(dg);
+        if (KEEP) {
+            accv[m] = acc;
+            dgv[m] = dg;
+        }
     }
 }
 
-template <bool DIR, bool SOR>
+// DEF (with SOR): also write each updated cell's defect f - L e after its update to dout
+// (indexed like es): after the over-relaxed half-sweep it is acc - diag e_new, no longer zero.
+template <bool DIR, bool SOR, bool DEF = false>
 __global__ void __launch_bounds__(256, 3)
 k_gsrb_otf_staged(Dims d, OtfParams P, int colour, float* __restrict__ es,
                   const float* __restrict__ eo, const float* __restrict__ rs,
-                  const float* __restrict__ rhos, const float* __restrict__ rhoo) {
+                  const float* __restrict__ rhos, const float* __restrict__ rhoo,
+                  float* __restrict__ dout = nullptr) {
     constexpr int V = kCellsPerThread;
     extern __shared__ __align__(128) float sm[];
     __shared__ int abort_flag;
@@ -282,11 +291,18 @@ k_gsrb_otf_staged(Dims d, OtfParams P, int colour, float* __restrict__ es,
     __syncthreads();
     FV<V> Eb = ldv<V>(sm + ctr), Rb = ldv<V>(sm + oth + ctr);
     FV<V> Ec = ldv<V>(sm + stage + ctr), Rc = ldv<V>(sm + stage + oth + ctr);
+    // SOR: the own cells' old values, loaded one plane ahead so that their latency overlaps a
+    // whole plane's work
+    const float* eown = es + (long)j * hn0 + c0;
+    FV<V> Enext;
+    if (SOR) Enext = ldv<V>(eown + (long)k0 * plane);
     for (int k = k0; k < kend; ++k) {
         const int q = k - k0 + 1;
-        // SOR: the own cells' old values, loaded before the wait so that their latency overlaps it
         FV<V> Eold;
-        if (SOR) Eold = ldv<V>(es + (long)k * plane + (long)j * hn0 + c0);
+        if (SOR) {
+            Eold = Enext;
+            if (k + 1 < kend) Enext = ldv<V>(eown + (long)(k + 1) * plane);
+        }
         wait_plane(q + 1);
         // every thread is done with stage (q - 1) % kStages: refill it with plane q - 1 + kStages
         __syncthreads();
@@ -306,30 +322,39 @@ k_gsrb_otf_staged(Dims d, OtfParams P, int colour, float* __restrict__ es,
         const float fyl = jl ? fy : 0.f, fyh = jh ? fy : 0.f;
         const float fzl = P.fac[2 * st_n + k], fzh = P.fac[3 * st_n + k];
         const float fxl0 = wlo ? 0.f : fx, fxhV = whi ? 0.f : fx;
-        float out[V];
+        float out[V], accv[V], dgv[V];
         if (DIR) {
             const float wmid = P.fac[4 * st_n + k] + (dy ? fy : 0.f);
             const float wx0 = wmid + (dxl ? fx : 0.f), wxV = wmid + (dxh ? fx : 0.f);
             if (s)
-                update_group<V, 1, true>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp, Ryp, Fo,
-                                         Ro, fx, fxl0, fxhV, fyl, fyh, fzl, fzh, wx0, wxV, wmid,
-                                         out);
+                update_group<V, 1, true, false, DEF>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp,
+                                                     Ryp, Fo, Ro, fx, fxl0, fxhV, fyl, fyh, fzl,
+                                                     fzh, wx0, wxV, wmid, out, nullptr, accv, dgv);
             else
-                update_group<V, 0, true>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp, Ryp, Fo,
-                                         Ro, fx, fxl0, fxhV, fyl, fyh, fzl, fzh, wx0, wxV, wmid,
-                                         out);
+                update_group<V, 0, true, false, DEF>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp,
+                                                     Ryp, Fo, Ro, fx, fxl0, fxhV, fyl, fyh, fzl,
+                                                     fzh, wx0, wxV, wmid, out, nullptr, accv, dgv);
         } else if (s) {
-            update_group<V, 1, false>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp, Ryp, Fo, Ro,
-                                      fx, fxl0, fxhV, fyl, fyh, fzl, fzh, 0.f, 0.f, 0.f, out);
+            update_group<V, 1, false, false, DEF>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp,
+                                                  Ryp, Fo, Ro, fx, fxl0, fxhV, fyl, fyh, fzl, fzh,
+                                                  0.f, 0.f, 0.f, out, nullptr, accv, dgv);
         } else {
-            update_group<V, 0, false>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp, Ryp, Fo, Ro,
-                                      fx, fxl0, fxhV, fyl, fyh, fzl, fzh, 0.f, 0.f, 0.f, out);
+            update_group<V, 0, false, false, DEF>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp,
+                                                  Ryp, Fo, Ro, fx, fxl0, fxhV, fyl, fyh, fzl, fzh,
+                                                  0.f, 0.f, 0.f, out, nullptr, accv, dgv);
         }
         if (SOR) {
 #pragma unroll
             for (int m = 0; m < V; ++m) out[m] = fmaf(P.omega, out[m] - Eold.v[m], Eold.v[m]);
         }
-        stv<V>(es + (long)k * plane + (long)j * hn0 + c0, out);
+        const long cell = (long)k * plane + (long)j * hn0 + c0;
+        stv<V>(es + cell, out);
+        if (DEF) {
+            float dv[V];
+#pragma unroll
+            for (int m = 0; m < V; ++m) dv[m] = fmaf(-dgv[m], out[m], accv[m]);
+            stv<V>(dout + cell, dv);
+        }
         Eb = Ec;
         Rb = Rc;
         Ec = Ea;
@@ -351,12 +376,16 @@ k_gsrb_otf_staged(Dims d, OtfParams P, int colour, float* __restrict__ es,
 // then writes the 4 coarse values (two float2 per colour half of the coarse level) and zeroes the
 // coarse correction there.  Same per-cell arithmetic as k_resid_restrict_otf; the eight children
 // are summed as (plane pair per row) then (row pair).
-template <bool DIR>
-__global__ void __launch_bounds__(256)
+// BLK: the colour-1 defects are not zero (an over-relaxed colour-1 half-sweep came last) and
+// were written by that half-sweep into blk (colour-1 half indexing): each thread adds those of
+// its row's colour-1 cells, the same colour-half columns, to its sums.
+template <bool DIR, bool BLK = false>
+__global__ void __launch_bounds__(256, 3)
 k_resid_restrict_staged(Dims d, Dims C, OtfParams P, const float* __restrict__ eo,
                         const float* __restrict__ eown, const float* __restrict__ rs,
                         const float* __restrict__ rhos, const float* __restrict__ rhoo,
-                        float* __restrict__ fc, float* __restrict__ ec) {
+                        float* __restrict__ fc, float* __restrict__ ec,
+                        const float* __restrict__ blk = nullptr) {
     constexpr int V = kCellsPerThread;
     constexpr int colour = 0;
     extern __shared__ __align__(128) float sm[];
@@ -441,6 +470,8 @@ k_resid_restrict_staged(Dims d, Dims C, OtfParams P, const float* __restrict__ e
     float racc[V];
     for (int k = k0; k < kend; ++k) {
         const int q = k - k0 + 1;
+        FV<V> Db;
+        if (BLK) Db = ldv<V>(blk + (long)k * plane + (long)j * hn0 + c0);
         wait_plane(q + 1);
         __syncthreads();
         if (abort_flag) break;
@@ -481,6 +512,10 @@ k_resid_restrict_staged(Dims d, Dims C, OtfParams P, const float* __restrict__ e
             update_group<V, 0, false, true>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp, Ryp, Fo,
                                             Ro, fx, fxl0, fxhV, fyl, fyh, fzl, fzh, 0.f, 0.f, 0.f,
                                             res, Eown.v);
+        }
+        if (BLK) {
+#pragma unroll
+            for (int m = 0; m < V; ++m) res[m] += Db.v[m];
         }
         if ((k & 1) == 0) {
 #pragma unroll
@@ -558,17 +593,24 @@ k_resid_restrict_otf(Dims F, Dims C, OtfParams P, const float* __restrict__ e,
 }  // namespace
 
 void launch_gsrb_otf(const Dims& d, const OtfParams& P, int colour, float* e, const float* r,
-                     cudaStream_t s) {
+                     cudaStream_t s, float* dout) {
     const int own = colour * d.half, oth = (colour ^ 1) * d.half;
     const Grid3 g = grid3(d.hn0, d.n1, d.n2);
     const bool sor = P.omega != 1.f;
     if (P.dm == 3 && P.ty > 0) {
         const dim3 grid(d.n1 / P.ty, P.nz);
         const int nt = P.ty * d.hn0 / kCellsPerThread;
+        if (sor && dout) {
+            auto kern = P.has_dir ? k_gsrb_otf_staged<true, true, true>
+                                  : k_gsrb_otf_staged<false, true, true>;
+            launch_chain(kern, grid, dim3(nt), (size_t)P.smem, s, d, P, colour, e + own,
+                         (const float*)(e + oth), r + own, P.rho + own, P.rho + oth, dout);
+            return;
+        }
         auto kern = P.has_dir ? (sor ? k_gsrb_otf_staged<true, true> : k_gsrb_otf_staged<true, false>)
                               : (sor ? k_gsrb_otf_staged<false, true> : k_gsrb_otf_staged<false, false>);
         launch_chain(kern, grid, dim3(nt), (size_t)P.smem, s, d, P, colour, e + own,
-                     (const float*)(e + oth), r + own, P.rho + own, P.rho + oth);
+                     (const float*)(e + oth), r + own, P.rho + own, P.rho + oth, (float*)nullptr);
     } else if (P.dm == 3) {
         auto kern = sor ? k_gsrb_otf<3, true> : k_gsrb_otf<3, false>;
         launch_chain(kern, g.grid, g.block, 0, s, d, P, colour, e + own, (const float*)(e + oth),
@@ -611,6 +653,12 @@ void plan_otf_tile(const Dims& d, int dm, int sms, OtfParams& P) {
                     cudaSuccess ||
                 cudaFuncSetAttribute(k_gsrb_otf_staged<true, true>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_gsrb_otf_staged<false, true, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_gsrb_otf_staged<true, true, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
                     cudaSuccess) {
                 cudaGetLastError();
                 return;
@@ -648,6 +696,12 @@ void plan_otf_tile(const Dims& d, int dm, int sms, OtfParams& P) {
                     cudaSuccess ||
                 cudaFuncSetAttribute(k_resid_restrict_staged<true>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, rsmem) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_resid_restrict_staged<false, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, rsmem) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_resid_restrict_staged<true, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, rsmem) !=
                     cudaSuccess) {
                 cudaGetLastError();
                 return;
@@ -675,19 +729,20 @@ void plan_otf_tile(const Dims& d, int dm, int sms, OtfParams& P) {
 
 void launch_resid_restrict_otf(const Dims& fine, const Dims& coarse, const OtfParams& P,
                                const float* e, const float* r, float* fc, float* ec,
-                               bool red_only, cudaStream_t s) {
-    if (P.dm == 3 && P.rty > 0 && red_only && coarse.split) {
-        // colour 0 is "own": its e, f and rho; colour 1 the other colour's e and rho
+                               bool red_only, cudaStream_t s, const float* blk) {
+    if (P.dm == 3 && P.rty > 0 && (red_only || blk) && coarse.split) {
+        // colour 0 is "own": its e, f and rho; colour 1 the other colour's e and rho (and, after
+        // an over-relaxed colour-1 half-sweep, its defects in blk)
         const dim3 grid(fine.n1 / P.rty, P.rnz);
         const int nt = P.rty * fine.hn0 / kCellsPerThread;
         const float* eo = e + fine.half;
         const float* rhoo = P.rho + fine.half;
-        if (P.has_dir)
-            launch_chain(k_resid_restrict_staged<true>, grid, dim3(nt), (size_t)P.rsmem, s, fine,
-                         coarse, P, eo, e, r, (const float*)P.rho, rhoo, fc, ec);
-        else
-            launch_chain(k_resid_restrict_staged<false>, grid, dim3(nt), (size_t)P.rsmem, s, fine,
-                         coarse, P, eo, e, r, (const float*)P.rho, rhoo, fc, ec);
+        auto kern = red_only ? (P.has_dir ? k_resid_restrict_staged<true>
+                                          : k_resid_restrict_staged<false>)
+                             : (P.has_dir ? k_resid_restrict_staged<true, true>
+                                          : k_resid_restrict_staged<false, true>);
+        launch_chain(kern, grid, dim3(nt), (size_t)P.rsmem, s, fine, coarse, P, eo, e, r,
+                     (const float*)P.rho, rhoo, fc, ec, red_only ? (const float*)nullptr : blk);
         return;
     }
     const Grid3 g = grid3(coarse.n0, coarse.n1, coarse.n2);

@@ -197,26 +197,32 @@ void vcycle(mac_ctx* c, int l) {
         return;
     }
     const OtfParams P = otf ? otf_params(c) : OtfParams{};
-    auto sweep = [&]() {
+    Level& C = c->lev[l + 1];
+    LevelArrays<T>& ac = arrays<T>(C);
+    // over-relaxed finest level with the staged kernels: the last pre-smoothing colour-1
+    // half-sweep writes its cells' defects, and the staged restriction forms only the colour-0
+    // ones (instead of both colours cell by cell)
+    float* blk = otf && !gs && nu1 > 0 && c->def_b && otf_staged(P) && C.d.split ? c->def_b
+                                                                                  : nullptr;
+    auto sweep = [&](bool last_down) {
         for (int colour = 0; colour < 2; ++colour) {
             if (otf)
                 launch_gsrb_otf(L.d, P, colour, reinterpret_cast<float*>(a.phi),
-                                reinterpret_cast<const float*>(a.f), c->stream);
+                                reinterpret_cast<const float*>(a.f), c->stream,
+                                last_down && colour == 1 ? blk : nullptr);
             else
                 launch_gsrb<T>(L.d, colour, a, c->stream, omega);
         }
         c->issued += 2;
     };
     mark(c, tm, 0);
-    for (int s = 0; s < nu1; ++s) sweep();
-    Level& C = c->lev[l + 1];
-    LevelArrays<T>& ac = arrays<T>(C);
+    for (int s = 0; s < nu1; ++s) sweep(s == nu1 - 1);
     mark(c, tm, 1);
     if (otf)
         launch_resid_restrict_otf(L.d, C.d, P, reinterpret_cast<const float*>(a.phi),
                                   reinterpret_cast<const float*>(a.f),
                                   reinterpret_cast<float*>(ac.f), reinterpret_cast<float*>(ac.phi),
-                                  gs && nu1 > 0, c->stream);
+                                  gs && nu1 > 0, c->stream, blk);
     else
         launch_resid_restrict<T>(L.d, C.d, a, ac.f, ac.phi, gs && nu1 > 0, c->stream);
     ++c->issued;
@@ -227,7 +233,7 @@ void vcycle(mac_ctx* c, int l) {
     launch_prolong_add<T>(L.d, C.d, bc_desc(c), ac.phi, a.phi, gs && nu2 > 0, c->stream);
     ++c->issued;
     mark(c, tm, 4);
-    for (int s = 0; s < nu2; ++s) sweep();
+    for (int s = 0; s < nu2; ++s) sweep(false);
     mark(c, tm, 5);
 }
 
@@ -427,6 +433,9 @@ int run_solve(mac_ctx* c, mac_stats* st) {
         int rc = setup_fp32_copies(c);
         if (rc) return rc;
         if (use_krylov(c, prec) && (rc = ensure_krylov(c))) return rc;
+        if (c->o.inner_omega != 1.0 && c->otf && !c->def_b &&
+            (rc = alloc_arr(c, &c->def_b, (size_t)F.d.half)))
+            return rc;
         if (exact_bottom(c)) {
             if (!c->inv_pending) {   // (a caller that built the levels some other way)
                 int rc2 = issue_bottom_inverse(c);
