@@ -100,17 +100,16 @@ typedef struct mac_opts {
                                only as many inner V-cycles (<= inner_vcycles) as the contraction
                                just observed predicts the tolerance needs; 0: always
                                inner_vcycles                                                   */
-    int inner_krylov;       /* mixed precision with nu2 > 0: 1 = the inner FP32 V-cycles of a
-                               step precondition a flexible conjugate-gradient iteration (one
-                               previous direction kept; each V-cycle starts from zero on the
-                               current FP32 residual): fewer V-cycles, but at the same residual
-                               tolerance the projected velocity can be further from the
-                               converged one; 0 (default) = plain V-cycles, the reference's
-                               iteration                                                       */
-    int inner_nu1, inner_nu2; /* mixed precision: GS-RB sweeps down / up the inner FP32
-                               V-cycles (default 2 / 1: at 256^3 one V-cycle more than with
-                               2 / 2, each a sixth cheaper; -1: nu1 / nu2); the FP64 V-cycle
-                               always uses nu1 / nu2                                           */
+    int inner_krylov;       /* mixed precision with inner_nu2 > 0 and inner_omega = 1: 1 = the
+                               inner FP32 V-cycles of a step precondition a flexible
+                               conjugate-gradient iteration (one previous direction kept; each
+                               V-cycle starts from zero on the current FP32 residual): fewer
+                               V-cycles, but at the same residual tolerance the projected
+                               velocity can be further from the converged one; 0 (default) =
+                               the V-cycles applied one after the other                        */
+    int inner_nu1, inner_nu2; /* mixed precision: red/black sweeps down / up the inner FP32
+                               V-cycles (default 2 / 1; -1: nu1 / nu2); the FP64 V-cycle always
+                               uses nu1 / nu2                                                  */
     int inner_exact_bottom; /* mixed precision, 1 (default): the inner V-cycles solve a bottom of
                                at most 64 cells exactly, by its dense FP64 (pseudo-)inverse
                                formed once per solve; 0: FP64 BiCGStab as the FP64 V-cycle     */
@@ -120,7 +119,7 @@ typedef struct mac_opts {
 } mac_opts;
 
 /* Kernel classes of mac_stats.ktime_* (finest level unless stated). */
-#define MAC_KT_SMOOTH    0   /* red/black Gauss-Seidel half sweeps                            */
+#define MAC_KT_SMOOTH    0   /* red/black half sweeps (Gauss-Seidel or over-relaxed)          */
 #define MAC_KT_RESTRICT  1   /* defect + restriction to level 1                               */
 #define MAC_KT_COARSE    2   /* everything on levels >= 1 incl. the bottom solve              */
 #define MAC_KT_PROLONG   3   /* prolongation from level 1                                     */

@@ -81,3 +81,45 @@ def test_cell_to_edge_matches_oracle(lib):
     from maestro_gb300.macproject import cell_to_edge
     b = 1e7 ** (1 / 1.4) * np.exp(-np.linspace(0, 4, 64) / 1.4)
     np.testing.assert_array_equal(cell_to_edge(b), O.cell_to_edge(b))
+
+
+def test_mixed_precision_inner_defaults(lib):
+    o = capi.default_opts()
+    # inner FP32 V(2,1)-cycles with over-relaxed half-sweeps, at most 3 a refinement step,
+    # adaptive count, exact bottom; the flexible-CG combination is opt-in
+    assert (o.inner_nu1, o.inner_nu2, o.inner_vcycles) == (2, 1, 3)
+    assert o.inner_omega == 1.25 and o.adaptive_inner == 1 and o.inner_exact_bottom == 1
+    assert o.inner_krylov == 0 and o.coarse_tail == 1
+
+
+def test_ctypes_structs_match_the_c_header(tmp_path):
+    # the ctypes mirrors (and so the Fortran bind(C) types written from the same header) must
+    # have the C layout: sizes and every field offset, from the header compiled by the C compiler
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"mac_opts": capi.MacOpts, "mac_stats": capi.MacStats, "mac_geom": capi.MacGeom}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "maestro_mac.h"',
+             "int main(void) {"]
+    for cname, cls in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-std=c11", "-I", inc, str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {}
+    for ln in out:
+        if ln.strip():
+            parts = ln.split()
+            got[(parts[0], parts[1])] = int(parts[2])
+    for cname, cls in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert got[(cname, fname)] == getattr(cls, fname).offset, (cname, fname)
