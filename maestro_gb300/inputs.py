@@ -196,6 +196,58 @@ def make_case(name: str = "custom", dm: int = 3, n=(64, 64, 64), box=None, H_fra
                    phi0=np.zeros(n, order="F"), w=w, seed=seed)
 
 
+def make_spherical_case(name: str = "spherical", n=(64, 64, 64), box=None, H_frac: float = 0.2,
+                        noise: float = 0.01, kmax: int = 6, seed: int = 4321, u_amp: float = 1e6,
+                        s_amp: float = 1e-3, bc: str = "outflow") -> MacCase:
+    """A 3-D star-like case for the spherical form of the projection (beta0 on every face).
+
+    MAESTRO's spherical geometry keeps a Cartesian grid and hands macproject beta0 as a 3-D face
+    multifab (beta0_cart_edge) instead of 1-D arrays.  Here rho0(r) = 1e7 exp(-r / H) with r the
+    distance from the domain centre, cell rho = rho0(r_cell) exp(sigma N(0,1)), beta0 =
+    rho0^(1/1.4) evaluated at every face centre (returned as ``case.b0c``, one array per
+    direction), macrhs = beta0(r_cell) (S - Sbar) with S Gaussian noise, U_edge a random
+    divergent Fourier field.  ``bc``: "outflow" (Dirichlet phi on every face, the usual spherical
+    setup) or "periodic".  ``beta0``/``beta0_edge`` are None.
+    """
+    dm = 3
+    n = tuple(int(v) for v in n)
+    box = tuple(box) if box is not None else n
+    rng = np.random.default_rng(seed)
+    dx = tuple(1.0 / n[d] for d in range(dm))
+    H = H_frac
+
+    def rho0(x, y, z):
+        r = np.sqrt((x - 0.5) ** 2 + (y - 0.5) ** 2 + (z - 0.5) ** 2)
+        return 1e7 * np.exp(-r / H)
+
+    xc = [(np.arange(n[d]) + 0.5) / n[d] for d in range(dm)]
+    X, Y, Z = np.meshgrid(*xc, indexing="ij")
+    r0c = rho0(X, Y, Z)
+    rho = np.asfortranarray(r0c * np.exp(noise * rng.standard_normal(n)))
+    b0c = []
+    for d in range(dm):
+        pos = [xc[e] if e != d else np.arange(n[d] + 1) / n[d] for e in range(dm)]
+        F = np.meshgrid(*pos, indexing="ij")
+        b0c.append(np.asfortranarray(rho0(*F) ** (1.0 / 1.4)))
+    umac = []
+    for d in range(dm):
+        u = _fourier_component(rng, n, dm, d, kmax)
+        m = np.max(np.abs(u))
+        umac.append(np.asfortranarray(u * (u_amp / m if m > 0 else 1.0)))
+    s = rng.standard_normal(n) * s_amp
+    if bc == "periodic":
+        s = s - s.mean()
+        bc_lo = bc_hi = (BC_PER, BC_PER, BC_PER)
+    else:
+        bc_lo = bc_hi = (BC_DIR, BC_DIR, BC_DIR)
+    macrhs = np.asfortranarray(r0c ** (1.0 / 1.4) * s)
+    c = MacCase(name=name, dm=dm, n=n, box=box, dx=dx, bc_lo=bc_lo, bc_hi=bc_hi, rho=rho,
+                beta0=None, beta0_edge=None, umac=umac, macrhs=macrhs,
+                phi0=np.zeros(n, order="F"), seed=seed)
+    c.b0c = b0c
+    return c
+
+
 # The five MAC-projection workloads (sizes, boxes, stratification, noise, spectrum).
 CONFIGS = {
     "2d_128": dict(dm=2, n=(128, 128), box=(128, 128), H_frac=0.25, noise=0.01,

@@ -101,6 +101,8 @@ def lib():
         d = P(ctypes.c_double)
         L.orc_macproject.argtypes = [P(OrcOpts), d, d, d, d, d, d, d, d, P(OrcStats)]
         L.orc_macproject.restype = ctypes.c_int
+        L.orc_macproject_cart.argtypes = [P(OrcOpts), d, d, d, d, d, d, d, d, d, P(OrcStats)]
+        L.orc_macproject_cart.restype = ctypes.c_int
         L.orc_mac_multigrid.argtypes = [P(OrcOpts), d, d, d, d, d, d, P(OrcStats)]
         L.orc_mac_multigrid.restype = ctypes.c_int
         L.orc_apply_op.argtypes = [P(OrcOpts), d, d, d, d, d, d]
@@ -196,6 +198,37 @@ def macproject(umac, phi, rho, dx, bc_lo, bc_hi, macrhs=None, beta0=None, beta0_
     uz = u[2] if dm == 3 else None
     lib().orc_macproject(ctypes.byref(o), _ptr(u[0]), _ptr(u[1]), _ptr(uz), _ptr(phi), _ptr(rho),
                          _ptr(rhs), _ptr(b0), _ptr(b0e), ctypes.byref(st))
+    return u, phi, st.as_dict()
+
+
+def macproject_cart(umac, phi, rho, dx, bc_lo, bc_hi, beta0_cart_edge, macrhs=None,
+                    nlevels=None, rel_eps=EPS_MAC, abs_eps=-1.0, max_vcycles=100, nu1=2, nu2=2,
+                    nub=10, bottom_eps=EPS_MAC_BOTTOM, bottom_max_iter=200,
+                    alt_energy_fix=False, threads=0):
+    """Oracle MAC projection with beta0 given on every face (the spherical form,
+    beta0_cart_edge: one face array per direction, n[d]+1 faces along d).  Returns
+    (umac_new, phi_new, stats)."""
+    phi = _f64f(phi).copy(order="F")
+    rho = _f64f(rho)
+    shape = phi.shape
+    dm = len(shape)
+    u = [_f64f(x).copy(order="F") for x in umac]
+    b = [_f64f(x) for x in beta0_cart_edge]
+    for d in range(dm):
+        exp = list(shape)
+        exp[d] += 1
+        assert u[d].shape == tuple(exp) and b[d].shape == tuple(exp), (d, u[d].shape, exp)
+    if nlevels is None:
+        nlevels = nlevels_for_boxes([shape])
+    o = _opts(shape, dx, bc_lo, bc_hi, nlevels, rel_eps, abs_eps, max_vcycles, nu1, nu2, nub,
+              bottom_eps, bottom_max_iter, alt_energy_fix, threads)
+    st = OrcStats()
+    rhs = _f64f(macrhs) if macrhs is not None else None
+    uz = u[2] if dm == 3 else None
+    bz = b[2] if dm == 3 else None
+    lib().orc_macproject_cart(ctypes.byref(o), _ptr(u[0]), _ptr(u[1]), _ptr(uz), _ptr(phi),
+                              _ptr(rho), _ptr(rhs), _ptr(b[0]), _ptr(b[1]), _ptr(bz),
+                              ctypes.byref(st))
     return u, phi, st.as_dict()
 
 

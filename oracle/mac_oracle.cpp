@@ -555,31 +555,35 @@ void orc_mac_coeffs(const orc_opts* o, const double* rho, const double* beta0,
     }
 }
 
-// Full MAC projection on one level (Source/macproject.f90:51-328), natural layout:
-// u[d] has n[d]+1 faces along d; phi is the in/out initial guess; rho is the cell density;
-// macrhs (nullable) the cell source; beta0 (nr = n[dm-1]) and beta0_edge (nr+1) nullable together.
-int orc_macproject(const orc_opts* o, double* ux, double* uy, double* uz, double* phi,
-                   const double* rho, const double* macrhs, const double* beta0,
-                   const double* beta0_edge, orc_stats* st) {
+}  // extern "C"
+
+namespace {
+
+// Full MAC projection on one level (Source/macproject.f90:51-328), natural layout: u[d] has
+// n[d]+1 faces along d; phi is the in/out initial guess; rho is the cell density; macrhs
+// (nullable) the cell source.  The beta0 of face (d, i, j, k) comes from b0face (null: no beta0):
+// the 1-D arrays for planar geometry (mult_edge_by_1d_coeff), the 3-D face multifab
+// beta0_cart_edge for spherical geometry (multifab_mult_mult / multifab_div_div,
+// Source/macproject.f90:155-161, 194-201, 236-241).
+template <class B0>
+int macproject_impl(const orc_opts* o, double* const* u, double* phi, const double* rho,
+                    const double* macrhs, bool have_b0, const B0& b0face, orc_stats* st) {
     set_threads(o);
     const int* n = o->n;
-    const int dm = o->dm, va = dm - 1;
-    double* u[3] = {ux, uy, uz};
+    const int dm = o->dm;
     const size_t N = (size_t)n[0] * n[1] * n[2];
-    auto vcoord = [&](int i, int j, int k) { return va == 0 ? i : va == 1 ? j : k; };
 
-    // mult_edge_by_1d_coeff(..., .true.)
     auto scale_edges = [&](bool mult) {
-        if (!beta0) return;
+        if (!have_b0) return;
         for (int d = 0; d < dm; ++d) {
             const int m[3] = {n[0] + (d == 0), n[1] + (d == 1), n[2] + (d == 2)};
 #pragma omp parallel for schedule(static)
             for (int k = 0; k < m[2]; ++k)
                 for (int j = 0; j < m[1]; ++j)
                     for (int i = 0; i < m[0]; ++i) {
-                        const int r = vcoord(i, j, k);
-                        const double bb = (d == va) ? beta0_edge[r] : beta0[r];
-                        double& x = u[d][fidx(n, d, i, j, k)];
+                        const size_t fi = fidx(n, d, i, j, k);
+                        const double bb = b0face(d, fi, i, j, k);
+                        double& x = u[d][fi];
                         x = mult ? x * bb : x / bb;
                     }
         }
@@ -603,11 +607,24 @@ int orc_macproject(const orc_opts* o, double* ux, double* uy, double* uz, double
                 rh[c] = -dv;
             }
 
-    // solver_beta = beta0^p / rho_face
+    // solver_beta = beta0^p / rho_face (mk_mac_coeffs, then the beta0 multiplies)
     std::vector<double> bf[3];
     for (int d = 0; d < 3; ++d)
         bf[d].assign(d < dm ? (size_t)(n[0] + (d == 0)) * (n[1] + (d == 1)) * (n[2] + (d == 2)) : 1, 0.0);
-    orc_mac_coeffs(o, rho, beta0, beta0_edge, bf[0].data(), bf[1].data(), bf[2].data());
+    orc_mac_coeffs(o, rho, nullptr, nullptr, bf[0].data(), bf[1].data(), bf[2].data());
+    if (have_b0)
+        for (int d = 0; d < dm; ++d) {
+            const int m[3] = {n[0] + (d == 0), n[1] + (d == 1), n[2] + (d == 2)};
+#pragma omp parallel for schedule(static)
+            for (int k = 0; k < m[2]; ++k)
+                for (int j = 0; j < m[1]; ++j)
+                    for (int i = 0; i < m[0]; ++i) {
+                        const size_t fi = fidx(n, d, i, j, k);
+                        const double bb = b0face(d, fi, i, j, k);
+                        bf[d][fi] *= bb;
+                        if (o->alt_energy_fix) bf[d][fi] *= bb;
+                    }
+        }
 
     Ctx C;
     C.o = *o;
@@ -645,6 +662,34 @@ int orc_macproject(const orc_opts* o, double* ux, double* uy, double* uz, double
     }
     scale_edges(false);
     return status;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Planar geometry: beta0 (nr = n[dm-1]) and beta0_edge (nr+1), nullable together.
+int orc_macproject(const orc_opts* o, double* ux, double* uy, double* uz, double* phi,
+                   const double* rho, const double* macrhs, const double* beta0,
+                   const double* beta0_edge, orc_stats* st) {
+    const int va = o->dm - 1;
+    double* u[3] = {ux, uy, uz};
+    auto b0 = [&](int d, size_t, int i, int j, int k) {
+        const int r = va == 0 ? i : va == 1 ? j : k;
+        return (d == va) ? beta0_edge[r] : beta0[r];
+    };
+    return macproject_impl(o, u, phi, rho, macrhs, beta0 != nullptr, b0, st);
+}
+
+// Spherical geometry: beta0 given on every face (beta0_cart_edge, natural face layout, n[d]+1
+// faces along d), b0x / b0y / b0z.
+int orc_macproject_cart(const orc_opts* o, double* ux, double* uy, double* uz, double* phi,
+                        const double* rho, const double* macrhs, const double* b0x,
+                        const double* b0y, const double* b0z, orc_stats* st) {
+    double* u[3] = {ux, uy, uz};
+    const double* bc[3] = {b0x, b0y, b0z};
+    auto b0 = [&](int d, size_t fi, int, int, int) { return bc[d][fi]; };
+    return macproject_impl(o, u, phi, rho, macrhs, true, b0, st);
 }
 
 // beta0 cell -> edge (Source/cell_to_edge.f90:14-70), single level, no coarse-fine chunks.
