@@ -218,6 +218,32 @@ int mac_macproject_dense(mac_ctx* ctx, double* ux, double* uy, double* uz, doubl
                          const double* beta0_edge, mac_stats* stats);
 
 /*
+ * MAC projection in the spherical form: beta0 given on every face (the beta0_cart_edge
+ * multifab argument of macproject, Source/macproject.f90:79, 103-109, 155-161, 194-201,
+ * 236-241), as MAESTRO's spherical geometry calls it on its Cartesian grid.  Arguments as
+ * mac_macproject with beta0_1d / beta0_1d_edge replaced by
+ *   beta0_cart_edge[d*nboxes + b] : edge fab of box b normal to direction d, ng_b ghosts (in)
+ * All fabs live where `ptr_kind` says.  U *= beta0 face by face, solver beta = beta0^p 2 /
+ * (rho_L + rho_R) (p = 1, 2 with use_alt_energy_fix), U = (beta0 U - beta grad phi) / beta0.
+ */
+int mac_macproject_cart(mac_ctx* ctx, int ptr_kind,
+                        double* const* umac, int ng_u,
+                        double* const* phi, int ng_phi,
+                        const double* const* rho, int ng_rho, int rho_ncomp, int rho_comp,
+                        const double* const* macrhs, int ng_rhs,
+                        const double* const* beta0_cart_edge, int ng_b,
+                        mac_stats* stats);
+
+/*
+ * Whole-domain device-array variant of mac_macproject_cart (natural layout as in
+ * mac_macproject_dense): b0x (nx+1,ny,nz), b0y (nx,ny+1,nz), b0z (nx,ny,nz+1) the beta0 faces
+ * (b0z unused in 2-D); macrhs may be NULL.
+ */
+int mac_macproject_cart_dense(mac_ctx* ctx, double* ux, double* uy, double* uz, double* phi,
+                              const double* rho, const double* macrhs, const double* b0x,
+                              const double* b0y, const double* b0z, mac_stats* stats);
+
+/*
  * Adjoint (reverse-mode derivative) of the whole-domain MAC projection; no counterpart in the
  * reference.  Forward map (beta0 form, p = 1 + use_alt_energy_fix):
  *   U_proj = U - c .* G phi,  A phi = f,  A = D diag(beta_f) G  (negated, alpha = 0),

@@ -33,6 +33,7 @@ EXPORTED = (
     "mac_ctx_set_opts", "mac_ctx_levels", "mac_macproject", "mac_multigrid",
     "mac_macproject_dense", "mac_macproject_adjoint_dense", "mac_cell_to_edge",
     "mac_solve_small_noalloc", "mac_make_macrhs", "mac_make_macrhs_dense", "mac_make_at_halftime",
+    "mac_macproject_cart", "mac_macproject_cart_dense",
 )
 MAC_NOALLOC_MAX_CELLS = 4096
 
@@ -166,6 +167,12 @@ def lib():
     L.mac_multigrid.restype = ctypes.c_int
     L.mac_macproject_dense.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, P(MacStats)]
     L.mac_macproject_dense.restype = ctypes.c_int
+    L.mac_macproject_cart.argtypes = [vp, ctypes.c_int, dpp, ctypes.c_int, dpp, ctypes.c_int,
+                                      dpp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dpp,
+                                      ctypes.c_int, dpp, ctypes.c_int, P(MacStats)]
+    L.mac_macproject_cart.restype = ctypes.c_int
+    L.mac_macproject_cart_dense.argtypes = [vp] * 10 + [P(MacStats)]
+    L.mac_macproject_cart_dense.restype = ctypes.c_int
     L.mac_macproject_adjoint_dense.argtypes = [vp] + [vp] * 17 + [P(MacStats)]
     L.mac_macproject_adjoint_dense.restype = ctypes.c_int
     L.mac_cell_to_edge.argtypes = [ctypes.c_int, dp, dp]

@@ -293,6 +293,9 @@ struct mac_ctx {
     mac::KrylovBufs kry;                          // flexible-CG vectors (allocated on first use)
     bool mean_pending = false;                    // f still holds the mean (singular problem)
     float* def_b = nullptr;                       // colour-1 defects of the finest FP32 level
+    // spherical form (beta0 on every face): solver beta and beta0 face arrays (lazily allocated)
+    double* cbeta[3] = {nullptr, nullptr, nullptr};
+    double* cb0[3] = {nullptr, nullptr, nullptr};
     double* bot_inv = nullptr;                    // dense bottom (pseudo-)inverse (small bottoms)
     cudaStream_t aux = nullptr;                   // side stream of the bottom inverse
     cudaEvent_t aux_ev[2] = {nullptr, nullptr};   // [0] operators ready, [1] inverse done
@@ -412,8 +415,10 @@ void launch_sub_mean(mac_ctx* c);
 int correct_velocity(mac_ctx* c, bool have_beta0,
                      const std::function<int(int)>* after_dir = nullptr,
                      double* phi_nat_out = nullptr);
+// reset_flags: clear the device flags (bad density, ...) first; false when a kernel of the same
+// setup already raised one
 int setup_fine_from_faces(mac_ctx* c, const double* fx, const double* fy, const double* fz,
-                          const double* alpha_nat);
+                          const double* alpha_nat, bool reset_flags = true);
 int setup_rhs_from(mac_ctx* c, const double* rh_nat, const double* phi_nat = nullptr);
 int natural_to_level0(mac_ctx* c, const double* src, double* dst);
 int level0_to_natural(mac_ctx* c, const double* src, double* dst);
@@ -449,6 +454,9 @@ int run_solve(mac_ctx* c, mac_stats* st);
 // level-0 coefficients and phi (level-0 layout) in place.
 int forward_projection(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats* st);
 int set_call_state(mac_ctx* c, bool with_alpha);
+// finest FP32 level with coefficients from rho on the fly (mixed MAC projection) or stored
+int set_otf_mode(mac_ctx* c, bool on);
+void report_call(const mac_ctx* c, const char* what, const mac_stats* st);
 int load_beta0(mac_ctx* c, int ptr_kind, const double* b0, const double* b0e);
 void begin_call_stats(mac_ctx* c, mac_stats* st);
 void end_call_stats(mac_ctx* c, mac_stats* st);

@@ -1131,7 +1131,7 @@ int scatter_faces(mac_ctx* c, int ptr_kind, double* const* fabs, int ng, int dir
 
 
 int setup_fine_from_faces(mac_ctx* c, const double* fx, const double* fy, const double* fz,
-                          const double* alpha_nat) {
+                          const double* alpha_nat, bool reset_flags) {
     Level& L = c->lev[0];
     FineParams P;
     for (int d = 0; d < 3; ++d) {
@@ -1143,7 +1143,7 @@ int setup_fine_from_faces(mac_ctx* c, const double* fx, const double* fy, const 
     }
     P.va = c->va;
     P.p = 0;
-    MAC_CUDA_TRY(cudaMemsetAsync(c->red.counters, 0, 4 * sizeof(int), c->stream));
+    if (reset_flags) MAC_CUDA_TRY(cudaMemsetAsync(c->red.counters, 0, 4 * sizeof(int), c->stream));
     const Grid3 g = grid3(L.d.n0, L.d.n1, L.d.n2);
     k_fine_coef_faces<<<g.grid, g.block, 0, c->stream>>>(
         P, L.d, fx, fy, fz, alpha_nat, alpha_nat ? L.alpha : nullptr, L.a64.bx, L.a64.by,

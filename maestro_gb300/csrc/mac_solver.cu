@@ -875,6 +875,8 @@ int forward_projection(mac_ctx* c, const double* macrhs, bool have_beta0, mac_st
     return core_macproject(c, macrhs, have_beta0, st);
 }
 int set_call_state(mac_ctx* c, bool with_alpha) { return set_call_state_impl(c, with_alpha); }
+int set_otf_mode(mac_ctx* c, bool on) { return set_otf(c, on); }
+void report_call(const mac_ctx* c, const char* what, const mac_stats* st) { report(c, what, st); }
 
 int issue_bottom_inverse(mac_ctx* c) {
     // an inverse issued by a call that stopped before its solve may still read the operator the

@@ -204,6 +204,22 @@ class MacProjector:
         self._check(rc, "mac_macproject", st, strict)
         return st.as_dict()
 
+    def macproject_cart(self, umac, phi, rho, beta0_cart_edge, macrhs=None, ng_u=1, ng_phi=1,
+                        ng_rho=1, ng_rhs=0, ng_b=1, rho_ncomp=1, rho_comp=0, strict=False):
+        """Spherical form of macproject on per-box fabs in place: beta0 on every face
+        (beta0_cart_edge: list over directions of lists over boxes of edge fabs)."""
+        nb = len(self.layout.boxes)
+        flat_u = [umac[d][b] for d in range(self.dm) for b in range(nb)]
+        flat_b = [beta0_cart_edge[d][b] for d in range(self.dm) for b in range(nb)]
+        st = capi.MacStats()
+        rc = capi.lib().mac_macproject_cart(
+            self.ctx, capi.MAC_PTR_HOST, _ptr_array(flat_u), ng_u, _ptr_array(phi), ng_phi,
+            _ptr_array(rho), ng_rho, rho_ncomp, rho_comp,
+            _ptr_array(macrhs) if macrhs is not None else None, ng_rhs, _ptr_array(flat_b),
+            ng_b, ctypes.byref(st))
+        self._check(rc, "mac_macproject_cart", st, strict)
+        return st.as_dict()
+
     def mac_multigrid(self, rh, phi, solver_beta, solver_alpha=None, ng_rh=0, ng_phi=1,
                       ng_alpha=1, ng_beta=1, strict=False):
         """Solve (alpha - div beta grad) phi = rh on per-box fabs (Source/mac_multigrid.f90)."""
@@ -256,6 +272,17 @@ class MacProjector:
         self._check(rc, "mac_macproject_dense", st, strict)
         return st.as_dict()
 
+    def macproject_cart_dense(self, ux, uy, uz, phi, rho, b0x, b0y, b0z, macrhs=None,
+                              strict=False):
+        """Whole-domain spherical form on device pointers (ints)."""
+        st = capi.MacStats()
+        v = ctypes.c_void_p
+        rc = capi.lib().mac_macproject_cart_dense(
+            self.ctx, v(ux), v(uy), v(uz or 0), v(phi), v(rho), v(macrhs or 0), v(b0x), v(b0y),
+            v(b0z or 0), ctypes.byref(st))
+        self._check(rc, "mac_macproject_cart_dense", st, strict)
+        return st.as_dict()
+
     def adjoint_dense(self, u, rho, macrhs, beta0, beta0_edge, w, du, drinv=None, dbeta0=None,
                       dmacrhs=None, phi_out=None, strict=True):
         """Adjoint of the whole-domain projection on device pointers (see maestro_mac.h)."""
@@ -290,6 +317,29 @@ def macproject(umac, phi, rho, dx, the_bc_tower: BcTower, macrhs=None, beta0_1d=
     P = MacProjector(lay, dx, the_bc_tower, precision=precision, **opts)
     try:
         st = P.macproject(fu, fphi, frho, frhs, beta0_1d, beta0_1d_edge)
+    finally:
+        P.close()
+    u_new = [lay.from_fabs(fu[d], ng=1, face_dir=d) for d in range(dm)]
+    return u_new, lay.from_fabs(fphi, ng=1), st
+
+
+def macproject_cart(umac, phi, rho, dx, the_bc_tower: BcTower, beta0_cart_edge, macrhs=None,
+                    box=None, precision="fp64", **opts):
+    """One-shot spherical-form MAC projection on whole-domain numpy arrays (beta0 on every
+    face, one face array per direction).  Returns (umac_new list, phi_new, stats)."""
+    phi = np.asfortranarray(phi, dtype=np.float64)
+    n = phi.shape
+    dm = len(n)
+    lay = Layout.tiled(n, box or n)
+    per = [the_bc_tower.lo[d] == BC_PER for d in range(dm)]
+    fu = [lay.to_fabs(umac[d], ng=1, face_dir=d, periodic=per) for d in range(dm)]
+    fb = [lay.to_fabs(beta0_cart_edge[d], ng=1, face_dir=d, periodic=per) for d in range(dm)]
+    fphi = lay.to_fabs(phi, ng=1, periodic=per)
+    frho = lay.to_fabs(rho, ng=1, periodic=per)
+    frhs = lay.to_fabs(macrhs, ng=0) if macrhs is not None else None
+    P = MacProjector(lay, dx, the_bc_tower, precision=precision, **opts)
+    try:
+        st = P.macproject_cart(fu, fphi, frho, fb, frhs)
     finally:
         P.close()
     u_new = [lay.from_fabs(fu[d], ng=1, face_dir=d) for d in range(dm)]
