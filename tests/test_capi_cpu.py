@@ -75,6 +75,31 @@ def test_invalid_geometry_rejected_without_device(lib):
     assert lib.mac_ctx_create(ctypes.byref(ctx), ctypes.byref(g), None, None) == capi.MAC_ERR_INVALID
     assert lib.mac_ctx_destroy(None) == capi.MAC_ERR_INVALID
     assert lib.mac_macproject_dense(None, *([None] * 8), None) == capi.MAC_ERR_INVALID
+    assert lib.mac_macproject_cart_dense(None, *([None] * 9), None) == capi.MAC_ERR_INVALID
+    assert lib.mac_macproject_cart(None, capi.MAC_PTR_HOST, None, 1, None, 1, None, 1, 1, 0,
+                                   None, 0, None, 1, None) == capi.MAC_ERR_INVALID
+
+
+def test_invalid_inner_options_rejected_without_device(lib):
+    # options are checked before anything touches a device
+    ctx = ctypes.c_void_p()
+    g = capi.MacGeom()
+    g.dm = 2
+    g.domain_hi[0] = 7
+    g.domain_hi[1] = 7
+    g.dx[0] = g.dx[1] = 1.0 / 8
+    g.bc_lo[0] = g.bc_hi[0] = capi.MAC_BC_PER
+    g.bc_lo[1] = g.bc_hi[1] = capi.MAC_BC_NEU
+    lo = (ctypes.c_int * 3)(0, 0, 0)
+    hi = (ctypes.c_int * 3)(7, 7, 0)
+    g.nboxes = 1
+    g.box_lo = ctypes.cast(lo, ctypes.POINTER(ctypes.c_int))
+    g.box_hi = ctypes.cast(hi, ctypes.POINTER(ctypes.c_int))
+    for bad in (dict(inner_omega=0.0), dict(inner_omega=2.0), dict(inner_omega=float("nan")),
+                dict(inner_nu1=-2), dict(inner_nu2=-3), dict(nu1=-1)):
+        o = capi.default_opts(precision=capi.MAC_PREC_MIXED, **bad)
+        rc = lib.mac_ctx_create(ctypes.byref(ctx), ctypes.byref(g), ctypes.byref(o), None)
+        assert rc == capi.MAC_ERR_INVALID, bad
 
 
 def test_cell_to_edge_matches_oracle(lib):
