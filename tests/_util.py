@@ -20,6 +20,8 @@ def load_golden(name):
     d["dx"] = tuple(float(v) for v in z["dx"])
     d["box"] = tuple(int(v) for v in z["box"])
     d["p"] = int(z["p"])
+    if "b0c0" in z.files:   # spherical form: beta0 on every face
+        d["b0c"] = [np.asfortranarray(z[f"b0c{i}"]) for i in range(dm)]
     return d
 
 

@@ -27,7 +27,7 @@ import scipy.sparse.linalg as spl
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
-from maestro_gb300.inputs import BC_DIR, BC_NEU, BC_PER, make_case  # noqa: E402
+from maestro_gb300.inputs import BC_DIR, BC_NEU, BC_PER, make_case, make_spherical_case  # noqa: E402
 
 
 def face_coeffs(rho, beta0, beta0_edge, bc_lo, bc_hi, p):
@@ -170,6 +170,41 @@ def reference_projection(case, p=1):
     return phi, u_new, rh
 
 
+def reference_projection_cart(case, p=1):
+    """The spherical form: beta0 given on every face (case.b0c), Source/macproject.f90:155-161,
+    194-201, 236-241; otherwise as reference_projection."""
+    dm = case.dm
+    n = case.n
+    beta = face_coeffs(case.rho, None, None, case.bc_lo, case.bc_hi, p)
+    beta = [np.asfortranarray(beta[d] * case.b0c[d] ** p) for d in range(dm)]
+    bu = [case.umac[d] * case.b0c[d] for d in range(dm)]
+    div = sum(np.diff(bu[d], axis=d) / case.dx[d] for d in range(dm))
+    rh = -(div - case.macrhs)
+    A = matrix(beta, case.dx, case.bc_lo, case.bc_hi, n)
+    f = rh.ravel(order="F")
+    N = f.size
+    singular = all(b != BC_DIR for b in case.bc_lo + case.bc_hi)
+    if singular:
+        f = f - f.mean()
+        one = sp.csr_matrix(np.ones((1, N)))
+        Aaug = sp.bmat([[A, one.T], [one, None]]).tocsc()
+        x = spl.spsolve(Aaug, np.concatenate([f, [0.0]]))[:N]
+    else:
+        x = spl.spsolve(A.tocsc(), f)
+    phi = x.reshape(n, order="F")
+    u_new = []
+    for d in range(dm):
+        g = grad(phi, case.dx, case.bc_lo, case.bc_hi, d)
+        u_new.append(np.asfortranarray((bu[d] - beta[d] * g) / case.b0c[d]))
+    return phi, u_new, rh
+
+
+# spherical-form cases (beta0 on every face): name -> make_spherical_case kwargs
+CART_CASES = {
+    "sph3d_16": dict(n=(16, 16, 16), box=(8, 8, 8), bc="outflow", kmax=3, seed=16),
+}
+
+
 CASES = {
     # name: (make_case kwargs, BC override, beta0 exponent)
     "strat2d_32": (dict(dm=2, n=(32, 32), box=(32, 32), H_frac=0.25, noise=0.01,
@@ -204,6 +239,19 @@ def main():
         for d in range(c.dm):
             arrs[f"u{d}"] = c.umac[d]
             arrs[f"unew{d}"] = u_new[d]
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **arrs)
+        print(path, os.path.getsize(path))
+    for name, kw in CART_CASES.items():
+        c = make_spherical_case(name=name, **kw)
+        phi, u_new, rh = reference_projection_cart(c, 1)
+        arrs = dict(rho=c.rho, macrhs=c.macrhs, phi=phi, rh=rh, bc_lo=np.array(c.bc_lo),
+                    bc_hi=np.array(c.bc_hi), dx=np.array(c.dx), box=np.array(c.box),
+                    p=np.array(1))
+        for d in range(c.dm):
+            arrs[f"u{d}"] = c.umac[d]
+            arrs[f"unew{d}"] = u_new[d]
+            arrs[f"b0c{d}"] = c.b0c[d]
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **arrs)
         print(path, os.path.getsize(path))

@@ -9,7 +9,7 @@ import pytest
 import oracle as O
 from maestro_gb300.inputs import BC_DIR, make_case, make_spherical_case
 from maestro_gb300.macproject import BcTower, Layout, MacProjector, macproject, macproject_cart
-from tests._util import phi_rel_err, u_rel_err
+from tests._util import load_golden, phi_rel_err, u_rel_err
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -91,3 +91,16 @@ def test_cart_with_planar_beta0_is_the_planar_projection(cuda_lib):
                                  box=c.box, rel_eps=1e-12)
     assert s1["status"] == 0 and s2["status"] == 0
     assert phi_rel_err(p1, p2, False) <= 1e-10 and u_rel_err(u1, u2) <= 1e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cart_matches_the_direct_solve_fixture(cuda_lib, precision):
+    # tests/golden/sph3d_16.npz: the spherical form solved by sparse LU, no multigrid involved
+    g = load_golden("sph3d_16")
+    phi0 = np.zeros(g["rho"].shape, order="F")
+    u, phi, st = macproject_cart(g["umac"], phi0, g["rho"], g["dx"],
+                                 BcTower(g["bc_lo"], g["bc_hi"]), g["b0c"], macrhs=g["macrhs"],
+                                 box=g["box"], precision=precision, rel_eps=1e-12)
+    assert st["status"] == 0 and st["rel_resid"] <= 1e-12
+    assert phi_rel_err(phi, g["phi"], False) <= 1e-9
+    assert u_rel_err(u, g["unew"]) <= 1e-9

@@ -13,7 +13,7 @@ import pytest
 
 import oracle as O
 from maestro_gb300.inputs import make_case, make_spherical_case
-from tests._util import phi_rel_err, u_rel_err
+from tests._util import load_golden, phi_rel_err, u_rel_err
 
 
 def _constraint(u, uin, b0c, dx, rhs):
@@ -54,3 +54,15 @@ def test_cart_form_projects_onto_the_constraint(bc):
     u2, _, _ = O.macproject_cart(u, p, c.rho, c.dx, c.bc_lo, c.bc_hi, c.b0c, macrhs=c.macrhs,
                                  nlevels=O.nlevels_for_boxes([c.box]))
     assert u_rel_err(u2, u) <= 1e-8
+
+
+def test_cart_form_matches_the_direct_solve_fixture():
+    # tests/golden/sph3d_16.npz: the spherical form solved by sparse LU (make_golden.py), no MG
+    g = load_golden("sph3d_16")
+    phi0 = np.zeros(g["rho"].shape, order="F")
+    u, p, st = O.macproject_cart(g["umac"], phi0, g["rho"], g["dx"], g["bc_lo"], g["bc_hi"],
+                                 g["b0c"], macrhs=g["macrhs"],
+                                 nlevels=O.nlevels_for_boxes([g["box"]]), rel_eps=1e-12)
+    assert st["status"] == 0
+    assert phi_rel_err(p, g["phi"], False) <= 1e-9
+    assert u_rel_err(u, g["unew"]) <= 1e-9
