@@ -1,7 +1,7 @@
 """GPU parity: the CUDA MAC projection (called through the C ABI) against the CPU oracle and the
 golden fixtures, FP64 and mixed precision.
 
-Tolerances (spec parity bar): relative residual <= 1e-10; phi (mean removed for singular
+Tolerances (the parity bar): relative residual <= 1e-10; phi (mean removed for singular
 problems) and the corrected U within 1e-9 relative (max-norm, relative to the oracle's max) for
 the FP64 solve.  The mixed-precision solve converges to the same 1e-10 residual along a different
 iterate sequence; its distance to the FP64 oracle is bounded by 1e-8 here and reported by bench.

@@ -20,7 +20,7 @@ def test_oracle_matches_direct_solve(name):
                               beta0_edge=g["beta0_edge"], nlevels=nlev, rel_eps=1e-12,
                               alt_energy_fix=g["p"] == 2)
     assert st["status"] == 0 and st["rel_resid"] <= 1e-12
-    # both sides solve the same discrete system; tolerance 1e-9 relative (spec parity bar)
+    # both sides solve the same discrete system; tolerance 1e-9 relative (the parity bar)
     assert phi_rel_err(phi, g["phi"], singular) <= 1e-9
     assert u_rel_err(u, g["unew"]) <= 1e-9
 
