@@ -150,3 +150,35 @@ def test_divergence_constraint_after_projection():
         shp[va] = bb.size
         div0 = div0 + np.diff(c.umac[d] * bb.reshape(shp), axis=d) / c.dx[d]
     assert rel_err(div, c.macrhs + 0 * div) <= 2e-10 * np.max(np.abs(div0 - c.macrhs)) / np.max(np.abs(c.macrhs))
+
+
+def _golden_module():
+    import importlib.util
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "make_golden.py")
+    spec = importlib.util.spec_from_file_location("make_golden", path)
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m
+
+
+@pytest.mark.parametrize("bcs", ["wall", "outlet"])
+def test_oracle_helmholtz_matches_direct_solve(bcs):
+    # mac_multigrid with alpha != 0 (the thermal-diffusion form, Source/thermal_conduct.f90:375)
+    # against a sparse LU solve of (alpha - div beta grad) phi = rh with the same discretisation
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+    from maestro_gb300.inputs import BC_DIR, make_case
+    g = _golden_module()
+    c = make_case(dm=3, n=(16, 16, 16), box=(8, 8, 8), kmax=3, seed=21)
+    if bcs == "outlet":
+        c.bc_hi = (c.bc_hi[0], c.bc_hi[1], BC_DIR)
+    beta = g.face_coeffs(c.rho, c.beta0, c.beta0_edge, c.bc_lo, c.bc_hi, 1)
+    alpha = np.asfortranarray(c.rho * 1e-3)
+    rh = np.asfortranarray(np.random.default_rng(4).standard_normal(c.n))
+    A = g.matrix(beta, c.dx, c.bc_lo, c.bc_hi, c.n) + sp.diags(alpha.ravel(order="F"))
+    x = spl.spsolve(A.tocsc(), rh.ravel(order="F")).reshape(c.n, order="F")
+    phi, st = O.mac_multigrid(rh, np.zeros(c.n, order="F"), beta, c.dx, c.bc_lo, c.bc_hi,
+                              alpha=alpha, nlevels=O.nlevels_for_boxes([c.box]), rel_eps=1e-12)
+    assert st["status"] == 0
+    assert rel_err(phi, x) <= 1e-9
