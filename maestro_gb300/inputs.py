@@ -271,3 +271,149 @@ def config_case(key: str, seed: int = 1234, scale: int = 1) -> MacCase:
         kw["box"] = tuple(max(2, v // scale) for v in kw["box"])
         kw["kmax"] = max(2, kw["kmax"] // scale)
     return make_case(name=key, seed=seed, **kw)
+
+
+# ------------------------------------------------------------------ multi-level (AMR) inputs
+
+@dataclasses.dataclass
+class AmrCase:
+    """A MAC-projection input set on an AMR hierarchy with refinement ratio 2.
+
+    Level l spans the whole level domain (n0 << l cells per direction) as dense arrays; only the
+    cells of its boxes (`boxes[l]`, (lo, hi) inclusive in level-l indices; level 0 is the
+    domain) carry data.  rho, macrhs, phi0: cell arrays per level; umac: dm face arrays per
+    level; beta0 / beta0_edge: the planar base state of every level."""
+
+    name: str
+    dm: int
+    n0: tuple
+    dx0: tuple
+    bc_lo: tuple
+    bc_hi: tuple
+    boxes: list
+    rho: list
+    beta0: list
+    beta0_edge: list
+    umac: list
+    macrhs: list
+    phi0: list
+    seed: int = 0
+
+    @property
+    def nlev(self) -> int:
+        return len(self.boxes)
+
+    def shape(self, l: int) -> tuple:
+        return tuple(int(v) << l for v in self.n0)
+
+    def dx(self, l: int) -> tuple:
+        return tuple(h / (1 << l) for h in self.dx0)
+
+
+def _smooth_cell_field(seed: int, n, dm: int, kmax: int):
+    """Seeded smooth cell-centred field of unit max: cosine modes, periodic horizontally,
+    cos(k pi z) vertically, so every resolution samples the same function."""
+    rng = np.random.default_rng(seed)
+    pos = [(np.arange(n[e]) + 0.5) / n[e] for e in range(dm)]
+    X = np.meshgrid(*pos, indexing="ij")
+    f = np.zeros(tuple(n))
+    for _ in range(4 * kmax):
+        k = rng.integers(-kmax, kmax + 1, size=dm)
+        k[dm - 1] = abs(k[dm - 1])
+        ph = rng.uniform(0, 2 * np.pi, size=dm)
+        a = rng.standard_normal() / (1.0 + float(np.sum(k * k)))
+        t = a * np.cos(np.pi * k[dm - 1] * X[dm - 1] + ph[dm - 1])
+        for e in range(dm - 1):
+            t = t * np.cos(2 * np.pi * k[e] * X[e] + ph[e])
+        f += t
+    m = np.max(np.abs(f))
+    return f / (m if m > 0 else 1.0)
+
+
+def average_down(fine: np.ndarray) -> np.ndarray:
+    """Mean of the 2^dm children of every coarse cell."""
+    dm = fine.ndim
+    out = 0.0
+    for a in range(1 << dm):
+        out = out + fine[tuple(slice((a >> e) & 1, None, 2) for e in range(dm))]
+    return out / (1 << dm)
+
+
+def region_mask(shape, boxes) -> np.ndarray:
+    m = np.zeros(shape, dtype=bool)
+    for lo, hi in boxes:
+        m[tuple(slice(lo[e], hi[e] + 1) for e in range(len(shape)))] = True
+    return m
+
+
+def make_amr_case(name: str = "amr", dm: int = 2, n0=(32, 32), boxes=None, H_frac: float = 0.25,
+                  noise: float = 0.05, kmax: int = 4, seed: int = 2024, u_amp: float = 1e6,
+                  s_amp: float = 1e-3, bc: str = "wall") -> AmrCase:
+    """Seeded stratified-atmosphere MAC case on an AMR hierarchy (the planar workload of
+    `make_case`, smooth so that every level samples the same fields).
+
+    rho = rho0(z) exp(noise P(x)) with P a smooth unit-max field, beta0 = rho0^(1/1.4) per level
+    with cell_to_edge edges, U the Fourier field of `make_case` sampled on each level's faces,
+    macrhs = beta0 (S - Sbar) with S smooth and Sbar its layer mean on each level.  The density of
+    covered cells is the mean of their children (the state after MAESTRO's average-down).
+    bc: "wall" (periodic horizontally, slip walls vertically) or "periodic"."""
+    n0 = tuple(int(v) for v in n0)
+    assert len(n0) == dm
+    boxes = [[]] + [list(b) for b in (boxes or [])[1:]] if boxes else [[]]
+    nlev = len(boxes)
+    dx0 = tuple(1.0 / n0[0] for _ in range(dm))
+    bc_v = BC_PER if bc == "periodic" else BC_NEU
+    bc_lo = tuple([BC_PER] * (dm - 1) + [bc_v])
+    bc_hi = bc_lo
+    rho, b0, b0e, umac, macrhs, phi0 = [], [], [], [], [], []
+    # U normalisation from level 0 so all levels carry the same field
+    norms = []
+    for d in range(dm):
+        u0 = _fourier_component(np.random.default_rng(seed + 10 + d), n0, dm, d, kmax)
+        m = float(np.max(np.abs(u0)))
+        norms.append(u_amp / m if m > 0 else 1.0)
+    for l in range(nlev):
+        n = tuple(v << l for v in n0)
+        nz = n[dm - 1]
+        z = (np.arange(nz) + 0.5) / nz
+        rho0 = 1e7 * np.exp(-z / H_frac)
+        shp = [1] * dm
+        shp[dm - 1] = nz
+        P = _smooth_cell_field(seed, n, dm, kmax)
+        rho.append(rho0.reshape(shp) * np.exp(noise * P))
+        beta0 = rho0 ** (1.0 / 1.4)
+        b0.append(beta0)
+        b0e.append(cell_to_edge(beta0))
+        umac.append([np.asfortranarray(
+            _fourier_component(np.random.default_rng(seed + 10 + d), n, dm, d, kmax) * norms[d])
+            for d in range(dm)])
+        S = s_amp * _smooth_cell_field(seed + 1, n, dm, kmax)
+        S = S - S.mean(axis=tuple(range(dm - 1)), keepdims=True)
+        macrhs.append(np.asfortranarray(beta0.reshape(shp) * S))
+        phi0.append(np.zeros(n, order="F"))
+    for l in range(nlev - 1, 0, -1):
+        cov = region_mask(tuple(v << (l - 1) for v in n0),
+                          [(tuple(a // 2 for a in lo), tuple(b // 2 for b in hi)) for lo, hi in boxes[l]])
+        rho[l - 1] = np.where(cov, average_down(rho[l]), rho[l - 1])
+    rho = [np.asfortranarray(r) for r in rho]
+    return AmrCase(name=name, dm=dm, n0=n0, dx0=dx0, bc_lo=bc_lo, bc_hi=bc_hi, boxes=boxes,
+                   rho=rho, beta0=b0, beta0_edge=b0e, umac=umac, macrhs=macrhs, phi0=phi0,
+                   seed=seed)
+
+
+AMR_CASES = {
+    # two levels, a fine patch in the middle of a 2-D atmosphere
+    "amr2d_32": dict(dm=2, n0=(32, 32), boxes=[[], [((16, 8), (47, 39))]]),
+    # two fine boxes, one wrapping the periodic x boundary, one on the bottom wall
+    "amr2d_wrap": dict(dm=2, n0=(32, 32), boxes=[[], [((0, 16), (11, 47)), ((52, 16), (63, 47)),
+                                                       ((24, 0), (39, 15))]]),
+    # three levels
+    "amr2d_3lev": dict(dm=2, n0=(32, 32), boxes=[[], [((8, 8), (55, 55))], [((32, 32), (79, 79))]]),
+    # 3-D, two levels, two boxes
+    "amr3d_16": dict(dm=3, n0=(16, 16, 16), boxes=[[], [((8, 8, 8), (23, 23, 23)),
+                                                          ((0, 0, 24), (7, 31, 31))]]),
+}
+
+
+def amr_case(key: str, seed: int = 2024) -> AmrCase:
+    return make_amr_case(name=key, seed=seed, **AMR_CASES[key])

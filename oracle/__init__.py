@@ -83,10 +83,13 @@ class OrcStats(ctypes.Structure):
 _lib = None
 
 
+_SOURCES = ("mac_oracle.cpp", "mac_oracle_ml.cpp", "mac_oracle_core.h")
+
+
 def build(force: bool = False) -> str:
-    """Compile mac_oracle.cpp into oracle/_build/libmac_oracle.so (g++ + OpenMP)."""
-    if force or not os.path.exists(_LIB_PATH) or (
-        os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "mac_oracle.cpp"))
+    """Compile the oracle sources into oracle/_build/libmac_oracle.so (g++ + OpenMP)."""
+    if force or not os.path.exists(_LIB_PATH) or any(
+        os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, f)) for f in _SOURCES
     ):
         subprocess.check_call(["make", "-s", "-C", _HERE], stdout=subprocess.DEVNULL)
     return _LIB_PATH
@@ -111,6 +114,15 @@ def lib():
         L.orc_mac_coeffs.restype = None
         L.orc_cell_to_edge.argtypes = [ctypes.c_int, d, d]
         L.orc_cell_to_edge.restype = None
+        pd = P(d)
+        ip = P(ctypes.c_int)
+        L.orc_ml_solve.argtypes = [P(OrcOpts), ctypes.c_int, ip, ip, pd, pd, pd, P(OrcStats)]
+        L.orc_ml_solve.restype = ctypes.c_int
+        L.orc_ml_residual.argtypes = [P(OrcOpts), ctypes.c_int, ip, ip, pd, pd, pd, pd]
+        L.orc_ml_residual.restype = ctypes.c_double
+        L.orc_macproject_ml.argtypes = [P(OrcOpts), ctypes.c_int, ip, ip, pd, pd, pd, pd, pd, pd,
+                                        P(OrcStats)]
+        L.orc_macproject_ml.restype = ctypes.c_int
         L.orc_max_threads.argtypes = []
         L.orc_max_threads.restype = ctypes.c_int
         _lib = L
@@ -323,3 +335,137 @@ def make_macrhs(S_cc, delta_gamma1_term, Sbar, beta0, gamma1bar=None, p0=None, d
 def make_at_halftime(sold, snew):
     """Source/make_at_halftime.f90:134-190: half = (old + new) / 2 cell by cell."""
     return 0.5 * (np.asarray(sold, dtype=np.float64) + np.asarray(snew, dtype=np.float64))
+
+
+# ---------------------------------------------------------------- multi-level (AMR) composite
+
+def _ml_layout(shape0, boxes):
+    """nboxes / boxes int arrays of the C entry points.  `boxes[l]` (l >= 1) is a list of
+    (lo, hi) tuples in level-l cell indices; boxes[0] is ignored (level 0 is the domain)."""
+    nlev = len(boxes)
+    dm = len(shape0)
+    nb = np.zeros(nlev, dtype=np.int32)
+    flat = []
+    for l in range(1, nlev):
+        nb[l] = len(boxes[l])
+        for lo, hi in boxes[l]:
+            flat += list(lo) + [0] * (3 - dm) + list(hi) + [0] * (3 - dm)
+    bx = np.asarray(flat if flat else [0], dtype=np.int32)
+    return nb, bx
+
+
+def _ptr_array(arrs):
+    t = ctypes.POINTER(ctypes.c_double) * len(arrs)
+    return t(*[_ptr(a) for a in arrs])
+
+
+def level_shape(shape0, l):
+    return tuple(int(n) << l for n in shape0)
+
+
+def ml_rel_eps(nlev: int) -> float:
+    """rel_solver_eps of Source/macproject.f90:217 for nlev AMR levels."""
+    return min(EPS_MAC * MAC_LEVEL_FACTOR ** (nlev - 1), EPS_MAC_MAX)
+
+
+def ml_solve(rh, phi, beta, dx, bc_lo, bc_hi, boxes, nlevels=None, rel_eps=None, abs_eps=-1.0,
+             max_vcycles=200, nu1=2, nu2=2, nub=10, bottom_eps=EPS_MAC_BOTTOM,
+             bottom_max_iter=200, threads=0):
+    """Composite multi-level solve of -div(beta grad phi) = rh (mac_oracle_ml.cpp).
+
+    rh[l], phi[l]: cell arrays over the whole level-l domain (shape0 << l); beta[l]: list of
+    face arrays of level l.  Returns (phi list, stats); covered cells of phi hold the mean of
+    their children."""
+    nlev = len(rh)
+    shape0 = np.shape(rh[0])
+    dm = len(shape0)
+    rh = [_f64f(r) for r in rh]
+    phi = [_f64f(p).copy(order="F") for p in phi]
+    bl = []
+    for l in range(nlev):
+        for d in range(3):
+            bl.append(_f64f(beta[l][d]) if d < dm else None)
+    if nlevels is None:
+        nlevels = nlevels_for_boxes([shape0])
+    if rel_eps is None:
+        rel_eps = ml_rel_eps(nlev)
+    o = _opts(shape0, dx, bc_lo, bc_hi, nlevels, rel_eps, abs_eps, max_vcycles, nu1, nu2, nub,
+              bottom_eps, bottom_max_iter, False, threads)
+    nb, bx = _ml_layout(shape0, boxes)
+    st = OrcStats()
+    rc = lib().orc_ml_solve(ctypes.byref(o), nlev, nb.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                            bx.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _ptr_array(rh),
+                            _ptr_array(phi), _ptr_array(bl), ctypes.byref(st))
+    if rc < 0:
+        raise ValueError("invalid AMR layout (alignment or proper nesting)")
+    return phi, st.as_dict()
+
+
+def ml_residual(rh, phi, beta, dx, bc_lo, bc_hi, boxes):
+    """Composite residual rh - L phi on every level.  Returns (list of arrays, max over valid
+    cells)."""
+    nlev = len(rh)
+    shape0 = np.shape(rh[0])
+    dm = len(shape0)
+    rh = [_f64f(r) for r in rh]
+    phi = [_f64f(p) for p in phi]
+    res = [np.zeros(level_shape(shape0, l), order="F") for l in range(nlev)]
+    bl = []
+    for l in range(nlev):
+        for d in range(3):
+            bl.append(_f64f(beta[l][d]) if d < dm else None)
+    o = _opts(shape0, dx, bc_lo, bc_hi, 1, 0, 0, 0, 0, 0, 0, 0, 0, False, 0)
+    nb, bx = _ml_layout(shape0, boxes)
+    r = lib().orc_ml_residual(ctypes.byref(o), nlev,
+                              nb.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                              bx.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _ptr_array(rh),
+                              _ptr_array(phi), _ptr_array(bl), _ptr_array(res))
+    if r < 0:
+        raise ValueError("invalid AMR layout (alignment or proper nesting)")
+    return res, float(r)
+
+
+def macproject_ml(umac, phi, rho, dx, bc_lo, bc_hi, boxes, macrhs=None, beta0=None,
+                  beta0_edge=None, nlevels=None, rel_eps=None, abs_eps=-1.0, max_vcycles=200,
+                  nu1=2, nu2=2, nub=10, bottom_eps=EPS_MAC_BOTTOM, bottom_max_iter=200,
+                  alt_energy_fix=False, threads=0):
+    """Oracle multi-level MAC projection (Source/macproject.f90:51-328, nlevs > 1).
+
+    umac[l]: list of dm face arrays over the whole level-l domain; phi[l], rho[l], macrhs[l]:
+    cell arrays of level l (rho read on the level's boxes plus one ghost cell); beta0[l],
+    beta0_edge[l]: planar base state of level l.  dx is the level-0 spacing.  rel_eps defaults
+    to min(eps_mac 10^(nlev-1), eps_mac_max).  Returns (umac list, phi list, stats)."""
+    nlev = len(phi)
+    shape0 = np.shape(phi[0])
+    dm = len(shape0)
+    phi = [_f64f(p).copy(order="F") for p in phi]
+    rho = [_f64f(r) for r in rho]
+    u = [[_f64f(x).copy(order="F") for x in umac[l]] for l in range(nlev)]
+    up = []
+    for l in range(nlev):
+        for d in range(3):
+            up.append(u[l][d] if d < dm else None)
+    mrl = None if macrhs is None else [None if m is None else _f64f(m) for m in macrhs]
+    mr = None if mrl is None else _ptr_array(mrl)
+    if beta0 is not None:
+        b0 = [np.ascontiguousarray(b, dtype=np.float64) for b in beta0]
+        b0e = [np.ascontiguousarray(b, dtype=np.float64) for b in beta0_edge]
+        pb0, pb0e = _ptr_array(b0), _ptr_array(b0e)
+    else:
+        pb0 = pb0e = None
+    if nlevels is None:
+        nlevels = nlevels_for_boxes([shape0])
+    if rel_eps is None:
+        rel_eps = ml_rel_eps(nlev)
+    o = _opts(shape0, dx, bc_lo, bc_hi, nlevels, rel_eps, abs_eps, max_vcycles, nu1, nu2, nub,
+              bottom_eps, bottom_max_iter, alt_energy_fix, threads)
+    nb, bx = _ml_layout(shape0, boxes)
+    st = OrcStats()
+    rc = lib().orc_macproject_ml(ctypes.byref(o), nlev,
+                                 nb.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                 bx.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _ptr_array(up),
+                                 _ptr_array(phi), _ptr_array(rho), mr, pb0, pb0e,
+                                 ctypes.byref(st))
+    if rc < 0:
+        raise ValueError("invalid AMR layout (alignment or proper nesting)")
+    return u, phi, st.as_dict()
