@@ -244,6 +244,37 @@ int mac_macproject_cart_dense(mac_ctx* ctx, double* ux, double* uy, double* uz, 
                               const double* b0y, const double* b0z, mac_stats* stats);
 
 /*
+ * Multi-level (AMR) hierarchy of a context, replacing the ml_layout `mla` of
+ * macproject(mla, umac(nlev,dm), phi(nlev), rho(nlev), dx(nlev,dm), the_bc_tower, macrhs(nlev),
+ * beta0_1d(nlev,:), beta0_1d_edge(nlev,:)) (Source/macproject.f90:51-76) for nlevs > 1.
+ * Level 0 is the context's own geometry; levels 1 .. nlev-1 refine by 2 and are given by their
+ * boxes in level-l cell indices: nboxes[l] boxes for l >= 1 (nboxes[0] is ignored), their lo / hi
+ * corners (3 ints each, level 1's boxes first) in box_lo / box_hi.  Every box is aligned to the
+ * ratio (even lo, odd hi) and properly nested: its cells coarsened and grown by one cell in every
+ * direction lie in the level below (or beyond a non-periodic domain face).  nlev == 1 drops the
+ * hierarchy.  Returns MAC_ERR_INVALID for a bad layout.
+ */
+int mac_ctx_set_amr(mac_ctx* ctx, int nlev, const int* nboxes, const int* box_lo,
+                    const int* box_hi);
+
+/*
+ * Multi-level MAC projection (Source/macproject.f90:51-328 with nlevs > 1) on whole-level-domain
+ * DEVICE arrays, Fortran order: level l spans (n[d] << l) cells along each direction of the
+ * context's domain; only the cells of its boxes (and for rho one cell around them) and the faces
+ * bordering them are read or written.  umac[3*l + d] faces of level l (n_l[d] + 1 along d; in/out),
+ * phi[l] cells (in: initial guess; out: the composite solution, covered cells the mean of their
+ * children), rho[l] cells, macrhs (NULL, or per level, entries may be NULL), beta0[l] /
+ * beta0_edge[l] the planar base state of level l (n_l[dm-1] and n_l[dm-1] + 1 values; NULL
+ * together: no beta0).  The composite problem (coarse-fine ghosts, reflux) is described in the
+ * library's mac_amr.cuh; the tolerance is min(rel_eps * 10^(nlev-1), 1e-8) as in MAESTRO
+ * (Source/macproject.f90:217); FP64 whatever the context's precision.  Needs mac_ctx_set_amr.
+ */
+int mac_macproject_ml_dense(mac_ctx* ctx, double* const* umac, double* const* phi,
+                            const double* const* rho, const double* const* macrhs,
+                            const double* const* beta0, const double* const* beta0_edge,
+                            mac_stats* stats);
+
+/*
  * Adjoint (reverse-mode derivative) of the whole-domain MAC projection; no counterpart in the
  * reference.  Forward map (beta0 form, p = 1 + use_alt_energy_fix):
  *   U_proj = U - c .* G phi,  A phi = f,  A = D diag(beta_f) G  (negated, alpha = 0),

@@ -33,7 +33,8 @@ EXPORTED = (
     "mac_ctx_set_opts", "mac_ctx_levels", "mac_macproject", "mac_multigrid",
     "mac_macproject_dense", "mac_macproject_adjoint_dense", "mac_cell_to_edge",
     "mac_solve_small_noalloc", "mac_make_macrhs", "mac_make_macrhs_dense", "mac_make_at_halftime",
-    "mac_macproject_cart", "mac_macproject_cart_dense",
+    "mac_macproject_cart", "mac_macproject_cart_dense", "mac_ctx_set_amr",
+    "mac_macproject_ml_dense",
 )
 MAC_NOALLOC_MAX_CELLS = 4096
 
@@ -189,6 +190,11 @@ def lib():
     L.mac_make_macrhs_dense.restype = ci
     L.mac_make_at_halftime.argtypes = [vp, ci, dpp, ci, ci, ci, dpp, ci, dpp, ci, ci, ci]
     L.mac_make_at_halftime.restype = ci
+    vpp = P(vp)
+    L.mac_ctx_set_amr.argtypes = [vp, ci, ip, ip, ip]
+    L.mac_ctx_set_amr.restype = ci
+    L.mac_macproject_ml_dense.argtypes = [vp, vpp, vpp, vpp, vpp, vpp, vpp, P(MacStats)]
+    L.mac_macproject_ml_dense.restype = ci
     _lib = L
     return L
 

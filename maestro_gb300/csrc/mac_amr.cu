@@ -1,0 +1,686 @@
+// Multi-level (AMR) MAC projection on the GPU: the composite cell functions of mac_amr.cuh as
+// kernels, the executor that runs amr_solve / amr_project on device arrays, and the C ABI
+// (mac_ctx_set_amr, mac_macproject_ml_dense).
+//
+// Level 0 is the context's own one-level geometry; its multigrid (the FP64 V-cycle of
+// mac_solver.cu, with the context's coarsening, tail and bottom solve) is the coarse correction
+// of the multi-level cycle.  Finer levels are dense FP64 arrays over their whole level domain
+// with a byte mask (kIn: the level's boxes; kCov: under the next finer level): one thread per
+// cell or face, masked.  All launches go to the context's stream; the host reads one residual
+// norm per multi-level cycle.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "mac_amr.cuh"
+#include "mac_internal.cuh"
+
+namespace mac {
+
+using amr::Geo;
+using amr::Lev;
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kReduceBlocks = 1024;   // per-level partial slots of the valid-cell reductions
+
+// ---- kernels (grid-stride over the cells / faces of one level) --------------------------------
+
+#define AMR_LOOP(N) for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < (N); \
+                         idx += (long)gridDim.x * blockDim.x)
+
+__global__ void k_defect(Geo G, Lev L, Lev C, const double* u, const double* cu, const double* f,
+                         double* r, long N) {
+    AMR_LOOP(N) amr::defect_cell(G, L, C, idx, u, cu, f, r);
+}
+
+__global__ void k_gsrb(Geo G, Lev L, int colour, double* u, const double* f, long N) {
+    AMR_LOOP(N) amr::gsrb_cell(G, L, idx, colour, u, f);
+}
+
+__global__ void k_reflux(Geo G, Lev F, Lev C, const double* uf, const double* uc, double* res,
+                         long N) {
+    AMR_LOOP(N) amr::reflux_cell(G, F, C, idx, uf, uc, res);
+}
+
+__global__ void k_restrict(Geo G, Lev F, Lev C, const double* fine, double* crse, long N) {
+    AMR_LOOP(N) amr::restrict_cell(G, F, C, idx, fine, crse);
+}
+
+__global__ void k_prolong(Geo G, Lev F, Lev C, const double* uc, double* uf, long N) {
+    AMR_LOOP(N) amr::prolong_cell(G, F, C, idx, uc, uf);
+}
+
+__global__ void k_axpy3(Lev L, double* uu, const double* hold, const double* du, long N) {
+    AMR_LOOP(N) if (amr::in_region(L, idx)) uu[idx] += hold[idx] + du[idx];
+}
+
+__global__ void k_add_region(Lev L, double* phi, const double* uu, long N) {
+    AMR_LOOP(N) if (amr::in_region(L, idx)) phi[idx] += uu[idx];
+}
+
+// Per-block partials over the cells of one level: [0] sum of vol * x, [1] max |x|, [2] NaN
+// count, [3] volume.  valid_only: valid cells (kIn without kCov), else every region cell.
+__global__ void k_reduce(Lev L, const double* x, double vol, int valid_only, double* part,
+                         long N) {
+    __shared__ double s_sum[kThreads / 32], s_max[kThreads / 32], s_nan[kThreads / 32],
+        s_vol[kThreads / 32];
+    double sum = 0.0, mx = 0.0, nan = 0.0, v = 0.0;
+    AMR_LOOP(N) {
+        const bool take = valid_only ? amr::is_valid(L, idx) : amr::in_region(L, idx);
+        if (!take) continue;
+        const double a = x[idx];
+        if (a != a) {
+            nan += 1.0;
+            continue;
+        }
+        sum += vol * a;
+        mx = fmax(mx, fabs(a));
+        v += vol;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        sum += __shfl_down_sync(0xffffffffu, sum, o);
+        mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+        nan += __shfl_down_sync(0xffffffffu, nan, o);
+        v += __shfl_down_sync(0xffffffffu, v, o);
+    }
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        s_sum[w] = sum;
+        s_max[w] = mx;
+        s_nan[w] = nan;
+        s_vol[w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < kThreads / 32; ++q) {
+            sum += s_sum[q];
+            mx = fmax(mx, s_max[q]);
+            nan += s_nan[q];
+            v += s_vol[q];
+        }
+        double* p = part + 4 * blockIdx.x;
+        p[0] = sum;
+        p[1] = mx;
+        p[2] = nan;
+        p[3] = v;
+    }
+}
+
+// out[0] sum, out[1] max, out[2] NaN count, out[3] volume, out[4] mean = sum / volume; one
+// block, fixed order (deterministic).
+__global__ void k_reduce_finish(const double* part, int nparts, double* out) {
+    __shared__ double s[4][kThreads];
+    double a[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int q = threadIdx.x; q < nparts; q += blockDim.x) {
+        a[0] += part[4 * q];
+        a[1] = fmax(a[1], part[4 * q + 1]);
+        a[2] += part[4 * q + 2];
+        a[3] += part[4 * q + 3];
+    }
+    for (int k = 0; k < 4; ++k) s[k][threadIdx.x] = a[k];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            s[0][threadIdx.x] += s[0][threadIdx.x + w];
+            s[1][threadIdx.x] = fmax(s[1][threadIdx.x], s[1][threadIdx.x + w]);
+            s[2][threadIdx.x] += s[2][threadIdx.x + w];
+            s[3][threadIdx.x] += s[3][threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 4; ++k) out[k] = s[k][0];
+        out[4] = s[3][0] > 0.0 ? s[0][0] / s[3][0] : 0.0;
+    }
+}
+
+// x -= *m on the valid cells (valid_only) or every region cell.
+__global__ void k_sub_scalar(Lev L, double* x, const double* m, int valid_only, long N) {
+    const double v = *m;
+    AMR_LOOP(N) {
+        const bool take = valid_only ? amr::is_valid(L, idx) : amr::in_region(L, idx);
+        if (take) x[idx] -= v;
+    }
+}
+
+__global__ void k_scale_b0(Geo G, Lev L, int d, double* u, const double* b0, const double* b0e,
+                           int mult, long N) {
+    AMR_LOOP(N) {
+        int f[3];
+        amr::face_coords(L, d, idx, f);
+        const double bb = amr::beta0_of_face(G, d, f, b0, b0e);
+        u[idx] = mult ? u[idx] * bb : u[idx] / bb;
+    }
+}
+
+__global__ void k_edge_restrict(Geo G, Lev F, Lev C, int d, double* uc, const double* uf, long N) {
+    AMR_LOOP(N) amr::edge_restrict_face(G, F, C, d, idx, uc, uf);
+}
+
+__global__ void k_divergence(Geo G, Lev L, const double* u0, const double* u1, const double* u2,
+                             const double* macrhs, double* rh, long N) {
+    AMR_LOOP(N) amr::divergence_cell(G, L, idx, u0, u1, u2, macrhs, rh);
+}
+
+__global__ void k_coeff(Geo G, Lev L, int d, const double* rho, const double* b0,
+                        const double* b0e, int alt, double* beta, long N) {
+    AMR_LOOP(N) amr::coeff_face(G, L, d, idx, rho, b0, b0e, alt, beta);
+}
+
+__global__ void k_correct(Geo G, Lev L, Lev C, int d, const double* phi, const double* cphi,
+                          const double* beta, double* u, long N) {
+    AMR_LOOP(N) amr::correct_face(G, L, C, d, idx, phi, cphi, beta, u);
+}
+
+// A density that is not positive and finite on a cell the level's faces read (its region and
+// one cell around it along each direction) raises flag[0].
+__global__ void k_check_rho(Geo G, Lev L, const double* rho, int* flag, long N) {
+    AMR_LOOP(N) {
+        int c[3];
+        amr::cell_coords(L, idx, c);
+        bool used = amr::in_region(L, idx);
+        for (int d = 0; d < G.dm && !used; ++d)
+            for (int s = -1; s <= 1 && !used; s += 2) {
+                const int q = amr::wrap(G, L, d, c[d] + s);
+                if (q < 0) continue;
+                int p[3] = {c[0], c[1], c[2]};
+                p[d] = q;
+                used = amr::in_region(L, amr::cix(L, p[0], p[1], p[2]));
+            }
+        if (!used) continue;
+        const double v = rho[idx];
+        if (!(v > 0.0) || !(v < INFINITY)) atomicExch(flag, 1);
+    }
+}
+
+inline int blocks_for(long n, int sms) {
+    const long b = (n + kThreads - 1) / kThreads;
+    const long cap = (long)std::max(1, sms) * 16;
+    return (int)std::max(1L, std::min(b, cap));
+}
+
+}  // namespace
+
+// ---- per-context multi-level state ---------------------------------------------------------------
+
+struct AmrState {
+    int nlev = 0;
+    Geo geo{};
+    std::vector<std::vector<int>> boxes;   // per level: lo[3], hi[3] per box (level indices)
+    struct LevelStore {
+        Lev lev{};
+        unsigned char* mask = nullptr;
+        double* beta[3] = {nullptr, nullptr, nullptr};
+        double* buf[amr::kNumBufs] = {};
+        double* phi_user = nullptr;   // the caller's phi of this call (aliases buf kPhi)
+        long ncell = 0;
+    };
+    std::vector<LevelStore> L;
+    double* part = nullptr;     // reduction partials: kReduceBlocks * 4 per level
+    double* out = nullptr;      // reduction result (5 doubles) + 8 scratch
+    double* h_out = nullptr;    // pinned mirror
+    int* flag = nullptr;        // device flag (bad density)
+    int* h_flag = nullptr;
+    std::vector<void*> allocs;
+    size_t bytes = 0;
+};
+
+void amr_release(mac_ctx* c) {
+    AmrState* A = c->amr;
+    if (!A) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (void* p : A->allocs) cudaFree(p);
+    if (A->h_out) cudaFreeHost(A->h_out);
+    if (A->h_flag) cudaFreeHost(A->h_flag);
+    delete A;
+    c->amr = nullptr;
+}
+
+namespace {
+
+template <typename T>
+int amr_alloc(AmrState* A, T** p, size_t n) {
+    void* q = nullptr;
+    const size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+    if (cudaMalloc(&q, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return MAC_ERR_ALLOC;
+    }
+    A->allocs.push_back(q);
+    A->bytes += bytes;
+    *p = static_cast<T*>(q);
+    return MAC_OK;
+}
+
+// Host-side layout check and masks (alignment to the ratio 2, boxes inside the level domain,
+// proper nesting with one coarse cell of buffer, diagonals included).
+int build_masks(const mac_ctx* c, int nlev, const int* nboxes, const int* box_lo,
+                const int* box_hi, std::vector<std::vector<unsigned char>>& masks,
+                std::vector<std::vector<int>>& boxes, int n_out[][3]) {
+    const int dm = c->dm;
+    masks.assign(nlev, {});
+    boxes.assign(nlev, {});
+    for (int l = 0; l < nlev; ++l) {
+        long N = 1;
+        for (int d = 0; d < 3; ++d) {
+            n_out[l][d] = d < dm ? (c->n[d] << l) : 1;
+            N *= n_out[l][d];
+        }
+        if (N > (1L << 31)) return MAC_ERR_TOO_LARGE;
+        masks[l].assign((size_t)N, l == 0 ? amr::kIn : 0);
+    }
+    int off = 0;
+    for (int l = 1; l < nlev; ++l) {
+        if (nboxes[l] < 1) return MAC_ERR_INVALID;
+        for (int b = 0; b < nboxes[l]; ++b, ++off) {
+            int lo[3], hi[3];
+            for (int d = 0; d < 3; ++d) {
+                lo[d] = box_lo[3 * off + d];
+                hi[d] = box_hi[3 * off + d];
+                if (d >= dm) {
+                    if (lo[d] != 0 || hi[d] != 0) return MAC_ERR_INVALID;
+                    continue;
+                }
+                if (lo[d] < 0 || hi[d] >= n_out[l][d] || hi[d] < lo[d]) return MAC_ERR_INVALID;
+                if ((lo[d] & 1) || !(hi[d] & 1)) return MAC_ERR_INVALID;
+            }
+            for (int d = 0; d < 3; ++d) boxes[l].push_back(lo[d]);
+            for (int d = 0; d < 3; ++d) boxes[l].push_back(hi[d]);
+            for (int k = lo[2]; k <= hi[2]; ++k)
+                for (int j = lo[1]; j <= hi[1]; ++j)
+                    for (int i = lo[0]; i <= hi[0]; ++i)
+                        masks[l][(size_t)i + (size_t)n_out[l][0] * (j + (size_t)n_out[l][1] * k)] = amr::kIn;
+        }
+    }
+    auto wrapq = [&](int l, int d, int q) {
+        const int n = n_out[l][d];
+        const bool per = c->bc_lo[d] == MAC_BC_PER;
+        if (q < 0) return per ? q + n : -1;
+        if (q >= n) return per ? q - n : -1;
+        return q;
+    };
+    for (int l = 1; l < nlev; ++l) {
+        const int* nf = n_out[l];
+        const int* nc = n_out[l - 1];
+        for (int k = 0; k < nf[2]; ++k)
+            for (int j = 0; j < nf[1]; ++j)
+                for (int i = 0; i < nf[0]; ++i) {
+                    if (!(masks[l][(size_t)i + (size_t)nf[0] * (j + (size_t)nf[1] * k)] & amr::kIn))
+                        continue;
+                    const int cc[3] = {dm > 0 ? i >> 1 : i, dm > 1 ? j >> 1 : j, dm > 2 ? k >> 1 : k};
+                    masks[l - 1][(size_t)cc[0] + (size_t)nc[0] * (cc[1] + (size_t)nc[1] * cc[2])] |= amr::kCov;
+                    for (int a2 = -(dm > 2); a2 <= (dm > 2); ++a2)
+                        for (int a1 = -(dm > 1); a1 <= (dm > 1); ++a1)
+                            for (int a0 = -1; a0 <= 1; ++a0) {
+                                const int q0 = wrapq(l - 1, 0, cc[0] + a0);
+                                const int q1 = wrapq(l - 1, 1, cc[1] + a1);
+                                const int q2 = wrapq(l - 1, 2, cc[2] + a2);
+                                if (q0 < 0 || q1 < 0 || q2 < 0) continue;
+                                if (!(masks[l - 1][(size_t)q0 + (size_t)nc[0] * (q1 + (size_t)nc[1] * q2)] & amr::kIn))
+                                    return MAC_ERR_INVALID;
+                            }
+                }
+    }
+    return MAC_OK;
+}
+
+// The executor of amr_solve / amr_project on the context's stream.
+struct GpuExec {
+    mac_ctx* c;
+    AmrState* A;
+    int nlev;
+    Geo geo;
+    bool singular;
+    int err = MAC_OK;
+    // this call's inputs (device pointers, level-domain arrays)
+    double* const* u = nullptr;            // [3 l + d]
+    const double* const* rho = nullptr;
+    const double* const* macrhs = nullptr;
+    const double* const* b0 = nullptr;
+    const double* const* b0e = nullptr;
+    int alt = 0;
+
+    Lev lev(int l) const { return A->L[l].lev; }
+    double* buf(int l, int which) const { return A->L[l].buf[which]; }
+    long ncell(int l) const { return A->L[l].ncell; }
+    int blocks(long n) const { return blocks_for(n, c->sms); }
+    void launched() {
+        ++c->issued;
+        if (!err && cudaPeekAtLastError() != cudaSuccess) {
+            set_last_cuda_error(cudaGetLastError(), "amr kernel launch", __FILE__, __LINE__);
+            err = MAC_ERR_CUDA;
+        }
+    }
+    int error() const { return err; }
+
+    void defect(int l, const double* uu, const double* cu, const double* f, double* r) {
+        const Lev C = l ? lev(l - 1) : lev(l);
+        k_defect<<<blocks(ncell(l)), kThreads, 0, c->stream>>>(geo, lev(l), C, uu, cu, f, r, ncell(l));
+        launched();
+    }
+    void gsrb(int l, double* uu, const double* f, int nu) {
+        for (int s = 0; s < nu; ++s)
+            for (int colour = 0; colour < 2; ++colour) {
+                k_gsrb<<<blocks(ncell(l)), kThreads, 0, c->stream>>>(geo, lev(l), colour, uu, f, ncell(l));
+                launched();
+            }
+    }
+    void reflux(int l, const double* uf, const double* uc, double* res) {
+        k_reflux<<<blocks(ncell(l - 1)), kThreads, 0, c->stream>>>(geo, lev(l), lev(l - 1), uf, uc, res, ncell(l - 1));
+        launched();
+    }
+    void restrict_cov(int l, const double* fine, double* crse) {
+        k_restrict<<<blocks(ncell(l - 1)), kThreads, 0, c->stream>>>(geo, lev(l), lev(l - 1), fine, crse, ncell(l - 1));
+        launched();
+    }
+    void prolong(int l, const double* uc, double* uf) {
+        k_prolong<<<blocks(ncell(l)), kThreads, 0, c->stream>>>(geo, lev(l), lev(l - 1), uc, uf, ncell(l));
+        launched();
+    }
+    void axpy3(int l, double* uu, const double* hold, const double* du) {
+        k_axpy3<<<blocks(ncell(l)), kThreads, 0, c->stream>>>(lev(l), uu, hold, du, ncell(l));
+        launched();
+    }
+    void add_region(int l, double* phi, const double* uu) {
+        k_add_region<<<blocks(ncell(l)), kThreads, 0, c->stream>>>(lev(l), phi, uu, ncell(l));
+        launched();
+    }
+    void zero(int l, double* x) {
+        if (!err && cudaMemsetAsync(x, 0, sizeof(double) * ncell(l), c->stream) != cudaSuccess) {
+            set_last_cuda_error(cudaGetLastError(), "cudaMemsetAsync", __FILE__, __LINE__);
+            err = MAC_ERR_CUDA;
+        }
+    }
+    void copy(int l, double* dst, const double* src) {
+        if (!err && cudaMemcpyAsync(dst, src, sizeof(double) * ncell(l), cudaMemcpyDeviceToDevice,
+                                    c->stream) != cudaSuccess) {
+            set_last_cuda_error(cudaGetLastError(), "cudaMemcpyAsync", __FILE__, __LINE__);
+            err = MAC_ERR_CUDA;
+        }
+    }
+    void swap_bufs(int l, int a, int b) { std::swap(A->L[l].buf[a], A->L[l].buf[b]); }
+
+    // Reduce `which` over the valid cells of every level (level_only >= 0: the region cells of
+    // that level alone) into A->out on the device.
+    void reduce(int which, int level_only, const double* x0 = nullptr) {
+        int nparts = 0;
+        for (int l = 0; l < nlev; ++l) {
+            if (level_only >= 0 && l != level_only) continue;
+            const double* x = (level_only >= 0 && x0) ? x0 : buf(l, which);
+            const Lev L = lev(l);
+            const double vol = L.h[0] * (geo.dm > 1 ? L.h[1] : 1.0) * (geo.dm > 2 ? L.h[2] : 1.0);
+            const int nb = std::min(kReduceBlocks, blocks(ncell(l)));
+            k_reduce<<<nb, kThreads, 0, c->stream>>>(L, x, vol, level_only < 0 ? 1 : 0,
+                                                     A->part + 4 * nparts, ncell(l));
+            launched();
+            nparts += nb;
+        }
+        k_reduce_finish<<<1, kThreads, 0, c->stream>>>(A->part, nparts, A->out);
+        launched();
+    }
+    bool fetch() {
+        if (err) return false;
+        if (cudaMemcpyAsync(A->h_out, A->out, 5 * sizeof(double), cudaMemcpyDeviceToHost,
+                            c->stream) != cudaSuccess ||
+            cudaStreamSynchronize(c->stream) != cudaSuccess) {
+            set_last_cuda_error(cudaGetLastError(), "amr reduction", __FILE__, __LINE__);
+            err = MAC_ERR_CUDA;
+            return false;
+        }
+        return true;
+    }
+    double valid_max(int which) {
+        reduce(which, -1);
+        if (!fetch()) return NAN;
+        return A->h_out[2] > 0.0 ? NAN : A->h_out[1];
+    }
+    double valid_mean(int which) {
+        reduce(which, -1);
+        if (!fetch()) return NAN;
+        return A->h_out[4];
+    }
+    void sub_valid(int which, double m) {
+        // the mean is still in A->out[4] from valid_mean (same stream, nothing in between)
+        (void)m;
+        for (int l = 0; l < nlev; ++l) {
+            k_sub_scalar<<<blocks(ncell(l)), kThreads, 0, c->stream>>>(lev(l), buf(l, which), A->out + 4, 1, ncell(l));
+            launched();
+        }
+    }
+
+    int prepare_level0() {
+        if (err) return err;
+        int rc = set_call_state(c, false);
+        if (!rc) rc = set_otf_mode(c, false);
+        if (!rc) rc = setup_fine_from_faces(c, A->L[0].beta[0], A->L[0].beta[1],
+                                            geo.dm == 3 ? A->L[0].beta[2] : nullptr, nullptr);
+        if (!rc) rc = setup_coarse_levels(c);
+        singular = c->singular;
+        return rc;
+    }
+    // One FP64 V-cycle of the level-0 multigrid on rhs from a zero guess into e (natural layout);
+    // for a singular problem the mean of the right-hand side is removed first and the mean of
+    // the correction after (the constant is in the null space of the composite operator).
+    int level0_correction(const double* rhs, double* e) {
+        if (err) return err;
+        Level& F = c->lev[0];
+        double* r0 = buf(0, amr::kTmp);
+        copy(0, r0, rhs);
+        if (singular) {
+            reduce(0, 0, r0);
+            k_sub_scalar<<<blocks(ncell(0)), kThreads, 0, c->stream>>>(lev(0), r0, A->out + 4, 0, ncell(0));
+            launched();
+        }
+        int rc = natural_to_level0(c, r0, F.a64.f);
+        if (!rc && cudaMemsetAsync(F.a64.phi, 0, sizeof(double) * (size_t)F.d.ncell, c->stream) != cudaSuccess)
+            rc = MAC_ERR_CUDA;
+        if (!rc) rc = level0_fp64_vcycle(c);
+        if (!rc) rc = level0_to_natural(c, F.a64.phi, e);
+        if (!rc && singular) {
+            reduce(0, 0, e);
+            k_sub_scalar<<<blocks(ncell(0)), kThreads, 0, c->stream>>>(lev(0), e, A->out + 4, 0, ncell(0));
+            launched();
+        }
+        if (rc && !err) err = rc;
+        return err;
+    }
+
+    // ---- projection steps ----
+    void scale_b0(int l, bool mult) {
+        if (!b0) return;
+        for (int d = 0; d < geo.dm; ++d) {
+            const long nf = amr::nfaces(lev(l), d);
+            k_scale_b0<<<blocks(nf), kThreads, 0, c->stream>>>(geo, lev(l), d, u[3 * l + d], b0[l], b0e[l], mult ? 1 : 0, nf);
+            launched();
+        }
+    }
+    void edge_restrict(int l) {
+        for (int d = 0; d < geo.dm; ++d) {
+            const long nf = amr::nfaces(lev(l - 1), d);
+            k_edge_restrict<<<blocks(nf), kThreads, 0, c->stream>>>(geo, lev(l), lev(l - 1), d, u[3 * (l - 1) + d], u[3 * l + d], nf);
+            launched();
+        }
+    }
+    void divergence(int l) {
+        k_divergence<<<blocks(ncell(l)), kThreads, 0, c->stream>>>(
+            geo, lev(l), u[3 * l], u[3 * l + 1], geo.dm == 3 ? u[3 * l + 2] : nullptr,
+            macrhs ? macrhs[l] : nullptr, buf(l, amr::kRh), ncell(l));
+        launched();
+    }
+    void coeffs(int l) {
+        for (int d = 0; d < geo.dm; ++d) {
+            const long nf = amr::nfaces(lev(l), d);
+            k_coeff<<<blocks(nf), kThreads, 0, c->stream>>>(geo, lev(l), d, rho[l], b0 ? b0[l] : nullptr,
+                                                            b0 ? b0e[l] : nullptr, alt, A->L[l].beta[d], nf);
+            launched();
+        }
+    }
+    void correct(int l) {
+        const Lev C = l ? lev(l - 1) : lev(l);
+        const double* cphi = l ? buf(l - 1, amr::kPhi) : nullptr;
+        for (int d = 0; d < geo.dm; ++d) {
+            const long nf = amr::nfaces(lev(l), d);
+            k_correct<<<blocks(nf), kThreads, 0, c->stream>>>(geo, lev(l), C, d, buf(l, amr::kPhi), cphi,
+                                                              A->L[l].beta[d], u[3 * l + d], nf);
+            launched();
+        }
+    }
+};
+
+}  // namespace
+
+int amr_configure(mac_ctx* c, int nlev, const int* nboxes, const int* box_lo, const int* box_hi) {
+    if (nlev < 2 || nlev > amr::kMaxLevels || !nboxes || !box_lo || !box_hi) return MAC_ERR_INVALID;
+    std::vector<std::vector<unsigned char>> masks;
+    std::vector<std::vector<int>> boxes;
+    int n[amr::kMaxLevels][3];
+    int rc = build_masks(c, nlev, nboxes, box_lo, box_hi, masks, boxes, n);
+    if (rc) return rc;
+    amr_release(c);
+    AmrState* A = new AmrState();
+    c->amr = A;
+    A->nlev = nlev;
+    A->boxes = boxes;
+    Geo& G = A->geo;
+    G.dm = c->dm;
+    G.va = c->dm - 1;
+    for (int d = 0; d < 3; ++d) {
+        G.per[d] = c->bc_lo[d] == MAC_BC_PER;
+        G.dlo[d] = c->bc_lo[d] == MAC_BC_DIR;
+        G.dhi[d] = c->bc_hi[d] == MAC_BC_DIR;
+    }
+    A->L.assign(nlev, AmrState::LevelStore());
+    for (int l = 0; l < nlev && !rc; ++l) {
+        AmrState::LevelStore& S = A->L[l];
+        long N = 1;
+        for (int d = 0; d < 3; ++d) {
+            S.lev.n[d] = n[l][d];
+            S.lev.h[d] = d < c->dm ? c->dx[d] / (double)(1 << l) : c->dx[d];
+            N *= n[l][d];
+        }
+        S.ncell = N;
+        rc = amr_alloc(A, &S.mask, (size_t)N);
+        for (int d = 0; d < c->dm && !rc; ++d) rc = amr_alloc(A, &S.beta[d], (size_t)amr::nfaces(S.lev, d));
+        for (int b = 0; b < amr::kNumBufs && !rc; ++b) rc = amr_alloc(A, &S.buf[b], (size_t)N);
+        if (rc) break;
+        if (cudaMemcpy(S.mask, masks[l].data(), (size_t)N, cudaMemcpyHostToDevice) != cudaSuccess) {
+            set_last_cuda_error(cudaGetLastError(), "cudaMemcpy(mask)", __FILE__, __LINE__);
+            rc = MAC_ERR_CUDA;
+            break;
+        }
+        S.lev.mask = S.mask;
+        for (int d = 0; d < 3; ++d) S.lev.b[d] = S.beta[d];
+    }
+    if (!rc) rc = amr_alloc(A, &A->part, (size_t)4 * kReduceBlocks * nlev);
+    if (!rc) rc = amr_alloc(A, &A->out, 16);
+    if (!rc) rc = amr_alloc(A, &A->flag, 1);
+    if (!rc && (cudaMallocHost((void**)&A->h_out, 16 * sizeof(double)) != cudaSuccess ||
+                cudaMallocHost((void**)&A->h_flag, sizeof(int)) != cudaSuccess)) {
+        cudaGetLastError();
+        rc = MAC_ERR_ALLOC;
+    }
+    if (rc) amr_release(c);
+    return rc;
+}
+
+}  // namespace mac
+
+using namespace mac;
+
+extern "C" {
+
+int mac_ctx_set_amr(mac_ctx* c, int nlev, const int* nboxes, const int* box_lo, const int* box_hi) {
+    if (!c) return MAC_ERR_INVALID;
+    if (nlev == 1) {
+        amr_release(c);
+        return MAC_OK;
+    }
+    return amr_configure(c, nlev, nboxes, box_lo, box_hi);
+}
+
+int mac_macproject_ml_dense(mac_ctx* c, double* const* umac, double* const* phi,
+                            const double* const* rho, const double* const* macrhs,
+                            const double* const* beta0, const double* const* beta0_edge,
+                            mac_stats* stats) {
+    mac_stats local;
+    mac_stats* st = stats ? stats : &local;
+    std::memset(st, 0, sizeof(*st));
+    if (!c || !c->amr || !umac || !phi || !rho) return st->status = MAC_ERR_INVALID;
+    if ((beta0 == nullptr) != (beta0_edge == nullptr)) return st->status = MAC_ERR_INVALID;
+    AmrState* A = c->amr;
+    const int nl = A->nlev;
+    for (int l = 0; l < nl; ++l) {
+        if (!phi[l] || !rho[l]) return st->status = MAC_ERR_INVALID;
+        for (int d = 0; d < c->dm; ++d)
+            if (!umac[3 * l + d]) return st->status = MAC_ERR_INVALID;
+        if (beta0 && (!beta0[l] || !beta0_edge[l])) return st->status = MAC_ERR_INVALID;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    begin_call_stats(c, st);
+    GpuExec ex{c, A, nl, A->geo, c->geom_singular};
+    ex.u = umac;
+    ex.rho = rho;
+    ex.macrhs = macrhs;
+    ex.b0 = beta0;
+    ex.b0e = beta0_edge;
+    ex.alt = c->o.use_alt_energy_fix;
+    // phi of this call stands in for the solution buffers
+    double* saved_phi[amr::kMaxLevels];
+    for (int l = 0; l < nl; ++l) {
+        saved_phi[l] = A->L[l].buf[amr::kPhi];
+        A->L[l].buf[amr::kPhi] = phi[l];
+    }
+    int rc = MAC_OK;
+    // densities a level's faces read must be positive and finite
+    if (cudaMemsetAsync(A->flag, 0, sizeof(int), c->stream) != cudaSuccess) rc = MAC_ERR_CUDA;
+    for (int l = 0; l < nl && !rc; ++l) {
+        k_check_rho<<<blocks_for(A->L[l].ncell, c->sms), kThreads, 0, c->stream>>>(
+            A->geo, A->L[l].lev, rho[l], A->flag, A->L[l].ncell);
+        ex.launched();
+    }
+    if (!rc && (cudaMemcpyAsync(A->h_flag, A->flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+                cudaStreamSynchronize(c->stream) != cudaSuccess)) {
+        set_last_cuda_error(cudaGetLastError(), "density check", __FILE__, __LINE__);
+        rc = MAC_ERR_CUDA;
+    }
+    if (!rc && ex.err) rc = ex.err;
+    if (!rc && *A->h_flag) rc = MAC_ERR_BAD_DENSITY;
+    // MAESTRO's tolerance for nlevs levels: min(eps_mac * 10^(nlevs-1), eps_mac_max)
+    // (Source/macproject.f90:217), with the context's rel_eps as eps_mac
+    double rel = c->o.rel_eps;
+    if (rel < 1e-8) rel = std::min(rel * std::pow(10.0, nl - 1), 1e-8);
+    amr::SolveStats S{};
+    cudaEventRecord(c->ev[0], c->stream);
+    if (!rc) {
+        rc = amr::amr_project(ex, rel, c->o.abs_eps, c->o.max_vcycles, c->o.nu1, c->o.nu2, &S);
+        if (rc == 1) rc = MAC_ERR_NOT_CONVERGED;
+        if (rc == -1 && S.status == -1) rc = MAC_ERR_NONFINITE;
+        if (rc == MAC_OK && std::isnan(S.rel_resid)) rc = MAC_ERR_NONFINITE;
+    }
+    cudaEventRecord(c->ev[2], c->stream);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess && !rc) {
+        set_last_cuda_error(cudaGetLastError(), "cudaStreamSynchronize", __FILE__, __LINE__);
+        rc = MAC_ERR_CUDA;
+    }
+    for (int l = 0; l < nl; ++l) A->L[l].buf[amr::kPhi] = saved_phi[l];
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->ev[0], c->ev[2]) == cudaSuccess) st->solve_ms = ms;
+    cudaGetLastError();
+    st->vcycles = S.cycles;
+    st->fnorm = S.fnorm;
+    st->resid0 = S.resid0;
+    st->rel_resid = S.rel_resid;
+    st->nhist = S.nhist;
+    for (int q = 0; q < S.nhist && q < 64; ++q) st->hist[q] = S.hist[q];
+    st->status = rc;
+    st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    end_call_stats(c, st);
+    report_call(c, "macproject_ml_dense", st);
+    return rc;
+}
+
+}  // extern "C"

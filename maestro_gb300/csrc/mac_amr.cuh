@@ -1,0 +1,531 @@
+// Multi-level (AMR) MAC projection: the composite discretisation cell by cell, and the
+// multi-level cycle and projection steps written once against an executor.
+//
+// MAESTRO's macproject with nlevs > 1 (Source/macproject.f90:51-328) hands FBoxLib's composite
+// solve ml_cc_solve a hierarchy of levels with refinement ratio 2 (Source/mac_multigrid.f90:56).
+// Level l is stored as dense arrays over its whole level domain (n0 << l cells per active
+// direction, natural layout i + n0 (j + n1 k)) with a byte mask: kIn for the cells of the level's
+// boxes, kCov for the cells under the next finer level.  Valid cells (kIn without kCov) carry the
+// composite unknowns; covered cells hold the mean of their children.
+//
+// Composite operator (the form FBoxLib describes in Docs/mg/mg.tex:124-155, stencil_order = 2):
+//   * fine arms beta_f (u_c - u_nb) / h^2; across a coarse-fine face the neighbour is the ghost
+//     u_c / 3 + 2/3 u_crse, the line through the first fine cell and the coarse value at the
+//     centre of the coarse cell across the face; u_crse is that coarse cell corrected along each
+//     tangential direction by the quadratic through its tangential neighbours at the ghost's
+//     offset +-1/4 (one-sided linear at a non-periodic domain face);
+//   * a valid coarse cell next to a covered one takes, for that face, the mean of the 2^(dm-1)
+//     fine fluxes beta_f (ghost - u_fine) / h_fine instead of its own flux (reflux);
+//   * physical faces: Neumann dropped, periodic wrapped, Dirichlet with the ghost -u_c.
+//
+// The per-cell functions below are plain C++ (host and device); mac_amr.cu launches them as
+// CUDA kernels.  `amr_solve` / `amr_project` sequence a multi-level V-cycle and the projection
+// steps through an executor `E` that owns the level arrays and applies the cell functions over
+// a level (see GpuExec in mac_amr.cu).
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+
+#if defined(__CUDACC__)
+#define AMR_HD __host__ __device__
+#else
+#define AMR_HD
+#endif
+
+namespace mac {
+namespace amr {
+
+constexpr int kMaxLevels = 8;
+constexpr unsigned char kIn = 1;
+constexpr unsigned char kCov = 2;
+
+struct Geo {
+    int dm;
+    int per[3];          // periodic direction
+    int dlo[3], dhi[3];  // Dirichlet (outflow) domain faces
+    int va;              // vertical direction (planar beta0 index): dm - 1
+};
+
+struct Lev {
+    int n[3];                  // level-domain cells (1 along inactive directions)
+    double h[3];
+    const unsigned char* mask; // kIn / kCov per cell
+    const double* b[3];        // face coefficients, natural face layout (n[d] + 1 along d)
+};
+
+AMR_HD inline long cix(const Lev& L, int i, int j, int k) {
+    return (long)i + (long)L.n[0] * ((long)j + (long)L.n[1] * k);
+}
+AMR_HD inline long fix(const Lev& L, int d, int i, int j, int k) {
+    const long m0 = L.n[0] + (d == 0), m1 = L.n[1] + (d == 1);
+    return (long)i + m0 * ((long)j + m1 * k);
+}
+AMR_HD inline long nfaces(const Lev& L, int d) {
+    return (long)(L.n[0] + (d == 0)) * (L.n[1] + (d == 1)) * (L.n[2] + (d == 2));
+}
+AMR_HD inline long ncells(const Lev& L) { return (long)L.n[0] * L.n[1] * L.n[2]; }
+
+// Index q along d wrapped into the level domain; -1 beyond a non-periodic domain face.
+AMR_HD inline int wrap(const Geo& G, const Lev& L, int d, int q) {
+    const int n = L.n[d];
+    if (q < 0) return G.per[d] ? q + n : -1;
+    if (q >= n) return G.per[d] ? q - n : -1;
+    return q;
+}
+AMR_HD inline bool in_region(const Lev& L, long c) { return (L.mask[c] & kIn) != 0; }
+AMR_HD inline bool is_valid(const Lev& L, long c) { return (L.mask[c] & (kIn | kCov)) == kIn; }
+
+AMR_HD inline double face_b(const Lev& L, int d, const int c[3], int s) {
+    int f[3] = {c[0], c[1], c[2]};
+    if (s > 0) f[d] += 1;
+    return L.b[d][fix(L, d, f[0], f[1], f[2])];
+}
+
+// Coarse value (level C, array cu) at the fine ghost cell q seen across a face normal to d.
+AMR_HD inline double coarse_at_ghost(const Geo& G, const Lev& C, const int q[3], int d,
+                                     const double* cu) {
+    int c[3];
+    for (int e = 0; e < 3; ++e) c[e] = e < G.dm ? q[e] >> 1 : q[e];
+    const double v0 = cu[cix(C, c[0], c[1], c[2])];
+    double v = v0;
+    for (int t = 0; t < G.dm; ++t) {
+        if (t == d) continue;
+        const double del = (q[t] & 1) ? 0.25 : -0.25;
+        int m[3] = {c[0], c[1], c[2]}, p[3] = {c[0], c[1], c[2]};
+        m[t] = wrap(G, C, t, c[t] - 1);
+        p[t] = wrap(G, C, t, c[t] + 1);
+        const bool hm = m[t] >= 0, hp = p[t] >= 0;
+        const double vm = hm ? cu[cix(C, m[0], m[1], m[2])] : 0.0;
+        const double vp = hp ? cu[cix(C, p[0], p[1], p[2])] : 0.0;
+        if (hm && hp)
+            v += del * 0.5 * (vp - vm) + 0.5 * del * del * (vp - 2.0 * v0 + vm);
+        else if (hp)
+            v += del * (vp - v0);
+        else if (hm)
+            v += del * (v0 - vm);
+    }
+    return v;
+}
+
+// Diagonal and off-diagonal parts of (L u)_c = diag u_c - off on level L (coarse level C for
+// the coarse-fine ghosts; cu null: zero coarse data).
+AMR_HD inline void cell_op(const Geo& G, const Lev& L, const Lev& C, const int c[3],
+                           const double* u, const double* cu, double& diag, double& off) {
+    diag = 0.0;
+    off = 0.0;
+    for (int d = 0; d < G.dm; ++d) {
+        const double ih2 = 1.0 / (L.h[d] * L.h[d]);
+        for (int s = -1; s <= 1; s += 2) {
+            const double w = face_b(L, d, c, s) * ih2;
+            const int qd = wrap(G, L, d, c[d] + s);
+            if (qd < 0) {
+                if (s < 0 ? G.dlo[d] : G.dhi[d]) diag += 2.0 * w;
+                continue;
+            }
+            int q[3] = {c[0], c[1], c[2]};
+            q[d] = qd;
+            const long qc = cix(L, q[0], q[1], q[2]);
+            if (in_region(L, qc)) {
+                diag += w;
+                off += w * u[qc];
+            } else {
+                diag += (2.0 / 3.0) * w;
+                if (cu) off += (2.0 / 3.0) * w * coarse_at_ghost(G, C, q, d, cu);
+            }
+        }
+    }
+}
+
+AMR_HD inline void cell_coords(const Lev& L, long idx, int c[3]) {
+    c[0] = (int)(idx % L.n[0]);
+    const long r = idx / L.n[0];
+    c[1] = (int)(r % L.n[1]);
+    c[2] = (int)(r / L.n[1]);
+}
+
+// r = f - L u on a region cell, 0 elsewhere.
+AMR_HD inline void defect_cell(const Geo& G, const Lev& L, const Lev& C, long idx,
+                               const double* u, const double* cu, const double* f, double* r) {
+    if (!in_region(L, idx)) {
+        r[idx] = 0.0;
+        return;
+    }
+    int c[3];
+    cell_coords(L, idx, c);
+    double dg, off;
+    cell_op(G, L, C, c, u, cu, dg, off);
+    r[idx] = f[idx] - (dg * u[idx] - off);
+}
+
+// Gauss-Seidel update of a region cell of the given colour, zero coarse data.
+AMR_HD inline void gsrb_cell(const Geo& G, const Lev& L, long idx, int colour, double* u,
+                             const double* f) {
+    int c[3];
+    cell_coords(L, idx, c);
+    if (((c[0] + c[1] + c[2]) & 1) != colour || !in_region(L, idx)) return;
+    double dg, off;
+    cell_op(G, L, L, c, u, nullptr, dg, off);
+    u[idx] = (f[idx] + off) / dg;
+}
+
+// Reflux into a valid coarse cell K (level C) next to cells covered by level F:
+// res += (T_coarse - mean T_fine) / h.  uc null: zero coarse data.
+AMR_HD inline void reflux_cell(const Geo& G, const Lev& F, const Lev& C, long kidx,
+                               const double* uf, const double* uc, double* res) {
+    if (!is_valid(C, kidx)) return;
+    int c[3];
+    cell_coords(C, kidx, c);
+    const int ntan = 1 << (G.dm - 1);
+    double acc = 0.0;
+    for (int d = 0; d < G.dm; ++d) {
+        for (int s = -1; s <= 1; s += 2) {
+            const int w = wrap(G, C, d, c[d] + s);
+            if (w < 0) continue;
+            int Q[3] = {c[0], c[1], c[2]};
+            Q[d] = w;
+            const long qc = cix(C, Q[0], Q[1], Q[2]);
+            if (!(C.mask[qc] & kCov)) continue;
+            const double Tc = uc ? face_b(C, d, c, s) * (uc[kidx] - uc[qc]) / C.h[d] : 0.0;
+            double Tf = 0.0;
+            for (int a = 0; a < (1 << G.dm); ++a) {
+                if ((a >> d) & 1) continue;
+                int fc[3] = {0, 0, 0}, gq[3] = {0, 0, 0};
+                for (int e = 0; e < G.dm; ++e) {
+                    if (e == d) {
+                        fc[e] = s > 0 ? 2 * Q[e] : 2 * Q[e] + 1;
+                        gq[e] = s > 0 ? 2 * c[e] + 1 : 2 * c[e];
+                    } else {
+                        fc[e] = gq[e] = 2 * c[e] + ((a >> e) & 1);
+                    }
+                }
+                const double ufv = uf[cix(F, fc[0], fc[1], fc[2])];
+                const double g = ufv / 3.0 + (uc ? (2.0 / 3.0) * coarse_at_ghost(G, C, gq, d, uc) : 0.0);
+                Tf += face_b(F, d, fc, -s) * (g - ufv) / F.h[d];
+            }
+            acc += (Tc - Tf / ntan) / C.h[d];
+        }
+    }
+    res[kidx] += acc;
+}
+
+// Covered coarse cell K (level C) = mean of its children (level F).
+AMR_HD inline void restrict_cell(const Geo& G, const Lev& F, const Lev& C, long kidx,
+                                 const double* fine, double* crse) {
+    if (!(C.mask[kidx] & kCov)) return;
+    int c[3];
+    cell_coords(C, kidx, c);
+    const int r0 = G.dm > 0 ? 2 : 1, r1 = G.dm > 1 ? 2 : 1, r2 = G.dm > 2 ? 2 : 1;
+    double s = 0.0;
+    for (int c2 = 0; c2 < r2; ++c2)
+        for (int c1 = 0; c1 < r1; ++c1)
+            for (int c0 = 0; c0 < r0; ++c0)
+                s += fine[cix(F, c[0] * r0 + c0, c[1] * r1 + c1, c[2] * r2 + c2)];
+    crse[kidx] = s / (r0 * r1 * r2);
+}
+
+// uf = multilinear interpolation (3/4, 1/4 per direction) of uc on a region cell of level F,
+// 0 elsewhere; physical faces reflect (Dirichlet odd, others even).
+AMR_HD inline void prolong_cell(const Geo& G, const Lev& F, const Lev& C, long idx,
+                                const double* uc, double* uf) {
+    if (!in_region(F, idx)) {
+        uf[idx] = 0.0;
+        return;
+    }
+    int fi[3];
+    cell_coords(F, idx, fi);
+    int pc[3], off[3];
+    for (int d = 0; d < 3; ++d) {
+        const bool act = d < G.dm;
+        pc[d] = act ? fi[d] >> 1 : fi[d];
+        off[d] = act ? ((fi[d] & 1) ? 1 : -1) : 0;
+    }
+    double s = 0.0;
+    for (int a2 = 0; a2 < (off[2] ? 2 : 1); ++a2)
+        for (int a1 = 0; a1 < (off[1] ? 2 : 1); ++a1)
+            for (int a0 = 0; a0 < (off[0] ? 2 : 1); ++a0) {
+                const int a[3] = {a0, a1, a2};
+                double w = 1.0, sgn = 1.0;
+                int q[3];
+                for (int d = 0; d < 3; ++d) {
+                    if (!off[d]) {
+                        q[d] = pc[d];
+                        continue;
+                    }
+                    w *= a[d] ? 0.25 : 0.75;
+                    const int want = pc[d] + (a[d] ? off[d] : 0);
+                    const int got = wrap(G, C, d, want);
+                    if (got >= 0) {
+                        q[d] = got;
+                    } else {
+                        q[d] = pc[d];
+                        if (want < 0 ? G.dlo[d] : G.dhi[d]) sgn = -sgn;
+                    }
+                }
+                s += w * sgn * uc[cix(C, q[0], q[1], q[2])];
+            }
+    uf[idx] = s;
+}
+
+// Whether the face (d, f) of level L borders a cell of its region.
+AMR_HD inline bool face_in_level(const Geo& G, const Lev& L, int d, const int f[3]) {
+    int lo[3] = {f[0], f[1], f[2]}, hi[3] = {f[0], f[1], f[2]};
+    lo[d] = wrap(G, L, d, f[d] - 1);
+    hi[d] = wrap(G, L, d, f[d]);
+    return (lo[d] >= 0 && in_region(L, cix(L, lo[0], lo[1], lo[2]))) ||
+           (hi[d] >= 0 && in_region(L, cix(L, hi[0], hi[1], hi[2])));
+}
+
+AMR_HD inline void face_coords(const Lev& L, int d, long idx, int f[3]) {
+    const int m0 = L.n[0] + (d == 0), m1 = L.n[1] + (d == 1);
+    f[0] = (int)(idx % m0);
+    const long r = idx / m0;
+    f[1] = (int)(r % m1);
+    f[2] = (int)(r / m1);
+}
+
+// ml_edge_restriction of one coarse face (direction d): the mean of the fine faces tiling it,
+// where the fine level has them.
+AMR_HD inline void edge_restrict_face(const Geo& G, const Lev& F, const Lev& C, int d, long idx,
+                                      double* uc, const double* uf) {
+    int cf[3];
+    face_coords(C, d, idx, cf);
+    int f0[3];
+    for (int e = 0; e < 3; ++e) f0[e] = e < G.dm ? 2 * cf[e] : cf[e];
+    if (!face_in_level(G, F, d, f0)) return;
+    double s = 0.0;
+    int cnt = 0;
+    for (int a = 0; a < (1 << G.dm); ++a) {
+        if ((a >> d) & 1) continue;
+        int f[3] = {f0[0], f0[1], f0[2]};
+        for (int e = 0; e < G.dm; ++e)
+            if (e != d) f[e] += (a >> e) & 1;
+        s += uf[fix(F, d, f[0], f[1], f[2])];
+        ++cnt;
+    }
+    uc[idx] = s / cnt;
+}
+
+// Planar beta0 of the face (d, f): beta0_edge along the vertical, beta0 otherwise.
+AMR_HD inline double beta0_of_face(const Geo& G, int d, const int f[3], const double* b0,
+                                   const double* b0e) {
+    const int r = f[G.va];
+    return d == G.va ? b0e[r] : b0[r];
+}
+
+// rh = -(div(beta0 U) - macrhs) on a region cell (U already holds beta0 U), 0 elsewhere.
+AMR_HD inline void divergence_cell(const Geo& G, const Lev& L, long idx, const double* u0,
+                                   const double* u1, const double* u2, const double* macrhs,
+                                   double* rh) {
+    if (!in_region(L, idx)) {
+        rh[idx] = 0.0;
+        return;
+    }
+    int c[3];
+    cell_coords(L, idx, c);
+    const double* u[3] = {u0, u1, u2};
+    double dv = 0.0;
+    for (int d = 0; d < G.dm; ++d) {
+        int hi[3] = {c[0], c[1], c[2]};
+        hi[d] += 1;
+        dv += (u[d][fix(L, d, hi[0], hi[1], hi[2])] - u[d][fix(L, d, c[0], c[1], c[2])]) / L.h[d];
+    }
+    if (macrhs) dv -= macrhs[idx];
+    rh[idx] = -dv;
+}
+
+// Solver coefficient of a face of the level: beta0^p * 2 / (rho_L + rho_R) (mk_mac_coeffs, the
+// ghost density the periodic image or the boundary cell); faces off the level are left alone.
+AMR_HD inline void coeff_face(const Geo& G, const Lev& L, int d, long idx, const double* rho,
+                              const double* b0, const double* b0e, int alt_energy_fix,
+                              double* beta) {
+    int f[3];
+    face_coords(L, d, idx, f);
+    if (!face_in_level(G, L, d, f)) return;
+    int lo[3] = {f[0], f[1], f[2]}, hi[3] = {f[0], f[1], f[2]};
+    const int n = L.n[d];
+    lo[d] = f[d] - 1;
+    if (lo[d] < 0) lo[d] = G.per[d] ? n - 1 : 0;
+    if (hi[d] >= n) hi[d] = G.per[d] ? 0 : n - 1;
+    double v = 2.0 / (rho[cix(L, hi[0], hi[1], hi[2])] + rho[cix(L, lo[0], lo[1], lo[2])]);
+    if (b0) {
+        const double bb = beta0_of_face(G, d, f, b0, b0e);
+        v *= bb;
+        if (alt_energy_fix) v *= bb;
+    }
+    beta[idx] = v;
+}
+
+// mkumac on a face of the level: beta0 U -= beta_f * G phi; coarse-fine faces use the composite
+// ghost (coarse phi cphi of level C), physical faces as on one level.
+AMR_HD inline void correct_face(const Geo& G, const Lev& L, const Lev& C, int d, long idx,
+                                const double* phi, const double* cphi, const double* beta,
+                                double* u) {
+    int f[3];
+    face_coords(L, d, idx, f);
+    if (!face_in_level(G, L, d, f)) return;
+    int lo[3] = {f[0], f[1], f[2]}, hi[3] = {f[0], f[1], f[2]};
+    lo[d] = wrap(G, L, d, f[d] - 1);
+    hi[d] = wrap(G, L, d, f[d]);
+    const bool lin = lo[d] >= 0 && in_region(L, cix(L, lo[0], lo[1], lo[2]));
+    const bool hin = hi[d] >= 0 && in_region(L, cix(L, hi[0], hi[1], hi[2]));
+    const double h = L.h[d];
+    double g;
+    if (lin && hin) {
+        g = (phi[cix(L, hi[0], hi[1], hi[2])] - phi[cix(L, lo[0], lo[1], lo[2])]) / h;
+    } else if (hin && lo[d] < 0) {
+        g = G.dlo[d] ? 2.0 * phi[cix(L, hi[0], hi[1], hi[2])] / h : 0.0;
+    } else if (lin && hi[d] < 0) {
+        g = G.dhi[d] ? -2.0 * phi[cix(L, lo[0], lo[1], lo[2])] / h : 0.0;
+    } else if (hin) {
+        const double pv = phi[cix(L, hi[0], hi[1], hi[2])];
+        const double gv = pv / 3.0 + (2.0 / 3.0) * coarse_at_ghost(G, C, lo, d, cphi);
+        g = (pv - gv) / h;
+    } else {
+        const double pv = phi[cix(L, lo[0], lo[1], lo[2])];
+        const double gv = pv / 3.0 + (2.0 / 3.0) * coarse_at_ghost(G, C, hi, d, cphi);
+        g = (gv - pv) / h;
+    }
+    u[idx] -= beta[idx] * g;
+}
+
+// ---- the multi-level cycle and the projection steps -------------------------------------------
+//
+// E provides, for levels l = 0 .. nlev-1 (arrays are E's own memory):
+//   int nlev; Geo geo; bool singular; Lev lev(l);
+//   double* buf(l, which)          work arrays: kF, kPhi, kRes, kUu, kHold, kTmp, kDu, kRh
+//   double* beta(l, d)             face coefficients of level l
+//   void defect(l, u, cu, f, r)    r = f - L u (cu: level l-1 data for the C-F ghosts or null)
+//   void gsrb(l, u, f, nu)         nu red/black sweeps, zero coarse data
+//   void reflux(l, uf, uc, res)    into level l-1 from level l
+//   void restrict_cov(l, fine, crse)
+//   void prolong(l, uc, uf)        level l-1 -> level l
+//   void axpy3(l, uu, hold, du)    uu += hold + du on the region
+//   void add_region(l, phi, uu)    phi += uu on the region
+//   void zero(l, x)
+//   double valid_max(which)        max over the valid cells of all levels (host value)
+//   double valid_mean(which)       volume-weighted mean over the valid cells (host value)
+//   void sub_valid(which, m)       x -= m on the valid cells of all levels
+//   int level0_correction(rhs, e)  one V-cycle of the level-0 multigrid, zero guess, constant
+//                                  removed when singular; returns 0 or an error code
+//   int error()                    sticky launch / device error (0: none)
+// and for the projection:
+//   void scale_b0(l, mult)  edge_restrict(l)  divergence(l)  coeffs(l)  correct(l)
+enum { kF = 0, kPhi, kRes, kUu, kHold, kTmp, kDu, kRh, kNumBufs };
+
+struct SolveStats {
+    int status;      // 0 converged, 1 not converged, < 0 error
+    int cycles;
+    double fnorm;
+    double resid0;
+    double rel_resid;
+    int nhist;
+    double hist[64];
+};
+
+template <class E>
+double composite_residual(E& ex) {
+    const int nl = ex.nlev;
+    for (int l = 0; l < nl; ++l)
+        ex.defect(l, ex.buf(l, kPhi), l ? ex.buf(l - 1, kPhi) : nullptr, ex.buf(l, kF),
+                  ex.buf(l, kRes));
+    for (int l = nl - 1; l >= 1; --l) {
+        ex.reflux(l, ex.buf(l, kPhi), ex.buf(l - 1, kPhi), ex.buf(l - 1, kRes));
+        ex.restrict_cov(l, ex.buf(l, kRes), ex.buf(l - 1, kRes));
+    }
+    return ex.valid_max(kRes);
+}
+
+template <class E>
+int ml_vcycle(E& ex, int nu1, int nu2) {
+    const int nl = ex.nlev;
+    for (int l = nl - 1; l >= 1; --l) {
+        ex.zero(l, ex.buf(l, kUu));
+        ex.gsrb(l, ex.buf(l, kUu), ex.buf(l, kRes), nu1);
+        ex.defect(l, ex.buf(l, kUu), nullptr, ex.buf(l, kRes), ex.buf(l, kTmp));
+        ex.swap_bufs(l, kRes, kTmp);
+        ex.copy(l, ex.buf(l, kHold), ex.buf(l, kUu));
+        ex.restrict_cov(l, ex.buf(l, kRes), ex.buf(l - 1, kRes));
+        ex.reflux(l, ex.buf(l, kUu), nullptr, ex.buf(l - 1, kRes));
+    }
+    int rc = ex.level0_correction(ex.buf(0, kRes), ex.buf(0, kUu));
+    if (rc) return rc;
+    for (int l = 1; l < nl; ++l) {
+        ex.prolong(l, ex.buf(l - 1, kUu), ex.buf(l, kUu));
+        ex.defect(l, ex.buf(l, kUu), ex.buf(l - 1, kUu), ex.buf(l, kRes), ex.buf(l, kTmp));
+        ex.zero(l, ex.buf(l, kDu));
+        ex.gsrb(l, ex.buf(l, kDu), ex.buf(l, kTmp), nu2);
+        ex.axpy3(l, ex.buf(l, kUu), ex.buf(l, kHold), ex.buf(l, kDu));
+    }
+    for (int l = 0; l < nl; ++l) ex.add_region(l, ex.buf(l, kPhi), ex.buf(l, kUu));
+    for (int l = nl - 1; l >= 1; --l) ex.restrict_cov(l, ex.buf(l, kPhi), ex.buf(l - 1, kPhi));
+    return ex.error();
+}
+
+// Composite solve of L phi = f with f in buf(l, kF) and the initial guess in buf(l, kPhi) (only
+// region cells are read).  rel_eps / abs_eps (<= 0: unused) as in mac_opts.
+template <class E>
+int amr_solve(E& ex, double rel_eps, double abs_eps, int max_cycles, int nu1, int nu2,
+              SolveStats* S) {
+    const int nl = ex.nlev;
+    *S = SolveStats{};
+    if (ex.singular) ex.sub_valid(kF, ex.valid_mean(kF));
+    for (int l = nl - 1; l >= 1; --l) ex.restrict_cov(l, ex.buf(l, kPhi), ex.buf(l - 1, kPhi));
+    const double fnorm = ex.valid_max(kF);
+    S->fnorm = fnorm;
+    if (!(fnorm > 0.0)) {
+        for (int l = 0; l < nl; ++l) ex.zero(l, ex.buf(l, kPhi));
+        S->status = std::isnan(fnorm) ? -1 : 0;
+        return ex.error() ? ex.error() : S->status;
+    }
+    auto converged = [&](double r) {
+        return r <= rel_eps * fnorm || (abs_eps > 0.0 && r <= abs_eps);
+    };
+    double res = composite_residual(ex);
+    S->resid0 = res;
+    int it = 0;
+    while (!converged(res) && it < max_cycles && !std::isnan(res)) {
+        int rc = ml_vcycle(ex, nu1, nu2);
+        if (rc) {
+            S->status = rc;
+            return rc;
+        }
+        ++it;
+        res = composite_residual(ex);
+        if (S->nhist < 64) S->hist[S->nhist++] = res / fnorm;
+    }
+    S->cycles = it;
+    S->rel_resid = res / fnorm;
+    S->status = converged(res) ? 0 : 1;
+    return ex.error() ? ex.error() : S->status;
+}
+
+// Multi-level MAC projection (Source/macproject.f90:51-328, nlevs > 1) on the executor's level
+// arrays: velocities, density, macrhs and beta0 already loaded; phi in buf(l, kPhi).
+template <class E>
+int amr_project(E& ex, double rel_eps, double abs_eps, int max_cycles, int nu1, int nu2,
+                SolveStats* S) {
+    const int nl = ex.nlev;
+    for (int l = 0; l < nl; ++l) ex.scale_b0(l, true);
+    for (int l = nl - 1; l >= 1; --l) ex.edge_restrict(l);
+    for (int l = 0; l < nl; ++l) ex.divergence(l);          // buf(l, kRh)
+    for (int l = nl - 1; l >= 1; --l) ex.restrict_cov(l, ex.buf(l, kRh), ex.buf(l - 1, kRh));
+    for (int l = 0; l < nl; ++l) {
+        ex.coeffs(l);
+        ex.copy(l, ex.buf(l, kF), ex.buf(l, kRh));
+    }
+    int rc = ex.prepare_level0();
+    if (rc) return rc;
+    rc = amr_solve(ex, rel_eps, abs_eps, max_cycles, nu1, nu2, S);
+    if (rc < 0) return rc;
+    const int status = rc;
+    for (int l = 0; l < nl; ++l) ex.correct(l);
+    for (int l = nl - 1; l >= 1; --l) ex.edge_restrict(l);
+    for (int l = 0; l < nl; ++l) ex.scale_b0(l, false);
+    for (int l = nl - 1; l >= 1; --l) ex.edge_restrict(l);
+    rc = ex.error();
+    return rc ? rc : status;
+}
+
+}  // namespace amr
+}  // namespace mac

@@ -225,6 +225,8 @@ struct KrylovBufs {
     unsigned* count = nullptr;
 };
 
+struct AmrState;   // multi-level (AMR) hierarchy of a context (mac_amr.cu)
+
 }  // namespace mac
 
 constexpr int kInnerGraphs = 8;   // mixed-precision steps of up to 8 inner V-cycles are graphed
@@ -304,6 +306,8 @@ struct mac_ctx {
     size_t tail_smem[2] = {0, 0};
     double ktime_ms[8] = {};
     int ktime_launches[8] = {};
+
+    mac::AmrState* amr = nullptr;                 // finer AMR levels (mac_ctx_set_amr); null: one level
 
     size_t bytes_allocated = 0;
     std::vector<void*> allocations;
@@ -450,6 +454,13 @@ int scatter_faces(mac_ctx* c, int ptr_kind, double* const* fabs, int ng, int dir
 
 // ---- solver (mac_solver.cu) -----------------------------------------------------------------
 int run_solve(mac_ctx* c, mac_stats* st);
+// One FP64 V-cycle of the level-0 multigrid on (lev[0].a64.phi, lev[0].a64.f), in place.
+int level0_fp64_vcycle(mac_ctx* c);
+
+// ---- multi-level hierarchy (mac_amr.cu) -------------------------------------------------------
+// Validate and store the finer levels' boxes (levels 1 .. nlev-1) and allocate their arrays.
+int amr_configure(mac_ctx* c, int nlev, const int* nboxes, const int* box_lo, const int* box_hi);
+void amr_release(mac_ctx* c);
 // Forward projection on the whole-domain arrays already in c->u / c->rho / c->phin; leaves the
 // level-0 coefficients and phi (level-0 layout) in place.
 int forward_projection(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats* st);

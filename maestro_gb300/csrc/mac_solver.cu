@@ -724,6 +724,7 @@ int ctx_alloc(mac_ctx* c) {
 }
 
 void ctx_free(mac_ctx* c) {
+    amr_release(c);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->xfer) cudaStreamSynchronize(c->xfer);
     if (c->aux) cudaStreamSynchronize(c->aux);
@@ -871,6 +872,11 @@ void report(const mac_ctx* c, const char* what, const mac_stats* st) {
 }  // namespace
 
 namespace mac {
+int level0_fp64_vcycle(mac_ctx* c) {
+    vcycle<double>(c, 0);
+    MAC_CUDA_TRY(cudaGetLastError());
+    return MAC_OK;
+}
 int forward_projection(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats* st) {
     return core_macproject(c, macrhs, have_beta0, st);
 }

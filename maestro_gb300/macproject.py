@@ -283,6 +283,45 @@ class MacProjector:
         self._check(rc, "mac_macproject_cart_dense", st, strict)
         return st.as_dict()
 
+    def set_amr(self, boxes):
+        """Multi-level hierarchy (mac_ctx_set_amr): boxes[l] for l >= 1 is a list of (lo, hi)
+        inclusive corners in level-l cell indices (ratio 2); boxes[0] is ignored (level 0 is
+        this projector's layout).  A list of one level drops the hierarchy."""
+        nlev = len(boxes)
+        dm = self.dm
+        nb = (ctypes.c_int * max(1, nlev))()
+        lo, hi = [], []
+        for l in range(1, nlev):
+            nb[l] = len(boxes[l])
+            for a, b in boxes[l]:
+                lo += list(a) + [0] * (3 - dm)
+                hi += list(b) + [0] * (3 - dm)
+        clo = (ctypes.c_int * max(1, len(lo)))(*lo)
+        chi = (ctypes.c_int * max(1, len(hi)))(*hi)
+        rc = capi.lib().mac_ctx_set_amr(self.ctx, nlev, nb, clo, chi)
+        if rc != 0:
+            raise MacError(rc, "mac_ctx_set_amr")
+        self.amr_levels = nlev
+
+    def macproject_ml_dense(self, umac, phi, rho, macrhs=None, beta0=None, beta0_edge=None,
+                            strict=False):
+        """Multi-level projection on whole-level-domain device arrays (ints: device pointers):
+        umac[l] a list of dm face arrays, phi[l], rho[l], macrhs[l] (or None) cells, beta0[l] /
+        beta0_edge[l] the planar base state of level l."""
+        nlev = len(phi)
+        dm = self.dm
+        v = ctypes.c_void_p
+        U = (v * (3 * nlev))(*[(umac[l][d] if d < dm else 0) for l in range(nlev) for d in range(3)])
+        Ph = (v * nlev)(*phi)
+        R = (v * nlev)(*rho)
+        M = None if macrhs is None else (v * nlev)(*[(m or 0) for m in macrhs])
+        B0 = None if beta0 is None else (v * nlev)(*beta0)
+        B0e = None if beta0_edge is None else (v * nlev)(*beta0_edge)
+        st = capi.MacStats()
+        rc = capi.lib().mac_macproject_ml_dense(self.ctx, U, Ph, R, M, B0, B0e, ctypes.byref(st))
+        self._check(rc, "mac_macproject_ml_dense", st, strict)
+        return st.as_dict()
+
     def adjoint_dense(self, u, rho, macrhs, beta0, beta0_edge, w, du, drinv=None, dbeta0=None,
                       dmacrhs=None, phi_out=None, strict=True):
         """Adjoint of the whole-domain projection on device pointers (see maestro_mac.h)."""

@@ -1,0 +1,253 @@
+// Host execution of the library's multi-level MAC projection (TEST INFRASTRUCTURE ONLY).
+//
+// Runs the per-cell functions and the amr_solve / amr_project sequencing of
+// maestro_gb300/csrc/mac_amr.cuh -- the code the CUDA kernels of mac_amr.cu launch -- with plain
+// loops over the cells and faces of each level, so the library's composite arithmetic and cycle
+// order can be checked against the oracle without a GPU.  The level-0 coarse correction (the
+// library's own one-level FP64 V-cycle on the device) is stood in for by one V-cycle of the
+// oracle's one-level multigrid; it only sets the convergence rate, not the converged answer.
+//
+// Built by tests/test_amr_host_exec.py with g++ (no CUDA involved).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "mac_amr.cuh"
+#include "mac_oracle_core.h"
+
+using namespace mac;
+
+namespace {
+
+struct HostExec {
+    int nlev = 0;
+    amr::Geo geo{};
+    bool singular = false;
+    int err = 0;
+    std::vector<amr::Lev> L;
+    std::vector<std::vector<unsigned char>> mask;
+    std::vector<std::vector<double>> store[amr::kNumBufs];
+    std::vector<double*> bufp[amr::kNumBufs];
+    std::vector<std::vector<double>> beta[3];
+    orc::Ctx base;
+    orc_opts o{};
+    double out_mean = 0.0;
+    // this call's inputs
+    double* const* u = nullptr;
+    const double* const* rho = nullptr;
+    const double* const* macrhs = nullptr;
+    const double* const* b0 = nullptr;
+    const double* const* b0e = nullptr;
+    int alt = 0;
+
+    amr::Lev lev(int l) const { return L[l]; }
+    double* buf(int l, int which) const { return bufp[which][l]; }
+    long ncell(int l) const { return amr::ncells(L[l]); }
+    int error() const { return err; }
+
+    void defect(int l, const double* uu, const double* cu, const double* f, double* r) {
+        const amr::Lev C = l ? L[l - 1] : L[l];
+        for (long i = 0; i < ncell(l); ++i) amr::defect_cell(geo, L[l], C, i, uu, cu, f, r);
+    }
+    void gsrb(int l, double* uu, const double* f, int nu) {
+        for (int s = 0; s < nu; ++s)
+            for (int colour = 0; colour < 2; ++colour)
+                for (long i = 0; i < ncell(l); ++i) amr::gsrb_cell(geo, L[l], i, colour, uu, f);
+    }
+    void reflux(int l, const double* uf, const double* uc, double* res) {
+        for (long i = 0; i < ncell(l - 1); ++i) amr::reflux_cell(geo, L[l], L[l - 1], i, uf, uc, res);
+    }
+    void restrict_cov(int l, const double* fine, double* crse) {
+        for (long i = 0; i < ncell(l - 1); ++i) amr::restrict_cell(geo, L[l], L[l - 1], i, fine, crse);
+    }
+    void prolong(int l, const double* uc, double* uf) {
+        for (long i = 0; i < ncell(l); ++i) amr::prolong_cell(geo, L[l], L[l - 1], i, uc, uf);
+    }
+    void axpy3(int l, double* uu, const double* hold, const double* du) {
+        for (long i = 0; i < ncell(l); ++i)
+            if (amr::in_region(L[l], i)) uu[i] += hold[i] + du[i];
+    }
+    void add_region(int l, double* phi, const double* uu) {
+        for (long i = 0; i < ncell(l); ++i)
+            if (amr::in_region(L[l], i)) phi[i] += uu[i];
+    }
+    void zero(int l, double* x) { std::fill(x, x + ncell(l), 0.0); }
+    void copy(int l, double* dst, const double* src) { std::copy(src, src + ncell(l), dst); }
+    void swap_bufs(int l, int a, int b) { std::swap(bufp[a][l], bufp[b][l]); }
+
+    double vol(int l) const {
+        return L[l].h[0] * (geo.dm > 1 ? L[l].h[1] : 1.0) * (geo.dm > 2 ? L[l].h[2] : 1.0);
+    }
+    double valid_max(int which) {
+        double mx = 0.0;
+        bool nan = false;
+        for (int l = 0; l < nlev; ++l)
+            for (long i = 0; i < ncell(l); ++i)
+                if (amr::is_valid(L[l], i)) {
+                    const double a = buf(l, which)[i];
+                    nan = nan || a != a;
+                    mx = std::max(mx, std::fabs(a));
+                }
+        return nan ? NAN : mx;
+    }
+    double valid_mean(int which) {
+        double s = 0.0, v = 0.0;
+        for (int l = 0; l < nlev; ++l)
+            for (long i = 0; i < ncell(l); ++i)
+                if (amr::is_valid(L[l], i)) {
+                    s += vol(l) * buf(l, which)[i];
+                    v += vol(l);
+                }
+        return s / v;
+    }
+    void sub_valid(int which, double m) {
+        for (int l = 0; l < nlev; ++l)
+            for (long i = 0; i < ncell(l); ++i)
+                if (amr::is_valid(L[l], i)) buf(l, which)[i] -= m;
+    }
+    int prepare_level0() {
+        const double* b[3] = {beta[0][0].data(), beta[1][0].data(),
+                              geo.dm == 3 ? beta[2][0].data() : nullptr};
+        base = orc::Ctx();
+        base.o = o;
+        orc::build_hierarchy(base, b, nullptr);
+        singular = base.singular;
+        return 0;
+    }
+    int level0_correction(const double* rhs, double* e) {
+        orc::Level& B = base.lev[0];
+        B.f.assign(rhs, rhs + ncell(0));
+        if (singular) orc::sub_mean(B.f);
+        B.phi.assign(B.f.size(), 0.0);
+        orc::vcycle(base, 0);
+        if (singular) orc::sub_mean(B.phi);
+        std::copy(B.phi.begin(), B.phi.end(), e);
+        return 0;
+    }
+    void scale_b0(int l, bool mult) {
+        if (!b0) return;
+        for (int d = 0; d < geo.dm; ++d) {
+            double* x = u[3 * l + d];
+            for (long i = 0; i < amr::nfaces(L[l], d); ++i) {
+                int f[3];
+                amr::face_coords(L[l], d, i, f);
+                const double bb = amr::beta0_of_face(geo, d, f, b0[l], b0e[l]);
+                x[i] = mult ? x[i] * bb : x[i] / bb;
+            }
+        }
+    }
+    void edge_restrict(int l) {
+        for (int d = 0; d < geo.dm; ++d)
+            for (long i = 0; i < amr::nfaces(L[l - 1], d); ++i)
+                amr::edge_restrict_face(geo, L[l], L[l - 1], d, i, u[3 * (l - 1) + d], u[3 * l + d]);
+    }
+    void divergence(int l) {
+        for (long i = 0; i < ncell(l); ++i)
+            amr::divergence_cell(geo, L[l], i, u[3 * l], u[3 * l + 1],
+                                 geo.dm == 3 ? u[3 * l + 2] : nullptr,
+                                 macrhs ? macrhs[l] : nullptr, buf(l, amr::kRh));
+    }
+    void coeffs(int l) {
+        for (int d = 0; d < geo.dm; ++d)
+            for (long i = 0; i < amr::nfaces(L[l], d); ++i)
+                amr::coeff_face(geo, L[l], d, i, rho[l], b0 ? b0[l] : nullptr,
+                                b0 ? b0e[l] : nullptr, alt, beta[d][l].data());
+    }
+    void correct(int l) {
+        const amr::Lev C = l ? L[l - 1] : L[l];
+        const double* cphi = l ? buf(l - 1, amr::kPhi) : nullptr;
+        for (int d = 0; d < geo.dm; ++d)
+            for (long i = 0; i < amr::nfaces(L[l], d); ++i)
+                amr::correct_face(geo, L[l], C, d, i, buf(l, amr::kPhi), cphi, beta[d][l].data(),
+                                  u[3 * l + d]);
+    }
+};
+
+// Masks from the boxes (no layout validation here: the oracle's own checks cover it).
+void build(HostExec& E, const orc_opts* o, int nlev, const int* nboxes, const int* boxes) {
+    E.o = *o;
+    E.nlev = nlev;
+    E.geo.dm = o->dm;
+    E.geo.va = o->dm - 1;
+    for (int d = 0; d < 3; ++d) {
+        E.geo.per[d] = o->bc_lo[d] == ORC_BC_PER;
+        E.geo.dlo[d] = o->bc_lo[d] == ORC_BC_DIR;
+        E.geo.dhi[d] = o->bc_hi[d] == ORC_BC_DIR;
+    }
+    E.L.assign(nlev, amr::Lev{});
+    E.mask.assign(nlev, {});
+    for (int b = 0; b < amr::kNumBufs; ++b) {
+        E.store[b].assign(nlev, {});
+        E.bufp[b].assign(nlev, nullptr);
+    }
+    for (int d = 0; d < 3; ++d) E.beta[d].assign(nlev, {});
+    for (int l = 0; l < nlev; ++l) {
+        amr::Lev& V = E.L[l];
+        for (int d = 0; d < 3; ++d) {
+            V.n[d] = d < o->dm ? (o->n[d] << l) : 1;
+            V.h[d] = d < o->dm ? o->dx[d] / (double)(1 << l) : o->dx[d];
+        }
+        const long N = amr::ncells(V);
+        E.mask[l].assign((size_t)N, l == 0 ? amr::kIn : 0);
+        for (int b = 0; b < amr::kNumBufs; ++b) {
+            E.store[b][l].assign((size_t)N, 0.0);
+            E.bufp[b][l] = E.store[b][l].data();
+        }
+        for (int d = 0; d < o->dm; ++d) E.beta[d][l].assign((size_t)amr::nfaces(V, d), 0.0);
+    }
+    const int* bx = boxes;
+    for (int l = 1; l < nlev; ++l)
+        for (int b = 0; b < nboxes[l]; ++b, bx += 6)
+            for (int k = bx[2]; k <= bx[5]; ++k)
+                for (int j = bx[1]; j <= bx[4]; ++j)
+                    for (int i = bx[0]; i <= bx[3]; ++i)
+                        E.mask[l][amr::cix(E.L[l], i, j, k)] = amr::kIn;
+    for (int l = 1; l < nlev; ++l)
+        for (long i = 0; i < amr::ncells(E.L[l]); ++i) {
+            if (!E.mask[l][i]) continue;
+            int c[3];
+            amr::cell_coords(E.L[l], i, c);
+            int p[3];
+            for (int d = 0; d < 3; ++d) p[d] = d < o->dm ? c[d] >> 1 : c[d];
+            E.mask[l - 1][amr::cix(E.L[l - 1], p[0], p[1], p[2])] |= amr::kCov;
+        }
+    for (int l = 0; l < nlev; ++l) {
+        E.L[l].mask = E.mask[l].data();
+        for (int d = 0; d < 3; ++d) E.L[l].b[d] = d < o->dm ? E.beta[d][l].data() : nullptr;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+// The library's multi-level projection run on the host; arguments as orc_macproject_ml
+// (phi[l] in/out, umac[3 l + d] in/out).  Returns the solve status (0 converged).
+int amrh_macproject(const orc_opts* o, int nlev, const int* nboxes, const int* boxes,
+                    double* const* umac, double* const* phi, const double* const* rho,
+                    const double* const* macrhs, const double* const* beta0,
+                    const double* const* beta0_edge, double* stats_out) {
+    HostExec E;
+    build(E, o, nlev, nboxes, boxes);
+    E.u = umac;
+    E.rho = rho;
+    E.macrhs = macrhs;
+    E.b0 = beta0;
+    E.b0e = beta0_edge;
+    E.alt = o->alt_energy_fix;
+    for (int l = 0; l < nlev; ++l) {
+        E.bufp[amr::kPhi][l] = phi[l];
+    }
+    amr::SolveStats S{};
+    const int rc = amr::amr_project(E, o->rel_eps, o->abs_eps, o->max_vcycles, o->nu1, o->nu2, &S);
+    if (stats_out) {
+        stats_out[0] = rc;
+        stats_out[1] = S.cycles;
+        stats_out[2] = S.rel_resid;
+        stats_out[3] = S.fnorm;
+    }
+    return rc;
+}
+
+}  // extern "C"

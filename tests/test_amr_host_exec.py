@@ -1,0 +1,91 @@
+"""The library's multi-level projection code executed on the host (no GPU).
+
+tests/csrc/amr_host.cpp runs the per-cell functions and the amr_project / amr_solve sequencing of
+maestro_gb300/csrc/mac_amr.cuh -- what the CUDA kernels of mac_amr.cu launch -- with loops over
+the cells, so the composite arithmetic and the cycle order are checked against the golden direct
+solves before any GPU runs them."""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle as O
+from maestro_gb300.inputs import AMR_CASES
+from tests.test_oracle_amr import G, load_amr, phi_err, u_err
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def host_lib(tmp_path_factory):
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    out = str(tmp_path_factory.mktemp("amrh") / "libamr_host.so")
+    cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-fopenmp", "-shared",
+           "-I", os.path.join(ROOT, "maestro_gb300", "csrc"), "-I", os.path.join(ROOT, "oracle"),
+           os.path.join(ROOT, "tests", "csrc", "amr_host.cpp"),
+           os.path.join(ROOT, "oracle", "mac_oracle.cpp"), "-o", out]
+    subprocess.run(cmd, check=True, capture_output=True)
+    L = ctypes.CDLL(out)
+    P = ctypes.POINTER
+    pd = P(P(ctypes.c_double))
+    ip = P(ctypes.c_int)
+    L.amrh_macproject.argtypes = [P(O.OrcOpts), ctypes.c_int, ip, ip, pd, pd, pd, pd, pd, pd,
+                                  P(ctypes.c_double)]
+    L.amrh_macproject.restype = ctypes.c_int
+    return L
+
+
+def run_host(L, c, rel_eps):
+    nlev = c["nlev"]
+    dm = c["dm"]
+    phi = [np.zeros_like(p, order="F") for p in c["phi"]]
+    u = [[np.array(x, order="F") for x in c["umac"][l]] for l in range(nlev)]
+    up = []
+    for l in range(nlev):
+        for d in range(3):
+            up.append(u[l][d] if d < dm else None)
+    rho = [np.asfortranarray(r) for r in c["rho"]]
+    mr = [np.asfortranarray(m) for m in c["macrhs"]]
+    b0 = [np.ascontiguousarray(b) for b in c["beta0"]]
+    b0e = [np.ascontiguousarray(b) for b in c["beta0_edge"]]
+    o = O._opts(c["n0"], c["dx0"], c["bc_lo"], c["bc_hi"], O.nlevels_for_boxes([c["n0"]]),
+                rel_eps, -1.0, 200, 2, 2, 10, O.EPS_MAC_BOTTOM, 200, False, 0)
+    nb, bx = O._ml_layout(c["n0"], c["boxes"])
+    st = (ctypes.c_double * 4)()
+    rc = L.amrh_macproject(ctypes.byref(o), nlev, nb.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                           bx.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), O._ptr_array(up),
+                           O._ptr_array(phi), O._ptr_array(rho), O._ptr_array(mr),
+                           O._ptr_array(b0), O._ptr_array(b0e), st)
+    return rc, u, phi, list(st)
+
+
+@pytest.mark.parametrize("name", sorted(AMR_CASES))
+def test_library_amr_code_on_host_matches_golden(host_lib, name):
+    c = load_amr(name)
+    H = G.Hierarchy(c["n0"], c["dx0"], c["bc_lo"], c["bc_hi"], c["boxes"])
+    rc, u, phi, st = run_host(host_lib, c, 1e-12)
+    assert rc == 0 and st[2] <= 1e-12, st
+    assert phi_err(H, phi, c["phi"]) <= 1e-9
+    assert u_err(H, u, c["unew"]) <= 1e-9
+
+
+@pytest.mark.parametrize("name", ["amr2d_3lev", "amr3d_16"])
+def test_library_amr_code_on_host_matches_oracle_at_maestro_tolerance(host_lib, name):
+    c = load_amr(name)
+    H = G.Hierarchy(c["n0"], c["dx0"], c["bc_lo"], c["bc_hi"], c["boxes"])
+    eps = O.ml_rel_eps(c["nlev"])
+    rc, u, phi, st = run_host(host_lib, c, eps)
+    assert rc == 0 and st[2] <= eps
+    uo, po, so = O.macproject_ml(c["umac"], [np.zeros_like(p) for p in c["phi"]], c["rho"],
+                                 c["dx0"], c["bc_lo"], c["bc_hi"], c["boxes"],
+                                 macrhs=c["macrhs"], beta0=c["beta0"],
+                                 beta0_edge=c["beta0_edge"], rel_eps=eps)
+    # same algorithm, same cycle count; only the level-0 correction differs in rounding
+    assert int(st[1]) == so["vcycles"]
+    assert phi_err(H, phi, po) <= 1e-10
+    assert u_err(H, u, uo) <= 1e-10
