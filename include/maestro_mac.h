@@ -275,6 +275,30 @@ int mac_macproject_ml_dense(mac_ctx* ctx, double* const* umac, double* const* ph
                             mac_stats* stats);
 
 /*
+ * Multi-level MAC projection on the caller's boxes, the drop-in for macproject with nlevs > 1
+ * (Source/macproject.f90:51-328).  Arguments as mac_macproject, with the fab lists of all levels
+ * one after the other (level 0 = the context's boxes, then the boxes of mac_ctx_set_amr in
+ * order):
+ *   umac   : per level, dm blocks of that level's nboxes edge fabs (direction-major, as in
+ *            mac_macproject), ng_u ghosts (in/out: the boxes' own faces are written)
+ *   phi    : per level, one cell fab per box, ng_phi ghosts (in: guess; out: the boxes' cells)
+ *   rho    : per level, one state fab per box, rho_ncomp components, ng_rho >= 1 ghosts (the
+ *            coarse-fine faces read the density one cell outside the level)
+ *   macrhs : per level, one cell fab per box, ng_rhs ghosts, or NULL
+ *   beta0 / beta0_edge : the levels' planar base states one after the other (n_l and n_l + 1
+ *            values, n_l = the level's vertical extent), or both NULL
+ * Ghost faces and ghost cells of the fabs are left as they came in (the reference refills them
+ * after the projection with create_umac_grown / multifab_fill_boundary).
+ */
+int mac_macproject_ml(mac_ctx* ctx, int ptr_kind,
+                      double* const* umac, int ng_u,
+                      double* const* phi, int ng_phi,
+                      const double* const* rho, int ng_rho, int rho_ncomp, int rho_comp,
+                      const double* const* macrhs, int ng_rhs,
+                      const double* beta0, const double* beta0_edge,
+                      mac_stats* stats);
+
+/*
  * Adjoint (reverse-mode derivative) of the whole-domain MAC projection; no counterpart in the
  * reference.  Forward map (beta0 form, p = 1 + use_alt_energy_fix):
  *   U_proj = U - c .* G phi,  A phi = f,  A = D diag(beta_f) G  (negated, alpha = 0),

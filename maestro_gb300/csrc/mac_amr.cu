@@ -197,6 +197,22 @@ __global__ void k_check_rho(Geo G, Lev L, const double* rho, int* flag, long N) 
     }
 }
 
+// Caller fabs of one level <-> the level array; blockIdx.y is the fab.
+__global__ void k_fabs_gather(Geo G, Lev L, int dir, const amr::FabDesc* T, int with_ghosts,
+                              double* level) {
+    const amr::FabDesc B = T[blockIdx.y];
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < B.count;
+         e += (long)gridDim.x * blockDim.x)
+        amr::fab_gather_elem(G, L, dir, B, e, with_ghosts, level);
+}
+
+__global__ void k_fabs_scatter(Geo G, Lev L, int dir, const amr::FabDesc* T, const double* level) {
+    const amr::FabDesc B = T[blockIdx.y];
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < B.count;
+         e += (long)gridDim.x * blockDim.x)
+        amr::fab_scatter_elem(G, L, dir, B, e, level);
+}
+
 inline int blocks_for(long n, int sms) {
     const long b = (n + kThreads - 1) / kThreads;
     const long cap = (long)std::max(1, sms) * 16;
@@ -220,6 +236,21 @@ struct AmrState {
         long ncell = 0;
     };
     std::vector<LevelStore> L;
+    // per-box (fab) calls: level arrays of the inputs, fab tables, host-pointer staging
+    struct FabArrays {
+        double* u[3] = {nullptr, nullptr, nullptr};
+        double* phi = nullptr;
+        double* rho = nullptr;
+        double* rhs = nullptr;
+        double* b0 = nullptr;
+        double* b0e = nullptr;
+    };
+    std::vector<FabArrays> F;
+    amr::FabDesc* h_tab = nullptr;   // pinned
+    amr::FabDesc* d_tab = nullptr;
+    size_t tab_cap = 0;
+    double* staging = nullptr;
+    size_t staging_cap = 0;
     double* part = nullptr;     // reduction partials: kReduceBlocks * 4 per level
     double* out = nullptr;      // reduction result (5 doubles) + 8 scratch
     double* h_out = nullptr;    // pinned mirror
@@ -234,6 +265,8 @@ void amr_release(mac_ctx* c) {
     if (!A) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (void* p : A->allocs) cudaFree(p);
+    if (A->staging) cudaFree(A->staging);
+    if (A->h_tab) cudaFreeHost(A->h_tab);
     if (A->h_out) cudaFreeHost(A->h_out);
     if (A->h_flag) cudaFreeHost(A->h_flag);
     delete A;
@@ -279,8 +312,8 @@ int build_masks(const mac_ctx* c, int nlev, const int* nboxes, const int* box_lo
         for (int b = 0; b < nboxes[l]; ++b, ++off) {
             int lo[3], hi[3];
             for (int d = 0; d < 3; ++d) {
-                lo[d] = box_lo[3 * off + d];
-                hi[d] = box_hi[3 * off + d];
+                lo[d] = box_lo[3 * off + d] - (d < dm ? (c->g.domain_lo[d] << l) : 0);
+                hi[d] = box_hi[3 * off + d] - (d < dm ? (c->g.domain_lo[d] << l) : 0);
                 if (d >= dm) {
                     if (lo[d] != 0 || hi[d] != 0) return MAC_ERR_INVALID;
                     continue;
@@ -587,40 +620,13 @@ int amr_configure(mac_ctx* c, int nlev, const int* nboxes, const int* box_lo, co
     return rc;
 }
 
-}  // namespace mac
-
-using namespace mac;
-
-extern "C" {
-
-int mac_ctx_set_amr(mac_ctx* c, int nlev, const int* nboxes, const int* box_lo, const int* box_hi) {
-    if (!c) return MAC_ERR_INVALID;
-    if (nlev == 1) {
-        amr_release(c);
-        return MAC_OK;
-    }
-    return amr_configure(c, nlev, nboxes, box_lo, box_hi);
-}
-
-int mac_macproject_ml_dense(mac_ctx* c, double* const* umac, double* const* phi,
-                            const double* const* rho, const double* const* macrhs,
-                            const double* const* beta0, const double* const* beta0_edge,
-                            mac_stats* stats) {
-    mac_stats local;
-    mac_stats* st = stats ? stats : &local;
-    std::memset(st, 0, sizeof(*st));
-    if (!c || !c->amr || !umac || !phi || !rho) return st->status = MAC_ERR_INVALID;
-    if ((beta0 == nullptr) != (beta0_edge == nullptr)) return st->status = MAC_ERR_INVALID;
+// The multi-level projection on level arrays already on the device (the caller's, or gathered
+// from fabs); fills the solve fields of *st and returns the status code.
+int ml_core(mac_ctx* c, double* const* umac, double* const* phi, const double* const* rho,
+            const double* const* macrhs, const double* const* beta0,
+            const double* const* beta0_edge, mac_stats* st) {
     AmrState* A = c->amr;
     const int nl = A->nlev;
-    for (int l = 0; l < nl; ++l) {
-        if (!phi[l] || !rho[l]) return st->status = MAC_ERR_INVALID;
-        for (int d = 0; d < c->dm; ++d)
-            if (!umac[3 * l + d]) return st->status = MAC_ERR_INVALID;
-        if (beta0 && (!beta0[l] || !beta0_edge[l])) return st->status = MAC_ERR_INVALID;
-    }
-    const auto t0 = std::chrono::steady_clock::now();
-    begin_call_stats(c, st);
     GpuExec ex{c, A, nl, A->geo, c->geom_singular};
     ex.u = umac;
     ex.rho = rho;
@@ -676,10 +682,316 @@ int mac_macproject_ml_dense(mac_ctx* c, double* const* umac, double* const* phi,
     st->rel_resid = S.rel_resid;
     st->nhist = S.nhist;
     for (int q = 0; q < S.nhist && q < 64; ++q) st->hist[q] = S.hist[q];
+    return rc;
+}
+
+
+namespace {
+
+int fab_boxes(const mac_ctx* c, int l) {
+    return l == 0 ? c->g.nboxes : (int)(c->amr->boxes[l].size() / 6);
+}
+
+// Descriptor of box b of level l as a fab with ng ghosts (dir: face direction, -1 cells).
+amr::FabDesc fab_desc(const mac_ctx* c, int l, int b, int dir, int ng) {
+    amr::FabDesc D{};
+    long cnt = 1;
+    for (int d = 0; d < 3; ++d) {
+        if (d >= c->dm) {
+            D.lo[d] = D.hi[d] = 0;
+            D.ext[d] = 1;
+            continue;
+        }
+        if (l == 0) {
+            D.lo[d] = c->box_lo[3 * b + d] - c->g.domain_lo[d];
+            D.hi[d] = c->box_hi[3 * b + d] - c->g.domain_lo[d];
+        } else {
+            D.lo[d] = c->amr->boxes[l][6 * b + d];
+            D.hi[d] = c->amr->boxes[l][6 * b + 3 + d];
+        }
+        D.ext[d] = D.hi[d] - D.lo[d] + 1 + (dir == d ? 1 : 0) + 2 * ng;
+        cnt *= D.ext[d];
+    }
+    D.ng = ng;
+    D.count = cnt;
+    return D;
+}
+
+template <typename T>
+int grow_device(T** p, size_t* cap, size_t need) {
+    if (need <= *cap) return MAC_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    if (cudaMalloc((void**)p, need * sizeof(T)) != cudaSuccess) {
+        cudaGetLastError();
+        return MAC_ERR_ALLOC;
+    }
+    *cap = need;
+    return MAC_OK;
+}
+
+int ensure_fab_arrays(mac_ctx* c, bool rhs, bool b0) {
+    AmrState* A = c->amr;
+    if (A->F.size() != (size_t)A->nlev) A->F.assign(A->nlev, AmrState::FabArrays());
+    for (int l = 0; l < A->nlev; ++l) {
+        AmrState::FabArrays& F = A->F[l];
+        const Lev& L = A->L[l].lev;
+        const long N = A->L[l].ncell;
+        int rc = MAC_OK;
+        for (int d = 0; d < c->dm && !rc; ++d)
+            if (!F.u[d]) rc = amr_alloc(A, &F.u[d], (size_t)amr::nfaces(L, d));
+        if (!rc && !F.phi) rc = amr_alloc(A, &F.phi, (size_t)N);
+        if (!rc && !F.rho) rc = amr_alloc(A, &F.rho, (size_t)N);
+        if (!rc && rhs && !F.rhs) rc = amr_alloc(A, &F.rhs, (size_t)N);
+        const int nr = L.n[c->dm - 1];
+        if (!rc && b0 && !F.b0) rc = amr_alloc(A, &F.b0, (size_t)nr);
+        if (!rc && b0 && !F.b0e) rc = amr_alloc(A, &F.b0e, (size_t)nr + 1);
+        if (rc) return rc;
+    }
+    return MAC_OK;
+}
+
+}  // namespace
+
+// Per-box entry: gather the caller's fabs into the level arrays, project, scatter back.
+int ml_fabs(mac_ctx* c, int ptr_kind, double* const* umac, int ng_u, double* const* phi,
+            int ng_phi, const double* const* rho, int ng_rho, int rho_comp,
+            const double* const* macrhs, int ng_rhs, const double* beta0,
+            const double* beta0_edge, mac_stats* st) {
+    AmrState* A = c->amr;
+    const int nl = A->nlev;
+    const int dm = c->dm;
+    const bool host = ptr_kind == MAC_PTR_HOST;
+    int rc = ensure_fab_arrays(c, macrhs != nullptr, beta0 != nullptr);
+    if (rc) return rc;
+    // tables and staging
+    size_t ntab = 0, nstage = 0;
+    for (int l = 0; l < nl; ++l) {
+        const int nb = fab_boxes(c, l);
+        ntab += (size_t)nb * (dm + 3);
+        for (int b = 0; b < nb; ++b) {
+            for (int d = 0; d < dm; ++d) nstage += (size_t)fab_desc(c, l, b, d, ng_u).count;
+            nstage += (size_t)fab_desc(c, l, b, -1, ng_phi).count;
+            nstage += (size_t)fab_desc(c, l, b, -1, ng_rho).count;
+            if (macrhs) nstage += (size_t)fab_desc(c, l, b, -1, ng_rhs).count;
+        }
+    }
+    if (ntab > A->tab_cap) {
+        MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        if (A->h_tab) cudaFreeHost(A->h_tab);
+        if (A->d_tab) cudaFree(A->d_tab);
+        A->h_tab = nullptr;
+        A->d_tab = nullptr;
+        A->tab_cap = 0;
+        if (cudaMallocHost((void**)&A->h_tab, ntab * sizeof(amr::FabDesc)) != cudaSuccess ||
+            cudaMalloc((void**)&A->d_tab, ntab * sizeof(amr::FabDesc)) != cudaSuccess) {
+            cudaGetLastError();
+            return MAC_ERR_ALLOC;
+        }
+        A->tab_cap = ntab;
+    }
+    if (host) {
+        MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        rc = grow_device(&A->staging, &A->staging_cap, nstage);
+        if (rc) return rc;
+    }
+    size_t tcur = 0, scur = 0;
+    std::vector<size_t> tab_u(nl * 3), tab_phi(nl);
+    // one array of one level: descriptors, host copies, table upload, gather kernel
+    auto gather = [&](int l, int dir, int ng, const double* const* ptrs, long comp_stride_comp,
+                      int with_ghosts, double* level, size_t* tab_at) -> int {
+        const int nb = fab_boxes(c, l);
+        amr::FabDesc* H = A->h_tab + tcur;
+        long maxc = 1;
+        for (int b = 0; b < nb; ++b) {
+            amr::FabDesc D = fab_desc(c, l, b, dir, ng);
+            const double* src = ptrs[b] + D.count * comp_stride_comp;
+            if (host) {
+                double* region = A->staging + scur;
+                scur += (size_t)D.count;
+                MAC_CUDA_TRY(cudaMemcpyAsync(region, src, (size_t)D.count * sizeof(double),
+                                             cudaMemcpyHostToDevice, c->stream));
+                D.src = region;
+                D.dst = region;
+            } else {
+                D.src = src;
+                D.dst = const_cast<double*>(src);
+            }
+            H[b] = D;
+            maxc = std::max(maxc, D.count);
+        }
+        MAC_CUDA_TRY(cudaMemcpyAsync(A->d_tab + tcur, H, (size_t)nb * sizeof(amr::FabDesc),
+                                     cudaMemcpyHostToDevice, c->stream));
+        const dim3 grid((unsigned)std::min<long>((maxc + kThreads - 1) / kThreads, 1024), (unsigned)nb);
+        k_fabs_gather<<<grid, kThreads, 0, c->stream>>>(A->geo, A->L[l].lev, dir, A->d_tab + tcur,
+                                                       with_ghosts, level);
+        MAC_CUDA_TRY(cudaGetLastError());
+        ++c->issued;
+        if (tab_at) *tab_at = tcur;
+        tcur += (size_t)nb;
+        return MAC_OK;
+    };
+    int uoff = 0, boff = 0;
+    size_t roff = 0;
+    std::vector<double*> up(3 * nl, nullptr), pp(nl), rp(nl), mp(nl), b0p(nl), b0ep(nl);
+    for (int l = 0; l < nl && !rc; ++l) {
+        const int nb = fab_boxes(c, l);
+        AmrState::FabArrays& F = A->F[l];
+        for (int d = 0; d < dm && !rc; ++d) {
+            rc = gather(l, d, ng_u, umac + uoff + d * nb, 0, 0, F.u[d], &tab_u[3 * l + d]);
+            up[3 * l + d] = F.u[d];
+        }
+        if (!rc) rc = gather(l, -1, ng_phi, phi + boff, 0, 0, F.phi, &tab_phi[l]);
+        if (!rc) rc = gather(l, -1, ng_rho, rho + boff, rho_comp, 1, F.rho, nullptr);
+        if (!rc && macrhs) rc = gather(l, -1, ng_rhs, macrhs + boff, 0, 0, F.rhs, nullptr);
+        pp[l] = F.phi;
+        rp[l] = F.rho;
+        mp[l] = F.rhs;
+        if (!rc && beta0) {
+            const size_t nr = (size_t)A->L[l].lev.n[dm - 1];
+            if (host) {
+                MAC_CUDA_TRY(cudaMemcpyAsync(F.b0, beta0 + roff, nr * sizeof(double),
+                                             cudaMemcpyHostToDevice, c->stream));
+                MAC_CUDA_TRY(cudaMemcpyAsync(F.b0e, beta0_edge + roff + l, (nr + 1) * sizeof(double),
+                                             cudaMemcpyHostToDevice, c->stream));
+                b0p[l] = F.b0;
+                b0ep[l] = F.b0e;
+            } else {
+                b0p[l] = const_cast<double*>(beta0 + roff);
+                b0ep[l] = const_cast<double*>(beta0_edge + roff + l);
+            }
+            roff += nr;
+        }
+        uoff += dm * nb;
+        boff += nb;
+    }
+    if (rc) return rc;
+    const int solve_rc = ml_core(c, up.data(), pp.data(), rp.data(), macrhs ? mp.data() : nullptr,
+                                 beta0 ? b0p.data() : nullptr, beta0 ? b0ep.data() : nullptr, st);
+    if (solve_rc != MAC_OK && solve_rc != MAC_ERR_NOT_CONVERGED) return solve_rc;
+    // scatter umac and phi back (the tables of the gathers carry dst)
+    for (int l = 0; l < nl; ++l) {
+        const int nb = fab_boxes(c, l);
+        long maxu = 1, maxp = 1;
+        for (int b = 0; b < nb; ++b) {
+            for (int d = 0; d < dm; ++d) maxu = std::max(maxu, A->h_tab[tab_u[3 * l + d] + b].count);
+            maxp = std::max(maxp, A->h_tab[tab_phi[l] + b].count);
+        }
+        for (int d = 0; d < dm; ++d) {
+            const dim3 grid((unsigned)std::min<long>((maxu + kThreads - 1) / kThreads, 1024), (unsigned)nb);
+            k_fabs_scatter<<<grid, kThreads, 0, c->stream>>>(A->geo, A->L[l].lev, d,
+                                                            A->d_tab + tab_u[3 * l + d], A->F[l].u[d]);
+            MAC_CUDA_TRY(cudaGetLastError());
+            ++c->issued;
+        }
+        const dim3 grid((unsigned)std::min<long>((maxp + kThreads - 1) / kThreads, 1024), (unsigned)nb);
+        k_fabs_scatter<<<grid, kThreads, 0, c->stream>>>(A->geo, A->L[l].lev, -1,
+                                                        A->d_tab + tab_phi[l], A->F[l].phi);
+        MAC_CUDA_TRY(cudaGetLastError());
+        ++c->issued;
+    }
+    if (host) {
+        uoff = 0;
+        boff = 0;
+        for (int l = 0; l < nl; ++l) {
+            const int nb = fab_boxes(c, l);
+            for (int d = 0; d < dm; ++d)
+                for (int b = 0; b < nb; ++b) {
+                    const amr::FabDesc& D = A->h_tab[tab_u[3 * l + d] + b];
+                    MAC_CUDA_TRY(cudaMemcpyAsync(umac[uoff + d * nb + b], D.src,
+                                                 (size_t)D.count * sizeof(double),
+                                                 cudaMemcpyDeviceToHost, c->stream));
+                }
+            for (int b = 0; b < nb; ++b) {
+                const amr::FabDesc& D = A->h_tab[tab_phi[l] + b];
+                MAC_CUDA_TRY(cudaMemcpyAsync(phi[boff + b], D.src, (size_t)D.count * sizeof(double),
+                                             cudaMemcpyDeviceToHost, c->stream));
+            }
+            uoff += dm * nb;
+            boff += nb;
+        }
+    }
+    MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return solve_rc;
+}
+
+}  // namespace mac
+
+using namespace mac;
+
+extern "C" {
+
+int mac_ctx_set_amr(mac_ctx* c, int nlev, const int* nboxes, const int* box_lo, const int* box_hi) {
+    if (!c) return MAC_ERR_INVALID;
+    if (nlev == 1) {
+        amr_release(c);
+        return MAC_OK;
+    }
+    return amr_configure(c, nlev, nboxes, box_lo, box_hi);
+}
+
+int mac_macproject_ml_dense(mac_ctx* c, double* const* umac, double* const* phi,
+                            const double* const* rho, const double* const* macrhs,
+                            const double* const* beta0, const double* const* beta0_edge,
+                            mac_stats* stats) {
+    mac_stats local;
+    mac_stats* st = stats ? stats : &local;
+    std::memset(st, 0, sizeof(*st));
+    if (!c || !c->amr || !umac || !phi || !rho) return st->status = MAC_ERR_INVALID;
+    if ((beta0 == nullptr) != (beta0_edge == nullptr)) return st->status = MAC_ERR_INVALID;
+    AmrState* A = c->amr;
+    const int nl = A->nlev;
+    for (int l = 0; l < nl; ++l) {
+        if (!phi[l] || !rho[l]) return st->status = MAC_ERR_INVALID;
+        for (int d = 0; d < c->dm; ++d)
+            if (!umac[3 * l + d]) return st->status = MAC_ERR_INVALID;
+        if (beta0 && (!beta0[l] || !beta0_edge[l])) return st->status = MAC_ERR_INVALID;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    begin_call_stats(c, st);
+    const int rc = ml_core(c, umac, phi, rho, macrhs, beta0, beta0_edge, st);
     st->status = rc;
     st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     end_call_stats(c, st);
     report_call(c, "macproject_ml_dense", st);
+    return rc;
+}
+
+
+int mac_macproject_ml(mac_ctx* c, int ptr_kind, double* const* umac, int ng_u,
+                      double* const* phi, int ng_phi, const double* const* rho, int ng_rho,
+                      int rho_ncomp, int rho_comp, const double* const* macrhs, int ng_rhs,
+                      const double* beta0, const double* beta0_edge, mac_stats* stats) {
+    mac_stats local;
+    mac_stats* st = stats ? stats : &local;
+    std::memset(st, 0, sizeof(*st));
+    if (!c || !c->amr || !umac || !phi || !rho) return st->status = MAC_ERR_INVALID;
+    if (ptr_kind != MAC_PTR_HOST && ptr_kind != MAC_PTR_DEVICE) return st->status = MAC_ERR_INVALID;
+    if (ng_u < 0 || ng_phi < 0 || ng_rho < 1 || ng_rhs < 0) return st->status = MAC_ERR_INVALID;
+    if (rho_ncomp < 1 || rho_comp < 0 || rho_comp >= rho_ncomp) return st->status = MAC_ERR_INVALID;
+    if ((beta0 == nullptr) != (beta0_edge == nullptr)) return st->status = MAC_ERR_INVALID;
+    AmrState* A = c->amr;
+    int uoff = 0, boff = 0;
+    for (int l = 0; l < A->nlev; ++l) {
+        const int nb = fab_boxes(c, l);
+        for (int b = 0; b < nb; ++b) {
+            if (!phi[boff + b] || !rho[boff + b] || (macrhs && !macrhs[boff + b]))
+                return st->status = MAC_ERR_INVALID;
+            for (int d = 0; d < c->dm; ++d)
+                if (!umac[uoff + d * nb + b]) return st->status = MAC_ERR_INVALID;
+        }
+        uoff += c->dm * nb;
+        boff += nb;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    begin_call_stats(c, st);
+    const int rc = ml_fabs(c, ptr_kind, umac, ng_u, phi, ng_phi, rho, ng_rho, rho_comp, macrhs,
+                           ng_rhs, beta0, beta0_edge, st);
+    st->status = rc;
+    st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    end_call_stats(c, st);
+    report_call(c, "macproject_ml", st);
     return rc;
 }
 

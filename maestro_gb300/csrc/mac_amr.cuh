@@ -389,6 +389,67 @@ AMR_HD inline void correct_face(const Geo& G, const Lev& L, const Lev& C, int d,
     u[idx] -= beta[idx] * g;
 }
 
+// ---- caller fabs <-> level arrays -------------------------------------------------------------
+//
+// One fab of the caller's layout on a level: box [lo, hi] in level indices, ng ghost cells,
+// natural (Fortran) order over ext[] = box extent + 2 ng (+1 along a face direction); one
+// component starting at src (gather) / dst (scatter).
+struct FabDesc {
+    const double* src;
+    double* dst;
+    int lo[3], hi[3];
+    int ext[3];
+    int ng;
+    long count;
+};
+
+// Level-array index of element e of fab B (dir: face direction, -1 cells).  Returns 1 for the
+// box's own cells / faces, 2 for a ghost cell inside the domain (periodic images wrapped), 0 for
+// anything else (ghost faces, ghosts beyond a non-periodic domain face).
+AMR_HD inline int fab_elem(const Geo& G, const Lev& L, int dir, const FabDesc& B, long e,
+                           long* tgt) {
+    int a[3];
+    a[0] = (int)(e % B.ext[0]);
+    const long r = e / B.ext[0];
+    a[1] = (int)(r % B.ext[1]);
+    a[2] = (int)(r / B.ext[1]);
+    int g[3] = {0, 0, 0};
+    bool interior = true;
+    for (int d = 0; d < G.dm; ++d) {
+        g[d] = B.lo[d] - B.ng + a[d];
+        const int top = B.hi[d] + (dir == d ? 1 : 0);
+        if (g[d] < B.lo[d] || g[d] > top) interior = false;
+    }
+    if (interior) {
+        *tgt = dir < 0 ? cix(L, g[0], g[1], g[2]) : fix(L, dir, g[0], g[1], g[2]);
+        return 1;
+    }
+    if (dir >= 0) return 0;
+    for (int d = 0; d < G.dm; ++d) {
+        const int q = wrap(G, L, d, g[d]);
+        if (q < 0) return 0;
+        g[d] = q;
+    }
+    *tgt = cix(L, g[0], g[1], g[2]);
+    return 2;
+}
+
+// Gather element e of fab B into the level array: the box's own entries always, ghost cells
+// (with_ghosts) only where the cell lies outside the level's region.
+AMR_HD inline void fab_gather_elem(const Geo& G, const Lev& L, int dir, const FabDesc& B, long e,
+                                   int with_ghosts, double* level) {
+    long t;
+    const int kind = fab_elem(G, L, dir, B, e, &t);
+    if (kind == 1 || (kind == 2 && with_ghosts && !in_region(L, t))) level[t] = B.src[e];
+}
+
+// Scatter the box's own entries of the level array into element e of fab B.
+AMR_HD inline void fab_scatter_elem(const Geo& G, const Lev& L, int dir, const FabDesc& B, long e,
+                                    const double* level) {
+    long t;
+    if (fab_elem(G, L, dir, B, e, &t) == 1) B.dst[e] = level[t];
+}
+
 // ---- the multi-level cycle and the projection steps -------------------------------------------
 //
 // E provides, for levels l = 0 .. nlev-1 (arrays are E's own memory):

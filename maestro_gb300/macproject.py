@@ -322,6 +322,33 @@ class MacProjector:
         self._check(rc, "mac_macproject_ml_dense", st, strict)
         return st.as_dict()
 
+    def macproject_ml(self, umac, phi, rho, macrhs=None, beta0=None, beta0_edge=None, ng_u=1,
+                      ng_phi=1, ng_rho=1, ng_rhs=0, rho_ncomp=1, rho_comp=0, strict=False):
+        """Multi-level MAC projection of per-box host fabs in place (mac_macproject_ml; needs
+        set_amr).  umac[l][d][b], phi[l][b], rho[l][b], macrhs[l][b] (or None) for every level
+        l; beta0[l] / beta0_edge[l] the planar base state of level l (or None)."""
+        nlev = len(phi)
+        flat_u, flat_p, flat_r, flat_m = [], [], [], []
+        for l in range(nlev):
+            nb = len(phi[l])
+            flat_u += [umac[l][d][b] for d in range(self.dm) for b in range(nb)]
+            flat_p += list(phi[l])
+            flat_r += list(rho[l])
+            if macrhs is not None:
+                flat_m += list(macrhs[l])
+        b0 = None if beta0 is None else np.concatenate([np.asarray(b, dtype=np.float64)
+                                                        for b in beta0])
+        b0e = None if beta0_edge is None else np.concatenate([np.asarray(b, dtype=np.float64)
+                                                              for b in beta0_edge])
+        st = capi.MacStats()
+        rc = capi.lib().mac_macproject_ml(
+            self.ctx, capi.MAC_PTR_HOST, _ptr_array(flat_u), ng_u, _ptr_array(flat_p), ng_phi,
+            _ptr_array(flat_r), ng_rho, rho_ncomp, rho_comp,
+            _ptr_array(flat_m) if macrhs is not None else None, ng_rhs, _dptr(b0), _dptr(b0e),
+            ctypes.byref(st))
+        self._check(rc, "mac_macproject_ml", st, strict)
+        return st.as_dict()
+
     def adjoint_dense(self, u, rho, macrhs, beta0, beta0_edge, w, du, drinv=None, dbeta0=None,
                       dmacrhs=None, phi_out=None, strict=True):
         """Adjoint of the whole-domain projection on device pointers (see maestro_mac.h)."""

@@ -250,4 +250,37 @@ int amrh_macproject(const orc_opts* o, int nlev, const int* nboxes, const int* b
     return rc;
 }
 
+
+// Caller fabs <-> a level array with the library's fab functions.  fabs[b] are the fab images of
+// level l's boxes (level 0: the single domain box is not used; l >= 1), dir the face direction
+// (-1 cells).  gather: level += nothing, entries set from the fabs; scatter: fab entries of the
+// boxes set from the level array.
+void amrh_fabs(const orc_opts* o, int nlev, const int* nboxes, const int* boxes, int l, int dir,
+               int ng, int with_ghosts, int scatter, double* const* fabs, double* level) {
+    HostExec E;
+    build(E, o, nlev, nboxes, boxes);
+    const int* bx = boxes;
+    for (int q = 1; q < l; ++q) bx += 6 * nboxes[q];
+    for (int b = 0; b < nboxes[l]; ++b, bx += 6) {
+        amr::FabDesc D{};
+        long cnt = 1;
+        for (int d = 0; d < 3; ++d) {
+            D.lo[d] = bx[d];
+            D.hi[d] = bx[3 + d];
+            D.ext[d] = d < o->dm ? D.hi[d] - D.lo[d] + 1 + (dir == d) + 2 * ng : 1;
+            cnt *= D.ext[d];
+        }
+        D.ng = ng;
+        D.count = cnt;
+        D.src = fabs[b];
+        D.dst = fabs[b];
+        for (long e = 0; e < cnt; ++e) {
+            if (scatter)
+                amr::fab_scatter_elem(E.geo, E.L[l], dir, D, e, level);
+            else
+                amr::fab_gather_elem(E.geo, E.L[l], dir, D, e, with_ghosts, level);
+        }
+    }
+}
+
 }  // extern "C"

@@ -37,6 +37,9 @@ def host_lib(tmp_path_factory):
     L.amrh_macproject.argtypes = [P(O.OrcOpts), ctypes.c_int, ip, ip, pd, pd, pd, pd, pd, pd,
                                   P(ctypes.c_double)]
     L.amrh_macproject.restype = ctypes.c_int
+    L.amrh_fabs.argtypes = [P(O.OrcOpts), ctypes.c_int, ip, ip, ctypes.c_int, ctypes.c_int,
+                            ctypes.c_int, ctypes.c_int, ctypes.c_int, pd, P(ctypes.c_double)]
+    L.amrh_fabs.restype = None
     return L
 
 
@@ -89,3 +92,51 @@ def test_library_amr_code_on_host_matches_oracle_at_maestro_tolerance(host_lib, 
     assert int(st[1]) == so["vcycles"]
     assert phi_err(H, phi, po) <= 1e-10
     assert u_err(H, u, uo) <= 1e-10
+
+
+@pytest.mark.parametrize("dir_", [-1, 0, 1])
+def test_fab_gather_and_scatter_of_a_fine_level(host_lib, dir_):
+    # level 1 of the layout with a box wrapping the periodic x boundary and one on the wall
+    from maestro_gb300.macproject import Layout
+    c = load_amr("amr2d_wrap")
+    H = G.Hierarchy(c["n0"], c["dx0"], c["bc_lo"], c["bc_hi"], c["boxes"])
+    shape = list(H.shape[1])
+    if dir_ >= 0:
+        shape[dir_] += 1
+    rng = np.random.default_rng(3)
+    arr = np.asfortranarray(rng.standard_normal(shape))
+    ng = 2
+    lay = Layout(H.shape[1], c["boxes"][1])
+    per = [b == O.BC_PER for b in c["bc_lo"]]
+    fabs = lay.to_fabs(arr, ng=ng, face_dir=None if dir_ < 0 else dir_, periodic=per)
+    o = O._opts(c["n0"], c["dx0"], c["bc_lo"], c["bc_hi"], 1, 0, 0, 0, 0, 0, 0, 0, 0, False, 0)
+    nb, bx = O._ml_layout(c["n0"], c["boxes"])
+    ipp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))  # noqa: E731
+    level = np.zeros(shape, order="F")
+    host_lib.amrh_fabs(ctypes.byref(o), 2, ipp(nb), ipp(bx), 1, dir_, ng, 1, 0,
+                       O._ptr_array(fabs), level.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    if dir_ < 0:
+        # the boxes' cells and their ng ghost layers (corners included) that lie in the domain,
+        # periodic images wrapped
+        want = np.zeros(H.shape[1], dtype=bool)
+        for lo, hi in c["boxes"][1]:
+            idx = []
+            for d in range(2):
+                r = np.arange(lo[d] - ng, hi[d] + 1 + ng)
+                r = r % H.shape[1][d] if per[d] else r[(r >= 0) & (r < H.shape[1][d])]
+                idx.append(r)
+            want[np.ix_(*idx)] = True
+    else:
+        want = G.face_member(H, 1, dir_)
+    np.testing.assert_array_equal(level[want], arr[want])
+    assert np.all(level[~want] == 0.0)
+    # scatter: the boxes' own entries of every fab come from the level array
+    out = [np.zeros_like(f) for f in fabs]
+    host_lib.amrh_fabs(ctypes.byref(o), 2, ipp(nb), ipp(bx), 1, dir_, ng, 0, 1,
+                       O._ptr_array(out), arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    for f, g, (lo, hi) in zip(out, fabs, c["boxes"][1]):
+        sl = tuple(slice(ng, ng + hi[d] - lo[d] + 1 + (1 if d == dir_ else 0)) for d in range(2))
+        np.testing.assert_array_equal(f[sl], g[sl])
+        mask = np.ones(f.shape, dtype=bool)
+        mask[sl] = False
+        assert np.all(f[mask] == 0.0)

@@ -82,3 +82,46 @@ def test_amr_layout_and_density_errors():
     with pytest.raises(MacError) as e:
         _run(c, rho=rho)
     assert e.value.code == capi.MAC_ERR_BAD_DENSITY
+
+
+@pytest.mark.parametrize("name", ["amr2d_wrap", "amr3d_16"])
+def test_amr_projection_on_host_fabs(name):
+    # the drop-in form: per-box host fabs of every level (several boxes on level 0 too), rho with
+    # two ghost cells, umac with one
+    c = load_amr(name)
+    H = G.Hierarchy(c["n0"], c["dx0"], c["bc_lo"], c["bc_hi"], c["boxes"])
+    dm = c["dm"]
+    nlev = c["nlev"]
+    per = [b == O.BC_PER for b in c["bc_lo"]]
+    lays = [Layout.tiled(c["n0"], tuple(v // 2 for v in c["n0"]))] + [
+        Layout(H.shape[l], c["boxes"][l]) for l in range(1, nlev)]
+    umac = [[lays[l].to_fabs(c["umac"][l][d], ng=1, face_dir=d, periodic=per) for d in range(dm)]
+            for l in range(nlev)]
+    phi = [lays[l].to_fabs(np.zeros(H.shape[l]), ng=1, periodic=per) for l in range(nlev)]
+    rho = [lays[l].to_fabs(c["rho"][l], ng=2, periodic=per) for l in range(nlev)]
+    rhs = [lays[l].to_fabs(c["macrhs"][l], ng=0, periodic=per) for l in range(nlev)]
+    P = MacProjector(lays[0], c["dx0"], BcTower(c["bc_lo"], c["bc_hi"]), precision="fp64",
+                     rel_eps=1e-13)
+    try:
+        P.set_amr(c["boxes"])
+        st = P.macproject_ml(umac, phi, rho, macrhs=rhs, beta0=c["beta0"],
+                             beta0_edge=c["beta0_edge"], ng_u=1, ng_phi=1, ng_rho=2, ng_rhs=0,
+                             strict=True)
+    finally:
+        P.close()
+    assert st["status"] == 0
+    # compare the boxes' own faces and cells with the golden solution (phi up to the constant)
+    ref_phi = [lays[l].to_fabs(c["phi"][l], ng=1, periodic=per) for l in range(nlev)]
+    shift = None
+    scale = max(np.max(np.abs(p)) for p in c["phi"])
+    for l in range(nlev):
+        for b, (lo, hi) in enumerate(lays[l].boxes):
+            sl = tuple(slice(1, 1 + hi[d] - lo[d] + 1) for d in range(dm))
+            diff = phi[l][b][sl] - ref_phi[l][b][sl]
+            shift = diff.flat[0] if shift is None else shift
+            assert np.max(np.abs(diff - shift)) <= 1e-9 * scale
+            for d in range(dm):
+                ref_u = lays[l].to_fabs(c["unew"][l][d], ng=1, face_dir=d, periodic=per)[b]
+                slu = tuple(slice(1, 1 + hi[e] - lo[e] + 1 + (1 if e == d else 0)) for e in range(dm))
+                den = np.max(np.abs(c["unew"][l][d][G.face_member(H, l, d)]))
+                assert np.max(np.abs(umac[l][d][b][slu] - ref_u[slu])) <= 1e-9 * den
