@@ -80,10 +80,30 @@ class OrcStats(ctypes.Structure):
         }
 
 
+class OrcHgOpts(ctypes.Structure):
+    _fields_ = [
+        ("dm", ctypes.c_int),
+        ("n", ctypes.c_int * 3),
+        ("dx", ctypes.c_double * 3),
+        ("bc_lo", ctypes.c_int * 3),
+        ("bc_hi", ctypes.c_int * 3),
+        ("dense", ctypes.c_int),
+        ("proj_type", ctypes.c_int),
+        ("dt", ctypes.c_double),
+        ("alt_energy_fix", ctypes.c_int),
+        ("rel_eps", ctypes.c_double),
+        ("max_vcycles", ctypes.c_int),
+        ("nu1", ctypes.c_int),
+        ("nu2", ctypes.c_int),
+        ("bottom_eps", ctypes.c_double),
+        ("nthreads", ctypes.c_int),
+    ]
+
+
 _lib = None
 
 
-_SOURCES = ("mac_oracle.cpp", "mac_oracle_ml.cpp", "mac_oracle_core.h")
+_SOURCES = ("mac_oracle.cpp", "mac_oracle_ml.cpp", "hg_oracle.cpp", "mac_oracle_core.h")
 
 
 def build(force: bool = False) -> str:
@@ -123,6 +143,16 @@ def lib():
         L.orc_macproject_ml.argtypes = [P(OrcOpts), ctypes.c_int, ip, ip, pd, pd, pd, pd, pd, pd,
                                         P(OrcStats)]
         L.orc_macproject_ml.restype = ctypes.c_int
+        L.orc_hg_apply.argtypes = [P(OrcHgOpts), d, d, d]
+        L.orc_hg_apply.restype = None
+        L.orc_hg_divu.argtypes = [P(OrcHgOpts), d, d]
+        L.orc_hg_divu.restype = None
+        L.orc_hg_grad.argtypes = [P(OrcHgOpts), d, d]
+        L.orc_hg_grad.restype = None
+        L.orc_hg_solve.argtypes = [P(OrcHgOpts), d, d, d, P(OrcStats)]
+        L.orc_hg_solve.restype = ctypes.c_int
+        L.orc_hgproject.argtypes = [P(OrcHgOpts), d, d, d, d, d, d, d, d, P(OrcStats)]
+        L.orc_hgproject.restype = ctypes.c_int
         L.orc_max_threads.argtypes = []
         L.orc_max_threads.restype = ctypes.c_int
         _lib = L
@@ -469,3 +499,107 @@ def macproject_ml(umac, phi, rho, dx, bc_lo, bc_hi, boxes, macrhs=None, beta0=No
     if rc < 0:
         raise ValueError("invalid AMR layout (alignment or proper nesting)")
     return u, phi, st.as_dict()
+
+
+# ------------------------------------------------------------------------- nodal (HG) projection
+
+# proj_type values (Source/proj_parameters.f90)
+HG_INITIAL, HG_DIVU_ITERS, HG_PRESSURE_ITERS, HG_REGULAR = 1, 2, 3, 4
+# Source/mg_eps.f90:26-30
+EPS_HG, EPS_HG_MAX, HG_LEVEL_FACTOR, EPS_HG_BOTTOM = 1e-12, 1e-10, 10.0, 1e-4
+
+
+def _hg_opts(shape, dx, bc_lo, bc_hi, dense=True, proj_type=HG_INITIAL, dt=1.0,
+             alt_energy_fix=False, rel_eps=EPS_HG, max_vcycles=100, nu1=2, nu2=2,
+             bottom_eps=EPS_HG_BOTTOM, threads=0):
+    dm = len(shape)
+    o = OrcHgOpts()
+    o.dm = dm
+    for d in range(3):
+        o.n[d] = int(shape[d]) if d < dm else 1
+        o.dx[d] = float(dx[d]) if d < dm else 1.0
+        o.bc_lo[d] = int(bc_lo[d]) if d < dm else BC_NEU
+        o.bc_hi[d] = int(bc_hi[d]) if d < dm else BC_NEU
+    o.dense = int(bool(dense))
+    o.proj_type = int(proj_type)
+    o.dt = float(dt)
+    o.alt_energy_fix = int(bool(alt_energy_fix))
+    o.rel_eps = float(rel_eps)
+    o.max_vcycles = int(max_vcycles)
+    o.nu1, o.nu2 = int(nu1), int(nu2)
+    o.bottom_eps = float(bottom_eps)
+    o.nthreads = int(threads)
+    return o
+
+
+def node_shape(shape):
+    return tuple(int(v) + 1 for v in shape)
+
+
+def hg_apply(sigma, phi, dx, bc_lo, bc_hi, dense=True):
+    """Nodal operator L phi (cell coefficients sigma, node array phi)."""
+    sigma = _f64f(sigma)
+    phi = _f64f(phi)
+    o = _hg_opts(sigma.shape, dx, bc_lo, bc_hi, dense=dense)
+    out = np.zeros(node_shape(sigma.shape), order="F")
+    lib().orc_hg_apply(ctypes.byref(o), _ptr(sigma), _ptr(phi), _ptr(out))
+    return out
+
+
+def hg_divu(u, dx, bc_lo, bc_hi):
+    """Node-centred divergence of a cell vector field u (shape cells + (dm,))."""
+    u = _f64f(u)
+    shape = u.shape[:-1]
+    o = _hg_opts(shape, dx, bc_lo, bc_hi)
+    out = np.zeros(node_shape(shape), order="F")
+    lib().orc_hg_divu(ctypes.byref(o), _ptr(u), _ptr(out))
+    return out
+
+
+def hg_grad(phi, dx, bc_lo, bc_hi):
+    """Cell gradient of a nodal field (mkgphi); returns shape cells + (dm,)."""
+    phi = _f64f(phi)
+    shape = tuple(v - 1 for v in phi.shape)
+    o = _hg_opts(shape, dx, bc_lo, bc_hi)
+    g = np.zeros(shape + (len(shape),), order="F")
+    lib().orc_hg_grad(ctypes.byref(o), _ptr(phi), _ptr(g))
+    return g
+
+
+def hg_solve(sigma, rh, dx, bc_lo, bc_hi, phi=None, dense=True, rel_eps=EPS_HG,
+             max_vcycles=100, threads=0):
+    """Nodal solve L phi = rh.  Returns (phi, stats)."""
+    sigma = _f64f(sigma)
+    rh = _f64f(rh)
+    phi = np.zeros(rh.shape, order="F") if phi is None else _f64f(phi).copy(order="F")
+    o = _hg_opts(sigma.shape, dx, bc_lo, bc_hi, dense=dense, rel_eps=rel_eps,
+                 max_vcycles=max_vcycles, threads=threads)
+    st = OrcStats()
+    lib().orc_hg_solve(ctypes.byref(o), _ptr(sigma), _ptr(rh), _ptr(phi), ctypes.byref(st))
+    return phi, st.as_dict()
+
+
+def hgproject(unew, uold, gpi, rhohalf, pi, dx, bc_lo, bc_hi, proj_type=HG_REGULAR, dt=1.0,
+              beta0_cart=None, nodalrhs=None, dense=True, alt_energy_fix=False, rel_eps=EPS_HG,
+              max_vcycles=100, threads=0):
+    """Oracle nodal projection on one level (Source/hgproject.f90:32-264).
+
+    Cell vector fields unew / uold / gpi have shape cells + (dm,); rhohalf and beta0_cart are
+    cell arrays; pi and nodalrhs node arrays (cells + 1 per direction).  Returns
+    (unew, gpi, pi, phi, stats)."""
+    unew = _f64f(unew).copy(order="F")
+    gpi = _f64f(gpi).copy(order="F")
+    pi = _f64f(pi).copy(order="F")
+    uold = _f64f(uold)
+    rhohalf = _f64f(rhohalf)
+    shape = rhohalf.shape
+    b0 = None if beta0_cart is None else _f64f(beta0_cart)
+    nr = None if nodalrhs is None else _f64f(nodalrhs)
+    phi = np.zeros(node_shape(shape), order="F")
+    o = _hg_opts(shape, dx, bc_lo, bc_hi, dense=dense, proj_type=proj_type, dt=dt,
+                 alt_energy_fix=alt_energy_fix, rel_eps=rel_eps, max_vcycles=max_vcycles,
+                 threads=threads)
+    st = OrcStats()
+    lib().orc_hgproject(ctypes.byref(o), _ptr(unew), _ptr(uold), _ptr(gpi), _ptr(rhohalf),
+                        _ptr(pi), _ptr(b0), _ptr(nr), _ptr(phi), ctypes.byref(st))
+    return unew, gpi, pi, phi, st.as_dict()
