@@ -298,6 +298,28 @@ int mac_macproject_ml(mac_ctx* ctx, int ptr_kind,
                       const double* beta0, const double* beta0_edge,
                       mac_stats* stats);
 
+/* proj_type values of the nodal projection (Source/proj_parameters.f90) */
+#define MAC_HG_INITIAL        1   /* initial projection: U projected, pi = gpi = 0             */
+#define MAC_HG_DIVU_ITERS     2   /* divu iterations: as the initial projection                */
+#define MAC_HG_PRESSURE_ITERS 3   /* (U - Uold)/dt projected; U = Uold + dt U; pi, gpi += ...   */
+#define MAC_HG_REGULAR        4   /* U + dt gpi/rhohalf projected; pi = phi/dt, gpi = gphi/dt  */
+
+/*
+ * Nodal (HG) projection on one level, the drop-in for hgproject (Source/hgproject.f90:32-264,
+ * solve Source/hg_multigrid.f90:18-239) on whole-domain DEVICE arrays of the context's geometry
+ * (Fortran order, no ghosts): unew / uold / gpi cell vector fields (n0, n1[, n2], dm),
+ * rhohalf and beta0_cart (NULL: 1) cells, pi and nodalrhs (NULL: none) nodes
+ * (n0+1, n1+1[, n2+1]).  proj_type MAC_HG_*, dt the time step (> 0 for the pressure iterations
+ * and the regular time step), dense_stencil 1 for hg_dense_stencil (9/27-point) else the cross
+ * stencil, rel_eps the solver tolerance (<= 0: eps_hg = 1e-12).  Walls (U.n = 0), periodic and
+ * outflow (phi = 0) faces; the context's use_alt_energy_fix, max_vcycles, nu1 and nu2 apply.
+ * unew, gpi and pi are updated in place.
+ */
+int mac_hgproject_dense(mac_ctx* ctx, int proj_type, double dt, int dense_stencil, double rel_eps,
+                        double* unew, const double* uold, double* gpi, const double* rhohalf,
+                        double* pi, const double* beta0_cart, const double* nodalrhs,
+                        mac_stats* stats);
+
 /*
  * Adjoint (reverse-mode derivative) of the whole-domain MAC projection; no counterpart in the
  * reference.  Forward map (beta0 form, p = 1 + use_alt_energy_fix):

@@ -1,0 +1,461 @@
+// Nodal (HG) projection on one level: the node- and cell-wise arithmetic, and the nodal V-cycle
+// and projection steps written once against an executor.
+//
+// MAESTRO's hgproject (Source/hgproject.f90:32-264) projects the cell-centred velocity with a
+// node-centred potential: hg_multigrid (Source/hg_multigrid.f90:18-239) forms the coefficient
+// sigma = beta0 / rhohalf per cell (0 outside non-periodic faces), the node-centred divergence
+// of beta0 U and solves L phi = DU - nodalrhs with FBoxLib's nodal multigrid; mkgphi takes the
+// cell gradient of phi and hg_update corrects U, pi and gpi per projection type.
+//
+// Storage: natural layout, FP64.  Cells n[d] per active direction; nodes n[d] + 1 per active
+// direction, the node n[d] of a periodic direction being the image of node 0 (kernels always
+// read through node_wrap, images are refreshed only for the caller's output).  Nodes on an
+// outflow (Dirichlet) face hold 0.  Vector cell fields are component-major (d * ncell + c).
+//
+// Operators (the discretisation of Docs/mg/mg.tex:479-500):
+//   dense : (L phi)_p = - sum_{cells c of p} sigma_c sum_{nodes m of c} sum_d h_d^-2
+//           S(p_d, m_d) prod_{e != d} M(p_e, m_e) phi_m   -- the (bi/tri)linear finite-element
+//           stiffness over the nodal volume, S = [[1,-1],[-1,1]], M = [[1/3,1/6],[1/6,1/3]];
+//   cross : (L phi)_p = sum_d h_d^-2 sum_s sigma_edge (phi_{p+s e_d} - phi_p), sigma_edge the
+//           mean of sigma over the 2^(dm-1) cells along the edge;
+//   DU_p  = sum_d h_d^-1 2^(1-dm) [sum u_d over the cells on the + side of p - the same on the
+//           - side] (U = 0 outside non-periodic faces);
+//   gphi  = the cell gradient: mean of the nodal differences across the cell (mkgphi).
+// Multigrid: 2^dm-colour Gauss-Seidel (node parity), full-weighting restriction of the defect,
+// multilinear prolongation, coarse sigma = mean of the fine cells, Gauss-Seidel sweeps on the
+// coarsest level.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+
+#if defined(__CUDACC__)
+#define HG_HD __host__ __device__
+#else
+#define HG_HD
+#endif
+
+namespace mac {
+namespace hg {
+
+constexpr int kMaxLevels = 24;
+enum { kInitial = 1, kDivuIters = 2, kPressureIters = 3, kRegular = 4 };
+
+struct Geo {
+    int dm;
+    int per[3];
+    int dlo[3], dhi[3];
+    int dense;
+};
+
+struct Lev {
+    int n[3];          // cells (1 along inactive directions)
+    int nn[3];         // node storage (n + 1 along active directions)
+    double h[3];
+    const double* sig; // cell coefficients
+};
+
+HG_HD inline long nix(const Lev& L, int i, int j, int k) {
+    return (long)i + (long)L.nn[0] * ((long)j + (long)L.nn[1] * k);
+}
+HG_HD inline long cix(const Lev& L, int i, int j, int k) {
+    return (long)i + (long)L.n[0] * ((long)j + (long)L.n[1] * k);
+}
+HG_HD inline long nnodes(const Lev& L) { return (long)L.nn[0] * L.nn[1] * L.nn[2]; }
+HG_HD inline long ncells(const Lev& L) { return (long)L.n[0] * L.n[1] * L.n[2]; }
+
+HG_HD inline void node_coords(const Lev& L, long idx, int p[3]) {
+    p[0] = (int)(idx % L.nn[0]);
+    const long r = idx / L.nn[0];
+    p[1] = (int)(r % L.nn[1]);
+    p[2] = (int)(r / L.nn[1]);
+}
+HG_HD inline void cell_coords(const Lev& L, long idx, int c[3]) {
+    c[0] = (int)(idx % L.n[0]);
+    const long r = idx / L.n[0];
+    c[1] = (int)(r % L.n[1]);
+    c[2] = (int)(r / L.n[1]);
+}
+
+// Node index q along d folded onto the carrying node (periodic wrap); -1 outside.
+HG_HD inline int node_wrap(const Geo& G, const Lev& L, int d, int q) {
+    if (d >= G.dm) return q == 0 ? 0 : -1;
+    const int n = L.n[d];
+    if (G.per[d]) return ((q % n) + n) % n;
+    return (q < 0 || q > n) ? -1 : q;
+}
+HG_HD inline int cell_wrap(const Geo& G, const Lev& L, int d, int c) {
+    if (d >= G.dm) return c == 0 ? 0 : -1;
+    const int n = L.n[d];
+    if (G.per[d]) return ((c % n) + n) % n;
+    return (c < 0 || c >= n) ? -1 : c;
+}
+// An unknown: not a periodic image, not on an outflow face.
+HG_HD inline bool is_unknown(const Geo& G, const Lev& L, const int p[3]) {
+    for (int d = 0; d < G.dm; ++d) {
+        if (G.per[d]) {
+            if (p[d] == L.n[d]) return false;
+        } else if ((p[d] == 0 && G.dlo[d]) || (p[d] == L.n[d] && G.dhi[d])) {
+            return false;
+        }
+    }
+    return true;
+}
+
+// (L phi)_p = diag * phi_p - off.
+HG_HD inline void node_op(const Geo& G, const Lev& L, const int p[3], const double* phi,
+                          double& diag, double& off) {
+    const int dm = G.dm;
+    double dK = 0.0, oK = 0.0;
+    if (G.dense) {
+        const double Mw[2][2] = {{1.0 / 3.0, 1.0 / 6.0}, {1.0 / 6.0, 1.0 / 3.0}};
+        const long pi = nix(L, p[0], p[1], p[2]);
+        for (int a = 0; a < (1 << dm); ++a) {
+            int c[3] = {0, 0, 0}, loc[3] = {0, 0, 0};
+            bool out = false;
+            for (int d = 0; d < dm; ++d) {
+                loc[d] = (a >> d) & 1;
+                const int cw = cell_wrap(G, L, d, p[d] - loc[d]);
+                if (cw < 0) out = true;
+                c[d] = cw;
+            }
+            if (out) continue;
+            const double s = L.sig[cix(L, c[0], c[1], c[2])];
+            for (int b = 0; b < (1 << dm); ++b) {
+                int m[3] = {0, 0, 0}, ml[3] = {0, 0, 0};
+                for (int d = 0; d < dm; ++d) {
+                    ml[d] = (b >> d) & 1;
+                    m[d] = node_wrap(G, L, d, c[d] + ml[d]);
+                }
+                double k = 0.0;
+                for (int d = 0; d < dm; ++d) {
+                    double t = (loc[d] == ml[d] ? 1.0 : -1.0) / (L.h[d] * L.h[d]);
+                    for (int e = 0; e < dm; ++e)
+                        if (e != d) t *= Mw[loc[e]][ml[e]];
+                    k += t;
+                }
+                const long mi = nix(L, m[0], m[1], m[2]);
+                if (mi == pi)
+                    dK += s * k;
+                else
+                    oK -= s * k * phi[mi];
+            }
+        }
+        diag = -dK;
+        off = -oK;
+    } else {
+        for (int d = 0; d < dm; ++d)
+            for (int sd = -1; sd <= 1; sd += 2) {
+                const int q = node_wrap(G, L, d, p[d] + sd);
+                if (q < 0) continue;
+                double sum = 0.0;
+                int cnt = 0;
+                for (int a = 0; a < (1 << dm); ++a) {
+                    if ((a >> d) & 1) continue;
+                    int c[3] = {0, 0, 0};
+                    bool out = false;
+                    for (int e = 0; e < dm; ++e) {
+                        const int want = e == d ? (sd < 0 ? p[d] - 1 : p[d]) : p[e] - ((a >> e) & 1);
+                        const int cw = cell_wrap(G, L, e, want);
+                        if (cw < 0) out = true;
+                        c[e] = cw;
+                    }
+                    ++cnt;
+                    if (!out) sum += L.sig[cix(L, c[0], c[1], c[2])];
+                }
+                const double se = sum / cnt / (L.h[d] * L.h[d]);
+                int qq[3] = {p[0], p[1], p[2]};
+                qq[d] = q;
+                dK -= se;
+                oK -= se * phi[nix(L, qq[0], qq[1], qq[2])];
+            }
+        diag = dK;
+        off = oK;
+    }
+}
+
+// r = f - L phi on the unknowns, 0 elsewhere.
+HG_HD inline void defect_node(const Geo& G, const Lev& L, long idx, const double* phi,
+                              const double* f, double* r) {
+    int p[3];
+    node_coords(L, idx, p);
+    if (!is_unknown(G, L, p)) {
+        r[idx] = 0.0;
+        return;
+    }
+    double dg, off;
+    node_op(G, L, p, phi, dg, off);
+    r[idx] = f[idx] - (dg * phi[idx] - off);
+}
+
+HG_HD inline void gs_node(const Geo& G, const Lev& L, long idx, int colour, double* phi,
+                          const double* f) {
+    int p[3];
+    node_coords(L, idx, p);
+    int col = 0;
+    for (int d = 0; d < G.dm; ++d) col |= (p[d] & 1) << d;
+    if (col != colour || !is_unknown(G, L, p)) return;
+    double dg, off;
+    node_op(G, L, p, phi, dg, off);
+    phi[idx] = (f[idx] + off) / dg;
+}
+
+// Coarse right-hand side = full-weighting restriction of the fine defect (coarse node P <- fine
+// nodes 2P + a, a in {-1,0,1}^dm, weights prod (1 or 1/2), divided by 2^dm).
+HG_HD inline void restrict_node(const Geo& G, const Lev& F, const Lev& K, long idx,
+                                const double* rF, double* fK) {
+    int P[3];
+    node_coords(K, idx, P);
+    if (!is_unknown(G, K, P)) {
+        fK[idx] = 0.0;
+        return;
+    }
+    const int dm = G.dm;
+    double s = 0.0;
+    for (int a2 = -(dm > 2); a2 <= (dm > 2); ++a2)
+        for (int a1 = -(dm > 1); a1 <= (dm > 1); ++a1)
+            for (int a0 = -1; a0 <= 1; ++a0) {
+                const int a[3] = {a0, a1, a2};
+                int q[3] = {0, 0, 0};
+                double w = 1.0;
+                bool out = false;
+                for (int d = 0; d < dm; ++d) {
+                    if (a[d]) w *= 0.5;
+                    const int qq = node_wrap(G, F, d, 2 * P[d] + a[d]);
+                    if (qq < 0) out = true;
+                    q[d] = qq;
+                }
+                if (!out) s += w * rF[nix(F, q[0], q[1], q[2])];
+            }
+    fK[idx] = s / (1 << dm);
+}
+
+// Fine unknowns += multilinear interpolation of the coarse correction.
+HG_HD inline void prolong_node(const Geo& G, const Lev& K, const Lev& F, long idx,
+                               const double* eK, double* phiF) {
+    int p[3];
+    node_coords(F, idx, p);
+    if (!is_unknown(G, F, p)) return;
+    const int dm = G.dm;
+    int lo[3] = {0, 0, 0}, odd[3] = {0, 0, 0};
+    for (int d = 0; d < dm; ++d) {
+        lo[d] = p[d] >> 1;
+        odd[d] = p[d] & 1;
+    }
+    double s = 0.0;
+    for (int a2 = 0; a2 <= odd[2]; ++a2)
+        for (int a1 = 0; a1 <= odd[1]; ++a1)
+            for (int a0 = 0; a0 <= odd[0]; ++a0) {
+                const int a[3] = {a0, a1, a2};
+                int q[3] = {0, 0, 0};
+                double w = 1.0;
+                for (int d = 0; d < dm; ++d) {
+                    if (odd[d]) w *= 0.5;
+                    q[d] = node_wrap(G, K, d, lo[d] + a[d]);
+                }
+                s += w * eK[nix(K, q[0], q[1], q[2])];
+            }
+    phiF[idx] += s;
+}
+
+HG_HD inline void coarsen_sig_cell(const Geo& G, const Lev& F, const Lev& K, long idx,
+                                   double* sK) {
+    int c[3];
+    cell_coords(K, idx, c);
+    const int r0 = G.dm > 0 ? 2 : 1, r1 = G.dm > 1 ? 2 : 1, r2 = G.dm > 2 ? 2 : 1;
+    double s = 0.0;
+    for (int c2 = 0; c2 < r2; ++c2)
+        for (int c1 = 0; c1 < r1; ++c1)
+            for (int c0 = 0; c0 < r0; ++c0)
+                s += F.sig[cix(F, c[0] * r0 + c0, c[1] * r1 + c1, c[2] * r2 + c2)];
+    sK[idx] = s / (r0 * r1 * r2);
+}
+
+// Periodic image nodes take the value of the node they stand for; outflow nodes hold 0.
+HG_HD inline void finish_node(const Geo& G, const Lev& L, long idx, double* x) {
+    int p[3];
+    node_coords(L, idx, p);
+    if (is_unknown(G, L, p)) return;
+    int q[3] = {p[0], p[1], p[2]};
+    bool fixed = false;
+    for (int d = 0; d < G.dm; ++d) {
+        if (G.per[d])
+            q[d] = node_wrap(G, L, d, p[d]);
+        else if ((p[d] == 0 && G.dlo[d]) || (p[d] == L.n[d] && G.dhi[d]))
+            fixed = true;
+    }
+    x[idx] = fixed ? 0.0 : x[nix(L, q[0], q[1], q[2])];
+}
+
+// Node-centred divergence of beta0 U (u component-major over the cells; b0 null: 1), minus
+// the nodal source (nullable).
+HG_HD inline void divu_node(const Geo& G, const Lev& L, long idx, const double* u,
+                            const double* b0, const double* nodalrhs, double* rh) {
+    int p[3];
+    node_coords(L, idx, p);
+    const int dm = G.dm;
+    const long nc = ncells(L);
+    double s = 0.0;
+    for (int a = 0; a < (1 << dm); ++a) {
+        int c[3] = {0, 0, 0};
+        bool out = false;
+        for (int d = 0; d < dm; ++d) {
+            const int cw = cell_wrap(G, L, d, p[d] - ((a >> d) & 1));
+            if (cw < 0) out = true;
+            c[d] = cw;
+        }
+        if (out) continue;
+        const long ci = cix(L, c[0], c[1], c[2]);
+        const double bb = b0 ? b0[ci] : 1.0;
+        for (int d = 0; d < dm; ++d) s += (((a >> d) & 1) ? -1.0 : 1.0) * bb * u[d * nc + ci] / L.h[d];
+    }
+    s /= (1 << (dm - 1));
+    if (nodalrhs) s -= nodalrhs[idx];
+    rh[idx] = s;
+}
+
+// mkgphi: component d of the cell gradient of phi at cell idx.
+HG_HD inline double grad_cell(const Geo& G, const Lev& L, long idx, int d, const double* phi) {
+    int c[3];
+    cell_coords(L, idx, c);
+    const int dm = G.dm;
+    double s = 0.0;
+    for (int b = 0; b < (1 << dm); ++b) {
+        int m[3] = {0, 0, 0};
+        for (int e = 0; e < dm; ++e) m[e] = node_wrap(G, L, e, c[e] + ((b >> e) & 1));
+        s += (((b >> d) & 1) ? 1.0 : -1.0) * phi[nix(L, m[0], m[1], m[2])];
+    }
+    return s / (1 << (dm - 1)) / L.h[d];
+}
+
+// create_uvec_for_projection (Source/hgproject.f90:437-513) and the solver coefficient of a
+// cell: sigma = beta0 / rhohalf (beta0^2 / rhohalf with the alt energy fix outside the initial
+// and divu projections).
+HG_HD inline void uvec_cell(const Geo& G, long idx, long nc, int proj_type, double dt,
+                            double* unew, const double* uold, const double* gpi,
+                            const double* rhohalf, const double* b0, int alt, double* sig) {
+    for (int d = 0; d < G.dm; ++d) {
+        double& u = unew[d * nc + idx];
+        if (proj_type == kPressureIters) u = (u - uold[d * nc + idx]) / dt;
+        else if (proj_type == kRegular) u = u + dt * gpi[d * nc + idx] / rhohalf[idx];
+    }
+    const double bb = b0 ? b0[idx] : 1.0;
+    double rho = rhohalf[idx] / bb;
+    if (alt) rho /= bb;
+    sig[idx] = 1.0 / rho;
+}
+
+// hg_update (Source/hgproject.f90:867-1009) on one cell; gphi written to gpi per proj_type.
+HG_HD inline void update_cell(const Geo& G, const Lev& L, long idx, int proj_type, double dt,
+                              const double* phi, double* unew, const double* uold, double* gpi,
+                              const double* rhohalf, const double* b0, int alt) {
+    const long nc = ncells(L);
+    for (int d = 0; d < G.dm; ++d) {
+        double g = grad_cell(G, L, idx, d, phi);
+        if (alt) g *= b0 ? b0[idx] : 1.0;
+        double& u = unew[d * nc + idx];
+        u -= g / rhohalf[idx];
+        if (proj_type == kPressureIters) u = uold[d * nc + idx] + dt * u;
+        double& gp = gpi[d * nc + idx];
+        if (proj_type == kInitial || proj_type == kDivuIters) gp = 0.0;
+        else if (proj_type == kPressureIters) gp += g;
+        else if (proj_type == kRegular) gp = g / dt;
+    }
+}
+
+HG_HD inline void update_pi_node(const Lev& L, long idx, int proj_type, double dt,
+                                 const double* phi, double* pi) {
+    if (proj_type == kInitial || proj_type == kDivuIters) pi[idx] = 0.0;
+    else if (proj_type == kPressureIters) pi[idx] += phi[idx];
+    else if (proj_type == kRegular) pi[idx] = phi[idx] / dt;
+    (void)L;
+}
+
+// ---- the nodal V-cycle and the projection -----------------------------------------------------
+//
+// E provides: int nlev; Geo geo; bool singular; Lev lev(l);
+//   double* buf(l, which) node arrays kPhi, kF, kR per level;
+//   void defect(l, phi, f, r); void gs(l, phi, f, nu) (nu colour-ordered sweeps);
+//   void bottom_gs(l, phi, f, nu) (the same on the coarsest level, one launch on the GPU);
+//   void restrict_to(lc, rF, fK) and void prolong(lc, eK, phiF) between levels lc - 1 and lc;
+//   void zero(l, x); void finish(l, x); double unknown_max(l, x) (host value);
+//   void sub_unknown_mean(l, x) (device-side); int error();
+// and for the projection: void uvec(); int build_levels(); void divu(); void update(); level
+// 0's buffers hold phi (kPhi) and the right-hand side (kF).
+enum { kPhi = 0, kF = 1, kR = 2, kNumBufs = 3 };
+constexpr int kBottomSweeps = 60;
+
+template <class E>
+void vcycle(E& ex, int l, int nu1, int nu2) {
+    if (l == ex.nlev - 1) {
+        if (ex.singular) ex.sub_unknown_mean(l, ex.buf(l, kF));
+        ex.bottom_gs(l, ex.buf(l, kPhi), ex.buf(l, kF), kBottomSweeps);
+        if (ex.singular) ex.sub_unknown_mean(l, ex.buf(l, kPhi));
+        return;
+    }
+    ex.gs(l, ex.buf(l, kPhi), ex.buf(l, kF), nu1);
+    ex.defect(l, ex.buf(l, kPhi), ex.buf(l, kF), ex.buf(l, kR));
+    ex.restrict_to(l + 1, ex.buf(l, kR), ex.buf(l + 1, kF));
+    ex.zero(l + 1, ex.buf(l + 1, kPhi));
+    vcycle(ex, l + 1, nu1, nu2);
+    ex.prolong(l + 1, ex.buf(l + 1, kPhi), ex.buf(l, kPhi));
+    ex.gs(l, ex.buf(l, kPhi), ex.buf(l, kF), nu2);
+}
+
+struct SolveStats {
+    int status;
+    int cycles;
+    double fnorm, resid0, rel_resid;
+    int nhist;
+    double hist[64];
+};
+
+// Solve L phi = f on level 0 (phi: initial guess in buf(0, kPhi), f in buf(0, kF)).
+template <class E>
+int solve(E& ex, double rel_eps, int max_cycles, int nu1, int nu2, SolveStats* S) {
+    *S = SolveStats{};
+    if (ex.singular) ex.sub_unknown_mean(0, ex.buf(0, kF));
+    const double fnorm = ex.unknown_max(0, ex.buf(0, kF));
+    S->fnorm = fnorm;
+    if (!(fnorm > 0.0)) {
+        ex.zero(0, ex.buf(0, kPhi));
+        S->status = std::isnan(fnorm) ? -1 : 0;
+        return ex.error() ? ex.error() : S->status;
+    }
+    ex.defect(0, ex.buf(0, kPhi), ex.buf(0, kF), ex.buf(0, kR));
+    double res = ex.unknown_max(0, ex.buf(0, kR));
+    S->resid0 = res;
+    int it = 0;
+    while (!(res <= rel_eps * fnorm) && it < max_cycles && !std::isnan(res)) {
+        vcycle(ex, 0, nu1, nu2);
+        ++it;
+        ex.defect(0, ex.buf(0, kPhi), ex.buf(0, kF), ex.buf(0, kR));
+        res = ex.unknown_max(0, ex.buf(0, kR));
+        if (S->nhist < 64) S->hist[S->nhist++] = res / fnorm;
+        if (ex.error()) return ex.error();
+    }
+    S->cycles = it;
+    S->rel_resid = res / fnorm;
+    S->status = res <= rel_eps * fnorm ? 0 : (std::isnan(res) ? -1 : 1);
+    return ex.error() ? ex.error() : S->status;
+}
+
+// hgproject on one level with the caller's arrays loaded in the executor.
+template <class E>
+int project(E& ex, double rel_eps, int max_cycles, int nu1, int nu2, SolveStats* S) {
+    ex.uvec();                   // U per proj_type, sigma of level 0
+    int rc = ex.build_levels();  // coarse sigma
+    if (rc) return rc;
+    ex.divu();                   // buf(0, kF) = D(beta0 U) - nodalrhs
+    ex.zero(0, ex.buf(0, kPhi));
+    rc = solve(ex, rel_eps, max_cycles, nu1, nu2, S);
+    if (rc < 0) return rc;
+    const int status = rc;
+    ex.finish(0, ex.buf(0, kPhi));
+    ex.update();                 // U, gpi, pi
+    rc = ex.error();
+    return rc ? rc : status;
+}
+
+}  // namespace hg
+}  // namespace mac

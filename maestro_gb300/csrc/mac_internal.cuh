@@ -226,6 +226,7 @@ struct KrylovBufs {
 };
 
 struct AmrState;   // multi-level (AMR) hierarchy of a context (mac_amr.cu)
+struct HgState;    // nodal (HG) projection hierarchy of a context (hg_nodal.cu)
 
 }  // namespace mac
 
@@ -308,6 +309,7 @@ struct mac_ctx {
     int ktime_launches[8] = {};
 
     mac::AmrState* amr = nullptr;                 // finer AMR levels (mac_ctx_set_amr); null: one level
+    mac::HgState* hgs = nullptr;                  // nodal projection levels (first nodal call)
 
     size_t bytes_allocated = 0;
     std::vector<void*> allocations;
@@ -461,6 +463,8 @@ int level0_fp64_vcycle(mac_ctx* c);
 // Validate and store the finer levels' boxes (levels 1 .. nlev-1) and allocate their arrays.
 int amr_configure(mac_ctx* c, int nlev, const int* nboxes, const int* box_lo, const int* box_hi);
 void amr_release(mac_ctx* c);
+// ---- nodal projection (hg_nodal.cu) -----------------------------------------------------------
+void hg_release(mac_ctx* c);
 // Forward projection on the whole-domain arrays already in c->u / c->rho / c->phin; leaves the
 // level-0 coefficients and phi (level-0 layout) in place.
 int forward_projection(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats* st);

@@ -725,6 +725,7 @@ int ctx_alloc(mac_ctx* c) {
 
 void ctx_free(mac_ctx* c) {
     amr_release(c);
+    hg_release(c);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->xfer) cudaStreamSynchronize(c->xfer);
     if (c->aux) cudaStreamSynchronize(c->aux);

@@ -349,6 +349,20 @@ class MacProjector:
         self._check(rc, "mac_macproject_ml", st, strict)
         return st.as_dict()
 
+    def hgproject_dense(self, proj_type, dt, unew, uold, gpi, rhohalf, pi, beta0_cart=None,
+                        nodalrhs=None, dense_stencil=True, rel_eps=1e-12, strict=False):
+        """Nodal (HG) projection on this projector's domain (mac_hgproject_dense), device
+        pointers (ints): cell vector fields unew / uold / gpi (cells x dm, component-major),
+        rhohalf and beta0_cart cells, pi and nodalrhs nodes (cells + 1 per direction)."""
+        st = capi.MacStats()
+        v = ctypes.c_void_p
+        rc = capi.lib().mac_hgproject_dense(
+            self.ctx, int(proj_type), float(dt), int(bool(dense_stencil)), float(rel_eps), v(unew),
+            v(uold or 0), v(gpi), v(rhohalf), v(pi), v(beta0_cart or 0), v(nodalrhs or 0),
+            ctypes.byref(st))
+        self._check(rc, "mac_hgproject_dense", st, strict)
+        return st.as_dict()
+
     def adjoint_dense(self, u, rho, macrhs, beta0, beta0_edge, w, du, drinv=None, dbeta0=None,
                       dmacrhs=None, phi_out=None, strict=True):
         """Adjoint of the whole-domain projection on device pointers (see maestro_mac.h)."""

@@ -1,0 +1,86 @@
+"""Nodal (HG) projection on the GPU (mac_hgproject_dense) against the golden direct solves and the
+oracle: dense and cross stencils, 2-D and 3-D, periodic / wall / outflow faces, the initial,
+pressure-iteration and regular projections with beta0, a nodal source and the alt energy fix.
+The kernels' node arithmetic is the code tests/test_hg_host_exec.py runs on the host."""
+import numpy as np
+import pytest
+
+import oracle as O
+from maestro_gb300 import capi
+from maestro_gb300.inputs import BC_DIR, BC_NEU, BC_PER
+from maestro_gb300.macproject import BcTower, Layout, MacError, MacProjector
+from tests.test_oracle_hg import G, _unknown_mask, load_hg
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _run(shape, dx, bc_lo, bc_hi, proj, dt, unew, uold, gpi, rhohalf, pi, b0=None, nodalrhs=None,
+         dense=True, alt=False, rel_eps=1e-13):
+    dev = torch.device("cuda", 0)
+    t = lambda a: None if a is None else torch.from_numpy(  # noqa: E731
+        np.ascontiguousarray(np.asarray(a, dtype=np.float64).transpose())).to(dev)
+    tensors = [t(a) for a in (unew, uold, gpi, rhohalf, pi, b0, nodalrhs)]
+    ptr = lambda x: 0 if x is None else x.data_ptr()  # noqa: E731
+    dm = len(shape)
+    P = MacProjector(Layout(shape, [((0,) * dm, tuple(v - 1 for v in shape))]), dx,
+                     BcTower(bc_lo, bc_hi), precision="fp64",
+                     stream=torch.cuda.current_stream().cuda_stream, use_alt_energy_fix=int(alt))
+    try:
+        st = P.hgproject_dense(proj, dt, *[ptr(x) for x in tensors[:5]],
+                               beta0_cart=ptr(tensors[5]) or None,
+                               nodalrhs=ptr(tensors[6]) or None, dense_stencil=dense,
+                               rel_eps=rel_eps, strict=True)
+    finally:
+        P.close()
+    torch.cuda.synchronize()
+    back = lambda x: np.asfortranarray(x.cpu().numpy().transpose())  # noqa: E731
+    return back(tensors[0]), back(tensors[2]), back(tensors[4]), st
+
+
+@pytest.mark.parametrize("name", sorted(G.HG_CASES))
+def test_hgproject_matches_golden(name):
+    c = load_hg(name)
+    shape = c["rhohalf"].shape
+    u, gpi, pi, st = _run(shape, c["dx"], c["bc_lo"], c["bc_hi"], int(c["proj"]), float(c["dt"]),
+                          c["unew"], c["uold"], c["gpi"], c["rhohalf"], c["pi"],
+                          b0=c.get("beta0"), nodalrhs=c.get("nodalrhs"), dense=bool(c["dense"]),
+                          alt=bool(c["alt"]))
+    assert st["status"] == 0 and st["rel_resid"] <= 1e-13
+    assert np.max(np.abs(u - c["u_out"])) <= 1e-9 * np.max(np.abs(c["u_out"]))
+    assert np.max(np.abs(gpi - c["gpi_out"])) <= 1e-9 * max(np.max(np.abs(c["gpi_out"])),
+                                                             np.max(np.abs(c["gpi"])))
+    m = _unknown_mask(shape, c["dx"], c["bc_lo"], c["bc_hi"])
+    assert np.ptp((pi - c["pi_out"])[m]) <= 1e-9 * max(np.max(np.abs(c["pi_out"])), 1.0)
+
+
+@pytest.mark.parametrize("dense", [True, False])
+def test_hgproject_matches_oracle_3d(dense):
+    rng = np.random.default_rng(23)
+    shape = (32, 32, 32)
+    dx = (1 / 32,) * 3
+    bc = (BC_PER, BC_PER, BC_NEU)
+    unew = rng.standard_normal(shape + (3,))
+    gpi = rng.standard_normal(shape + (3,))
+    rho = np.exp(0.3 * rng.standard_normal(shape))
+    pi = np.zeros((33, 33, 33))
+    u, g, p, st = _run(shape, dx, bc, bc, O.HG_REGULAR, 0.01, unew, unew, gpi, rho, pi,
+                       dense=dense, rel_eps=O.EPS_HG)
+    assert st["status"] == 0 and st["rel_resid"] <= O.EPS_HG
+    uo, go, po, pho, so = O.hgproject(unew, unew, gpi, rho, pi, dx, bc, bc,
+                                      proj_type=O.HG_REGULAR, dt=0.01, dense=dense,
+                                      rel_eps=O.EPS_HG)
+    assert np.max(np.abs(u - uo)) <= 1e-9 * np.max(np.abs(uo))
+    assert np.max(np.abs(g - go)) <= 1e-9 * np.max(np.abs(go))
+
+
+def test_hgproject_rejects_bad_input():
+    shape = (8, 8)
+    dx = (1 / 8, 1 / 8)
+    bc = (BC_PER, BC_NEU)
+    z = np.zeros(shape + (2,))
+    rho = np.ones(shape)
+    rho[3, 3] = 0.0
+    with pytest.raises(MacError) as e:
+        _run(shape, dx, bc, bc, O.HG_INITIAL, 1.0, z, z, z, rho, np.zeros((9, 9)))
+    assert e.value.code == capi.MAC_ERR_BAD_DENSITY

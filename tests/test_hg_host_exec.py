@@ -1,0 +1,103 @@
+"""The library's nodal (HG) projection code executed on the host (no GPU).
+
+tests/csrc/hg_host.cpp runs the node / cell functions and the hg::project sequencing of
+maestro_gb300/csrc/hg_nodal.cuh -- what the CUDA kernels of hg_nodal.cu launch -- with loops, so
+the nodal arithmetic and the V-cycle are checked against the golden direct solves and the oracle
+before a GPU runs them."""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle as O
+from maestro_gb300.inputs import BC_DIR, BC_NEU, BC_PER
+from tests.test_oracle_hg import G, _unknown_mask, load_hg
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def host_lib(tmp_path_factory):
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    out = str(tmp_path_factory.mktemp("hgh") / "libhg_host.so")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-I",
+                    os.path.join(ROOT, "maestro_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "csrc", "hg_host.cpp"), "-o", out],
+                   check=True, capture_output=True)
+    L = ctypes.CDLL(out)
+    d = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    ci, cd = ctypes.c_int, ctypes.c_double
+    L.hgh_project.argtypes = [ci, ip, d, ip, ip, ip, ci, ci, cd, ci, cd, ci, ci, ci, d, d, d, d,
+                              d, d, d, d, d]
+    L.hgh_project.restype = ci
+    return L
+
+
+def run_host(L, shape, dx, bc_lo, bc_hi, proj, dt, unew, uold, gpi, rhohalf, pi, b0=None,
+             nodalrhs=None, dense=True, alt=False, rel_eps=1e-13, max_cycles=200):
+    dm = len(shape)
+    arr = lambda a: None if a is None else np.asfortranarray(a, dtype=np.float64)  # noqa: E731
+    ptr = lambda a: None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+    ia = lambda v: (ctypes.c_int * 3)(*(list(v) + [0] * (3 - len(v))))  # noqa: E731
+    u = arr(unew).copy(order="F")
+    g = arr(gpi).copy(order="F")
+    p = arr(pi).copy(order="F")
+    uo, rh, bb, nr = arr(uold), arr(rhohalf), arr(b0), arr(nodalrhs)
+    phi = np.zeros(tuple(v + 1 for v in shape), order="F")
+    st = (ctypes.c_double * 4)()
+    rc = L.hgh_project(dm, ia(shape), (ctypes.c_double * 3)(*(list(dx) + [1.0] * (3 - dm))),
+                       ia([b == BC_PER for b in bc_lo]), ia([b == BC_DIR for b in bc_lo]),
+                       ia([b == BC_DIR for b in bc_hi]), int(dense), int(proj), float(dt),
+                       int(alt), rel_eps, max_cycles, 2, 2, ptr(u), ptr(uo), ptr(g), ptr(rh),
+                       ptr(p), ptr(bb), ptr(nr), ptr(phi), st)
+    return rc, u, g, p, phi, list(st)
+
+
+@pytest.mark.parametrize("name", sorted(G.HG_CASES))
+def test_library_hg_code_on_host_matches_golden(host_lib, name):
+    c = load_hg(name)
+    shape = c["rhohalf"].shape
+    rc, u, gpi, pi, phi, st = run_host(host_lib, shape, c["dx"], c["bc_lo"], c["bc_hi"],
+                                       int(c["proj"]), float(c["dt"]), c["unew"], c["uold"],
+                                       c["gpi"], c["rhohalf"], c["pi"], b0=c.get("beta0"),
+                                       nodalrhs=c.get("nodalrhs"), dense=bool(c["dense"]),
+                                       alt=bool(c["alt"]))
+    assert rc == 0 and st[2] <= 1e-13, st
+    m = _unknown_mask(shape, c["dx"], c["bc_lo"], c["bc_hi"])
+    a, b = phi[m], c["phi_out"][m]
+    if BC_DIR not in c["bc_lo"] + c["bc_hi"]:
+        a, b = a - a.mean(), b - b.mean()
+    assert np.max(np.abs(a - b)) <= 1e-9 * np.max(np.abs(b))
+    assert np.max(np.abs(u - c["u_out"])) <= 1e-9 * np.max(np.abs(c["u_out"]))
+    assert np.max(np.abs(gpi - c["gpi_out"])) <= 1e-9 * max(np.max(np.abs(c["gpi_out"])),
+                                                             np.max(np.abs(c["gpi"])))
+    # pi: the golden one up to the constant phi is fixed to (singular problems)
+    dpi = (pi - c["pi_out"])[m]
+    assert np.ptp(dpi) <= 1e-9 * max(np.max(np.abs(c["pi_out"])), 1.0)
+
+
+@pytest.mark.parametrize("dense", [True, False])
+@pytest.mark.parametrize("shape,bc", [((32, 32), (BC_PER, BC_NEU)), ((16, 16, 16), (BC_PER, BC_PER, BC_NEU)),
+                                      ((24, 16), (BC_NEU, BC_DIR))])
+def test_library_hg_code_on_host_matches_oracle_at_eps_hg(host_lib, dense, shape, bc):
+    rng = np.random.default_rng(17)
+    dm = len(shape)
+    dx = tuple(1.0 / shape[0] for _ in shape)
+    bc_lo, bc_hi = bc, bc
+    unew = rng.standard_normal(shape + (dm,))
+    gpi = np.zeros(shape + (dm,))
+    rho = np.exp(0.3 * rng.standard_normal(shape))
+    pi = np.zeros(tuple(v + 1 for v in shape))
+    rc, u, g, p, phi, st = run_host(host_lib, shape, dx, bc_lo, bc_hi, O.HG_INITIAL, 1.0, unew,
+                                    unew, gpi, rho, pi, dense=dense, rel_eps=O.EPS_HG)
+    assert rc == 0 and st[2] <= O.EPS_HG
+    uo, go, po, pho, so = O.hgproject(unew, unew, gpi, rho, pi, dx, bc_lo, bc_hi,
+                                      proj_type=O.HG_INITIAL, dense=dense, rel_eps=O.EPS_HG)
+    # both at eps_hg = 1e-12 on the same system (different bottom solvers): within 1e-9
+    assert np.max(np.abs(u - uo)) <= 1e-9 * np.max(np.abs(uo))
