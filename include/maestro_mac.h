@@ -321,6 +321,21 @@ int mac_hgproject_dense(mac_ctx* ctx, int proj_type, double dt, int dense_stenci
                         mac_stats* stats);
 
 /*
+ * Nodal (HG) projection on the caller's boxes (the context's layout), the drop-in for hgproject
+ * (Source/hgproject.f90:32-264) on one level.  Per box b: unew[b], uold[b] (NULL array unless
+ * MAC_HG_PRESSURE_ITERS), gpi[b] cell fabs with dm components; rhohalf[b] and beta0_cart[b]
+ * (NULL array: beta0 = 1) cell fabs; pi[b] and nodalrhs[b] (NULL array: none) node fabs (one more
+ * entry than the box along every direction); each array with its ghost width.  The boxes' own
+ * cells of unew and gpi and their nodes of pi are written; ghosts are left as they came in.
+ * Other arguments as mac_hgproject_dense.
+ */
+int mac_hgproject(mac_ctx* ctx, int ptr_kind, int proj_type, double dt, int dense_stencil,
+                  double rel_eps, double* const* unew, int ng_u, const double* const* uold,
+                  int ng_uo, double* const* gpi, int ng_gp, const double* const* rhohalf,
+                  int ng_rho, double* const* pi, int ng_pi, const double* const* beta0_cart,
+                  int ng_b0, const double* const* nodalrhs, int ng_nr, mac_stats* stats);
+
+/*
  * Adjoint (reverse-mode derivative) of the whole-domain MAC projection; no counterpart in the
  * reference.  Forward map (beta0 form, p = 1 + use_alt_energy_fix):
  *   U_proj = U - c .* G phi,  A phi = f,  A = D diag(beta_f) G  (negated, alpha = 0),

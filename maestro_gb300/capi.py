@@ -34,7 +34,7 @@ EXPORTED = (
     "mac_macproject_dense", "mac_macproject_adjoint_dense", "mac_cell_to_edge",
     "mac_solve_small_noalloc", "mac_make_macrhs", "mac_make_macrhs_dense", "mac_make_at_halftime",
     "mac_macproject_cart", "mac_macproject_cart_dense", "mac_ctx_set_amr",
-    "mac_macproject_ml_dense", "mac_macproject_ml", "mac_hgproject_dense",
+    "mac_macproject_ml_dense", "mac_macproject_ml", "mac_hgproject_dense", "mac_hgproject",
 )
 MAC_NOALLOC_MAX_CELLS = 4096
 
@@ -199,6 +199,9 @@ def lib():
     L.mac_macproject_ml.restype = ci
     L.mac_hgproject_dense.argtypes = [vp, ci, cd, ci, cd, vp, vp, vp, vp, vp, vp, vp, P(MacStats)]
     L.mac_hgproject_dense.restype = ci
+    L.mac_hgproject.argtypes = [vp, ci, ci, cd, ci, cd, dpp, ci, dpp, ci, dpp, ci, dpp, ci, dpp, ci,
+                                dpp, ci, dpp, ci, P(MacStats)]
+    L.mac_hgproject.restype = ci
     _lib = L
     return L
 

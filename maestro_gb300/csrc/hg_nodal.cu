@@ -162,6 +162,29 @@ __global__ void k_hg_check(const double* rhohalf, const double* b0, int* flag, l
     }
 }
 
+// Caller fabs <-> whole-domain arrays, ncomp components (component stride `stride` in the
+// array, B.count in the fab); blockIdx.y is the fab.
+__global__ void k_hg_fabs_gather(hg::Geo G, hg::Lev L, const hg::Fab* T, int ncomp, long stride,
+                                 double* arr) {
+    const hg::Fab B = T[blockIdx.y];
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < B.count;
+         e += (long)gridDim.x * blockDim.x) {
+        const long t = hg::fab_target(G, L, B, e);
+        if (t < 0) continue;
+        for (int q = 0; q < ncomp; ++q) arr[q * stride + t] = B.src[q * B.count + e];
+    }
+}
+__global__ void k_hg_fabs_scatter(hg::Geo G, hg::Lev L, const hg::Fab* T, int ncomp, long stride,
+                                  const double* arr) {
+    const hg::Fab B = T[blockIdx.y];
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < B.count;
+         e += (long)gridDim.x * blockDim.x) {
+        const long t = hg::fab_target(G, L, B, e);
+        if (t < 0) continue;
+        for (int q = 0; q < ncomp; ++q) B.dst[q * B.count + e] = arr[q * stride + t];
+    }
+}
+
 inline int blocks_for(long n, int sms) {
     const long b = (n + kThreads - 1) / kThreads;
     const long cap = (long)std::max(1, sms) * 16;
@@ -186,6 +209,19 @@ struct HgState {
     int* flag = nullptr;
     int* h_flag = nullptr;
     std::vector<void*> allocs;
+    // per-box calls: whole-domain copies of the fields, fab tables, host staging
+    double* fu = nullptr;     // unew (dm components)
+    double* fuo = nullptr;    // uold
+    double* fg = nullptr;     // gpi
+    double* frho = nullptr;
+    double* fpi = nullptr;    // nodes
+    double* fb0 = nullptr;
+    double* fnr = nullptr;    // nodes
+    hg::Fab* h_tab = nullptr;
+    hg::Fab* d_tab = nullptr;
+    size_t tab_cap = 0;
+    double* staging = nullptr;
+    size_t staging_cap = 0;
 };
 
 void hg_release(mac_ctx* c) {
@@ -193,6 +229,9 @@ void hg_release(mac_ctx* c) {
     if (!H) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (void* p : H->allocs) cudaFree(p);
+    if (H->d_tab) cudaFree(H->d_tab);
+    if (H->staging) cudaFree(H->staging);
+    if (H->h_tab) cudaFreeHost(H->h_tab);
     if (H->h_out) cudaFreeHost(H->h_out);
     if (H->h_flag) cudaFreeHost(H->h_flag);
     delete H;
@@ -386,31 +425,12 @@ struct HgExec {
 
 }  // namespace
 
-}  // namespace mac
-
-using namespace mac;
-
-extern "C" {
-
-int mac_hgproject_dense(mac_ctx* c, int proj_type, double dt, int dense_stencil, double rel_eps,
-                        double* unew, const double* uold, double* gpi, const double* rhohalf,
-                        double* pi, const double* beta0_cart, const double* nodalrhs,
-                        mac_stats* stats) {
-    mac_stats local;
-    mac_stats* st = stats ? stats : &local;
-    std::memset(st, 0, sizeof(*st));
-    if (!c || !unew || !gpi || !rhohalf || !pi) return st->status = MAC_ERR_INVALID;
-    if (proj_type < hg::kInitial || proj_type > hg::kRegular) return st->status = MAC_ERR_INVALID;
-    if (proj_type == hg::kPressureIters && !uold) return st->status = MAC_ERR_INVALID;
-    if ((proj_type == hg::kPressureIters || proj_type == hg::kRegular) && !(dt > 0.0))
-        return st->status = MAC_ERR_INVALID;
-    // the colour-parallel sweeps need even periodic extents (same-colour nodes uncoupled)
-    for (int d = 0; d < c->dm; ++d)
-        if (c->bc_lo[d] == MAC_BC_PER && (c->n[d] & 1)) return st->status = MAC_ERR_UNSUPPORTED;
-    const auto t0 = std::chrono::steady_clock::now();
-    begin_call_stats(c, st);
-    int rc = hg_ensure(c);
-    if (rc) return st->status = rc;
+// The nodal projection on whole-domain device arrays (arguments validated by the caller); fills
+// the solve fields of *st and returns the status code.
+int hg_core(mac_ctx* c, int proj_type, double dt, int dense_stencil, double rel_eps,
+            double* unew, const double* uold, double* gpi, const double* rhohalf, double* pi,
+            const double* beta0_cart, const double* nodalrhs, mac_stats* st) {
+    int rc = MAC_OK;
     HgState* H = c->hgs;
     H->geo.dense = dense_stencil ? 1 : 0;
     HgExec ex{c, H, (int)H->L.size(), H->geo, !(H->geo.dlo[0] || H->geo.dhi[0] || H->geo.dlo[1] ||
@@ -461,10 +481,243 @@ int mac_hgproject_dense(mac_ctx* c, int proj_type, double dt, int dense_stencil,
     st->rel_resid = S.rel_resid;
     st->nhist = S.nhist;
     for (int q = 0; q < S.nhist && q < 64; ++q) st->hist[q] = S.hist[q];
+    return rc;
+}
+
+
+namespace {
+
+int hg_check_args(const mac_ctx* c, int proj_type, double dt, bool have_uold) {
+    if (proj_type < hg::kInitial || proj_type > hg::kRegular) return MAC_ERR_INVALID;
+    if (proj_type == hg::kPressureIters && !have_uold) return MAC_ERR_INVALID;
+    if ((proj_type == hg::kPressureIters || proj_type == hg::kRegular) && !(dt > 0.0))
+        return MAC_ERR_INVALID;
+    // the colour-parallel sweeps need even periodic extents (same-colour nodes uncoupled)
+    for (int d = 0; d < c->dm; ++d)
+        if (c->bc_lo[d] == MAC_BC_PER && (c->n[d] & 1)) return MAC_ERR_UNSUPPORTED;
+    return MAC_OK;
+}
+
+// Descriptor of box b of the context's layout as a fab with ng ghosts, cell- or node-centred.
+hg::Fab hg_fab(const mac_ctx* c, int b, int ng, int nodal) {
+    hg::Fab F{};
+    long cnt = 1;
+    for (int d = 0; d < 3; ++d) {
+        if (d >= c->dm) {
+            F.ext[d] = 1;
+            continue;
+        }
+        F.lo[d] = c->box_lo[3 * b + d] - c->g.domain_lo[d];
+        F.hi[d] = c->box_hi[3 * b + d] - c->g.domain_lo[d];
+        F.ext[d] = F.hi[d] - F.lo[d] + 1 + nodal + 2 * ng;
+        cnt *= F.ext[d];
+    }
+    F.ng = ng;
+    F.nodal = nodal;
+    F.count = cnt;
+    return F;
+}
+
+template <typename T>
+int hg_grow(T** p, size_t* cap, size_t need, bool pinned) {
+    if (need <= *cap) return MAC_OK;
+    if (*p) {
+        if (pinned)
+            cudaFreeHost(*p);
+        else
+            cudaFree(*p);
+    }
+    *p = nullptr;
+    *cap = 0;
+    const cudaError_t e = pinned ? cudaMallocHost((void**)p, need * sizeof(T))
+                                 : cudaMalloc((void**)p, need * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return MAC_ERR_ALLOC;
+    }
+    *cap = need;
+    return MAC_OK;
+}
+
+// Per-box entry: gather the fabs into whole-domain arrays, project, scatter unew, gpi and pi.
+int hg_fabs(mac_ctx* c, int ptr_kind, int proj_type, double dt, int dense_stencil, double rel_eps,
+            double* const* unew, int ng_u, const double* const* uold, int ng_uo,
+            double* const* gpi, int ng_gp, const double* const* rhohalf, int ng_rho,
+            double* const* pi, int ng_pi, const double* const* beta0_cart, int ng_b0,
+            const double* const* nodalrhs, int ng_nr, mac_stats* st) {
+    HgState* H = c->hgs;
+    const int dm = c->dm;
+    const int nb = c->g.nboxes;
+    const bool host = ptr_kind == MAC_PTR_HOST;
+    const long nc = H->L[0].nc, nn = H->L[0].nn;
+    int rc = MAC_OK;
+    if (!H->fu) {
+        rc = hg_alloc(H, &H->fu, (size_t)dm * nc);
+        if (!rc) rc = hg_alloc(H, &H->fuo, (size_t)dm * nc);
+        if (!rc) rc = hg_alloc(H, &H->fg, (size_t)dm * nc);
+        if (!rc) rc = hg_alloc(H, &H->frho, (size_t)nc);
+        if (!rc) rc = hg_alloc(H, &H->fpi, (size_t)nn);
+        if (!rc) rc = hg_alloc(H, &H->fb0, (size_t)nc);
+        if (!rc) rc = hg_alloc(H, &H->fnr, (size_t)nn);
+        if (rc) return rc;
+    }
+    // arrays of this call: (fabs, ng, nodal, ncomp, whole-domain array, scattered back)
+    struct Arr {
+        const double* const* fabs;
+        int ng, nodal, ncomp;
+        double* dst;
+        bool back;
+    };
+    Arr arrs[7] = {{(const double* const*)unew, ng_u, 0, dm, H->fu, true},
+                   {uold, ng_uo, 0, dm, H->fuo, false},
+                   {(const double* const*)gpi, ng_gp, 0, dm, H->fg, true},
+                   {rhohalf, ng_rho, 0, 1, H->frho, false},
+                   {(const double* const*)pi, ng_pi, 1, 1, H->fpi, true},
+                   {beta0_cart, ng_b0, 0, 1, H->fb0, false},
+                   {nodalrhs, ng_nr, 1, 1, H->fnr, false}};
+    size_t ntab = 0, nstage = 0;
+    for (const Arr& A : arrs) {
+        if (!A.fabs) continue;
+        ntab += nb;
+        for (int b = 0; b < nb; ++b) nstage += (size_t)hg_fab(c, b, A.ng, A.nodal).count * A.ncomp;
+    }
+    if (ntab > H->tab_cap) {
+        MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        size_t cap = H->tab_cap;
+        rc = hg_grow(&H->h_tab, &cap, ntab, true);
+        if (!rc) {
+            size_t cap2 = H->tab_cap;
+            rc = hg_grow(&H->d_tab, &cap2, ntab, false);
+        }
+        if (rc) return rc;
+        H->tab_cap = ntab;
+    }
+    if (host) {
+        MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        rc = hg_grow(&H->staging, &H->staging_cap, std::max<size_t>(nstage, 1), false);
+        if (rc) return rc;
+    }
+    size_t tcur = 0, scur = 0;
+    size_t tab_at[7] = {0, 0, 0, 0, 0, 0, 0};
+    const hg::Lev L0 = H->L[0].lev;
+    for (int k = 0; k < 7; ++k) {
+        const Arr& A = arrs[k];
+        if (!A.fabs) continue;
+        hg::Fab* T = H->h_tab + tcur;
+        long maxc = 1;
+        for (int b = 0; b < nb; ++b) {
+            hg::Fab F = hg_fab(c, b, A.ng, A.nodal);
+            const size_t elems = (size_t)F.count * A.ncomp;
+            if (host) {
+                double* region = H->staging + scur;
+                scur += elems;
+                MAC_CUDA_TRY(cudaMemcpyAsync(region, A.fabs[b], elems * sizeof(double),
+                                             cudaMemcpyHostToDevice, c->stream));
+                F.src = region;
+                F.dst = region;
+            } else {
+                F.src = A.fabs[b];
+                F.dst = const_cast<double*>(A.fabs[b]);
+            }
+            T[b] = F;
+            maxc = std::max(maxc, F.count);
+        }
+        MAC_CUDA_TRY(cudaMemcpyAsync(H->d_tab + tcur, T, (size_t)nb * sizeof(hg::Fab),
+                                     cudaMemcpyHostToDevice, c->stream));
+        const dim3 grid((unsigned)std::min<long>((maxc + kThreads - 1) / kThreads, 1024), (unsigned)nb);
+        k_hg_fabs_gather<<<grid, kThreads, 0, c->stream>>>(H->geo, L0, H->d_tab + tcur, A.ncomp,
+                                                           A.nodal ? nn : nc, A.dst);
+        MAC_CUDA_TRY(cudaGetLastError());
+        ++c->issued;
+        tab_at[k] = tcur;
+        tcur += (size_t)nb;
+    }
+    const int solve_rc = hg_core(c, proj_type, dt, dense_stencil, rel_eps, H->fu,
+                                 uold ? H->fuo : nullptr, H->fg, H->frho, H->fpi,
+                                 beta0_cart ? H->fb0 : nullptr, nodalrhs ? H->fnr : nullptr, st);
+    if (solve_rc != MAC_OK && solve_rc != MAC_ERR_NOT_CONVERGED) return solve_rc;
+    for (int k = 0; k < 7; ++k) {
+        const Arr& A = arrs[k];
+        if (!A.fabs || !A.back) continue;
+        long maxc = 1;
+        for (int b = 0; b < nb; ++b) maxc = std::max(maxc, H->h_tab[tab_at[k] + b].count);
+        const dim3 grid((unsigned)std::min<long>((maxc + kThreads - 1) / kThreads, 1024), (unsigned)nb);
+        k_hg_fabs_scatter<<<grid, kThreads, 0, c->stream>>>(H->geo, L0, H->d_tab + tab_at[k], A.ncomp,
+                                                            A.nodal ? nn : nc, A.dst);
+        MAC_CUDA_TRY(cudaGetLastError());
+        ++c->issued;
+        if (host)
+            for (int b = 0; b < nb; ++b) {
+                const hg::Fab& F = H->h_tab[tab_at[k] + b];
+                MAC_CUDA_TRY(cudaMemcpyAsync(const_cast<double*>(A.fabs[b]), F.src,
+                                             (size_t)F.count * A.ncomp * sizeof(double),
+                                             cudaMemcpyDeviceToHost, c->stream));
+            }
+    }
+    MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return solve_rc;
+}
+
+}  // namespace
+
+}  // namespace mac
+
+using namespace mac;
+
+extern "C" {
+
+int mac_hgproject_dense(mac_ctx* c, int proj_type, double dt, int dense_stencil, double rel_eps,
+                        double* unew, const double* uold, double* gpi, const double* rhohalf,
+                        double* pi, const double* beta0_cart, const double* nodalrhs,
+                        mac_stats* stats) {
+    mac_stats local;
+    mac_stats* st = stats ? stats : &local;
+    std::memset(st, 0, sizeof(*st));
+    if (!c || !unew || !gpi || !rhohalf || !pi) return st->status = MAC_ERR_INVALID;
+    int rc = hg_check_args(c, proj_type, dt, uold != nullptr);
+    if (rc) return st->status = rc;
+    const auto t0 = std::chrono::steady_clock::now();
+    begin_call_stats(c, st);
+    rc = hg_ensure(c);
+    if (!rc)
+        rc = hg_core(c, proj_type, dt, dense_stencil, rel_eps, unew, uold, gpi, rhohalf, pi,
+                     beta0_cart, nodalrhs, st);
     st->status = rc;
     st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     end_call_stats(c, st);
     report_call(c, "hgproject_dense", st);
+    return rc;
+}
+
+
+int mac_hgproject(mac_ctx* c, int ptr_kind, int proj_type, double dt, int dense_stencil,
+                  double rel_eps, double* const* unew, int ng_u, const double* const* uold,
+                  int ng_uo, double* const* gpi, int ng_gp, const double* const* rhohalf,
+                  int ng_rho, double* const* pi, int ng_pi, const double* const* beta0_cart,
+                  int ng_b0, const double* const* nodalrhs, int ng_nr, mac_stats* stats) {
+    mac_stats local;
+    mac_stats* st = stats ? stats : &local;
+    std::memset(st, 0, sizeof(*st));
+    if (!c || !unew || !gpi || !rhohalf || !pi) return st->status = MAC_ERR_INVALID;
+    if (ptr_kind != MAC_PTR_HOST && ptr_kind != MAC_PTR_DEVICE) return st->status = MAC_ERR_INVALID;
+    if (ng_u < 0 || ng_uo < 0 || ng_gp < 0 || ng_rho < 0 || ng_pi < 0 || ng_b0 < 0 || ng_nr < 0)
+        return st->status = MAC_ERR_INVALID;
+    for (int b = 0; b < c->g.nboxes; ++b)
+        if (!unew[b] || !gpi[b] || !rhohalf[b] || !pi[b] || (uold && !uold[b]) ||
+            (beta0_cart && !beta0_cart[b]) || (nodalrhs && !nodalrhs[b]))
+            return st->status = MAC_ERR_INVALID;
+    int rc = hg_check_args(c, proj_type, dt, uold != nullptr);
+    if (rc) return st->status = rc;
+    const auto t0 = std::chrono::steady_clock::now();
+    begin_call_stats(c, st);
+    rc = hg_ensure(c);
+    if (!rc)
+        rc = hg_fabs(c, ptr_kind, proj_type, dt, dense_stencil, rel_eps, unew, ng_u, uold, ng_uo,
+                     gpi, ng_gp, rhohalf, ng_rho, pi, ng_pi, beta0_cart, ng_b0, nodalrhs, ng_nr, st);
+    st->status = rc;
+    st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    end_call_stats(c, st);
+    report_call(c, "hgproject", st);
     return rc;
 }
 

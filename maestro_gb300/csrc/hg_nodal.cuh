@@ -371,6 +371,36 @@ HG_HD inline void update_pi_node(const Lev& L, long idx, int proj_type, double d
     (void)L;
 }
 
+// ---- caller fabs <-> whole-domain arrays --------------------------------------------------------
+//
+// One fab of the caller's layout: box [lo, hi] in cells, ng ghosts, cell- or node-centred
+// (nodal: one more entry along every active direction), components of `count` entries each.
+struct Fab {
+    const double* src;
+    double* dst;
+    int lo[3], hi[3];
+    int ext[3];
+    int ng;
+    int nodal;
+    long count;
+};
+
+// Whole-domain index (cells or nodes) of entry e of one component of fab B when it is the box's
+// own cell / node, else -1 (ghosts are neither read nor written).
+HG_HD inline long fab_target(const Geo& G, const Lev& L, const Fab& B, long e) {
+    int a[3];
+    a[0] = (int)(e % B.ext[0]);
+    const long r = e / B.ext[0];
+    a[1] = (int)(r % B.ext[1]);
+    a[2] = (int)(r / B.ext[1]);
+    int g[3] = {0, 0, 0};
+    for (int d = 0; d < G.dm; ++d) {
+        g[d] = B.lo[d] - B.ng + a[d];
+        if (g[d] < B.lo[d] || g[d] > B.hi[d] + B.nodal) return -1;
+    }
+    return B.nodal ? nix(L, g[0], g[1], g[2]) : cix(L, g[0], g[1], g[2]);
+}
+
 // ---- the nodal V-cycle and the projection -----------------------------------------------------
 //
 // E provides: int nlev; Geo geo; bool singular; Lev lev(l);

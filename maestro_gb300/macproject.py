@@ -363,6 +363,22 @@ class MacProjector:
         self._check(rc, "mac_hgproject_dense", st, strict)
         return st.as_dict()
 
+    def hgproject(self, proj_type, dt, unew, uold, gpi, rhohalf, pi, beta0_cart=None,
+                  nodalrhs=None, ng_u=1, ng_uo=1, ng_gp=1, ng_rho=1, ng_pi=1, ng_b0=1, ng_nr=1,
+                  dense_stencil=True, rel_eps=1e-12, strict=False):
+        """Nodal (HG) projection of per-box host fabs in place (mac_hgproject): unew, uold, gpi
+        cell fabs with dm components (lists over boxes), rhohalf / beta0_cart cell fabs, pi /
+        nodalrhs node fabs."""
+        opt = lambda a: None if a is None else _ptr_array(a)  # noqa: E731
+        st = capi.MacStats()
+        rc = capi.lib().mac_hgproject(
+            self.ctx, capi.MAC_PTR_HOST, int(proj_type), float(dt), int(bool(dense_stencil)),
+            float(rel_eps), _ptr_array(unew), ng_u, opt(uold), ng_uo, _ptr_array(gpi), ng_gp,
+            _ptr_array(rhohalf), ng_rho, _ptr_array(pi), ng_pi, opt(beta0_cart), ng_b0,
+            opt(nodalrhs), ng_nr, ctypes.byref(st))
+        self._check(rc, "mac_hgproject", st, strict)
+        return st.as_dict()
+
     def adjoint_dense(self, u, rho, macrhs, beta0, beta0_edge, w, du, drinv=None, dbeta0=None,
                       dmacrhs=None, phi_out=None, strict=True):
         """Adjoint of the whole-domain projection on device pointers (see maestro_mac.h)."""

@@ -185,4 +185,44 @@ int hgh_project(int dm, const int* n, const double* dx, const int* per, const in
     return rc;
 }
 
+
+// Caller fabs <-> a whole-domain cell / node array with the library's fab mapping; boxes as
+// lo[3], hi[3] per box; scatter: fabs <- array, else array <- fabs.
+void hgh_fabs(int dm, const int* n, const int* per, int nboxes, const int* boxes, int ng,
+              int nodal, int ncomp, int scatter, double* const* fabs, double* arr) {
+    hg::Geo G{};
+    G.dm = dm;
+    for (int d = 0; d < 3; ++d) G.per[d] = d < dm ? per[d] : 0;
+    hg::Lev L{};
+    for (int d = 0; d < 3; ++d) {
+        L.n[d] = d < dm ? n[d] : 1;
+        L.nn[d] = d < dm ? n[d] + 1 : 1;
+        L.h[d] = 1.0;
+    }
+    const long stride = nodal ? hg::nnodes(L) : hg::ncells(L);
+    for (int b = 0; b < nboxes; ++b) {
+        hg::Fab F{};
+        long cnt = 1;
+        for (int d = 0; d < 3; ++d) {
+            F.lo[d] = boxes[6 * b + d];
+            F.hi[d] = boxes[6 * b + 3 + d];
+            F.ext[d] = d < dm ? F.hi[d] - F.lo[d] + 1 + nodal + 2 * ng : 1;
+            cnt *= F.ext[d];
+        }
+        F.ng = ng;
+        F.nodal = nodal;
+        F.count = cnt;
+        for (long e = 0; e < cnt; ++e) {
+            const long t = hg::fab_target(G, L, F, e);
+            if (t < 0) continue;
+            for (int q = 0; q < ncomp; ++q) {
+                if (scatter)
+                    fabs[b][q * cnt + e] = arr[q * stride + t];
+                else
+                    arr[q * stride + t] = fabs[b][q * cnt + e];
+            }
+        }
+    }
+}
+
 }  // extern "C"

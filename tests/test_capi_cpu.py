@@ -79,6 +79,9 @@ def test_invalid_geometry_rejected_without_device(lib):
     assert lib.mac_macproject_cart(None, capi.MAC_PTR_HOST, None, 1, None, 1, None, 1, 1, 0,
                                    None, 0, None, 1, None) == capi.MAC_ERR_INVALID
     assert lib.mac_ctx_set_amr(None, 2, None, None, None) == capi.MAC_ERR_INVALID
+    assert lib.mac_hgproject_dense(None, 1, 1.0, 1, 0.0, *([None] * 7), None) == capi.MAC_ERR_INVALID
+    assert lib.mac_hgproject(None, capi.MAC_PTR_HOST, 1, 1.0, 1, 0.0, None, 1, None, 1, None, 1,
+                             None, 1, None, 1, None, 1, None, 1, None) == capi.MAC_ERR_INVALID
     assert lib.mac_macproject_ml_dense(None, None, None, None, None, None, None,
                                        None) == capi.MAC_ERR_INVALID
 

@@ -84,3 +84,42 @@ def test_hgproject_rejects_bad_input():
     with pytest.raises(MacError) as e:
         _run(shape, dx, bc, bc, O.HG_INITIAL, 1.0, z, z, z, rho, np.zeros((9, 9)))
     assert e.value.code == capi.MAC_ERR_BAD_DENSITY
+
+
+@pytest.mark.parametrize("name", ["hg2d_32", "hg3d_12"])
+def test_hgproject_on_host_fabs(name):
+    # the drop-in form: per-box host fabs (several boxes, ghost cells / nodes) of every field
+    from tests.test_hg_host_exec import make_fabs
+    c = load_hg(name)
+    shape = c["rhohalf"].shape
+    dm = len(shape)
+    per = [b == BC_PER for b in c["bc_lo"]]
+    half = tuple(v // 2 for v in shape)
+    lay = Layout.tiled(shape, half)
+    boxes = lay.boxes
+    fab = lambda a, nodal, ncomp=1: make_fabs(a, boxes, 1, nodal, per, ncomp)  # noqa: E731
+    unew, uold, gpi = fab(c["unew"], 0, dm), fab(c["uold"], 0, dm), fab(c["gpi"], 0, dm)
+    rho, b0 = fab(c["rhohalf"], 0), fab(c["beta0"], 0)
+    pi, nr = fab(c["pi"], 1), fab(c["nodalrhs"], 1)
+    P = MacProjector(lay, c["dx"], BcTower(c["bc_lo"], c["bc_hi"]), precision="fp64",
+                     use_alt_energy_fix=int(c["alt"]))
+    try:
+        st = P.hgproject(int(c["proj"]), float(c["dt"]), unew, uold, gpi, rho, pi, beta0_cart=b0,
+                         nodalrhs=nr, dense_stencil=bool(c["dense"]), rel_eps=1e-13,
+                         strict=True)
+    finally:
+        P.close()
+    assert st["status"] == 0
+    ref_u, ref_g = fab(c["u_out"], 0, dm), fab(c["gpi_out"], 0, dm)
+    ref_pi = fab(c["pi_out"], 1)
+    su = np.max(np.abs(c["u_out"]))
+    sg = max(np.max(np.abs(c["gpi_out"])), np.max(np.abs(c["gpi"])))
+    shift = None
+    for b, (lo, hi) in enumerate(boxes):
+        sl = tuple(slice(1, 1 + hi[d] - lo[d] + 1) for d in range(dm))
+        sn = tuple(slice(1, 1 + hi[d] - lo[d] + 2) for d in range(dm))
+        assert np.max(np.abs(unew[b][sl] - ref_u[b][sl])) <= 1e-9 * su
+        assert np.max(np.abs(gpi[b][sl] - ref_g[b][sl])) <= 1e-9 * sg
+        dpi = pi[b][sn] - ref_pi[b][sn]
+        shift = dpi.flat[0] if shift is None else shift
+        assert np.max(np.abs(dpi - shift)) <= 1e-9 * max(np.max(np.abs(c["pi_out"])), 1.0)

@@ -36,6 +36,8 @@ def host_lib(tmp_path_factory):
     L.hgh_project.argtypes = [ci, ip, d, ip, ip, ip, ci, ci, cd, ci, cd, ci, ci, ci, d, d, d, d,
                               d, d, d, d, d]
     L.hgh_project.restype = ci
+    L.hgh_fabs.argtypes = [ci, ip, ip, ci, ip, ci, ci, ci, ci, ctypes.POINTER(d), d]
+    L.hgh_fabs.restype = None
     return L
 
 
@@ -101,3 +103,53 @@ def test_library_hg_code_on_host_matches_oracle_at_eps_hg(host_lib, dense, shape
                                       proj_type=O.HG_INITIAL, dense=dense, rel_eps=O.EPS_HG)
     # both at eps_hg = 1e-12 on the same system (different bottom solvers): within 1e-9
     assert np.max(np.abs(u - uo)) <= 1e-9 * np.max(np.abs(uo))
+
+
+def make_fabs(arr, boxes, ng, nodal, per, ncomp=1):
+    """Per-box fabs (Fortran order, components last) cut from a whole-domain cell / node array;
+    ghosts wrapped where periodic, clamped elsewhere."""
+    dm = len(boxes[0][0])
+    full = np.asarray(arr)
+    ext = full.shape[:dm]
+    out = []
+    for lo, hi in boxes:
+        idx = []
+        for d in range(dm):
+            r = np.arange(lo[d] - ng, hi[d] + 1 + nodal + ng)
+            n = ext[d] - nodal
+            r = np.where(r < 0, r + n, r) if per[d] else np.clip(r, 0, ext[d] - 1)
+            r = np.where(r >= ext[d], r - n, r) if per[d] else r
+            idx.append(r)
+        sub = full[np.ix_(*idx)] if ncomp == 1 else full[np.ix_(*idx, np.arange(ncomp))]
+        out.append(np.asfortranarray(sub))
+    return out
+
+
+@pytest.mark.parametrize("nodal,ncomp", [(0, 2), (1, 1)])
+def test_hg_fab_mapping(host_lib, nodal, ncomp):
+    shape = (16, 12)
+    per = [True, False]
+    boxes = [((0, 0), (7, 5)), ((8, 0), (15, 5)), ((0, 6), (7, 11)), ((8, 6), (15, 11))]
+    rng = np.random.default_rng(2)
+    ashape = tuple(v + nodal for v in shape) + ((ncomp,) if ncomp > 1 else ())
+    arr = np.asfortranarray(rng.standard_normal(ashape))
+    fabs = make_fabs(arr, boxes, 2, nodal, per, ncomp)
+    flat = np.array([list(lo) + [0] + list(hi) + [0] for lo, hi in boxes], dtype=np.int32).ravel()
+    ip = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))  # noqa: E731
+    n = np.array(list(shape) + [1], dtype=np.int32)
+    pe = np.array([1, 0, 0], dtype=np.int32)
+    got = np.zeros_like(arr, order="F")
+    host_lib.hgh_fabs(2, ip(n), ip(pe), len(boxes), ip(flat), 2, nodal, ncomp, 0,
+                      O._ptr_array(fabs), got.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    # every cell / node of the domain belongs to some box (the last node row of a periodic
+    # direction is the image and is written too)
+    np.testing.assert_array_equal(got, arr)
+    back = [np.zeros_like(f, order="F") for f in fabs]
+    host_lib.hgh_fabs(2, ip(n), ip(pe), len(boxes), ip(flat), 2, nodal, ncomp, 1,
+                      O._ptr_array(back), arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    for f, g, (lo, hi) in zip(back, fabs, boxes):
+        sl = tuple(slice(2, 2 + hi[d] - lo[d] + 1 + nodal) for d in range(2))
+        np.testing.assert_array_equal(f[sl], g[sl])
+        mask = np.ones(f.shape, dtype=bool)
+        mask[sl] = False
+        assert np.all(f[mask] == 0.0)
