@@ -356,7 +356,8 @@ def make_amr_case(name: str = "amr", dm: int = 2, n0=(32, 32), boxes=None, H_fra
     with cell_to_edge edges, U the Fourier field of `make_case` sampled on each level's faces,
     macrhs = beta0 (S - Sbar) with S smooth and Sbar its layer mean on each level.  The density of
     covered cells is the mean of their children (the state after MAESTRO's average-down).
-    bc: "wall" (periodic horizontally, slip walls vertically) or "periodic"."""
+    bc: "wall" (periodic horizontally, slip walls vertically), "periodic", or "outflow" (periodic
+    horizontally, a slip wall below and an outflow face, phi = 0, above)."""
     n0 = tuple(int(v) for v in n0)
     assert len(n0) == dm
     boxes = [[]] + [list(b) for b in (boxes or [])[1:]] if boxes else [[]]
@@ -364,7 +365,7 @@ def make_amr_case(name: str = "amr", dm: int = 2, n0=(32, 32), boxes=None, H_fra
     dx0 = tuple(1.0 / n0[0] for _ in range(dm))
     bc_v = BC_PER if bc == "periodic" else BC_NEU
     bc_lo = tuple([BC_PER] * (dm - 1) + [bc_v])
-    bc_hi = bc_lo
+    bc_hi = tuple([BC_PER] * (dm - 1) + [BC_DIR]) if bc == "outflow" else bc_lo
     rho, b0, b0e, umac, macrhs, phi0 = [], [], [], [], [], []
     # U normalisation from level 0 so all levels carry the same field
     norms = []
@@ -412,6 +413,9 @@ AMR_CASES = {
     # 3-D, two levels, two boxes
     "amr3d_16": dict(dm=3, n0=(16, 16, 16), boxes=[[], [((8, 8, 8), (23, 23, 23)),
                                                           ((0, 0, 24), (7, 31, 31))]]),
+    # outflow (Dirichlet) top with a fine box against it, three levels
+    "amr2d_outflow": dict(dm=2, n0=(32, 16), bc="outflow",
+                          boxes=[[], [((16, 8), (47, 31))], [((40, 24), (79, 63))]]),
 }
 
 
