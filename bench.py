@@ -46,6 +46,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default=CONFIG_KEY)
+    ap.add_argument("--workload", default="mac", choices=["mac", "amr", "hg"],
+                    help="mac: the MAC projection headline (default); amr: the two-level "
+                         "projection; hg: the nodal projection")
     ap.add_argument("--e2e-steps", type=int, default=24)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
@@ -251,12 +254,178 @@ def run_reference(args, rank, world):
     return 0
 
 
+
+# ---- the other rows: multi-level and nodal projections (run with --workload) -------------------
+AMR_N0, AMR_BOX, AMR_FINE = (128, 128, 128), (64, 64, 64), ((64, 64, 64), (191, 191, 191))
+HG_N, HG_BOX = (256, 256, 256), (128, 128, 128)
+
+
+def _amr_inputs(n0, fine, seed):
+    from maestro_gb300.inputs import make_amr_case
+    return make_amr_case(name="amr_bench", dm=3, n0=n0, boxes=[[], [fine]], kmax=4, noise=0.05,
+                         seed=seed)
+
+
+def _hg_inputs(n, seed):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    z = (np.arange(n[-1]) + 0.5) / n[-1]
+    rho0 = 1e7 * np.exp(-z / 0.25)
+    rho = rho0.reshape(1, 1, -1) * np.exp(0.01 * rng.standard_normal(n))
+    u = 1e6 * rng.standard_normal(tuple(n) + (3,))
+    gpi = np.zeros(tuple(n) + (3,))
+    b0 = np.broadcast_to((rho0 ** (1 / 1.4)).reshape(1, 1, -1), n).copy()
+    pi = np.zeros(tuple(v + 1 for v in n))
+    return dict(unew=u, gpi=gpi, rhohalf=rho, beta0=b0, pi=pi)
+
+
+def run_extra(args, rank, world, local):
+    """One JSON line for the multi-level (amr) or nodal (hg) projection."""
+    import numpy as np
+    import oracle as O
+    if args.workload == "amr":
+        metric = "two-level MAC solves/s (128^3 base + 128^3 patch at 2x) to MAESTRO's tolerance"
+        cfg = {"workload": "amr_2lev", "n0": list(AMR_N0), "box": list(AMR_BOX),
+               "fine_box": [list(AMR_FINE[0]), list(AMR_FINE[1])], "rel_eps": O.ml_rel_eps(2)}
+        sample_n0, sample_fine = (32, 32, 32), ((16, 16, 16), (47, 47, 47))
+        full_cells = np.prod(AMR_N0) + np.prod([b - a + 1 for a, b in zip(*AMR_FINE)])
+        sample_cells = np.prod(sample_n0) + np.prod([b - a + 1 for a, b in zip(*sample_fine)])
+    else:
+        metric = "nodal (HG) projections/s at 256^3 (dense stencil, regular time step) to 1e-12"
+        cfg = {"workload": "hg_256", "n": list(HG_N), "box": list(HG_BOX), "rel_eps": O.EPS_HG,
+               "stencil": "dense"}
+        full_cells = np.prod(HG_N)
+        sample_n = (64, 64, 64)
+        sample_cells = np.prod(sample_n)
+    threads = host_cores()
+    sample_in = (_amr_inputs(sample_n0, sample_fine, args.seed) if args.workload == "amr"
+                 else _hg_inputs(sample_n, args.seed))
+
+    def cpu_step():
+        t = time.perf_counter()
+        if args.workload == "amr":
+            c = sample_in
+            st = O.macproject_ml(c.umac, c.phi0, c.rho, c.dx0, c.bc_lo, c.bc_hi, c.boxes,
+                                 macrhs=c.macrhs, beta0=c.beta0, beta0_edge=c.beta0_edge,
+                                 threads=threads)[2]
+        else:
+            h = sample_in
+            bc = (O.BC_PER, O.BC_PER, O.BC_NEU)
+            st = O.hgproject(h["unew"], h["unew"], h["gpi"], h["rhohalf"], h["pi"],
+                             tuple(1.0 / v for v in sample_n), bc, bc, proj_type=O.HG_REGULAR,
+                             dt=1e-3, beta0_cart=h["beta0"], threads=threads)[4]
+        assert st["status"] == 0
+        return time.perf_counter() - t
+
+    sample = (f"per step one solve of the same workload at {sample_cells / full_cells:.4g} of the "
+              f"cells, scaled by the cell ratio; the C++/OpenMP oracle (FBoxLib unbuildable)")
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        for _ in range(args.warmup):
+            cpu_step()
+        secs = sum(cpu_step() for _ in range(args.steps))
+        value = args.steps / secs * (sample_cells / full_cells)
+        print(json.dumps({
+            "impl": "reference", "metric": metric, "value": value, "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": cfg,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}))
+        return 0
+
+    import torch
+    from maestro_gb300.build import build
+    from maestro_gb300.macproject import BcTower, Layout, MacProjector
+    build()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    to_dev = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a).transpose())).to(dev)  # noqa: E731
+    nsteps = args.steps + args.warmup
+    stats = []
+    if args.workload == "amr":
+        c = _amr_inputs(AMR_N0, AMR_FINE, args.seed + rank)
+        lay = Layout.tiled(c.n0, AMR_BOX)
+        P = MacProjector(lay, c.dx0, BcTower(c.bc_lo, c.bc_hi), precision="fp64",
+                         stream=stream.cuda_stream)
+        P.set_amr(c.boxes)
+        u0 = [[to_dev(x) for x in c.umac[l]] for l in range(2)]
+        rho = [to_dev(r) for r in c.rho]
+        rhs = [to_dev(m) for m in c.macrhs]
+        b0 = [torch.from_numpy(b).to(dev) for b in c.beta0]
+        b0e = [torch.from_numpy(b).to(dev) for b in c.beta0_edge]
+        work = [([[x.clone() for x in u0[l]] for l in range(2)],
+                 [torch.zeros_like(r) for r in rho]) for _ in range(nsteps)]
+
+        def one(k):
+            u, phi = work[k]
+            return P.macproject_ml_dense([[x.data_ptr() for x in u[l]] for l in range(2)],
+                                         [p.data_ptr() for p in phi], [r.data_ptr() for r in rho],
+                                         macrhs=[m.data_ptr() for m in rhs],
+                                         beta0=[b.data_ptr() for b in b0],
+                                         beta0_edge=[b.data_ptr() for b in b0e], strict=True)
+    else:
+        h = _hg_inputs(HG_N, args.seed + rank)
+        lay = Layout.tiled(HG_N, HG_BOX)
+        P = MacProjector(lay, tuple(1.0 / v for v in HG_N),
+                         BcTower((-1, -1, 2), (-1, -1, 2)), precision="fp64",
+                         stream=stream.cuda_stream)
+        fields = {k: to_dev(v) for k, v in h.items()}
+        work = [(fields["unew"].clone(), fields["gpi"].clone(), fields["pi"].clone())
+                for _ in range(nsteps)]
+
+        def one(k):
+            u, g, pi = work[k]
+            return P.hgproject_dense(4, 1e-3, u.data_ptr(), u.data_ptr(), g.data_ptr(),
+                                     fields["rhohalf"].data_ptr(), pi.data_ptr(),
+                                     beta0_cart=fields["beta0"].data_ptr(), rel_eps=O.EPS_HG,
+                                     strict=True)
+    for k in range(args.warmup):
+        one(k)
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(args.warmup, nsteps):
+        stats.append(one(k))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    P.close()
+    K = args.steps
+    value = world * K / (ms / 1e3)
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        secs = cpu_step()
+        cpu = {"value": (sample_cells / full_cells) / secs, "unit": UNIT, "cores": threads,
+               "kind": "port", "sample": sample}
+    out = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+           "warmup": args.warmup, "ms_per_step": ms / K, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+           "config": cfg, "roofline": None, "cpu_baseline": cpu, "e2e": None,
+           "gpu_launches": sum(s["launches"] for s in stats),
+           "vcycles": stats[-1]["vcycles"], "rel_resid": max(s["rel_resid"] for s in stats),
+           "clocks": ck}
+    if rank == 0:
+        print(json.dumps(out))
+    return 0
+
+
 # ---- our arm ----------------------------------------------------------------------------------
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.workload != "mac":
+        return run_extra(args, rank, world, local)
     if args.impl == "reference":
         return run_reference(args, rank, world)
 
