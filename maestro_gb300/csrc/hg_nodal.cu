@@ -74,7 +74,8 @@ __global__ void k_hg_bottom(hg::Geo G, hg::Lev L, double* phi, const double* f, 
     for (int s = 0; s < nu; ++s)
         for (int colour = 0; colour < (1 << G.dm); ++colour) {
             if (active)
-                for (long idx = start; idx < N; idx += step) hg::gs_node(G, L, idx, colour, phi, f);
+                for (long idx = start; idx < hg::colour_count(G, L, colour); idx += step)
+                    hg::gs_node(G, L, idx, colour, phi, f);
             __syncthreads();
         }
 }
@@ -284,6 +285,7 @@ int hg_ensure(mac_ctx* c) {
         for (int b = 0; b < hg::kNumBufs && !rc; ++b) rc = hg_alloc(H, &S.buf[b], (size_t)S.nn);
         if (rc) break;
         S.lev.sig = S.sig;
+        hg::set_dense_weights(c->dm, S.lev);
         H->L.push_back(S);
         bool more = (int)H->L.size() < hg::kMaxLevels;
         for (int d = 0; d < c->dm; ++d) more = more && n[d] % 2 == 0 && n[d] >= 4;
@@ -345,7 +347,8 @@ struct HgExec {
     void gs(int l, double* phi, const double* f, int nu) {
         for (int s = 0; s < nu; ++s)
             for (int colour = 0; colour < (1 << geo.dm); ++colour) {
-                k_hg_gs<<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), colour, phi, f, nn(l));
+                const long m = hg::colour_count(geo, lev(l), colour);
+                k_hg_gs<<<blocks(m), kThreads, 0, c->stream>>>(geo, lev(l), colour, phi, f, m);
                 launched();
             }
     }

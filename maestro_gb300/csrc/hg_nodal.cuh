@@ -53,7 +53,25 @@ struct Lev {
     int nn[3];         // node storage (n + 1 along active directions)
     double h[3];
     const double* sig; // cell coefficients
+    // dense stencil: finite-element weight of a cell between its corners a and b, which depends
+    // on a ^ b only (set by set_dense_weights)
+    double kw[8];
 };
+
+// kw[x] = sum_d h_d^-2 S(x_d) prod_{e != d} M(x_e) with S(0) = 1, S(1) = -1, M(0) = 1/3,
+// M(1) = 1/6 (x_d = 1: the two corners differ along d).
+HG_HD inline void set_dense_weights(int dm, Lev& L) {
+    for (int x = 0; x < 8; ++x) {
+        double k = 0.0;
+        for (int d = 0; d < dm; ++d) {
+            double t = (((x >> d) & 1) ? -1.0 : 1.0) / (L.h[d] * L.h[d]);
+            for (int e = 0; e < dm; ++e)
+                if (e != d) t *= ((x >> e) & 1) ? 1.0 / 6.0 : 1.0 / 3.0;
+            k += t;
+        }
+        L.kw[x] = x < (1 << dm) ? k : 0.0;
+    }
+}
 
 HG_HD inline long nix(const Lev& L, int i, int j, int k) {
     return (long)i + (long)L.nn[0] * ((long)j + (long)L.nn[1] * k);
@@ -108,38 +126,30 @@ HG_HD inline void node_op(const Geo& G, const Lev& L, const int p[3], const doub
     const int dm = G.dm;
     double dK = 0.0, oK = 0.0;
     if (G.dense) {
-        const double Mw[2][2] = {{1.0 / 3.0, 1.0 / 6.0}, {1.0 / 6.0, 1.0 / 3.0}};
         const long pi = nix(L, p[0], p[1], p[2]);
-        for (int a = 0; a < (1 << dm); ++a) {
-            int c[3] = {0, 0, 0}, loc[3] = {0, 0, 0};
+        for (int a = 0; a < (1 << dm); ++a) {   // a: the corner of cell c that p is
+            int c[3] = {0, 0, 0};
             bool out = false;
             for (int d = 0; d < dm; ++d) {
-                loc[d] = (a >> d) & 1;
-                const int cw = cell_wrap(G, L, d, p[d] - loc[d]);
+                const int cw = cell_wrap(G, L, d, p[d] - ((a >> d) & 1));
                 if (cw < 0) out = true;
                 c[d] = cw;
             }
             if (out) continue;
             const double s = L.sig[cix(L, c[0], c[1], c[2])];
+            double acc = 0.0;
             for (int b = 0; b < (1 << dm); ++b) {
-                int m[3] = {0, 0, 0}, ml[3] = {0, 0, 0};
-                for (int d = 0; d < dm; ++d) {
-                    ml[d] = (b >> d) & 1;
-                    m[d] = node_wrap(G, L, d, c[d] + ml[d]);
-                }
-                double k = 0.0;
-                for (int d = 0; d < dm; ++d) {
-                    double t = (loc[d] == ml[d] ? 1.0 : -1.0) / (L.h[d] * L.h[d]);
-                    for (int e = 0; e < dm; ++e)
-                        if (e != d) t *= Mw[loc[e]][ml[e]];
-                    k += t;
-                }
+                if (b == a) continue;
+                int m[3] = {0, 0, 0};
+                for (int d = 0; d < dm; ++d) m[d] = node_wrap(G, L, d, c[d] + ((b >> d) & 1));
                 const long mi = nix(L, m[0], m[1], m[2]);
-                if (mi == pi)
-                    dK += s * k;
+                if (mi == pi)   // a periodic wrap of extent 1 folds a corner onto p
+                    dK += s * L.kw[a ^ b];
                 else
-                    oK -= s * k * phi[mi];
+                    acc += L.kw[a ^ b] * phi[mi];
             }
+            dK += s * L.kw[0];
+            oK -= s * acc;
         }
         diag = -dK;
         off = -oK;
@@ -188,13 +198,30 @@ HG_HD inline void defect_node(const Geo& G, const Lev& L, long idx, const double
     r[idx] = f[idx] - (dg * phi[idx] - off);
 }
 
-HG_HD inline void gs_node(const Geo& G, const Lev& L, long idx, int colour, double* phi,
+// Nodes of one colour (parity pattern `colour` of the node coordinates): how many, and the k-th.
+HG_HD inline long colour_count(const Geo& G, const Lev& L, int colour) {
+    long m = 1;
+    for (int d = 0; d < G.dm; ++d) m *= (L.nn[d] - ((colour >> d) & 1) + 1) / 2;
+    return m;
+}
+HG_HD inline void colour_node(const Geo& G, const Lev& L, int colour, long k, int p[3]) {
+    p[0] = p[1] = p[2] = 0;
+    for (int d = 0; d < G.dm; ++d) {
+        const int b = (colour >> d) & 1;
+        const long m = (L.nn[d] - b + 1) / 2;
+        p[d] = 2 * (int)(k % m) + b;
+        k /= m;
+    }
+}
+
+// Gauss-Seidel update of the k-th node of a colour (nodes of one colour share no cell, so a
+// colour updates in parallel).
+HG_HD inline void gs_node(const Geo& G, const Lev& L, long k, int colour, double* phi,
                           const double* f) {
     int p[3];
-    node_coords(L, idx, p);
-    int col = 0;
-    for (int d = 0; d < G.dm; ++d) col |= (p[d] & 1) << d;
-    if (col != colour || !is_unknown(G, L, p)) return;
+    colour_node(G, L, colour, k, p);
+    if (!is_unknown(G, L, p)) return;
+    const long idx = nix(L, p[0], p[1], p[2]);
     double dg, off;
     node_op(G, L, p, phi, dg, off);
     phi[idx] = (f[idx] + off) / dg;

@@ -48,8 +48,10 @@ struct HostExec {
     }
     void gs(int l, double* phi, const double* f, int nu) {
         for (int s = 0; s < nu; ++s)
-            for (int colour = 0; colour < (1 << geo.dm); ++colour)
-                for (long i = 0; i < nn(l); ++i) hg::gs_node(geo, L[l].lev, i, colour, phi, f);
+            for (int colour = 0; colour < (1 << geo.dm); ++colour) {
+                const long m = hg::colour_count(geo, L[l].lev, colour);
+                for (long i = 0; i < m; ++i) hg::gs_node(geo, L[l].lev, i, colour, phi, f);
+            }
     }
     void bottom_gs(int l, double* phi, const double* f, int nu) { gs(l, phi, f, nu); }
     void restrict_to(int lc, const double* rF, double* fK) {
@@ -161,7 +163,10 @@ int hgh_project(int dm, const int* n, const double* dx, const int* per, const in
             h[d] *= 2;
         }
     }
-    for (HostLevel& S : E.L) S.lev.sig = S.sig.data();
+    for (HostLevel& S : E.L) {
+        S.lev.sig = S.sig.data();
+        hg::set_dense_weights(dm, S.lev);
+    }
     E.nlev = (int)E.L.size();
     E.proj_type = proj_type;
     E.dt = dt;
