@@ -140,3 +140,13 @@ def test_fab_gather_and_scatter_of_a_fine_level(host_lib, dir_):
         mask = np.ones(f.shape, dtype=bool)
         mask[sl] = False
         assert np.all(f[mask] == 0.0)
+
+
+def test_library_amr_code_reports_a_nonfinite_input(host_lib):
+    # a NaN velocity reaches the right-hand side: the driver stops with its non-finite status
+    # (the C entry turns it into MAC_ERR_NONFINITE) instead of cycling on NaNs
+    c = load_amr("amr2d_32")
+    c["umac"] = [[np.array(x, order="F") for x in c["umac"][l]] for l in range(c["nlev"])]
+    c["umac"][1][0][30, 20] = np.nan
+    rc, u, phi, st = run_host(host_lib, c, 1e-10)
+    assert rc < 0

@@ -153,3 +153,14 @@ def test_hg_fab_mapping(host_lib, nodal, ncomp):
         mask = np.ones(f.shape, dtype=bool)
         mask[sl] = False
         assert np.all(f[mask] == 0.0)
+
+
+def test_library_hg_code_reports_a_nonfinite_input(host_lib):
+    shape = (16, 16)
+    dx = (1 / 16, 1 / 16)
+    bc = (BC_PER, BC_NEU)
+    u = np.zeros(shape + (2,))
+    u[5, 5, 0] = np.nan
+    rc, *_ = run_host(host_lib, shape, dx, bc, bc, O.HG_INITIAL, 1.0, u, u, np.zeros_like(u),
+                      np.ones(shape), np.zeros((17, 17)))
+    assert rc < 0
