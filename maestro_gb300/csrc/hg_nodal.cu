@@ -19,29 +19,32 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kReduceBlocks = 1024;
+constexpr int kMixedInner = 2;   // FP32 V-cycles per FP64 refinement step of the mixed solve
 
 #define HG_LOOP(N) for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < (N); \
                         idx += (long)gridDim.x * blockDim.x)
 
-__global__ void k_hg_defect(hg::Geo G, hg::Lev L, const double* phi, const double* f, double* r,
-                            long N) {
+template <typename T>
+__global__ void k_hg_defect(hg::Geo G, hg::LevT<T> L, const T* phi, const T* f, T* r, long N) {
     HG_LOOP(N) hg::defect_node(G, L, idx, phi, f, r);
 }
-__global__ void k_hg_gs(hg::Geo G, hg::Lev L, int colour, double* phi, const double* f, long N) {
+template <typename T>
+__global__ void k_hg_gs(hg::Geo G, hg::LevT<T> L, int colour, T* phi, const T* f, long N) {
     HG_LOOP(N) hg::gs_node(G, L, idx, colour, phi, f);
 }
-__global__ void k_hg_restrict(hg::Geo G, hg::Lev F, hg::Lev K, const double* rF, double* fK,
-                              long N) {
+template <typename T>
+__global__ void k_hg_restrict(hg::Geo G, hg::LevT<T> F, hg::LevT<T> K, const T* rF, T* fK, long N) {
     HG_LOOP(N) hg::restrict_node(G, F, K, idx, rF, fK);
 }
-__global__ void k_hg_prolong(hg::Geo G, hg::Lev K, hg::Lev F, const double* eK, double* phiF,
-                             long N) {
+template <typename T>
+__global__ void k_hg_prolong(hg::Geo G, hg::LevT<T> K, hg::LevT<T> F, const T* eK, T* phiF, long N) {
     HG_LOOP(N) hg::prolong_node(G, K, F, idx, eK, phiF);
 }
 __global__ void k_hg_coarsen(hg::Geo G, hg::Lev F, hg::Lev K, double* sK, long N) {
     HG_LOOP(N) hg::coarsen_sig_cell(G, F, K, idx, sK);
 }
-__global__ void k_hg_finish(hg::Geo G, hg::Lev L, double* x, long N) {
+template <typename T>
+__global__ void k_hg_finish(hg::Geo G, hg::LevT<T> L, T* x, long N) {
     HG_LOOP(N) hg::finish_node(G, L, idx, x);
 }
 __global__ void k_hg_uvec(hg::Geo G, long nc, int proj_type, double dt, double* unew,
@@ -65,7 +68,8 @@ __global__ void k_hg_update_pi(hg::Lev L, int proj_type, double dt, const double
 
 // nu colour-ordered Gauss-Seidel sweeps of the coarsest level in one block.  An odd periodic
 // extent couples nodes of one colour across the wrap: then one thread sweeps in order.
-__global__ void k_hg_bottom(hg::Geo G, hg::Lev L, double* phi, const double* f, int nu, long N) {
+template <typename T>
+__global__ void k_hg_bottom(hg::Geo G, hg::LevT<T> L, T* phi, const T* f, int nu, long N) {
     bool serial = false;
     for (int d = 0; d < G.dm; ++d) serial = serial || (G.per[d] && (L.n[d] & 1));
     const long start = serial ? 0 : threadIdx.x;
@@ -80,15 +84,26 @@ __global__ void k_hg_bottom(hg::Geo G, hg::Lev L, double* phi, const double* f, 
         }
 }
 
+__global__ void k_hg_to_single(const double* r, float* r32, long N) {
+    HG_LOOP(N) hg::to_single_node(idx, r, r32);
+}
+__global__ void k_hg_accumulate(hg::Geo G, hg::Lev L, double* phi, const float* e, long N) {
+    HG_LOOP(N) hg::accumulate_node(G, L, idx, phi, e);
+}
+__global__ void k_hg_sig_single(const double* s, float* s32, long N) {
+    HG_LOOP(N) s32[idx] = (float)s[idx];
+}
+
 // Per-block partials over the unknown nodes: [0] sum, [1] max |x|, [2] NaN count, [3] count.
-__global__ void k_hg_reduce(hg::Geo G, hg::Lev L, const double* x, double* part, long N) {
+template <typename T>
+__global__ void k_hg_reduce(hg::Geo G, hg::LevT<T> L, const T* x, double* part, long N) {
     __shared__ double s[4][kThreads / 32];
     double a[4] = {0.0, 0.0, 0.0, 0.0};
     HG_LOOP(N) {
         int p[3];
         hg::node_coords(L, idx, p);
         if (!hg::is_unknown(G, L, p)) continue;
-        const double v = x[idx];
+        const double v = (double)x[idx];
         if (v != v) {
             a[2] += 1.0;
             continue;
@@ -145,8 +160,9 @@ __global__ void k_hg_reduce_finish(const double* part, int nparts, double* out) 
     }
 }
 
-__global__ void k_hg_sub_mean(hg::Geo G, hg::Lev L, double* x, const double* m, long N) {
-    const double v = *m;
+template <typename T>
+__global__ void k_hg_sub_mean(hg::Geo G, hg::LevT<T> L, T* x, const double* m, long N) {
+    const T v = (T)*m;
     HG_LOOP(N) {
         int p[3];
         hg::node_coords(L, idx, p);
@@ -201,6 +217,9 @@ struct HgState {
         hg::Lev lev{};
         double* sig = nullptr;
         double* buf[hg::kNumBufs] = {};
+        hg::LevT<float> lev32{};          // FP32 copy of the level (mixed precision)
+        float* sig32 = nullptr;
+        float* buf32[hg::kNumBufs] = {};
         long nn = 0, nc = 0;
     };
     std::vector<Level> L;
@@ -307,27 +326,29 @@ int hg_ensure(mac_ctx* c) {
     return rc;
 }
 
-struct HgExec {
+// Level accessors per precision.
+template <typename T> struct HgAccess;
+template <> struct HgAccess<double> {
+    static hg::LevT<double> lev(const HgState::Level& S) { return S.lev; }
+    static double* buf(const HgState::Level& S, int w) { return S.buf[w]; }
+};
+template <> struct HgAccess<float> {
+    static hg::LevT<float> lev(const HgState::Level& S) { return S.lev32; }
+    static float* buf(const HgState::Level& S, int w) { return S.buf32[w]; }
+};
+
+// The multigrid half of the executor in precision T on the context's stream.
+template <typename T>
+struct HgMg {
     mac_ctx* c;
     HgState* H;
     int nlev;
     hg::Geo geo;
     bool singular;
     int err = MAC_OK;
-    // this call
-    int proj_type = hg::kRegular;
-    double dt = 1.0;
-    double* unew = nullptr;
-    const double* uold = nullptr;
-    double* gpi = nullptr;
-    const double* rhohalf = nullptr;
-    double* pi = nullptr;
-    const double* b0 = nullptr;
-    const double* nodalrhs = nullptr;
-    int alt = 0;
 
-    hg::Lev lev(int l) const { return H->L[l].lev; }
-    double* buf(int l, int w) const { return H->L[l].buf[w]; }
+    hg::LevT<T> lev(int l) const { return HgAccess<T>::lev(H->L[l]); }
+    T* buf(int l, int w) const { return HgAccess<T>::buf(H->L[l], w); }
     long nn(int l) const { return H->L[l].nn; }
     long nc(int l) const { return H->L[l].nc; }
     int blocks(long n) const { return blocks_for(n, c->sms); }
@@ -339,49 +360,48 @@ struct HgExec {
             err = MAC_ERR_CUDA;
         }
     }
-
-    void defect(int l, const double* phi, const double* f, double* r) {
-        k_hg_defect<<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), phi, f, r, nn(l));
+    void defect(int l, const T* phi, const T* f, T* r) {
+        k_hg_defect<T><<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), phi, f, r, nn(l));
         launched();
     }
-    void gs(int l, double* phi, const double* f, int nu) {
+    void gs(int l, T* phi, const T* f, int nu) {
         for (int s = 0; s < nu; ++s)
             for (int colour = 0; colour < (1 << geo.dm); ++colour) {
                 const long m = hg::colour_count(geo, lev(l), colour);
-                k_hg_gs<<<blocks(m), kThreads, 0, c->stream>>>(geo, lev(l), colour, phi, f, m);
+                k_hg_gs<T><<<blocks(m), kThreads, 0, c->stream>>>(geo, lev(l), colour, phi, f, m);
                 launched();
             }
     }
-    void bottom_gs(int l, double* phi, const double* f, int nu) {
-        k_hg_bottom<<<1, 1024, 0, c->stream>>>(geo, lev(l), phi, f, nu, nn(l));
+    void bottom_gs(int l, T* phi, const T* f, int nu) {
+        k_hg_bottom<T><<<1, 1024, 0, c->stream>>>(geo, lev(l), phi, f, nu, nn(l));
         launched();
     }
-    void restrict_to(int lc, const double* rF, double* fK) {
-        k_hg_restrict<<<blocks(nn(lc)), kThreads, 0, c->stream>>>(geo, lev(lc - 1), lev(lc), rF, fK, nn(lc));
+    void restrict_to(int lc, const T* rF, T* fK) {
+        k_hg_restrict<T><<<blocks(nn(lc)), kThreads, 0, c->stream>>>(geo, lev(lc - 1), lev(lc), rF, fK, nn(lc));
         launched();
     }
-    void prolong(int lc, const double* eK, double* phiF) {
-        k_hg_prolong<<<blocks(nn(lc - 1)), kThreads, 0, c->stream>>>(geo, lev(lc), lev(lc - 1), eK, phiF, nn(lc - 1));
+    void prolong(int lc, const T* eK, T* phiF) {
+        k_hg_prolong<T><<<blocks(nn(lc - 1)), kThreads, 0, c->stream>>>(geo, lev(lc), lev(lc - 1), eK, phiF, nn(lc - 1));
         launched();
     }
-    void zero(int l, double* x) {
-        if (!err && cudaMemsetAsync(x, 0, sizeof(double) * nn(l), c->stream) != cudaSuccess) {
+    void zero(int l, T* x) {
+        if (!err && cudaMemsetAsync(x, 0, sizeof(T) * nn(l), c->stream) != cudaSuccess) {
             set_last_cuda_error(cudaGetLastError(), "cudaMemsetAsync", __FILE__, __LINE__);
             err = MAC_ERR_CUDA;
         }
     }
-    void finish(int l, double* x) {
-        k_hg_finish<<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), x, nn(l));
+    void finish(int l, T* x) {
+        k_hg_finish<T><<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), x, nn(l));
         launched();
     }
-    void reduce(int l, const double* x) {
+    void reduce(int l, const T* x) {
         const int nb = std::min(kReduceBlocks, blocks(nn(l)));
-        k_hg_reduce<<<nb, kThreads, 0, c->stream>>>(geo, lev(l), x, H->part, nn(l));
+        k_hg_reduce<T><<<nb, kThreads, 0, c->stream>>>(geo, lev(l), x, H->part, nn(l));
         launched();
         k_hg_reduce_finish<<<1, kThreads, 0, c->stream>>>(H->part, nb, H->out);
         launched();
     }
-    double unknown_max(int l, const double* x) {
+    double unknown_max(int l, const T* x) {
         reduce(l, x);
         if (err) return NAN;
         if (cudaMemcpyAsync(H->h_out, H->out, 5 * sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
@@ -392,11 +412,25 @@ struct HgExec {
         }
         return H->h_out[2] > 0.0 ? NAN : H->h_out[1];
     }
-    void sub_unknown_mean(int l, double* x) {
+    void sub_unknown_mean(int l, T* x) {
         reduce(l, x);
-        k_hg_sub_mean<<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), x, H->out + 4, nn(l));
+        k_hg_sub_mean<T><<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), x, H->out + 4, nn(l));
         launched();
     }
+};
+
+// FP64 executor: the multigrid, the projection steps and the hand-over to the FP32 cycles.
+struct HgExec : HgMg<double> {
+    int proj_type = hg::kRegular;
+    double dt = 1.0;
+    double* unew = nullptr;
+    const double* uold = nullptr;
+    double* gpi = nullptr;
+    const double* rhohalf = nullptr;
+    double* pi = nullptr;
+    const double* b0 = nullptr;
+    const double* nodalrhs = nullptr;
+    int alt = 0;
 
     void uvec() {
         k_hg_uvec<<<blocks(nc(0)), kThreads, 0, c->stream>>>(geo, nc(0), proj_type, dt, unew, uold, gpi,
@@ -410,6 +444,21 @@ struct HgExec {
             launched();
         }
         return err;
+    }
+    void sig_to_single() {
+        for (size_t l = 0; l < H->L.size(); ++l) {
+            k_hg_sig_single<<<blocks(nc((int)l)), kThreads, 0, c->stream>>>(H->L[l].sig, H->L[l].sig32,
+                                                                          nc((int)l));
+            launched();
+        }
+    }
+    void to_single(const double* r, float* r32) {
+        k_hg_to_single<<<blocks(nn(0)), kThreads, 0, c->stream>>>(r, r32, nn(0));
+        launched();
+    }
+    void accumulate(double* phi, const float* e) {
+        k_hg_accumulate<<<blocks(nn(0)), kThreads, 0, c->stream>>>(geo, lev(0), phi, e, nn(0));
+        launched();
     }
     void divu() {
         k_hg_divu<<<blocks(nn(0)), kThreads, 0, c->stream>>>(geo, lev(0), unew, b0, nodalrhs,
@@ -426,6 +475,25 @@ struct HgExec {
     }
 };
 
+// FP32 copies of the hierarchy for the mixed-precision solve (allocated on first use).
+int hg_ensure_single(mac_ctx* c) {
+    HgState* H = c->hgs;
+    if (H->L[0].sig32) return MAC_OK;
+    for (HgState::Level& S : H->L) {
+        int rc = hg_alloc(H, &S.sig32, (size_t)S.nc);
+        for (int b = 0; b < hg::kNumBufs && !rc; ++b) rc = hg_alloc(H, &S.buf32[b], (size_t)S.nn);
+        if (rc) return rc;
+        for (int d = 0; d < 3; ++d) {
+            S.lev32.n[d] = S.lev.n[d];
+            S.lev32.nn[d] = S.lev.nn[d];
+            S.lev32.h[d] = S.lev.h[d];
+        }
+        S.lev32.sig = S.sig32;
+        hg::set_dense_weights(H->geo.dm, S.lev32);
+    }
+    return MAC_OK;
+}
+
 }  // namespace
 
 // The nodal projection on whole-domain device arrays (arguments validated by the caller); fills
@@ -436,8 +504,14 @@ int hg_core(mac_ctx* c, int proj_type, double dt, int dense_stencil, double rel_
     int rc = MAC_OK;
     HgState* H = c->hgs;
     H->geo.dense = dense_stencil ? 1 : 0;
-    HgExec ex{c, H, (int)H->L.size(), H->geo, !(H->geo.dlo[0] || H->geo.dhi[0] || H->geo.dlo[1] ||
-                                                 H->geo.dhi[1] || H->geo.dlo[2] || H->geo.dhi[2])};
+    const bool singular = !(H->geo.dlo[0] || H->geo.dhi[0] || H->geo.dlo[1] || H->geo.dhi[1] ||
+                            H->geo.dlo[2] || H->geo.dhi[2]);
+    HgExec ex;
+    ex.c = c;
+    ex.H = H;
+    ex.nlev = (int)H->L.size();
+    ex.geo = H->geo;
+    ex.singular = singular;
     ex.proj_type = proj_type;
     ex.dt = dt;
     ex.unew = unew;
@@ -464,8 +538,23 @@ int hg_core(mac_ctx* c, int proj_type, double dt, int dense_stencil, double rel_
     }
     hg::SolveStats S{};
     cudaEventRecord(c->ev[0], c->stream);
+    const double eps = rel_eps > 0.0 ? rel_eps : 1e-12;
+    const bool mixed = c->o.precision == MAC_PREC_MIXED;
+    if (!rc && mixed) rc = hg_ensure_single(c);
     if (!rc) {
-        rc = hg::project(ex, rel_eps > 0.0 ? rel_eps : 1e-12, c->o.max_vcycles, c->o.nu1, c->o.nu2, &S);
+        if (mixed) {
+            // FP32 V-cycles (kMixedInner per FP64 refinement step) under FP64 refinement
+            HgMg<float> ex32;
+            ex32.c = c;
+            ex32.H = H;
+            ex32.nlev = ex.nlev;
+            ex32.geo = ex.geo;
+            ex32.singular = singular;
+            rc = hg::project_mixed(ex, ex32, eps, c->o.max_vcycles, c->o.nu1, c->o.nu2,
+                                   kMixedInner, &S);
+        } else {
+            rc = hg::project(ex, eps, c->o.max_vcycles, c->o.nu1, c->o.nu2, &S);
+        }
         if (rc == 1) rc = MAC_ERR_NOT_CONVERGED;
         if (rc == -1) rc = MAC_ERR_NONFINITE;
     }

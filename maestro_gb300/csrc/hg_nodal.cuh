@@ -48,19 +48,24 @@ struct Geo {
     int dense;
 };
 
-struct Lev {
+// A level in the precision T of its coefficients and smoother (FP64; FP32 for the inner cycles
+// of the mixed-precision solve).
+template <typename T>
+struct LevT {
     int n[3];          // cells (1 along inactive directions)
     int nn[3];         // node storage (n + 1 along active directions)
     double h[3];
-    const double* sig; // cell coefficients
+    const T* sig;      // cell coefficients
     // dense stencil: finite-element weight of a cell between its corners a and b, which depends
     // on a ^ b only (set by set_dense_weights)
-    double kw[8];
+    T kw[8];
 };
+using Lev = LevT<double>;
 
 // kw[x] = sum_d h_d^-2 S(x_d) prod_{e != d} M(x_e) with S(0) = 1, S(1) = -1, M(0) = 1/3,
 // M(1) = 1/6 (x_d = 1: the two corners differ along d).
-HG_HD inline void set_dense_weights(int dm, Lev& L) {
+template <typename T>
+HG_HD inline void set_dense_weights(int dm, LevT<T>& L) {
     for (int x = 0; x < 8; ++x) {
         double k = 0.0;
         for (int d = 0; d < dm; ++d) {
@@ -69,26 +74,32 @@ HG_HD inline void set_dense_weights(int dm, Lev& L) {
                 if (e != d) t *= ((x >> e) & 1) ? 1.0 / 6.0 : 1.0 / 3.0;
             k += t;
         }
-        L.kw[x] = x < (1 << dm) ? k : 0.0;
+        L.kw[x] = (T)(x < (1 << dm) ? k : 0.0);
     }
 }
 
-HG_HD inline long nix(const Lev& L, int i, int j, int k) {
+template <typename T>
+HG_HD inline long nix(const LevT<T>& L, int i, int j, int k) {
     return (long)i + (long)L.nn[0] * ((long)j + (long)L.nn[1] * k);
 }
-HG_HD inline long cix(const Lev& L, int i, int j, int k) {
+template <typename T>
+HG_HD inline long cix(const LevT<T>& L, int i, int j, int k) {
     return (long)i + (long)L.n[0] * ((long)j + (long)L.n[1] * k);
 }
-HG_HD inline long nnodes(const Lev& L) { return (long)L.nn[0] * L.nn[1] * L.nn[2]; }
-HG_HD inline long ncells(const Lev& L) { return (long)L.n[0] * L.n[1] * L.n[2]; }
+template <typename T>
+HG_HD inline long nnodes(const LevT<T>& L) { return (long)L.nn[0] * L.nn[1] * L.nn[2]; }
+template <typename T>
+HG_HD inline long ncells(const LevT<T>& L) { return (long)L.n[0] * L.n[1] * L.n[2]; }
 
-HG_HD inline void node_coords(const Lev& L, long idx, int p[3]) {
+template <typename T>
+HG_HD inline void node_coords(const LevT<T>& L, long idx, int p[3]) {
     p[0] = (int)(idx % L.nn[0]);
     const long r = idx / L.nn[0];
     p[1] = (int)(r % L.nn[1]);
     p[2] = (int)(r / L.nn[1]);
 }
-HG_HD inline void cell_coords(const Lev& L, long idx, int c[3]) {
+template <typename T>
+HG_HD inline void cell_coords(const LevT<T>& L, long idx, int c[3]) {
     c[0] = (int)(idx % L.n[0]);
     const long r = idx / L.n[0];
     c[1] = (int)(r % L.n[1]);
@@ -96,20 +107,23 @@ HG_HD inline void cell_coords(const Lev& L, long idx, int c[3]) {
 }
 
 // Node index q along d folded onto the carrying node (periodic wrap); -1 outside.
-HG_HD inline int node_wrap(const Geo& G, const Lev& L, int d, int q) {
+template <typename T>
+HG_HD inline int node_wrap(const Geo& G, const LevT<T>& L, int d, int q) {
     if (d >= G.dm) return q == 0 ? 0 : -1;
     const int n = L.n[d];
     if (G.per[d]) return ((q % n) + n) % n;
     return (q < 0 || q > n) ? -1 : q;
 }
-HG_HD inline int cell_wrap(const Geo& G, const Lev& L, int d, int c) {
+template <typename T>
+HG_HD inline int cell_wrap(const Geo& G, const LevT<T>& L, int d, int c) {
     if (d >= G.dm) return c == 0 ? 0 : -1;
     const int n = L.n[d];
     if (G.per[d]) return ((c % n) + n) % n;
     return (c < 0 || c >= n) ? -1 : c;
 }
 // An unknown: not a periodic image, not on an outflow face.
-HG_HD inline bool is_unknown(const Geo& G, const Lev& L, const int p[3]) {
+template <typename T>
+HG_HD inline bool is_unknown(const Geo& G, const LevT<T>& L, const int p[3]) {
     for (int d = 0; d < G.dm; ++d) {
         if (G.per[d]) {
             if (p[d] == L.n[d]) return false;
@@ -121,10 +135,11 @@ HG_HD inline bool is_unknown(const Geo& G, const Lev& L, const int p[3]) {
 }
 
 // (L phi)_p = diag * phi_p - off.
-HG_HD inline void node_op(const Geo& G, const Lev& L, const int p[3], const double* phi,
-                          double& diag, double& off) {
+template <typename T>
+HG_HD inline void node_op(const Geo& G, const LevT<T>& L, const int p[3], const T* phi, T& diag,
+                          T& off) {
     const int dm = G.dm;
-    double dK = 0.0, oK = 0.0;
+    T dK = 0, oK = 0;
     if (G.dense) {
         const long pi = nix(L, p[0], p[1], p[2]);
         for (int a = 0; a < (1 << dm); ++a) {   // a: the corner of cell c that p is
@@ -136,8 +151,8 @@ HG_HD inline void node_op(const Geo& G, const Lev& L, const int p[3], const doub
                 c[d] = cw;
             }
             if (out) continue;
-            const double s = L.sig[cix(L, c[0], c[1], c[2])];
-            double acc = 0.0;
+            const T s = L.sig[cix(L, c[0], c[1], c[2])];
+            T acc = 0;
             for (int b = 0; b < (1 << dm); ++b) {
                 if (b == a) continue;
                 int m[3] = {0, 0, 0};
@@ -158,7 +173,7 @@ HG_HD inline void node_op(const Geo& G, const Lev& L, const int p[3], const doub
             for (int sd = -1; sd <= 1; sd += 2) {
                 const int q = node_wrap(G, L, d, p[d] + sd);
                 if (q < 0) continue;
-                double sum = 0.0;
+                T sum = 0;
                 int cnt = 0;
                 for (int a = 0; a < (1 << dm); ++a) {
                     if ((a >> d) & 1) continue;
@@ -173,7 +188,7 @@ HG_HD inline void node_op(const Geo& G, const Lev& L, const int p[3], const doub
                     ++cnt;
                     if (!out) sum += L.sig[cix(L, c[0], c[1], c[2])];
                 }
-                const double se = sum / cnt / (L.h[d] * L.h[d]);
+                const T se = sum / (T)cnt / (T)(L.h[d] * L.h[d]);
                 int qq[3] = {p[0], p[1], p[2]};
                 qq[d] = q;
                 dK -= se;
@@ -185,26 +200,29 @@ HG_HD inline void node_op(const Geo& G, const Lev& L, const int p[3], const doub
 }
 
 // r = f - L phi on the unknowns, 0 elsewhere.
-HG_HD inline void defect_node(const Geo& G, const Lev& L, long idx, const double* phi,
-                              const double* f, double* r) {
+template <typename T>
+HG_HD inline void defect_node(const Geo& G, const LevT<T>& L, long idx, const T* phi, const T* f,
+                              T* r) {
     int p[3];
     node_coords(L, idx, p);
     if (!is_unknown(G, L, p)) {
-        r[idx] = 0.0;
+        r[idx] = 0;
         return;
     }
-    double dg, off;
+    T dg, off;
     node_op(G, L, p, phi, dg, off);
     r[idx] = f[idx] - (dg * phi[idx] - off);
 }
 
 // Nodes of one colour (parity pattern `colour` of the node coordinates): how many, and the k-th.
-HG_HD inline long colour_count(const Geo& G, const Lev& L, int colour) {
+template <typename T>
+HG_HD inline long colour_count(const Geo& G, const LevT<T>& L, int colour) {
     long m = 1;
     for (int d = 0; d < G.dm; ++d) m *= (L.nn[d] - ((colour >> d) & 1) + 1) / 2;
     return m;
 }
-HG_HD inline void colour_node(const Geo& G, const Lev& L, int colour, long k, int p[3]) {
+template <typename T>
+HG_HD inline void colour_node(const Geo& G, const LevT<T>& L, int colour, long k, int p[3]) {
     p[0] = p[1] = p[2] = 0;
     for (int d = 0; d < G.dm; ++d) {
         const int b = (colour >> d) & 1;
@@ -216,50 +234,52 @@ HG_HD inline void colour_node(const Geo& G, const Lev& L, int colour, long k, in
 
 // Gauss-Seidel update of the k-th node of a colour (nodes of one colour share no cell, so a
 // colour updates in parallel).
-HG_HD inline void gs_node(const Geo& G, const Lev& L, long k, int colour, double* phi,
-                          const double* f) {
+template <typename T>
+HG_HD inline void gs_node(const Geo& G, const LevT<T>& L, long k, int colour, T* phi, const T* f) {
     int p[3];
     colour_node(G, L, colour, k, p);
     if (!is_unknown(G, L, p)) return;
     const long idx = nix(L, p[0], p[1], p[2]);
-    double dg, off;
+    T dg, off;
     node_op(G, L, p, phi, dg, off);
     phi[idx] = (f[idx] + off) / dg;
 }
 
 // Coarse right-hand side = full-weighting restriction of the fine defect (coarse node P <- fine
 // nodes 2P + a, a in {-1,0,1}^dm, weights prod (1 or 1/2), divided by 2^dm).
-HG_HD inline void restrict_node(const Geo& G, const Lev& F, const Lev& K, long idx,
-                                const double* rF, double* fK) {
+template <typename T>
+HG_HD inline void restrict_node(const Geo& G, const LevT<T>& F, const LevT<T>& K, long idx,
+                                const T* rF, T* fK) {
     int P[3];
     node_coords(K, idx, P);
     if (!is_unknown(G, K, P)) {
-        fK[idx] = 0.0;
+        fK[idx] = 0;
         return;
     }
     const int dm = G.dm;
-    double s = 0.0;
+    T s = 0;
     for (int a2 = -(dm > 2); a2 <= (dm > 2); ++a2)
         for (int a1 = -(dm > 1); a1 <= (dm > 1); ++a1)
             for (int a0 = -1; a0 <= 1; ++a0) {
                 const int a[3] = {a0, a1, a2};
                 int q[3] = {0, 0, 0};
-                double w = 1.0;
+                T w = 1;
                 bool out = false;
                 for (int d = 0; d < dm; ++d) {
-                    if (a[d]) w *= 0.5;
+                    if (a[d]) w *= (T)0.5;
                     const int qq = node_wrap(G, F, d, 2 * P[d] + a[d]);
                     if (qq < 0) out = true;
                     q[d] = qq;
                 }
                 if (!out) s += w * rF[nix(F, q[0], q[1], q[2])];
             }
-    fK[idx] = s / (1 << dm);
+    fK[idx] = s / (T)(1 << dm);
 }
 
 // Fine unknowns += multilinear interpolation of the coarse correction.
-HG_HD inline void prolong_node(const Geo& G, const Lev& K, const Lev& F, long idx,
-                               const double* eK, double* phiF) {
+template <typename T>
+HG_HD inline void prolong_node(const Geo& G, const LevT<T>& K, const LevT<T>& F, long idx,
+                               const T* eK, T* phiF) {
     int p[3];
     node_coords(F, idx, p);
     if (!is_unknown(G, F, p)) return;
@@ -269,15 +289,15 @@ HG_HD inline void prolong_node(const Geo& G, const Lev& K, const Lev& F, long id
         lo[d] = p[d] >> 1;
         odd[d] = p[d] & 1;
     }
-    double s = 0.0;
+    T s = 0;
     for (int a2 = 0; a2 <= odd[2]; ++a2)
         for (int a1 = 0; a1 <= odd[1]; ++a1)
             for (int a0 = 0; a0 <= odd[0]; ++a0) {
                 const int a[3] = {a0, a1, a2};
                 int q[3] = {0, 0, 0};
-                double w = 1.0;
+                T w = 1;
                 for (int d = 0; d < dm; ++d) {
-                    if (odd[d]) w *= 0.5;
+                    if (odd[d]) w *= (T)0.5;
                     q[d] = node_wrap(G, K, d, lo[d] + a[d]);
                 }
                 s += w * eK[nix(K, q[0], q[1], q[2])];
@@ -285,21 +305,23 @@ HG_HD inline void prolong_node(const Geo& G, const Lev& K, const Lev& F, long id
     phiF[idx] += s;
 }
 
-HG_HD inline void coarsen_sig_cell(const Geo& G, const Lev& F, const Lev& K, long idx,
-                                   double* sK) {
+template <typename T>
+HG_HD inline void coarsen_sig_cell(const Geo& G, const LevT<T>& F, const LevT<T>& K, long idx,
+                                   T* sK) {
     int c[3];
     cell_coords(K, idx, c);
     const int r0 = G.dm > 0 ? 2 : 1, r1 = G.dm > 1 ? 2 : 1, r2 = G.dm > 2 ? 2 : 1;
-    double s = 0.0;
+    T s = 0;
     for (int c2 = 0; c2 < r2; ++c2)
         for (int c1 = 0; c1 < r1; ++c1)
             for (int c0 = 0; c0 < r0; ++c0)
                 s += F.sig[cix(F, c[0] * r0 + c0, c[1] * r1 + c1, c[2] * r2 + c2)];
-    sK[idx] = s / (r0 * r1 * r2);
+    sK[idx] = s / (T)(r0 * r1 * r2);
 }
 
 // Periodic image nodes take the value of the node they stand for; outflow nodes hold 0.
-HG_HD inline void finish_node(const Geo& G, const Lev& L, long idx, double* x) {
+template <typename T>
+HG_HD inline void finish_node(const Geo& G, const LevT<T>& L, long idx, T* x) {
     int p[3];
     node_coords(L, idx, p);
     if (is_unknown(G, L, p)) return;
@@ -311,7 +333,7 @@ HG_HD inline void finish_node(const Geo& G, const Lev& L, long idx, double* x) {
         else if ((p[d] == 0 && G.dlo[d]) || (p[d] == L.n[d] && G.dhi[d]))
             fixed = true;
     }
-    x[idx] = fixed ? 0.0 : x[nix(L, q[0], q[1], q[2])];
+    x[idx] = fixed ? (T)0 : x[nix(L, q[0], q[1], q[2])];
 }
 
 // Node-centred divergence of beta0 U (u component-major over the cells; b0 null: 1), minus
@@ -396,6 +418,18 @@ HG_HD inline void update_pi_node(const Lev& L, long idx, int proj_type, double d
     else if (proj_type == kPressureIters) pi[idx] += phi[idx];
     else if (proj_type == kRegular) pi[idx] = phi[idx] / dt;
     (void)L;
+}
+
+// ---- mixed precision: FP32 inner cycles inside FP64 iterative refinement ---------------------
+//
+// The FP32 right-hand side of an inner solve is the FP64 defect rounded; the FP64 solution takes
+// the FP32 correction on the unknowns; the FP32 coefficients are the FP64 ones rounded.
+HG_HD inline void to_single_node(long idx, const double* r, float* r32) { r32[idx] = (float)r[idx]; }
+HG_HD inline void accumulate_node(const Geo& G, const Lev& L, long idx, double* phi,
+                                  const float* e) {
+    int p[3];
+    node_coords(L, idx, p);
+    if (is_unknown(G, L, p)) phi[idx] += (double)e[idx];
 }
 
 // ---- caller fabs <-> whole-domain arrays --------------------------------------------------------
@@ -510,6 +544,60 @@ int project(E& ex, double rel_eps, int max_cycles, int nu1, int nu2, SolveStats*
     const int status = rc;
     ex.finish(0, ex.buf(0, kPhi));
     ex.update();                 // U, gpi, pi
+    rc = ex.error();
+    return rc ? rc : status;
+}
+
+// Mixed-precision solve: FP64 defect, `inner` FP32 V-cycles on it from zero (ex32: the FP32
+// view of the same hierarchy), FP64 accumulation, until the FP64 residual meets rel_eps.
+template <class E, class E32>
+int solve_mixed(E& ex, E32& ex32, double rel_eps, int max_iters, int nu1, int nu2, int inner,
+                SolveStats* S) {
+    *S = SolveStats{};
+    if (ex.singular) ex.sub_unknown_mean(0, ex.buf(0, kF));
+    const double fnorm = ex.unknown_max(0, ex.buf(0, kF));
+    S->fnorm = fnorm;
+    if (!(fnorm > 0.0)) {
+        ex.zero(0, ex.buf(0, kPhi));
+        S->status = std::isnan(fnorm) ? -1 : 0;
+        return ex.error() ? ex.error() : S->status;
+    }
+    ex.defect(0, ex.buf(0, kPhi), ex.buf(0, kF), ex.buf(0, kR));
+    double res = ex.unknown_max(0, ex.buf(0, kR));
+    S->resid0 = res;
+    int it = 0;
+    while (!(res <= rel_eps * fnorm) && it < max_iters && !std::isnan(res)) {
+        ex.to_single(ex.buf(0, kR), ex32.buf(0, kF));
+        ex32.zero(0, ex32.buf(0, kPhi));
+        for (int v = 0; v < inner; ++v) vcycle(ex32, 0, nu1, nu2);
+        ex.accumulate(ex.buf(0, kPhi), ex32.buf(0, kPhi));
+        ex.defect(0, ex.buf(0, kPhi), ex.buf(0, kF), ex.buf(0, kR));
+        res = ex.unknown_max(0, ex.buf(0, kR));
+        ++it;
+        if (S->nhist < 64) S->hist[S->nhist++] = res / fnorm;
+        if (ex.error() || ex32.error()) return ex.error() ? ex.error() : ex32.error();
+    }
+    S->cycles = it * inner;
+    S->rel_resid = res / fnorm;
+    S->status = res <= rel_eps * fnorm ? 0 : (std::isnan(res) ? -1 : 1);
+    return ex.error() ? ex.error() : S->status;
+}
+
+// hgproject with the mixed-precision solve.
+template <class E, class E32>
+int project_mixed(E& ex, E32& ex32, double rel_eps, int max_iters, int nu1, int nu2, int inner,
+                  SolveStats* S) {
+    ex.uvec();
+    int rc = ex.build_levels();
+    if (rc) return rc;
+    ex.sig_to_single();   // FP32 coefficients of every level
+    ex.divu();
+    ex.zero(0, ex.buf(0, kPhi));
+    rc = solve_mixed(ex, ex32, rel_eps, max_iters, nu1, nu2, inner, S);
+    if (rc < 0) return rc;
+    const int status = rc;
+    ex.finish(0, ex.buf(0, kPhi));
+    ex.update();
     rc = ex.error();
     return rc ? rc : status;
 }

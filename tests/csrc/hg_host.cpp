@@ -14,18 +14,96 @@ using namespace mac;
 
 namespace {
 
-struct HostLevel {
-    hg::Lev lev{};
-    std::vector<double> sig;
-    std::vector<double> buf[hg::kNumBufs];
-};
-
-struct HostExec {
+// The multigrid half of the executor in precision T (FP64, or FP32 for the inner cycles).
+template <typename T>
+struct HostMg {
     int nlev = 0;
     hg::Geo geo{};
     bool singular = true;
-    std::vector<HostLevel> L;
-    double last_mean = 0.0;
+    std::vector<hg::LevT<T>> L;
+    std::vector<std::vector<T>> sig;
+    std::vector<std::vector<T>> store[hg::kNumBufs];
+
+    void build(const hg::Geo& G, bool sing, const std::vector<hg::LevT<double>>& shape) {
+        geo = G;
+        singular = sing;
+        nlev = (int)shape.size();
+        L.assign(nlev, hg::LevT<T>{});
+        sig.assign(nlev, {});
+        for (int b = 0; b < hg::kNumBufs; ++b) store[b].assign(nlev, {});
+        for (int l = 0; l < nlev; ++l) {
+            for (int d = 0; d < 3; ++d) {
+                L[l].n[d] = shape[l].n[d];
+                L[l].nn[d] = shape[l].nn[d];
+                L[l].h[d] = shape[l].h[d];
+            }
+            sig[l].assign((size_t)hg::ncells(L[l]), (T)0);
+            for (int b = 0; b < hg::kNumBufs; ++b) store[b][l].assign((size_t)hg::nnodes(L[l]), (T)0);
+            L[l].sig = sig[l].data();
+            hg::set_dense_weights(geo.dm, L[l]);
+        }
+    }
+    hg::LevT<T> lev(int l) const { return L[l]; }
+    T* buf(int l, int w) { return store[w][l].data(); }
+    long nn(int l) const { return hg::nnodes(L[l]); }
+    long nc(int l) const { return hg::ncells(L[l]); }
+    int error() const { return 0; }
+
+    void defect(int l, const T* phi, const T* f, T* r) {
+        for (long i = 0; i < nn(l); ++i) hg::defect_node(geo, L[l], i, phi, f, r);
+    }
+    void gs(int l, T* phi, const T* f, int nu) {
+        for (int s = 0; s < nu; ++s)
+            for (int colour = 0; colour < (1 << geo.dm); ++colour) {
+                const long m = hg::colour_count(geo, L[l], colour);
+                for (long i = 0; i < m; ++i) hg::gs_node(geo, L[l], i, colour, phi, f);
+            }
+    }
+    void bottom_gs(int l, T* phi, const T* f, int nu) { gs(l, phi, f, nu); }
+    void restrict_to(int lc, const T* rF, T* fK) {
+        for (long i = 0; i < nn(lc); ++i) hg::restrict_node(geo, L[lc - 1], L[lc], i, rF, fK);
+    }
+    void prolong(int lc, const T* eK, T* phiF) {
+        for (long i = 0; i < nn(lc - 1); ++i) hg::prolong_node(geo, L[lc], L[lc - 1], i, eK, phiF);
+    }
+    void zero(int l, T* x) { std::fill(x, x + nn(l), (T)0); }
+    void finish(int l, T* x) {
+        for (long i = 0; i < nn(l); ++i) hg::finish_node(geo, L[l], i, x);
+    }
+    double unknown_max(int l, const T* x) {
+        double mx = 0.0;
+        bool nan = false;
+        for (long i = 0; i < nn(l); ++i) {
+            int p[3];
+            hg::node_coords(L[l], i, p);
+            if (!hg::is_unknown(geo, L[l], p)) continue;
+            nan = nan || x[i] != x[i];
+            mx = std::max(mx, (double)std::fabs(x[i]));
+        }
+        return nan ? NAN : mx;
+    }
+    void sub_unknown_mean(int l, T* x) {
+        double s = 0.0;
+        long cnt = 0;
+        for (long i = 0; i < nn(l); ++i) {
+            int p[3];
+            hg::node_coords(L[l], i, p);
+            if (!hg::is_unknown(geo, L[l], p)) continue;
+            s += x[i];
+            ++cnt;
+        }
+        const T m = (T)(cnt ? s / cnt : 0.0);
+        for (long i = 0; i < nn(l); ++i) {
+            int p[3];
+            hg::node_coords(L[l], i, p);
+            if (hg::is_unknown(geo, L[l], p)) x[i] -= m;
+        }
+    }
+};
+
+// FP64 executor: the multigrid plus the projection steps and the precision hand-over.
+struct HostExec : HostMg<double> {
+    HostMg<float>* v32 = nullptr;
     int proj_type = hg::kRegular;
     double dt = 1.0;
     double* unew = nullptr;
@@ -37,82 +115,35 @@ struct HostExec {
     const double* nodalrhs = nullptr;
     int alt = 0;
 
-    hg::Lev lev(int l) const { return L[l].lev; }
-    double* buf(int l, int w) { return L[l].buf[w].data(); }
-    long nn(int l) const { return hg::nnodes(L[l].lev); }
-    long nc(int l) const { return hg::ncells(L[l].lev); }
-    int error() const { return 0; }
-
-    void defect(int l, const double* phi, const double* f, double* r) {
-        for (long i = 0; i < nn(l); ++i) hg::defect_node(geo, L[l].lev, i, phi, f, r);
-    }
-    void gs(int l, double* phi, const double* f, int nu) {
-        for (int s = 0; s < nu; ++s)
-            for (int colour = 0; colour < (1 << geo.dm); ++colour) {
-                const long m = hg::colour_count(geo, L[l].lev, colour);
-                for (long i = 0; i < m; ++i) hg::gs_node(geo, L[l].lev, i, colour, phi, f);
-            }
-    }
-    void bottom_gs(int l, double* phi, const double* f, int nu) { gs(l, phi, f, nu); }
-    void restrict_to(int lc, const double* rF, double* fK) {
-        for (long i = 0; i < nn(lc); ++i) hg::restrict_node(geo, L[lc - 1].lev, L[lc].lev, i, rF, fK);
-    }
-    void prolong(int lc, const double* eK, double* phiF) {
-        for (long i = 0; i < nn(lc - 1); ++i) hg::prolong_node(geo, L[lc].lev, L[lc - 1].lev, i, eK, phiF);
-    }
-    void zero(int l, double* x) { std::fill(x, x + nn(l), 0.0); }
-    void finish(int l, double* x) {
-        for (long i = 0; i < nn(l); ++i) hg::finish_node(geo, L[l].lev, i, x);
-    }
-    double unknown_max(int l, const double* x) {
-        double mx = 0.0;
-        bool nan = false;
-        for (long i = 0; i < nn(l); ++i) {
-            int p[3];
-            hg::node_coords(L[l].lev, i, p);
-            if (!hg::is_unknown(geo, L[l].lev, p)) continue;
-            nan = nan || x[i] != x[i];
-            mx = std::max(mx, std::fabs(x[i]));
-        }
-        return nan ? NAN : mx;
-    }
-    void sub_unknown_mean(int l, double* x) {
-        double s = 0.0;
-        long cnt = 0;
-        for (long i = 0; i < nn(l); ++i) {
-            int p[3];
-            hg::node_coords(L[l].lev, i, p);
-            if (!hg::is_unknown(geo, L[l].lev, p)) continue;
-            s += x[i];
-            ++cnt;
-        }
-        const double m = cnt ? s / cnt : 0.0;
-        for (long i = 0; i < nn(l); ++i) {
-            int p[3];
-            hg::node_coords(L[l].lev, i, p);
-            if (hg::is_unknown(geo, L[l].lev, p)) x[i] -= m;
-        }
-    }
     void uvec() {
         for (long i = 0; i < nc(0); ++i)
-            hg::uvec_cell(geo, i, nc(0), proj_type, dt, unew, uold, gpi, rhohalf, b0, alt, L[0].sig.data());
+            hg::uvec_cell(geo, i, nc(0), proj_type, dt, unew, uold, gpi, rhohalf, b0, alt, sig[0].data());
     }
     int build_levels() {
         for (int l = 1; l < nlev; ++l)
-            for (long i = 0; i < nc(l); ++i)
-                hg::coarsen_sig_cell(geo, L[l - 1].lev, L[l].lev, i, L[l].sig.data());
+            for (long i = 0; i < nc(l); ++i) hg::coarsen_sig_cell(geo, L[l - 1], L[l], i, sig[l].data());
         return 0;
+    }
+    void sig_to_single() {
+        for (int l = 0; l < nlev; ++l)
+            for (long i = 0; i < nc(l); ++i) v32->sig[l][i] = (float)sig[l][i];
+    }
+    void to_single(const double* r, float* r32) {
+        for (long i = 0; i < nn(0); ++i) hg::to_single_node(i, r, r32);
+    }
+    void accumulate(double* phi, const float* e) {
+        for (long i = 0; i < nn(0); ++i) hg::accumulate_node(geo, L[0], i, phi, e);
     }
     void divu() {
         for (long i = 0; i < nn(0); ++i)
-            hg::divu_node(geo, L[0].lev, i, unew, b0, nodalrhs, buf(0, hg::kF));
+            hg::divu_node(geo, L[0], i, unew, b0, nodalrhs, buf(0, hg::kF));
     }
     void update() {
         for (long i = 0; i < nc(0); ++i)
-            hg::update_cell(geo, L[0].lev, i, proj_type, dt, buf(0, hg::kPhi), unew, uold, gpi,
+            hg::update_cell(geo, L[0], i, proj_type, dt, buf(0, hg::kPhi), unew, uold, gpi,
                             rhohalf, b0, alt);
         for (long i = 0; i < nn(0); ++i)
-            hg::update_pi_node(L[0].lev, i, proj_type, dt, buf(0, hg::kPhi), pi);
+            hg::update_pi_node(L[0], i, proj_type, dt, buf(0, hg::kPhi), pi);
     }
 };
 
@@ -123,22 +154,24 @@ extern "C" {
 // The library's nodal projection on the host.  Geometry: dm, n[3], dx[3], per/dlo/dhi flags;
 // arrays as mac_hgproject_dense.  phi_out (nullable) receives the nodal solution.  stats_out:
 // [status, cycles, rel_resid, fnorm].
-int hgh_project(int dm, const int* n, const double* dx, const int* per, const int* dlo,
-                const int* dhi, int dense, int proj_type, double dt, int alt, double rel_eps,
-                int max_cycles, int nu1, int nu2, double* unew, const double* uold, double* gpi,
-                const double* rhohalf, double* pi, const double* b0, const double* nodalrhs,
-                double* phi_out, double* stats_out) {
-    HostExec E;
-    E.geo.dm = dm;
+// inner > 0: the mixed-precision solve with `inner` FP32 V-cycles per FP64 refinement step.
+int hgh_project_prec(int dm, const int* n, const double* dx, const int* per, const int* dlo,
+                     const int* dhi, int dense, int proj_type, double dt, int alt, double rel_eps,
+                     int max_cycles, int nu1, int nu2, int inner, double* unew,
+                     const double* uold, double* gpi, const double* rhohalf, double* pi,
+                     const double* b0, const double* nodalrhs, double* phi_out,
+                     double* stats_out) {
+    hg::Geo G{};
+    G.dm = dm;
     for (int d = 0; d < 3; ++d) {
-        E.geo.per[d] = d < dm ? per[d] : 0;
-        E.geo.dlo[d] = d < dm ? dlo[d] : 0;
-        E.geo.dhi[d] = d < dm ? dhi[d] : 0;
+        G.per[d] = d < dm ? per[d] : 0;
+        G.dlo[d] = d < dm ? dlo[d] : 0;
+        G.dhi[d] = d < dm ? dhi[d] : 0;
     }
-    E.geo.dense = dense;
+    G.dense = dense;
     bool dir = false;
-    for (int d = 0; d < dm; ++d) dir = dir || E.geo.dlo[d] || E.geo.dhi[d];
-    E.singular = !dir;
+    for (int d = 0; d < dm; ++d) dir = dir || G.dlo[d] || G.dhi[d];
+    std::vector<hg::LevT<double>> shape;
     int nn[3];
     double h[3];
     for (int d = 0; d < 3; ++d) {
@@ -146,16 +179,14 @@ int hgh_project(int dm, const int* n, const double* dx, const int* per, const in
         h[d] = d < dm ? dx[d] : 1.0;
     }
     while (true) {
-        HostLevel S;
+        hg::LevT<double> S{};
         for (int d = 0; d < 3; ++d) {
-            S.lev.n[d] = nn[d];
-            S.lev.nn[d] = d < dm ? nn[d] + 1 : 1;
-            S.lev.h[d] = h[d];
+            S.n[d] = nn[d];
+            S.nn[d] = d < dm ? nn[d] + 1 : 1;
+            S.h[d] = h[d];
         }
-        S.sig.assign((size_t)hg::ncells(S.lev), 0.0);
-        for (int b = 0; b < hg::kNumBufs; ++b) S.buf[b].assign((size_t)hg::nnodes(S.lev), 0.0);
-        E.L.push_back(std::move(S));
-        bool more = (int)E.L.size() < hg::kMaxLevels;
+        shape.push_back(S);
+        bool more = (int)shape.size() < hg::kMaxLevels;
         for (int d = 0; d < dm; ++d) more = more && nn[d] % 2 == 0 && nn[d] >= 4;
         if (!more) break;
         for (int d = 0; d < dm; ++d) {
@@ -163,11 +194,11 @@ int hgh_project(int dm, const int* n, const double* dx, const int* per, const in
             h[d] *= 2;
         }
     }
-    for (HostLevel& S : E.L) {
-        S.lev.sig = S.sig.data();
-        hg::set_dense_weights(dm, S.lev);
-    }
-    E.nlev = (int)E.L.size();
+    HostExec E;
+    E.build(G, !dir, shape);
+    HostMg<float> E32;
+    E32.build(G, !dir, shape);
+    E.v32 = &E32;
     E.proj_type = proj_type;
     E.dt = dt;
     E.unew = unew;
@@ -179,8 +210,10 @@ int hgh_project(int dm, const int* n, const double* dx, const int* per, const in
     E.nodalrhs = nodalrhs;
     E.alt = (proj_type != hg::kInitial && proj_type != hg::kDivuIters && alt) ? 1 : 0;
     hg::SolveStats S{};
-    const int rc = hg::project(E, rel_eps, max_cycles, nu1, nu2, &S);
-    if (phi_out) std::copy(E.L[0].buf[hg::kPhi].begin(), E.L[0].buf[hg::kPhi].end(), phi_out);
+    const int rc = inner > 0
+                       ? hg::project_mixed(E, E32, rel_eps, max_cycles, nu1, nu2, inner, &S)
+                       : hg::project(E, rel_eps, max_cycles, nu1, nu2, &S);
+    if (phi_out) std::copy(E.store[hg::kPhi][0].begin(), E.store[hg::kPhi][0].end(), phi_out);
     if (stats_out) {
         stats_out[0] = rc;
         stats_out[1] = S.cycles;
@@ -188,6 +221,16 @@ int hgh_project(int dm, const int* n, const double* dx, const int* per, const in
         stats_out[3] = S.fnorm;
     }
     return rc;
+}
+
+int hgh_project(int dm, const int* n, const double* dx, const int* per, const int* dlo,
+                const int* dhi, int dense, int proj_type, double dt, int alt, double rel_eps,
+                int max_cycles, int nu1, int nu2, double* unew, const double* uold, double* gpi,
+                const double* rhohalf, double* pi, const double* b0, const double* nodalrhs,
+                double* phi_out, double* stats_out) {
+    return hgh_project_prec(dm, n, dx, per, dlo, dhi, dense, proj_type, dt, alt, rel_eps,
+                            max_cycles, nu1, nu2, 0, unew, uold, gpi, rhohalf, pi, b0, nodalrhs,
+                            phi_out, stats_out);
 }
 
 

@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _run(shape, dx, bc_lo, bc_hi, proj, dt, unew, uold, gpi, rhohalf, pi, b0=None, nodalrhs=None,
-         dense=True, alt=False, rel_eps=1e-13):
+         dense=True, alt=False, rel_eps=1e-13, precision="fp64"):
     dev = torch.device("cuda", 0)
     t = lambda a: None if a is None else torch.from_numpy(  # noqa: E731
         np.ascontiguousarray(np.asarray(a, dtype=np.float64).transpose())).to(dev)
@@ -24,7 +24,7 @@ def _run(shape, dx, bc_lo, bc_hi, proj, dt, unew, uold, gpi, rhohalf, pi, b0=Non
     ptr = lambda x: 0 if x is None else x.data_ptr()  # noqa: E731
     dm = len(shape)
     P = MacProjector(Layout(shape, [((0,) * dm, tuple(v - 1 for v in shape))]), dx,
-                     BcTower(bc_lo, bc_hi), precision="fp64",
+                     BcTower(bc_lo, bc_hi), precision=precision,
                      stream=torch.cuda.current_stream().cuda_stream, use_alt_energy_fix=int(alt))
     try:
         st = P.hgproject_dense(proj, dt, *[ptr(x) for x in tensors[:5]],
@@ -38,14 +38,15 @@ def _run(shape, dx, bc_lo, bc_hi, proj, dt, unew, uold, gpi, rhohalf, pi, b0=Non
     return back(tensors[0]), back(tensors[2]), back(tensors[4]), st
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("name", sorted(G.HG_CASES))
-def test_hgproject_matches_golden(name):
+def test_hgproject_matches_golden(name, precision):
     c = load_hg(name)
     shape = c["rhohalf"].shape
     u, gpi, pi, st = _run(shape, c["dx"], c["bc_lo"], c["bc_hi"], int(c["proj"]), float(c["dt"]),
                           c["unew"], c["uold"], c["gpi"], c["rhohalf"], c["pi"],
                           b0=c.get("beta0"), nodalrhs=c.get("nodalrhs"), dense=bool(c["dense"]),
-                          alt=bool(c["alt"]))
+                          alt=bool(c["alt"]), precision=precision)
     assert st["status"] == 0 and st["rel_resid"] <= 1e-13
     assert np.max(np.abs(u - c["u_out"])) <= 1e-9 * np.max(np.abs(c["u_out"]))
     assert np.max(np.abs(gpi - c["gpi_out"])) <= 1e-9 * max(np.max(np.abs(c["gpi_out"])),
@@ -54,8 +55,9 @@ def test_hgproject_matches_golden(name):
     assert np.ptp((pi - c["pi_out"])[m]) <= 1e-9 * max(np.max(np.abs(c["pi_out"])), 1.0)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("dense", [True, False])
-def test_hgproject_matches_oracle_3d(dense):
+def test_hgproject_matches_oracle_3d(dense, precision):
     rng = np.random.default_rng(23)
     shape = (32, 32, 32)
     dx = (1 / 32,) * 3
@@ -65,7 +67,7 @@ def test_hgproject_matches_oracle_3d(dense):
     rho = np.exp(0.3 * rng.standard_normal(shape))
     pi = np.zeros((33, 33, 33))
     u, g, p, st = _run(shape, dx, bc, bc, O.HG_REGULAR, 0.01, unew, unew, gpi, rho, pi,
-                       dense=dense, rel_eps=O.EPS_HG)
+                       dense=dense, rel_eps=O.EPS_HG, precision=precision)
     assert st["status"] == 0 and st["rel_resid"] <= O.EPS_HG
     uo, go, po, pho, so = O.hgproject(unew, unew, gpi, rho, pi, dx, bc, bc,
                                       proj_type=O.HG_REGULAR, dt=0.01, dense=dense,

@@ -36,13 +36,16 @@ def host_lib(tmp_path_factory):
     L.hgh_project.argtypes = [ci, ip, d, ip, ip, ip, ci, ci, cd, ci, cd, ci, ci, ci, d, d, d, d,
                               d, d, d, d, d]
     L.hgh_project.restype = ci
+    L.hgh_project_prec.argtypes = [ci, ip, d, ip, ip, ip, ci, ci, cd, ci, cd, ci, ci, ci, ci, d,
+                                   d, d, d, d, d, d, d, d]
+    L.hgh_project_prec.restype = ci
     L.hgh_fabs.argtypes = [ci, ip, ip, ci, ip, ci, ci, ci, ci, ctypes.POINTER(d), d]
     L.hgh_fabs.restype = None
     return L
 
 
 def run_host(L, shape, dx, bc_lo, bc_hi, proj, dt, unew, uold, gpi, rhohalf, pi, b0=None,
-             nodalrhs=None, dense=True, alt=False, rel_eps=1e-13, max_cycles=200):
+             nodalrhs=None, dense=True, alt=False, rel_eps=1e-13, max_cycles=200, inner=0):
     dm = len(shape)
     arr = lambda a: None if a is None else np.asfortranarray(a, dtype=np.float64)  # noqa: E731
     ptr = lambda a: None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
@@ -53,23 +56,25 @@ def run_host(L, shape, dx, bc_lo, bc_hi, proj, dt, unew, uold, gpi, rhohalf, pi,
     uo, rh, bb, nr = arr(uold), arr(rhohalf), arr(b0), arr(nodalrhs)
     phi = np.zeros(tuple(v + 1 for v in shape), order="F")
     st = (ctypes.c_double * 4)()
-    rc = L.hgh_project(dm, ia(shape), (ctypes.c_double * 3)(*(list(dx) + [1.0] * (3 - dm))),
-                       ia([b == BC_PER for b in bc_lo]), ia([b == BC_DIR for b in bc_lo]),
-                       ia([b == BC_DIR for b in bc_hi]), int(dense), int(proj), float(dt),
-                       int(alt), rel_eps, max_cycles, 2, 2, ptr(u), ptr(uo), ptr(g), ptr(rh),
-                       ptr(p), ptr(bb), ptr(nr), ptr(phi), st)
+    rc = L.hgh_project_prec(dm, ia(shape), (ctypes.c_double * 3)(*(list(dx) + [1.0] * (3 - dm))),
+                            ia([b == BC_PER for b in bc_lo]), ia([b == BC_DIR for b in bc_lo]),
+                            ia([b == BC_DIR for b in bc_hi]), int(dense), int(proj), float(dt),
+                            int(alt), rel_eps, max_cycles, 2, 2, int(inner), ptr(u), ptr(uo),
+                            ptr(g), ptr(rh), ptr(p), ptr(bb), ptr(nr), ptr(phi), st)
     return rc, u, g, p, phi, list(st)
 
 
+@pytest.mark.parametrize("inner", [0, 2])
 @pytest.mark.parametrize("name", sorted(G.HG_CASES))
-def test_library_hg_code_on_host_matches_golden(host_lib, name):
+def test_library_hg_code_on_host_matches_golden(host_lib, name, inner):
+    # inner = 0: the FP64 solve; inner = 2: FP32 V-cycles under FP64 refinement (mixed)
     c = load_hg(name)
     shape = c["rhohalf"].shape
     rc, u, gpi, pi, phi, st = run_host(host_lib, shape, c["dx"], c["bc_lo"], c["bc_hi"],
                                        int(c["proj"]), float(c["dt"]), c["unew"], c["uold"],
                                        c["gpi"], c["rhohalf"], c["pi"], b0=c.get("beta0"),
                                        nodalrhs=c.get("nodalrhs"), dense=bool(c["dense"]),
-                                       alt=bool(c["alt"]))
+                                       alt=bool(c["alt"]), inner=inner)
     assert rc == 0 and st[2] <= 1e-13, st
     m = _unknown_mask(shape, c["dx"], c["bc_lo"], c["bc_hi"])
     a, b = phi[m], c["phi_out"][m]
