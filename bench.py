@@ -371,8 +371,9 @@ def run_extra(args, rank, world, local):
     else:
         h = _hg_inputs(HG_N, args.seed + rank)
         lay = Layout.tiled(HG_N, HG_BOX)
+        # mixed precision: FP32 V-cycles under FP64 refinement (the FP64 rate is printed too)
         P = MacProjector(lay, tuple(1.0 / v for v in HG_N),
-                         BcTower((-1, -1, 2), (-1, -1, 2)), precision="fp64",
+                         BcTower((-1, -1, 2), (-1, -1, 2)), precision="mixed",
                          stream=stream.cuda_stream)
         fields = {k: to_dev(v) for k, v in h.items()}
         work = [(fields["unew"].clone(), fields["gpi"].clone(), fields["pi"].clone())
@@ -401,6 +402,23 @@ def run_extra(args, rank, world, local):
     P.close()
     K = args.steps
     value = world * K / (ms / 1e3)
+    fp64 = None
+    if args.workload == "hg":
+        P = MacProjector(lay, tuple(1.0 / v for v in HG_N),
+                         BcTower((-1, -1, 2), (-1, -1, 2)), precision="fp64",
+                         stream=stream.cuda_stream)
+        work = [(fields["unew"].clone(), fields["gpi"].clone(), fields["pi"].clone())
+                for _ in range(nsteps)]
+        one(0)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        st64 = [one(k) for k in range(1, nsteps)]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1) / (nsteps - 1)
+        P.close()
+        fp64 = {"value": 1e3 / ms64, "unit": UNIT, "ms_per_step": ms64,
+                "vcycles": st64[-1]["vcycles"], "rel_resid": st64[-1]["rel_resid"]}
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         secs = cpu_step()
@@ -413,6 +431,9 @@ def run_extra(args, rank, world, local):
            "gpu_launches": sum(s["launches"] for s in stats),
            "vcycles": stats[-1]["vcycles"], "rel_resid": max(s["rel_resid"] for s in stats),
            "clocks": ck}
+    if fp64 is not None:
+        out["fp64"] = fp64
+        out["dtype"] = "f32 V-cycles + f64 refinement"
     if rank == 0:
         print(json.dumps(out))
     return 0
