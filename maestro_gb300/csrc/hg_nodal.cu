@@ -212,7 +212,6 @@ inline int blocks_for(long n, int sms) {
 
 struct HgState {
     hg::Geo geo{};
-    int dense = -1;
     struct Level {
         hg::Lev lev{};
         double* sig = nullptr;

@@ -32,7 +32,6 @@ struct HostExec {
     std::vector<std::vector<double>> beta[3];
     orc::Ctx base;
     orc_opts o{};
-    double out_mean = 0.0;
     // this call's inputs
     double* const* u = nullptr;
     const double* const* rho = nullptr;
