@@ -416,6 +416,9 @@ AMR_CASES = {
     # outflow (Dirichlet) top with a fine box against it, three levels
     "amr2d_outflow": dict(dm=2, n0=(32, 16), bc="outflow",
                           boxes=[[], [((16, 8), (47, 31))], [((40, 24), (79, 63))]]),
+    # 3-D, three levels, the finest box against the bottom wall
+    "amr3d_3lev": dict(dm=3, n0=(8, 8, 8), boxes=[[], [((2, 2, 0), (13, 13, 9))],
+                                                   [((8, 8, 0), (19, 19, 11))]]),
 }
 
 
