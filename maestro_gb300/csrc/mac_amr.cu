@@ -12,6 +12,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "mac_amr.cuh"
@@ -26,45 +27,54 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kReduceBlocks = 1024;   // per-level partial slots of the valid-cell reductions
+constexpr int kMixedInner = 2;        // FP32 multi-level V-cycles per FP64 step (mixed precision)
 
 // ---- kernels (grid-stride over the cells / faces of one level) --------------------------------
 
 #define AMR_LOOP(N) for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < (N); \
                          idx += (long)gridDim.x * blockDim.x)
 
-__global__ void k_defect(Geo G, Lev L, Lev C, const double* u, const double* cu, const double* f,
-                         double* r, long N) {
+template <typename T>
+__global__ void k_defect(Geo G, amr::LevT<T> L, amr::LevT<T> C, const T* u, const T* cu,
+                         const T* f, T* r, long N) {
     AMR_LOOP(N) amr::defect_cell(G, L, C, idx, u, cu, f, r);
 }
 
-__global__ void k_gsrb(Geo G, Lev L, int colour, double* u, const double* f, long N) {
+template <typename T>
+__global__ void k_gsrb(Geo G, amr::LevT<T> L, int colour, T* u, const T* f, long N) {
     AMR_LOOP(N) amr::gsrb_cell(G, L, idx, colour, u, f);
 }
 
-__global__ void k_reflux(Geo G, Lev F, Lev C, const double* uf, const double* uc, double* res,
+template <typename T>
+__global__ void k_reflux(Geo G, amr::LevT<T> F, amr::LevT<T> C, const T* uf, const T* uc, T* res,
                          long N) {
     AMR_LOOP(N) amr::reflux_cell(G, F, C, idx, uf, uc, res);
 }
 
-__global__ void k_restrict(Geo G, Lev F, Lev C, const double* fine, double* crse, long N) {
+template <typename T>
+__global__ void k_restrict(Geo G, amr::LevT<T> F, amr::LevT<T> C, const T* fine, T* crse, long N) {
     AMR_LOOP(N) amr::restrict_cell(G, F, C, idx, fine, crse);
 }
 
-__global__ void k_prolong(Geo G, Lev F, Lev C, const double* uc, double* uf, long N) {
+template <typename T>
+__global__ void k_prolong(Geo G, amr::LevT<T> F, amr::LevT<T> C, const T* uc, T* uf, long N) {
     AMR_LOOP(N) amr::prolong_cell(G, F, C, idx, uc, uf);
 }
 
-__global__ void k_axpy3(Lev L, double* uu, const double* hold, const double* du, long N) {
+template <typename T>
+__global__ void k_axpy3(amr::LevT<T> L, T* uu, const T* hold, const T* du, long N) {
     AMR_LOOP(N) if (amr::in_region(L, idx)) uu[idx] += hold[idx] + du[idx];
 }
 
-__global__ void k_add_region(Lev L, double* phi, const double* uu, long N) {
+template <typename T>
+__global__ void k_add_region(amr::LevT<T> L, T* phi, const T* uu, long N) {
     AMR_LOOP(N) if (amr::in_region(L, idx)) phi[idx] += uu[idx];
 }
 
 // Per-block partials over the cells of one level: [0] sum of vol * x, [1] max |x|, [2] NaN
 // count, [3] volume.  valid_only: valid cells (kIn without kCov), else every region cell.
-__global__ void k_reduce(Lev L, const double* x, double vol, int valid_only, double* part,
+template <typename T>
+__global__ void k_reduce(amr::LevT<T> L, const T* x, double vol, int valid_only, double* part,
                          long N) {
     __shared__ double s_sum[kThreads / 32], s_max[kThreads / 32], s_nan[kThreads / 32],
         s_vol[kThreads / 32];
@@ -72,7 +82,7 @@ __global__ void k_reduce(Lev L, const double* x, double vol, int valid_only, dou
     AMR_LOOP(N) {
         const bool take = valid_only ? amr::is_valid(L, idx) : amr::in_region(L, idx);
         if (!take) continue;
-        const double a = x[idx];
+        const double a = (double)x[idx];
         if (a != a) {
             nan += 1.0;
             continue;
@@ -139,8 +149,9 @@ __global__ void k_reduce_finish(const double* part, int nparts, double* out) {
 }
 
 // x -= *m on the valid cells (valid_only) or every region cell.
-__global__ void k_sub_scalar(Lev L, double* x, const double* m, int valid_only, long N) {
-    const double v = *m;
+template <typename T>
+__global__ void k_sub_scalar(amr::LevT<T> L, T* x, const double* m, int valid_only, long N) {
+    const T v = (T)*m;
     AMR_LOOP(N) {
         const bool take = valid_only ? amr::is_valid(L, idx) : amr::in_region(L, idx);
         if (take) x[idx] -= v;
@@ -197,6 +208,16 @@ __global__ void k_check_rho(Geo G, Lev L, const double* rho, int* flag, long N) 
     }
 }
 
+__global__ void k_to_single(const double* x, float* y, long N) {
+    AMR_LOOP(N) amr::to_single_cell(idx, x, y);
+}
+__global__ void k_accumulate(Lev L, double* phi, const float* e, long N) {
+    AMR_LOOP(N) amr::accumulate_cell(L, idx, phi, e);
+}
+__global__ void k_to_double(const float* x, double* y, long N) {
+    AMR_LOOP(N) y[idx] = (double)x[idx];
+}
+
 // Caller fabs of one level <-> the level array; blockIdx.y is the fab.
 __global__ void k_fabs_gather(Geo G, Lev L, int dir, const amr::FabDesc* T, int with_ghosts,
                               double* level) {
@@ -232,6 +253,10 @@ struct AmrState {
         unsigned char* mask = nullptr;
         double* beta[3] = {nullptr, nullptr, nullptr};
         double* buf[amr::kNumBufs] = {};
+        // FP32 copy of the level (mixed precision; allocated on first use)
+        amr::LevT<float> lev32{};
+        float* beta32[3] = {nullptr, nullptr, nullptr};
+        float* buf32[amr::kNumBufs] = {};
         double* phi_user = nullptr;   // the caller's phi of this call (aliases buf kPhi)
         long ncell = 0;
     };
@@ -362,23 +387,31 @@ int build_masks(const mac_ctx* c, int nlev, const int* nboxes, const int* box_lo
 }
 
 // The executor of amr_solve / amr_project on the context's stream.
-struct GpuExec {
+// Level accessors per precision.
+template <typename T> struct AmrAccess;
+template <> struct AmrAccess<double> {
+    static amr::LevT<double> lev(const AmrState::LevelStore& S) { return S.lev; }
+    static double*& buf(AmrState::LevelStore& S, int w) { return S.buf[w]; }
+};
+template <> struct AmrAccess<float> {
+    static amr::LevT<float> lev(const AmrState::LevelStore& S) { return S.lev32; }
+    static float*& buf(AmrState::LevelStore& S, int w) { return S.buf32[w]; }
+};
+
+// The multigrid half of the executor in precision T on the context's stream (FP64; FP32 for the
+// inner cycles of the mixed-precision solve, whose level-0 correction is still the FP64
+// one-level V-cycle).
+template <typename T>
+struct GpuMl {
     mac_ctx* c;
     AmrState* A;
     int nlev;
     Geo geo;
     bool singular;
     int err = MAC_OK;
-    // this call's inputs (device pointers, level-domain arrays)
-    double* const* u = nullptr;            // [3 l + d]
-    const double* const* rho = nullptr;
-    const double* const* macrhs = nullptr;
-    const double* const* b0 = nullptr;
-    const double* const* b0e = nullptr;
-    int alt = 0;
 
-    Lev lev(int l) const { return A->L[l].lev; }
-    double* buf(int l, int which) const { return A->L[l].buf[which]; }
+    amr::LevT<T> lev(int l) const { return AmrAccess<T>::lev(A->L[l]); }
+    T* buf(int l, int which) const { return AmrAccess<T>::buf(A->L[l], which); }
     long ncell(int l) const { return A->L[l].ncell; }
     int blocks(long n) const { return blocks_for(n, c->sms); }
     void launched() {
@@ -390,70 +423,73 @@ struct GpuExec {
     }
     int error() const { return err; }
 
-    void defect(int l, const double* uu, const double* cu, const double* f, double* r) {
-        const Lev C = l ? lev(l - 1) : lev(l);
-        k_defect<<<blocks(ncell(l)), kThreads, 0, c->stream>>>(geo, lev(l), C, uu, cu, f, r, ncell(l));
+    void defect(int l, const T* uu, const T* cu, const T* f, T* r) {
+        const amr::LevT<T> C = l ? lev(l - 1) : lev(l);
+        k_defect<T><<<blocks(ncell(l)), kThreads, 0, c->stream>>>(geo, lev(l), C, uu, cu, f, r, ncell(l));
         launched();
     }
-    void gsrb(int l, double* uu, const double* f, int nu) {
+    void gsrb(int l, T* uu, const T* f, int nu) {
         for (int s = 0; s < nu; ++s)
             for (int colour = 0; colour < 2; ++colour) {
-                k_gsrb<<<blocks(ncell(l)), kThreads, 0, c->stream>>>(geo, lev(l), colour, uu, f, ncell(l));
+                k_gsrb<T><<<blocks(ncell(l)), kThreads, 0, c->stream>>>(geo, lev(l), colour, uu, f, ncell(l));
                 launched();
             }
     }
-    void reflux(int l, const double* uf, const double* uc, double* res) {
-        k_reflux<<<blocks(ncell(l - 1)), kThreads, 0, c->stream>>>(geo, lev(l), lev(l - 1), uf, uc, res, ncell(l - 1));
+    void reflux(int l, const T* uf, const T* uc, T* res) {
+        k_reflux<T><<<blocks(ncell(l - 1)), kThreads, 0, c->stream>>>(geo, lev(l), lev(l - 1), uf, uc, res, ncell(l - 1));
         launched();
     }
-    void restrict_cov(int l, const double* fine, double* crse) {
-        k_restrict<<<blocks(ncell(l - 1)), kThreads, 0, c->stream>>>(geo, lev(l), lev(l - 1), fine, crse, ncell(l - 1));
+    void restrict_cov(int l, const T* fine, T* crse) {
+        k_restrict<T><<<blocks(ncell(l - 1)), kThreads, 0, c->stream>>>(geo, lev(l), lev(l - 1), fine, crse, ncell(l - 1));
         launched();
     }
-    void prolong(int l, const double* uc, double* uf) {
-        k_prolong<<<blocks(ncell(l)), kThreads, 0, c->stream>>>(geo, lev(l), lev(l - 1), uc, uf, ncell(l));
+    void prolong(int l, const T* uc, T* uf) {
+        k_prolong<T><<<blocks(ncell(l)), kThreads, 0, c->stream>>>(geo, lev(l), lev(l - 1), uc, uf, ncell(l));
         launched();
     }
-    void axpy3(int l, double* uu, const double* hold, const double* du) {
-        k_axpy3<<<blocks(ncell(l)), kThreads, 0, c->stream>>>(lev(l), uu, hold, du, ncell(l));
+    void axpy3(int l, T* uu, const T* hold, const T* du) {
+        k_axpy3<T><<<blocks(ncell(l)), kThreads, 0, c->stream>>>(lev(l), uu, hold, du, ncell(l));
         launched();
     }
-    void add_region(int l, double* phi, const double* uu) {
-        k_add_region<<<blocks(ncell(l)), kThreads, 0, c->stream>>>(lev(l), phi, uu, ncell(l));
+    void add_region(int l, T* phi, const T* uu) {
+        k_add_region<T><<<blocks(ncell(l)), kThreads, 0, c->stream>>>(lev(l), phi, uu, ncell(l));
         launched();
     }
-    void zero(int l, double* x) {
-        if (!err && cudaMemsetAsync(x, 0, sizeof(double) * ncell(l), c->stream) != cudaSuccess) {
+    void zero(int l, T* x) {
+        if (!err && cudaMemsetAsync(x, 0, sizeof(T) * ncell(l), c->stream) != cudaSuccess) {
             set_last_cuda_error(cudaGetLastError(), "cudaMemsetAsync", __FILE__, __LINE__);
             err = MAC_ERR_CUDA;
         }
     }
-    void copy(int l, double* dst, const double* src) {
-        if (!err && cudaMemcpyAsync(dst, src, sizeof(double) * ncell(l), cudaMemcpyDeviceToDevice,
+    void copy(int l, T* dst, const T* src) {
+        if (!err && cudaMemcpyAsync(dst, src, sizeof(T) * ncell(l), cudaMemcpyDeviceToDevice,
                                     c->stream) != cudaSuccess) {
             set_last_cuda_error(cudaGetLastError(), "cudaMemcpyAsync", __FILE__, __LINE__);
             err = MAC_ERR_CUDA;
         }
     }
-    void swap_bufs(int l, int a, int b) { std::swap(A->L[l].buf[a], A->L[l].buf[b]); }
+    void swap_bufs(int l, int a, int b) { std::swap(AmrAccess<T>::buf(A->L[l], a), AmrAccess<T>::buf(A->L[l], b)); }
 
-    // Reduce `which` over the valid cells of every level (level_only >= 0: the region cells of
-    // that level alone) into A->out on the device.
-    void reduce(int which, int level_only, const double* x0 = nullptr) {
-        int nparts = 0;
-        for (int l = 0; l < nlev; ++l) {
-            if (level_only >= 0 && l != level_only) continue;
-            const double* x = (level_only >= 0 && x0) ? x0 : buf(l, which);
-            const Lev L = lev(l);
-            const double vol = L.h[0] * (geo.dm > 1 ? L.h[1] : 1.0) * (geo.dm > 2 ? L.h[2] : 1.0);
-            const int nb = std::min(kReduceBlocks, blocks(ncell(l)));
-            k_reduce<<<nb, kThreads, 0, c->stream>>>(L, x, vol, level_only < 0 ? 1 : 0,
-                                                     A->part + 4 * nparts, ncell(l));
-            launched();
-            nparts += nb;
-        }
+    // Partials of x over the valid cells (valid_only) or the region cells of level l, appended at
+    // slot *nparts of A->part.
+    template <typename U>
+    void reduce_level(int l, const U* x, int valid_only, int* nparts) {
+        const amr::LevT<U> L = AmrAccess<U>::lev(A->L[l]);
+        const double vol = L.h[0] * (geo.dm > 1 ? L.h[1] : 1.0) * (geo.dm > 2 ? L.h[2] : 1.0);
+        const int nb = std::min(kReduceBlocks, blocks(ncell(l)));
+        k_reduce<U><<<nb, kThreads, 0, c->stream>>>(L, x, vol, valid_only, A->part + 4 * *nparts, ncell(l));
+        launched();
+        *nparts += nb;
+    }
+    void finish_reduce(int nparts) {
         k_reduce_finish<<<1, kThreads, 0, c->stream>>>(A->part, nparts, A->out);
         launched();
+    }
+    // Reduce buf(which) over the valid cells of every level into A->out on the device.
+    void reduce(int which) {
+        int nparts = 0;
+        for (int l = 0; l < nlev; ++l) reduce_level<T>(l, buf(l, which), 1, &nparts);
+        finish_reduce(nparts);
     }
     bool fetch() {
         if (err) return false;
@@ -467,12 +503,12 @@ struct GpuExec {
         return true;
     }
     double valid_max(int which) {
-        reduce(which, -1);
+        reduce(which);
         if (!fetch()) return NAN;
         return A->h_out[2] > 0.0 ? NAN : A->h_out[1];
     }
     double valid_mean(int which) {
-        reduce(which, -1);
+        reduce(which);
         if (!fetch()) return NAN;
         return A->h_out[4];
     }
@@ -480,10 +516,70 @@ struct GpuExec {
         // the mean is still in A->out[4] from valid_mean (same stream, nothing in between)
         (void)m;
         for (int l = 0; l < nlev; ++l) {
-            k_sub_scalar<<<blocks(ncell(l)), kThreads, 0, c->stream>>>(lev(l), buf(l, which), A->out + 4, 1, ncell(l));
+            k_sub_scalar<T><<<blocks(ncell(l)), kThreads, 0, c->stream>>>(lev(l), buf(l, which), A->out + 4, 1, ncell(l));
             launched();
         }
     }
+
+    // One FP64 V-cycle of the level-0 multigrid on rhs from a zero guess into e (natural layout);
+    // for a singular problem the mean of the right-hand side is removed first and the mean of
+    // the correction after (the constant is in the null space of the composite operator).
+    int level0_fp64(const double* rhs, double* e) {
+        if (err) return err;
+        Level& F = c->lev[0];
+        double* r0 = A->L[0].buf[amr::kTmp];
+        const amr::LevT<double> L0 = A->L[0].lev;
+        if (cudaMemcpyAsync(r0, rhs, sizeof(double) * ncell(0), cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess)
+            err = MAC_ERR_CUDA;
+        if (!err && singular) {
+            int np = 0;
+            reduce_level<double>(0, r0, 0, &np);
+            finish_reduce(np);
+            k_sub_scalar<double><<<blocks(ncell(0)), kThreads, 0, c->stream>>>(L0, r0, A->out + 4, 0, ncell(0));
+            launched();
+        }
+        int rc = err ? err : natural_to_level0(c, r0, F.a64.f);
+        if (!rc && cudaMemsetAsync(F.a64.phi, 0, sizeof(double) * (size_t)F.d.ncell, c->stream) != cudaSuccess)
+            rc = MAC_ERR_CUDA;
+        if (!rc) rc = level0_fp64_vcycle(c);
+        if (!rc) rc = level0_to_natural(c, F.a64.phi, e);
+        if (!rc && singular) {
+            int np = 0;
+            reduce_level<double>(0, e, 0, &np);
+            finish_reduce(np);
+            k_sub_scalar<double><<<blocks(ncell(0)), kThreads, 0, c->stream>>>(L0, e, A->out + 4, 0, ncell(0));
+            launched();
+        }
+        if (rc && !err) err = rc;
+        return err;
+    }
+    int level0_correction(const T* rhs, T* e) {
+        if constexpr (std::is_same<T, double>::value) {
+            return level0_fp64(rhs, e);
+        } else {
+            // FP32 cycle: the level-0 correction in FP64 on scratch copies
+            double* r64 = A->L[0].buf[amr::kHold];
+            double* e64 = A->L[0].buf[amr::kDu];
+            k_to_double<<<blocks(ncell(0)), kThreads, 0, c->stream>>>(rhs, r64, ncell(0));
+            launched();
+            const int rc = level0_fp64(r64, e64);
+            if (rc) return rc;
+            k_to_single<<<blocks(ncell(0)), kThreads, 0, c->stream>>>(e64, e, ncell(0));
+            launched();
+            return err;
+        }
+    }
+};
+
+// The FP64 executor: the multigrid, the projection steps, and the hand-over to the FP32 cycles.
+struct GpuExec : GpuMl<double> {
+    // this call's inputs (device pointers, level-domain arrays)
+    double* const* u = nullptr;            // [3 l + d]
+    const double* const* rho = nullptr;
+    const double* const* macrhs = nullptr;
+    const double* const* b0 = nullptr;
+    const double* const* b0e = nullptr;
+    int alt = 0;
 
     int prepare_level0() {
         if (err) return err;
@@ -495,31 +591,21 @@ struct GpuExec {
         singular = c->singular;
         return rc;
     }
-    // One FP64 V-cycle of the level-0 multigrid on rhs from a zero guess into e (natural layout);
-    // for a singular problem the mean of the right-hand side is removed first and the mean of
-    // the correction after (the constant is in the null space of the composite operator).
-    int level0_correction(const double* rhs, double* e) {
-        if (err) return err;
-        Level& F = c->lev[0];
-        double* r0 = buf(0, amr::kTmp);
-        copy(0, r0, rhs);
-        if (singular) {
-            reduce(0, 0, r0);
-            k_sub_scalar<<<blocks(ncell(0)), kThreads, 0, c->stream>>>(lev(0), r0, A->out + 4, 0, ncell(0));
-            launched();
-        }
-        int rc = natural_to_level0(c, r0, F.a64.f);
-        if (!rc && cudaMemsetAsync(F.a64.phi, 0, sizeof(double) * (size_t)F.d.ncell, c->stream) != cudaSuccess)
-            rc = MAC_ERR_CUDA;
-        if (!rc) rc = level0_fp64_vcycle(c);
-        if (!rc) rc = level0_to_natural(c, F.a64.phi, e);
-        if (!rc && singular) {
-            reduce(0, 0, e);
-            k_sub_scalar<<<blocks(ncell(0)), kThreads, 0, c->stream>>>(lev(0), e, A->out + 4, 0, ncell(0));
-            launched();
-        }
-        if (rc && !err) err = rc;
-        return err;
+    void faces_to_single() {
+        for (int l = 0; l < nlev; ++l)
+            for (int d = 0; d < geo.dm; ++d) {
+                const long nf = amr::nfaces(lev(l), d);
+                k_to_single<<<blocks(nf), kThreads, 0, c->stream>>>(A->L[l].beta[d], A->L[l].beta32[d], nf);
+                launched();
+            }
+    }
+    void to_single(int l, const double* x, float* y) {
+        k_to_single<<<blocks(ncell(l)), kThreads, 0, c->stream>>>(x, y, ncell(l));
+        launched();
+    }
+    void accumulate(int l, double* phi, const float* e) {
+        k_accumulate<<<blocks(ncell(l)), kThreads, 0, c->stream>>>(lev(l), phi, e, ncell(l));
+        launched();
     }
 
     // ---- projection steps ----
@@ -620,6 +706,25 @@ int amr_configure(mac_ctx* c, int nlev, const int* nboxes, const int* box_lo, co
     return rc;
 }
 
+// FP32 copies of the levels for the mixed-precision solve (allocated on first use).
+int amr_ensure_single(mac_ctx* c) {
+    AmrState* A = c->amr;
+    if (A->L[0].buf32[0]) return MAC_OK;
+    for (AmrState::LevelStore& S : A->L) {
+        int rc = MAC_OK;
+        for (int d = 0; d < c->dm && !rc; ++d) rc = amr_alloc(A, &S.beta32[d], (size_t)amr::nfaces(S.lev, d));
+        for (int b = 0; b < amr::kNumBufs && !rc; ++b) rc = amr_alloc(A, &S.buf32[b], (size_t)S.ncell);
+        if (rc) return rc;
+        for (int d = 0; d < 3; ++d) {
+            S.lev32.n[d] = S.lev.n[d];
+            S.lev32.h[d] = S.lev.h[d];
+            S.lev32.b[d] = S.beta32[d];
+        }
+        S.lev32.mask = S.lev.mask;
+    }
+    return MAC_OK;
+}
+
 // The multi-level projection on level arrays already on the device (the caller's, or gathered
 // from fabs); fills the solve fields of *st and returns the status code.
 int ml_core(mac_ctx* c, double* const* umac, double* const* phi, const double* const* rho,
@@ -627,7 +732,12 @@ int ml_core(mac_ctx* c, double* const* umac, double* const* phi, const double* c
             const double* const* beta0_edge, mac_stats* st) {
     AmrState* A = c->amr;
     const int nl = A->nlev;
-    GpuExec ex{c, A, nl, A->geo, c->geom_singular};
+    GpuExec ex;
+    ex.c = c;
+    ex.A = A;
+    ex.nlev = nl;
+    ex.geo = A->geo;
+    ex.singular = c->geom_singular;
     ex.u = umac;
     ex.rho = rho;
     ex.macrhs = macrhs;
@@ -662,7 +772,21 @@ int ml_core(mac_ctx* c, double* const* umac, double* const* phi, const double* c
     amr::SolveStats S{};
     cudaEventRecord(c->ev[0], c->stream);
     if (!rc) {
-        rc = amr::amr_project(ex, rel, c->o.abs_eps, c->o.max_vcycles, c->o.nu1, c->o.nu2, &S);
+        if (c->o.precision == MAC_PREC_MIXED) {
+            // FP32 multi-level cycles (kMixedInner per FP64 step) under FP64 refinement
+            rc = amr_ensure_single(c);
+            GpuMl<float> ex32;
+            ex32.c = c;
+            ex32.A = A;
+            ex32.nlev = nl;
+            ex32.geo = A->geo;
+            ex32.singular = c->geom_singular;
+            if (!rc)
+                rc = amr::amr_project(ex, rel, c->o.abs_eps, c->o.max_vcycles, c->o.nu1, c->o.nu2,
+                                      &S, &ex32, kMixedInner);
+        } else {
+            rc = amr::amr_project(ex, rel, c->o.abs_eps, c->o.max_vcycles, c->o.nu1, c->o.nu2, &S);
+        }
         if (rc == 1) rc = MAC_ERR_NOT_CONVERGED;
         if (rc == -1 && S.status == -1) rc = MAC_ERR_NONFINITE;
         if (rc == MAC_OK && std::isnan(S.rel_resid)) rc = MAC_ERR_NONFINITE;

@@ -26,6 +26,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <type_traits>
 
 #if defined(__CUDACC__)
 #define AMR_HD __host__ __device__
@@ -47,59 +48,72 @@ struct Geo {
     int va;              // vertical direction (planar beta0 index): dm - 1
 };
 
-struct Lev {
+// A level with its face coefficients in precision T (FP64; FP32 for the inner cycles of the
+// mixed-precision solve).
+template <typename T>
+struct LevT {
     int n[3];                  // level-domain cells (1 along inactive directions)
     double h[3];
     const unsigned char* mask; // kIn / kCov per cell
-    const double* b[3];        // face coefficients, natural face layout (n[d] + 1 along d)
+    const T* b[3];             // face coefficients, natural face layout (n[d] + 1 along d)
 };
+using Lev = LevT<double>;
 
-AMR_HD inline long cix(const Lev& L, int i, int j, int k) {
+template <typename T>
+AMR_HD inline long cix(const LevT<T>& L, int i, int j, int k) {
     return (long)i + (long)L.n[0] * ((long)j + (long)L.n[1] * k);
 }
-AMR_HD inline long fix(const Lev& L, int d, int i, int j, int k) {
+template <typename T>
+AMR_HD inline long fix(const LevT<T>& L, int d, int i, int j, int k) {
     const long m0 = L.n[0] + (d == 0), m1 = L.n[1] + (d == 1);
     return (long)i + m0 * ((long)j + m1 * k);
 }
-AMR_HD inline long nfaces(const Lev& L, int d) {
+template <typename T>
+AMR_HD inline long nfaces(const LevT<T>& L, int d) {
     return (long)(L.n[0] + (d == 0)) * (L.n[1] + (d == 1)) * (L.n[2] + (d == 2));
 }
-AMR_HD inline long ncells(const Lev& L) { return (long)L.n[0] * L.n[1] * L.n[2]; }
+template <typename T>
+AMR_HD inline long ncells(const LevT<T>& L) { return (long)L.n[0] * L.n[1] * L.n[2]; }
 
 // Index q along d wrapped into the level domain; -1 beyond a non-periodic domain face.
-AMR_HD inline int wrap(const Geo& G, const Lev& L, int d, int q) {
+template <typename T>
+AMR_HD inline int wrap(const Geo& G, const LevT<T>& L, int d, int q) {
     const int n = L.n[d];
     if (q < 0) return G.per[d] ? q + n : -1;
     if (q >= n) return G.per[d] ? q - n : -1;
     return q;
 }
-AMR_HD inline bool in_region(const Lev& L, long c) { return (L.mask[c] & kIn) != 0; }
-AMR_HD inline bool is_valid(const Lev& L, long c) { return (L.mask[c] & (kIn | kCov)) == kIn; }
+template <typename T>
+AMR_HD inline bool in_region(const LevT<T>& L, long c) { return (L.mask[c] & kIn) != 0; }
+template <typename T>
+AMR_HD inline bool is_valid(const LevT<T>& L, long c) { return (L.mask[c] & (kIn | kCov)) == kIn; }
 
-AMR_HD inline double face_b(const Lev& L, int d, const int c[3], int s) {
+template <typename T>
+AMR_HD inline T face_b(const LevT<T>& L, int d, const int c[3], int s) {
     int f[3] = {c[0], c[1], c[2]};
     if (s > 0) f[d] += 1;
     return L.b[d][fix(L, d, f[0], f[1], f[2])];
 }
 
 // Coarse value (level C, array cu) at the fine ghost cell q seen across a face normal to d.
-AMR_HD inline double coarse_at_ghost(const Geo& G, const Lev& C, const int q[3], int d,
-                                     const double* cu) {
+template <typename T>
+AMR_HD inline T coarse_at_ghost(const Geo& G, const LevT<T>& C, const int q[3], int d,
+                                const T* cu) {
     int c[3];
     for (int e = 0; e < 3; ++e) c[e] = e < G.dm ? q[e] >> 1 : q[e];
-    const double v0 = cu[cix(C, c[0], c[1], c[2])];
-    double v = v0;
+    const T v0 = cu[cix(C, c[0], c[1], c[2])];
+    T v = v0;
     for (int t = 0; t < G.dm; ++t) {
         if (t == d) continue;
-        const double del = (q[t] & 1) ? 0.25 : -0.25;
+        const T del = (q[t] & 1) ? (T)0.25 : (T)-0.25;
         int m[3] = {c[0], c[1], c[2]}, p[3] = {c[0], c[1], c[2]};
         m[t] = wrap(G, C, t, c[t] - 1);
         p[t] = wrap(G, C, t, c[t] + 1);
         const bool hm = m[t] >= 0, hp = p[t] >= 0;
-        const double vm = hm ? cu[cix(C, m[0], m[1], m[2])] : 0.0;
-        const double vp = hp ? cu[cix(C, p[0], p[1], p[2])] : 0.0;
+        const T vm = hm ? cu[cix(C, m[0], m[1], m[2])] : (T)0;
+        const T vp = hp ? cu[cix(C, p[0], p[1], p[2])] : (T)0;
         if (hm && hp)
-            v += del * 0.5 * (vp - vm) + 0.5 * del * del * (vp - 2.0 * v0 + vm);
+            v += del * (T)0.5 * (vp - vm) + (T)0.5 * del * del * (vp - (T)2 * v0 + vm);
         else if (hp)
             v += del * (vp - v0);
         else if (hm)
@@ -110,17 +124,18 @@ AMR_HD inline double coarse_at_ghost(const Geo& G, const Lev& C, const int q[3],
 
 // Diagonal and off-diagonal parts of (L u)_c = diag u_c - off on level L (coarse level C for
 // the coarse-fine ghosts; cu null: zero coarse data).
-AMR_HD inline void cell_op(const Geo& G, const Lev& L, const Lev& C, const int c[3],
-                           const double* u, const double* cu, double& diag, double& off) {
-    diag = 0.0;
-    off = 0.0;
+template <typename T>
+AMR_HD inline void cell_op(const Geo& G, const LevT<T>& L, const LevT<T>& C, const int c[3],
+                           const T* u, const T* cu, T& diag, T& off) {
+    diag = 0;
+    off = 0;
     for (int d = 0; d < G.dm; ++d) {
-        const double ih2 = 1.0 / (L.h[d] * L.h[d]);
+        const T ih2 = (T)(1.0 / (L.h[d] * L.h[d]));
         for (int s = -1; s <= 1; s += 2) {
-            const double w = face_b(L, d, c, s) * ih2;
+            const T w = face_b(L, d, c, s) * ih2;
             const int qd = wrap(G, L, d, c[d] + s);
             if (qd < 0) {
-                if (s < 0 ? G.dlo[d] : G.dhi[d]) diag += 2.0 * w;
+                if (s < 0 ? G.dlo[d] : G.dhi[d]) diag += (T)2 * w;
                 continue;
             }
             int q[3] = {c[0], c[1], c[2]};
@@ -130,14 +145,15 @@ AMR_HD inline void cell_op(const Geo& G, const Lev& L, const Lev& C, const int c
                 diag += w;
                 off += w * u[qc];
             } else {
-                diag += (2.0 / 3.0) * w;
-                if (cu) off += (2.0 / 3.0) * w * coarse_at_ghost(G, C, q, d, cu);
+                diag += (T)(2.0 / 3.0) * w;
+                if (cu) off += (T)(2.0 / 3.0) * w * coarse_at_ghost(G, C, q, d, cu);
             }
         }
     }
 }
 
-AMR_HD inline void cell_coords(const Lev& L, long idx, int c[3]) {
+template <typename T>
+AMR_HD inline void cell_coords(const LevT<T>& L, long idx, int c[3]) {
     c[0] = (int)(idx % L.n[0]);
     const long r = idx / L.n[0];
     c[1] = (int)(r % L.n[1]);
@@ -145,39 +161,42 @@ AMR_HD inline void cell_coords(const Lev& L, long idx, int c[3]) {
 }
 
 // r = f - L u on a region cell, 0 elsewhere.
-AMR_HD inline void defect_cell(const Geo& G, const Lev& L, const Lev& C, long idx,
-                               const double* u, const double* cu, const double* f, double* r) {
+template <typename T>
+AMR_HD inline void defect_cell(const Geo& G, const LevT<T>& L, const LevT<T>& C, long idx,
+                               const T* u, const T* cu, const T* f, T* r) {
     if (!in_region(L, idx)) {
-        r[idx] = 0.0;
+        r[idx] = 0;
         return;
     }
     int c[3];
     cell_coords(L, idx, c);
-    double dg, off;
+    T dg, off;
     cell_op(G, L, C, c, u, cu, dg, off);
     r[idx] = f[idx] - (dg * u[idx] - off);
 }
 
 // Gauss-Seidel update of a region cell of the given colour, zero coarse data.
-AMR_HD inline void gsrb_cell(const Geo& G, const Lev& L, long idx, int colour, double* u,
-                             const double* f) {
+template <typename T>
+AMR_HD inline void gsrb_cell(const Geo& G, const LevT<T>& L, long idx, int colour, T* u,
+                             const T* f) {
     int c[3];
     cell_coords(L, idx, c);
     if (((c[0] + c[1] + c[2]) & 1) != colour || !in_region(L, idx)) return;
-    double dg, off;
-    cell_op(G, L, L, c, u, nullptr, dg, off);
+    T dg, off;
+    cell_op<T>(G, L, L, c, u, nullptr, dg, off);
     u[idx] = (f[idx] + off) / dg;
 }
 
 // Reflux into a valid coarse cell K (level C) next to cells covered by level F:
 // res += (T_coarse - mean T_fine) / h.  uc null: zero coarse data.
-AMR_HD inline void reflux_cell(const Geo& G, const Lev& F, const Lev& C, long kidx,
-                               const double* uf, const double* uc, double* res) {
+template <typename T>
+AMR_HD inline void reflux_cell(const Geo& G, const LevT<T>& F, const LevT<T>& C, long kidx,
+                               const T* uf, const T* uc, T* res) {
     if (!is_valid(C, kidx)) return;
     int c[3];
     cell_coords(C, kidx, c);
     const int ntan = 1 << (G.dm - 1);
-    double acc = 0.0;
+    T acc = 0;
     for (int d = 0; d < G.dm; ++d) {
         for (int s = -1; s <= 1; s += 2) {
             const int w = wrap(G, C, d, c[d] + s);
@@ -186,8 +205,8 @@ AMR_HD inline void reflux_cell(const Geo& G, const Lev& F, const Lev& C, long ki
             Q[d] = w;
             const long qc = cix(C, Q[0], Q[1], Q[2]);
             if (!(C.mask[qc] & kCov)) continue;
-            const double Tc = uc ? face_b(C, d, c, s) * (uc[kidx] - uc[qc]) / C.h[d] : 0.0;
-            double Tf = 0.0;
+            const T Tc = uc ? face_b(C, d, c, s) * (uc[kidx] - uc[qc]) / (T)C.h[d] : (T)0;
+            T Tf = 0;
             for (int a = 0; a < (1 << G.dm); ++a) {
                 if ((a >> d) & 1) continue;
                 int fc[3] = {0, 0, 0}, gq[3] = {0, 0, 0};
@@ -199,37 +218,39 @@ AMR_HD inline void reflux_cell(const Geo& G, const Lev& F, const Lev& C, long ki
                         fc[e] = gq[e] = 2 * c[e] + ((a >> e) & 1);
                     }
                 }
-                const double ufv = uf[cix(F, fc[0], fc[1], fc[2])];
-                const double g = ufv / 3.0 + (uc ? (2.0 / 3.0) * coarse_at_ghost(G, C, gq, d, uc) : 0.0);
-                Tf += face_b(F, d, fc, -s) * (g - ufv) / F.h[d];
+                const T ufv = uf[cix(F, fc[0], fc[1], fc[2])];
+                const T g = ufv / (T)3 + (uc ? (T)(2.0 / 3.0) * coarse_at_ghost(G, C, gq, d, uc) : (T)0);
+                Tf += face_b(F, d, fc, -s) * (g - ufv) / (T)F.h[d];
             }
-            acc += (Tc - Tf / ntan) / C.h[d];
+            acc += (Tc - Tf / (T)ntan) / (T)C.h[d];
         }
     }
     res[kidx] += acc;
 }
 
 // Covered coarse cell K (level C) = mean of its children (level F).
-AMR_HD inline void restrict_cell(const Geo& G, const Lev& F, const Lev& C, long kidx,
-                                 const double* fine, double* crse) {
+template <typename T>
+AMR_HD inline void restrict_cell(const Geo& G, const LevT<T>& F, const LevT<T>& C, long kidx,
+                                 const T* fine, T* crse) {
     if (!(C.mask[kidx] & kCov)) return;
     int c[3];
     cell_coords(C, kidx, c);
     const int r0 = G.dm > 0 ? 2 : 1, r1 = G.dm > 1 ? 2 : 1, r2 = G.dm > 2 ? 2 : 1;
-    double s = 0.0;
+    T s = 0;
     for (int c2 = 0; c2 < r2; ++c2)
         for (int c1 = 0; c1 < r1; ++c1)
             for (int c0 = 0; c0 < r0; ++c0)
                 s += fine[cix(F, c[0] * r0 + c0, c[1] * r1 + c1, c[2] * r2 + c2)];
-    crse[kidx] = s / (r0 * r1 * r2);
+    crse[kidx] = s / (T)(r0 * r1 * r2);
 }
 
 // uf = multilinear interpolation (3/4, 1/4 per direction) of uc on a region cell of level F,
 // 0 elsewhere; physical faces reflect (Dirichlet odd, others even).
-AMR_HD inline void prolong_cell(const Geo& G, const Lev& F, const Lev& C, long idx,
-                                const double* uc, double* uf) {
+template <typename T>
+AMR_HD inline void prolong_cell(const Geo& G, const LevT<T>& F, const LevT<T>& C, long idx,
+                                const T* uc, T* uf) {
     if (!in_region(F, idx)) {
-        uf[idx] = 0.0;
+        uf[idx] = 0;
         return;
     }
     int fi[3];
@@ -240,19 +261,19 @@ AMR_HD inline void prolong_cell(const Geo& G, const Lev& F, const Lev& C, long i
         pc[d] = act ? fi[d] >> 1 : fi[d];
         off[d] = act ? ((fi[d] & 1) ? 1 : -1) : 0;
     }
-    double s = 0.0;
+    T s = 0;
     for (int a2 = 0; a2 < (off[2] ? 2 : 1); ++a2)
         for (int a1 = 0; a1 < (off[1] ? 2 : 1); ++a1)
             for (int a0 = 0; a0 < (off[0] ? 2 : 1); ++a0) {
                 const int a[3] = {a0, a1, a2};
-                double w = 1.0, sgn = 1.0;
+                T w = 1, sgn = 1;
                 int q[3];
                 for (int d = 0; d < 3; ++d) {
                     if (!off[d]) {
                         q[d] = pc[d];
                         continue;
                     }
-                    w *= a[d] ? 0.25 : 0.75;
+                    w *= a[d] ? (T)0.25 : (T)0.75;
                     const int want = pc[d] + (a[d] ? off[d] : 0);
                     const int got = wrap(G, C, d, want);
                     if (got >= 0) {
@@ -268,7 +289,8 @@ AMR_HD inline void prolong_cell(const Geo& G, const Lev& F, const Lev& C, long i
 }
 
 // Whether the face (d, f) of level L borders a cell of its region.
-AMR_HD inline bool face_in_level(const Geo& G, const Lev& L, int d, const int f[3]) {
+template <typename T>
+AMR_HD inline bool face_in_level(const Geo& G, const LevT<T>& L, int d, const int f[3]) {
     int lo[3] = {f[0], f[1], f[2]}, hi[3] = {f[0], f[1], f[2]};
     lo[d] = wrap(G, L, d, f[d] - 1);
     hi[d] = wrap(G, L, d, f[d]);
@@ -276,7 +298,8 @@ AMR_HD inline bool face_in_level(const Geo& G, const Lev& L, int d, const int f[
            (hi[d] >= 0 && in_region(L, cix(L, hi[0], hi[1], hi[2])));
 }
 
-AMR_HD inline void face_coords(const Lev& L, int d, long idx, int f[3]) {
+template <typename T>
+AMR_HD inline void face_coords(const LevT<T>& L, int d, long idx, int f[3]) {
     const int m0 = L.n[0] + (d == 0), m1 = L.n[1] + (d == 1);
     f[0] = (int)(idx % m0);
     const long r = idx / m0;
@@ -389,6 +412,13 @@ AMR_HD inline void correct_face(const Geo& G, const Lev& L, const Lev& C, int d,
     u[idx] -= beta[idx] * g;
 }
 
+// ---- mixed precision: hand-over between the FP64 solution and the FP32 correction ------------
+AMR_HD inline void to_single_cell(long idx, const double* x, float* y) { y[idx] = (float)x[idx]; }
+template <typename T>
+AMR_HD inline void accumulate_cell(const LevT<T>& L, long idx, double* phi, const float* e) {
+    if (in_region(L, idx)) phi[idx] += (double)e[idx];
+}
+
 // ---- caller fabs <-> level arrays -------------------------------------------------------------
 //
 // One fab of the caller's layout on a level: box [lo, hi] in level indices, ng ghost cells,
@@ -484,8 +514,9 @@ struct SolveStats {
     double hist[64];
 };
 
+// Composite defect of buf(kPhi) against buf(kF) into buf(kRes) on every level.
 template <class E>
-double composite_residual(E& ex) {
+void composite_defect(E& ex) {
     const int nl = ex.nlev;
     for (int l = 0; l < nl; ++l)
         ex.defect(l, ex.buf(l, kPhi), l ? ex.buf(l - 1, kPhi) : nullptr, ex.buf(l, kF),
@@ -494,6 +525,11 @@ double composite_residual(E& ex) {
         ex.reflux(l, ex.buf(l, kPhi), ex.buf(l - 1, kPhi), ex.buf(l - 1, kRes));
         ex.restrict_cov(l, ex.buf(l, kRes), ex.buf(l - 1, kRes));
     }
+}
+
+template <class E>
+double composite_residual(E& ex) {
+    composite_defect(ex);
     return ex.valid_max(kRes);
 }
 
@@ -561,11 +597,64 @@ int amr_solve(E& ex, double rel_eps, double abs_eps, int max_cycles, int nu1, in
     return ex.error() ? ex.error() : S->status;
 }
 
+// Mixed precision: the FP64 composite residual, `inner` FP32 multi-level V-cycles on it from a
+// zero correction (ex32: FP32 copies of the levels and coefficients; its level-0 correction is
+// the FP64 one-level V-cycle), the correction added to the FP64 solution, until the FP64
+// composite residual meets the tolerance.
+template <class E, class E32>
+int amr_solve_mixed(E& ex, E32& ex32, double rel_eps, double abs_eps, int max_iters, int nu1,
+                    int nu2, int inner, SolveStats* S) {
+    const int nl = ex.nlev;
+    *S = SolveStats{};
+    if (ex.singular) ex.sub_valid(kF, ex.valid_mean(kF));
+    for (int l = nl - 1; l >= 1; --l) ex.restrict_cov(l, ex.buf(l, kPhi), ex.buf(l - 1, kPhi));
+    const double fnorm = ex.valid_max(kF);
+    S->fnorm = fnorm;
+    if (!(fnorm > 0.0)) {
+        for (int l = 0; l < nl; ++l) ex.zero(l, ex.buf(l, kPhi));
+        S->status = std::isnan(fnorm) ? -1 : 0;
+        return ex.error() ? ex.error() : S->status;
+    }
+    auto converged = [&](double r) {
+        return r <= rel_eps * fnorm || (abs_eps > 0.0 && r <= abs_eps);
+    };
+    double res = composite_residual(ex);
+    S->resid0 = res;
+    int it = 0;
+    while (!converged(res) && it < max_iters && !std::isnan(res)) {
+        for (int l = 0; l < nl; ++l) {
+            ex.to_single(l, ex.buf(l, kRes), ex32.buf(l, kF));
+            ex32.zero(l, ex32.buf(l, kPhi));
+        }
+        for (int v = 0; v < inner; ++v) {
+            if (v == 0)
+                for (int l = 0; l < nl; ++l) ex32.copy(l, ex32.buf(l, kRes), ex32.buf(l, kF));
+            else
+                composite_defect(ex32);
+            int rc = ml_vcycle(ex32, nu1, nu2);
+            if (rc) {
+                S->status = rc;
+                return rc;
+            }
+        }
+        for (int l = 0; l < nl; ++l) ex.accumulate(l, ex.buf(l, kPhi), ex32.buf(l, kPhi));
+        for (int l = nl - 1; l >= 1; --l) ex.restrict_cov(l, ex.buf(l, kPhi), ex.buf(l - 1, kPhi));
+        res = composite_residual(ex);
+        ++it;
+        if (S->nhist < 64) S->hist[S->nhist++] = res / fnorm;
+        if (ex.error() || ex32.error()) return ex.error() ? ex.error() : ex32.error();
+    }
+    S->cycles = it * inner;
+    S->rel_resid = res / fnorm;
+    S->status = converged(res) ? 0 : 1;
+    return ex.error() ? ex.error() : S->status;
+}
+
 // Multi-level MAC projection (Source/macproject.f90:51-328, nlevs > 1) on the executor's level
 // arrays: velocities, density, macrhs and beta0 already loaded; phi in buf(l, kPhi).
-template <class E>
+template <class E, class E32 = E>
 int amr_project(E& ex, double rel_eps, double abs_eps, int max_cycles, int nu1, int nu2,
-                SolveStats* S) {
+                SolveStats* S, E32* ex32 = nullptr, int inner = 0) {
     const int nl = ex.nlev;
     for (int l = 0; l < nl; ++l) ex.scale_b0(l, true);
     for (int l = nl - 1; l >= 1; --l) ex.edge_restrict(l);
@@ -577,7 +666,16 @@ int amr_project(E& ex, double rel_eps, double abs_eps, int max_cycles, int nu1, 
     }
     int rc = ex.prepare_level0();
     if (rc) return rc;
-    rc = amr_solve(ex, rel_eps, abs_eps, max_cycles, nu1, nu2, S);
+    if constexpr (!std::is_same<E32, E>::value) {
+        if (ex32) {
+            ex.faces_to_single();   // FP32 face coefficients of every level
+            rc = amr_solve_mixed(ex, *ex32, rel_eps, abs_eps, max_cycles, nu1, nu2, inner, S);
+        } else {
+            rc = amr_solve(ex, rel_eps, abs_eps, max_cycles, nu1, nu2, S);
+        }
+    } else {
+        rc = amr_solve(ex, rel_eps, abs_eps, max_cycles, nu1, nu2, S);
+    }
     if (rc < 0) return rc;
     const int status = rc;
     for (int l = 0; l < nl; ++l) ex.correct(l);

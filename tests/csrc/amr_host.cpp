@@ -20,59 +20,57 @@ using namespace mac;
 
 namespace {
 
-struct HostExec {
+// The multigrid half of the executor in precision T (FP64, or FP32 for the inner cycles of the
+// mixed-precision solve).  Level geometry and masks are shared with the FP64 executor.
+template <typename T>
+struct HostMl {
     int nlev = 0;
     amr::Geo geo{};
     bool singular = false;
     int err = 0;
-    std::vector<amr::Lev> L;
-    std::vector<std::vector<unsigned char>> mask;
-    std::vector<std::vector<double>> store[amr::kNumBufs];
-    std::vector<double*> bufp[amr::kNumBufs];
-    std::vector<std::vector<double>> beta[3];
-    orc::Ctx base;
-    orc_opts o{};
-    // this call's inputs
-    double* const* u = nullptr;
-    const double* const* rho = nullptr;
-    const double* const* macrhs = nullptr;
-    const double* const* b0 = nullptr;
-    const double* const* b0e = nullptr;
-    int alt = 0;
+    std::vector<amr::LevT<T>> L;
+    std::vector<std::vector<T>> store[amr::kNumBufs];
+    std::vector<T*> bufp[amr::kNumBufs];
+    std::vector<std::vector<T>> beta[3];
+    // the level-0 correction: the one-level FP64 V-cycle (of the FP64 executor for T = float)
+    struct Level0 {
+        orc::Ctx* base = nullptr;
+        bool singular = false;
+    } l0;
 
-    amr::Lev lev(int l) const { return L[l]; }
-    double* buf(int l, int which) const { return bufp[which][l]; }
+    amr::LevT<T> lev(int l) const { return L[l]; }
+    T* buf(int l, int which) const { return bufp[which][l]; }
     long ncell(int l) const { return amr::ncells(L[l]); }
     int error() const { return err; }
 
-    void defect(int l, const double* uu, const double* cu, const double* f, double* r) {
-        const amr::Lev C = l ? L[l - 1] : L[l];
+    void defect(int l, const T* uu, const T* cu, const T* f, T* r) {
+        const amr::LevT<T> C = l ? L[l - 1] : L[l];
         for (long i = 0; i < ncell(l); ++i) amr::defect_cell(geo, L[l], C, i, uu, cu, f, r);
     }
-    void gsrb(int l, double* uu, const double* f, int nu) {
+    void gsrb(int l, T* uu, const T* f, int nu) {
         for (int s = 0; s < nu; ++s)
             for (int colour = 0; colour < 2; ++colour)
                 for (long i = 0; i < ncell(l); ++i) amr::gsrb_cell(geo, L[l], i, colour, uu, f);
     }
-    void reflux(int l, const double* uf, const double* uc, double* res) {
+    void reflux(int l, const T* uf, const T* uc, T* res) {
         for (long i = 0; i < ncell(l - 1); ++i) amr::reflux_cell(geo, L[l], L[l - 1], i, uf, uc, res);
     }
-    void restrict_cov(int l, const double* fine, double* crse) {
+    void restrict_cov(int l, const T* fine, T* crse) {
         for (long i = 0; i < ncell(l - 1); ++i) amr::restrict_cell(geo, L[l], L[l - 1], i, fine, crse);
     }
-    void prolong(int l, const double* uc, double* uf) {
+    void prolong(int l, const T* uc, T* uf) {
         for (long i = 0; i < ncell(l); ++i) amr::prolong_cell(geo, L[l], L[l - 1], i, uc, uf);
     }
-    void axpy3(int l, double* uu, const double* hold, const double* du) {
+    void axpy3(int l, T* uu, const T* hold, const T* du) {
         for (long i = 0; i < ncell(l); ++i)
             if (amr::in_region(L[l], i)) uu[i] += hold[i] + du[i];
     }
-    void add_region(int l, double* phi, const double* uu) {
+    void add_region(int l, T* phi, const T* uu) {
         for (long i = 0; i < ncell(l); ++i)
             if (amr::in_region(L[l], i)) phi[i] += uu[i];
     }
-    void zero(int l, double* x) { std::fill(x, x + ncell(l), 0.0); }
-    void copy(int l, double* dst, const double* src) { std::copy(src, src + ncell(l), dst); }
+    void zero(int l, T* x) { std::fill(x, x + ncell(l), (T)0); }
+    void copy(int l, T* dst, const T* src) { std::copy(src, src + ncell(l), dst); }
     void swap_bufs(int l, int a, int b) { std::swap(bufp[a][l], bufp[b][l]); }
 
     double vol(int l) const {
@@ -103,8 +101,33 @@ struct HostExec {
     void sub_valid(int which, double m) {
         for (int l = 0; l < nlev; ++l)
             for (long i = 0; i < ncell(l); ++i)
-                if (amr::is_valid(L[l], i)) buf(l, which)[i] -= m;
+                if (amr::is_valid(L[l], i)) buf(l, which)[i] -= (T)m;
     }
+    int level0_correction(const T* rhs, T* e) {
+        orc::Level& B = l0.base->lev[0];
+        B.f.assign(rhs, rhs + ncell(0));
+        if (l0.singular) orc::sub_mean(B.f);
+        B.phi.assign(B.f.size(), 0.0);
+        orc::vcycle(*l0.base, 0);
+        if (l0.singular) orc::sub_mean(B.phi);
+        for (long i = 0; i < ncell(0); ++i) e[i] = (T)B.phi[i];
+        return 0;
+    }
+};
+
+struct HostExec : HostMl<double> {
+    std::vector<std::vector<unsigned char>> mask;
+    orc::Ctx base;
+    orc_opts o{};
+    HostMl<float>* v32 = nullptr;
+    // this call's inputs
+    double* const* u = nullptr;
+    const double* const* rho = nullptr;
+    const double* const* macrhs = nullptr;
+    const double* const* b0 = nullptr;
+    const double* const* b0e = nullptr;
+    int alt = 0;
+
     int prepare_level0() {
         const double* b[3] = {beta[0][0].data(), beta[1][0].data(),
                               geo.dm == 3 ? beta[2][0].data() : nullptr};
@@ -112,17 +135,25 @@ struct HostExec {
         base.o = o;
         orc::build_hierarchy(base, b, nullptr);
         singular = base.singular;
+        l0.base = &base;
+        l0.singular = singular;
+        if (v32) {
+            v32->singular = singular;
+            v32->l0.base = &base;
+            v32->l0.singular = singular;
+        }
         return 0;
     }
-    int level0_correction(const double* rhs, double* e) {
-        orc::Level& B = base.lev[0];
-        B.f.assign(rhs, rhs + ncell(0));
-        if (singular) orc::sub_mean(B.f);
-        B.phi.assign(B.f.size(), 0.0);
-        orc::vcycle(base, 0);
-        if (singular) orc::sub_mean(B.phi);
-        std::copy(B.phi.begin(), B.phi.end(), e);
-        return 0;
+    void faces_to_single() {
+        for (int l = 0; l < nlev; ++l)
+            for (int d = 0; d < geo.dm; ++d)
+                for (size_t i = 0; i < beta[d][l].size(); ++i) v32->beta[d][l][i] = (float)beta[d][l][i];
+    }
+    void to_single(int l, const double* x, float* y) {
+        for (long i = 0; i < ncell(l); ++i) amr::to_single_cell(i, x, y);
+    }
+    void accumulate(int l, double* phi, const float* e) {
+        for (long i = 0; i < ncell(l); ++i) amr::accumulate_cell(L[l], i, phi, e);
     }
     void scale_b0(int l, bool mult) {
         if (!b0) return;
@@ -163,6 +194,36 @@ struct HostExec {
     }
 };
 
+// Level storage of one precision from the FP64 executor's geometry and masks.
+template <typename T>
+void build_levels(HostMl<T>& M, const HostExec& E0) {
+    const HostExec& E = E0;
+    const std::vector<amr::Lev> geom = E.L;   // (M may be E itself)
+    M.nlev = E.nlev;
+    M.geo = E.geo;
+    M.L.assign(E.nlev, amr::LevT<T>{});
+    for (int b = 0; b < amr::kNumBufs; ++b) {
+        M.store[b].assign(E.nlev, {});
+        M.bufp[b].assign(E.nlev, nullptr);
+    }
+    for (int d = 0; d < 3; ++d) M.beta[d].assign(E.nlev, {});
+    for (int l = 0; l < E.nlev; ++l) {
+        amr::LevT<T>& V = M.L[l];
+        for (int d = 0; d < 3; ++d) {
+            V.n[d] = geom[l].n[d];
+            V.h[d] = geom[l].h[d];
+        }
+        V.mask = E.mask[l].data();
+        const long N = amr::ncells(V);
+        for (int b = 0; b < amr::kNumBufs; ++b) {
+            M.store[b][l].assign((size_t)N, (T)0);
+            M.bufp[b][l] = M.store[b][l].data();
+        }
+        for (int d = 0; d < E.geo.dm; ++d) M.beta[d][l].assign((size_t)amr::nfaces(V, d), (T)0);
+        for (int d = 0; d < 3; ++d) V.b[d] = d < E.geo.dm ? M.beta[d][l].data() : nullptr;
+    }
+}
+
 // Masks from the boxes (no layout validation here: the oracle's own checks cover it).
 void build(HostExec& E, const orc_opts* o, int nlev, const int* nboxes, const int* boxes) {
     E.o = *o;
@@ -176,24 +237,13 @@ void build(HostExec& E, const orc_opts* o, int nlev, const int* nboxes, const in
     }
     E.L.assign(nlev, amr::Lev{});
     E.mask.assign(nlev, {});
-    for (int b = 0; b < amr::kNumBufs; ++b) {
-        E.store[b].assign(nlev, {});
-        E.bufp[b].assign(nlev, nullptr);
-    }
-    for (int d = 0; d < 3; ++d) E.beta[d].assign(nlev, {});
     for (int l = 0; l < nlev; ++l) {
         amr::Lev& V = E.L[l];
         for (int d = 0; d < 3; ++d) {
             V.n[d] = d < o->dm ? (o->n[d] << l) : 1;
             V.h[d] = d < o->dm ? o->dx[d] / (double)(1 << l) : o->dx[d];
         }
-        const long N = amr::ncells(V);
-        E.mask[l].assign((size_t)N, l == 0 ? amr::kIn : 0);
-        for (int b = 0; b < amr::kNumBufs; ++b) {
-            E.store[b][l].assign((size_t)N, 0.0);
-            E.bufp[b][l] = E.store[b][l].data();
-        }
-        for (int d = 0; d < o->dm; ++d) E.beta[d][l].assign((size_t)amr::nfaces(V, d), 0.0);
+        E.mask[l].assign((size_t)amr::ncells(V), l == 0 ? amr::kIn : 0);
     }
     const int* bx = boxes;
     for (int l = 1; l < nlev; ++l)
@@ -211,10 +261,8 @@ void build(HostExec& E, const orc_opts* o, int nlev, const int* nboxes, const in
             for (int d = 0; d < 3; ++d) p[d] = d < o->dm ? c[d] >> 1 : c[d];
             E.mask[l - 1][amr::cix(E.L[l - 1], p[0], p[1], p[2])] |= amr::kCov;
         }
-    for (int l = 0; l < nlev; ++l) {
-        E.L[l].mask = E.mask[l].data();
-        for (int d = 0; d < 3; ++d) E.L[l].b[d] = d < o->dm ? E.beta[d][l].data() : nullptr;
-    }
+    for (int l = 0; l < nlev; ++l) E.L[l].mask = E.mask[l].data();
+    build_levels<double>(E, E);
 }
 
 }  // namespace
@@ -223,12 +271,29 @@ extern "C" {
 
 // The library's multi-level projection run on the host; arguments as orc_macproject_ml
 // (phi[l] in/out, umac[3 l + d] in/out).  Returns the solve status (0 converged).
+int amrh_macproject_prec(const orc_opts* o, int nlev, const int* nboxes, const int* boxes,
+                         double* const* umac, double* const* phi, const double* const* rho,
+                         const double* const* macrhs, const double* const* beta0,
+                         const double* const* beta0_edge, int inner, double* stats_out);
+
 int amrh_macproject(const orc_opts* o, int nlev, const int* nboxes, const int* boxes,
                     double* const* umac, double* const* phi, const double* const* rho,
                     const double* const* macrhs, const double* const* beta0,
                     const double* const* beta0_edge, double* stats_out) {
+    return amrh_macproject_prec(o, nlev, nboxes, boxes, umac, phi, rho, macrhs, beta0,
+                                beta0_edge, 0, stats_out);
+}
+
+// inner > 0: the mixed-precision solve, `inner` FP32 multi-level V-cycles per FP64 step.
+int amrh_macproject_prec(const orc_opts* o, int nlev, const int* nboxes, const int* boxes,
+                         double* const* umac, double* const* phi, const double* const* rho,
+                         const double* const* macrhs, const double* const* beta0,
+                         const double* const* beta0_edge, int inner, double* stats_out) {
     HostExec E;
     build(E, o, nlev, nboxes, boxes);
+    HostMl<float> E32;
+    build_levels<float>(E32, E);
+    E.v32 = &E32;
     E.u = umac;
     E.rho = rho;
     E.macrhs = macrhs;
@@ -239,7 +304,8 @@ int amrh_macproject(const orc_opts* o, int nlev, const int* nboxes, const int* b
         E.bufp[amr::kPhi][l] = phi[l];
     }
     amr::SolveStats S{};
-    const int rc = amr::amr_project(E, o->rel_eps, o->abs_eps, o->max_vcycles, o->nu1, o->nu2, &S);
+    const int rc = amr::amr_project(E, o->rel_eps, o->abs_eps, o->max_vcycles, o->nu1, o->nu2,
+                                    &S, inner > 0 ? &E32 : nullptr, inner);
     if (stats_out) {
         stats_out[0] = rc;
         stats_out[1] = S.cycles;

@@ -37,13 +37,16 @@ def host_lib(tmp_path_factory):
     L.amrh_macproject.argtypes = [P(O.OrcOpts), ctypes.c_int, ip, ip, pd, pd, pd, pd, pd, pd,
                                   P(ctypes.c_double)]
     L.amrh_macproject.restype = ctypes.c_int
+    L.amrh_macproject_prec.argtypes = [P(O.OrcOpts), ctypes.c_int, ip, ip, pd, pd, pd, pd, pd, pd,
+                                       ctypes.c_int, P(ctypes.c_double)]
+    L.amrh_macproject_prec.restype = ctypes.c_int
     L.amrh_fabs.argtypes = [P(O.OrcOpts), ctypes.c_int, ip, ip, ctypes.c_int, ctypes.c_int,
                             ctypes.c_int, ctypes.c_int, ctypes.c_int, pd, P(ctypes.c_double)]
     L.amrh_fabs.restype = None
     return L
 
 
-def run_host(L, c, rel_eps):
+def run_host(L, c, rel_eps, inner=0):
     nlev = c["nlev"]
     dm = c["dm"]
     phi = [np.zeros_like(p, order="F") for p in c["phi"]]
@@ -60,18 +63,21 @@ def run_host(L, c, rel_eps):
                 rel_eps, -1.0, 200, 2, 2, 10, O.EPS_MAC_BOTTOM, 200, False, 0)
     nb, bx = O._ml_layout(c["n0"], c["boxes"])
     st = (ctypes.c_double * 4)()
-    rc = L.amrh_macproject(ctypes.byref(o), nlev, nb.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
-                           bx.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), O._ptr_array(up),
-                           O._ptr_array(phi), O._ptr_array(rho), O._ptr_array(mr),
-                           O._ptr_array(b0), O._ptr_array(b0e), st)
+    rc = L.amrh_macproject_prec(ctypes.byref(o), nlev,
+                                nb.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                bx.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), O._ptr_array(up),
+                                O._ptr_array(phi), O._ptr_array(rho), O._ptr_array(mr),
+                                O._ptr_array(b0), O._ptr_array(b0e), int(inner), st)
     return rc, u, phi, list(st)
 
 
+@pytest.mark.parametrize("inner", [0, 2])
 @pytest.mark.parametrize("name", sorted(AMR_CASES))
-def test_library_amr_code_on_host_matches_golden(host_lib, name):
+def test_library_amr_code_on_host_matches_golden(host_lib, name, inner):
+    # inner = 0: the FP64 solve; inner = 2: FP32 multi-level cycles under FP64 refinement
     c = load_amr(name)
     H = G.Hierarchy(c["n0"], c["dx0"], c["bc_lo"], c["bc_hi"], c["boxes"])
-    rc, u, phi, st = run_host(host_lib, c, 1e-12)
+    rc, u, phi, st = run_host(host_lib, c, 1e-12, inner=inner)
     assert rc == 0 and st[2] <= 1e-12, st
     assert phi_err(H, phi, c["phi"]) <= 1e-9
     assert u_err(H, u, c["unew"]) <= 1e-9

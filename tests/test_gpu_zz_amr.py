@@ -15,7 +15,7 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 
-def _run(c, strict=True, rho=None, boxes=None, **opts):
+def _run(c, strict=True, rho=None, boxes=None, precision="fp64", **opts):
     dev = torch.device("cuda", 0)
     t = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a).transpose())).to(dev)  # noqa: E731
     nlev = c["nlev"]
@@ -27,7 +27,7 @@ def _run(c, strict=True, rho=None, boxes=None, **opts):
     b0 = [t(b) for b in c["beta0"]]
     b0e = [t(b) for b in c["beta0_edge"]]
     P = MacProjector(Layout(c["n0"], [((0,) * dm, tuple(v - 1 for v in c["n0"]))]), c["dx0"],
-                     BcTower(c["bc_lo"], c["bc_hi"]), precision="fp64",
+                     BcTower(c["bc_lo"], c["bc_hi"]), precision=precision,
                      stream=torch.cuda.current_stream().cuda_stream, **opts)
     try:
         P.set_amr(boxes if boxes is not None else c["boxes"])
@@ -43,12 +43,14 @@ def _run(c, strict=True, rho=None, boxes=None, **opts):
     return [[back(x) for x in u[l]] for l in range(nlev)], [back(p) for p in phi], st
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("name", sorted(AMR_CASES))
-def test_amr_projection_matches_golden(name):
+def test_amr_projection_matches_golden(name, precision):
     c = load_amr(name)
     H = G.Hierarchy(c["n0"], c["dx0"], c["bc_lo"], c["bc_hi"], c["boxes"])
-    # rel_eps 1e-13 -> the composite tolerance min(1e-13 * 10^(nlev-1), 1e-8)
-    u, phi, st = _run(c, rel_eps=1e-13)
+    # rel_eps 1e-13 -> the composite tolerance min(1e-13 * 10^(nlev-1), 1e-8); mixed: FP32
+    # multi-level cycles under FP64 refinement, the same tolerance on the FP64 residual
+    u, phi, st = _run(c, rel_eps=1e-13, precision=precision)
     assert st["status"] == 0 and st["rel_resid"] <= 1e-13 * 10 ** (c["nlev"] - 1)
     assert phi_err(H, phi, c["phi"]) <= 1e-9
     assert u_err(H, u, c["unew"]) <= 1e-9
