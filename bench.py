@@ -350,7 +350,8 @@ def run_extra(args, rank, world, local):
     if args.workload == "amr":
         c = _amr_inputs(AMR_N0, AMR_FINE, args.seed + rank)
         lay = Layout.tiled(c.n0, AMR_BOX)
-        P = MacProjector(lay, c.dx0, BcTower(c.bc_lo, c.bc_hi), precision="fp64",
+        # mixed precision: FP32 multi-level cycles under FP64 refinement (FP64 printed too)
+        P = MacProjector(lay, c.dx0, BcTower(c.bc_lo, c.bc_hi), precision="mixed",
                          stream=stream.cuda_stream)
         P.set_amr(c.boxes)
         u0 = [[to_dev(x) for x in c.umac[l]] for l in range(2)]
@@ -403,22 +404,29 @@ def run_extra(args, rank, world, local):
     K = args.steps
     value = world * K / (ms / 1e3)
     fp64 = None
+    # the FP64 rate of the same workload
     if args.workload == "hg":
         P = MacProjector(lay, tuple(1.0 / v for v in HG_N),
                          BcTower((-1, -1, 2), (-1, -1, 2)), precision="fp64",
                          stream=stream.cuda_stream)
         work = [(fields["unew"].clone(), fields["gpi"].clone(), fields["pi"].clone())
                 for _ in range(nsteps)]
-        one(0)
-        torch.cuda.synchronize()
-        e0.record(stream)
-        st64 = [one(k) for k in range(1, nsteps)]
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms64 = e0.elapsed_time(e1) / (nsteps - 1)
-        P.close()
-        fp64 = {"value": 1e3 / ms64, "unit": UNIT, "ms_per_step": ms64,
-                "vcycles": st64[-1]["vcycles"], "rel_resid": st64[-1]["rel_resid"]}
+    else:
+        P = MacProjector(lay, c.dx0, BcTower(c.bc_lo, c.bc_hi), precision="fp64",
+                         stream=stream.cuda_stream)
+        P.set_amr(c.boxes)
+        work = [([[x.clone() for x in u0[l]] for l in range(2)],
+                 [torch.zeros_like(r) for r in rho]) for _ in range(nsteps)]
+    one(0)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    st64 = [one(k) for k in range(1, nsteps)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms64 = e0.elapsed_time(e1) / (nsteps - 1)
+    P.close()
+    fp64 = {"value": 1e3 / ms64, "unit": UNIT, "ms_per_step": ms64,
+            "vcycles": st64[-1]["vcycles"], "rel_resid": st64[-1]["rel_resid"]}
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         secs = cpu_step()
@@ -431,9 +439,8 @@ def run_extra(args, rank, world, local):
            "gpu_launches": sum(s["launches"] for s in stats),
            "vcycles": stats[-1]["vcycles"], "rel_resid": max(s["rel_resid"] for s in stats),
            "clocks": ck}
-    if fp64 is not None:
-        out["fp64"] = fp64
-        out["dtype"] = "f32 V-cycles + f64 refinement"
+    out["fp64"] = fp64
+    out["dtype"] = "f32 V-cycles + f64 refinement"
     if rank == 0:
         print(json.dumps(out))
     return 0
