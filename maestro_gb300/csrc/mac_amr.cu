@@ -200,12 +200,31 @@ __global__ void k_check_rho(Geo G, Lev L, const double* rho, int* flag, long N) 
                 if (q < 0) continue;
                 int p[3] = {c[0], c[1], c[2]};
                 p[d] = q;
-                used = amr::in_region(L, amr::cix(L, p[0], p[1], p[2]));
+                used = amr::inside(L, p) && amr::in_region(L, amr::cix(L, p[0], p[1], p[2]));
             }
         if (!used) continue;
         const double v = rho[idx];
         if (!(v > 0.0) || !(v < INFINITY)) atomicExch(flag, 1);
     }
+}
+
+// The caller's whole-level-domain arrays <-> the level's box arrays (back: the level's own faces
+// and region cells only).
+__global__ void k_full_to_box_faces(Lev L, int d, const double* full, double* box, long N) {
+    AMR_LOOP(N) box[idx] = full[amr::full_face(L, d, idx)];
+}
+__global__ void k_full_to_box_cells(Lev L, const double* full, double* box, long N) {
+    AMR_LOOP(N) box[idx] = full[amr::full_cell(L, idx)];
+}
+__global__ void k_box_to_full_faces(Geo G, Lev L, int d, const double* box, double* full, long N) {
+    AMR_LOOP(N) {
+        int f[3];
+        amr::face_coords(L, d, idx, f);
+        if (amr::face_in_level(G, L, d, f)) full[amr::full_face(L, d, idx)] = box[idx];
+    }
+}
+__global__ void k_box_to_full_cells(Lev L, const double* box, double* full, long N) {
+    AMR_LOOP(N) if (amr::in_region(L, idx)) full[amr::full_cell(L, idx)] = box[idx];
 }
 
 __global__ void k_to_single(const double* x, float* y, long N) {
@@ -314,26 +333,30 @@ int amr_alloc(AmrState* A, T** p, size_t n) {
     return MAC_OK;
 }
 
-// Host-side layout check and masks (alignment to the ratio 2, boxes inside the level domain,
-// proper nesting with one coarse cell of buffer, diagonals included).
+// Host-side layout check, level boxes and masks (alignment to the ratio 2, boxes inside the level
+// domain, proper nesting with one coarse cell of buffer, diagonals included).  Each level's
+// arrays cover the bounding box of its boxes grown by one cell (amr::level_box); level 0 the
+// domain.
 int build_masks(const mac_ctx* c, int nlev, const int* nboxes, const int* box_lo,
                 const int* box_hi, std::vector<std::vector<unsigned char>>& masks,
-                std::vector<std::vector<int>>& boxes, int n_out[][3]) {
+                std::vector<std::vector<int>>& boxes, std::vector<Lev>& geom) {
     const int dm = c->dm;
     masks.assign(nlev, {});
     boxes.assign(nlev, {});
-    for (int l = 0; l < nlev; ++l) {
-        long N = 1;
-        for (int d = 0; d < 3; ++d) {
-            n_out[l][d] = d < dm ? (c->n[d] << l) : 1;
-            N *= n_out[l][d];
-        }
-        if (N > (1L << 31)) return MAC_ERR_TOO_LARGE;
-        masks[l].assign((size_t)N, l == 0 ? amr::kIn : 0);
-    }
+    geom.assign(nlev, Lev{});
+    int per[3];
+    for (int d = 0; d < 3; ++d) per[d] = d < dm && c->bc_lo[d] == MAC_BC_PER;
     int off = 0;
-    for (int l = 1; l < nlev; ++l) {
+    for (int l = 0; l < nlev; ++l) {
+        Lev& V = geom[l];
+        for (int d = 0; d < 3; ++d) {
+            V.n[d] = d < dm ? (c->n[d] << l) : 1;
+            V.lo[d] = 0;
+            V.ext[d] = V.n[d];
+        }
+        if (l == 0) continue;
         if (nboxes[l] < 1) return MAC_ERR_INVALID;
+        int rlo[3] = {1 << 30, 1 << 30, 1 << 30}, rhi[3] = {-1, -1, -1};
         for (int b = 0; b < nboxes[l]; ++b, ++off) {
             int lo[3], hi[3];
             for (int d = 0; d < 3; ++d) {
@@ -343,45 +366,55 @@ int build_masks(const mac_ctx* c, int nlev, const int* nboxes, const int* box_lo
                     if (lo[d] != 0 || hi[d] != 0) return MAC_ERR_INVALID;
                     continue;
                 }
-                if (lo[d] < 0 || hi[d] >= n_out[l][d] || hi[d] < lo[d]) return MAC_ERR_INVALID;
+                if (lo[d] < 0 || hi[d] >= V.n[d] || hi[d] < lo[d]) return MAC_ERR_INVALID;
                 if ((lo[d] & 1) || !(hi[d] & 1)) return MAC_ERR_INVALID;
             }
-            for (int d = 0; d < 3; ++d) boxes[l].push_back(lo[d]);
+            for (int d = 0; d < 3; ++d) {
+                boxes[l].push_back(lo[d]);
+                rlo[d] = std::min(rlo[d], lo[d]);
+                rhi[d] = std::max(rhi[d], hi[d]);
+            }
             for (int d = 0; d < 3; ++d) boxes[l].push_back(hi[d]);
-            for (int k = lo[2]; k <= hi[2]; ++k)
-                for (int j = lo[1]; j <= hi[1]; ++j)
-                    for (int i = lo[0]; i <= hi[0]; ++i)
-                        masks[l][(size_t)i + (size_t)n_out[l][0] * (j + (size_t)n_out[l][1] * k)] = amr::kIn;
         }
+        amr::level_box(dm, V.n, per, rlo, rhi, V.lo, V.ext);
+    }
+    for (int l = 0; l < nlev; ++l) {
+        const Lev& V = geom[l];
+        const long N = amr::ncells(V);
+        if (N > (1L << 31)) return MAC_ERR_TOO_LARGE;
+        masks[l].assign((size_t)N, l == 0 ? amr::kIn : 0);
+        for (size_t q = 0; q + 5 < boxes[l].size(); q += 6)
+            for (int k = boxes[l][q + 2]; k <= boxes[l][q + 5]; ++k)
+                for (int j = boxes[l][q + 1]; j <= boxes[l][q + 4]; ++j)
+                    for (int i = boxes[l][q]; i <= boxes[l][q + 3]; ++i)
+                        masks[l][(size_t)amr::cix(V, i, j, k)] = amr::kIn;
     }
     auto wrapq = [&](int l, int d, int q) {
-        const int n = n_out[l][d];
-        const bool per = c->bc_lo[d] == MAC_BC_PER;
-        if (q < 0) return per ? q + n : -1;
-        if (q >= n) return per ? q - n : -1;
+        const int n = geom[l].n[d];
+        if (q < 0) return per[d] ? q + n : -1;
+        if (q >= n) return per[d] ? q - n : -1;
         return q;
     };
     for (int l = 1; l < nlev; ++l) {
-        const int* nf = n_out[l];
-        const int* nc = n_out[l - 1];
-        for (int k = 0; k < nf[2]; ++k)
-            for (int j = 0; j < nf[1]; ++j)
-                for (int i = 0; i < nf[0]; ++i) {
-                    if (!(masks[l][(size_t)i + (size_t)nf[0] * (j + (size_t)nf[1] * k)] & amr::kIn))
-                        continue;
-                    const int cc[3] = {dm > 0 ? i >> 1 : i, dm > 1 ? j >> 1 : j, dm > 2 ? k >> 1 : k};
-                    masks[l - 1][(size_t)cc[0] + (size_t)nc[0] * (cc[1] + (size_t)nc[1] * cc[2])] |= amr::kCov;
-                    for (int a2 = -(dm > 2); a2 <= (dm > 2); ++a2)
-                        for (int a1 = -(dm > 1); a1 <= (dm > 1); ++a1)
-                            for (int a0 = -1; a0 <= 1; ++a0) {
-                                const int q0 = wrapq(l - 1, 0, cc[0] + a0);
-                                const int q1 = wrapq(l - 1, 1, cc[1] + a1);
-                                const int q2 = wrapq(l - 1, 2, cc[2] + a2);
-                                if (q0 < 0 || q1 < 0 || q2 < 0) continue;
-                                if (!(masks[l - 1][(size_t)q0 + (size_t)nc[0] * (q1 + (size_t)nc[1] * q2)] & amr::kIn))
-                                    return MAC_ERR_INVALID;
-                            }
-                }
+        const Lev& F = geom[l];
+        const Lev& K = geom[l - 1];
+        for (long idx = 0; idx < amr::ncells(F); ++idx) {
+            if (!(masks[l][(size_t)idx] & amr::kIn)) continue;
+            int fc[3];
+            amr::cell_coords(F, idx, fc);
+            const int cc[3] = {dm > 0 ? fc[0] >> 1 : fc[0], dm > 1 ? fc[1] >> 1 : fc[1],
+                               dm > 2 ? fc[2] >> 1 : fc[2]};
+            masks[l - 1][(size_t)amr::cix(K, cc[0], cc[1], cc[2])] |= amr::kCov;
+            for (int a2 = -(dm > 2); a2 <= (dm > 2); ++a2)
+                for (int a1 = -(dm > 1); a1 <= (dm > 1); ++a1)
+                    for (int a0 = -1; a0 <= 1; ++a0) {
+                        const int q[3] = {wrapq(l - 1, 0, cc[0] + a0), wrapq(l - 1, 1, cc[1] + a1),
+                                          wrapq(l - 1, 2, cc[2] + a2)};
+                        if (q[0] < 0 || q[1] < 0 || q[2] < 0) continue;
+                        if (!amr::inside(K, q) || !(masks[l - 1][(size_t)amr::cix(K, q[0], q[1], q[2])] & amr::kIn))
+                            return MAC_ERR_INVALID;
+                    }
+        }
     }
     return MAC_OK;
 }
@@ -656,8 +689,8 @@ int amr_configure(mac_ctx* c, int nlev, const int* nboxes, const int* box_lo, co
     if (nlev < 2 || nlev > amr::kMaxLevels || !nboxes || !box_lo || !box_hi) return MAC_ERR_INVALID;
     std::vector<std::vector<unsigned char>> masks;
     std::vector<std::vector<int>> boxes;
-    int n[amr::kMaxLevels][3];
-    int rc = build_masks(c, nlev, nboxes, box_lo, box_hi, masks, boxes, n);
+    std::vector<Lev> geom;
+    int rc = build_masks(c, nlev, nboxes, box_lo, box_hi, masks, boxes, geom);
     if (rc) return rc;
     amr_release(c);
     AmrState* A = new AmrState();
@@ -675,12 +708,13 @@ int amr_configure(mac_ctx* c, int nlev, const int* nboxes, const int* box_lo, co
     A->L.assign(nlev, AmrState::LevelStore());
     for (int l = 0; l < nlev && !rc; ++l) {
         AmrState::LevelStore& S = A->L[l];
-        long N = 1;
         for (int d = 0; d < 3; ++d) {
-            S.lev.n[d] = n[l][d];
+            S.lev.n[d] = geom[l].n[d];
+            S.lev.lo[d] = geom[l].lo[d];
+            S.lev.ext[d] = geom[l].ext[d];
             S.lev.h[d] = d < c->dm ? c->dx[d] / (double)(1 << l) : c->dx[d];
-            N *= n[l][d];
         }
+        const long N = amr::ncells(S.lev);
         S.ncell = N;
         rc = amr_alloc(A, &S.mask, (size_t)N);
         for (int d = 0; d < c->dm && !rc; ++d) rc = amr_alloc(A, &S.beta[d], (size_t)amr::nfaces(S.lev, d));
@@ -717,6 +751,8 @@ int amr_ensure_single(mac_ctx* c) {
         if (rc) return rc;
         for (int d = 0; d < 3; ++d) {
             S.lev32.n[d] = S.lev.n[d];
+            S.lev32.lo[d] = S.lev.lo[d];
+            S.lev32.ext[d] = S.lev.ext[d];
             S.lev32.h[d] = S.lev.h[d];
             S.lev32.b[d] = S.beta32[d];
         }
@@ -1040,6 +1076,67 @@ int ml_fabs(mac_ctx* c, int ptr_kind, double* const* umac, int ng_u, double* con
     return solve_rc;
 }
 
+
+// Whole-level-domain entry: the caller's arrays are copied into the levels' box arrays, projected,
+// and the levels' own faces and region cells copied back.
+int ml_dense(mac_ctx* c, double* const* umac, double* const* phi, const double* const* rho,
+             const double* const* macrhs, const double* const* beta0,
+             const double* const* beta0_edge, mac_stats* st) {
+    AmrState* A = c->amr;
+    const int nl = A->nlev;
+    const int dm = c->dm;
+    int rc = ensure_fab_arrays(c, macrhs != nullptr, false);
+    if (rc) return rc;
+    std::vector<double*> up(3 * nl, nullptr), pp(nl), rp(nl), mp(nl, nullptr);
+    auto launched = [&]() -> int {
+        ++c->issued;
+        if (cudaPeekAtLastError() != cudaSuccess) {
+            set_last_cuda_error(cudaGetLastError(), "amr copy launch", __FILE__, __LINE__);
+            return MAC_ERR_CUDA;
+        }
+        return MAC_OK;
+    };
+    for (int l = 0; l < nl && !rc; ++l) {
+        AmrState::FabArrays& F = A->F[l];
+        const Lev L = A->L[l].lev;
+        const long N = A->L[l].ncell;
+        for (int d = 0; d < dm && !rc; ++d) {
+            const long nf = amr::nfaces(L, d);
+            k_full_to_box_faces<<<blocks_for(nf, c->sms), kThreads, 0, c->stream>>>(L, d, umac[3 * l + d], F.u[d], nf);
+            rc = launched();
+            up[3 * l + d] = F.u[d];
+        }
+        k_full_to_box_cells<<<blocks_for(N, c->sms), kThreads, 0, c->stream>>>(L, rho[l], F.rho, N);
+        if (!rc) rc = launched();
+        k_full_to_box_cells<<<blocks_for(N, c->sms), kThreads, 0, c->stream>>>(L, phi[l], F.phi, N);
+        if (!rc) rc = launched();
+        if (macrhs && macrhs[l]) {
+            k_full_to_box_cells<<<blocks_for(N, c->sms), kThreads, 0, c->stream>>>(L, macrhs[l], F.rhs, N);
+            if (!rc) rc = launched();
+            mp[l] = F.rhs;
+        }
+        pp[l] = F.phi;
+        rp[l] = F.rho;
+    }
+    if (rc) return rc;
+    const int solve_rc = ml_core(c, up.data(), pp.data(), rp.data(), macrhs ? mp.data() : nullptr,
+                                 beta0, beta0_edge, st);
+    if (solve_rc != MAC_OK && solve_rc != MAC_ERR_NOT_CONVERGED) return solve_rc;
+    for (int l = 0; l < nl && !rc; ++l) {
+        AmrState::FabArrays& F = A->F[l];
+        const Lev L = A->L[l].lev;
+        const long N = A->L[l].ncell;
+        for (int d = 0; d < dm && !rc; ++d) {
+            const long nf = amr::nfaces(L, d);
+            k_box_to_full_faces<<<blocks_for(nf, c->sms), kThreads, 0, c->stream>>>(A->geo, L, d, F.u[d], umac[3 * l + d], nf);
+            rc = launched();
+        }
+        k_box_to_full_cells<<<blocks_for(N, c->sms), kThreads, 0, c->stream>>>(L, F.phi, phi[l], N);
+        if (!rc) rc = launched();
+    }
+    if (!rc) MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return rc ? rc : solve_rc;
+}
 }  // namespace mac
 
 using namespace mac;
@@ -1074,7 +1171,7 @@ int mac_macproject_ml_dense(mac_ctx* c, double* const* umac, double* const* phi,
     }
     const auto t0 = std::chrono::steady_clock::now();
     begin_call_stats(c, st);
-    const int rc = ml_core(c, umac, phi, rho, macrhs, beta0, beta0_edge, st);
+    const int rc = ml_dense(c, umac, phi, rho, macrhs, beta0, beta0_edge, st);
     st->status = rc;
     st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     end_call_stats(c, st);

@@ -53,27 +53,65 @@ struct Geo {
 template <typename T>
 struct LevT {
     int n[3];                  // level-domain cells (1 along inactive directions)
+    int lo[3], ext[3];         // the array box: cells lo .. lo + ext - 1 of the level domain
     double h[3];
-    const unsigned char* mask; // kIn / kCov per cell
-    const T* b[3];             // face coefficients, natural face layout (n[d] + 1 along d)
+    const unsigned char* mask; // kIn / kCov per cell of the box
+    const T* b[3];             // face coefficients over the box (ext[d] + 1 faces along d)
 };
 using Lev = LevT<double>;
 
+// Array box of a level: the bounding box [rlo, rhi] of its cells grown by one cell and clipped
+// to the domain; a periodic direction whose grown box would cross the domain face takes the
+// whole extent (neighbours across the face are then in the box).  Level 0: the domain.
+inline void level_box(int dm, const int n[3], const int per[3], const int rlo[3],
+                      const int rhi[3], int lo[3], int ext[3]) {
+    for (int d = 0; d < 3; ++d) {
+        if (d >= dm) {
+            lo[d] = 0;
+            ext[d] = 1;
+            continue;
+        }
+        int a = rlo[d] - 1, b = rhi[d] + 1;
+        if (per[d] && (a < 0 || b > n[d] - 1)) {
+            a = 0;
+            b = n[d] - 1;
+        }
+        a = a < 0 ? 0 : a;
+        b = b > n[d] - 1 ? n[d] - 1 : b;
+        lo[d] = a;
+        ext[d] = b - a + 1;
+    }
+}
+
+// Index of cell / face (i, j, k) of the level domain in the box arrays (the caller keeps it in
+// the box).
 template <typename T>
 AMR_HD inline long cix(const LevT<T>& L, int i, int j, int k) {
-    return (long)i + (long)L.n[0] * ((long)j + (long)L.n[1] * k);
+    return (long)(i - L.lo[0]) + (long)L.ext[0] * ((long)(j - L.lo[1]) + (long)L.ext[1] * (k - L.lo[2]));
 }
 template <typename T>
 AMR_HD inline long fix(const LevT<T>& L, int d, int i, int j, int k) {
-    const long m0 = L.n[0] + (d == 0), m1 = L.n[1] + (d == 1);
-    return (long)i + m0 * ((long)j + m1 * k);
+    const long m0 = L.ext[0] + (d == 0), m1 = L.ext[1] + (d == 1);
+    return (long)(i - L.lo[0]) + m0 * ((long)(j - L.lo[1]) + m1 * (k - L.lo[2]));
 }
 template <typename T>
 AMR_HD inline long nfaces(const LevT<T>& L, int d) {
-    return (long)(L.n[0] + (d == 0)) * (L.n[1] + (d == 1)) * (L.n[2] + (d == 2));
+    return (long)(L.ext[0] + (d == 0)) * (L.ext[1] + (d == 1)) * (L.ext[2] + (d == 2));
 }
 template <typename T>
-AMR_HD inline long ncells(const LevT<T>& L) { return (long)L.n[0] * L.n[1] * L.n[2]; }
+AMR_HD inline long ncells(const LevT<T>& L) { return (long)L.ext[0] * L.ext[1] * L.ext[2]; }
+template <typename T>
+AMR_HD inline bool inside(const LevT<T>& L, const int c[3]) {
+    for (int d = 0; d < 3; ++d)
+        if (c[d] < L.lo[d] || c[d] >= L.lo[d] + L.ext[d]) return false;
+    return true;
+}
+template <typename T>
+AMR_HD inline bool inside_face(const LevT<T>& L, int dir, const int f[3]) {
+    for (int d = 0; d < 3; ++d)
+        if (f[d] < L.lo[d] || f[d] >= L.lo[d] + L.ext[d] + (d == dir)) return false;
+    return true;
+}
 
 // Index q along d wrapped into the level domain; -1 beyond a non-periodic domain face.
 template <typename T>
@@ -140,8 +178,9 @@ AMR_HD inline void cell_op(const Geo& G, const LevT<T>& L, const LevT<T>& C, con
             }
             int q[3] = {c[0], c[1], c[2]};
             q[d] = qd;
-            const long qc = cix(L, q[0], q[1], q[2]);
-            if (in_region(L, qc)) {
+            const bool qin = inside(L, q);
+            const long qc = qin ? cix(L, q[0], q[1], q[2]) : 0;
+            if (qin && in_region(L, qc)) {
                 diag += w;
                 off += w * u[qc];
             } else {
@@ -154,10 +193,10 @@ AMR_HD inline void cell_op(const Geo& G, const LevT<T>& L, const LevT<T>& C, con
 
 template <typename T>
 AMR_HD inline void cell_coords(const LevT<T>& L, long idx, int c[3]) {
-    c[0] = (int)(idx % L.n[0]);
-    const long r = idx / L.n[0];
-    c[1] = (int)(r % L.n[1]);
-    c[2] = (int)(r / L.n[1]);
+    c[0] = L.lo[0] + (int)(idx % L.ext[0]);
+    const long r = idx / L.ext[0];
+    c[1] = L.lo[1] + (int)(r % L.ext[1]);
+    c[2] = L.lo[2] + (int)(r / L.ext[1]);
 }
 
 // r = f - L u on a region cell, 0 elsewhere.
@@ -294,17 +333,17 @@ AMR_HD inline bool face_in_level(const Geo& G, const LevT<T>& L, int d, const in
     int lo[3] = {f[0], f[1], f[2]}, hi[3] = {f[0], f[1], f[2]};
     lo[d] = wrap(G, L, d, f[d] - 1);
     hi[d] = wrap(G, L, d, f[d]);
-    return (lo[d] >= 0 && in_region(L, cix(L, lo[0], lo[1], lo[2]))) ||
-           (hi[d] >= 0 && in_region(L, cix(L, hi[0], hi[1], hi[2])));
+    return (lo[d] >= 0 && inside(L, lo) && in_region(L, cix(L, lo[0], lo[1], lo[2]))) ||
+           (hi[d] >= 0 && inside(L, hi) && in_region(L, cix(L, hi[0], hi[1], hi[2])));
 }
 
 template <typename T>
 AMR_HD inline void face_coords(const LevT<T>& L, int d, long idx, int f[3]) {
-    const int m0 = L.n[0] + (d == 0), m1 = L.n[1] + (d == 1);
-    f[0] = (int)(idx % m0);
+    const int m0 = L.ext[0] + (d == 0), m1 = L.ext[1] + (d == 1);
+    f[0] = L.lo[0] + (int)(idx % m0);
     const long r = idx / m0;
-    f[1] = (int)(r % m1);
-    f[2] = (int)(r / m1);
+    f[1] = L.lo[1] + (int)(r % m1);
+    f[2] = L.lo[2] + (int)(r / m1);
 }
 
 // ml_edge_restriction of one coarse face (direction d): the mean of the fine faces tiling it,
@@ -390,8 +429,8 @@ AMR_HD inline void correct_face(const Geo& G, const Lev& L, const Lev& C, int d,
     int lo[3] = {f[0], f[1], f[2]}, hi[3] = {f[0], f[1], f[2]};
     lo[d] = wrap(G, L, d, f[d] - 1);
     hi[d] = wrap(G, L, d, f[d]);
-    const bool lin = lo[d] >= 0 && in_region(L, cix(L, lo[0], lo[1], lo[2]));
-    const bool hin = hi[d] >= 0 && in_region(L, cix(L, hi[0], hi[1], hi[2]));
+    const bool lin = lo[d] >= 0 && inside(L, lo) && in_region(L, cix(L, lo[0], lo[1], lo[2]));
+    const bool hin = hi[d] >= 0 && inside(L, hi) && in_region(L, cix(L, hi[0], hi[1], hi[2]));
     const double h = L.h[d];
     double g;
     if (lin && hin) {
@@ -417,6 +456,21 @@ AMR_HD inline void to_single_cell(long idx, const double* x, float* y) { y[idx] 
 template <typename T>
 AMR_HD inline void accumulate_cell(const LevT<T>& L, long idx, double* phi, const float* e) {
     if (in_region(L, idx)) phi[idx] += (double)e[idx];
+}
+
+// ---- whole-level-domain arrays <-> box arrays ---------------------------------------------------
+template <typename T>
+AMR_HD inline long full_cell(const LevT<T>& L, long idx) {
+    int c[3];
+    cell_coords(L, idx, c);
+    return (long)c[0] + (long)L.n[0] * ((long)c[1] + (long)L.n[1] * c[2]);
+}
+template <typename T>
+AMR_HD inline long full_face(const LevT<T>& L, int d, long idx) {
+    int f[3];
+    face_coords(L, d, idx, f);
+    const long m0 = L.n[0] + (d == 0), m1 = L.n[1] + (d == 1);
+    return (long)f[0] + m0 * ((long)f[1] + m1 * f[2]);
 }
 
 // ---- caller fabs <-> level arrays -------------------------------------------------------------
@@ -451,6 +505,7 @@ AMR_HD inline int fab_elem(const Geo& G, const Lev& L, int dir, const FabDesc& B
         if (g[d] < B.lo[d] || g[d] > top) interior = false;
     }
     if (interior) {
+        if (dir < 0 ? !inside(L, g) : !inside_face(L, dir, g)) return 0;
         *tgt = dir < 0 ? cix(L, g[0], g[1], g[2]) : fix(L, dir, g[0], g[1], g[2]);
         return 1;
     }
@@ -460,6 +515,7 @@ AMR_HD inline int fab_elem(const Geo& G, const Lev& L, int dir, const FabDesc& B
         if (q < 0) return 0;
         g[d] = q;
     }
+    if (!inside(L, g)) return 0;
     *tgt = cix(L, g[0], g[1], g[2]);
     return 2;
 }

@@ -211,6 +211,8 @@ void build_levels(HostMl<T>& M, const HostExec& E0) {
         amr::LevT<T>& V = M.L[l];
         for (int d = 0; d < 3; ++d) {
             V.n[d] = geom[l].n[d];
+            V.lo[d] = geom[l].lo[d];
+            V.ext[d] = geom[l].ext[d];
             V.h[d] = geom[l].h[d];
         }
         V.mask = E.mask[l].data();
@@ -237,15 +239,29 @@ void build(HostExec& E, const orc_opts* o, int nlev, const int* nboxes, const in
     }
     E.L.assign(nlev, amr::Lev{});
     E.mask.assign(nlev, {});
+    const int per[3] = {E.geo.per[0], E.geo.per[1], E.geo.per[2]};
+    const int* bx = boxes;
     for (int l = 0; l < nlev; ++l) {
         amr::Lev& V = E.L[l];
         for (int d = 0; d < 3; ++d) {
             V.n[d] = d < o->dm ? (o->n[d] << l) : 1;
             V.h[d] = d < o->dm ? o->dx[d] / (double)(1 << l) : o->dx[d];
+            V.lo[d] = 0;
+            V.ext[d] = V.n[d];
+        }
+        if (l > 0) {   // the bounding box of the level's boxes, grown by one cell
+            int rlo[3] = {1 << 30, 1 << 30, 1 << 30}, rhi[3] = {-1, -1, -1};
+            for (int b = 0; b < nboxes[l]; ++b)
+                for (int d = 0; d < 3; ++d) {
+                    rlo[d] = std::min(rlo[d], bx[6 * b + d]);
+                    rhi[d] = std::max(rhi[d], bx[6 * b + 3 + d]);
+                }
+            amr::level_box(o->dm, V.n, per, rlo, rhi, V.lo, V.ext);
+            bx += 6 * nboxes[l];
         }
         E.mask[l].assign((size_t)amr::ncells(V), l == 0 ? amr::kIn : 0);
     }
-    const int* bx = boxes;
+    bx = boxes;
     for (int l = 1; l < nlev; ++l)
         for (int b = 0; b < nboxes[l]; ++b, bx += 6)
             for (int k = bx[2]; k <= bx[5]; ++k)
@@ -294,18 +310,53 @@ int amrh_macproject_prec(const orc_opts* o, int nlev, const int* nboxes, const i
     HostMl<float> E32;
     build_levels<float>(E32, E);
     E.v32 = &E32;
-    E.u = umac;
-    E.rho = rho;
-    E.macrhs = macrhs;
+    // the caller's whole-level-domain arrays -> the levels' box arrays
+    const int dm = o->dm;
+    std::vector<std::vector<double>> ub(3 * nlev), rb(nlev), mb(nlev);
+    std::vector<double*> up(3 * nlev, nullptr);
+    std::vector<const double*> rp(nlev), mp(nlev, nullptr);
+    for (int l = 0; l < nlev; ++l) {
+        const amr::Lev& V = E.L[l];
+        for (int d = 0; d < dm; ++d) {
+            ub[3 * l + d].resize((size_t)amr::nfaces(V, d));
+            for (long i = 0; i < amr::nfaces(V, d); ++i)
+                ub[3 * l + d][i] = umac[3 * l + d][amr::full_face(V, d, i)];
+            up[3 * l + d] = ub[3 * l + d].data();
+        }
+        rb[l].resize((size_t)amr::ncells(V));
+        for (long i = 0; i < amr::ncells(V); ++i) {
+            rb[l][i] = rho[l][amr::full_cell(V, i)];
+            E.buf(l, amr::kPhi)[i] = phi[l][amr::full_cell(V, i)];
+        }
+        rp[l] = rb[l].data();
+        if (macrhs && macrhs[l]) {
+            mb[l].resize((size_t)amr::ncells(V));
+            for (long i = 0; i < amr::ncells(V); ++i) mb[l][i] = macrhs[l][amr::full_cell(V, i)];
+            mp[l] = mb[l].data();
+        }
+    }
+    E.u = up.data();
+    E.rho = rp.data();
+    E.macrhs = macrhs ? mp.data() : nullptr;
     E.b0 = beta0;
     E.b0e = beta0_edge;
     E.alt = o->alt_energy_fix;
-    for (int l = 0; l < nlev; ++l) {
-        E.bufp[amr::kPhi][l] = phi[l];
-    }
     amr::SolveStats S{};
     const int rc = amr::amr_project(E, o->rel_eps, o->abs_eps, o->max_vcycles, o->nu1, o->nu2,
                                     &S, inner > 0 ? &E32 : nullptr, inner);
+    // back: the levels' own faces and region cells
+    for (int l = 0; l < nlev; ++l) {
+        const amr::Lev& V = E.L[l];
+        for (int d = 0; d < dm; ++d)
+            for (long i = 0; i < amr::nfaces(V, d); ++i) {
+                int f[3];
+                amr::face_coords(V, d, i, f);
+                if (amr::face_in_level(E.geo, V, d, f))
+                    umac[3 * l + d][amr::full_face(V, d, i)] = ub[3 * l + d][i];
+            }
+        for (long i = 0; i < amr::ncells(V); ++i)
+            if (amr::in_region(V, i)) phi[l][amr::full_cell(V, i)] = E.buf(l, amr::kPhi)[i];
+    }
     if (stats_out) {
         stats_out[0] = rc;
         stats_out[1] = S.cycles;
@@ -324,6 +375,13 @@ void amrh_fabs(const orc_opts* o, int nlev, const int* nboxes, const int* boxes,
                int ng, int with_ghosts, int scatter, double* const* fabs, double* level) {
     HostExec E;
     build(E, o, nlev, nboxes, boxes);
+    const amr::Lev& V = E.L[l];
+    // the whole-level-domain array of the caller <-> the level's box array
+    const long nbox = dir < 0 ? amr::ncells(V) : amr::nfaces(V, dir);
+    std::vector<double> box((size_t)nbox, 0.0);
+    auto full = [&](long i) { return dir < 0 ? amr::full_cell(V, i) : amr::full_face(V, dir, i); };
+    if (scatter)
+        for (long i = 0; i < nbox; ++i) box[i] = level[full(i)];
     const int* bx = boxes;
     for (int q = 1; q < l; ++q) bx += 6 * nboxes[q];
     for (int b = 0; b < nboxes[l]; ++b, bx += 6) {
@@ -341,11 +399,13 @@ void amrh_fabs(const orc_opts* o, int nlev, const int* nboxes, const int* boxes,
         D.dst = fabs[b];
         for (long e = 0; e < cnt; ++e) {
             if (scatter)
-                amr::fab_scatter_elem(E.geo, E.L[l], dir, D, e, level);
+                amr::fab_scatter_elem(E.geo, V, dir, D, e, box.data());
             else
-                amr::fab_gather_elem(E.geo, E.L[l], dir, D, e, with_ghosts, level);
+                amr::fab_gather_elem(E.geo, V, dir, D, e, with_ghosts, box.data());
         }
     }
+    if (!scatter)
+        for (long i = 0; i < nbox; ++i) level[full(i)] = box[i];
 }
 
 }  // extern "C"

@@ -123,7 +123,8 @@ def test_fab_gather_and_scatter_of_a_fine_level(host_lib, dir_):
                        O._ptr_array(fabs), level.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
     if dir_ < 0:
         # the boxes' cells and their ng ghost layers (corners included) that lie in the domain,
-        # periodic images wrapped
+        # periodic images wrapped -- as far as the level stores cells: the bounding box of its
+        # boxes grown by one cell (the whole extent of a periodic direction it would cross)
         want = np.zeros(H.shape[1], dtype=bool)
         for lo, hi in c["boxes"][1]:
             idx = []
@@ -132,6 +133,19 @@ def test_fab_gather_and_scatter_of_a_fine_level(host_lib, dir_):
                 r = r % H.shape[1][d] if per[d] else r[(r >= 0) & (r < H.shape[1][d])]
                 idx.append(r)
             want[np.ix_(*idx)] = True
+        stored = np.ones(H.shape[1], dtype=bool)
+        for d in range(2):
+            a = min(lo[d] for lo, _ in c["boxes"][1]) - 1
+            b = max(hi[d] for _, hi in c["boxes"][1]) + 1
+            n = H.shape[1][d]
+            if per[d] and (a < 0 or b > n - 1):
+                a, b = 0, n - 1
+            a, b = max(a, 0), min(b, n - 1)
+            sl = [slice(None)] * 2
+            keep = np.zeros(n, dtype=bool)
+            keep[a:b + 1] = True
+            stored &= keep.reshape([-1 if e == d else 1 for e in range(2)])
+        want &= stored
     else:
         want = G.face_member(H, 1, dir_)
     np.testing.assert_array_equal(level[want], arr[want])
