@@ -4,10 +4,10 @@
 //
 // Level 0 is the context's own one-level geometry; its multigrid (the FP64 V-cycle of
 // mac_solver.cu, with the context's coarsening, tail and bottom solve) is the coarse correction
-// of the multi-level cycle.  Finer levels are dense FP64 arrays over their whole level domain
-// with a byte mask (kIn: the level's boxes; kCov: under the next finer level): one thread per
-// cell or face, masked.  All launches go to the context's stream; the host reads one residual
-// norm per multi-level cycle.
+// of the multi-level cycle.  Finer levels are FP64 arrays over the bounding box of their boxes
+// grown by one cell (amr::level_box) with a byte mask (kIn: the level's boxes; kCov: under the
+// next finer level): one thread per cell or face of that box, masked.  All launches go to the
+// context's stream; the host reads one residual norm per multi-level cycle.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -404,6 +404,7 @@ int build_masks(const mac_ctx* c, int nlev, const int* nboxes, const int* box_lo
             amr::cell_coords(F, idx, fc);
             const int cc[3] = {dm > 0 ? fc[0] >> 1 : fc[0], dm > 1 ? fc[1] >> 1 : fc[1],
                                dm > 2 ? fc[2] >> 1 : fc[2]};
+            if (!amr::inside(K, cc)) return MAC_ERR_INVALID;
             masks[l - 1][(size_t)amr::cix(K, cc[0], cc[1], cc[2])] |= amr::kCov;
             for (int a2 = -(dm > 2); a2 <= (dm > 2); ++a2)
                 for (int a1 = -(dm > 1); a1 <= (dm > 1); ++a1)

@@ -3,9 +3,10 @@
 //
 // MAESTRO's macproject with nlevs > 1 (Source/macproject.f90:51-328) hands FBoxLib's composite
 // solve ml_cc_solve a hierarchy of levels with refinement ratio 2 (Source/mac_multigrid.f90:56).
-// Level l is stored as dense arrays over its whole level domain (n0 << l cells per active
-// direction, natural layout i + n0 (j + n1 k)) with a byte mask: kIn for the cells of the level's
-// boxes, kCov for the cells under the next finer level.  Valid cells (kIn without kCov) carry the
+// Level l (n0 << l cells per active direction) is stored as arrays over its array box -- the
+// bounding box of its boxes grown by one cell (level_box; level 0: the whole domain) -- in
+// natural layout (i - lo0) + ext0 ((j - lo1) + ext1 (k - lo2)), with a byte mask: kIn for the
+// cells of the level's boxes, kCov for the cells under the next finer level.  Valid cells (kIn without kCov) carry the
 // composite unknowns; covered cells hold the mean of their children.
 //
 // Composite operator (the form FBoxLib describes in Docs/mg/mg.tex:124-155, stencil_order = 2):
