@@ -227,6 +227,10 @@ __global__ void k_box_to_full_cells(Lev L, const double* box, double* full, long
     AMR_LOOP(N) if (amr::in_region(L, idx)) full[amr::full_cell(L, idx)] = box[idx];
 }
 
+__global__ void k_sync_periodic_faces(Geo G, Lev L, int d, double* u, long N) {
+    AMR_LOOP(N) amr::sync_periodic_face(G, L, d, idx, u);
+}
+
 __global__ void k_to_single(const double* x, float* y, long N) {
     AMR_LOOP(N) amr::to_single_cell(idx, x, y);
 }
@@ -1028,6 +1032,17 @@ int ml_fabs(mac_ctx* c, int ptr_kind, double* const* umac, int ng_u, double* con
         boff += nb;
     }
     if (rc) return rc;
+    // the periodic image copy of a fine level's domain-face velocities (only one copy is owned)
+    for (int l = 1; l < nl; ++l) {
+        const Lev& L = A->L[l].lev;
+        for (int d = 0; d < dm; ++d) {
+            if (!A->geo.per[d] || L.lo[d] != 0 || L.ext[d] != L.n[d]) continue;
+            const long nt = A->L[l].ncell / L.ext[d];
+            k_sync_periodic_faces<<<blocks_for(nt, c->sms), kThreads, 0, c->stream>>>(A->geo, L, d, A->F[l].u[d], nt);
+            MAC_CUDA_TRY(cudaGetLastError());
+            ++c->issued;
+        }
+    }
     const int solve_rc = ml_core(c, up.data(), pp.data(), rp.data(), macrhs ? mp.data() : nullptr,
                                  beta0 ? b0p.data() : nullptr, beta0 ? b0ep.data() : nullptr, st);
     if (solve_rc != MAC_OK && solve_rc != MAC_ERR_NOT_CONVERGED) return solve_rc;

@@ -369,6 +369,30 @@ AMR_HD inline void edge_restrict_face(const Geo& G, const Lev& F, const Lev& C, 
     uc[idx] = s / cnt;
 }
 
+// Periodic image faces of a fine level's face array gathered from fabs: along a periodic
+// direction d spanned by the array box, faces 0 and n are one face stored twice.  A box owns
+// face 0 when its cell 0 is in the region, face n when its cell n - 1 is; the caller's fabs set
+// only the owned copy, so the other copy is set from it (t: the face's position across d).
+AMR_HD inline void sync_periodic_face(const Geo& G, const Lev& L, int d, long t, double* u) {
+    if (d >= G.dm || !G.per[d] || L.lo[d] != 0 || L.ext[d] != L.n[d]) return;
+    int c[3], e0 = -1, e1 = -1;
+    for (int e = 0; e < 3; ++e)
+        if (e != d) (e0 < 0 ? e0 : e1) = e;
+    c[e0] = L.lo[e0] + (int)(t % L.ext[e0]);
+    c[e1] = L.lo[e1] + (int)(t / L.ext[e0]);
+    c[d] = 0;
+    const bool own0 = in_region(L, cix(L, c[0], c[1], c[2]));
+    c[d] = L.n[d] - 1;
+    const bool own1 = in_region(L, cix(L, c[0], c[1], c[2]));
+    int f[3] = {c[0], c[1], c[2]};
+    f[d] = 0;
+    const long i0 = fix(L, d, f[0], f[1], f[2]);
+    f[d] = L.n[d];
+    const long i1 = fix(L, d, f[0], f[1], f[2]);
+    if (own0 && !own1) u[i1] = u[i0];
+    if (own1 && !own0) u[i0] = u[i1];
+}
+
 // Planar beta0 of the face (d, f): beta0_edge along the vertical, beta0 otherwise.
 AMR_HD inline double beta0_of_face(const Geo& G, int d, const int f[3], const double* b0,
                                    const double* b0e) {

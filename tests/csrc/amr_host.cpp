@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <vector>
 
 #include "mac_amr.cuh"
@@ -217,11 +218,14 @@ void build_levels(HostMl<T>& M, const HostExec& E0) {
         }
         V.mask = E.mask[l].data();
         const long N = amr::ncells(V);
+        // work arrays and coefficients start as NaN: the device arrays they stand for are not
+        // initialised, so any read before a write shows up in the results
+        const T nan = std::numeric_limits<T>::quiet_NaN();
         for (int b = 0; b < amr::kNumBufs; ++b) {
-            M.store[b][l].assign((size_t)N, (T)0);
+            M.store[b][l].assign((size_t)N, nan);
             M.bufp[b][l] = M.store[b][l].data();
         }
-        for (int d = 0; d < E.geo.dm; ++d) M.beta[d][l].assign((size_t)amr::nfaces(V, d), (T)0);
+        for (int d = 0; d < E.geo.dm; ++d) M.beta[d][l].assign((size_t)amr::nfaces(V, d), nan);
         for (int d = 0; d < 3; ++d) V.b[d] = d < E.geo.dm ? M.beta[d][l].data() : nullptr;
     }
 }
@@ -290,21 +294,26 @@ extern "C" {
 int amrh_macproject_prec(const orc_opts* o, int nlev, const int* nboxes, const int* boxes,
                          double* const* umac, double* const* phi, const double* const* rho,
                          const double* const* macrhs, const double* const* beta0,
-                         const double* const* beta0_edge, int inner, double* stats_out);
+                         const double* const* beta0_edge, int inner, int fab_inputs,
+                         double* stats_out);
 
 int amrh_macproject(const orc_opts* o, int nlev, const int* nboxes, const int* boxes,
                     double* const* umac, double* const* phi, const double* const* rho,
                     const double* const* macrhs, const double* const* beta0,
                     const double* const* beta0_edge, double* stats_out) {
     return amrh_macproject_prec(o, nlev, nboxes, boxes, umac, phi, rho, macrhs, beta0,
-                                beta0_edge, 0, stats_out);
+                                beta0_edge, 0, 0, stats_out);
 }
 
 // inner > 0: the mixed-precision solve, `inner` FP32 multi-level V-cycles per FP64 step.
+// fab_inputs: the fine levels' input arrays hold only what the per-box entry gathers from fabs
+// (each box's own faces and cells, density ghosts one cell deep); everything else is NaN, as
+// the uninitialised device arrays of that entry.
 int amrh_macproject_prec(const orc_opts* o, int nlev, const int* nboxes, const int* boxes,
                          double* const* umac, double* const* phi, const double* const* rho,
                          const double* const* macrhs, const double* const* beta0,
-                         const double* const* beta0_edge, int inner, double* stats_out) {
+                         const double* const* beta0_edge, int inner, int fab_inputs,
+                         double* stats_out) {
     HostExec E;
     build(E, o, nlev, nboxes, boxes);
     HostMl<float> E32;
@@ -333,6 +342,50 @@ int amrh_macproject_prec(const orc_opts* o, int nlev, const int* nboxes, const i
             mb[l].resize((size_t)amr::ncells(V));
             for (long i = 0; i < amr::ncells(V); ++i) mb[l][i] = macrhs[l][amr::full_cell(V, i)];
             mp[l] = mb[l].data();
+        }
+    }
+    if (fab_inputs) {
+        const double nan = std::numeric_limits<double>::quiet_NaN();
+        const int* bx = boxes;
+        for (int l = 1; l < nlev; ++l) {
+            const amr::Lev& V = E.L[l];
+            std::vector<char> face_set[3], cell_set((size_t)amr::ncells(V), 0),
+                rho_set((size_t)amr::ncells(V), 0);
+            for (int d = 0; d < dm; ++d) face_set[d].assign((size_t)amr::nfaces(V, d), 0);
+            for (int b = 0; b < nboxes[l]; ++b, bx += 6) {
+                for (int dir = -1; dir < dm; ++dir) {
+                    amr::FabDesc D{};
+                    long cnt = 1;
+                    for (int d = 0; d < 3; ++d) {
+                        D.lo[d] = bx[d];
+                        D.hi[d] = bx[3 + d];
+                        D.ext[d] = d < dm ? D.hi[d] - D.lo[d] + 1 + (dir == d) + 2 : 1;
+                        cnt *= D.ext[d];
+                    }
+                    D.ng = 1;
+                    D.count = cnt;
+                    for (long e = 0; e < cnt; ++e) {
+                        long t;
+                        const int kind = amr::fab_elem(E.geo, V, dir, D, e, &t);
+                        if (dir >= 0 && kind == 1) face_set[dir][t] = 1;
+                        if (dir < 0 && kind == 1) cell_set[t] = 1;
+                        if (dir < 0 && kind >= 1) rho_set[t] = 1;
+                    }
+                }
+            }
+            for (int d = 0; d < dm; ++d) {
+                for (long i = 0; i < amr::nfaces(V, d); ++i)
+                    if (!face_set[d][i]) ub[3 * l + d][i] = nan;
+                const long nt = amr::ncells(V) / V.ext[d];
+                for (long t = 0; t < nt; ++t) amr::sync_periodic_face(E.geo, V, d, t, ub[3 * l + d].data());
+            }
+            for (long i = 0; i < amr::ncells(V); ++i) {
+                if (!rho_set[i]) rb[l][i] = nan;
+                if (!cell_set[i]) {
+                    E.buf(l, amr::kPhi)[i] = nan;
+                    if (mp[l]) mb[l][i] = nan;
+                }
+            }
         }
     }
     E.u = up.data();

@@ -6,6 +6,7 @@
 // a GPU.  Built by tests/test_hg_host_exec.py with g++ (no CUDA involved).
 #include <algorithm>
 #include <cmath>
+#include <limits>
 #include <vector>
 
 #include "hg_nodal.cuh"
@@ -31,14 +32,17 @@ struct HostMg {
         L.assign(nlev, hg::LevT<T>{});
         sig.assign(nlev, {});
         for (int b = 0; b < hg::kNumBufs; ++b) store[b].assign(nlev, {});
+        // work arrays start as NaN: the device arrays they stand for are not initialised, so
+        // any read before a write shows up in the results
+        const T nan = std::numeric_limits<T>::quiet_NaN();
         for (int l = 0; l < nlev; ++l) {
             for (int d = 0; d < 3; ++d) {
                 L[l].n[d] = shape[l].n[d];
                 L[l].nn[d] = shape[l].nn[d];
                 L[l].h[d] = shape[l].h[d];
             }
-            sig[l].assign((size_t)hg::ncells(L[l]), (T)0);
-            for (int b = 0; b < hg::kNumBufs; ++b) store[b][l].assign((size_t)hg::nnodes(L[l]), (T)0);
+            sig[l].assign((size_t)hg::ncells(L[l]), nan);
+            for (int b = 0; b < hg::kNumBufs; ++b) store[b][l].assign((size_t)hg::nnodes(L[l]), nan);
             L[l].sig = sig[l].data();
             hg::set_dense_weights(geo.dm, L[l]);
         }

@@ -38,7 +38,7 @@ def host_lib(tmp_path_factory):
                                   P(ctypes.c_double)]
     L.amrh_macproject.restype = ctypes.c_int
     L.amrh_macproject_prec.argtypes = [P(O.OrcOpts), ctypes.c_int, ip, ip, pd, pd, pd, pd, pd, pd,
-                                       ctypes.c_int, P(ctypes.c_double)]
+                                       ctypes.c_int, ctypes.c_int, P(ctypes.c_double)]
     L.amrh_macproject_prec.restype = ctypes.c_int
     L.amrh_fabs.argtypes = [P(O.OrcOpts), ctypes.c_int, ip, ip, ctypes.c_int, ctypes.c_int,
                             ctypes.c_int, ctypes.c_int, ctypes.c_int, pd, P(ctypes.c_double)]
@@ -46,7 +46,7 @@ def host_lib(tmp_path_factory):
     return L
 
 
-def run_host(L, c, rel_eps, inner=0):
+def run_host(L, c, rel_eps, inner=0, fab_inputs=False):
     nlev = c["nlev"]
     dm = c["dm"]
     phi = [np.zeros_like(p, order="F") for p in c["phi"]]
@@ -67,7 +67,8 @@ def run_host(L, c, rel_eps, inner=0):
                                 nb.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
                                 bx.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), O._ptr_array(up),
                                 O._ptr_array(phi), O._ptr_array(rho), O._ptr_array(mr),
-                                O._ptr_array(b0), O._ptr_array(b0e), int(inner), st)
+                                O._ptr_array(b0), O._ptr_array(b0e), int(inner), int(fab_inputs),
+                                st)
     return rc, u, phi, list(st)
 
 
@@ -78,6 +79,19 @@ def test_library_amr_code_on_host_matches_golden(host_lib, name, inner):
     c = load_amr(name)
     H = G.Hierarchy(c["n0"], c["dx0"], c["bc_lo"], c["bc_hi"], c["boxes"])
     rc, u, phi, st = run_host(host_lib, c, 1e-12, inner=inner)
+    assert rc == 0 and st[2] <= 1e-12, st
+    assert phi_err(H, phi, c["phi"]) <= 1e-9
+    assert u_err(H, u, c["unew"]) <= 1e-9
+
+
+@pytest.mark.parametrize("inner", [0, 2])
+@pytest.mark.parametrize("name", sorted(AMR_CASES))
+def test_library_amr_code_reads_only_what_the_fab_entry_defines(host_lib, name, inner):
+    # the per-box entry defines a fine level's faces and cells only inside its boxes (density:
+    # one ghost cell deeper); the rest of its arrays, and every work array, is NaN here
+    c = load_amr(name)
+    H = G.Hierarchy(c["n0"], c["dx0"], c["bc_lo"], c["bc_hi"], c["boxes"])
+    rc, u, phi, st = run_host(host_lib, c, 1e-12, inner=inner, fab_inputs=True)
     assert rc == 0 and st[2] <= 1e-12, st
     assert phi_err(H, phi, c["phi"]) <= 1e-9
     assert u_err(H, u, c["unew"]) <= 1e-9
