@@ -680,7 +680,10 @@ int hg_fabs(mac_ctx* c, int ptr_kind, int proj_type, double dt, int dense_stenci
             size_t cap2 = H->tab_cap;
             rc = hg_grow(&H->d_tab, &cap2, ntab, false);
         }
-        if (rc) return rc;
+        if (rc) {
+            H->tab_cap = 0;   // one of the two tables may be gone: regrow both next call
+            return rc;
+        }
         H->tab_cap = ntab;
     }
     if (host) {
