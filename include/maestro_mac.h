@@ -288,7 +288,9 @@ int mac_macproject_ml_dense(mac_ctx* ctx, double* const* umac, double* const* ph
  *   beta0 / beta0_edge : the levels' planar base states one after the other (n_l and n_l + 1
  *            values, n_l = the level's vertical extent), or both NULL
  * Ghost faces and ghost cells of the fabs are left as they came in (the reference refills them
- * after the projection with create_umac_grown / multifab_fill_boundary).
+ * after the projection with create_umac_grown / multifab_fill_boundary).  Along a periodic
+ * direction a domain face is read from the box that owns it (a box at the low end owns face 0,
+ * one at the high end face n_l); where only one end has a box, that copy stands for both.
  */
 int mac_macproject_ml(mac_ctx* ctx, int ptr_kind,
                       double* const* umac, int ng_u,
