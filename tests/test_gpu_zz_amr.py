@@ -86,7 +86,7 @@ def test_amr_layout_and_density_errors():
     assert e.value.code == capi.MAC_ERR_BAD_DENSITY
 
 
-@pytest.mark.parametrize("name", ["amr2d_wrap", "amr3d_16"])
+@pytest.mark.parametrize("name", ["amr2d_wrap", "amr3d_16", "amr3d_3lev"])
 def test_amr_projection_on_host_fabs(name):
     # the drop-in form: per-box host fabs of every level (several boxes on level 0 too), rho with
     # two ghost cells, umac with one
