@@ -40,9 +40,13 @@ __global__ void k_defect(Geo G, amr::LevT<T> L, amr::LevT<T> C, const T* u, cons
     AMR_LOOP(N) amr::defect_cell(G, L, C, idx, u, cu, f, r);
 }
 
+// One colour of a sweep: one thread per cell of that colour (N = amr::colour_threads).
 template <typename T>
 __global__ void k_gsrb(Geo G, amr::LevT<T> L, int colour, T* u, const T* f, long N) {
-    AMR_LOOP(N) amr::gsrb_cell(G, L, idx, colour, u, f);
+    AMR_LOOP(N) {
+        const long c = amr::colour_cell(L, idx, colour);
+        if (c >= 0) amr::gsrb_cell(G, L, c, colour, u, f);
+    }
 }
 
 template <typename T>
@@ -469,7 +473,8 @@ struct GpuMl {
     void gsrb(int l, T* uu, const T* f, int nu) {
         for (int s = 0; s < nu; ++s)
             for (int colour = 0; colour < 2; ++colour) {
-                k_gsrb<T><<<blocks(ncell(l)), kThreads, 0, c->stream>>>(geo, lev(l), colour, uu, f, ncell(l));
+                const long nt = amr::colour_threads(lev(l));
+                k_gsrb<T><<<blocks(nt), kThreads, 0, c->stream>>>(geo, lev(l), colour, uu, f, nt);
                 launched();
             }
     }

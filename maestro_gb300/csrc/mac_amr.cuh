@@ -6,8 +6,8 @@
 // Level l (n0 << l cells per active direction) is stored as arrays over its array box -- the
 // bounding box of its boxes grown by one cell (level_box; level 0: the whole domain) -- in
 // natural layout (i - lo0) + ext0 ((j - lo1) + ext1 (k - lo2)), with a byte mask: kIn for the
-// cells of the level's boxes, kCov for the cells under the next finer level.  Valid cells (kIn without kCov) carry the
-// composite unknowns; covered cells hold the mean of their children.
+// cells of the level's boxes, kCov for the cells under the next finer level.  Valid cells (kIn
+// without kCov) carry the composite unknowns; covered cells hold the mean of their children.
 //
 // Composite operator (the form FBoxLib describes in Docs/mg/mg.tex:124-155, stencil_order = 2):
 //   * fine arms beta_f (u_c - u_nb) / h^2; across a coarse-fine face the neighbour is the ghost
@@ -216,6 +216,24 @@ AMR_HD inline void defect_cell(const Geo& G, const LevT<T>& L, const LevT<T>& C,
 }
 
 // Gauss-Seidel update of a region cell of the given colour, zero coarse data.
+// Cells of one colour, half a row each: thread t covers row t / hw (hw = ceil(ext0 / 2)) at
+// x = 2 (t % hw) + the row's first cell of that colour.  Returns the box index, or -1 past the
+// row's end (odd ext0).  t < colour_threads(L) keeps the row inside the box.
+template <typename T>
+AMR_HD inline long colour_threads(const LevT<T>& L) {
+    return (long)((L.ext[0] + 1) / 2) * L.ext[1] * L.ext[2];
+}
+template <typename T>
+AMR_HD inline long colour_cell(const LevT<T>& L, long t, int colour) {
+    const int hw = (L.ext[0] + 1) / 2;
+    const long row = t / hw;
+    const int j = (int)(row % L.ext[1]), k = (int)(row / L.ext[1]);
+    const int x0 = (colour + L.lo[0] + L.lo[1] + j + L.lo[2] + k) & 1;
+    const int x = 2 * (int)(t % hw) + x0;
+    if (x >= L.ext[0]) return -1;
+    return (long)x + (long)L.ext[0] * ((long)j + (long)L.ext[1] * k);
+}
+
 template <typename T>
 AMR_HD inline void gsrb_cell(const Geo& G, const LevT<T>& L, long idx, int colour, T* u,
                              const T* f) {

@@ -51,7 +51,10 @@ struct HostMl {
     void gsrb(int l, T* uu, const T* f, int nu) {
         for (int s = 0; s < nu; ++s)
             for (int colour = 0; colour < 2; ++colour)
-                for (long i = 0; i < ncell(l); ++i) amr::gsrb_cell(geo, L[l], i, colour, uu, f);
+                for (long t = 0; t < amr::colour_threads(L[l]); ++t) {
+                    const long i = amr::colour_cell(L[l], t, colour);
+                    if (i >= 0) amr::gsrb_cell(geo, L[l], i, colour, uu, f);
+                }
     }
     void reflux(int l, const T* uf, const T* uc, T* res) {
         for (long i = 0; i < ncell(l - 1); ++i) amr::reflux_cell(geo, L[l], L[l - 1], i, uf, uc, res);
@@ -459,6 +462,31 @@ void amrh_fabs(const orc_opts* o, int nlev, const int* nboxes, const int* boxes,
     }
     if (!scatter)
         for (long i = 0; i < nbox; ++i) level[full(i)] = box[i];
+}
+
+// The colour map of the smoother launches over a box lo[3], ext[3] (dm active directions):
+// returns 0 when every cell of each colour is hit exactly once and nothing else is.
+int amrh_check_colour_map(int dm, const int* lo, const int* ext) {
+    amr::Lev L{};
+    for (int d = 0; d < 3; ++d) {
+        L.lo[d] = d < dm ? lo[d] : 0;
+        L.ext[d] = d < dm ? ext[d] : 1;
+    }
+    for (int colour = 0; colour < 2; ++colour) {
+        std::vector<int> hits((size_t)amr::ncells(L), 0);
+        for (long t = 0; t < amr::colour_threads(L); ++t) {
+            const long i = amr::colour_cell(L, t, colour);
+            if (i < -1 || i >= amr::ncells(L)) return 1;
+            if (i >= 0) ++hits[(size_t)i];
+        }
+        for (long i = 0; i < amr::ncells(L); ++i) {
+            int c[3];
+            amr::cell_coords(L, i, c);
+            const int want = ((c[0] + c[1] + c[2]) & 1) == colour ? 1 : 0;
+            if (hits[(size_t)i] != want) return 2;
+        }
+    }
+    return 0;
 }
 
 }  // extern "C"

@@ -43,6 +43,8 @@ def host_lib(tmp_path_factory):
     L.amrh_fabs.argtypes = [P(O.OrcOpts), ctypes.c_int, ip, ip, ctypes.c_int, ctypes.c_int,
                             ctypes.c_int, ctypes.c_int, ctypes.c_int, pd, P(ctypes.c_double)]
     L.amrh_fabs.restype = None
+    L.amrh_check_colour_map.argtypes = [ctypes.c_int, ip, ip]
+    L.amrh_check_colour_map.restype = ctypes.c_int
     return L
 
 
@@ -184,3 +186,12 @@ def test_library_amr_code_reports_a_nonfinite_input(host_lib):
     c["umac"][1][0][30, 20] = np.nan
     rc, u, phi, st = run_host(host_lib, c, 1e-10)
     assert rc < 0
+
+
+@pytest.mark.parametrize("dm,lo,ext", [(2, (0, 0), (8, 8)), (2, (3, 5), (7, 9)), (2, (1, 0), (1, 5)),
+                                       (3, (0, 0, 0), (6, 6, 6)), (3, (5, 2, 7), (9, 4, 11)),
+                                       (3, (2, 3, 1), (1, 1, 3))])
+def test_smoother_colour_map_covers_each_colour_once(host_lib, dm, lo, ext):
+    # the compact GS-RB launch: one thread per cell of the colour, odd extents and offset boxes
+    ia = lambda v: (ctypes.c_int * 3)(*(list(v) + [0] * (3 - len(v))))  # noqa: E731
+    assert host_lib.amrh_check_colour_map(dm, ia(lo), ia(ext)) == 0
