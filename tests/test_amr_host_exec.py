@@ -19,13 +19,22 @@ from tests.test_oracle_amr import G, load_amr, phi_err, u_err
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
+def _opt_flags():
+    """-O2; with MAESTRO_HOST_ASAN=1 an AddressSanitizer build instead (run pytest with
+    LD_PRELOAD=$(gcc -print-file-name=libasan.so) ASAN_OPTIONS=detect_leaks=0): every array access
+    of the library's cell functions is then bounds-checked on the host."""
+    if os.environ.get("MAESTRO_HOST_ASAN") == "1":
+        return ["-O1", "-g", "-fsanitize=address", "-fno-omit-frame-pointer"]
+    return ["-O2"]
+
+
 @pytest.fixture(scope="module")
 def host_lib(tmp_path_factory):
     cxx = shutil.which("g++") or shutil.which("c++")
     if cxx is None:
         pytest.skip("no C++ compiler")
     out = str(tmp_path_factory.mktemp("amrh") / "libamr_host.so")
-    cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-fopenmp", "-shared",
+    cmd = [cxx, *_opt_flags(), "-std=c++17", "-fPIC", "-fopenmp", "-shared",
            "-I", os.path.join(ROOT, "maestro_gb300", "csrc"), "-I", os.path.join(ROOT, "oracle"),
            os.path.join(ROOT, "tests", "csrc", "amr_host.cpp"),
            os.path.join(ROOT, "oracle", "mac_oracle.cpp"), "-o", out]

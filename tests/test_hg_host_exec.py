@@ -19,13 +19,22 @@ from tests.test_oracle_hg import G, _unknown_mask, load_hg
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
+def _opt_flags():
+    """-O2; with MAESTRO_HOST_ASAN=1 an AddressSanitizer build instead (run pytest with
+    LD_PRELOAD=$(gcc -print-file-name=libasan.so) ASAN_OPTIONS=detect_leaks=0): every array access
+    of the library's cell functions is then bounds-checked on the host."""
+    if os.environ.get("MAESTRO_HOST_ASAN") == "1":
+        return ["-O1", "-g", "-fsanitize=address", "-fno-omit-frame-pointer"]
+    return ["-O2"]
+
+
 @pytest.fixture(scope="module")
 def host_lib(tmp_path_factory):
     cxx = shutil.which("g++") or shutil.which("c++")
     if cxx is None:
         pytest.skip("no C++ compiler")
     out = str(tmp_path_factory.mktemp("hgh") / "libhg_host.so")
-    subprocess.run([cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-I",
+    subprocess.run([cxx, *_opt_flags(), "-std=c++17", "-fPIC", "-shared", "-I",
                     os.path.join(ROOT, "maestro_gb300", "csrc"),
                     os.path.join(ROOT, "tests", "csrc", "hg_host.cpp"), "-o", out],
                    check=True, capture_output=True)
