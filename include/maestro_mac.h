@@ -267,7 +267,10 @@ int mac_ctx_set_amr(mac_ctx* ctx, int nlev, const int* nboxes, const int* box_lo
  * beta0_edge[l] the planar base state of level l (n_l[dm-1] and n_l[dm-1] + 1 values; NULL
  * together: no beta0).  The composite problem (coarse-fine ghosts, reflux) is described in the
  * library's mac_amr.cuh; the tolerance is min(rel_eps * 10^(nlev-1), 1e-8) as in MAESTRO
- * (Source/macproject.f90:217); FP64 whatever the context's precision.  Needs mac_ctx_set_amr.
+ * (Source/macproject.f90:217).  A context created with MAC_PREC_FP64 runs FP64 multi-level cycles;
+ * one created with MAC_PREC_MIXED runs FP32 multi-level cycles under FP64 refinement (FP64
+ * composite residual, accumulation and convergence test; the level-0 coarse correction is an
+ * FP64 V-cycle).  Needs mac_ctx_set_amr.
  */
 int mac_macproject_ml_dense(mac_ctx* ctx, double* const* umac, double* const* phi,
                             const double* const* rho, const double* const* macrhs,

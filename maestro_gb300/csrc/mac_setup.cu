@@ -627,10 +627,12 @@ DiagParams diag_params(const mac_ctx* c, const Level& L) {
 bool mixed(const mac_ctx* c) { return c->o.precision == MAC_PREC_MIXED; }
 
 // diag (+ 1/diag in FP64 where an FP64 smoother or the bottom solve reads it, + FP32 copies
-// for the mixed-precision inner cycle) of level l.
+// for the mixed-precision inner cycle) of level l.  A mixed-precision context still runs FP64
+// V-cycles of level 0 when an AMR hierarchy is set (the coarse correction of the composite
+// cycle), so every level then needs the FP64 1/diag too.
 int build_diag(mac_ctx* c, int l, bool fp32) {
     Level& L = c->lev[l];
-    const bool need_inv64 = !mixed(c) || l == c->nlevels - 1;
+    const bool need_inv64 = !mixed(c) || l == c->nlevels - 1 || c->amr != nullptr;
     const Grid3 g = grid3(L.d.n0, L.d.n1, L.d.n2);
     k_build_diag<<<g.grid, g.block, 0, c->stream>>>(
         L.d, diag_params(c, L), L.a64.bx, L.a64.by, L.a64.bz, L.alpha, L.a64.diag,
