@@ -195,6 +195,13 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi"}
 
 
+# ---- the workload's config object, identical in both arms ------------------------------------
+def mac_config(name, n, box, world):
+    return {"workload": name, "n": list(n), "box": list(box), "rel_eps": 1e-10,
+            "l2": "inputs larger than L2 (0.5 GB per step, a distinct copy per step)",
+            "parallelism": f"replicas x{world}"}
+
+
 # ---- reference arm: the CPU oracle ------------------------------------------------------------
 def host_cores():
     try:
@@ -209,16 +216,9 @@ def run_reference(args, rank, world):
     import oracle as O
     from maestro_gb300.inputs import CONFIGS, make_case
     kw = dict(CONFIGS[args.config])
-    # bounded sample per step: the same stratified workload on one 128^3 box (1/8 of the cells,
-    # the same 7-level hierarchy), solves/s scaled to the 256^3 domain by the cell ratio
-    full = 1
-    for v in kw["n"]:
-        full *= v
-    kw["n"] = tuple(kw["box"])
-    sample_cells = 1
-    for v in kw["n"]:
-        sample_cells *= v
-    c = make_case(name=args.config + "_sample", seed=args.seed, **kw)
+    # every step is one full solve of the benchmark configuration itself (256^3, 8 boxes of
+    # 128^3): the same inputs, hierarchy and tolerance as the GPU arm
+    c = make_case(name=args.config, seed=args.seed, **kw)
     nlev = O.nlevels_for_boxes([c.box])
     # every host core (a launcher may have set OMP_NUM_THREADS=1 for its ranks)
     threads = host_cores()
@@ -235,19 +235,18 @@ def run_reference(args, rank, world):
         step()
     ts = [step() for _ in range(args.steps)]
     secs = sum(ts)
-    value = args.steps / secs * (sample_cells / full)
+    value = args.steps / secs
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded stratified atmosphere)",
-        "config": {"workload": args.config, "n": list(CONFIGS[args.config]["n"]),
-                   "box": list(CONFIGS[args.config]["box"]), "rel_eps": 1e-10},
+        "config": mac_config(args.config, c.n, c.box, world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"per step one {kw['n'][0]}^3 solve of the same workload "
-                                   f"({sample_cells / full:.4g} of the cells), solves/s scaled "
-                                   f"by the cell ratio; C++/OpenMP FP64 restatement of MAESTRO's "
-                                   f"macproject + FBoxLib MG (Fortran reference unbuildable)"},
+                         "sample": f"per step one full {'x'.join(map(str, c.n))} solve of the "
+                                   f"benchmark workload (the same configuration as the GPU arm); "
+                                   f"C++/OpenMP FP64 restatement of MAESTRO's macproject + "
+                                   f"FBoxLib MG (Fortran reference unbuildable)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
@@ -710,9 +709,8 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_mixed / K, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 V-cycles + f64 refinement",
         "data": "synthetic (seeded stratified atmosphere)",
-        "config": {"workload": args.config, "n": list(c.n), "box": list(c.box), "rel_eps": 1e-10,
-                   "precision": "mixed", "l2": "inputs larger than L2 (0.5 GB per step, "
-                   "a distinct copy per step)", "parallelism": f"replicas x{world}"},
+        "config": mac_config(args.config, c.n, c.box, world),
+        "precision": "mixed",
         "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": ms_fp64 / K,
                  "vcycles": st_fp64[-1]["vcycles"], "rel_resid": st_fp64[-1]["rel_resid"]},
         "mixed_over_fp64": value / fp64_value,
