@@ -19,8 +19,10 @@
 //   * calls that overlap on the GPU (different streams, or different host threads) race on the
 //     array -- serialise them (one stream does that);
 //   * the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress while that device is current; make that first call before any stream
-//     capture that should contain later calls.
+//     cudaGetSymbolAddress while that device is current; that first call should come before any
+//     stream capture on the device.
+//   * every max-norm propagates NaN (a NaN input makes the call return MAC_ERR_NONFINITE, never a
+//     converged status).
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -144,12 +146,18 @@ __device__ double cta_sum(double v, double* sm) {
     return r;
 }
 
+// max that keeps a NaN from either side (the library's fmax drops NaN and would hide a
+// non-finite input)
+__device__ __forceinline__ double nan_max(double acc, double v) {
+    return (v > acc || v != v) ? v : acc;
+}
+
 __device__ double cta_max(double v, double* sm) {
     const int t = threadIdx.x;
     sm[t] = v;
     __syncthreads();
     for (int o = kThreads / 2; o > 0; o >>= 1) {
-        if (t < o) sm[t] = fmax(sm[t], sm[t + o]);
+        if (t < o) sm[t] = nan_max(sm[t], sm[t + o]);
         __syncthreads();
     }
     const double r = sm[0];
@@ -165,10 +173,12 @@ __device__ void apply(const View& v, const double* x, double* y) {
 // One CTA: BiCGStab (Jacobi right preconditioner) on the whole level to
 // ||f - A x||_inf <= eps ||f||_inf, restarted from the current x when the true residual is still
 // above the tolerance after the recursive one met it.  All nine work vectors are (re)written
-// before they are read.
+// before they are read.  The problem is singular when no face is Dirichlet (geom_singular) and
+// alpha is NULL or zero everywhere; the mean of rh is then removed.
 __global__ void __launch_bounds__(kThreads)
-k_na_solve(View v, double* __restrict__ phi, const double* __restrict__ rh, double* __restrict__ vec,
-           double* __restrict__ result, int singular, double eps, int max_iter) {
+k_na_solve(View v, double* __restrict__ phi, const double* __restrict__ rh,
+           const double* __restrict__ alpha, double* __restrict__ vec,
+           double* __restrict__ result, int geom_singular, double eps, int max_iter) {
     __shared__ double sm[kThreads];
     const int N = v.N;
     const int tid = threadIdx.x;
@@ -188,10 +198,16 @@ k_na_solve(View v, double* __restrict__ phi, const double* __restrict__ rh, doub
         loc += f[c];
     }
     const double mean = cta_sum(loc, sm) / N;
+    bool singular = geom_singular != 0;
+    if (singular && alpha) {
+        loc = 0.0;
+        for (int c = tid; c < N; c += kThreads) loc = nan_max(loc, fabs(alpha[c]));
+        singular = cta_max(loc, sm) == 0.0;
+    }
     loc = 0.0;
     for (int c = tid; c < N; c += kThreads) {
         if (singular) f[c] -= mean;
-        loc = fmax(loc, fabs(f[c]));
+        loc = nan_max(loc, fabs(f[c]));
     }
     const double fnorm = cta_max(loc, sm);
     int iters = 0;
@@ -211,7 +227,7 @@ k_na_solve(View v, double* __restrict__ phi, const double* __restrict__ rh, doub
                 rh0[c] = r[c];
                 p[c] = 0.0;
                 vv[c] = 0.0;
-                loc = fmax(loc, fabs(r[c]));
+                loc = nan_max(loc, fabs(r[c]));
             }
             const double rn0 = cta_max(loc, sm);
             rel = rn0 / fnorm;
@@ -255,7 +271,7 @@ k_na_solve(View v, double* __restrict__ phi, const double* __restrict__ rh, doub
                 for (int c = tid; c < N; c += kThreads) {
                     x[c] += omega * y[c];
                     r[c] = s[c] - omega * t[c];
-                    loc = fmax(loc, fabs(r[c]));
+                    loc = nan_max(loc, fabs(r[c]));
                 }
                 const double rn = cta_max(loc, sm);
                 if (!(rn > 0.5 * tol) || omega == 0.0) restart = true;
@@ -266,7 +282,7 @@ k_na_solve(View v, double* __restrict__ phi, const double* __restrict__ rh, doub
         // final true residual
         apply(v, x, t);
         loc = 0.0;
-        for (int c = tid; c < N; c += kThreads) loc = fmax(loc, fabs(f[c] - t[c]));
+        for (int c = tid; c < N; c += kThreads) loc = nan_max(loc, fabs(f[c] - t[c]));
         rel = cta_max(loc, sm) / fnorm;
     }
     for (int c = tid; c < N; c += kThreads) phi[c] = x[c];
@@ -335,8 +351,8 @@ extern "C" int mac_solve_small_noalloc(int dm, const int* n, const double* dx, c
     v.bz = op + 2 * G.N;
     v.dg = op + 3 * G.N;
     v.idg = op + 4 * G.N;
-    const bool singular = !has_dir && alpha == nullptr;
-    k_na_solve<<<1, kThreads, 0, s>>>(v, phi, rh, vec, result, singular ? 1 : 0, rel_eps, max_iter);
+    k_na_solve<<<1, kThreads, 0, s>>>(v, phi, rh, alpha, vec, result, has_dir ? 0 : 1, rel_eps,
+                                      max_iter);
     MAC_CUDA_TRY(cudaGetLastError());
     double res[3] = {0.0, 0.0, 0.0};
     MAC_CUDA_TRY(cudaMemcpyAsync(res, result, sizeof(res), cudaMemcpyDeviceToHost, s));
