@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=24)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other workload configurations (2-D 128^2, 512^3 mixed, "
+                         "384^3 stiff, 256^3 adjoint)")
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--inner", type=int, default=None,
                     help="mixed precision: most FP32 V-cycles per FP64 refinement step")
@@ -446,6 +449,164 @@ def run_extra(args, rank, world, local):
     return 0
 
 
+# ---- the other workload configurations (2-D 128^2, 512^3 mixed, 384^3 stiff, 256^3 adjoint) ----
+def measure_configs(dev, with_cpu=False, steps=3, warmup=1, seed=17):
+    """Solves/s of every workload configuration on this GPU (device-resident inputs, CUDA events
+    on the library's stream, a distinct input copy per timed solve), FP64 and mixed precision,
+    with refinement / V-cycle counts and the mixed results' error against the FP64 GPU solve; the
+    adjoint (forward + adjoint solve) of the 256^3 adjoint and 384^3 stiff configurations, FP64
+    and FP32-smoothed (mixed context).  with_cpu: the 2-D configuration's CPU baseline (the
+    oracle's own rate on the host cores).  Errors against the oracle are the GPU tests' business
+    (tests/test_gpu_full_configs.py)."""
+    import numpy as np
+    import torch
+
+    from maestro_gb300.inputs import cell_to_edge, config_case  # noqa: F401
+    from maestro_gb300.macproject import BcTower, Layout, MacProjector
+
+    stream = torch.cuda.current_stream(dev)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a).transpose())).to(dev)  # noqa: E731
+
+    def rel(a, b, demean=False):
+        if demean:
+            a, b = a - a.mean(), b - b.mean()
+        return float((a - b).abs().max() / b.abs().max())
+
+    def solves(c, precision, n_steps, rel_eps=1e-10):
+        u0 = [t(a) for a in c.umac]
+        rho, rhs = t(c.rho), t(c.macrhs)
+        b0 = torch.from_numpy(c.beta0).to(dev)
+        b0e = torch.from_numpy(c.beta0_edge).to(dev)
+        work = [([x.clone() for x in u0], torch.zeros_like(rho)) for _ in range(n_steps)]
+        P = MacProjector(Layout.tiled(c.n, c.box), c.dx, BcTower(c.bc_lo, c.bc_hi),
+                         precision=precision, rel_eps=rel_eps, stream=stream.cuda_stream)
+        sts = []
+        try:
+            def one(k):
+                u, phi = work[k]
+                return P.macproject_dense(u[0].data_ptr(), u[1].data_ptr(),
+                                          u[2].data_ptr() if c.dm == 3 else 0, phi.data_ptr(),
+                                          rho.data_ptr(), rhs.data_ptr(), b0.data_ptr(),
+                                          b0e.data_ptr(), strict=True)
+            for k in range(warmup):
+                one(k)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for k in range(warmup, n_steps):
+                sts.append(one(k))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / (n_steps - warmup)
+        finally:
+            P.close()
+        u, phi = work[-1]
+        del work[:-1]
+        return 1e3 / ms, sts[-1], u, phi
+
+    def adjoints(c, precision, n_steps, rel_eps=1e-10):
+        u = [t(a) for a in c.umac]
+        w = [t(a) for a in c.w]
+        du = [torch.zeros_like(x) for x in u]
+        rho, rhs = t(c.rho), t(c.macrhs)
+        b0 = torch.from_numpy(c.beta0).to(dev)
+        b0e = torch.from_numpy(c.beta0_edge).to(dev)
+        drinv, dmac = torch.zeros_like(rho), torch.zeros_like(rho)
+        db0 = torch.zeros_like(b0)
+        P = MacProjector(Layout.tiled(c.n, c.box), c.dx, BcTower(c.bc_lo, c.bc_hi),
+                         precision=precision, rel_eps=rel_eps, stream=stream.cuda_stream)
+        try:
+            def one():
+                return P.adjoint_dense([x.data_ptr() for x in u], rho.data_ptr(), rhs.data_ptr(),
+                                       b0.data_ptr(), b0e.data_ptr(), [x.data_ptr() for x in w],
+                                       [x.data_ptr() for x in du], drinv.data_ptr(),
+                                       db0.data_ptr(), dmac.data_ptr(), 0)
+            for _ in range(warmup):
+                one()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(n_steps - warmup):
+                st = one()
+            torch.cuda.synchronize()
+            secs = (time.perf_counter() - t0) / (n_steps - warmup)
+        finally:
+            P.close()
+        return 1.0 / secs, st, du, dmac
+
+    out = {}
+    n_steps = warmup + steps
+
+    # 2-D 128^2 FP64 (and mixed) against the oracle's own rate on the host cores
+    c = config_case("2d_128", seed=seed)
+    r64, st64, u64, p64 = solves(c, "fp64", n_steps)
+    r32, st32, u32, p32 = solves(c, "mixed", n_steps)
+    e2d = {"fp64": r64, "mixed": r32, "fp64_vcycles": st64["vcycles"],
+           "mixed_vcycles": st32["vcycles"], "refine_iters": st32["refine_iters"],
+           "u_err_mixed_vs_fp64": max(rel(a, b) for a, b in zip(u32, u64))}
+    if with_cpu:
+        import oracle as O
+        nlev = O.nlevels_for_boxes([c.box])
+        threads = host_cores()
+        t0 = time.perf_counter()
+        for _ in range(20):
+            O.macproject(c.umac, c.phi0, c.rho, c.dx, c.bc_lo, c.bc_hi, macrhs=c.macrhs,
+                         beta0=c.beta0, beta0_edge=c.beta0_edge, nlevels=nlev, threads=threads)
+        e2d["cpu_baseline"] = {"value": 20 / (time.perf_counter() - t0), "unit": UNIT,
+                               "cores": threads, "kind": "port",
+                               "sample": "20 full 128^2 FP64 solves by the C++/OpenMP oracle"}
+    out["2d_128"] = e2d
+    del c
+
+    # 512^3 mixed (and FP64)
+    c = config_case("3d_512_mixed", seed=seed)
+    r32, st32, u32, p32 = solves(c, "mixed", n_steps)
+    r64, st64, u64, p64 = solves(c, "fp64", n_steps)
+    e5 = {"mixed": r32, "fp64": r64, "mixed_over_fp64": r32 / r64,
+          "refine_iters": st32["refine_iters"], "mixed_vcycles": st32["vcycles"],
+          "fp64_vcycles": st64["vcycles"], "rel_resid_mixed": st32["rel_resid"],
+          "phi_err_mixed_vs_fp64": rel(p32, p64, True),
+          "u_err_mixed_vs_fp64": max(rel(a, b) for a, b in zip(u32, u64))}
+    del u64, p64
+    out["3d_512_mixed"] = e5
+    del c, u32, p32
+    torch.cuda.empty_cache()
+
+    # 256^3 adjoint: forward + adjoint solve, FP64 and FP32-smoothed
+    c = config_case("3d_256_adjoint", seed=seed)
+    a64, sa64, du64, _ = adjoints(c, "fp64", n_steps)
+    a32, sa32, du32, _ = adjoints(c, "mixed", n_steps)
+    out["3d_256_adjoint"] = {
+        "adjoints_per_s_fp64": a64, "adjoints_per_s_mixed": a32,
+        "vcycles_fp64": sa64["vcycles"], "vcycles_mixed": sa32["vcycles"],
+        "du_err_mixed_vs_fp64": max(rel(a, b) for a, b in zip(du32, du64)),
+        "note": "one call = forward projection + adjoint solve + gradient kernels "
+                "(host-timed around the call); FD checks in the GPU tests"}
+    del c, du64, du32
+    torch.cuda.empty_cache()
+
+    # 384^3 stiff: mixed vs FP64 forward, then the FP32-smoothed adjoint
+    c = config_case("3d_384_stiff", seed=seed)
+    rng = np.random.default_rng(seed + 1000)
+    c.w = [np.asfortranarray(rng.standard_normal(u.shape)) for u in c.umac]
+    r32, st32, u32, p32 = solves(c, "mixed", n_steps)
+    r64, st64, u64, p64 = solves(c, "fp64", n_steps)
+    a32, sa32, du32, dm32 = adjoints(c, "mixed", n_steps)
+    a64, sa64, du64, dm64 = adjoints(c, "fp64", n_steps)
+    e6 = {"mixed": r32, "fp64": r64, "mixed_over_fp64": r32 / r64,
+          "refine_iters": st32["refine_iters"], "mixed_vcycles": st32["vcycles"],
+          "fp64_vcycles": st64["vcycles"], "rel_resid_mixed": st32["rel_resid"],
+          "phi_err_mixed_vs_fp64": rel(p32, p64, True),
+          "u_err_mixed_vs_fp64": max(rel(a, b) for a, b in zip(u32, u64)),
+          "adjoints_per_s_mixed": a32, "adjoints_per_s_fp64": a64,
+          "adjoint_mixed_over_fp64": a32 / a64,
+          "adjoint_refine_iters_mixed": sa32["refine_iters"],
+          "du_err_mixed_vs_fp64": max(rel(a, b) for a, b in zip(du32, du64)),
+          "dmacrhs_err_mixed_vs_fp64": rel(dm32, dm64)}
+    del u64, p64, du64, dm64
+    out["3d_384_stiff"] = e6
+    return out
+
+
 # ---- our arm ----------------------------------------------------------------------------------
 def main():
     args = parse()
@@ -702,6 +863,14 @@ def main():
                "sample": f"one full {c.n[0]}^3 FP64 solve ({sto['vcycles']} V-cycles), "
                          f"C++/OpenMP restatement of MAESTRO macproject + FBoxLib MG"}
 
+    # ---- the other configurations (rank 0, N = 1; after every timed region of the headline) ---
+    configs = None
+    if not args.no_configs and rank == 0 and world == 1:
+        try:
+            configs = measure_configs(dev, with_cpu=not args.no_cpu)
+        except Exception as ex:   # reported in the line, the headline stands
+            configs = {"error": repr(ex)[:400]}
+
     launches = sum(s["launches"] for s in st_mixed)
     rr = max(s["rel_resid"] for s in st_mixed)
     out = {
@@ -729,6 +898,7 @@ def main():
         "gpu_launches": launches,
         "clocks": ck_mixed,
         "clocks_fp64": ck_fp64,
+        "configs": configs,
     }
     if rank == 0:
         print(json.dumps(out))

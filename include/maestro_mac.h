@@ -116,6 +116,14 @@ typedef struct mac_opts {
     double inner_omega;     /* mixed precision: relaxation weight of the inner V-cycles'
                                red/black half-sweeps, 0 < omega < 2 (default 1.25; 1:
                                Gauss-Seidel)                                                   */
+    double wait_limit_s;    /* seconds a kernel waits for its own asynchronous copies before it
+                               gives up, records the failure and returns; the call then reports
+                               MAC_ERR_DEVICE_TIMEOUT (0 < wait_limit_s <= 10; default 1)      */
+    int inject_wait_expiry; /* fault injection for failure-handling tests (default 0): 1 = the
+                               first wait of every staged finest-level kernel waits on a barrier
+                               that no copy completes, so it expires after wait_limit_s and the
+                               call returns MAC_ERR_DEVICE_TIMEOUT; the GPU and the context stay
+                               usable                                                          */
 } mac_opts;
 
 /* Kernel classes of mac_stats.ktime_* (finest level unless stated). */

@@ -77,6 +77,8 @@ class MacOpts(ctypes.Structure):
         ("inner_nu2", ctypes.c_int),
         ("inner_exact_bottom", ctypes.c_int),
         ("inner_omega", ctypes.c_double),
+        ("wait_limit_s", ctypes.c_double),
+        ("inject_wait_expiry", ctypes.c_int),
     ]
 
 

@@ -208,6 +208,8 @@ struct OtfParams {
     int rty, rzc, rnz, rsmem;   // the same for the staged defect + restriction (rty == 0: none)
     int* err;             // device flag: a bounded wait on a copy gave up
     float omega;          // relaxation weight of the half-sweeps (1: Gauss-Seidel)
+    unsigned long long wait_ns;   // limit of a wait for the block's own copies (ns)
+    int inject_expiry;    // test: the first wait targets a barrier no copy completes
 };
 // Tile plan of the staged half-sweep for the finest level (OtfParams.ty/zc/nz/smem).
 void plan_otf_tile(const Dims& d, int dm, int sms, OtfParams& P);

@@ -52,13 +52,14 @@ k_gsrb_otf(Dims d, OtfParams P, int colour, float* __restrict__ es, const float*
 // own cells of one row (float4 reads of the stage); the other colour's centre row of planes
 // k-1 / k / k+1 is carried in registers.  Arithmetic per cell is that of otf_cell, in the same
 // order (the x-parity and the Dirichlet terms resolved at compile time).  Every wait is bounded
-// (about one second of %globaltimer); on expiry the block records the failure in P.err, waits
-// (bounded) for the copies it issued and leaves.  4 ring stages at 256^3 (ty = 8): 72 KB of
+// (P.wait_ns of %globaltimer, mac_opts.wait_limit_s, one second by default); on expiry the block
+// records the failure in P.err, waits (bounded by kDrainNs) for the copies it issued and leaves.  4 ring stages at 256^3 (ty = 8): 72 KB of
 // shared memory and 80 registers a thread, 3 blocks per SM.
 constexpr int kStages = 4;          // planes in the shared-memory ring
 constexpr int kRStages = 3;         // the same for the staged restriction (one more array a plane)
 constexpr int kCellsPerThread = 4;  // consecutive colour-half columns (one float4) per thread
-constexpr unsigned long long kWaitNs = 1000000000ull;
+// waits for copies a block has already seen arrive or that are draining after a failed wait
+constexpr unsigned long long kDrainNs = 1000000000ull;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -95,13 +96,13 @@ __device__ __forceinline__ unsigned long long global_ns() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
-// Wait for phase `parity` of the mbarrier; false after about kWaitNs without completion.
-__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// Wait for phase `parity` of the mbarrier; false after about limit_ns without completion.
+__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
     if (mbar_try_wait(bar, parity)) return true;
     const unsigned long long t0 = global_ns();
     for (unsigned n = 1;; ++n) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((n & 63u) == 0 && global_ns() - t0 > kWaitNs) return false;
+        if ((n & 63u) == 0 && global_ns() - t0 > limit_ns) return false;
     }
 }
 
@@ -218,8 +219,10 @@ k_gsrb_otf_staged(Dims d, OtfParams P, int colour, float* __restrict__ es,
     const int nq = kend - k0 + 2;      // planes k0-1 .. kend, local index q = p - (k0 - 1)
     const long plane = (long)n1 * hn0;
     const int t = threadIdx.x;
+    __shared__ unsigned long long never_bar;   // fault injection: no copy ever completes it
     if (t == 0) {
         for (int q = 0; q < kStages; ++q) mbar_init(smem_addr(&bars[q]), 1);
+        if (P.inject_expiry) mbar_init(smem_addr(&never_bar), 1);
         abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -261,7 +264,11 @@ k_gsrb_otf_staged(Dims d, OtfParams P, int colour, float* __restrict__ es,
     // stage (and a failed wait) to the other threads, which do not poll the barrier
     auto wait_plane = [&](int q) {
         if (t != 0 || abort_flag) return;
-        if (mbar_wait(smem_addr(&bars[q % kStages]), (uint32_t)((q / kStages) & 1))) {
+        const bool ok = (P.inject_expiry && q == 0)
+                            ? mbar_wait(smem_addr(&never_bar), 0u, P.wait_ns)
+                            : mbar_wait(smem_addr(&bars[q % kStages]),
+                                        (uint32_t)((q / kStages) & 1), P.wait_ns);
+        if (ok) {
             confirmed = q + 1;
         } else {
             abort_flag = 1;
@@ -363,7 +370,7 @@ k_gsrb_otf_staged(Dims d, OtfParams P, int colour, float* __restrict__ es,
     if (t == 0 && confirmed < issued) {
         // a wait gave up: leave no copy in flight into this block's shared memory (bounded)
         for (int q = confirmed; q < issued; ++q)
-            mbar_wait(smem_addr(&bars[q % kStages]), (uint32_t)((q / kStages) & 1));
+            mbar_wait(smem_addr(&bars[q % kStages]), (uint32_t)((q / kStages) & 1), kDrainNs);
     }
 }
 
@@ -402,8 +409,10 @@ k_resid_restrict_staged(Dims d, Dims C, OtfParams P, const float* __restrict__ e
     const int nq = kend - k0 + 2;
     const long plane = (long)n1 * hn0;
     const int t = threadIdx.x;
+    __shared__ unsigned long long never_bar;   // fault injection: no copy ever completes it
     if (t == 0) {
         for (int q = 0; q < kRStages; ++q) mbar_init(smem_addr(&bars[q]), 1);
+        if (P.inject_expiry) mbar_init(smem_addr(&never_bar), 1);
         abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -442,7 +451,11 @@ k_resid_restrict_staged(Dims d, Dims C, OtfParams P, const float* __restrict__ e
     }
     auto wait_plane = [&](int q) {
         if (t != 0 || abort_flag) return;
-        if (mbar_wait(smem_addr(&bars[q % kRStages]), (uint32_t)((q / kRStages) & 1))) {
+        const bool ok = (P.inject_expiry && q == 0)
+                            ? mbar_wait(smem_addr(&never_bar), 0u, P.wait_ns)
+                            : mbar_wait(smem_addr(&bars[q % kRStages]),
+                                        (uint32_t)((q / kRStages) & 1), P.wait_ns);
+        if (ok) {
             confirmed = q + 1;
         } else {
             abort_flag = 1;
@@ -546,7 +559,7 @@ k_resid_restrict_staged(Dims d, Dims C, OtfParams P, const float* __restrict__ e
     }
     if (t == 0 && confirmed < issued) {
         for (int q = confirmed; q < issued; ++q)
-            mbar_wait(smem_addr(&bars[q % kRStages]), (uint32_t)((q / kRStages) & 1));
+            mbar_wait(smem_addr(&bars[q % kRStages]), (uint32_t)((q / kRStages) & 1), kDrainNs);
     }
 }
 

@@ -117,6 +117,8 @@ OtfParams otf_params(const mac_ctx* c) {
     P.rsmem = c->otf_tile.rsmem;
     P.err = c->red.counters + 2;
     P.omega = (float)c->o.inner_omega;
+    P.wait_ns = (unsigned long long)(c->o.wait_limit_s * 1e9);
+    P.inject_expiry = c->o.inject_wait_expiry;
     return P;
 }
 
@@ -518,7 +520,11 @@ int run_solve(mac_ctx* c, mac_stats* st) {
         if (!std::isfinite(res)) {
             st->vcycles = nv_total;
             st->rel_resid = res / fnorm;
-            return MAC_ERR_NONFINITE;
+            // a staged kernel that gave up a wait left its part of the sweep undone: report that
+            MAC_CUDA_TRY(cudaMemcpyAsync(c->red.h_counters, c->red.counters, 3 * sizeof(int),
+                                         cudaMemcpyDeviceToHost, c->stream));
+            MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));
+            return c->red.h_counters[2] ? MAC_ERR_DEVICE_TIMEOUT : MAC_ERR_NONFINITE;
         }
         if (prec == MAC_PREC_MIXED && o.adaptive_inner)
             c->cur_inner = next_inner(res_prev, res, nv, target, inner_max);
@@ -594,6 +600,8 @@ int check_opts(const mac_opts* o) {
     if (o->inner_nu1 < -1 || o->inner_nu2 < -1) return MAC_ERR_INVALID;
     if (!(o->inner_omega > 0.0 && o->inner_omega < 2.0)) return MAC_ERR_INVALID;
     if (!(o->rel_eps >= 0.0)) return MAC_ERR_INVALID;
+    if (!(o->wait_limit_s > 0.0 && o->wait_limit_s <= 10.0)) return MAC_ERR_INVALID;
+    if (o->inject_wait_expiry != 0 && o->inject_wait_expiry != 1) return MAC_ERR_INVALID;
     return MAC_OK;
 }
 
@@ -936,6 +944,8 @@ void mac_default_opts(mac_opts* o) {
     o->inner_nu2 = 1;
     o->inner_exact_bottom = 1;
     o->inner_omega = 1.25;
+    o->wait_limit_s = 1.0;
+    o->inject_wait_expiry = 0;
 }
 
 const char* mac_strerror(int code) {

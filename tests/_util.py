@@ -43,3 +43,48 @@ def phi_rel_err(a, b, singular=True):
 
 def u_rel_err(ua, ub):
     return max(rel_err(x, y) for x, y in zip(ua, ub))
+
+
+def adjoint_reference(c, beta, rel_eps=1e-13, threads=0):
+    """The oracle's gradient of L = sum(w . U_proj) (no beta0 derivative): nu, the mean-free
+    solution of L mu = lambda with lambda = G^T(c w) (c = beta_f / beta0_f, walls excluded, the
+    two copies of a periodic face summed), solved by the oracle's FP64 multigrid, and
+    dL/dU_d = w_d + beta0_f (nu_hi - nu_lo) / dx_d (nu zero outside the domain).
+    Returns (nu, [dU_d], stats)."""
+    import oracle as O
+    n = c.n
+    dm = len(n)
+    va = dm - 1
+    lam = np.zeros(n)
+    for d in range(dm):
+        shp = [1] * dm
+        bb = c.beta0_edge if d == va else c.beta0
+        shp[va] = bb.size
+        cw = beta[d] / bb.reshape(shp) * c.w[d]
+        lo = [slice(None)] * dm
+        lo[d] = slice(0, 1)
+        hi = [slice(None)] * dm
+        hi[d] = slice(n[d], n[d] + 1)
+        if c.bc_lo[d] == O.BC_PER:
+            tot = cw[tuple(lo)] + cw[tuple(hi)]
+            cw[tuple(lo)] = tot
+            cw[tuple(hi)] = tot
+        else:
+            cw[tuple(lo)] = 0.0
+            cw[tuple(hi)] = 0.0
+        lam += np.diff(cw, axis=d) / c.dx[d]
+        del cw
+    mu, st = O.mac_multigrid(np.asfortranarray(lam), np.zeros(n, order="F"), beta, c.dx, c.bc_lo,
+                             c.bc_hi, nlevels=O.nlevels_for_boxes([c.box]), rel_eps=rel_eps,
+                             threads=threads)
+    del lam
+    nu = mu - mu.mean()
+    du = []
+    for d in range(dm):
+        pad = [(0, 0)] * dm
+        pad[d] = (1, 1)
+        shp = [1] * dm
+        bb = c.beta0_edge if d == va else c.beta0
+        shp[va] = bb.size
+        du.append(c.w[d] + bb.reshape(shp) * np.diff(np.pad(nu, pad), axis=d) / c.dx[d])
+    return nu, du, st

@@ -47,7 +47,7 @@ def test_cart_dense_matches_oracle(cuda_lib, bc, precision):
     u_o, phi_o, st_o = _oracle(c)
     u, phi, st = _dense(c, precision)
     assert st["status"] == 0 and st["rel_resid"] <= 1e-10
-    tol = 1e-9 if precision == "fp64" else 1e-8
+    tol = 1e-9   # FP64 and mixed alike
     singular = bc == "periodic"
     assert phi_rel_err(phi, phi_o, singular) <= tol
     assert u_rel_err(u, u_o) <= tol
@@ -62,7 +62,7 @@ def test_cart_box_api_host_fabs_matches_oracle(cuda_lib, precision):
     u, phi, st = macproject_cart(c.umac, c.phi0, c.rho, c.dx, BcTower(c.bc_lo, c.bc_hi), c.b0c,
                                  macrhs=c.macrhs, box=c.box, precision=precision)
     assert st["status"] == 0 and st["rel_resid"] <= 1e-10
-    tol = 1e-9 if precision == "fp64" else 1e-8
+    tol = 1e-9   # FP64 and mixed alike
     assert phi_rel_err(phi, phi_o, False) <= tol
     assert u_rel_err(u, u_o) <= tol
 

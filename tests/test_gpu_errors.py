@@ -69,3 +69,52 @@ def test_zero_rhs_gives_zero_phi(cuda_lib):
     c.macrhs[...] = 0.0
     u, phi, st = run(c)
     assert st["status"] == 0 and np.all(phi == 0.0)
+
+
+def test_wait_expiry_reports_device_timeout_and_context_recovers(cuda_lib):
+    """Fault injection on the staged finest-level kernels of the mixed-precision solve (64^3: the
+    staged half-sweep and restriction run): with inject_wait_expiry the first wait of each block
+    targets a barrier that no copy ever completes, so it gives up after wait_limit_s (1 ms here),
+    the block drains its own copies and leaves, and the call returns MAC_ERR_DEVICE_TIMEOUT.  The
+    same context then solves normally, bitwise equal to a fresh context."""
+    from maestro_gb300.macproject import Layout, MacProjector
+    c = make_case(dm=3, n=(64, 64, 64), box=(32, 32, 32), kmax=4, seed=43)
+    lay = Layout.tiled(c.n, c.box)
+    per = [b == capi.MAC_BC_PER for b in c.bc_lo]
+
+    def project(P, strict=True):
+        fu = [lay.to_fabs(c.umac[d], ng=1, face_dir=d, periodic=per) for d in range(3)]
+        fphi = lay.to_fabs(c.phi0, ng=1)
+        st = P.macproject(fu, fphi, lay.to_fabs(c.rho, ng=1, periodic=per),
+                          lay.to_fabs(c.macrhs, ng=0), c.beta0, c.beta0_edge, strict=strict)
+        return lay.from_fabs(fphi, ng=1), [lay.from_fabs(fu[d], ng=1, face_dir=d) for d in range(3)], st
+
+    P = MacProjector(lay, c.dx, BcTower(c.bc_lo, c.bc_hi), precision="mixed", wait_limit_s=1e-3,
+                     inject_wait_expiry=1)
+    try:
+        with pytest.raises(MacError) as e:
+            project(P)
+        assert e.value.code == capi.MAC_ERR_DEVICE_TIMEOUT
+        P.set_opts(inject_wait_expiry=0, wait_limit_s=1.0)
+        phi, u, st = project(P)
+        assert st["status"] == 0 and st["rel_resid"] <= 1e-10
+    finally:
+        P.close()
+    Q = MacProjector(lay, c.dx, BcTower(c.bc_lo, c.bc_hi), precision="mixed")
+    try:
+        phi_f, u_f, st_f = project(Q)
+    finally:
+        Q.close()
+    np.testing.assert_array_equal(phi, phi_f)
+    for a, b in zip(u, u_f):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_wait_limit_option_is_checked(cuda_lib):
+    from maestro_gb300.macproject import Layout, MacProjector
+    c = small()
+    lay = Layout.tiled(c.n, c.box)
+    for bad in (dict(wait_limit_s=0.0), dict(wait_limit_s=11.0), dict(inject_wait_expiry=2)):
+        with pytest.raises(MacError) as e:
+            MacProjector(lay, c.dx, BcTower(c.bc_lo, c.bc_hi), **bad)
+        assert e.value.code == capi.MAC_ERR_INVALID

@@ -1,21 +1,33 @@
-"""The workload configurations at their full sizes, through size-independent properties (the CPU
-oracle is too slow at these sizes; its parity with the GPU path is established on the smaller
-cases of test_gpu_parity.py / test_gpu_adjoint.py):
+"""The workload configurations at their full sizes, against the CPU oracle (its full-size solves
+take seconds to tens of seconds on the host cores) and through size-independent properties.
 
-* 512^3 mixed precision (64 boxes of 128^3, ~1e3 density contrast) and the 384^3 stiff stress
-  case (27 boxes, ~1e6 contrast, 5% noise): the mixed-precision and the FP64 GPU solves both
-  reach 1e-10 relative residual and agree to 1e-9 (phi with its mean removed, U);
-* 256^3 adjoint (the loss L = sum(w . U_proj)): the adjoint gradients with respect to U_edge and
-  1/rho match central finite differences of the forward FP64 solve along seeded random
-  directions, to 1e-6 relative.
+* 256^3 (8 boxes of 128^3, the benchmark workload), FP64 and mixed precision: phi (mean
+  removed) and U within 1e-9 of the oracle's solve, both at 1e-10.
+* 512^3 mixed precision (64 boxes, ~1e3 density contrast): within 1e-9 of the oracle at 1e-10,
+  and within 1e-9 of the FP64 GPU solve.
+* 384^3 stiff stress case (27 boxes, ~1e6 contrast, 5% noise): at 1e-10 the mixed and FP64 GPU
+  solves agree to 1e-9; against the oracle both solvers are driven to 1e-12 (at 1e-10 the
+  solution error kappa * 1e-10 exceeds 1e-9 on this case, for the oracle itself too) and agree
+  to 1e-9.  Then the FP32-smoothed adjoint (the adjoint of a mixed-precision context) against
+  the oracle's FP64 solve of the adjoint right-hand side, both at 1e-12: 1e-9.
+* 256^3 adjoint (L = sum(w . U_proj)): gradients with respect to U_edge, 1/rho and beta0
+  against central finite differences of the forward FP64 solve (driven to 1e-13) along 32
+  seeded directions each, step 1e-6 relative, to 1e-6 relative; dL/dmacrhs and dL/dU against
+  the oracle's solve of the adjoint right-hand side, to 1e-9.
 """
+import functools
+
 import numpy as np
 import pytest
 
+import oracle as O
 from maestro_gb300.inputs import cell_to_edge, config_case
 from maestro_gb300.macproject import BcTower, Layout, MacProjector
+from tests._util import adjoint_reference
 
 pytestmark = pytest.mark.gpu
+
+N_DIRS = 32
 
 
 @pytest.fixture(scope="module")
@@ -23,116 +35,259 @@ def torch():
     return pytest.importorskip("torch")
 
 
-def _dev_case(torch, c):
+@functools.lru_cache(maxsize=1)
+def case(key, seed, with_w=False):
+    c = config_case(key, seed=seed)
+    if with_w and getattr(c, "w", None) is None:
+        rng = np.random.default_rng(seed + 1000)
+        c.w = [np.asfortranarray(rng.standard_normal(u.shape)) for u in c.umac]
+    return c
+
+
+@functools.lru_cache(maxsize=1)
+def oracle_solution(key, seed, rel_eps):
+    c = case(key, seed)
+    u, phi, st = O.macproject(c.umac, c.phi0, c.rho, c.dx, c.bc_lo, c.bc_hi, macrhs=c.macrhs,
+                              beta0=c.beta0, beta0_edge=c.beta0_edge,
+                              nlevels=O.nlevels_for_boxes([c.box]), rel_eps=rel_eps)
+    assert st["status"] == 0 and st["rel_resid"] <= rel_eps, st
+    return u, phi
+
+
+def _to_dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(a).transpose())).to(torch.device("cuda", 0))
+
+
+def _projector(torch, c, precision, rel_eps):
+    return MacProjector(Layout.tiled(c.n, c.box), c.dx, BcTower(c.bc_lo, c.bc_hi),
+                        precision=precision, rel_eps=rel_eps,
+                        stream=torch.cuda.current_stream().cuda_stream)
+
+
+def _solve(torch, c, precision, rel_eps=1e-10, u_in=None, rho_in=None, b0=None, P=None):
+    """One projection on device arrays; u_in / rho_in: device tensors (or None: the case's),
+    b0: beta0 cell values (host; edges by cell_to_edge)."""
     dev = torch.device("cuda", 0)
-    t = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a).transpose())).to(dev)  # noqa: E731
-    return t, dev
-
-
-def _solve(torch, c, precision, rel_eps=1e-10, u_in=None, rho_in=None, **opts):
-    t, dev = _dev_case(torch, c)
-    u = [t(a) for a in (u_in if u_in is not None else c.umac)]
-    phi = t(c.phi0)
-    rho = t(rho_in if rho_in is not None else c.rho)
-    rhs = t(c.macrhs)
-    b0 = torch.from_numpy(np.ascontiguousarray(c.beta0)).to(dev)
-    b0e = torch.from_numpy(np.ascontiguousarray(c.beta0_edge)).to(dev)
-    lay = Layout.tiled(c.n, c.box)
-    P = MacProjector(lay, c.dx, BcTower(c.bc_lo, c.bc_hi), precision=precision, rel_eps=rel_eps,
-                     stream=torch.cuda.current_stream().cuda_stream, **opts)
+    u = [x.clone() for x in u_in] if u_in is not None else [_to_dev(torch, a) for a in c.umac]
+    phi = torch.zeros(tuple(reversed(c.n)), dtype=torch.float64, device=dev)
+    rho = rho_in if rho_in is not None else _to_dev(torch, c.rho)
+    rhs = _to_dev(torch, c.macrhs)
+    b0c = c.beta0 if b0 is None else b0
+    b0d = torch.from_numpy(np.ascontiguousarray(b0c)).to(dev)
+    b0e = torch.from_numpy(np.ascontiguousarray(cell_to_edge(b0c) if b0 is not None
+                                                else c.beta0_edge)).to(dev)
+    own = P is None
+    if own:
+        P = _projector(torch, c, precision, rel_eps)
     try:
         st = P.macproject_dense(u[0].data_ptr(), u[1].data_ptr(), u[2].data_ptr(),
-                                phi.data_ptr(), rho.data_ptr(), rhs.data_ptr(), b0.data_ptr(),
+                                phi.data_ptr(), rho.data_ptr(), rhs.data_ptr(), b0d.data_ptr(),
                                 b0e.data_ptr(), strict=True)
     finally:
-        P.close()
+        if own:
+            P.close()
     torch.cuda.synchronize()
     return u, phi, st
 
 
-@pytest.mark.parametrize("key", ["3d_512_mixed", "3d_384_stiff"])
-def test_large_configs_mixed_matches_fp64(cuda_lib, torch, key):
-    c = config_case(key, seed=17)
+def _errors(torch, u, phi, u_ref, phi_ref):
+    """(phi error with the mean removed, max over components of the U error), relative max-norm;
+    u_ref / phi_ref host (numpy) or device arrays."""
+    ref = lambda a: a if hasattr(a, "data_ptr") else _to_dev(torch, a)  # noqa: E731
+    pr = ref(phi_ref)
+    pr = pr - pr.mean()
+    p = phi - phi.mean()
+    ep = float((p - pr).abs().max() / pr.abs().max())
+    eu = 0.0
+    for a, b in zip(u, u_ref):
+        b = ref(b)
+        eu = max(eu, float((a - b).abs().max() / b.abs().max()))
+    return ep, eu
+
+
+# ---- 256^3, the benchmark workload ------------------------------------------------------------
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_config_256_matches_oracle(cuda_lib, torch, precision):
+    c = case("3d_256", 17)
+    u_o, phi_o = oracle_solution("3d_256", 17, 1e-10)
+    u, phi, st = _solve(torch, c, precision)
+    assert st["status"] == 0 and st["rel_resid"] <= 1e-10
+    ep, eu = _errors(torch, u, phi, u_o, phi_o)
+    print(f"\n256^3 {precision} vs oracle (1e-10): phi {ep:.2e} U {eu:.2e} vcycles {st['vcycles']}")
+    assert ep <= 1e-9 and eu <= 1e-9, (precision, ep, eu)
+
+
+# ---- 512^3 mixed ------------------------------------------------------------------------------
+def test_config_512_mixed_matches_oracle_and_fp64(cuda_lib, torch):
+    c = case("3d_512_mixed", 17)
     u64, p64, st64 = _solve(torch, c, "fp64")
     u32, p32, st32 = _solve(torch, c, "mixed")
     assert st64["status"] == 0 and st64["rel_resid"] <= 1e-10
     assert st32["status"] == 0 and st32["rel_resid"] <= 1e-10
     assert st32["refine_iters"] <= 6
-    scale = lambda x: float(x.abs().max())  # noqa: E731
-    p64, p32 = p64 - p64.mean(), p32 - p32.mean()
-    assert float((p32 - p64).abs().max()) <= 1e-9 * scale(p64)
-    for a, b in zip(u32, u64):
-        assert float((a - b).abs().max()) <= 1e-9 * scale(b)
+    ep, eu = _errors(torch, u32, p32, u64, p64)
+    print(f"\n512^3 mixed vs FP64 GPU: phi {ep:.2e} U {eu:.2e} refine {st32['refine_iters']} "
+          f"vcycles {st32['vcycles']} (FP64 {st64['vcycles']})")
+    assert ep <= 1e-9 and eu <= 1e-9, ("mixed vs fp64", ep, eu)
+    del u64, p64
+    u_o, phi_o = oracle_solution("3d_512_mixed", 17, 1e-10)
+    ep, eu = _errors(torch, u32, p32, u_o, phi_o)
+    print(f"512^3 mixed vs oracle (1e-10): phi {ep:.2e} U {eu:.2e}")
+    assert ep <= 1e-9 and eu <= 1e-9, ("mixed vs oracle", ep, eu)
 
 
-def test_adjoint_256_matches_finite_differences(cuda_lib, torch):
-    c = config_case("3d_256_adjoint", seed=5)
-    t, dev = _dev_case(torch, c)
-    lay = Layout.tiled(c.n, c.box)
-    P = MacProjector(lay, c.dx, BcTower(c.bc_lo, c.bc_hi), precision="fp64", rel_eps=1e-13,
-                     stream=torch.cuda.current_stream().cuda_stream)
+# ---- 384^3 stiff ------------------------------------------------------------------------------
+def test_config_384_stiff_mixed_matches_fp64(cuda_lib, torch):
+    c = case("3d_384_stiff", 17)
+    u64, p64, st64 = _solve(torch, c, "fp64")
+    u32, p32, st32 = _solve(torch, c, "mixed")
+    assert st64["status"] == 0 and st64["rel_resid"] <= 1e-10
+    assert st32["status"] == 0 and st32["rel_resid"] <= 1e-10
+    assert st32["refine_iters"] <= 6
+    ep, eu = _errors(torch, u32, p32, u64, p64)
+    print(f"\n384^3 stiff mixed vs FP64 GPU (1e-10): phi {ep:.2e} U {eu:.2e} refine "
+          f"{st32['refine_iters']} vcycles {st32['vcycles']} (FP64 {st64['vcycles']})")
+    assert ep <= 1e-9 and eu <= 1e-9, (ep, eu)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_config_384_stiff_matches_oracle_tight(cuda_lib, torch, precision):
+    c = case("3d_384_stiff", 17)
+    u_o, phi_o = oracle_solution("3d_384_stiff", 17, 1e-12)
+    u, phi, st = _solve(torch, c, precision, rel_eps=1e-12)
+    assert st["status"] == 0 and st["rel_resid"] <= 1e-12
+    ep, eu = _errors(torch, u, phi, u_o, phi_o)
+    print(f"\n384^3 stiff {precision} vs oracle (both 1e-12): phi {ep:.2e} U {eu:.2e}")
+    assert ep <= 1e-9 and eu <= 1e-9, (precision, ep, eu)
+
+
+def _gradient(torch, c, precision, rel_eps):
+    dev = torch.device("cuda", 0)
+    u = [_to_dev(torch, a) for a in c.umac]
+    w = [_to_dev(torch, a) for a in c.w]
+    du = [torch.zeros_like(x) for x in u]
+    rho = _to_dev(torch, c.rho)
+    rhs = _to_dev(torch, c.macrhs)
+    b0 = torch.from_numpy(c.beta0).to(dev)
+    b0e = torch.from_numpy(c.beta0_edge).to(dev)
+    drinv = torch.zeros_like(rho)
+    dmac = torch.zeros_like(rho)
+    phi = torch.zeros_like(rho)
+    db0 = torch.zeros_like(b0)
+    P = _projector(torch, c, precision, rel_eps)
     try:
-        u = [t(a) for a in c.umac]
-        w = [t(a) for a in c.w]
-        du = [torch.zeros_like(x) for x in u]
-        rho = t(c.rho)
-        rhs = t(c.macrhs)
-        b0 = torch.from_numpy(c.beta0).to(dev)
-        b0e = torch.from_numpy(c.beta0_edge).to(dev)
-        drinv = torch.zeros_like(rho)
-        dmac = torch.zeros_like(rho)
-        phi = torch.zeros_like(rho)
-        db0 = torch.zeros_like(b0)
         st = P.adjoint_dense([x.data_ptr() for x in u], rho.data_ptr(), rhs.data_ptr(),
                              b0.data_ptr(), b0e.data_ptr(), [x.data_ptr() for x in w],
                              [x.data_ptr() for x in du], drinv.data_ptr(), db0.data_ptr(),
                              dmac.data_ptr(), phi.data_ptr())
-        torch.cuda.synchronize()
-        assert st["status"] == 0
     finally:
         P.close()
-    back = lambda x: np.asfortranarray(x.cpu().numpy().transpose())  # noqa: E731
-    gu = [back(x) for x in du]
-    grinv = back(drinv)
+    torch.cuda.synchronize()
+    return dict(du=du, drinv=drinv, db0=db0, dmac=dmac, phi=phi, w=w, st=st)
 
-    def loss(umac, rho_):
-        uo, _, s = _solve(torch, c, "fp64", rel_eps=1e-13, u_in=umac, rho_in=rho_)
-        assert s["status"] == 0
-        return sum(float(np.sum(back(uo[d]) * c.w[d])) for d in range(3))
 
-    rng = np.random.default_rng(8)
-    umax = max(float(np.abs(a).max()) for a in c.umac)
-    for _ in range(2):
-        v = [rng.standard_normal(a.shape) for a in c.umac]
-        h = 1e-6 * umax
-        lp = loss([a + h * b for a, b in zip(c.umac, v)], c.rho)
-        lm = loss([a - h * b for a, b in zip(c.umac, v)], c.rho)
-        fd = (lp - lm) / (2 * h)
-        an = sum(float(np.sum(g * b)) for g, b in zip(gu, v))
-        assert abs(fd - an) <= 1e-6 * max(abs(fd), abs(an))
-    rinv = 1.0 / c.rho
-    for _ in range(2):
-        v = rng.standard_normal(c.rho.shape)
-        h = 1e-6
-        lp = loss(c.umac, 1.0 / (rinv * (1.0 + h * v)))
-        lm = loss(c.umac, 1.0 / (rinv * (1.0 - h * v)))
-        fd = (lp - lm) / (2 * h)
-        an = float(np.sum(grinv * rinv * v))
-        assert abs(fd - an) <= 1e-6 * max(abs(fd), abs(an))
+def _gradient_vs_oracle(torch, c, g, rel_eps):
+    beta = O.mac_coeffs(c.rho, c.dx, c.bc_lo, c.bc_hi, c.beta0, c.beta0_edge)
+    nu, du_ref, st = adjoint_reference(c, beta, rel_eps=rel_eps)
+    del beta
+    assert st["status"] == 0
+    nud = _to_dev(torch, nu)
+    e_nu = float((g["dmac"] - nud).abs().max() / nud.abs().max())
+    e_du = 0.0
+    for a, b in zip(g["du"], du_ref):
+        b = _to_dev(torch, b)
+        e_du = max(e_du, float((a - b).abs().max() / b.abs().max()))
+    return e_nu, e_du
+
+
+def test_config_384_stiff_fp32_smoothed_adjoint_matches_oracle(cuda_lib, torch):
+    """The adjoint solve of a mixed-precision context (FP32-smoothed V-cycles under FP64
+    refinement) on the stiff 384^3 case against the oracle's FP64 solve of the same adjoint
+    right-hand side, both at 1e-12."""
+    c = case("3d_384_stiff", 17, with_w=True)
+    g = _gradient(torch, c, "mixed", 1e-12)
+    assert g["st"]["status"] == 0
+    e_nu, e_du = _gradient_vs_oracle(torch, c, g, 1e-12)
+    print(f"\n384^3 stiff FP32-smoothed adjoint vs oracle (1e-12): dL/dmacrhs {e_nu:.2e} "
+          f"dL/dU {e_du:.2e} refine {g['st']['refine_iters']} vcycles {g['st']['vcycles']}")
+    assert e_nu <= 1e-9 and e_du <= 1e-9, (e_nu, e_du)
+
+
+# ---- 256^3 adjoint ----------------------------------------------------------------------------
+def test_config_256_adjoint(cuda_lib, torch):
+    c = case("3d_256_adjoint", 5)
+    g = _gradient(torch, c, "fp64", 1e-13)
+    assert g["st"]["status"] == 0
+    e_nu, e_du = _gradient_vs_oracle(torch, c, g, 1e-13)
+    print(f"\n256^3 adjoint vs oracle (1e-13): dL/dmacrhs {e_nu:.2e} dL/dU {e_du:.2e}")
+    assert e_nu <= 1e-9 and e_du <= 1e-9, (e_nu, e_du)
+
+    # central finite differences: dL = sum w (U+ - U-) (the difference taken face by face before
+    # the sum, so the large loss itself never cancels)
+    dev = torch.device("cuda", 0)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(2024)
+    P = _projector(torch, c, "fp64", 1e-13)
+    u0 = [_to_dev(torch, a) for a in c.umac]
+    rho0 = _to_dev(torch, c.rho)
+    rinv = 1.0 / rho0
+    umax = max(float(x.abs().max()) for x in u0)
+    w = g["w"]
+
+    def dloss(plus, minus):
+        up, _, sp = _solve(torch, c, "fp64", P=P, **plus)
+        um, _, sm = _solve(torch, c, "fp64", P=P, **minus)
+        assert sp["status"] == 0 and sm["status"] == 0
+        return sum(float(((a - b) * wd).sum()) for a, b, wd in zip(up, um, w))
+
+    worst = {"U": 0.0, "1/rho": 0.0, "beta0": 0.0}
+    rng = np.random.default_rng(11)
+    try:
+        for _ in range(N_DIRS):
+            v = [torch.randn(x.shape, generator=gen, device=dev, dtype=torch.float64) for x in u0]
+            h = 1e-6 * umax
+            fd = dloss(dict(u_in=[a + h * b for a, b in zip(u0, v)]),
+                       dict(u_in=[a - h * b for a, b in zip(u0, v)])) / (2 * h)
+            an = sum(float((gd * b).sum()) for gd, b in zip(g["du"], v))
+            worst["U"] = max(worst["U"], abs(fd - an) / max(abs(fd), abs(an)))
+
+            v = torch.randn(rho0.shape, generator=gen, device=dev, dtype=torch.float64)
+            h = 1e-6
+            fd = dloss(dict(rho_in=1.0 / (rinv * (1.0 + h * v))),
+                       dict(rho_in=1.0 / (rinv * (1.0 - h * v)))) / (2 * h)
+            an = float((g["drinv"] * rinv * v).sum())
+            worst["1/rho"] = max(worst["1/rho"], abs(fd - an) / max(abs(fd), abs(an)))
+
+            vb = rng.standard_normal(c.beta0.shape)
+            fd = dloss(dict(b0=c.beta0 * (1.0 + h * vb)), dict(b0=c.beta0 * (1.0 - h * vb))) / (2 * h)
+            an = float(np.sum(g["db0"].cpu().numpy() * c.beta0 * vb))
+            worst["beta0"] = max(worst["beta0"], abs(fd - an) / max(abs(fd), abs(an)))
+    finally:
+        P.close()
+    print("256^3 adjoint vs central FD, worst of 32 directions: " +
+          ", ".join(f"{k} {v:.2e}" for k, v in worst.items()))
+    assert all(v <= 1e-6 for v in worst.values()), worst
 
 
 def test_krylov_inner_option_256(cuda_lib, torch):
     """The opt-in flexible-CG inner solve (inner_krylov=1, which needs plain Gauss-Seidel
     half-sweeps: inner_omega = 1) reaches the tolerance with fewer FP32 V-cycles than the same
     cycles applied one after the other and stays within 1e-9 of the FP64 solve."""
-    c = config_case("3d_256", seed=17)
-    u64, p64, st64 = _solve(torch, c, "fp64")
-    _, _, stgs = _solve(torch, c, "mixed", inner_omega=1.0, inner_vcycles=4)
-    u32, p32, st32 = _solve(torch, c, "mixed", inner_krylov=1, inner_omega=1.0, inner_vcycles=4)
+    c = case("3d_256", 17)
+
+    def run(precision, **opts):
+        P = MacProjector(Layout.tiled(c.n, c.box), c.dx, BcTower(c.bc_lo, c.bc_hi),
+                         precision=precision, stream=torch.cuda.current_stream().cuda_stream,
+                         **opts)
+        try:
+            return _solve(torch, c, precision, P=P)
+        finally:
+            P.close()
+
+    u64, p64, st64 = run("fp64")
+    _, _, stgs = run("mixed", inner_omega=1.0, inner_vcycles=4)
+    u32, p32, st32 = run("mixed", inner_krylov=1, inner_omega=1.0, inner_vcycles=4)
     assert st32["status"] == 0 and st32["rel_resid"] <= 1e-10
     assert stgs["status"] == 0 and st32["vcycles"] < stgs["vcycles"]
-    scale = lambda x: float(x.abs().max())  # noqa: E731
-    p64, p32 = p64 - p64.mean(), p32 - p32.mean()
-    assert float((p32 - p64).abs().max()) <= 1e-9 * scale(p64)
-    for a, b in zip(u32, u64):
-        assert float((a - b).abs().max()) <= 1e-9 * scale(b)
+    ep, eu = _errors(torch, u32, p32, u64, p64)
+    assert ep <= 1e-9 and eu <= 1e-9, (ep, eu)

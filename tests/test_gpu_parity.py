@@ -2,9 +2,12 @@
 golden fixtures, FP64 and mixed precision.
 
 Tolerances (the parity bar): relative residual <= 1e-10; phi (mean removed for singular
-problems) and the corrected U within 1e-9 relative (max-norm, relative to the oracle's max) for
-the FP64 solve.  The mixed-precision solve converges to the same 1e-10 residual along a different
-iterate sequence; its distance to the FP64 oracle is bounded by 1e-8 here and reported by bench.
+problems) and the corrected U within 1e-9 relative (max-norm, relative to the oracle's max), for
+the FP64 and the mixed-precision solve alike.  The mixed-precision solve converges to the same
+residual along a different iterate sequence, so where the two stop inside the tolerance differs;
+on the stiff case (density contrast ~1e6) that difference is bounded by the conditioning, not by
+the tolerance: at 1e-10 the oracle's own velocities are ~8e-9 from the converged solution
+(kappa * 1e-10 > 1e-9).  There both solvers are driven to 1e-12 and compared at 1e-9.
 """
 import functools
 
@@ -91,9 +94,8 @@ def test_config_2d_128_full_size(cuda_lib, precision):
     u, phi, st = gpu_project(c, precision)
     assert st["status"] == 0 and st["rel_resid"] <= 1e-10
     assert true_rel_resid(c, phi) <= 1.5e-10
-    tol = 1e-9 if precision == "fp64" else 1e-8
-    assert phi_rel_err(phi, phi_o) <= tol
-    assert u_rel_err(u, u_o) <= tol
+    assert phi_rel_err(phi, phi_o) <= 1e-9
+    assert u_rel_err(u, u_o) <= 1e-9
     if precision == "fp64":
         assert abs(st["vcycles"] - st_o["vcycles"]) <= 1
 
@@ -110,6 +112,10 @@ CASES3D = {
 }
 
 
+# density contrast ~1e6: compared with both solvers driven to 1e-12 in mixed precision (above)
+STIFF = {"stiff48_b16"}
+
+
 def build3d(name):
     kw, bcs = CASES3D[name]
     c = make_case(name=name, **kw)
@@ -123,13 +129,13 @@ def build3d(name):
 def test_3d_cases_match_oracle(cuda_lib, name, precision):
     c = build3d(name)
     singular = all(b != BC_DIR for b in c.bc_lo + c.bc_hi)
-    u_o, phi_o, st_o = oracle_project(c)
-    u, phi, st = gpu_project(c, precision)
-    assert st["status"] == 0 and st["rel_resid"] <= 1e-10, st
-    assert true_rel_resid(c, phi) <= 1.5e-10
-    tol = 1e-9 if precision == "fp64" else 1e-8
-    assert phi_rel_err(phi, phi_o, singular) <= tol
-    assert u_rel_err(u, u_o) <= tol
+    eps = 1e-12 if (precision == "mixed" and name in STIFF) else 1e-10
+    u_o, phi_o, st_o = oracle_project(c, rel_eps=eps)
+    u, phi, st = gpu_project(c, precision, rel_eps=eps)
+    assert st["status"] == 0 and st["rel_resid"] <= eps, st
+    assert true_rel_resid(c, phi) <= 1.5 * eps
+    assert phi_rel_err(phi, phi_o, singular) <= 1e-9
+    assert u_rel_err(u, u_o) <= 1e-9
     if precision == "fp64":
         assert abs(st["vcycles"] - st_o["vcycles"]) <= 1
         assert st["nlevels"] == O.nlevels_for_boxes([c.box])
@@ -246,7 +252,7 @@ def test_mac_multigrid_helmholtz_matches_oracle(cuda_lib, precision):
         P.close()
     phi = lay.from_fabs(fphi, ng=1)
     assert st["status"] == 0 and st["rel_resid"] <= 1e-10
-    assert rel_err(phi, phi_o) <= (1e-9 if precision == "fp64" else 1e-8)
+    assert rel_err(phi, phi_o) <= 1e-9
 
 
 def test_repeat_calls_bitwise_identical(cuda_lib):
@@ -366,6 +372,6 @@ def test_mixed_exact_bottom(cuda_lib, name, exact):
     u, phi, st = gpu_project(c, "mixed", inner_exact_bottom=exact)
     assert st["status"] == 0 and st["rel_resid"] <= 1e-10
     assert true_rel_resid(c, phi) <= 1.5e-10
-    assert phi_rel_err(phi, phi_o, singular) <= 1e-8
-    assert u_rel_err(u, u_o) <= 1e-8
+    assert phi_rel_err(phi, phi_o, singular) <= 1e-9
+    assert u_rel_err(u, u_o) <= 1e-9
     assert (st["bottom_iters"] == 0) == bool(exact)
