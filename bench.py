@@ -732,35 +732,53 @@ def main():
     Pm.close()
     Pd.close()
 
-    # ---- roofline of the dominant kernel: finest-level GS-RB half sweeps (mixed, FP32) ------
+    # ---- roofline of the dominant kernel: the finest level's red/black sweeps (mixed, FP32) --
     hbm_peak, peak_kind = peaks()
     kt_ms = sum(s["ktime_ms"][capi.KT_NAMES.index("smooth")] for s in st_mixed)
     kt_n = sum(s["ktime_launches"][capi.KT_NAMES.index("smooth")] for s in st_mixed)
-    # algorithmic bytes per half-sweep launch of the on-the-fly design (per cell of the level):
-    # the other colour's e (2 B) and both colours' rho (4 B) read, the own colour's f read (2 B)
-    # and e write (2 B) = 10 B; the over-relaxed half-sweep (inner_omega != 1) also reads the own
-    # colour's old e (2 B) = 12 B; coefficients are formed from rho in registers, none is stored
-    omega = capi.default_opts().inner_omega
+    nv = sum(s["vcycles"] for s in st_mixed)
+    dopts = capi.default_opts(**inner_opts)
+    omega = dopts.inner_omega
     sor = omega != 1.0
-    alg_bytes = (12 if sor else 10) * N
+    sweeps_per_cycle = dopts.inner_nu1 + dopts.inner_nu2
+    # the fused kernel runs one launch a sweep, the half-sweep kernels two
+    fused = bool(dopts.fused_sweep) and kt_n == nv * sweeps_per_cycle
+    if fused:
+        # one whole sweep a launch, per cell of the level: e of both colours read (4 B; plain
+        # Gauss-Seidel does not read the colour-0 old e: 2 B), rho (4 B) and f (4 B) read, e
+        # written (4 B) = 16 B over-relaxed / 14 B Gauss-Seidel; the last pre-smoothing sweep of
+        # each V-cycle also writes the colour-1 defects (2 B); coefficients from rho in registers
+        per_launch = (16 if sor else 14) * N
+        alg_total = kt_n * per_launch + (nv * 2 * N if sor else 0)
+        kname = ("k_sweep_otf_fused (finest level, one whole red/black sweep, out of place, FP32, "
+                 "coefficients from rho on the fly%s)" % (
+                     ", over-relaxed omega=%.2f" % omega if sor else ""))
+        tkey = "sweep_otf_fused_sor_fine" if sor else "sweep_otf_fused_fine"
+    else:
+        # one colour half-sweep a launch: the other colour's e (2 B) and both colours' rho (4 B)
+        # read, the own colour's f read (2 B) and e written (2 B) = 10 B; over-relaxed also reads
+        # the own colour's old e (2 B) = 12 B
+        per_launch = (12 if sor else 10) * N
+        alg_total = kt_n * per_launch
+        kname = ("k_gsrb_otf_staged (finest level, one colour half-sweep, FP32, coefficients "
+                 "from rho on the fly%s)" % (", over-relaxed omega=%.2f" % omega if sor else ""))
+        tkey = "gsrb_otf_staged_sor_fine" if sor else "gsrb_otf_staged_fine"
     avg_s = (kt_ms / kt_n) / 1e3 if kt_n else float("nan")
+    alg_bytes = alg_total / kt_n if kt_n else float("nan")
     achieved = alg_bytes / avg_s / 1e9
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
             tj = json.load(f)
-        ent = tj.get("gsrb_otf_staged_sor_fine" if sor else "gsrb_otf_staged_fine")
+        ent = tj.get(tkey)
         if ent and ent.get("cells"):
             traffic = ent["dram_bytes_per_launch"] * N / ent["cells"]
-    roofline = {"bound": "hbm",
-                "kernel": "k_gsrb_otf_staged (finest level, one colour half-sweep, FP32, "
-                          "coefficients from rho on the fly%s)" % (
-                              ", over-relaxed omega=%.2f" % omega if sor else ""),
+    roofline = {"bound": "hbm", "kernel": kname,
                 "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "traffic": traffic,
                 "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_s * 1e3,
-                "peak_kind": peak_kind}
+                "launches": kt_n, "peak_kind": peak_kind}
     cls_ms = {nm: sum(s["ktime_ms"][i] for s in st_mixed) / K for i, nm in enumerate(capi.KT_NAMES)}
 
     # ---- e2e through the public C ABI with pinned host fabs ---------------------------------

@@ -124,6 +124,9 @@ typedef struct mac_opts {
                                that no copy completes, so it expires after wait_limit_s and the
                                call returns MAC_ERR_DEVICE_TIMEOUT; the GPU and the context stay
                                usable                                                          */
+    int fused_sweep;        /* mixed precision, 1: each red/black sweep of the finest FP32 level
+                               runs as one kernel (one HBM pass, the same arithmetic, bitwise
+                               the same result); 0 (default): two half-sweep kernels          */
 } mac_opts;
 
 /* Kernel classes of mac_stats.ktime_* (finest level unless stated). */

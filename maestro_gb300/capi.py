@@ -79,6 +79,7 @@ class MacOpts(ctypes.Structure):
         ("inner_omega", ctypes.c_double),
         ("wait_limit_s", ctypes.c_double),
         ("inject_wait_expiry", ctypes.c_int),
+        ("fused_sweep", ctypes.c_int),
     ]
 
 

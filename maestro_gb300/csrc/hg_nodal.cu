@@ -586,6 +586,10 @@ int hg_check_args(const mac_ctx* c, int proj_type, double dt, bool have_uold) {
     // the colour-parallel sweeps need even periodic extents (same-colour nodes uncoupled)
     for (int d = 0; d < c->dm; ++d)
         if (c->bc_lo[d] == MAC_BC_PER && (c->n[d] & 1)) return MAC_ERR_UNSUPPORTED;
+    // node and cell coordinates are formed in 32-bit arithmetic
+    long nodes = 1;
+    for (int d = 0; d < c->dm; ++d) nodes *= (long)c->n[d] + 1;
+    if (nodes >= (1L << 31)) return MAC_ERR_TOO_LARGE;
     return MAC_OK;
 }
 

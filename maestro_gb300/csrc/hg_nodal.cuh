@@ -91,34 +91,45 @@ HG_HD inline long nnodes(const LevT<T>& L) { return (long)L.nn[0] * L.nn[1] * L.
 template <typename T>
 HG_HD inline long ncells(const LevT<T>& L) { return (long)L.n[0] * L.n[1] * L.n[2]; }
 
+// Coordinates of a node / cell index (32-bit: a level holds fewer than 2^31 nodes, checked where
+// the hierarchy is built; 32-bit division is several times cheaper than 64-bit on the GPU).
 template <typename T>
 HG_HD inline void node_coords(const LevT<T>& L, long idx, int p[3]) {
-    p[0] = (int)(idx % L.nn[0]);
-    const long r = idx / L.nn[0];
-    p[1] = (int)(r % L.nn[1]);
-    p[2] = (int)(r / L.nn[1]);
+    const unsigned u = (unsigned)idx, n0 = (unsigned)L.nn[0], n1 = (unsigned)L.nn[1];
+    const unsigned r = u / n0;
+    p[0] = (int)(u - r * n0);
+    p[2] = (int)(r / n1);
+    p[1] = (int)(r - (unsigned)p[2] * n1);
 }
 template <typename T>
 HG_HD inline void cell_coords(const LevT<T>& L, long idx, int c[3]) {
-    c[0] = (int)(idx % L.n[0]);
-    const long r = idx / L.n[0];
-    c[1] = (int)(r % L.n[1]);
-    c[2] = (int)(r / L.n[1]);
+    const unsigned u = (unsigned)idx, n0 = (unsigned)L.n[0], n1 = (unsigned)L.n[1];
+    const unsigned r = u / n0;
+    c[0] = (int)(u - r * n0);
+    c[2] = (int)(r / n1);
+    c[1] = (int)(r - (unsigned)c[2] * n1);
 }
 
+// Periodic fold of q onto [0, n): every caller passes a q within a few periods of the range
+// (a node or cell index +- 1, or 2 P + a of the restriction), so a few adds replace the modulo.
+HG_HD inline int fold_periodic(int q, int n) {
+    while (q < 0) q += n;
+    while (q >= n) q -= n;
+    return q;
+}
 // Node index q along d folded onto the carrying node (periodic wrap); -1 outside.
 template <typename T>
 HG_HD inline int node_wrap(const Geo& G, const LevT<T>& L, int d, int q) {
     if (d >= G.dm) return q == 0 ? 0 : -1;
     const int n = L.n[d];
-    if (G.per[d]) return ((q % n) + n) % n;
+    if (G.per[d]) return fold_periodic(q, n);
     return (q < 0 || q > n) ? -1 : q;
 }
 template <typename T>
 HG_HD inline int cell_wrap(const Geo& G, const LevT<T>& L, int d, int c) {
     if (d >= G.dm) return c == 0 ? 0 : -1;
     const int n = L.n[d];
-    if (G.per[d]) return ((c % n) + n) % n;
+    if (G.per[d]) return fold_periodic(c, n);
     return (c < 0 || c >= n) ? -1 : c;
 }
 // An unknown: not a periodic image, not on an outflow face.
@@ -224,11 +235,13 @@ HG_HD inline long colour_count(const Geo& G, const LevT<T>& L, int colour) {
 template <typename T>
 HG_HD inline void colour_node(const Geo& G, const LevT<T>& L, int colour, long k, int p[3]) {
     p[0] = p[1] = p[2] = 0;
+    unsigned u = (unsigned)k;
     for (int d = 0; d < G.dm; ++d) {
         const int b = (colour >> d) & 1;
-        const long m = (L.nn[d] - b + 1) / 2;
-        p[d] = 2 * (int)(k % m) + b;
-        k /= m;
+        const unsigned m = (unsigned)((L.nn[d] - b + 1) / 2);
+        const unsigned qd = u / m;
+        p[d] = 2 * (int)(u - qd * m) + b;
+        u = qd;
     }
 }
 

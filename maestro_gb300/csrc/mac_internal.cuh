@@ -210,6 +210,12 @@ struct OtfParams {
     float omega;          // relaxation weight of the half-sweeps (1: Gauss-Seidel)
     unsigned long long wait_ns;   // limit of a wait for the block's own copies (ns)
     int inject_expiry;    // test: the first wait targets a barrier no copy completes
+    // fused red + black sweep (fty == 0: not applicable, the half-sweeps run instead)
+    int fty;              // rows of a tile
+    int fzc, fnz;         // planes per block, blocks along z
+    int fst;              // shared-memory ring stages
+    int fsmem;            // dynamic shared memory bytes
+    int fthreads;         // threads per block: (fty + 2) rows x hn0 / 4
 };
 // Tile plan of the staged half-sweep for the finest level (OtfParams.ty/zc/nz/smem).
 void plan_otf_tile(const Dims& d, int dm, int sms, OtfParams& P);
@@ -298,6 +304,7 @@ struct mac_ctx {
     mac::KrylovBufs kry;                          // flexible-CG vectors (allocated on first use)
     bool mean_pending = false;                    // f still holds the mean (singular problem)
     float* def_b = nullptr;                       // colour-1 defects of the finest FP32 level
+    float* e_alt = nullptr;                       // second finest FP32 correction (fused sweeps)
     // spherical form (beta0 on every face): solver beta and beta0 face arrays (lazily allocated)
     double* cbeta[3] = {nullptr, nullptr, nullptr};
     double* cb0[3] = {nullptr, nullptr, nullptr};
@@ -326,9 +333,11 @@ void launch_gsrb(const Dims& d, int colour, LevelArrays<T>& a, cudaStream_t s, T
 template <typename T>
 void launch_resid_restrict(const Dims& fine, const Dims& coarse, const LevelArrays<T>& a,
                            T* fc, T* ec, bool red_only, cudaStream_t s);
+// phi_in (optional): read the fine values from phi_in instead of phi_fine (out of place; the
+// cells the kernel does not update keep phi_fine's values)
 template <typename T>
 void launch_prolong_add(const Dims& fine, const Dims& coarse, const BcDesc& bc, const T* ec,
-                        T* phi_fine, bool black_only, cudaStream_t s);
+                        T* phi_fine, bool black_only, cudaStream_t s, const T* phi_in = nullptr);
 template <typename T>
 void launch_resid_norm(const Dims& d, const LevelArrays<T>& a, bool red_only,
                        unsigned long long* maxbits, cudaStream_t s);
@@ -362,6 +371,11 @@ void launch_resid_restrict_otf(const Dims& fine, const Dims& coarse, const OtfPa
                                bool red_only, cudaStream_t s, const float* blk = nullptr);
 // whether the staged half-sweep and defect kernels run on this level (then dout/blk apply)
 inline bool otf_staged(const OtfParams& P) { return P.dm == 3 && P.ty > 0 && P.rty > 0; }
+// one whole red/black sweep of the finest FP32 level, ein -> eout (both colours; ein != eout);
+// dout (optional): the colour-1 defects after the sweep, as launch_gsrb_otf's colour-1 dout
+void launch_sweep_otf_fused(const Dims& d, const OtfParams& P, const float* ein, float* eout,
+                            const float* r, cudaStream_t s, float* dout = nullptr);
+
 
 template <typename Tio>
 void launch_bottom(const Dims& d, const LevelArrays<double>& a64, Tio* x, const Tio* f,

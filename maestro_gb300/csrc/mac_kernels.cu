@@ -258,9 +258,11 @@ __device__ __forceinline__ void coarse_nb(int q, int n, int blo, int bhi, int& q
 // BLACK_ONLY: add the correction to colour-1 cells only.  When post-smoothing follows, its first
 // half-sweep overwrites every colour-0 cell without reading it (a red/black update reads only the
 // other colour), so the colour-0 corrections would never be used: half the read-modify-write.
+// uin: the fine values read (uin == u: in place; otherwise u gets uin + correction and the cells
+// not updated keep u's values).
 template <typename T, bool Z2, bool BLACK_ONLY>
 __global__ void __launch_bounds__(kBlock)
-k_prolong_add(Dims F, Dims C, BcDesc bc, const T* __restrict__ ec, T* __restrict__ u) {
+k_prolong_add(Dims F, Dims C, BcDesc bc, const T* __restrict__ ec, T* u, const T* uin) {
     pdl_wait();
     pdl_trigger();
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
@@ -320,10 +322,10 @@ k_prolong_add(Dims F, Dims C, BcDesc bc, const T* __restrict__ ec, T* __restrict
                 const int base = (2 * J + yc + n1 * (Z2 ? 2 * K + zc : K)) * hn0 + I;
                 const int c0 = (yc + zc) & 1;
                 if (BLACK_ONLY) {
-                    fold[zc][yc][0] = u[F.half + base];
+                    fold[zc][yc][0] = uin[F.half + base];
                 } else {
-                    fold[zc][yc][0] = u[c0 * F.half + base];
-                    fold[zc][yc][1] = u[(c0 ^ 1) * F.half + base];
+                    fold[zc][yc][0] = uin[c0 * F.half + base];
+                    fold[zc][yc][1] = uin[(c0 ^ 1) * F.half + base];
                 }
             }
     }
@@ -721,10 +723,11 @@ void launch_resid_restrict(const Dims& fine, const Dims& coarse, const LevelArra
 
 template <typename T>
 void launch_prolong_add(const Dims& fine, const Dims& coarse, const BcDesc& bc, const T* ec,
-                        T* phi_fine, bool black_only, cudaStream_t s) {
+                        T* phi_fine, bool black_only, cudaStream_t s, const T* phi_in) {
     const Grid3 g = grid3(coarse.n0, coarse.n1, coarse.n2);
+    const T* uin = phi_in ? phi_in : phi_fine;
     if (std::is_same<T, double>::value && fine.rz == 2 && fine.split &&
-        fine.ncell >= (1 << 22)) {
+        fine.ncell >= (1 << 22) && uin == phi_fine) {
         // z-marching kernel for large FP64 levels (measured: FP64 solve +2.4% at 256^3; the FP32
         // level-0 prolongation stays faster with one thread per coarse cell): warps of 30
         // columns, up to 8 warps a block along x; planes per thread as many as still leave ~48
@@ -744,17 +747,17 @@ void launch_prolong_add(const Dims& fine, const Dims& coarse, const BcDesc& bc, 
     } else if (fine.rz == 2) {
         if (black_only)
             launch_chain(k_prolong_add<T, true, true>, g.grid, g.block, 0, s, fine, coarse, bc, ec,
-                       phi_fine);
+                       phi_fine, uin);
         else
             launch_chain(k_prolong_add<T, true, false>, g.grid, g.block, 0, s, fine, coarse, bc, ec,
-                       phi_fine);
+                       phi_fine, uin);
     } else {
         if (black_only)
             launch_chain(k_prolong_add<T, false, true>, g.grid, g.block, 0, s, fine, coarse, bc, ec,
-                       phi_fine);
+                       phi_fine, uin);
         else
             launch_chain(k_prolong_add<T, false, false>, g.grid, g.block, 0, s, fine, coarse, bc, ec,
-                       phi_fine);
+                       phi_fine, uin);
     }
 }
 
@@ -839,9 +842,9 @@ template void launch_resid_restrict<double>(const Dims&, const Dims&, const Leve
 template void launch_resid_restrict<float>(const Dims&, const Dims&, const LevelArrays<float>&,
                                             float*, float*, bool, cudaStream_t);
 template void launch_prolong_add<double>(const Dims&, const Dims&, const BcDesc&, const double*,
-                                         double*, bool, cudaStream_t);
+                                         double*, bool, cudaStream_t, const double*);
 template void launch_prolong_add<float>(const Dims&, const Dims&, const BcDesc&, const float*,
-                                         float*, bool, cudaStream_t);
+                                         float*, bool, cudaStream_t, const float*);
 template void launch_resid_norm<double>(const Dims&, const LevelArrays<double>&, bool,
                                         unsigned long long*, cudaStream_t);
 template void launch_resid_norm<float>(const Dims&, const LevelArrays<float>&, bool,

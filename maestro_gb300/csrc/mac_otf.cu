@@ -563,6 +563,255 @@ k_resid_restrict_staged(Dims d, Dims C, OtfParams P, const float* __restrict__ e
     }
 }
 
+// ---- fused red + black sweep -----------------------------------------------------------------
+// One whole sweep (colour 0, then colour 1 from the new colour-0 values) of the finest FP32
+// level in one HBM pass, out of place: ein -> eout (both colours), so no block ever reads a value
+// another block has already updated.  A block owns T rows of whole colour-half planes and a
+// chunk of planes [k0, kend) and marches a wavefront up z: step s updates colour 0 on plane s
+// (its T rows and one halo row on each side, which the colour-1 updates of its edge rows need;
+// planes k0-1 and kend likewise) and colour 1 on plane s-1 from the new colour-0 values of planes
+// s-2, s-1, s.  The shared-memory ring holds, per plane, only what other threads read: the old
+// colour-1 e and rho on rows j0-2 .. j0+T+1 and the colour-0 rho on rows j0-1 .. j0+T, copied by
+// bulk async copies; values of a thread's own row travel in registers along z, and the new
+// colour-0 values of the last plane are exchanged through a double-buffered shared plane.  The
+// per-cell arithmetic is update_group's, in the same order as the two half-sweeps, so the result
+// is bitwise that of k_gsrb_otf_staged colour 0 then colour 1.  DEF: the colour-1 cells' defects
+// after their update go to dout (colour-half indexing), as the DEF half-sweep writes them.
+constexpr int kFMaxThreads = 320;   // (T + 2) rows x hn0 / 4 groups (two blocks an SM)
+
+template <bool DIR, bool SOR, bool DEF>
+__global__ void __launch_bounds__(kFMaxThreads, 2)
+k_sweep_otf_fused(Dims d, OtfParams P, const float* __restrict__ ein, float* __restrict__ eout,
+                  const float* __restrict__ rhs, float* __restrict__ dout) {
+    constexpr int V = kCellsPerThread;
+    extern __shared__ __align__(128) float sm[];
+    __shared__ int abort_flag;
+    __shared__ unsigned long long never_bar;   // fault injection: no copy ever completes it
+    const int hn0 = d.hn0, n1 = d.n1, n2 = d.n2, T = P.fty, NS = P.fst;
+    const long half = d.half;
+    const int rE = T + 4, r0 = T + 2;                 // rows of the colour-1 / colour-0 arrays
+    const int stage = (2 * rE + r0) * hn0;            // floats: e1, rho1, rho0
+    float* nbuf = sm + NS * stage;                    // [2][T + 2][hn0] new colour-0 e
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(nbuf + 2 * r0 * hn0);
+    const int j0 = blockIdx.x * T;
+    const int k0 = blockIdx.y * P.fzc;
+    const int kend = min(k0 + P.fzc, n2);
+    const int nq = kend - k0 + 4;      // planes k0-2 .. kend+1, local index q = p - (k0 - 2)
+    const long plane = (long)n1 * hn0;
+    const int t = threadIdx.x;
+    const float* e1in = ein + half;
+    const float* rho0 = P.rho;
+    const float* rho1 = P.rho + half;
+    if (t == 0) {
+        for (int q = 0; q < NS; ++q) mbar_init(smem_addr(&bars[q]), 1);
+        if (P.inject_expiry) mbar_init(smem_addr(&never_bar), 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    pdl_wait();
+    pdl_trigger();
+
+    auto wrapk = [&](int p) { return p < 0 ? p + n2 : (p >= n2 ? p - n2 : p); };
+    // thread 0: copy plane q into stage q % NS (rows wrapped; a tile row range may wrap around)
+    auto copy_rows = [&](float* dst, const float* src, int first, int nrows, uint32_t bar) {
+        int slot = 0;
+        while (slot < nrows) {
+            int row = first + slot;
+            row += (row < 0) ? n1 : 0;
+            row -= (row >= n1) ? n1 : 0;
+            const int len = min(nrows - slot, n1 - row);
+            bulk_g2s(smem_addr(dst + slot * hn0), src + (long)row * hn0,
+                     (uint32_t)(len * hn0) * 4u, bar);
+            slot += len;
+        }
+    };
+    auto issue = [&](int q) {
+        const int sidx = q % NS;
+        const long pb = (long)wrapk(k0 - 2 + q) * plane;
+        float* st = sm + sidx * stage;
+        const uint32_t bar = smem_addr(&bars[sidx]);
+        mbar_expect_tx(bar, (uint32_t)stage * 4u);
+        copy_rows(st, e1in + pb, j0 - 2, rE, bar);
+        copy_rows(st + rE * hn0, rho1 + pb, j0 - 2, rE, bar);
+        copy_rows(st + 2 * rE * hn0, rho0 + pb, j0 - 1, r0, bar);
+    };
+    int issued = 0, confirmed = 0;
+    if (t == 0) {
+        for (; issued < min(NS, nq); ++issued) issue(issued);
+    }
+    auto wait_plane = [&](int q) {
+        if (t != 0 || abort_flag) return;
+        const bool ok = (P.inject_expiry && q == 0)
+                            ? mbar_wait(smem_addr(&never_bar), 0u, P.wait_ns)
+                            : mbar_wait(smem_addr(&bars[q % NS]), (uint32_t)((q / NS) & 1),
+                                        P.wait_ns);
+        if (ok) {
+            confirmed = q + 1;
+        } else {
+            abort_flag = 1;
+            atomicExch(P.err, 1);
+        }
+    };
+
+    // this thread: row r of the tile (j = j0 - 1 + r, r = 0 and T + 1 are the halo rows that only
+    // get colour-0 updates), columns c0 .. c0 + V - 1 of the colour halves
+    const int G = hn0 / V;
+    const int r = t / G, c0 = (t - r * G) * V;
+    const bool own_row = r >= 1 && r <= T;
+    int j = j0 - 1 + r;
+    j += (j < 0) ? n1 : 0;
+    j -= (j >= n1) ? n1 : 0;
+    const int cm = (c0 == 0) ? hn0 - 1 : c0 - 1;
+    const int cp = (c0 + V == hn0) ? 0 : c0 + V;
+    const bool jl = j > 0 || P.per[1], jh = j < n1 - 1 || P.per[1];
+    const bool wlo = !P.per[0] && c0 == 0, whi = !P.per[0] && c0 + V == hn0;
+    const bool dxl = P.dlo[0] && c0 == 0, dxh = P.dhi[0] && c0 + V == hn0;
+    const bool dy = (j == 0 && P.dlo[1]) || (j == n1 - 1 && P.dhi[1]);
+    const int st_n = n2 + 1;
+    const long rowoff = (long)j * hn0 + c0;
+    // shared-memory offsets of this thread's columns: row r + 1 of the colour-1 arrays, row r of
+    // the colour-0 ones
+    const int o1 = (r + 1) * hn0 + c0, o0 = r * hn0 + c0;
+
+    // factors of plane k, and the update of one group of the given colour
+    auto group = [&](int colour, int k, float ex, float rx, const FV<V>& Ec, const FV<V>& Rc,
+                     const FV<V>& Eb, const FV<V>& Rb, const FV<V>& Ea, const FV<V>& Ra,
+                     const FV<V>& Eym, const FV<V>& Rym, const FV<V>& Eyp, const FV<V>& Ryp,
+                     const FV<V>& Fo, const FV<V>& Ro, float* out, float* accv, float* dgv) {
+        const int s = (colour + j + k) & 1;
+        const float fx = P.fac[k], fy = P.fac[st_n + k];
+        const float fyl = jl ? fy : 0.f, fyh = jh ? fy : 0.f;
+        const float fzl = P.fac[2 * st_n + k], fzh = P.fac[3 * st_n + k];
+        const float fxl0 = wlo ? 0.f : fx, fxhV = whi ? 0.f : fx;
+        if (DIR) {
+            const float wmid = P.fac[4 * st_n + k] + (dy ? fy : 0.f);
+            const float wx0 = wmid + (dxl ? fx : 0.f), wxV = wmid + (dxh ? fx : 0.f);
+            if (s)
+                update_group<V, 1, true, false, true>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym,
+                                                      Eyp, Ryp, Fo, Ro, fx, fxl0, fxhV, fyl, fyh,
+                                                      fzl, fzh, wx0, wxV, wmid, out, nullptr,
+                                                      accv, dgv);
+            else
+                update_group<V, 0, true, false, true>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym,
+                                                      Eyp, Ryp, Fo, Ro, fx, fxl0, fxhV, fyl, fyh,
+                                                      fzl, fzh, wx0, wxV, wmid, out, nullptr,
+                                                      accv, dgv);
+        } else if (s) {
+            update_group<V, 1, false, false, true>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp,
+                                                   Ryp, Fo, Ro, fx, fxl0, fxhV, fyl, fyh, fzl,
+                                                   fzh, 0.f, 0.f, 0.f, out, nullptr, accv, dgv);
+        } else {
+            update_group<V, 0, false, false, true>(ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp,
+                                                   Ryp, Fo, Ro, fx, fxl0, fxhV, fyl, fyh, fzl,
+                                                   fzh, 0.f, 0.f, 0.f, out, nullptr, accv, dgv);
+        }
+        return s;
+    };
+
+    // Per step s the stages of planes s - 1, s and s + 1 are resident: the old colour-1 values of
+    // the own row along z are read from them.  Registers carry only what no stage holds any more
+    // (colour-0 rho and new e of plane s - 2, for the colour-1 update of plane s - 1) and the own
+    // cells' f and old e (plain loads, issued one step ahead).
+    //   f0c/e0c: colour-0 f and old e of plane s; f1c: colour-1 f of plane s - 1 (own rows)
+    FV<V> r0m2, n0m2, f0c, e0c, f1c, f0n, e0n, f1n;
+#pragma unroll
+    for (int m = 0; m < V; ++m) {
+        r0m2.v[m] = n0m2.v[m] = 0.f;
+        e0c.v[m] = e0n.v[m] = f1c.v[m] = f1n.v[m] = 0.f;
+    }
+    // colour-0 f and old e of plane p, colour-1 f of plane p - 1 (the plane colour 1 is updated
+    // on in the same step as colour 0 on plane p)
+    auto load_own = [&](int p, FV<V>& f0x, FV<V>& e0x, FV<V>& f1x) {
+        const long base = (long)wrapk(p) * plane + rowoff;
+        f0x = ldv<V>(rhs + base);
+        if (SOR) e0x = ldv<V>(ein + base);
+        if (own_row) f1x = ldv<V>(rhs + half + (long)wrapk(p - 1) * plane + rowoff);
+    };
+    load_own(k0 - 1, f0c, e0c, f1c);   // (f1 of plane k0 - 2 is never used)
+
+    wait_plane(0);
+    wait_plane(1);
+    for (int s = k0 - 1; s <= kend; ++s) {
+        const int q = s - k0 + 2;           // local index of plane s
+        wait_plane(q + 1);
+        __syncthreads();                    // plane q + 1 landed; nbuf of plane s - 1 complete
+        if (abort_flag) break;
+        if (t == 0 && q >= 2 && issued < nq) issue(issued++);   // the slot of plane q - 2 is free
+        // the next plane's own values: their DRAM latency overlaps this step
+        if (s + 1 <= kend) load_own(s + 1, f0n, e0n, f1n);
+        const int ks = wrapk(s);
+        const float* sc = sm + (q % NS) * stage;              // plane s
+        const float* su = sm + ((q + 1) % NS) * stage;        // plane s + 1
+        const float* sd = sm + ((q + NS - 1) % NS) * stage;   // plane s - 1
+        const float* nb = nbuf + ((q - 1) & 1) * r0 * hn0;    // new colour 0, plane s - 1
+        const FV<V> r0c = ldv<V>(sc + 2 * rE * hn0 + o0);    // colour-0 rho, planes s, s - 1
+        const FV<V> r0m = ldv<V>(sd + 2 * rE * hn0 + o0);
+        const FV<V> n0m = ldv<V>(nb + o0);
+
+        // ---- colour 0 on plane s (all T + 2 rows)
+        FV<V> n0c;
+        {
+            const int sp = (j + ks) & 1;
+            const int cx = sp ? cp : cm;
+            const float ex = sc[o1 - c0 + cx], rx = sc[rE * hn0 + o1 - c0 + cx];
+            const FV<V> Ec = ldv<V>(sc + o1), Rc = ldv<V>(sc + rE * hn0 + o1);
+            const FV<V> Eb = ldv<V>(sd + o1), Rb = ldv<V>(sd + rE * hn0 + o1);
+            const FV<V> Ea = ldv<V>(su + o1), Ra = ldv<V>(su + rE * hn0 + o1);
+            const FV<V> Eym = ldv<V>(sc + o1 - hn0), Rym = ldv<V>(sc + rE * hn0 + o1 - hn0);
+            const FV<V> Eyp = ldv<V>(sc + o1 + hn0), Ryp = ldv<V>(sc + rE * hn0 + o1 + hn0);
+            float out[V], accv[V], dgv[V];
+            group(0, ks, ex, rx, Ec, Rc, Eb, Rb, Ea, Ra, Eym, Rym, Eyp, Ryp, f0c, r0c, out, accv,
+                  dgv);
+            if (SOR) {
+#pragma unroll
+                for (int m = 0; m < V; ++m) out[m] = fmaf(P.omega, out[m] - e0c.v[m], e0c.v[m]);
+            }
+#pragma unroll
+            for (int m = 0; m < V; ++m) n0c.v[m] = out[m];
+            stv<V>(nbuf + (q & 1) * r0 * hn0 + o0, out);
+            if (own_row && s >= k0 && s < kend) stv<V>(eout + (long)ks * plane + rowoff, out);
+        }
+        // ---- colour 1 on plane s - 1 (own rows), from the new colour-0 values
+        if (s >= k0 + 1 && own_row) {
+            const int km = wrapk(s - 1);
+            const float* rb = sd + 2 * rE * hn0;                 // colour-0 rho, plane s - 1
+            const int sp = (1 + j + km) & 1;
+            const int cx = sp ? cp : cm;
+            const float ex = nb[o0 - c0 + cx], rx = rb[o0 - c0 + cx];
+            const FV<V> Eym = ldv<V>(nb + o0 - hn0), Rym = ldv<V>(rb + o0 - hn0);
+            const FV<V> Eyp = ldv<V>(nb + o0 + hn0), Ryp = ldv<V>(rb + o0 + hn0);
+            const FV<V> Ro = ldv<V>(sd + rE * hn0 + o1);        // own rho, plane s - 1
+            float out[V], accv[V], dgv[V];
+            group(1, km, ex, rx, n0m, r0m, n0m2, r0m2, n0c, r0c, Eym, Rym, Eyp, Ryp, f1c, Ro,
+                  out, accv, dgv);
+            if (SOR) {
+                const FV<V> Eold = ldv<V>(sd + o1);              // own old e, plane s - 1
+#pragma unroll
+                for (int m = 0; m < V; ++m) out[m] = fmaf(P.omega, out[m] - Eold.v[m], Eold.v[m]);
+            }
+            const long cell = (long)km * plane + rowoff;
+            stv<V>(eout + half + cell, out);
+            if (DEF) {
+                float dv[V];
+#pragma unroll
+                for (int m = 0; m < V; ++m) dv[m] = fmaf(-dgv[m], out[m], accv[m]);
+                stv<V>(dout + cell, dv);
+            }
+        }
+        r0m2 = r0m;
+        n0m2 = n0m;
+        f0c = f0n;
+        e0c = e0n;
+        f1c = f1n;
+    }
+    if (t == 0 && confirmed < issued) {
+        // a wait gave up: leave no copy in flight into this block's shared memory (bounded)
+        for (int q = confirmed; q < issued; ++q)
+            mbar_wait(smem_addr(&bars[q % NS]), (uint32_t)((q / NS) & 1), kDrainNs);
+    }
+}
+
 template <int DM, bool RED_ONLY>
 __global__ void __launch_bounds__(kB)
 k_resid_restrict_otf(Dims F, Dims C, OtfParams P, const float* __restrict__ e,
@@ -633,6 +882,75 @@ void launch_gsrb_otf(const Dims& d, const OtfParams& P, int colour, float* e, co
         launch_chain(kern, g.grid, g.block, 0, s, d, P, colour, e + own, (const float*)(e + oth),
                      r + own, P.rho + own, P.rho + oth);
     }
+}
+
+// Tile plan of the fused sweep: T = the largest divisor of n1 with (T + 2) * hn0 / 4 <= 320
+// threads and T >= 4; the most ring stages (5, else 4) with which two blocks fit
+// on an SM; chunks of planes so that the blocks fill the resident slots of every SM once.  Sets
+// fty = 0 where the fused sweep does not apply.
+void plan_fused_tile(const Dims& d, int sms, OtfParams& P) {
+    static std::mutex mu;
+    static int fsmem_set = 0;
+    P.fty = P.fzc = P.fnz = P.fst = P.fsmem = P.fthreads = 0;
+    const int G = d.hn0 / kCellsPerThread;
+    int T = 0;
+    for (int cand = d.n1; cand >= 4; --cand) {
+        if (d.n1 % cand || (cand + 2) * G > kFMaxThreads) continue;
+        T = cand;
+        break;
+    }
+    if (T == 0 || d.n2 < 2) return;
+    const int stage = (2 * (T + 4) + (T + 2)) * d.hn0;
+    const int extra = 2 * (T + 2) * d.hn0;
+    int NS = 5;
+    int smem = (NS * stage + extra) * 4 + NS * 8;
+    if (2 * smem > 220 * 1024) {
+        NS = 4;
+        smem = (NS * stage + extra) * 4 + NS * 8;
+    }
+    if (smem > 200 * 1024) return;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (smem > fsmem_set) {
+            bool ok = true;
+            auto setmax = [&](auto kern) {
+                ok = ok && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                smem) == cudaSuccess;
+            };
+            setmax(k_sweep_otf_fused<false, false, false>);
+            setmax(k_sweep_otf_fused<true, false, false>);
+            setmax(k_sweep_otf_fused<false, true, false>);
+            setmax(k_sweep_otf_fused<true, true, false>);
+            setmax(k_sweep_otf_fused<false, true, true>);
+            setmax(k_sweep_otf_fused<true, true, true>);
+            setmax(k_sweep_otf_fused<false, false, true>);
+            setmax(k_sweep_otf_fused<true, false, true>);
+            if (!ok) {
+                cudaGetLastError();
+                return;
+            }
+            fsmem_set = smem;
+        }
+    }
+    const int nt = (T + 2) * G;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_otf_fused<false, true, false>,
+                                                      nt, smem) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return;
+    }
+    const int tiles = d.n1 / T;
+    long chunks = ((long)sms * per_sm) / tiles;
+    if (chunks < 1) chunks = 1;
+    int zc = ceil_div(d.n2, (int)std::min<long>(chunks, d.n2));
+    if (zc < 4) zc = std::min(4, d.n2);
+    P.fty = T;
+    P.fzc = zc;
+    P.fnz = ceil_div(d.n2, zc);
+    P.fst = NS;
+    P.fsmem = smem;
+    P.fthreads = nt;
 }
 
 // Tile plan of the staged half-sweep: ty = the largest power of two with ty * hn0 <= 1024 cells
@@ -738,6 +1056,19 @@ void plan_otf_tile(const Dims& d, int dm, int sms, OtfParams& P) {
     P.rzc = rzc;
     P.rnz = ceil_div(d.n2, rzc);
     P.rsmem = rsmem;
+    plan_fused_tile(d, sms, P);
+}
+
+void launch_sweep_otf_fused(const Dims& d, const OtfParams& P, const float* ein, float* eout,
+                            const float* r, cudaStream_t s, float* dout) {
+    const dim3 grid(d.n1 / P.fty, P.fnz);
+    const bool sor = P.omega != 1.f;
+    auto kern = P.has_dir
+                    ? (sor ? (dout ? k_sweep_otf_fused<true, true, true> : k_sweep_otf_fused<true, true, false>)
+                           : (dout ? k_sweep_otf_fused<true, false, true> : k_sweep_otf_fused<true, false, false>))
+                    : (sor ? (dout ? k_sweep_otf_fused<false, true, true> : k_sweep_otf_fused<false, true, false>)
+                           : (dout ? k_sweep_otf_fused<false, false, true> : k_sweep_otf_fused<false, false, false>));
+    launch_chain(kern, grid, dim3(P.fthreads), (size_t)P.fsmem, s, d, P, ein, eout, r, dout);
 }
 
 void launch_resid_restrict_otf(const Dims& fine, const Dims& coarse, const OtfParams& P,

@@ -119,12 +119,30 @@ OtfParams otf_params(const mac_ctx* c) {
     P.omega = (float)c->o.inner_omega;
     P.wait_ns = (unsigned long long)(c->o.wait_limit_s * 1e9);
     P.inject_expiry = c->o.inject_wait_expiry;
+    P.fty = c->otf_tile.fty;
+    P.fzc = c->otf_tile.fzc;
+    P.fnz = c->otf_tile.fnz;
+    P.fst = c->otf_tile.fst;
+    P.fsmem = c->otf_tile.fsmem;
+    P.fthreads = c->otf_tile.fthreads;
     return P;
 }
 
 inline void mark(mac_ctx* c, bool on, int slot) {
     if (on && c->vtimer < 4)
         cudaEventRecordWithFlags(c->tev[c->vtimer][slot], c->stream, cudaEventRecordExternal);
+}
+
+// Whole red/black sweeps of the finest FP32 level as one kernel each (ping-pong between a32.phi
+// and e_alt; the V-cycle ends in a32.phi).
+// The context's tile plans (otf_tile holds the plans only; its geometry fields are set per call
+// by otf_params) admit the fused sweep on level 0.
+bool fused_plan(const mac_ctx* c) {
+    const OtfParams& T = c->otf_tile;
+    return c->dm == 3 && T.ty > 0 && T.rty > 0 && T.fty > 0;
+}
+bool fused_sweeps(const mac_ctx* c) {
+    return c->otf && c->o.fused_sweep && c->e_alt != nullptr && fused_plan(c);
 }
 
 // The FP32 V-cycle's bottom solved exactly by the dense (pseudo-)inverse (small bottoms, run
@@ -206,6 +224,43 @@ void vcycle(mac_ctx* c, int l) {
     // ones (instead of both colours cell by cell)
     float* blk = otf && !gs && nu1 > 0 && c->def_b && otf_staged(P) && C.d.split ? c->def_b
                                                                                   : nullptr;
+    if (otf && C.d.split && fused_sweeps(c)) {
+        // one kernel a sweep, out of place: the correction alternates between a32.phi (A) and
+        // e_alt (B); the prolongation writes into whichever buffer makes the last post-smoothing
+        // sweep end in A
+        float* A = reinterpret_cast<float*>(a.phi);
+        float* B = c->e_alt;
+        const float* f = reinterpret_cast<const float*>(a.f);
+        float* cur = A;
+        mark(c, tm, 0);
+        for (int s = 0; s < nu1; ++s) {
+            float* out = cur == A ? B : A;
+            launch_sweep_otf_fused(L.d, P, cur, out, f, c->stream, s == nu1 - 1 ? blk : nullptr);
+            ++c->issued;
+            cur = out;
+        }
+        mark(c, tm, 1);
+        launch_resid_restrict_otf(L.d, C.d, P, cur, f, reinterpret_cast<float*>(ac.f),
+                                  reinterpret_cast<float*>(ac.phi), gs && nu1 > 0, c->stream, blk);
+        ++c->issued;
+        mark(c, tm, 2);
+        vcycle<T>(c, l + 1);
+        mark(c, tm, 3);
+        float* tgt = nu2 % 2 ? B : A;
+        launch_prolong_add<float>(L.d, C.d, bc_desc(c), reinterpret_cast<const float*>(ac.phi),
+                                  tgt, gs && nu2 > 0, c->stream, cur);
+        ++c->issued;
+        cur = tgt;
+        mark(c, tm, 4);
+        for (int s = 0; s < nu2; ++s) {
+            float* out = cur == A ? B : A;
+            launch_sweep_otf_fused(L.d, P, cur, out, f, c->stream);
+            ++c->issued;
+            cur = out;
+        }
+        mark(c, tm, 5);
+        return;
+    }
     auto sweep = [&](bool last_down) {
         for (int colour = 0; colour < 2; ++colour) {
             if (otf)
@@ -339,7 +394,8 @@ void collect_timing(mac_ctx* c, int prec) {
         }
         c->ktime_ms[MAC_KT_SMOOTH] += t[0] + t[4];
         c->ktime_launches[MAC_KT_SMOOTH] +=
-            2 * (sweeps_down(c, prec == MAC_PREC_MIXED) + sweeps_up(c, prec == MAC_PREC_MIXED));
+            (prec == MAC_PREC_MIXED && fused_sweeps(c) ? 1 : 2) *
+            (sweeps_down(c, prec == MAC_PREC_MIXED) + sweeps_up(c, prec == MAC_PREC_MIXED));
         c->ktime_ms[MAC_KT_RESTRICT] += t[1];
         c->ktime_launches[MAC_KT_RESTRICT] += 1;
         c->ktime_ms[MAC_KT_COARSE] += t[2];
@@ -437,6 +493,9 @@ int run_solve(mac_ctx* c, mac_stats* st) {
         if (use_krylov(c, prec) && (rc = ensure_krylov(c))) return rc;
         if (c->o.inner_omega != 1.0 && c->otf && !c->def_b &&
             (rc = alloc_arr(c, &c->def_b, (size_t)F.d.half)))
+            return rc;
+        if (c->o.fused_sweep && c->otf && fused_plan(c) && !c->e_alt &&
+            (rc = alloc_arr(c, &c->e_alt, (size_t)F.d.ncell)))
             return rc;
         if (exact_bottom(c)) {
             if (!c->inv_pending) {   // (a caller that built the levels some other way)
@@ -602,6 +661,7 @@ int check_opts(const mac_opts* o) {
     if (!(o->rel_eps >= 0.0)) return MAC_ERR_INVALID;
     if (!(o->wait_limit_s > 0.0 && o->wait_limit_s <= 10.0)) return MAC_ERR_INVALID;
     if (o->inject_wait_expiry != 0 && o->inject_wait_expiry != 1) return MAC_ERR_INVALID;
+    if (o->fused_sweep != 0 && o->fused_sweep != 1) return MAC_ERR_INVALID;
     return MAC_OK;
 }
 
@@ -946,6 +1006,7 @@ void mac_default_opts(mac_opts* o) {
     o->inner_omega = 1.25;
     o->wait_limit_s = 1.0;
     o->inject_wait_expiry = 0;
+    o->fused_sweep = 0;
 }
 
 const char* mac_strerror(int code) {
