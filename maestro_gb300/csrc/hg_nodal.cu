@@ -66,6 +66,179 @@ __global__ void k_hg_update_pi(hg::Lev L, int proj_type, double dt, const double
     HG_LOOP(N) hg::update_pi_node(L, idx, proj_type, dt, phi, pi);
 }
 
+// ---- dense 3-D stencil, interior nodes --------------------------------------------------------
+// For a node p and a neighbour offset o in {-1,0,1}^3 the dense finite-element weight is
+// kw[mask(o)] * (the sum of sigma over the cells p and p + o share), mask(o) = the directions
+// with o_d != 0: the weight table entry does not depend on which shared cell contributes.  A node
+// one or more nodes away from every domain face (no wrap, no missing cell, no image node) takes
+// this path: its 8 cell coefficients, 26 partial sums of them and 27 loads, all unrolled; the
+// others (and 2-D, cross stencils) take node_op.  The sums are formed in a fixed order, so the
+// result does not depend on the launch; it differs from node_op's only in rounding.
+template <typename T>
+__device__ __forceinline__ bool interior3(const hg::LevT<T>& L, const int p[3]) {
+    return p[0] >= 1 && p[0] <= L.n[0] - 2 && p[1] >= 1 && p[1] <= L.n[1] - 2 && p[2] >= 1 &&
+           p[2] <= L.n[2] - 2;
+}
+template <typename T>
+__device__ __forceinline__ void node_op_dense3(const hg::LevT<T>& L, const int p[3],
+                                               const T* __restrict__ phi, T& diag, T& off) {
+    const int n0 = L.n[0], n1 = L.n[1], m0 = L.nn[0], m1 = L.nn[1];
+    // s[z][y][x]: the cell whose low corner is p + (x - 1, y - 1, z - 1)
+    T s[2][2][2];
+    const T* sg = L.sig + (p[0] - 1) + (long)n0 * ((p[1] - 1) + (long)n1 * (p[2] - 1));
+#pragma unroll
+    for (int z = 0; z < 2; ++z)
+#pragma unroll
+        for (int y = 0; y < 2; ++y)
+#pragma unroll
+            for (int x = 0; x < 2; ++x) s[z][y][x] = sg[x + (long)n0 * (y + (long)n1 * z)];
+    // sums over the cells along x (index by the x offset of the neighbour: 0 -> -1, 1 -> 0, 2 -> +1)
+    T sx[2][2][3];
+#pragma unroll
+    for (int z = 0; z < 2; ++z)
+#pragma unroll
+        for (int y = 0; y < 2; ++y) {
+            sx[z][y][0] = s[z][y][0];
+            sx[z][y][1] = s[z][y][0] + s[z][y][1];
+            sx[z][y][2] = s[z][y][1];
+        }
+    T sxy[2][3][3];
+#pragma unroll
+    for (int z = 0; z < 2; ++z)
+#pragma unroll
+        for (int ox = 0; ox < 3; ++ox) {
+            sxy[z][0][ox] = sx[z][0][ox];
+            sxy[z][1][ox] = sx[z][0][ox] + sx[z][1][ox];
+            sxy[z][2][ox] = sx[z][1][ox];
+        }
+    const T* ph = phi + (p[0] - 1) + (long)m0 * ((p[1] - 1) + (long)m1 * (p[2] - 1));
+    T acc = 0;
+    T centre = 0;
+#pragma unroll
+    for (int oz = 0; oz < 3; ++oz)
+#pragma unroll
+        for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+            for (int ox = 0; ox < 3; ++ox) {
+                const T S = oz == 0 ? sxy[0][oy][ox]
+                                    : (oz == 2 ? sxy[1][oy][ox] : sxy[0][oy][ox] + sxy[1][oy][ox]);
+                const int mask = (ox != 1 ? 1 : 0) | (oy != 1 ? 2 : 0) | (oz != 1 ? 4 : 0);
+                if (mask == 0) {
+                    centre = S;
+                } else {
+                    acc = fma(L.kw[mask] * S, ph[ox + (long)m0 * (oy + (long)m1 * oz)], acc);
+                }
+            }
+    diag = -L.kw[0] * centre;
+    off = acc;
+}
+
+template <typename T>
+__global__ void k_hg_gs3(hg::Geo G, hg::LevT<T> L, int colour, T* phi, const T* f, long N) {
+    HG_LOOP(N) {
+        int p[3];
+        hg::colour_node(G, L, colour, idx, p);
+        if (interior3(L, p)) {
+            T dg, off;
+            node_op_dense3(L, p, phi, dg, off);
+            const long i = hg::nix(L, p[0], p[1], p[2]);
+            phi[i] = (f[i] + off) / dg;
+        } else {
+            hg::gs_node(G, L, idx, colour, phi, f);
+        }
+    }
+}
+template <typename T>
+__global__ void k_hg_defect3(hg::Geo G, hg::LevT<T> L, const T* phi, const T* f, T* r, long N) {
+    HG_LOOP(N) {
+        int p[3];
+        hg::node_coords(L, idx, p);
+        if (interior3(L, p)) {
+            T dg, off;
+            node_op_dense3(L, p, phi, dg, off);
+            r[idx] = f[idx] - (dg * phi[idx] - off);
+        } else {
+            hg::defect_node(G, L, idx, phi, f, r);
+        }
+    }
+}
+
+// ---- exact coarsest-level solve --------------------------------------------------------------
+constexpr int kExactMax = 128;   // unknown nodes of a coarsest level solved by its dense inverse
+constexpr int kExactThreads = 256;
+
+// One block: the operator of the coarsest level (FP64, rows by node_row) on its M unknown
+// nodes, plus sigma 1 1^T for the singular problem (sigma = mean diagonal / M: B^-1 f = A^+ f
+// for a mean-free f), inverted in place by Gauss-Jordan elimination without pivoting (B is
+// definite).  A: M x M, row-major.
+__global__ void __launch_bounds__(kExactThreads)
+k_hg_bottom_inverse(hg::Geo G, hg::Lev L, int M, const int* __restrict__ node,
+                    const int* __restrict__ map, int singular, double* __restrict__ A) {
+    __shared__ double col[kExactMax];
+    __shared__ double piv;
+    const int t = threadIdx.x;
+    for (int e = t; e < M * M; e += kExactThreads) A[e] = 0.0;
+    __syncthreads();
+    for (int u = t; u < M; u += kExactThreads) {
+        int p[3];
+        hg::node_coords(L, node[u], p);
+        double* row = A + (long)u * M;
+        hg::node_row(G, L, p, [&](long m, double w) {
+            const int v = map[m];
+            if (v >= 0) row[v] += w;
+        });
+    }
+    __syncthreads();
+    if (singular) {
+        if (t == 0) {
+            double s = 0.0;
+            for (int u = 0; u < M; ++u) s += A[(long)u * M + u];
+            piv = s / M / M;
+        }
+        __syncthreads();
+        const double sg = piv;
+        for (int e = t; e < M * M; e += kExactThreads) A[e] += sg;
+        __syncthreads();
+    }
+    for (int k = 0; k < M; ++k) {
+        if (t == 0) {
+            piv = 1.0 / A[(long)k * M + k];
+            A[(long)k * M + k] = 1.0;
+        }
+        __syncthreads();
+        const double ip = piv;
+        for (int j = t; j < M; j += kExactThreads) A[(long)k * M + j] *= ip;
+        for (int i = t; i < M; i += kExactThreads) {
+            if (i == k) continue;
+            col[i] = A[(long)i * M + k];
+            A[(long)i * M + k] = 0.0;
+        }
+        __syncthreads();
+        for (int e = t; e < M * M; e += kExactThreads) {
+            const int i = e / M, j = e - i * M;
+            if (i != k) A[e] -= col[i] * A[(long)k * M + j];
+        }
+        __syncthreads();
+    }
+}
+
+// phi = B^-1 f on the unknown nodes of the coarsest level (FP64 arithmetic; phi elsewhere
+// untouched).
+template <typename T>
+__global__ void __launch_bounds__(kExactThreads)
+k_hg_bottom_exact(int M, const int* __restrict__ node, const double* __restrict__ Binv,
+                  const T* __restrict__ f, T* __restrict__ phi) {
+    __shared__ double fs[kExactMax];
+    for (int v = threadIdx.x; v < M; v += kExactThreads) fs[v] = (double)f[node[v]];
+    __syncthreads();
+    for (int u = threadIdx.x; u < M; u += kExactThreads) {
+        const double* row = Binv + (long)u * M;
+        double x = 0.0;
+        for (int v = 0; v < M; ++v) x = fma(row[v], fs[v], x);
+        phi[node[u]] = (T)x;
+    }
+}
+
 // nu colour-ordered Gauss-Seidel sweeps of the coarsest level in one block.  An odd periodic
 // extent couples nodes of one colour across the wrap: then one thread sweeps in order.
 template <typename T>
@@ -222,6 +395,13 @@ struct HgState {
         long nn = 0, nc = 0;
     };
     std::vector<Level> L;
+    // exact solve of the coarsest level (at most kExactMax unknown nodes): its unknown nodes
+    // (storage indices), node -> unknown number (-1: not an unknown), and the dense inverse of
+    // its operator (B = A + sigma 1 1^T when singular), rebuilt with the coefficients each call
+    int bM = 0;
+    int* bnode = nullptr;
+    int* bmap = nullptr;
+    double* binv = nullptr;
     double* part = nullptr;
     double* out = nullptr;
     double* h_out = nullptr;
@@ -313,6 +493,32 @@ int hg_ensure(mac_ctx* c) {
             h[d] *= 2;
         }
     }
+    // the coarsest level's unknown nodes, for its exact solve when there are few
+    if (!rc && !H->L.empty()) {
+        const hg::Lev& B = H->L.back().lev;
+        const long nnb = hg::nnodes(B);
+        std::vector<int> map((size_t)nnb, -1), nodes;
+        for (long idx = 0; idx < nnb; ++idx) {
+            int p[3];
+            hg::node_coords(B, idx, p);
+            if (!hg::is_unknown(G, B, p)) continue;
+            map[(size_t)idx] = (int)nodes.size();
+            nodes.push_back((int)idx);
+        }
+        if (!nodes.empty() && (int)nodes.size() <= kExactMax) {
+            H->bM = (int)nodes.size();
+            rc = hg_alloc(H, &H->bnode, nodes.size());
+            if (!rc) rc = hg_alloc(H, &H->bmap, map.size());
+            if (!rc) rc = hg_alloc(H, &H->binv, nodes.size() * nodes.size());
+            if (!rc && (cudaMemcpy(H->bnode, nodes.data(), nodes.size() * sizeof(int),
+                                   cudaMemcpyHostToDevice) != cudaSuccess ||
+                        cudaMemcpy(H->bmap, map.data(), map.size() * sizeof(int),
+                                   cudaMemcpyHostToDevice) != cudaSuccess)) {
+                cudaGetLastError();
+                rc = MAC_ERR_CUDA;
+            }
+        }
+    }
     if (!rc) rc = hg_alloc(H, &H->part, (size_t)4 * kReduceBlocks);
     if (!rc) rc = hg_alloc(H, &H->out, 8);
     if (!rc) rc = hg_alloc(H, &H->flag, 1);
@@ -359,20 +565,32 @@ struct HgMg {
             err = MAC_ERR_CUDA;
         }
     }
+    bool dense3() const { return geo.dense && geo.dm == 3; }
     void defect(int l, const T* phi, const T* f, T* r) {
-        k_hg_defect<T><<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), phi, f, r, nn(l));
+        if (dense3())
+            k_hg_defect3<T><<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), phi, f, r, nn(l));
+        else
+            k_hg_defect<T><<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), phi, f, r, nn(l));
         launched();
     }
     void gs(int l, T* phi, const T* f, int nu) {
         for (int s = 0; s < nu; ++s)
             for (int colour = 0; colour < (1 << geo.dm); ++colour) {
                 const long m = hg::colour_count(geo, lev(l), colour);
-                k_hg_gs<T><<<blocks(m), kThreads, 0, c->stream>>>(geo, lev(l), colour, phi, f, m);
+                if (dense3())
+                    k_hg_gs3<T><<<blocks(m), kThreads, 0, c->stream>>>(geo, lev(l), colour, phi, f, m);
+                else
+                    k_hg_gs<T><<<blocks(m), kThreads, 0, c->stream>>>(geo, lev(l), colour, phi, f, m);
                 launched();
             }
     }
     void bottom_gs(int l, T* phi, const T* f, int nu) {
-        k_hg_bottom<T><<<1, 1024, 0, c->stream>>>(geo, lev(l), phi, f, nu, nn(l));
+        if (H->binv && l == (int)H->L.size() - 1) {
+            // the exact solve replaces the sweeps (the inverse is built with the coefficients)
+            k_hg_bottom_exact<T><<<1, kExactThreads, 0, c->stream>>>(H->bM, H->bnode, H->binv, f, phi);
+        } else {
+            k_hg_bottom<T><<<1, 1024, 0, c->stream>>>(geo, lev(l), phi, f, nu, nn(l));
+        }
         launched();
     }
     void restrict_to(int lc, const T* rF, T* fK) {
@@ -440,6 +658,11 @@ struct HgExec : HgMg<double> {
         for (size_t l = 1; l < H->L.size(); ++l) {
             k_hg_coarsen<<<blocks(nc((int)l)), kThreads, 0, c->stream>>>(geo, lev((int)l - 1), lev((int)l),
                                                                        H->L[l].sig, nc((int)l));
+            launched();
+        }
+        if (H->binv) {
+            k_hg_bottom_inverse<<<1, kExactThreads, 0, c->stream>>>(
+                geo, lev((int)H->L.size() - 1), H->bM, H->bnode, H->bmap, singular ? 1 : 0, H->binv);
             launched();
         }
         return err;

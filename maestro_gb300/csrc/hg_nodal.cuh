@@ -34,6 +34,11 @@
 #else
 #define HG_HD
 #endif
+#if defined(__CUDA_ARCH__)
+#define HG_UNROLL _Pragma("unroll")
+#else
+#define HG_UNROLL
+#endif
 
 namespace mac {
 namespace hg {
@@ -135,7 +140,9 @@ HG_HD inline int cell_wrap(const Geo& G, const LevT<T>& L, int d, int c) {
 // An unknown: not a periodic image, not on an outflow face.
 template <typename T>
 HG_HD inline bool is_unknown(const Geo& G, const LevT<T>& L, const int p[3]) {
-    for (int d = 0; d < G.dm; ++d) {
+    HG_UNROLL
+    for (int d = 0; d < 3; ++d) {   // (a static bound keeps p[] in registers)
+        if (d >= G.dm) break;
         if (G.per[d]) {
             if (p[d] == L.n[d]) return false;
         } else if ((p[d] == 0 && G.dlo[d]) || (p[d] == L.n[d] && G.dhi[d])) {
@@ -145,17 +152,20 @@ HG_HD inline bool is_unknown(const Geo& G, const LevT<T>& L, const int p[3]) {
     return true;
 }
 
-// (L phi)_p = diag * phi_p - off.
-template <typename T>
-HG_HD inline void node_op(const Geo& G, const LevT<T>& L, const int p[3], const T* phi, T& diag,
-                          T& off) {
-    const int dm = G.dm;
+// (L phi)_p = diag * phi_p - off; DM = G.dm as a compile-time constant, so the corner loops
+// unroll and the weight table is indexed statically.
+template <int DM, typename T>
+HG_HD inline void node_op_dm(const Geo& G, const LevT<T>& L, const int p[3], const T* phi,
+                             T& diag, T& off) {
+    constexpr int dm = DM;
     T dK = 0, oK = 0;
     if (G.dense) {
         const long pi = nix(L, p[0], p[1], p[2]);
+        HG_UNROLL
         for (int a = 0; a < (1 << dm); ++a) {   // a: the corner of cell c that p is
             int c[3] = {0, 0, 0};
             bool out = false;
+            HG_UNROLL
             for (int d = 0; d < dm; ++d) {
                 const int cw = cell_wrap(G, L, d, p[d] - ((a >> d) & 1));
                 if (cw < 0) out = true;
@@ -164,9 +174,11 @@ HG_HD inline void node_op(const Geo& G, const LevT<T>& L, const int p[3], const 
             if (out) continue;
             const T s = L.sig[cix(L, c[0], c[1], c[2])];
             T acc = 0;
+            HG_UNROLL
             for (int b = 0; b < (1 << dm); ++b) {
                 if (b == a) continue;
                 int m[3] = {0, 0, 0};
+                HG_UNROLL
                 for (int d = 0; d < dm; ++d) m[d] = node_wrap(G, L, d, c[d] + ((b >> d) & 1));
                 const long mi = nix(L, m[0], m[1], m[2]);
                 if (mi == pi)   // a periodic wrap of extent 1 folds a corner onto p
@@ -179,6 +191,76 @@ HG_HD inline void node_op(const Geo& G, const LevT<T>& L, const int p[3], const 
         }
         diag = -dK;
         off = -oK;
+    } else {
+        HG_UNROLL
+        for (int d = 0; d < dm; ++d)
+            HG_UNROLL
+            for (int sd = -1; sd <= 1; sd += 2) {
+                const int q = node_wrap(G, L, d, p[d] + sd);
+                if (q < 0) continue;
+                T sum = 0;
+                int cnt = 0;
+                HG_UNROLL
+                for (int a = 0; a < (1 << dm); ++a) {
+                    if ((a >> d) & 1) continue;
+                    int c[3] = {0, 0, 0};
+                    bool out = false;
+                    HG_UNROLL
+                    for (int e = 0; e < dm; ++e) {
+                        const int want = e == d ? (sd < 0 ? p[d] - 1 : p[d]) : p[e] - ((a >> e) & 1);
+                        const int cw = cell_wrap(G, L, e, want);
+                        if (cw < 0) out = true;
+                        c[e] = cw;
+                    }
+                    ++cnt;
+                    if (!out) sum += L.sig[cix(L, c[0], c[1], c[2])];
+                }
+                const T se = sum / (T)cnt / (T)(L.h[d] * L.h[d]);
+                int qq[3] = {p[0], p[1], p[2]};
+                qq[d] = q;
+                dK -= se;
+                oK -= se * phi[nix(L, qq[0], qq[1], qq[2])];
+            }
+        diag = dK;
+        off = oK;
+    }
+}
+
+template <typename T>
+HG_HD inline void node_op(const Geo& G, const LevT<T>& L, const int p[3], const T* phi, T& diag,
+                          T& off) {
+    if (G.dm == 3)
+        node_op_dm<3>(G, L, p, phi, diag, off);
+    else
+        node_op_dm<2>(G, L, p, phi, diag, off);
+}
+
+// Row p of the operator as weights on nodes: add(m, w) for every term w * phi_m of (L phi)_p,
+// with m the node storage index after the periodic fold (the diagonal term has m = the index of
+// p); the same terms node_op sums, so sum_m w_m phi_m = diag * phi_p - off.
+template <typename T, class Add>
+HG_HD inline void node_row(const Geo& G, const LevT<T>& L, const int p[3], Add add) {
+    const int dm = G.dm;
+    const long pi = nix(L, p[0], p[1], p[2]);
+    if (G.dense) {
+        for (int a = 0; a < (1 << dm); ++a) {
+            int c[3] = {0, 0, 0};
+            bool out = false;
+            for (int d = 0; d < dm; ++d) {
+                const int cw = cell_wrap(G, L, d, p[d] - ((a >> d) & 1));
+                if (cw < 0) out = true;
+                c[d] = cw;
+            }
+            if (out) continue;
+            const T s = L.sig[cix(L, c[0], c[1], c[2])];
+            for (int b = 0; b < (1 << dm); ++b) {
+                if (b == a) continue;
+                int m[3] = {0, 0, 0};
+                for (int d = 0; d < dm; ++d) m[d] = node_wrap(G, L, d, c[d] + ((b >> d) & 1));
+                add(nix(L, m[0], m[1], m[2]), -(s * L.kw[a ^ b]));
+            }
+            add(pi, -(s * L.kw[0]));
+        }
     } else {
         for (int d = 0; d < dm; ++d)
             for (int sd = -1; sd <= 1; sd += 2) {
@@ -202,11 +284,9 @@ HG_HD inline void node_op(const Geo& G, const LevT<T>& L, const int p[3], const 
                 const T se = sum / (T)cnt / (T)(L.h[d] * L.h[d]);
                 int qq[3] = {p[0], p[1], p[2]};
                 qq[d] = q;
-                dK -= se;
-                oK -= se * phi[nix(L, qq[0], qq[1], qq[2])];
+                add(pi, -se);
+                add(nix(L, qq[0], qq[1], qq[2]), se);
             }
-        diag = dK;
-        off = oK;
     }
 }
 
@@ -236,7 +316,9 @@ template <typename T>
 HG_HD inline void colour_node(const Geo& G, const LevT<T>& L, int colour, long k, int p[3]) {
     p[0] = p[1] = p[2] = 0;
     unsigned u = (unsigned)k;
-    for (int d = 0; d < G.dm; ++d) {
+    HG_UNROLL
+    for (int d = 0; d < 3; ++d) {   // (a static bound keeps p[] in registers)
+        if (d >= G.dm) break;
         const int b = (colour >> d) & 1;
         const unsigned m = (unsigned)((L.nn[d] - b + 1) / 2);
         const unsigned qd = u / m;
@@ -271,14 +353,21 @@ HG_HD inline void restrict_node(const Geo& G, const LevT<T>& F, const LevT<T>& K
     }
     const int dm = G.dm;
     T s = 0;
-    for (int a2 = -(dm > 2); a2 <= (dm > 2); ++a2)
-        for (int a1 = -(dm > 1); a1 <= (dm > 1); ++a1)
+    // (static bounds, the same terms in the same order: the small arrays stay in registers)
+    HG_UNROLL
+    for (int a2 = -1; a2 <= 1; ++a2)
+        HG_UNROLL
+        for (int a1 = -1; a1 <= 1; ++a1)
+            HG_UNROLL
             for (int a0 = -1; a0 <= 1; ++a0) {
+                if ((dm < 3 && a2 != 0) || (dm < 2 && a1 != 0)) continue;
                 const int a[3] = {a0, a1, a2};
                 int q[3] = {0, 0, 0};
                 T w = 1;
                 bool out = false;
-                for (int d = 0; d < dm; ++d) {
+                HG_UNROLL
+                for (int d = 0; d < 3; ++d) {
+                    if (d >= dm) break;
                     if (a[d]) w *= (T)0.5;
                     const int qq = node_wrap(G, F, d, 2 * P[d] + a[d]);
                     if (qq < 0) out = true;
@@ -298,18 +387,26 @@ HG_HD inline void prolong_node(const Geo& G, const LevT<T>& K, const LevT<T>& F,
     if (!is_unknown(G, F, p)) return;
     const int dm = G.dm;
     int lo[3] = {0, 0, 0}, odd[3] = {0, 0, 0};
-    for (int d = 0; d < dm; ++d) {
+    HG_UNROLL
+    for (int d = 0; d < 3; ++d) {   // (static bounds keep the small arrays in registers)
+        if (d >= dm) break;
         lo[d] = p[d] >> 1;
         odd[d] = p[d] & 1;
     }
     T s = 0;
-    for (int a2 = 0; a2 <= odd[2]; ++a2)
-        for (int a1 = 0; a1 <= odd[1]; ++a1)
-            for (int a0 = 0; a0 <= odd[0]; ++a0) {
+    HG_UNROLL
+    for (int a2 = 0; a2 <= 1; ++a2)
+        HG_UNROLL
+        for (int a1 = 0; a1 <= 1; ++a1)
+            HG_UNROLL
+            for (int a0 = 0; a0 <= 1; ++a0) {
+                if (a2 > odd[2] || a1 > odd[1] || a0 > odd[0]) continue;
                 const int a[3] = {a0, a1, a2};
                 int q[3] = {0, 0, 0};
                 T w = 1;
-                for (int d = 0; d < dm; ++d) {
+                HG_UNROLL
+                for (int d = 0; d < 3; ++d) {
+                    if (d >= dm) break;
                     if (odd[d]) w *= (T)0.5;
                     q[d] = node_wrap(G, K, d, lo[d] + a[d]);
                 }

@@ -55,7 +55,18 @@ k_gsrb_otf(Dims d, OtfParams P, int colour, float* __restrict__ es, const float*
 // (P.wait_ns of %globaltimer, mac_opts.wait_limit_s, one second by default); on expiry the block
 // records the failure in P.err, waits (bounded by kDrainNs) for the copies it issued and leaves.  4 ring stages at 256^3 (ty = 8): 72 KB of
 // shared memory and 80 registers a thread, 3 blocks per SM.
-constexpr int kStages = 4;          // planes in the shared-memory ring
+// Tunables of the staged half-sweep (compile-time; the defaults are the measured best at 256^3):
+// cells of a tile, ring stages, and the resident blocks per SM its register budget is set for.
+#ifndef MAC_OTF_TILE_CELLS
+#define MAC_OTF_TILE_CELLS 1024
+#endif
+#ifndef MAC_OTF_STAGES
+#define MAC_OTF_STAGES 4
+#endif
+#ifndef MAC_OTF_MIN_BLOCKS
+#define MAC_OTF_MIN_BLOCKS 3
+#endif
+constexpr int kStages = MAC_OTF_STAGES;   // planes in the shared-memory ring
 constexpr int kRStages = 3;         // the same for the staged restriction (one more array a plane)
 constexpr int kCellsPerThread = 4;  // consecutive colour-half columns (one float4) per thread
 // waits for copies a block has already seen arrive or that are draining after a failed wait
@@ -200,7 +211,7 @@ __device__ __forceinline__ void update_group(float ex, float rx, const FV<V>& Ec
 // DEF (with SOR): also write each updated cell's defect f - L e after its update to dout
 // (indexed like es): after the over-relaxed half-sweep it is acc - diag e_new, no longer zero.
 template <bool DIR, bool SOR, bool DEF = false>
-__global__ void __launch_bounds__(256, 3)
+__global__ void __launch_bounds__(MAC_OTF_TILE_CELLS / kCellsPerThread, MAC_OTF_MIN_BLOCKS)
 k_gsrb_otf_staged(Dims d, OtfParams P, int colour, float* __restrict__ es,
                   const float* __restrict__ eo, const float* __restrict__ rs,
                   const float* __restrict__ rhos, const float* __restrict__ rhoo,
@@ -964,7 +975,7 @@ void plan_otf_tile(const Dims& d, int dm, int sms, OtfParams& P) {
     P.rty = P.rzc = P.rnz = P.rsmem = 0;
     if (dm != 3 || !d.split || d.hn0 % 4 || d.hn0 > 1024 || d.n2 < 2) return;
     int ty = 1;
-    while (2 * ty * d.hn0 <= 1024 && d.n1 % (2 * ty) == 0) ty *= 2;
+    while (2 * ty * d.hn0 <= MAC_OTF_TILE_CELLS && d.n1 % (2 * ty) == 0) ty *= 2;
     const int nt = ty * d.hn0 / kCellsPerThread;
     if (nt < 32 || nt % 32) return;
     const int stage = (4 * ty + 4) * d.hn0;

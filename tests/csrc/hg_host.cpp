@@ -277,4 +277,48 @@ void hgh_fabs(int dm, const int* n, const int* per, int nboxes, const int* boxes
     }
 }
 
+// node_row against node_op on one level: random sigma and phi, every node; returns the largest
+// |sum_m w_m phi_m - (diag phi_p - off)| relative to max |diag phi_p - off| (0 when they agree).
+double hgh_row_check(int dm, const int* n, const double* dx, const int* per, const int* dlo,
+                     const int* dhi, int dense, unsigned seed) {
+    mac::hg::Geo G{};
+    G.dm = dm;
+    G.dense = dense;
+    for (int d = 0; d < 3; ++d) {
+        G.per[d] = d < dm ? per[d] : 0;
+        G.dlo[d] = d < dm ? dlo[d] : 0;
+        G.dhi[d] = d < dm ? dhi[d] : 0;
+    }
+    mac::hg::Lev L{};
+    for (int d = 0; d < 3; ++d) {
+        L.n[d] = d < dm ? n[d] : 1;
+        L.nn[d] = d < dm ? n[d] + 1 : 1;
+        L.h[d] = d < dm ? dx[d] : 1.0;
+    }
+    mac::hg::set_dense_weights(dm, L);
+    const long nc = mac::hg::ncells(L), nn = mac::hg::nnodes(L);
+    std::vector<double> sig(nc), phi(nn);
+    unsigned st = seed ? seed : 1u;
+    auto rnd = [&]() {
+        st = st * 1664525u + 1013904223u;
+        return (double)(st >> 8) / 16777216.0;
+    };
+    for (auto& v : sig) v = 0.5 + rnd();
+    for (auto& v : phi) v = rnd() - 0.5;
+    L.sig = sig.data();
+    double worst = 0.0, scale = 0.0;
+    for (long idx = 0; idx < nn; ++idx) {
+        int p[3];
+        mac::hg::node_coords(L, idx, p);
+        double dg, off;
+        mac::hg::node_op(G, L, p, phi.data(), dg, off);
+        const double ref = dg * phi[idx] - off;
+        double sum = 0.0;
+        mac::hg::node_row(G, L, p, [&](long m, double w) { sum += w * phi[m]; });
+        worst = std::max(worst, std::fabs(sum - ref));
+        scale = std::max(scale, std::fabs(ref));
+    }
+    return scale > 0.0 ? worst / scale : worst;
+}
+
 }  // extern "C"
