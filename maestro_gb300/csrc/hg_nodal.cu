@@ -133,19 +133,91 @@ __device__ __forceinline__ void node_op_dense3(const hg::LevT<T>& L, const int p
     off = acc;
 }
 
+// The same stencil for a node next to (or on) a domain face: cell and node indices folded through
+// the periodic wrap, a missing cell (outside a non-periodic face) contributing sigma = 0 and its
+// nodes read at a clamped index with weight 0, a neighbour that folds onto p itself (a periodic
+// extent of 1) moved to the diagonal.  Branch-free (selects instead of branches), so all 35
+// loads issue together; the terms are node_op's, grouped by neighbour.
+template <typename T>
+__device__ __forceinline__ void node_op_dense3_face(const hg::Geo& G, const hg::LevT<T>& L,
+                                                    const int p[3], const T* __restrict__ phi,
+                                                    T& diag, T& off) {
+    int cw[3][2], nw[3][3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+#pragma unroll
+        for (int x = 0; x < 2; ++x) cw[d][x] = hg::cell_wrap(G, L, d, p[d] - 1 + x);
+#pragma unroll
+        for (int o = 0; o < 3; ++o) nw[d][o] = hg::node_wrap(G, L, d, p[d] - 1 + o);
+    }
+    T s[2][2][2];
+#pragma unroll
+    for (int z = 0; z < 2; ++z)
+#pragma unroll
+        for (int y = 0; y < 2; ++y)
+#pragma unroll
+            for (int x = 0; x < 2; ++x) {
+                const bool ok = cw[0][x] >= 0 && cw[1][y] >= 0 && cw[2][z] >= 0;
+                const T v = L.sig[hg::cix(L, max(cw[0][x], 0), max(cw[1][y], 0), max(cw[2][z], 0))];
+                s[z][y][x] = ok ? v : T(0);
+            }
+    T sx[2][2][3];
+#pragma unroll
+    for (int z = 0; z < 2; ++z)
+#pragma unroll
+        for (int y = 0; y < 2; ++y) {
+            sx[z][y][0] = s[z][y][0];
+            sx[z][y][1] = s[z][y][0] + s[z][y][1];
+            sx[z][y][2] = s[z][y][1];
+        }
+    T sxy[2][3][3];
+#pragma unroll
+    for (int z = 0; z < 2; ++z)
+#pragma unroll
+        for (int ox = 0; ox < 3; ++ox) {
+            sxy[z][0][ox] = sx[z][0][ox];
+            sxy[z][1][ox] = sx[z][0][ox] + sx[z][1][ox];
+            sxy[z][2][ox] = sx[z][1][ox];
+        }
+    const long pi = hg::nix(L, p[0], p[1], p[2]);
+    T acc = 0, dsum = 0, centre = 0;
+#pragma unroll
+    for (int oz = 0; oz < 3; ++oz)
+#pragma unroll
+        for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+            for (int ox = 0; ox < 3; ++ox) {
+                const T S = oz == 0 ? sxy[0][oy][ox]
+                                    : (oz == 2 ? sxy[1][oy][ox] : sxy[0][oy][ox] + sxy[1][oy][ox]);
+                const int mask = (ox != 1 ? 1 : 0) | (oy != 1 ? 2 : 0) | (oz != 1 ? 4 : 0);
+                if (mask == 0) {
+                    centre = S;
+                } else {
+                    const long m = hg::nix(L, max(nw[0][ox], 0), max(nw[1][oy], 0), max(nw[2][oz], 0));
+                    const T w = L.kw[mask] * S;
+                    const T v = phi[m];
+                    const bool self = m == pi;
+                    dsum += self ? w : T(0);
+                    acc = fma(self ? T(0) : w, v, acc);
+                }
+            }
+    diag = -(L.kw[0] * centre + dsum);
+    off = acc;
+}
+
 template <typename T>
 __global__ void k_hg_gs3(hg::Geo G, hg::LevT<T> L, int colour, T* phi, const T* f, long N) {
     HG_LOOP(N) {
         int p[3];
         hg::colour_node(G, L, colour, idx, p);
-        if (interior3(L, p)) {
-            T dg, off;
+        if (!hg::is_unknown(G, L, p)) continue;
+        T dg, off;
+        if (interior3(L, p))
             node_op_dense3(L, p, phi, dg, off);
-            const long i = hg::nix(L, p[0], p[1], p[2]);
-            phi[i] = (f[i] + off) / dg;
-        } else {
-            hg::gs_node(G, L, idx, colour, phi, f);
-        }
+        else
+            node_op_dense3_face(G, L, p, phi, dg, off);
+        const long i = hg::nix(L, p[0], p[1], p[2]);
+        phi[i] = (f[i] + off) / dg;
     }
 }
 template <typename T>
@@ -153,13 +225,16 @@ __global__ void k_hg_defect3(hg::Geo G, hg::LevT<T> L, const T* phi, const T* f,
     HG_LOOP(N) {
         int p[3];
         hg::node_coords(L, idx, p);
-        if (interior3(L, p)) {
-            T dg, off;
-            node_op_dense3(L, p, phi, dg, off);
-            r[idx] = f[idx] - (dg * phi[idx] - off);
-        } else {
-            hg::defect_node(G, L, idx, phi, f, r);
+        if (!hg::is_unknown(G, L, p)) {
+            r[idx] = 0;
+            continue;
         }
+        T dg, off;
+        if (interior3(L, p))
+            node_op_dense3(L, p, phi, dg, off);
+        else
+            node_op_dense3_face(G, L, p, phi, dg, off);
+        r[idx] = f[idx] - (dg * phi[idx] - off);
     }
 }
 
