@@ -722,7 +722,7 @@ int amr_configure(mac_ctx* c, int nlev, const int* nboxes, const int* box_lo, co
             S.lev.n[d] = geom[l].n[d];
             S.lev.lo[d] = geom[l].lo[d];
             S.lev.ext[d] = geom[l].ext[d];
-            S.lev.h[d] = d < c->dm ? c->dx[d] / (double)(1 << l) : c->dx[d];
+            amr::set_spacing(S.lev, d, d < c->dm ? c->dx[d] / (double)(1 << l) : c->dx[d]);
         }
         const long N = amr::ncells(S.lev);
         S.ncell = N;
@@ -763,7 +763,7 @@ int amr_ensure_single(mac_ctx* c) {
             S.lev32.n[d] = S.lev.n[d];
             S.lev32.lo[d] = S.lev.lo[d];
             S.lev32.ext[d] = S.lev.ext[d];
-            S.lev32.h[d] = S.lev.h[d];
+            amr::set_spacing(S.lev32, d, S.lev.h[d]);
             S.lev32.b[d] = S.beta32[d];
         }
         S.lev32.mask = S.lev.mask;

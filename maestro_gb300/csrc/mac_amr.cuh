@@ -34,6 +34,11 @@
 #else
 #define AMR_HD
 #endif
+#if defined(__CUDA_ARCH__)
+#define AMR_UNROLL _Pragma("unroll")
+#else
+#define AMR_UNROLL
+#endif
 
 namespace mac {
 namespace amr {
@@ -56,10 +61,19 @@ struct LevT {
     int n[3];                  // level-domain cells (1 along inactive directions)
     int lo[3], ext[3];         // the array box: cells lo .. lo + ext - 1 of the level domain
     double h[3];
+    double ih[3], ih2[3];      // 1 / h and 1 / h^2 (set with h by set_spacing: no division in
+                               // the cell functions, FP64 division being slow on the GPU)
     const unsigned char* mask; // kIn / kCov per cell of the box
     const T* b[3];             // face coefficients over the box (ext[d] + 1 faces along d)
 };
 using Lev = LevT<double>;
+
+template <typename T>
+inline void set_spacing(LevT<T>& L, int d, double h) {
+    L.h[d] = h;
+    L.ih[d] = 1.0 / h;
+    L.ih2[d] = 1.0 / (h * h);
+}
 
 // Array box of a level: the bounding box [rlo, rhi] of its cells grown by one cell and clipped
 // to the domain; a periodic direction whose grown box would cross the domain face takes the
@@ -103,6 +117,7 @@ template <typename T>
 AMR_HD inline long ncells(const LevT<T>& L) { return (long)L.ext[0] * L.ext[1] * L.ext[2]; }
 template <typename T>
 AMR_HD inline bool inside(const LevT<T>& L, const int c[3]) {
+    AMR_UNROLL
     for (int d = 0; d < 3; ++d)
         if (c[d] < L.lo[d] || c[d] >= L.lo[d] + L.ext[d]) return false;
     return true;
@@ -139,10 +154,13 @@ template <typename T>
 AMR_HD inline T coarse_at_ghost(const Geo& G, const LevT<T>& C, const int q[3], int d,
                                 const T* cu) {
     int c[3];
+    AMR_UNROLL
     for (int e = 0; e < 3; ++e) c[e] = e < G.dm ? q[e] >> 1 : q[e];
     const T v0 = cu[cix(C, c[0], c[1], c[2])];
     T v = v0;
-    for (int t = 0; t < G.dm; ++t) {
+    AMR_UNROLL
+    for (int t = 0; t < 3; ++t) {
+        if (t >= G.dm) break;
         if (t == d) continue;
         const T del = (q[t] & 1) ? (T)0.25 : (T)-0.25;
         int m[3] = {c[0], c[1], c[2]}, p[3] = {c[0], c[1], c[2]};
@@ -168,8 +186,11 @@ AMR_HD inline void cell_op(const Geo& G, const LevT<T>& L, const LevT<T>& C, con
                            const T* u, const T* cu, T& diag, T& off) {
     diag = 0;
     off = 0;
-    for (int d = 0; d < G.dm; ++d) {
-        const T ih2 = (T)(1.0 / (L.h[d] * L.h[d]));
+    AMR_UNROLL
+    for (int d = 0; d < 3; ++d) {   // (static bounds keep the small arrays in registers)
+        if (d >= G.dm) break;
+        const T ih2 = (T)L.ih2[d];
+        AMR_UNROLL
         for (int s = -1; s <= 1; s += 2) {
             const T w = face_b(L, d, c, s) * ih2;
             const int qd = wrap(G, L, d, c[d] + s);
@@ -255,7 +276,10 @@ AMR_HD inline void reflux_cell(const Geo& G, const LevT<T>& F, const LevT<T>& C,
     cell_coords(C, kidx, c);
     const int ntan = 1 << (G.dm - 1);
     T acc = 0;
-    for (int d = 0; d < G.dm; ++d) {
+    AMR_UNROLL
+    for (int d = 0; d < 3; ++d) {
+        if (d >= G.dm) break;
+        AMR_UNROLL
         for (int s = -1; s <= 1; s += 2) {
             const int w = wrap(G, C, d, c[d] + s);
             if (w < 0) continue;
@@ -263,12 +287,16 @@ AMR_HD inline void reflux_cell(const Geo& G, const LevT<T>& F, const LevT<T>& C,
             Q[d] = w;
             const long qc = cix(C, Q[0], Q[1], Q[2]);
             if (!(C.mask[qc] & kCov)) continue;
-            const T Tc = uc ? face_b(C, d, c, s) * (uc[kidx] - uc[qc]) / (T)C.h[d] : (T)0;
+            const T Tc = uc ? face_b(C, d, c, s) * (uc[kidx] - uc[qc]) * (T)C.ih[d] : (T)0;
             T Tf = 0;
-            for (int a = 0; a < (1 << G.dm); ++a) {
+            AMR_UNROLL
+            for (int a = 0; a < 8; ++a) {
+                if (a >= (1 << G.dm)) break;
                 if ((a >> d) & 1) continue;
                 int fc[3] = {0, 0, 0}, gq[3] = {0, 0, 0};
-                for (int e = 0; e < G.dm; ++e) {
+                AMR_UNROLL
+                for (int e = 0; e < 3; ++e) {
+                    if (e >= G.dm) break;
                     if (e == d) {
                         fc[e] = s > 0 ? 2 * Q[e] : 2 * Q[e] + 1;
                         gq[e] = s > 0 ? 2 * c[e] + 1 : 2 * c[e];
@@ -278,9 +306,9 @@ AMR_HD inline void reflux_cell(const Geo& G, const LevT<T>& F, const LevT<T>& C,
                 }
                 const T ufv = uf[cix(F, fc[0], fc[1], fc[2])];
                 const T g = ufv / (T)3 + (uc ? (T)(2.0 / 3.0) * coarse_at_ghost(G, C, gq, d, uc) : (T)0);
-                Tf += face_b(F, d, fc, -s) * (g - ufv) / (T)F.h[d];
+                Tf += face_b(F, d, fc, -s) * (g - ufv) * (T)F.ih[d];
             }
-            acc += (Tc - Tf / (T)ntan) / (T)C.h[d];
+            acc += (Tc - Tf / (T)ntan) * (T)C.ih[d];
         }
     }
     res[kidx] += acc;

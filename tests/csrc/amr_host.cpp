@@ -217,7 +217,7 @@ void build_levels(HostMl<T>& M, const HostExec& E0) {
             V.n[d] = geom[l].n[d];
             V.lo[d] = geom[l].lo[d];
             V.ext[d] = geom[l].ext[d];
-            V.h[d] = geom[l].h[d];
+            amr::set_spacing(V, d, geom[l].h[d]);
         }
         V.mask = E.mask[l].data();
         const long N = amr::ncells(V);
@@ -252,7 +252,7 @@ void build(HostExec& E, const orc_opts* o, int nlev, const int* nboxes, const in
         amr::Lev& V = E.L[l];
         for (int d = 0; d < 3; ++d) {
             V.n[d] = d < o->dm ? (o->n[d] << l) : 1;
-            V.h[d] = d < o->dm ? o->dx[d] / (double)(1 << l) : o->dx[d];
+            amr::set_spacing(V, d, d < o->dm ? o->dx[d] / (double)(1 << l) : o->dx[d]);
             V.lo[d] = 0;
             V.ext[d] = V.n[d];
         }
