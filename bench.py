@@ -749,7 +749,7 @@ def main():
         # written (4 B) = 16 B over-relaxed / 14 B Gauss-Seidel; the last pre-smoothing sweep of
         # each V-cycle also writes the colour-1 defects (2 B); coefficients from rho in registers
         per_launch = (16 if sor else 14) * N
-        alg_total = kt_n * per_launch + (nv * 2 * N if sor else 0)
+        alg_total = kt_n * per_launch + (nv * 2 * N if sor and dopts.inner_nu1 > 0 else 0)
         kname = ("k_sweep_otf_fused (finest level, one whole red/black sweep, out of place, FP32, "
                  "coefficients from rho on the fly%s)" % (
                      ", over-relaxed omega=%.2f" % omega if sor else ""))
@@ -759,7 +759,9 @@ def main():
         # read, the own colour's f read (2 B) and e written (2 B) = 10 B; over-relaxed also reads
         # the own colour's old e (2 B) = 12 B
         per_launch = (12 if sor else 10) * N
-        alg_total = kt_n * per_launch
+        # over-relaxed: the last pre-smoothing colour-1 half-sweep of each V-cycle also writes
+        # its cells' defects (2 B per level cell) for the restriction
+        alg_total = kt_n * per_launch + (nv * 2 * N if sor and dopts.inner_nu1 > 0 else 0)
         kname = ("k_gsrb_otf_staged (finest level, one colour half-sweep, FP32, coefficients "
                  "from rho on the fly%s)" % (", over-relaxed omega=%.2f" % omega if sor else ""))
         tkey = "gsrb_otf_staged_sor_fine" if sor else "gsrb_otf_staged_fine"
