@@ -112,7 +112,9 @@ __device__ __forceinline__ void node_op_dense3(const hg::LevT<T>& L, const int p
             sxy[z][2][ox] = sx[z][1][ox];
         }
     const T* ph = phi + (p[0] - 1) + (long)m0 * ((p[1] - 1) + (long)m1 * (p[2] - 1));
-    T acc = 0;
+    // the neighbours grouped by weight class mask(o) (7 classes): sum S_o phi_o per class, then
+    // one multiplication by kw per class (26 fewer multiplications than weighting each term)
+    T am[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     T centre = 0;
 #pragma unroll
     for (int oz = 0; oz < 3; ++oz)
@@ -126,9 +128,12 @@ __device__ __forceinline__ void node_op_dense3(const hg::LevT<T>& L, const int p
                 if (mask == 0) {
                     centre = S;
                 } else {
-                    acc = fma(L.kw[mask] * S, ph[ox + (long)m0 * (oy + (long)m1 * oz)], acc);
+                    am[mask] = fma(S, ph[ox + (long)m0 * (oy + (long)m1 * oz)], am[mask]);
                 }
             }
+    T acc = 0;
+#pragma unroll
+    for (int m = 1; m < 8; ++m) acc = fma(L.kw[m], am[m], acc);
     diag = -L.kw[0] * centre;
     off = acc;
 }

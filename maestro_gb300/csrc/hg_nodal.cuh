@@ -60,6 +60,8 @@ struct LevT {
     int n[3];          // cells (1 along inactive directions)
     int nn[3];         // node storage (n + 1 along active directions)
     double h[3];
+    double ih[3];      // 1 / h (set by set_dense_weights: the one-pass cell and node functions
+                       // multiply, FP64 division being slow on the GPU)
     const T* sig;      // cell coefficients
     // dense stencil: finite-element weight of a cell between its corners a and b, which depends
     // on a ^ b only (set by set_dense_weights)
@@ -71,6 +73,7 @@ using Lev = LevT<double>;
 // M(1) = 1/6 (x_d = 1: the two corners differ along d).
 template <typename T>
 HG_HD inline void set_dense_weights(int dm, LevT<T>& L) {
+    for (int d = 0; d < 3; ++d) L.ih[d] = 1.0 / L.h[d];
     for (int x = 0; x < 8; ++x) {
         double k = 0.0;
         for (int d = 0; d < dm; ++d) {
@@ -455,10 +458,14 @@ HG_HD inline void divu_node(const Geo& G, const Lev& L, long idx, const double* 
     const int dm = G.dm;
     const long nc = ncells(L);
     double s = 0.0;
-    for (int a = 0; a < (1 << dm); ++a) {
+    HG_UNROLL
+    for (int a = 0; a < 8; ++a) {   // (static bounds keep the small arrays in registers)
+        if (a >= (1 << dm)) break;
         int c[3] = {0, 0, 0};
         bool out = false;
-        for (int d = 0; d < dm; ++d) {
+        HG_UNROLL
+        for (int d = 0; d < 3; ++d) {
+            if (d >= dm) break;
             const int cw = cell_wrap(G, L, d, p[d] - ((a >> d) & 1));
             if (cw < 0) out = true;
             c[d] = cw;
@@ -466,9 +473,13 @@ HG_HD inline void divu_node(const Geo& G, const Lev& L, long idx, const double* 
         if (out) continue;
         const long ci = cix(L, c[0], c[1], c[2]);
         const double bb = b0 ? b0[ci] : 1.0;
-        for (int d = 0; d < dm; ++d) s += (((a >> d) & 1) ? -1.0 : 1.0) * bb * u[d * nc + ci] / L.h[d];
+        HG_UNROLL
+        for (int d = 0; d < 3; ++d) {
+            if (d >= dm) break;
+            s += (((a >> d) & 1) ? -1.0 : 1.0) * bb * u[d * nc + ci] * L.ih[d];
+        }
     }
-    s /= (1 << (dm - 1));
+    s *= 1.0 / (1 << (dm - 1));
     if (nodalrhs) s -= nodalrhs[idx];
     rh[idx] = s;
 }
@@ -479,12 +490,18 @@ HG_HD inline double grad_cell(const Geo& G, const Lev& L, long idx, int d, const
     cell_coords(L, idx, c);
     const int dm = G.dm;
     double s = 0.0;
-    for (int b = 0; b < (1 << dm); ++b) {
+    HG_UNROLL
+    for (int b = 0; b < 8; ++b) {   // (static bounds keep the small arrays in registers)
+        if (b >= (1 << dm)) break;
         int m[3] = {0, 0, 0};
-        for (int e = 0; e < dm; ++e) m[e] = node_wrap(G, L, e, c[e] + ((b >> e) & 1));
+        HG_UNROLL
+        for (int e = 0; e < 3; ++e) {
+            if (e >= dm) break;
+            m[e] = node_wrap(G, L, e, c[e] + ((b >> e) & 1));
+        }
         s += (((b >> d) & 1) ? 1.0 : -1.0) * phi[nix(L, m[0], m[1], m[2])];
     }
-    return s / (1 << (dm - 1)) / L.h[d];
+    return s * (1.0 / (1 << (dm - 1))) * L.ih[d];
 }
 
 // create_uvec_for_projection (Source/hgproject.f90:437-513) and the solver coefficient of a
@@ -493,15 +510,16 @@ HG_HD inline double grad_cell(const Geo& G, const Lev& L, long idx, int d, const
 HG_HD inline void uvec_cell(const Geo& G, long idx, long nc, int proj_type, double dt,
                             double* unew, const double* uold, const double* gpi,
                             const double* rhohalf, const double* b0, int alt, double* sig) {
+    // one division per cell (FP64 division being slow on the GPU): 1 / rhohalf and 1 / dt
+    const double irho = 1.0 / rhohalf[idx];
+    const double idt = proj_type == kPressureIters ? 1.0 / dt : 0.0;
     for (int d = 0; d < G.dm; ++d) {
         double& u = unew[d * nc + idx];
-        if (proj_type == kPressureIters) u = (u - uold[d * nc + idx]) / dt;
-        else if (proj_type == kRegular) u = u + dt * gpi[d * nc + idx] / rhohalf[idx];
+        if (proj_type == kPressureIters) u = (u - uold[d * nc + idx]) * idt;
+        else if (proj_type == kRegular) u = u + dt * gpi[d * nc + idx] * irho;
     }
     const double bb = b0 ? b0[idx] : 1.0;
-    double rho = rhohalf[idx] / bb;
-    if (alt) rho /= bb;
-    sig[idx] = 1.0 / rho;
+    sig[idx] = (alt ? bb * bb : bb) * irho;
 }
 
 // hg_update (Source/hgproject.f90:867-1009) on one cell; gphi written to gpi per proj_type.
@@ -509,16 +527,19 @@ HG_HD inline void update_cell(const Geo& G, const Lev& L, long idx, int proj_typ
                               const double* phi, double* unew, const double* uold, double* gpi,
                               const double* rhohalf, const double* b0, int alt) {
     const long nc = ncells(L);
+    // one division per cell (FP64 division being slow on the GPU): 1 / rhohalf and 1 / dt
+    const double irho = 1.0 / rhohalf[idx];
+    const double idt = proj_type == kRegular ? 1.0 / dt : 0.0;
     for (int d = 0; d < G.dm; ++d) {
         double g = grad_cell(G, L, idx, d, phi);
         if (alt) g *= b0 ? b0[idx] : 1.0;
         double& u = unew[d * nc + idx];
-        u -= g / rhohalf[idx];
+        u -= g * irho;
         if (proj_type == kPressureIters) u = uold[d * nc + idx] + dt * u;
         double& gp = gpi[d * nc + idx];
         if (proj_type == kInitial || proj_type == kDivuIters) gp = 0.0;
         else if (proj_type == kPressureIters) gp += g;
-        else if (proj_type == kRegular) gp = g / dt;
+        else if (proj_type == kRegular) gp = g * idt;
     }
 }
 
