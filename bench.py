@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--inner", type=int, default=None,
                     help="mixed precision: most FP32 V-cycles per FP64 refinement step")
+    ap.add_argument("--fused-sweep", action="store_true",
+                    help="mixed precision: one kernel per finest-level red/black sweep "
+                         "(mac_opts.fused_sweep)")
     ap.add_argument("--fixed-inner", action="store_true",
                     help="mixed precision: always --inner V-cycles per step (no adaptive count)")
     return ap.parse_args()
@@ -633,6 +636,8 @@ def main():
         inner_opts["inner_vcycles"] = args.inner
     if args.fixed_inner:
         inner_opts["adaptive_inner"] = 0
+    if args.fused_sweep:
+        inner_opts["fused_sweep"] = 1
 
     build()
     torch.cuda.set_device(local)
