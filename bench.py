@@ -202,6 +202,29 @@ class Clocks:
 
 
 # ---- the workload's config object, identical in both arms ------------------------------------
+def link_rates(dev, nbytes=1 << 29, reps=3):
+    """Host<->device copy rates of this machine (one page-locked buffer, one device buffer, the
+    copy engines, current stream): what bounds the end-to-end call's input and output copies."""
+    import torch
+    n = nbytes // 8
+    h = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    d = torch.empty(n, dtype=torch.float64, device=dev)
+    out = {}
+    for name, dst, src in (("h2d_gbs", d, h), ("d2h_gbs", h, d)):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            dst.copy_(src, non_blocking=True)
+        e1.record()
+        e1.synchronize()
+        out[name] = round(reps * nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9, 1)
+    del h, d
+    return out
+
+
 def mac_config(name, n, box, world):
     return {"workload": name, "n": list(n), "box": list(box), "rel_eps": 1e-10,
             "l2": "inputs larger than L2 (0.5 GB per step, a distinct copy per step)",
@@ -864,6 +887,9 @@ def main():
         ck_e2e = ck_e2e.stop()
         secs = max_over_ranks(sum(step_s))
         P.close()
+        link = link_rates(dev)
+        link["h2d_ms_per_step"] = round(h2d / link["h2d_gbs"] / 1e6, 3)
+        link["d2h_ms_per_step"] = round(d2h / link["d2h_gbs"] / 1e6, 3)
         e2e = {"value": world * E / secs, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "steps": E,
                "ms_per_step": [round(x * 1e3, 3) for x in step_s],
@@ -871,7 +897,7 @@ def main():
                "api": "mac_macproject (MAC_PTR_HOST; page-locked per-box fabs, 8 boxes of 128^3 "
                       "+ 1 ghost, copied by the copy engines on a transfer stream overlapped "
                       "with the setup and the copy-back)",
-               "precision": "mixed", "clocks": ck_e2e}
+               "precision": "mixed", "clocks": ck_e2e, "link": link}
 
     # ---- CPU baseline: one full solve of the workload by the oracle (rank 0, N = 1) ---------
     cpu = None

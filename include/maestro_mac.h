@@ -328,7 +328,8 @@ int mac_macproject_ml(mac_ctx* ctx, int ptr_kind,
  * (n0+1, n1+1[, n2+1]).  proj_type MAC_HG_*, dt the time step (> 0 for the pressure iterations
  * and the regular time step), dense_stencil 1 for hg_dense_stencil (9/27-point) else the cross
  * stencil, rel_eps the solver tolerance (<= 0: eps_hg = 1e-12).  Walls (U.n = 0), periodic and
- * outflow (phi = 0) faces; the context's use_alt_energy_fix, max_vcycles, nu1 and nu2 apply.
+ * outflow (phi = 0) faces (inlets: mac_ctx_set_inflow, mac_hgproject_dense_inflow); the
+ * context's use_alt_energy_fix, max_vcycles, nu1 and nu2 apply.
  * unew, gpi and pi are updated in place.
  */
 int mac_hgproject_dense(mac_ctx* ctx, int proj_type, double dt, int dense_stencil, double rel_eps,
@@ -350,6 +351,36 @@ int mac_hgproject(mac_ctx* ctx, int ptr_kind, int proj_type, double dt, int dens
                   int ng_uo, double* const* gpi, int ng_gp, const double* const* rhohalf,
                   int ng_rho, double* const* pi, int ng_pi, const double* const* beta0_cart,
                   int ng_b0, const double* const* nodalrhs, int ng_nr, mac_stats* stats);
+
+/*
+ * Inflow (inlet) faces of the nodal projection: the phys_bc == INLET test of hg_multigrid
+ * (Source/hg_multigrid.f90:191-203).  lo_inflow[d] / hi_inflow[d] (0 or 1; entries >= dm
+ * ignored; NULL: none) mark the low / high face of direction d as an inlet, which must be a
+ * MAC_BC_NEU face (MAC_ERR_INVALID otherwise).  Until the next call, the node-centred divergence
+ * of the nodal entries takes at an inlet the flux through the face of the inflow velocity on the
+ * wall: the normal component of U in the ghost cell just outside the face, as hgproject leaves it
+ * (create_uvec_for_projection: (U - Uold) / dt for the pressure iterations, else unchanged;
+ * times beta0_cart there when beta0_cart has a ghost layer).  Cells outside other non-periodic
+ * faces carry U = 0.  mac_hgproject reads the ghost values from the fabs (ng_u >= 1, and
+ * ng_uo >= 1 for MAC_HG_PRESSURE_ITERS; MAC_ERR_INVALID otherwise); mac_hgproject_dense_inflow
+ * takes them as an array.  The MAC projection needs none of this: its inlet face velocities are
+ * part of umac.
+ */
+int mac_ctx_set_inflow(mac_ctx* ctx, const int* lo_inflow, const int* hi_inflow);
+
+/*
+ * mac_hgproject_dense with inflow faces.  inflow_wall (DEVICE): for each inflow face of
+ * mac_ctx_set_inflow in the order (d = 0 low, d = 0 high, d = 1 low, ...), the wall value of
+ * beta0 U_d (the ghost cell's normal velocity after create_uvec_for_projection and the beta0
+ * scaling) for every cell of the face, the face's other directions in Fortran order; NULL exactly
+ * when no inflow face is set (MAC_ERR_INVALID otherwise).  mac_hgproject_dense is this entry with
+ * inflow_wall NULL.
+ */
+int mac_hgproject_dense_inflow(mac_ctx* ctx, int proj_type, double dt, int dense_stencil,
+                               double rel_eps, double* unew, const double* uold, double* gpi,
+                               const double* rhohalf, double* pi, const double* beta0_cart,
+                               const double* nodalrhs, const double* inflow_wall,
+                               mac_stats* stats);
 
 /*
  * Adjoint (reverse-mode derivative) of the whole-domain MAC projection; no counterpart in the

@@ -35,6 +35,7 @@ EXPORTED = (
     "mac_solve_small_noalloc", "mac_make_macrhs", "mac_make_macrhs_dense", "mac_make_at_halftime",
     "mac_macproject_cart", "mac_macproject_cart_dense", "mac_ctx_set_amr",
     "mac_macproject_ml_dense", "mac_macproject_ml", "mac_hgproject_dense", "mac_hgproject",
+    "mac_ctx_set_inflow", "mac_hgproject_dense_inflow",
 )
 MAC_NOALLOC_MAX_CELLS = 4096
 
@@ -205,6 +206,11 @@ def lib():
     L.mac_hgproject.argtypes = [vp, ci, ci, cd, ci, cd, dpp, ci, dpp, ci, dpp, ci, dpp, ci, dpp, ci,
                                 dpp, ci, dpp, ci, P(MacStats)]
     L.mac_hgproject.restype = ci
+    L.mac_ctx_set_inflow.argtypes = [vp, ip, ip]
+    L.mac_ctx_set_inflow.restype = ci
+    L.mac_hgproject_dense_inflow.argtypes = [vp, ci, cd, ci, cd, vp, vp, vp, vp, vp, vp, vp, vp,
+                                             P(MacStats)]
+    L.mac_hgproject_dense_inflow.restype = ci
     _lib = L
     return L
 

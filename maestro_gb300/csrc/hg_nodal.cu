@@ -53,8 +53,8 @@ __global__ void k_hg_uvec(hg::Geo G, long nc, int proj_type, double dt, double* 
     HG_LOOP(nc) hg::uvec_cell(G, idx, nc, proj_type, dt, unew, uold, gpi, rhohalf, b0, alt, sig);
 }
 __global__ void k_hg_divu(hg::Geo G, hg::Lev L, const double* u, const double* b0,
-                          const double* nodalrhs, double* rh, long N) {
-    HG_LOOP(N) hg::divu_node(G, L, idx, u, b0, nodalrhs, rh);
+                          const double* nodalrhs, hg::Wall W, double* rh, long N) {
+    HG_LOOP(N) hg::divu_node(G, L, idx, u, b0, nodalrhs, W, rh);
 }
 __global__ void k_hg_update(hg::Geo G, hg::Lev L, int proj_type, double dt, const double* phi,
                             double* unew, const double* uold, double* gpi, const double* rhohalf,
@@ -225,6 +225,53 @@ __global__ void k_hg_gs3(hg::Geo G, hg::LevT<T> L, int colour, T* phi, const T* 
         phi[i] = (f[i] + off) / dg;
     }
 }
+// One half of a colour-ordered Gauss-Seidel sweep, by slabs.  The colours are the node-parity
+// patterns, colour = p_0 + 2 p_1 (+ 4 p_2), updated in that order; the slab direction is the last
+// active one (z in 3-D, y in 2-D).  A node's neighbours along the slab direction have the other
+// slab parity, so while the colours of one slab parity are updated those neighbours stay as they
+// are: the slabs of that parity are independent, and each only has to run its 2^(dm-1) in-slab
+// colours in order.  Block b owns slab 2 b + sp and runs them with a block barrier between them
+// (global writes of a block are visible to the block after the barrier): bitwise the update
+// sequence of the 2^(dm-1) global colour launches it replaces, reading the level's phi and sigma
+// about once per half instead of once per colour.
+constexpr int kSlabThreads = 512;   // most threads of a slab block
+template <typename T, bool DENSE3>
+__global__ void __launch_bounds__(kSlabThreads)
+k_hg_gs_slab(hg::Geo G, hg::LevT<T> L, int sp, T* phi, const T* f) {
+    const int dm = G.dm, sd = dm - 1;
+    const int slab = 2 * (int)blockIdx.x + sp;
+    if (slab >= (sd == 2 ? L.nn[2] : L.nn[1])) return;   // (a select: no dynamic index)
+    for (int cq = 0; cq < (1 << sd); ++cq) {
+        const int px = cq & 1, py = sd == 2 ? (cq >> 1) & 1 : 0;
+        const int mx = (L.nn[0] - px + 1) / 2;
+        const int my = sd == 2 ? (L.nn[1] - py + 1) / 2 : 1;
+        const int cnt = mx * my;
+        for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+            const int ty = t / mx;
+            int p[3] = {2 * (t - ty * mx) + px, 0, 0};
+            if (sd == 2) {
+                p[1] = 2 * ty + py;
+                p[2] = slab;
+            } else {
+                p[1] = slab;
+            }
+            if (!hg::is_unknown(G, L, p)) continue;
+            T dg, off;
+            if (DENSE3) {
+                if (interior3(L, p))
+                    node_op_dense3(L, p, phi, dg, off);
+                else
+                    node_op_dense3_face(G, L, p, phi, dg, off);
+            } else {
+                hg::node_op(G, L, p, phi, dg, off);
+            }
+            const long i = hg::nix(L, p[0], p[1], p[2]);
+            phi[i] = (f[i] + off) / dg;
+        }
+        __syncthreads();
+    }
+}
+
 template <typename T>
 __global__ void k_hg_defect3(hg::Geo G, hg::LevT<T> L, const T* phi, const T* f, T* r, long N) {
     HG_LOOP(N) {
@@ -455,6 +502,52 @@ __global__ void k_hg_fabs_scatter(hg::Geo G, hg::Lev L, const hg::Fab* T, int nc
     }
 }
 
+// Wall values of the inflow faces from the ghost cells just outside them (per-box entry), as the
+// divergence takes them: create_uvec_for_projection leaves an inlet face's ghost velocity as the
+// caller filled it (the inflow velocity on the wall), except that the pressure iterations project
+// (U - Uold) / dt there too (Source/hgproject.f90:461-474, the loops include the first ghost
+// layer); U is then scaled by beta0_cart on the ghost layers beta0_cart has
+// (Source/hgproject.f90:140-143, multifab_mult_mult_c over nghost(beta0_cart)).  One thread per
+// cell of a face that a box touches; blockIdx.y = box, blockIdx.z = face 2 d + side.  TU / TUO /
+// TB: the unew / uold / beta0_cart fab tables (TUO null unless pressure iterations; TB null, or
+// b0_ghost 0: no beta0 scaling of the ghost).
+__global__ void k_hg_fabs_wall(int dm, hg::Lev L, hg::Wall W, const hg::Fab* TU,
+                               const hg::Fab* TUO, const hg::Fab* TB, int b0_ghost, double dt,
+                               double* wall) {
+    const int f = blockIdx.z;
+    const int d = f >> 1, side = f & 1;
+    if (d >= dm || W.off[f] < 0) return;
+    const hg::Fab U = TU[blockIdx.y];
+    if (side == 0 ? U.lo[d] != 0 : U.hi[d] != L.n[d] - 1) return;   // not on this face
+    const int e1 = d == 0 ? 1 : 0;
+    const int e2 = d == 2 ? 1 : 2;
+    const int t1 = U.hi[e1] - U.lo[e1] + 1;
+    const int t2 = dm == 3 ? U.hi[e2] - U.lo[e2] + 1 : 1;
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < (long)t1 * t2;
+         e += (long)gridDim.x * blockDim.x) {
+        const int i1 = (int)(e % t1), i2 = (int)(e / t1);
+        // fab-local position of the ghost cell (valid cells start at ng)
+        auto at = [&](const hg::Fab& B) {
+            int a[3] = {0, 0, 0};
+            a[d] = side == 0 ? B.ng - 1 : B.ng + (B.hi[d] - B.lo[d] + 1);
+            a[e1] = B.ng + i1;
+            if (dm == 3) a[e2] = B.ng + i2;
+            return (long)a[0] + (long)B.ext[0] * (a[1] + (long)B.ext[1] * a[2]);
+        };
+        double w = U.src[(long)d * U.count + at(U)];
+        if (TUO) {
+            const hg::Fab O = TUO[blockIdx.y];
+            w = (w - O.src[(long)d * O.count + at(O)]) / dt;
+        }
+        if (TB && b0_ghost) {
+            const hg::Fab B = TB[blockIdx.y];
+            w *= B.src[at(B)];
+        }
+        const long t = (long)(U.lo[e1] + i1) + (dm == 3 ? (long)L.n[e1] * (U.lo[e2] + i2) : 0L);
+        wall[W.off[f] + t] = w;
+    }
+}
+
 inline int blocks_for(long n, int sms) {
     const long b = (n + kThreads - 1) / kThreads;
     const long cap = (long)std::max(1, sms) * 16;
@@ -478,6 +571,12 @@ struct HgState {
     // exact solve of the coarsest level (at most kExactMax unknown nodes): its unknown nodes
     // (storage indices), node -> unknown number (-1: not an unknown), and the dense inverse of
     // its operator (B = A + sigma 1 1^T when singular), rebuilt with the coefficients each call
+    // captured V-cycles (per precision: [0] FP64, [1] FP32), replayed while the key matches
+    struct Graph {
+        cudaGraphExec_t exec = nullptr;
+        int key[4] = {-1, -1, -1, -1};   // count, nu1, nu2, dense stencil
+        long long kernels = 0;
+    } graph[2];
     int bM = 0;
     int* bnode = nullptr;
     int* bmap = nullptr;
@@ -501,15 +600,20 @@ struct HgState {
     size_t tab_cap = 0;
     double* staging = nullptr;
     size_t staging_cap = 0;
+    double* fwall = nullptr;   // per-box calls: wall values of the inflow faces (hg::Wall)
+    size_t fwall_cap = 0;
 };
 
 void hg_release(mac_ctx* c) {
     HgState* H = c->hgs;
     if (!H) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& g : H->graph)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     for (void* p : H->allocs) cudaFree(p);
     if (H->d_tab) cudaFree(H->d_tab);
     if (H->staging) cudaFree(H->staging);
+    if (H->fwall) cudaFree(H->fwall);
     if (H->h_tab) cudaFreeHost(H->h_tab);
     if (H->h_out) cudaFreeHost(H->h_out);
     if (H->h_flag) cudaFreeHost(H->h_flag);
@@ -646,6 +750,45 @@ struct HgMg {
         }
     }
     bool dense3() const { return geo.dense && geo.dm == 3; }
+    // count V-cycles from level 0, captured once into a CUDA graph per (count, nu1, nu2,
+    // stencil) and replayed: the cycle issues one launch per colour, level and kernel kind,
+    // most of them small, and needs no host value inside
+    void run_cycles(int count, int nu1, int nu2) {
+        if (err) return;
+        HgState::Graph& g = H->graph[std::is_same<T, float>::value ? 1 : 0];
+        const int key[4] = {count, nu1, nu2, geo.dense};
+        if (!g.exec || std::memcmp(g.key, key, sizeof(key)) != 0) {
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+            const long long before = c->issued;
+            cudaGraph_t gr = nullptr;
+            if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                set_last_cuda_error(cudaGetLastError(), "cudaStreamBeginCapture", __FILE__, __LINE__);
+                err = MAC_ERR_CUDA;
+                return;
+            }
+            for (int v = 0; v < count; ++v) hg::vcycle(*this, 0, nu1, nu2);
+            const cudaError_t ec = cudaStreamEndCapture(c->stream, &gr);
+            if (ec != cudaSuccess || err ||
+                cudaGraphInstantiate(&g.exec, gr, 0) != cudaSuccess) {
+                set_last_cuda_error(cudaGetLastError(), "hg V-cycle graph", __FILE__, __LINE__);
+                if (gr) cudaGraphDestroy(gr);
+                g.exec = nullptr;
+                if (!err) err = MAC_ERR_CUDA;
+                return;
+            }
+            cudaGraphDestroy(gr);
+            std::memcpy(g.key, key, sizeof(key));
+            g.kernels = c->issued - before;
+            c->issued = before;   // captured, not launched yet
+        }
+        if (cudaGraphLaunch(g.exec, c->stream) != cudaSuccess) {
+            set_last_cuda_error(cudaGetLastError(), "cudaGraphLaunch", __FILE__, __LINE__);
+            err = MAC_ERR_CUDA;
+            return;
+        }
+        c->issued += g.kernels;
+    }
     void defect(int l, const T* phi, const T* f, T* r) {
         if (dense3())
             k_hg_defect3<T><<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), phi, f, r, nn(l));
@@ -653,14 +796,39 @@ struct HgMg {
             k_hg_defect<T><<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), phi, f, r, nn(l));
         launched();
     }
+    // nu sweeps, each as two slab-parity halves (k_hg_gs_slab: the same update sequence as one
+    // launch per colour)
+    // Levels whose in-slab colours fit one block (one node per thread, at most kSlabThreads)
+    // sweep by slabs, two launches a sweep; finer levels keep one launch per colour: there one
+    // block per slab would leave most of the SMs idle (128 blocks at 256^3, 15.1 against 22.9
+    // projections/s measured).  Both orders are the same update sequence.
     void gs(int l, T* phi, const T* f, int nu) {
+        const int dm = geo.dm;
+        const hg::LevT<T>& L = lev(l);
+        const int ns = L.nn[dm - 1];
+        const int per_slab = (L.nn[0] + 1) / 2 * (dm == 3 ? (L.nn[1] + 1) / 2 : 1);
+        if (per_slab > kSlabThreads) {
+            for (int s = 0; s < nu; ++s)
+                for (int colour = 0; colour < (1 << dm); ++colour) {
+                    const long m = hg::colour_count(geo, L, colour);
+                    if (dense3())
+                        k_hg_gs3<T><<<blocks(m), kThreads, 0, c->stream>>>(geo, L, colour, phi, f, m);
+                    else
+                        k_hg_gs<T><<<blocks(m), kThreads, 0, c->stream>>>(geo, L, colour, phi, f, m);
+                    launched();
+                }
+            return;
+        }
+        int threads = 32;
+        while (threads < per_slab) threads <<= 1;
         for (int s = 0; s < nu; ++s)
-            for (int colour = 0; colour < (1 << geo.dm); ++colour) {
-                const long m = hg::colour_count(geo, lev(l), colour);
+            for (int sp = 0; sp < 2; ++sp) {
+                const int nb = (ns - sp + 1) / 2;
+                if (nb <= 0) continue;
                 if (dense3())
-                    k_hg_gs3<T><<<blocks(m), kThreads, 0, c->stream>>>(geo, lev(l), colour, phi, f, m);
+                    k_hg_gs_slab<T, true><<<nb, threads, 0, c->stream>>>(geo, L, sp, phi, f);
                 else
-                    k_hg_gs<T><<<blocks(m), kThreads, 0, c->stream>>>(geo, lev(l), colour, phi, f, m);
+                    k_hg_gs_slab<T, false><<<nb, threads, 0, c->stream>>>(geo, L, sp, phi, f);
                 launched();
             }
     }
@@ -727,6 +895,7 @@ struct HgExec : HgMg<double> {
     double* pi = nullptr;
     const double* b0 = nullptr;
     const double* nodalrhs = nullptr;
+    hg::Wall wall{nullptr, {-1, -1, -1, -1, -1, -1}};
     int alt = 0;
 
     void uvec() {
@@ -763,7 +932,7 @@ struct HgExec : HgMg<double> {
         launched();
     }
     void divu() {
-        k_hg_divu<<<blocks(nn(0)), kThreads, 0, c->stream>>>(geo, lev(0), unew, b0, nodalrhs,
+        k_hg_divu<<<blocks(nn(0)), kThreads, 0, c->stream>>>(geo, lev(0), unew, b0, nodalrhs, wall,
                                                             buf(0, hg::kF), nn(0));
         launched();
     }
@@ -800,9 +969,27 @@ int hg_ensure_single(mac_ctx* c) {
 
 // The nodal projection on whole-domain device arrays (arguments validated by the caller); fills
 // the solve fields of *st and returns the status code.
+// Offsets of the context's inflow faces in a wall array (hg::Wall): face f = 2 d + side in that
+// order, each holding its cells (the face's other directions, Fortran order); returns the total
+// length (0: no inflow face).
+long hg_wall_layout(const mac_ctx* c, long off[6]) {
+    long tot = 0;
+    for (int f = 0; f < 6; ++f) {
+        off[f] = -1;
+        const int d = f >> 1;
+        if (d >= c->dm || !((f & 1) ? c->inflow_hi[d] : c->inflow_lo[d])) continue;
+        long m = 1;
+        for (int e = 0; e < c->dm; ++e)
+            if (e != d) m *= c->n[e];
+        off[f] = tot;
+        tot += m;
+    }
+    return tot;
+}
+
 int hg_core(mac_ctx* c, int proj_type, double dt, int dense_stencil, double rel_eps,
             double* unew, const double* uold, double* gpi, const double* rhohalf, double* pi,
-            const double* beta0_cart, const double* nodalrhs, mac_stats* st) {
+            const double* beta0_cart, const double* nodalrhs, const double* wall, mac_stats* st) {
     int rc = MAC_OK;
     HgState* H = c->hgs;
     H->geo.dense = dense_stencil ? 1 : 0;
@@ -823,6 +1010,10 @@ int hg_core(mac_ctx* c, int proj_type, double dt, int dense_stencil, double rel_
     ex.pi = pi;
     ex.b0 = beta0_cart;
     ex.nodalrhs = nodalrhs;
+    if (hg_wall_layout(c, ex.wall.off) > 0) {
+        if (!wall) return MAC_ERR_INVALID;
+        ex.wall.w = wall;
+    }
     ex.alt = (proj_type != hg::kInitial && proj_type != hg::kDivuIters && c->o.use_alt_energy_fix) ? 1 : 0;
     // rhohalf and beta0 must be positive and finite
     if (cudaMemsetAsync(H->flag, 0, sizeof(int), c->stream) != cudaSuccess) rc = MAC_ERR_CUDA;
@@ -1033,9 +1224,34 @@ int hg_fabs(mac_ctx* c, int ptr_kind, int proj_type, double dt, int dense_stenci
         tab_at[k] = tcur;
         tcur += (size_t)nb;
     }
+    long woff[6];
+    const long nwall = hg_wall_layout(c, woff);
+    if (nwall > 0) {
+        MAC_CUDA_TRY(cudaStreamSynchronize(c->stream));   // (the buffer may be regrown)
+        rc = hg_grow(&H->fwall, &H->fwall_cap, (size_t)nwall, false);
+        if (rc) return rc;
+        hg::Wall W{H->fwall, {woff[0], woff[1], woff[2], woff[3], woff[4], woff[5]}};
+        long maxf = 1;
+        for (int b = 0; b < nb; ++b)
+            for (int d = 0; d < dm; ++d) {
+                long m = 1;
+                for (int e = 0; e < dm; ++e)
+                    if (e != d) m *= (long)c->box_hi[3 * b + e] - c->box_lo[3 * b + e] + 1;
+                maxf = std::max(maxf, m);
+            }
+        const dim3 grid((unsigned)std::min<long>((maxf + kThreads - 1) / kThreads, 1024), (unsigned)nb,
+                        (unsigned)(2 * dm));
+        k_hg_fabs_wall<<<grid, kThreads, 0, c->stream>>>(
+            dm, L0, W, H->d_tab + tab_at[0],
+            proj_type == hg::kPressureIters ? H->d_tab + tab_at[1] : nullptr,
+            beta0_cart ? H->d_tab + tab_at[5] : nullptr, ng_b0 >= 1 ? 1 : 0, dt, H->fwall);
+        MAC_CUDA_TRY(cudaGetLastError());
+        ++c->issued;
+    }
     const int solve_rc = hg_core(c, proj_type, dt, dense_stencil, rel_eps, H->fu,
                                  uold ? H->fuo : nullptr, H->fg, H->frho, H->fpi,
-                                 beta0_cart ? H->fb0 : nullptr, nodalrhs ? H->fnr : nullptr, st);
+                                 beta0_cart ? H->fb0 : nullptr, nodalrhs ? H->fnr : nullptr,
+                                 nwall > 0 ? H->fwall : nullptr, st);
     if (solve_rc != MAC_OK && solve_rc != MAC_ERR_NOT_CONVERGED) return solve_rc;
     for (int k = 0; k < 7; ++k) {
         const Arr& A = arrs[k];
@@ -1071,10 +1287,21 @@ int mac_hgproject_dense(mac_ctx* c, int proj_type, double dt, int dense_stencil,
                         double* unew, const double* uold, double* gpi, const double* rhohalf,
                         double* pi, const double* beta0_cart, const double* nodalrhs,
                         mac_stats* stats) {
+    return mac_hgproject_dense_inflow(c, proj_type, dt, dense_stencil, rel_eps, unew, uold, gpi,
+                                      rhohalf, pi, beta0_cart, nodalrhs, nullptr, stats);
+}
+
+int mac_hgproject_dense_inflow(mac_ctx* c, int proj_type, double dt, int dense_stencil,
+                               double rel_eps, double* unew, const double* uold, double* gpi,
+                               const double* rhohalf, double* pi, const double* beta0_cart,
+                               const double* nodalrhs, const double* inflow_wall,
+                               mac_stats* stats) {
     mac_stats local;
     mac_stats* st = stats ? stats : &local;
     std::memset(st, 0, sizeof(*st));
     if (!c || !unew || !gpi || !rhohalf || !pi) return st->status = MAC_ERR_INVALID;
+    long woff[6];
+    if ((hg_wall_layout(c, woff) > 0) != (inflow_wall != nullptr)) return st->status = MAC_ERR_INVALID;
     int rc = hg_check_args(c, proj_type, dt, uold != nullptr);
     if (rc) return st->status = rc;
     const auto t0 = std::chrono::steady_clock::now();
@@ -1082,7 +1309,7 @@ int mac_hgproject_dense(mac_ctx* c, int proj_type, double dt, int dense_stencil,
     rc = hg_ensure(c);
     if (!rc)
         rc = hg_core(c, proj_type, dt, dense_stencil, rel_eps, unew, uold, gpi, rhohalf, pi,
-                     beta0_cart, nodalrhs, st);
+                     beta0_cart, nodalrhs, inflow_wall, st);
     st->status = rc;
     st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     end_call_stats(c, st);
@@ -1109,6 +1336,11 @@ int mac_hgproject(mac_ctx* c, int ptr_kind, int proj_type, double dt, int dense_
             return st->status = MAC_ERR_INVALID;
     int rc = hg_check_args(c, proj_type, dt, uold != nullptr);
     if (rc) return st->status = rc;
+    // inflow faces take their wall values from the first ghost layer outside them
+    long woff[6];
+    if (hg_wall_layout(c, woff) > 0 &&
+        (ng_u < 1 || (proj_type == hg::kPressureIters && ng_uo < 1)))
+        return st->status = MAC_ERR_INVALID;
     const auto t0 = std::chrono::steady_clock::now();
     begin_call_stats(c, st);
     rc = hg_ensure(c);
@@ -1120,6 +1352,24 @@ int mac_hgproject(mac_ctx* c, int ptr_kind, int proj_type, double dt, int dense_
     end_call_stats(c, st);
     report_call(c, "hgproject", st);
     return rc;
+}
+
+int mac_ctx_set_inflow(mac_ctx* c, const int* lo_inflow, const int* hi_inflow) {
+    if (!c) return MAC_ERR_INVALID;
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int d = 0; d < c->dm; ++d) {
+        lo[d] = lo_inflow ? lo_inflow[d] : 0;
+        hi[d] = hi_inflow ? hi_inflow[d] : 0;
+        if (lo[d] < 0 || lo[d] > 1 || hi[d] < 0 || hi[d] > 1) return MAC_ERR_INVALID;
+        // an inlet is a Neumann face of the pressure (Source/define_bc_tower.f90:329-392)
+        if ((lo[d] && c->bc_lo[d] != MAC_BC_NEU) || (hi[d] && c->bc_hi[d] != MAC_BC_NEU))
+            return MAC_ERR_INVALID;
+    }
+    for (int d = 0; d < 3; ++d) {
+        c->inflow_lo[d] = lo[d];
+        c->inflow_hi[d] = hi[d];
+    }
+    return MAC_OK;
 }
 
 }  // extern "C"

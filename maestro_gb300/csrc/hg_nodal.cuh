@@ -28,6 +28,8 @@
 
 #include <cmath>
 #include <cstdint>
+#include <type_traits>
+#include <utility>
 
 #if defined(__CUDACC__)
 #define HG_HD __host__ __device__
@@ -51,6 +53,14 @@ struct Geo {
     int per[3];
     int dlo[3], dhi[3];
     int dense;
+};
+
+// Inflow faces of the divergence: face f = 2 d + side (side 0 low, 1 high) is an inflow face when
+// off[f] >= 0; w + off[f] then holds the wall value of beta0 U_d there for each cell of the face,
+// the face's other directions in Fortran order (the cells a ghost layer outside it would hold).
+struct Wall {
+    const double* w;
+    long off[6];
 };
 
 // A level in the precision T of its coefficients and smoother (FP64; FP32 for the inner cycles
@@ -450,9 +460,11 @@ HG_HD inline void finish_node(const Geo& G, const LevT<T>& L, long idx, T* x) {
 }
 
 // Node-centred divergence of beta0 U (u component-major over the cells; b0 null: 1), minus
-// the nodal source (nullable).
+// the nodal source (nullable).  Cells outside a non-periodic face carry U = 0, except that at an
+// inflow face (W) the cell just outside contributes its wall value of beta0 U_d through the face:
+// the boundary flux of the finite-element divergence, with the inflow velocity on the wall.
 HG_HD inline void divu_node(const Geo& G, const Lev& L, long idx, const double* u,
-                            const double* b0, const double* nodalrhs, double* rh) {
+                            const double* b0, const double* nodalrhs, const Wall& W, double* rh) {
     int p[3];
     node_coords(L, idx, p);
     const int dm = G.dm;
@@ -462,21 +474,34 @@ HG_HD inline void divu_node(const Geo& G, const Lev& L, long idx, const double* 
     for (int a = 0; a < 8; ++a) {   // (static bounds keep the small arrays in registers)
         if (a >= (1 << dm)) break;
         int c[3] = {0, 0, 0};
-        bool out = false;
+        int nout = 0, dout = 0, side = 0;
         HG_UNROLL
         for (int d = 0; d < 3; ++d) {
             if (d >= dm) break;
-            const int cw = cell_wrap(G, L, d, p[d] - ((a >> d) & 1));
-            if (cw < 0) out = true;
+            const int raw = p[d] - ((a >> d) & 1);
+            const int cw = cell_wrap(G, L, d, raw);
+            if (cw < 0) {
+                ++nout;
+                dout = d;
+                side = raw < 0 ? 0 : 1;
+            }
             c[d] = cw;
         }
-        if (out) continue;
-        const long ci = cix(L, c[0], c[1], c[2]);
-        const double bb = b0 ? b0[ci] : 1.0;
-        HG_UNROLL
-        for (int d = 0; d < 3; ++d) {
-            if (d >= dm) break;
-            s += (((a >> d) & 1) ? -1.0 : 1.0) * bb * u[d * nc + ci] * L.ih[d];
+        if (nout == 0) {
+            const long ci = cix(L, c[0], c[1], c[2]);
+            const double bb = b0 ? b0[ci] : 1.0;
+            HG_UNROLL
+            for (int d = 0; d < 3; ++d) {
+                if (d >= dm) break;
+                s += (((a >> d) & 1) ? -1.0 : 1.0) * bb * u[d * nc + ci] * L.ih[d];
+            }
+        } else if (nout == 1 && W.off[2 * dout + side] >= 0) {
+            // the ghost cell just outside an inflow face: its normal velocity is the wall value
+            // (its flux through the face), the tangential ones carry no flux out of the domain
+            const int e1 = dout == 0 ? 1 : 0;
+            const int e2 = dout == 2 ? 1 : 2;
+            const long t = c[e1] + (dm == 3 ? (long)L.n[e1] * c[e2] : 0L);
+            s += (((a >> dout) & 1) ? -1.0 : 1.0) * W.w[W.off[2 * dout + side] + t] * L.ih[dout];
         }
     }
     s *= 1.0 / (1 << (dm - 1));
@@ -624,6 +649,23 @@ void vcycle(E& ex, int l, int nu1, int nu2) {
     ex.gs(l, ex.buf(l, kPhi), ex.buf(l, kF), nu2);
 }
 
+// `count` V-cycles from level 0.  An executor with a member run_cycles(count, nu1, nu2) runs
+// them itself (the GPU executor replays a captured CUDA graph of the cycles); otherwise they are
+// issued one after the other.
+template <class E, class = void>
+struct HasRunCycles : std::false_type {};
+template <class E>
+struct HasRunCycles<E, std::void_t<decltype(std::declval<E&>().run_cycles(0, 0, 0))>>
+    : std::true_type {};
+template <class E>
+void vcycles(E& ex, int count, int nu1, int nu2) {
+    if constexpr (HasRunCycles<E>::value) {
+        ex.run_cycles(count, nu1, nu2);
+    } else {
+        for (int v = 0; v < count; ++v) vcycle(ex, 0, nu1, nu2);
+    }
+}
+
 struct SolveStats {
     int status;
     int cycles;
@@ -632,7 +674,9 @@ struct SolveStats {
     double hist[64];
 };
 
-// Solve L phi = f on level 0 (phi: initial guess in buf(0, kPhi), f in buf(0, kF)).
+// Solve L phi = f on level 0 from phi = 0 (buf(0, kPhi) zeroed by the caller, f in buf(0, kF)).
+// With phi = 0 the defect is f on the unknown nodes, so the first residual norm is fnorm and
+// needs no operator pass.
 template <class E>
 int solve(E& ex, double rel_eps, int max_cycles, int nu1, int nu2, SolveStats* S) {
     *S = SolveStats{};
@@ -644,12 +688,11 @@ int solve(E& ex, double rel_eps, int max_cycles, int nu1, int nu2, SolveStats* S
         S->status = std::isnan(fnorm) ? -1 : 0;
         return ex.error() ? ex.error() : S->status;
     }
-    ex.defect(0, ex.buf(0, kPhi), ex.buf(0, kF), ex.buf(0, kR));
-    double res = ex.unknown_max(0, ex.buf(0, kR));
+    double res = fnorm;
     S->resid0 = res;
     int it = 0;
     while (!(res <= rel_eps * fnorm) && it < max_cycles && !std::isnan(res)) {
-        vcycle(ex, 0, nu1, nu2);
+        vcycles(ex, 1, nu1, nu2);
         ++it;
         ex.defect(0, ex.buf(0, kPhi), ex.buf(0, kF), ex.buf(0, kR));
         res = ex.unknown_max(0, ex.buf(0, kR));
@@ -679,8 +722,8 @@ int project(E& ex, double rel_eps, int max_cycles, int nu1, int nu2, SolveStats*
     return rc ? rc : status;
 }
 
-// Mixed-precision solve: FP64 defect, `inner` FP32 V-cycles on it from zero (ex32: the FP32
-// view of the same hierarchy), FP64 accumulation, until the FP64 residual meets rel_eps.
+// Mixed-precision solve from phi = 0: FP64 defect, `inner` FP32 V-cycles on it from zero (ex32:
+// the FP32 view of the same hierarchy), FP64 accumulation, until the FP64 residual meets rel_eps.
 template <class E, class E32>
 int solve_mixed(E& ex, E32& ex32, double rel_eps, int max_iters, int nu1, int nu2, int inner,
                 SolveStats* S) {
@@ -693,14 +736,15 @@ int solve_mixed(E& ex, E32& ex32, double rel_eps, int max_iters, int nu1, int nu
         S->status = std::isnan(fnorm) ? -1 : 0;
         return ex.error() ? ex.error() : S->status;
     }
-    ex.defect(0, ex.buf(0, kPhi), ex.buf(0, kF), ex.buf(0, kR));
-    double res = ex.unknown_max(0, ex.buf(0, kR));
+    // phi = 0: the first defect is f on the unknown nodes (the FP32 cycles read their right-hand
+    // side on unknown nodes only), and its norm is fnorm
+    double res = fnorm;
     S->resid0 = res;
     int it = 0;
     while (!(res <= rel_eps * fnorm) && it < max_iters && !std::isnan(res)) {
-        ex.to_single(ex.buf(0, kR), ex32.buf(0, kF));
+        ex.to_single(ex.buf(0, it == 0 ? kF : kR), ex32.buf(0, kF));
         ex32.zero(0, ex32.buf(0, kPhi));
-        for (int v = 0; v < inner; ++v) vcycle(ex32, 0, nu1, nu2);
+        vcycles(ex32, inner, nu1, nu2);
         ex.accumulate(ex.buf(0, kPhi), ex32.buf(0, kPhi));
         ex.defect(0, ex.buf(0, kPhi), ex.buf(0, kF), ex.buf(0, kR));
         res = ex.unknown_max(0, ex.buf(0, kR));

@@ -319,6 +319,8 @@ struct mac_ctx {
 
     mac::AmrState* amr = nullptr;                 // finer AMR levels (mac_ctx_set_amr); null: one level
     mac::HgState* hgs = nullptr;                  // nodal projection levels (first nodal call)
+    int inflow_lo[3] = {0, 0, 0};                 // nodal projection: inflow (inlet) faces
+    int inflow_hi[3] = {0, 0, 0};
 
     size_t bytes_allocated = 0;
     std::vector<void*> allocations;

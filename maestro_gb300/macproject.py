@@ -349,18 +349,33 @@ class MacProjector:
         self._check(rc, "mac_macproject_ml", st, strict)
         return st.as_dict()
 
+    def set_inflow(self, lo_inflow=(0, 0, 0), hi_inflow=(0, 0, 0)):
+        """Inlet faces of the nodal projection (mac_ctx_set_inflow): flags per direction."""
+        lo = (ctypes.c_int * 3)(*(list(lo_inflow) + [0] * (3 - len(lo_inflow))))
+        hi = (ctypes.c_int * 3)(*(list(hi_inflow) + [0] * (3 - len(hi_inflow))))
+        rc = capi.lib().mac_ctx_set_inflow(self.ctx, lo, hi)
+        if rc != capi.MAC_OK:
+            raise MacError(rc, "mac_ctx_set_inflow")
+
     def hgproject_dense(self, proj_type, dt, unew, uold, gpi, rhohalf, pi, beta0_cart=None,
-                        nodalrhs=None, dense_stencil=True, rel_eps=1e-12, strict=False):
-        """Nodal (HG) projection on this projector's domain (mac_hgproject_dense), device
-        pointers (ints): cell vector fields unew / uold / gpi (cells x dm, component-major),
-        rhohalf and beta0_cart cells, pi and nodalrhs nodes (cells + 1 per direction)."""
+                        nodalrhs=None, dense_stencil=True, rel_eps=1e-12, strict=False,
+                        inflow_wall=None):
+        """Nodal (HG) projection on this projector's domain (mac_hgproject_dense, or
+        mac_hgproject_dense_inflow with the inlet faces' wall values), device pointers (ints):
+        cell vector fields unew / uold / gpi (cells x dm, component-major), rhohalf and
+        beta0_cart cells, pi and nodalrhs nodes (cells + 1 per direction)."""
         st = capi.MacStats()
         v = ctypes.c_void_p
-        rc = capi.lib().mac_hgproject_dense(
-            self.ctx, int(proj_type), float(dt), int(bool(dense_stencil)), float(rel_eps), v(unew),
-            v(uold or 0), v(gpi), v(rhohalf), v(pi), v(beta0_cart or 0), v(nodalrhs or 0),
-            ctypes.byref(st))
-        self._check(rc, "mac_hgproject_dense", st, strict)
+        args = (self.ctx, int(proj_type), float(dt), int(bool(dense_stencil)), float(rel_eps),
+                v(unew), v(uold or 0), v(gpi), v(rhohalf), v(pi), v(beta0_cart or 0),
+                v(nodalrhs or 0))
+        if inflow_wall is None:
+            name = "mac_hgproject_dense"
+            rc = capi.lib().mac_hgproject_dense(*args, ctypes.byref(st))
+        else:
+            name = "mac_hgproject_dense_inflow"
+            rc = capi.lib().mac_hgproject_dense_inflow(*args, v(inflow_wall), ctypes.byref(st))
+        self._check(rc, name, st, strict)
         return st.as_dict()
 
     def hgproject(self, proj_type, dt, unew, uold, gpi, rhohalf, pi, beta0_cart=None,

@@ -97,6 +97,8 @@ class OrcHgOpts(ctypes.Structure):
         ("nu2", ctypes.c_int),
         ("bottom_eps", ctypes.c_double),
         ("nthreads", ctypes.c_int),
+        ("wall_off", ctypes.c_long * 6),
+        ("wall", ctypes.c_void_p),
     ]
 
 
@@ -529,7 +531,53 @@ def _hg_opts(shape, dx, bc_lo, bc_hi, dense=True, proj_type=HG_INITIAL, dt=1.0,
     o.nu1, o.nu2 = int(nu1), int(nu2)
     o.bottom_eps = float(bottom_eps)
     o.nthreads = int(threads)
+    for f in range(6):
+        o.wall_off[f] = -1
+    o.wall = None
     return o
+
+
+def hg_wall_layout(shape, inflow_lo, inflow_hi):
+    """Offsets of the inflow faces in a wall array: face f = 2 d + side in that order, each
+    holding its cells (the face's other directions, Fortran order).  Returns (offsets, total)."""
+    dm = len(shape)
+    off, tot = [-1] * 6, 0
+    for f in range(2 * dm):
+        d, side = divmod(f, 2)
+        if not (inflow_hi if side else inflow_lo)[d]:
+            continue
+        off[f] = tot
+        tot += int(np.prod([shape[e] for e in range(dm) if e != d]))
+    return off, tot
+
+
+def hg_wall_from_ghosts(shape, inflow_lo, inflow_hi, proj_type, dt, unew_pad, uold_pad=None,
+                        beta0_pad=None):
+    """The inflow faces' wall values of beta0 U_d as hgproject leaves the ghost cells outside
+    them: `*_pad` are whole-domain arrays with one ghost layer (cells + 2 per direction; unew /
+    uold with a trailing component axis).  create_uvec_for_projection forms (U - Uold) / dt on
+    the first ghost layer too for the pressure iterations and leaves an inlet's ghost cells
+    otherwise as filled (Source/hgproject.f90:461-474, 500-511: only walls and symmetry faces are
+    zeroed); U is then multiplied by beta0_cart on beta0_cart's ghost layers
+    (Source/hgproject.f90:140-143; beta0_pad None: beta0_cart has no ghost layer, no scaling)."""
+    dm = len(shape)
+    off, tot = hg_wall_layout(shape, inflow_lo, inflow_hi)
+    wall = np.zeros(max(tot, 1))
+    for f in range(2 * dm):
+        if off[f] < 0:
+            continue
+        d, side = divmod(f, 2)
+        sl = [slice(1, shape[e] + 1) for e in range(dm)]
+        sl[d] = 0 if side == 0 else shape[d] + 1
+        sl = tuple(sl)
+        w = np.asarray(unew_pad)[sl + (d,)].astype(np.float64)
+        if proj_type == HG_PRESSURE_ITERS:
+            w = (w - np.asarray(uold_pad)[sl + (d,)]) / dt
+        if beta0_pad is not None:
+            w = w * np.asarray(beta0_pad)[sl]
+        m = w.size
+        wall[off[f]:off[f] + m] = np.ravel(w, order="F")
+    return wall
 
 
 def node_shape(shape):
@@ -581,11 +629,12 @@ def hg_solve(sigma, rh, dx, bc_lo, bc_hi, phi=None, dense=True, rel_eps=EPS_HG,
 
 def hgproject(unew, uold, gpi, rhohalf, pi, dx, bc_lo, bc_hi, proj_type=HG_REGULAR, dt=1.0,
               beta0_cart=None, nodalrhs=None, dense=True, alt_energy_fix=False, rel_eps=EPS_HG,
-              max_vcycles=100, threads=0):
+              max_vcycles=100, threads=0, inflow_lo=(0, 0, 0), inflow_hi=(0, 0, 0), wall=None):
     """Oracle nodal projection on one level (Source/hgproject.f90:32-264).
 
     Cell vector fields unew / uold / gpi have shape cells + (dm,); rhohalf and beta0_cart are
-    cell arrays; pi and nodalrhs node arrays (cells + 1 per direction).  Returns
+    cell arrays; pi and nodalrhs node arrays (cells + 1 per direction).  Inlet faces:
+    inflow_lo / inflow_hi flags with `wall` their wall values (hg_wall_from_ghosts).  Returns
     (unew, gpi, pi, phi, stats)."""
     unew = _f64f(unew).copy(order="F")
     gpi = _f64f(gpi).copy(order="F")
@@ -599,6 +648,14 @@ def hgproject(unew, uold, gpi, rhohalf, pi, dx, bc_lo, bc_hi, proj_type=HG_REGUL
     o = _hg_opts(shape, dx, bc_lo, bc_hi, dense=dense, proj_type=proj_type, dt=dt,
                  alt_energy_fix=alt_energy_fix, rel_eps=rel_eps, max_vcycles=max_vcycles,
                  threads=threads)
+    off, tot = hg_wall_layout(shape, inflow_lo, inflow_hi)
+    if tot > 0:
+        wall = _f64f(wall)
+        if wall.size < tot:
+            raise ValueError("wall array shorter than the inflow faces")
+        for f in range(6):
+            o.wall_off[f] = off[f]
+        o.wall = wall.ctypes.data
     st = OrcStats()
     lib().orc_hgproject(ctypes.byref(o), _ptr(unew), _ptr(uold), _ptr(gpi), _ptr(rhohalf),
                         _ptr(pi), _ptr(b0), _ptr(nr), _ptr(phi), ctypes.byref(st))

@@ -24,7 +24,9 @@
 //                 node 0; nodes on an outflow (Dirichlet) face are fixed at 0.
 //   * divergence: DU_p = sum_d (1/h_d) 2^(1-dm) [sum of u_d over the cells on the + side of p -
 //                 the same on the - side] (Docs/mg/mg.tex:485-493); cells outside a non-periodic
-//                 face carry U = 0 (create_uvec sets wall ghosts to 0).
+//                 face carry U = 0 (create_uvec sets wall ghosts to 0), except that the ghost
+//                 cell outside an inlet face adds the flux of its normal velocity (orc_hg_opts
+//                 wall: the inflow on the wall, lo_inflow / hi_inflow of hg_multigrid).
 //   * dense     : the bilinear / trilinear finite-element stiffness per cell, scaled by the cell
 //                 coefficient sigma and divided by the nodal volume prod h_d:
 //                 (L phi)_p = - sum_{cells c of p} sigma_c sum_{nodes m of c} sum_d h_d^-2
@@ -71,6 +73,11 @@ typedef struct orc_hg_opts {
     int nu1, nu2;
     double bottom_eps;
     int nthreads;
+    // inflow (inlet) faces: face f = 2 d + side (0 low, 1 high) is an inlet when wall_off[f] >= 0;
+    // wall + wall_off[f] then holds, for each cell of the face (its other directions, Fortran
+    // order), the wall value of beta0 U_d the ghost cell outside it carries
+    long wall_off[6];
+    const double* wall;
 } orc_hg_opts;
 
 }  // extern "C"
@@ -547,7 +554,11 @@ int nodal_solve(NCtx& C, const double* rh, double* phi, orc_stats* st) {
 }
 
 // Node-centred divergence of the cell field u (dm components, component-major), U = 0 in cells
-// outside non-periodic faces.
+// outside non-periodic faces.  Inflow faces (hg_multigrid's lo_inflow / hi_inflow,
+// Source/hg_multigrid.f90:191-204): the ghost cell just outside the face contributes the normal
+// component it carries, the inflow velocity on the wall, i.e. the flux through the face; its
+// tangential components move nothing out of the domain.  (FBoxLib's divu is not in the MAESTRO
+// tree; this is the finite-element divergence with the prescribed boundary flux.)
 void nodal_divu(const NCtx& C, const NLev& L, const double* u, double* out) {
     const int dm = C.dm;
     const size_t nc = L.ncells();
@@ -558,17 +569,33 @@ void nodal_divu(const NCtx& C, const NLev& L, const double* u, double* out) {
                 double s = 0.0;
                 for (int a = 0; a < (1 << dm); ++a) {
                     int c[3] = {0, 0, 0};
-                    bool out = false;
+                    int nout = 0, dout = -1, side = 0;
                     for (int d = 0; d < dm; ++d) {
-                        const int cw = cell_wrap(C, L, d, p[d] - ((a >> d) & 1));
-                        if (cw < 0) out = true;
+                        const int raw = p[d] - ((a >> d) & 1);
+                        const int cw = cell_wrap(C, L, d, raw);
+                        if (cw < 0) {
+                            ++nout;
+                            dout = d;
+                            side = raw < 0 ? 0 : 1;
+                        }
                         c[d] = cw;
                     }
-                    if (out) continue;
-                    const size_t ci = cidx3(L, c[0], c[1], c[2]);
-                    for (int d = 0; d < dm; ++d) {
-                        const double sgn = ((a >> d) & 1) ? -1.0 : 1.0;   // cell on the - side
-                        s += sgn * u[d * nc + ci] / L.h[d];
+                    if (nout == 0) {
+                        const size_t ci = cidx3(L, c[0], c[1], c[2]);
+                        for (int d = 0; d < dm; ++d) {
+                            const double sgn = ((a >> d) & 1) ? -1.0 : 1.0;   // cell on the - side
+                            s += sgn * u[d * nc + ci] / L.h[d];
+                        }
+                    } else if (nout == 1 && C.o.wall && C.o.wall_off[2 * dout + side] >= 0) {
+                        // index of the ghost cell within the face: the other directions in order
+                        size_t t = 0, stride = 1;
+                        for (int e = 0; e < dm; ++e) {
+                            if (e == dout) continue;
+                            t += stride * (size_t)c[e];
+                            stride *= (size_t)L.n[e];
+                        }
+                        const double sgn = ((a >> dout) & 1) ? -1.0 : 1.0;
+                        s += sgn * C.o.wall[C.o.wall_off[2 * dout + side] + t] / L.h[dout];
                     }
                 }
                 out[nidx(L, i, j, k)] = s / (1 << (dm - 1));

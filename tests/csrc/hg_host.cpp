@@ -117,6 +117,7 @@ struct HostExec : HostMg<double> {
     double* pi = nullptr;
     const double* b0 = nullptr;
     const double* nodalrhs = nullptr;
+    hg::Wall wall{nullptr, {-1, -1, -1, -1, -1, -1}};
     int alt = 0;
 
     void uvec() {
@@ -140,7 +141,7 @@ struct HostExec : HostMg<double> {
     }
     void divu() {
         for (long i = 0; i < nn(0); ++i)
-            hg::divu_node(geo, L[0], i, unew, b0, nodalrhs, buf(0, hg::kF));
+            hg::divu_node(geo, L[0], i, unew, b0, nodalrhs, wall, buf(0, hg::kF));
     }
     void update() {
         for (long i = 0; i < nc(0); ++i)
@@ -151,9 +152,19 @@ struct HostExec : HostMg<double> {
     }
 };
 
+// inflow faces of the next projection (hgh_set_wall)
+hg::Wall g_wall{nullptr, {-1, -1, -1, -1, -1, -1}};
+
 }  // namespace
 
 extern "C" {
+
+// Inflow faces for the following hgh_project* calls: off[f] >= 0 marks face f = 2 d + side as an
+// inflow face with its wall values at w + off[f] (hg::Wall); off NULL: none.
+void hgh_set_wall(const long* off, const double* w) {
+    g_wall.w = off ? w : nullptr;
+    for (int f = 0; f < 6; ++f) g_wall.off[f] = off ? off[f] : -1;
+}
 
 // The library's nodal projection on the host.  Geometry: dm, n[3], dx[3], per/dlo/dhi flags;
 // arrays as mac_hgproject_dense.  phi_out (nullable) receives the nodal solution.  stats_out:
@@ -212,6 +223,7 @@ int hgh_project_prec(int dm, const int* n, const double* dx, const int* per, con
     E.pi = pi;
     E.b0 = b0;
     E.nodalrhs = nodalrhs;
+    E.wall = g_wall;
     E.alt = (proj_type != hg::kInitial && proj_type != hg::kDivuIters && alt) ? 1 : 0;
     hg::SolveStats S{};
     const int rc = inner > 0

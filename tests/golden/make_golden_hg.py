@@ -10,7 +10,9 @@ discrete problem, written with numpy/scipy and sharing no code with the oracle:
                      the closed tensor-product form); sigma = 0 outside non-periodic faces
   * cross operator   sigma on each node-to-node edge = mean of the 2^(dm-1) cells along it
   * divergence       Docs/mg/mg.tex:485-493: (DU)_node = sum_d [mean of u_d over the cells on the
-                     + side - the same on the - side] / h_d, U = 0 outside non-periodic faces
+                     + side - the same on the - side] / h_d, U = 0 outside non-periodic faces;
+                     at an inflow face (hg_multigrid's lo_inflow / hi_inflow) the ghost cell
+                     outside adds the flux of its normal velocity (the inflow on the wall)
   * solve            sparse LU on the unknown nodes (periodic images identified, outflow nodes
                      fixed at 0), the mean of phi over the unknowns pinned for the singular problem
   * hgproject        Source/hgproject.f90:32-264 (create_uvec, beta0 scaling, alt energy fix,
@@ -164,15 +166,30 @@ def operator(N: Nodes, sigma, dense=True):
     return sp.csr_matrix((vals, (rows, cols)), shape=(N.nunk, N.nunk))
 
 
-def divu(N: Nodes, u):
-    """Node-centred divergence (storage nodes), U = 0 outside non-periodic faces."""
+def divu(N: Nodes, u, upad=None, inflow_lo=(0, 0, 0), inflow_hi=(0, 0, 0)):
+    """Node-centred divergence (storage nodes), U = 0 outside non-periodic faces, except at an
+    inflow face: there the ghost cell just outside (upad: U with one ghost layer, the inflow
+    velocity on the wall) adds its normal component's flux through the face."""
     dm = N.dm
     out = np.zeros(N.nshape)
     for p in itertools.product(*[range(m) for m in N.nshape]):
         s = 0.0
         for a in itertools.product((0, 1), repeat=dm):
-            cc = N.cell(tuple(p[d] - a[d] for d in range(dm)))
+            raw = tuple(p[d] - a[d] for d in range(dm))
+            cc = N.cell(raw)
             if cc is None:
+                if upad is None:
+                    continue
+                # outside through exactly one inflow face (edges and corners carry nothing)
+                out_dirs = [d for d in range(dm)
+                            if not N.per[d] and (raw[d] < 0 or raw[d] >= N.shape[d])]
+                if len(out_dirs) != 1:
+                    continue
+                d = out_dirs[0]
+                if not (inflow_lo[d] if raw[d] < 0 else inflow_hi[d]):
+                    continue
+                g = tuple((raw[e] % N.shape[e] if N.per[e] else raw[e]) + 1 for e in range(dm))
+                s += (-1.0 if a[d] else 1.0) * upad[g + (d,)] / N.dx[d]
                 continue
             for d in range(dm):
                 s += (-1.0 if a[d] else 1.0) * u[cc + (d,)] / N.dx[d]
@@ -219,13 +236,27 @@ def solve(N: Nodes, sigma, rh, dense=True):
 
 
 def reference_hgproject(unew, uold, gpi, rhohalf, pi, dx, bc_lo, bc_hi, proj_type, dt,
-                        beta0=None, nodalrhs=None, dense=True, alt_energy_fix=False):
-    """Source/hgproject.f90:32-264 on one level, whole-domain arrays."""
+                        beta0=None, nodalrhs=None, dense=True, alt_energy_fix=False,
+                        inflow=None):
+    """Source/hgproject.f90:32-264 on one level, whole-domain arrays.
+
+    inflow: dict(lo, hi, unew_pad, uold_pad, beta0_pad) -- inlet face flags and the fields with
+    one ghost layer (beta0_pad None: beta0_cart without ghosts).  The ghost layer goes through
+    create_uvec_for_projection as the reference's loops take it ((U - Uold) / dt on the first
+    ghost layer for the pressure iterations, unchanged otherwise; walls and symmetry zeroed, which
+    the divergence's U = 0 outside already is) and the beta0 scaling on beta0's ghost layer."""
     N = Nodes(rhohalf.shape, dx, bc_lo, bc_hi)
     dm = N.dm
     u = np.array(unew, dtype=np.float64)
     rho = np.array(rhohalf, dtype=np.float64)
     b0 = np.ones(rho.shape) if beta0 is None else np.asarray(beta0, dtype=np.float64)
+    upad = None
+    if inflow is not None:
+        upad = np.array(inflow["unew_pad"], dtype=np.float64)
+        if proj_type == HG_PRESSURE_ITERS:
+            upad = (upad - inflow["uold_pad"]) / dt
+        if inflow.get("beta0_pad") is not None:
+            upad = upad * np.asarray(inflow["beta0_pad"])[..., None]
     if proj_type == HG_PRESSURE_ITERS:
         u = (u - uold) / dt
     elif proj_type == HG_REGULAR:
@@ -235,7 +266,10 @@ def reference_hgproject(unew, uold, gpi, rhohalf, pi, dx, bc_lo, bc_hi, proj_typ
     rho = rho / b0
     if alt:
         rho = rho / b0
-    rh = divu(N, u)
+    if upad is None:
+        rh = divu(N, u)
+    else:
+        rh = divu(N, u, upad, inflow["lo"], inflow["hi"])
     if nodalrhs is not None:
         rh = rh - nodalrhs
     phi = solve(N, 1.0 / rho, rh, dense)
@@ -294,6 +328,49 @@ HG_CASES = {
 }
 
 
+# Inflow (inlet) faces: Neumann faces whose ghost cells carry the inflow velocity.
+HG_INFLOW_CASES = {
+    # 3-D dense, periodic x/y, inlet below / outflow above, regular time step; beta0_cart with a
+    # ghost layer (the ghost velocity is scaled by it)
+    "hg3d_inflow": dict(shape=(8, 8, 12), bc=((BC_PER, BC_PER, BC_NEU), (BC_PER, BC_PER, BC_DIR)),
+                        proj=HG_REGULAR, dense=True, alt=False, seed=14, lo=(0, 0, 1), hi=(0, 0, 0),
+                        b0_ghost=True),
+    # 2-D dense, inlet on the left / outflow on the right, walls in y, pressure iterations with
+    # the alt energy fix; beta0_cart without ghosts (the ghost velocity is not scaled)
+    "hg2d_inflow_piters": dict(shape=(16, 12), bc=((BC_NEU, BC_NEU), (BC_DIR, BC_NEU)),
+                               proj=HG_PRESSURE_ITERS, dense=True, alt=True, seed=15, lo=(1, 0, 0),
+                               hi=(0, 0, 0), b0_ghost=False),
+    # 2-D cross stencil, inlets on both y faces (no outflow: singular), the initial projection
+    "hg2d_inflow_cross": dict(shape=(12, 16), bc=((BC_PER, BC_NEU), (BC_PER, BC_NEU)),
+                              proj=HG_INITIAL, dense=False, alt=False, seed=16, lo=(0, 1, 0),
+                              hi=(0, 1, 0), b0_ghost=True),
+}
+
+
+def build_inflow_case(name):
+    """Inputs with one ghost layer: the valid region as make_hg_case draws it, ghost cells drawn
+    independently (the caller's boundary fill)."""
+    c = HG_INFLOW_CASES[name]
+    shape = c["shape"]
+    dm = len(shape)
+    dx = tuple(1.0 / shape[0] for _ in shape)
+    bc_lo, bc_hi = c["bc"]
+    inp = make_hg_case(shape, bc_lo, bc_hi, c["seed"])
+    rng = np.random.default_rng(c["seed"] + 100)
+    pshape = tuple(n + 2 for n in shape)
+    inner = tuple(slice(1, n + 1) for n in shape)
+    upad = 0.5 + rng.standard_normal(pshape + (dm,))
+    upad[inner] = inp["unew"]
+    uopad = rng.standard_normal(pshape + (dm,))
+    uopad[inner] = inp["uold"]
+    bpad = None
+    if c["b0_ghost"]:
+        bpad = 1.0 + 0.2 * rng.random(pshape)
+        bpad[inner] = inp["beta0"]
+    inflow = dict(lo=c["lo"], hi=c["hi"], unew_pad=upad, uold_pad=uopad, beta0_pad=bpad)
+    return c, shape, dx, bc_lo, bc_hi, inp, inflow
+
+
 def build_case(name):
     c = HG_CASES[name]
     shape = c["shape"]
@@ -317,6 +394,26 @@ def main():
                    proj=np.array(c["proj"]), dense=np.array(int(c["dense"])),
                    alt=np.array(int(c["alt"])), dt=np.array(dt), u_out=u, gpi_out=gpi,
                    pi_out=pi, phi_out=phi)
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **out)
+        print(path)
+    for name in HG_INFLOW_CASES:
+        c, shape, dx, bc_lo, bc_hi, inp, inflow = build_inflow_case(name)
+        dt = 0.01
+        u, gpi, pi, phi = reference_hgproject(inp["unew"], inp["uold"], inp["gpi"],
+                                              inp["rhohalf"], inp["pi"], dx, bc_lo, bc_hi,
+                                              c["proj"], dt, beta0=inp["beta0"],
+                                              nodalrhs=inp["nodalrhs"], dense=c["dense"],
+                                              alt_energy_fix=c["alt"], inflow=inflow)
+        out = {k: v for k, v in inp.items() if v is not None}
+        out.update(dx=np.array(dx), bc_lo=np.array(bc_lo), bc_hi=np.array(bc_hi),
+                   proj=np.array(c["proj"]), dense=np.array(int(c["dense"])),
+                   alt=np.array(int(c["alt"])), dt=np.array(dt), u_out=u, gpi_out=gpi,
+                   pi_out=pi, phi_out=phi, inflow_lo=np.array(c["lo"]),
+                   inflow_hi=np.array(c["hi"]), unew_pad=inflow["unew_pad"],
+                   uold_pad=inflow["uold_pad"])
+        if inflow["beta0_pad"] is not None:
+            out["beta0_pad"] = inflow["beta0_pad"]
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **out)
         print(path)

@@ -125,3 +125,115 @@ def test_hgproject_on_host_fabs(name):
         dpi = pi[b][sn] - ref_pi[b][sn]
         shift = dpi.flat[0] if shift is None else shift
         assert np.max(np.abs(dpi - shift)) <= 1e-9 * max(np.max(np.abs(c["pi_out"])), 1.0)
+
+
+def _pad_fabs(pad, boxes, ncomp=1):
+    """Per-box fabs with one ghost layer cut from a whole-domain array that has one."""
+    out = []
+    for lo, hi in boxes:
+        sl = tuple(slice(lo[d], hi[d] + 3) for d in range(len(lo)))
+        out.append(np.asfortranarray(pad[sl], dtype=np.float64))
+    return out
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", sorted(G.HG_INFLOW_CASES))
+def test_hgproject_inflow_dense_matches_golden(name, precision):
+    # inlet faces through mac_hgproject_dense_inflow (wall values on the device)
+    from tests.test_oracle_hg import check_against_golden, load_inflow
+    c = load_inflow(name)
+    shape = c["rhohalf"].shape
+    dm = len(shape)
+    dev = torch.device("cuda", 0)
+    t = lambda a: None if a is None else torch.from_numpy(  # noqa: E731
+        np.ascontiguousarray(np.asarray(a, dtype=np.float64).transpose())).to(dev)
+    tens = [t(c.get(k)) for k in ("unew", "uold", "gpi", "rhohalf", "pi", "beta0", "nodalrhs")]
+    wall = torch.from_numpy(np.ascontiguousarray(c["wall"])).to(dev)
+    ptr = lambda x: 0 if x is None else x.data_ptr()  # noqa: E731
+    P = MacProjector(Layout(shape, [((0,) * dm, tuple(v - 1 for v in shape))]), c["dx"],
+                     BcTower(c["bc_lo"], c["bc_hi"]), precision=precision,
+                     stream=torch.cuda.current_stream().cuda_stream,
+                     use_alt_energy_fix=int(c["alt"]))
+    try:
+        P.set_inflow(c["lo"], c["hi"])
+        # an inlet needs its wall values
+        with pytest.raises(MacError) as e:
+            P.hgproject_dense(int(c["proj"]), float(c["dt"]), *[ptr(x) for x in tens[:5]],
+                              strict=True)
+        assert e.value.code == capi.MAC_ERR_INVALID
+        st = P.hgproject_dense(int(c["proj"]), float(c["dt"]), *[ptr(x) for x in tens[:5]],
+                               beta0_cart=ptr(tens[5]) or None, nodalrhs=ptr(tens[6]) or None,
+                               dense_stencil=bool(c["dense"]), rel_eps=1e-13, strict=True,
+                               inflow_wall=wall.data_ptr())
+    finally:
+        P.close()
+    torch.cuda.synchronize()
+    back = lambda x: np.asfortranarray(x.cpu().numpy().transpose())  # noqa: E731
+    assert st["status"] == 0 and st["rel_resid"] <= 1e-13
+    check_against_golden(c, back(tens[0]), back(tens[2]), back(tens[4]), None)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", sorted(G.HG_INFLOW_CASES))
+def test_hgproject_inflow_on_host_fabs(name, precision):
+    # the drop-in form: the inflow velocity in the ghost cells of the caller's fabs (four boxes)
+    from tests.test_hg_host_exec import make_fabs
+    from tests.test_oracle_hg import check_against_golden, load_inflow
+    c = load_inflow(name)
+    shape = c["rhohalf"].shape
+    dm = len(shape)
+    per = [b == BC_PER for b in c["bc_lo"]]
+    lay = Layout.tiled(shape, tuple(v // 2 for v in shape))
+    boxes = lay.boxes
+    fab = lambda a, nodal, ncomp=1, ng=1: make_fabs(a, boxes, ng, nodal, per, ncomp)  # noqa: E731
+    unew = _pad_fabs(c["unew_pad"], boxes)
+    uold = _pad_fabs(c["uold_pad"], boxes)
+    gpi, rho = fab(c["gpi"], 0, dm), fab(c["rhohalf"], 0)
+    if "beta0_pad" in c:
+        b0, ng_b0 = _pad_fabs(c["beta0_pad"], boxes), 1
+    else:
+        b0, ng_b0 = fab(c["beta0"], 0, ng=0), 0
+    pi, nr = fab(c["pi"], 1), fab(c["nodalrhs"], 1)
+    P = MacProjector(lay, c["dx"], BcTower(c["bc_lo"], c["bc_hi"]), precision=precision,
+                     use_alt_energy_fix=int(c["alt"]))
+    try:
+        P.set_inflow(c["lo"], c["hi"])
+        st = P.hgproject(int(c["proj"]), float(c["dt"]), unew, uold, gpi, rho, pi, beta0_cart=b0,
+                         nodalrhs=nr, ng_b0=ng_b0, dense_stencil=bool(c["dense"]),
+                         rel_eps=1e-13, strict=True)
+    finally:
+        P.close()
+    assert st["status"] == 0
+    ref_u, ref_g, ref_pi = fab(c["u_out"], 0, dm), fab(c["gpi_out"], 0, dm), fab(c["pi_out"], 1)
+    su = np.max(np.abs(c["u_out"]))
+    sg = max(np.max(np.abs(c["gpi_out"])), np.max(np.abs(c["gpi"])))
+    shift = None
+    for b, (lo, hi) in enumerate(boxes):
+        sl = tuple(slice(1, 1 + hi[d] - lo[d] + 1) for d in range(dm))
+        sn = tuple(slice(1, 1 + hi[d] - lo[d] + 2) for d in range(dm))
+        assert np.max(np.abs(unew[b][sl] - ref_u[b][sl])) <= 1e-9 * su
+        assert np.max(np.abs(gpi[b][sl] - ref_g[b][sl])) <= 1e-9 * sg
+        dpi = pi[b][sn] - ref_pi[b][sn]
+        shift = dpi.flat[0] if shift is None else shift
+        assert np.max(np.abs(dpi - shift)) <= 1e-9 * max(np.max(np.abs(c["pi_out"])), 1.0)
+
+
+def test_inflow_arguments_are_checked():
+    shape = (8, 8)
+    dx = (1 / 8, 1 / 8)
+    lay = Layout(shape, [((0, 0), (7, 7))])
+    P = MacProjector(lay, dx, BcTower((BC_PER, BC_NEU), (BC_PER, BC_DIR)), precision="fp64")
+    try:
+        for lo, hi in (((1, 0), (0, 0)), ((0, 0), (0, 1)), ((0, 2), (0, 0))):
+            with pytest.raises(MacError) as e:   # periodic face, outflow face, bad flag
+                P.set_inflow(lo, hi)
+            assert e.value.code == capi.MAC_ERR_INVALID
+        P.set_inflow((0, 1), (0, 0))
+        z = [np.zeros((8, 8, 2), order="F")]
+        with pytest.raises(MacError) as e:   # fabs without the ghost layer the inlet needs
+            P.hgproject(O.HG_INITIAL, 1.0, z, None, z, [np.ones((8, 8), order="F")],
+                        [np.zeros((9, 9), order="F")], ng_u=0, ng_gp=0, ng_rho=0, ng_pi=0,
+                        strict=True)
+        assert e.value.code == capi.MAC_ERR_INVALID
+    finally:
+        P.close()

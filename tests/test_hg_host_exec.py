@@ -50,6 +50,8 @@ def host_lib(tmp_path_factory):
     L.hgh_project_prec.restype = ci
     L.hgh_fabs.argtypes = [ci, ip, ip, ci, ip, ci, ci, ci, ci, ctypes.POINTER(d), d]
     L.hgh_fabs.restype = None
+    L.hgh_set_wall.argtypes = [ctypes.POINTER(ctypes.c_long), d]
+    L.hgh_set_wall.restype = None
     return L
 
 
@@ -197,3 +199,26 @@ def test_node_row_reproduces_node_op(host_lib, dm, n, per, dlo, dhi, dense):
     dx = (ctypes.c_double * 3)(*([0.5, 0.25, 0.125][:dm] + [1.0] * (3 - dm)))
     err = L.hgh_row_check(dm, ia(n), dx, ia(per), ia(dlo), ia(dhi), dense, 7)
     assert err <= 1e-14, err
+
+
+@pytest.mark.parametrize("inner", [0, 2])
+@pytest.mark.parametrize("name", sorted(G.HG_INFLOW_CASES))
+def test_library_hg_code_on_host_inflow_matches_golden(host_lib, name, inner):
+    # inlet faces: the library's divergence with the wall values of the ghost cells
+    from tests.test_oracle_hg import check_against_golden, load_inflow
+    c = load_inflow(name)
+    shape = c["rhohalf"].shape
+    off, _ = O.hg_wall_layout(shape, c["lo"], c["hi"])
+    wall = np.ascontiguousarray(c["wall"])
+    host_lib.hgh_set_wall((ctypes.c_long * 6)(*off),
+                          wall.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    try:
+        rc, u, gpi, pi, phi, st = run_host(host_lib, shape, c["dx"], c["bc_lo"], c["bc_hi"],
+                                           int(c["proj"]), float(c["dt"]), c["unew"], c["uold"],
+                                           c["gpi"], c["rhohalf"], c["pi"], b0=c.get("beta0"),
+                                           nodalrhs=c.get("nodalrhs"), dense=bool(c["dense"]),
+                                           alt=bool(c["alt"]), inner=inner)
+    finally:
+        host_lib.hgh_set_wall(None, None)
+    assert rc == 0 and st[2] <= 1e-13, st
+    check_against_golden(c, u, gpi, pi, phi)

@@ -132,3 +132,76 @@ def test_solve_reaches_maestro_tolerance_and_matches_direct_solve(dense):
     m = N.uid >= 0
     a, b = phi[m] - phi[m].mean(), ref[m] - ref[m].mean()
     assert np.max(np.abs(a - b)) <= 1e-8 * np.max(np.abs(b))
+
+
+def load_inflow(name):
+    c = load_hg(name)
+    c["lo"] = tuple(int(v) for v in c["inflow_lo"])
+    c["hi"] = tuple(int(v) for v in c["inflow_hi"])
+    c["wall"] = O.hg_wall_from_ghosts(c["rhohalf"].shape, c["lo"], c["hi"], int(c["proj"]),
+                                      float(c["dt"]), c["unew_pad"], c["uold_pad"],
+                                      c.get("beta0_pad"))
+    return c
+
+
+def check_against_golden(c, u, gpi, pi, phi):
+    """phi (mean-free when singular), U, gpi within 1e-9 of the direct solve; pi up to phi's
+    constant."""
+    shape = c["rhohalf"].shape
+    m = _unknown_mask(shape, c["dx"], c["bc_lo"], c["bc_hi"])
+    if phi is not None:
+        a, b = phi[m], c["phi_out"][m]
+        if BC_DIR not in c["bc_lo"] + c["bc_hi"]:
+            a, b = a - a.mean(), b - b.mean()
+        assert np.max(np.abs(a - b)) <= 1e-9 * np.max(np.abs(b))
+    assert np.max(np.abs(u - c["u_out"])) <= 1e-9 * np.max(np.abs(c["u_out"]))
+    assert np.max(np.abs(gpi - c["gpi_out"])) <= 1e-9 * max(np.max(np.abs(c["gpi_out"])),
+                                                             np.max(np.abs(c["gpi"])))
+    assert np.ptp((pi - c["pi_out"])[m]) <= 1e-9 * max(np.max(np.abs(c["pi_out"])), 1.0)
+
+
+@pytest.mark.parametrize("name", sorted(G.HG_INFLOW_CASES))
+def test_oracle_hgproject_inflow_matches_golden(name):
+    c = load_inflow(name)
+    kw = dict(proj_type=int(c["proj"]), dt=float(c["dt"]), beta0_cart=c.get("beta0"),
+              nodalrhs=c.get("nodalrhs"), dense=bool(c["dense"]),
+              alt_energy_fix=bool(c["alt"]), rel_eps=1e-13)
+    args = (c["unew"], c["uold"], c["gpi"], c["rhohalf"], c["pi"], c["dx"], c["bc_lo"],
+            c["bc_hi"])
+    u, gpi, pi, phi, st = O.hgproject(*args, inflow_lo=c["lo"], inflow_hi=c["hi"],
+                                      wall=c["wall"], **kw)
+    assert st["status"] == 0
+    check_against_golden(c, u, gpi, pi, phi)
+    # the inlets matter: without them U is far from the golden one
+    u0, _, _, _, _ = O.hgproject(*args, **kw)
+    assert np.max(np.abs(u0 - c["u_out"])) > 1e-3 * np.max(np.abs(c["u_out"]))
+
+
+@pytest.mark.parametrize("shape,bc_lo,bc_hi,lo,hi", [
+    ((6, 8, 5), (BC_PER, BC_NEU, BC_NEU), (BC_PER, BC_NEU, BC_DIR), (0, 1, 1), (0, 1, 0)),
+    ((7, 6), (BC_NEU, BC_NEU), (BC_NEU, BC_DIR), (1, 1), (1, 0)),
+])
+def test_inflow_divergence_matches_assembly(shape, bc_lo, bc_hi, lo, hi):
+    # the oracle's inflow divergence (via a projection's right-hand side: L phi = DU) against
+    # the fixture script's ghost-cell divergence, anisotropic spacing, several inlets at once
+    rng = np.random.default_rng(9)
+    dm = len(shape)
+    dx = tuple(1.0 / (n + 2) for n in shape)
+    upad = rng.standard_normal(tuple(n + 2 for n in shape) + (dm,))
+    inner = tuple(slice(1, n + 1) for n in shape)
+    u = upad[inner]
+    N = G.Nodes(shape, dx, bc_lo, bc_hi)
+    ref = G.divu(N, u, upad, lo, hi)
+    wall = O.hg_wall_from_ghosts(shape, lo, hi, O.HG_INITIAL, 1.0, upad)
+    # the divergence of the initial projection is L phi on the unknown nodes
+    rho = np.ones(shape)
+    _, _, _, phi, st = O.hgproject(u, u, np.zeros_like(u), rho, np.zeros(N.nshape), dx, bc_lo,
+                                   bc_hi, proj_type=O.HG_INITIAL, dense=True, rel_eps=1e-13,
+                                   inflow_lo=lo, inflow_hi=hi, wall=wall)
+    assert st["status"] == 0
+    Lphi = O.hg_apply(1.0 / rho, phi, dx, bc_lo, bc_hi, dense=True)
+    m = N.uid >= 0
+    r = ref[m]
+    if BC_DIR not in bc_lo + bc_hi:
+        r = r - r.mean()
+    assert np.max(np.abs(Lphi[m] - r)) <= 1e-10 * np.max(np.abs(r))
