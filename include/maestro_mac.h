@@ -301,8 +301,12 @@ int mac_macproject_ml_dense(mac_ctx* ctx, double* const* umac, double* const* ph
  *   macrhs : per level, one cell fab per box, ng_rhs ghosts, or NULL
  *   beta0 / beta0_edge : the levels' planar base states one after the other (n_l and n_l + 1
  *            values, n_l = the level's vertical extent), or both NULL
- * Ghost faces and ghost cells of the fabs are left as they came in (the reference refills them
- * after the projection with create_umac_grown / multifab_fill_boundary).  Along a periodic
+ * After the projection the fine levels' ghost faces (ng_u >= 1) are filled as create_umac_grown
+ * fills them (Source/macproject.f90:264-272): a ghost face bordering a cell of the level (another
+ * box, periodic images) takes the level's value, any other the coarser level's -- piecewise
+ * constant across the face, linear along its normal.  Ghost faces beyond a non-periodic domain
+ * face (multifab_physbc_edgevel), level 0's ghost faces and all ghost cells of phi are left as
+ * they came in.  Along a periodic
  * direction a domain face is read from the box that owns it (a box at the low end owns face 0,
  * one at the high end face n_l); where only one end has a box, that copy stands for both.
  */

@@ -261,6 +261,15 @@ __global__ void k_fabs_scatter(Geo G, Lev L, int dir, const amr::FabDesc* T, con
         amr::fab_scatter_elem(G, L, dir, B, e, level);
 }
 
+// create_umac_grown: the ghost faces of fine level F's face fabs from F and the next coarser C.
+__global__ void k_fabs_grow(Geo G, Lev F, Lev C, int dir, const amr::FabDesc* T, const double* uf,
+                            const double* uc) {
+    const amr::FabDesc B = T[blockIdx.y];
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < B.count;
+         e += (long)gridDim.x * blockDim.x)
+        amr::fab_grow_elem(G, F, C, dir, B, e, uf, uc);
+}
+
 inline int blocks_for(long n, int sms) {
     const long b = (n + kThreads - 1) / kThreads;
     const long cap = (long)std::max(1, sms) * 16;
@@ -1065,6 +1074,15 @@ int ml_fabs(mac_ctx* c, int ptr_kind, double* const* umac, int ng_u, double* con
                                                             A->d_tab + tab_u[3 * l + d], A->F[l].u[d]);
             MAC_CUDA_TRY(cudaGetLastError());
             ++c->issued;
+            // the fine levels' ghost faces, as create_umac_grown fills them after the projection
+            // (Source/macproject.f90:264-272; the coarsest level's ghosts are left alone there)
+            if (l >= 1 && ng_u >= 1) {
+                k_fabs_grow<<<grid, kThreads, 0, c->stream>>>(A->geo, A->L[l].lev, A->L[l - 1].lev, d,
+                                                             A->d_tab + tab_u[3 * l + d], A->F[l].u[d],
+                                                             A->F[l - 1].u[d]);
+                MAC_CUDA_TRY(cudaGetLastError());
+                ++c->issued;
+            }
         }
         const dim3 grid((unsigned)std::min<long>((maxp + kThreads - 1) / kThreads, 1024), (unsigned)nb);
         k_fabs_scatter<<<grid, kThreads, 0, c->stream>>>(A->geo, A->L[l].lev, -1,

@@ -607,6 +607,85 @@ AMR_HD inline void fab_scatter_elem(const Geo& G, const Lev& L, int dir, const F
     if (fab_elem(G, L, dir, B, e, &t) == 1) B.dst[e] = level[t];
 }
 
+// create_umac_grown (Source/macproject.f90:264-272; the routine is FBoxLib's and not in the
+// MAESTRO tree, so it is written here from what it is for): after the projection a fine level's
+// edge velocities in the ghost faces of its fabs come from the level itself where the face
+// borders one of the level's cells (a neighbouring box's face, periodic images wrapped: the
+// fill_boundary the routine ends with), else from the coarser level -- piecewise constant
+// across the face, linear along its normal: a fine face on a coarse face plane takes that
+// coarse face's value, one between two coarse planes their mean.  g: the ghost face (index
+// along dir, cells along the other directions) in the fine level's domain.  Returns false for
+// a face beyond a non-periodic domain face (the caller's physical-boundary fill) and leaves
+// *out alone.
+AMR_HD inline bool grow_face(const Geo& G, const Lev& F, const Lev& C, int dir, const int g_in[3],
+                             const double* uf, const double* uc, double* out) {
+    int g[3] = {g_in[0], g_in[1], g_in[2]};
+    for (int d = 0; d < G.dm; ++d) {
+        const int n = F.n[d];
+        if (d == dir) {   // faces 0 .. n
+            if (g[d] < 0 || g[d] > n) {
+                if (!G.per[d]) return false;
+                g[d] += g[d] < 0 ? n : -n;
+            }
+        } else {
+            const int q = wrap(G, F, d, g[d]);
+            if (q < 0) return false;
+            g[d] = q;
+        }
+    }
+    // the two cells the face separates, when they exist
+    const int n = F.n[dir];
+    bool own = false;
+    for (int s = 0; s < 2 && !own; ++s) {
+        int cc[3] = {g[0], g[1], g[2]};
+        cc[dir] = g[dir] - 1 + s;
+        if (cc[dir] < 0 || cc[dir] >= n) {
+            if (!G.per[dir]) continue;
+            cc[dir] += cc[dir] < 0 ? n : -n;
+        }
+        own = inside(F, cc) && (F.mask[cix(F, cc[0], cc[1], cc[2])] & kIn);
+    }
+    if (own) {
+        if (!inside_face(F, dir, g)) return false;
+        *out = uf[fix(F, dir, g[0], g[1], g[2])];
+        return true;
+    }
+    int c[3] = {g[0] >> 1, g[1] >> 1, g[2] >> 1};
+    if ((g[dir] & 1) == 0) {
+        c[dir] = g[dir] >> 1;
+        if (!inside_face(C, dir, c)) return false;
+        *out = uc[fix(C, dir, c[0], c[1], c[2])];
+        return true;
+    }
+    int c1[3] = {c[0], c[1], c[2]};
+    c[dir] = (g[dir] - 1) >> 1;
+    c1[dir] = (g[dir] + 1) >> 1;
+    if (!inside_face(C, dir, c) || !inside_face(C, dir, c1)) return false;
+    *out = 0.5 * (uc[fix(C, dir, c[0], c[1], c[2])] + uc[fix(C, dir, c1[0], c1[1], c1[2])]);
+    return true;
+}
+
+// The ghost faces of element e of face fab B (dir) by grow_face; the box's own faces and faces
+// beyond a non-periodic domain face are left alone.
+AMR_HD inline void fab_grow_elem(const Geo& G, const Lev& F, const Lev& C, int dir,
+                                 const FabDesc& B, long e, const double* uf, const double* uc) {
+    int a[3];
+    a[0] = (int)(e % B.ext[0]);
+    const long r = e / B.ext[0];
+    a[1] = (int)(r % B.ext[1]);
+    a[2] = (int)(r / B.ext[1]);
+    int g[3] = {0, 0, 0};
+    bool interior = true;
+    for (int d = 0; d < G.dm; ++d) {
+        g[d] = B.lo[d] - B.ng + a[d];
+        const int top = B.hi[d] + (dir == d ? 1 : 0);
+        if (g[d] < B.lo[d] || g[d] > top) interior = false;
+    }
+    if (interior) return;
+    double v;
+    if (grow_face(G, F, C, dir, g, uf, uc, &v)) B.dst[e] = v;
+}
+
 // ---- the multi-level cycle and the projection steps -------------------------------------------
 //
 // E provides, for levels l = 0 .. nlev-1 (arrays are E's own memory):

@@ -503,6 +503,58 @@ def macproject_ml(umac, phi, rho, dx, bc_lo, bc_hi, boxes, macrhs=None, beta0=No
     return u, phi, st.as_dict()
 
 
+def create_umac_grown_fab(uf, uc, inm, d, lo, hi, ng, per):
+    """create_umac_grown (Source/macproject.f90:264-272) for one face fab of a fine level.
+
+    FBoxLib's routine is not in the MAESTRO tree; restated from its purpose: a ghost face that
+    borders a cell of the fine level (inm: its cell mask over the level domain; periodic images
+    wrapped) takes the fine level's value uf (the fill_boundary it ends with), any other ghost
+    face the coarse level's uc after the edge restriction -- piecewise constant across the face,
+    linear along its normal (mean of the two coarse faces around a fine face between coarse
+    planes).  uf, uc: whole-level face arrays normal to d.  Returns the fab (box lo..hi, ng
+    ghosts) with those ghost faces filled; NaN on the box's own faces and beyond a non-periodic
+    domain face (the caller's physical-boundary fill)."""
+    dm = len(lo)
+    n = inm.shape
+    shape = tuple(hi[e] - lo[e] + 1 + 2 * ng + (1 if e == d else 0) for e in range(dm))
+    out = np.full(shape, np.nan)
+    for a in np.ndindex(*shape):
+        g = [lo[e] - ng + a[e] for e in range(dm)]
+        if all(lo[e] <= g[e] <= hi[e] + (1 if e == d else 0) for e in range(dm)):
+            continue
+        ok = True
+        for e in range(dm):
+            top = n[e] if e == d else n[e] - 1
+            if g[e] < 0 or g[e] > top:
+                if not per[e]:
+                    ok = False
+                    break
+                g[e] = g[e] + n[e] if g[e] < 0 else g[e] - n[e]
+        if not ok:
+            continue
+        own = False
+        for s in (0, 1):
+            cc = list(g)
+            cc[d] = g[d] - 1 + s
+            if cc[d] < 0 or cc[d] >= n[d]:
+                if not per[d]:
+                    continue
+                cc[d] %= n[d]
+            own = own or bool(inm[tuple(cc)])
+        if own:
+            out[a] = uf[tuple(g)]
+            continue
+        c = [v // 2 for v in g]
+        if g[d] % 2 == 0:
+            c[d] = g[d] // 2
+            out[a] = uc[tuple(c)]
+        else:
+            c0, c1 = list(c), list(c)
+            c0[d], c1[d] = (g[d] - 1) // 2, (g[d] + 1) // 2
+            out[a] = 0.5 * (uc[tuple(c0)] + uc[tuple(c1)])
+    return out
+
+
 # ------------------------------------------------------------------------- nodal (HG) projection
 
 # proj_type values (Source/proj_parameters.f90)

@@ -86,10 +86,12 @@ def test_amr_layout_and_density_errors():
     assert e.value.code == capi.MAC_ERR_BAD_DENSITY
 
 
-@pytest.mark.parametrize("name", ["amr2d_wrap", "amr3d_16", "amr3d_3lev"])
+@pytest.mark.parametrize("name", ["amr2d_32", "amr2d_outflow", "amr2d_wrap", "amr3d_16",
+                                  "amr3d_3lev"])
 def test_amr_projection_on_host_fabs(name):
     # the drop-in form: per-box host fabs of every level (several boxes on level 0 too), rho with
-    # two ghost cells, umac with one
+    # two ghost cells, umac with one (the fine levels' ghost faces filled as create_umac_grown
+    # fills them)
     c = load_amr(name)
     H = G.Hierarchy(c["n0"], c["dx0"], c["bc_lo"], c["bc_hi"], c["boxes"])
     dm = c["dm"]
@@ -127,3 +129,11 @@ def test_amr_projection_on_host_fabs(name):
                 slu = tuple(slice(1, 1 + hi[e] - lo[e] + 1 + (1 if e == d else 0)) for e in range(dm))
                 den = np.max(np.abs(c["unew"][l][d][G.face_member(H, l, d)]))
                 assert np.max(np.abs(umac[l][d][b][slu] - ref_u[slu])) <= 1e-9 * den
+                if l == 0:
+                    continue
+                # create_umac_grown: the fine fabs' ghost faces inside the domain
+                exp = O.create_umac_grown_fab(c["unew"][l][d], c["unew"][l - 1][d], H.inm[l], d,
+                                              lo, hi, 1, per)
+                m = ~np.isnan(exp)
+                assert m.any()
+                assert np.max(np.abs(umac[l][d][b][m] - exp[m])) <= 1e-9 * den
