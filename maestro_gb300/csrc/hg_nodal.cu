@@ -19,7 +19,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kReduceBlocks = 1024;
-constexpr int kMixedInner = 2;   // FP32 V-cycles per FP64 refinement step of the mixed solve
+constexpr int kMixedInner = 3;   // FP32 V-cycles per FP64 refinement step of the mixed solve
 
 #define HG_LOOP(N) for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < (N); \
                         idx += (long)gridDim.x * blockDim.x)
