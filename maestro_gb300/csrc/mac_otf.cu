@@ -238,10 +238,40 @@ k_gsrb_otf_staged(Dims d, OtfParams P, int colour, float* __restrict__ es,
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    pdl_wait();
-    pdl_trigger();
 
-    // thread 0: copy plane q into stage q % kStages
+    // thread 0: copy plane q into stage q % kStages.  Part 1: the densities of both colours,
+    // with the expected bytes of the whole stage; part 2: the other colour's e and the own
+    // right-hand side.  The FP32 densities are written by the setup only, launches before any
+    // half-sweep, so part 1 of the first planes goes out before the launch-dependency wait and
+    // overlaps the end of the previous launch; the previous launch may have written part 2.
+    auto issue_part = [&](int q, int part) {
+        const int sidx = q % kStages;
+        int p = k0 - 1 + q;
+        p += (p < 0) ? n2 : 0;
+        p -= (p >= n2) ? n2 : 0;
+        float* st = sm + sidx * stage;
+        const uint32_t bar = smem_addr(&bars[sidx]);
+        if (part == 1) mbar_expect_tx(bar, (uint32_t)stage * 4u);
+        const long pb = (long)p * plane;
+        const float* rows = part == 1 ? rhoo : eo;
+        float* dst = part == 1 ? st + oth : st;
+        int slot = 0;
+        while (slot < TY + 2) {
+            int row = j0 - 1 + slot;
+            row += (row < 0) ? n1 : 0;
+            row -= (row >= n1) ? n1 : 0;
+            const int len = min(TY + 2 - slot, n1 - row);
+            const uint32_t bytes = (uint32_t)(len * hn0) * 4u;
+            bulk_g2s(smem_addr(dst + slot * hn0), rows + pb + (long)row * hn0, bytes, bar);
+            slot += len;
+        }
+        if (part == 1)
+            bulk_g2s(smem_addr(st + 2 * oth + own), rhos + pb + (long)j0 * hn0,
+                     (uint32_t)own * 4u, bar);
+        else
+            bulk_g2s(smem_addr(st + 2 * oth), rs + pb + (long)j0 * hn0, (uint32_t)own * 4u, bar);
+    };
+    // the refills: the whole stage, each row's e and density copies issued together
     auto issue = [&](int q) {
         const int sidx = q % kStages;
         int p = k0 - 1 + q;
@@ -268,8 +298,13 @@ k_gsrb_otf_staged(Dims d, OtfParams P, int colour, float* __restrict__ es,
     };
     int issued = 0;      // planes issued so far (thread 0)
     int confirmed = 0;   // planes whose copies thread 0 has seen complete
+    const int first = min(kStages, nq);
+    if (t == 0)
+        for (int q = 0; q < first; ++q) issue_part(q, 1);
+    pdl_wait();
+    pdl_trigger();
     if (t == 0) {
-        for (; issued < min(kStages, nq); ++issued) issue(issued);
+        for (; issued < first; ++issued) issue_part(issued, 2);
     }
     // thread 0 waits for plane q; the __syncthreads that follows every call publishes the
     // stage (and a failed wait) to the other threads, which do not poll the barrier
