@@ -234,6 +234,208 @@ __global__ void k_hg_gs3(hg::Geo G, hg::LevT<T> L, int colour, T* phi, const T* 
 // (global writes of a block are visible to the block after the barrier): bitwise the update
 // sequence of the 2^(dm-1) global colour launches it replaces, reading the level's phi and sigma
 // about once per half instead of once per colour.
+// ---- tiled Gauss-Seidel of the fine 3-D dense levels -------------------------------------------
+// A sweep in two launches (slab parity sp = 0, then 1) instead of eight colour launches.  The
+// colours p_0 + 2 p_1 + 4 p_2 of one slab parity are the four in-slab colours of the slabs of that
+// parity, and a node's z-neighbours lie in slabs of the other parity, which the launch does not
+// change.  A block owns a kTileX x kTileY tile of one slab: it stages in shared memory the slab
+// and its two neighbour slabs over the tile grown by kTileH nodes, the cell coefficients of the
+// two cell layers around the slab and the right-hand side, then runs the four colours in order
+// on the tile grown by 3, 2, 1, 0 nodes (recomputing its neighbours' share of the ring, so the
+// tile's nodes see exactly the values the global colour order gives them) and writes the tile.
+// Reads come from src (the slab itself and, in the first launch, its neighbours) and srcnb (the
+// neighbour slabs), writes go to dst != src: the caller alternates two arrays (the first launch
+// reads and leaves src, the second reads the new even slabs from dst).  Node and cell indices
+// fold through the periodic wrap when staged; outside a non-periodic face the staged values are
+// 0.  Each node takes node_op_dense3's arithmetic when interior3, node_op_dense3_face's
+// otherwise, so the results are bitwise those of the colour launches.
+// One element global -> shared without passing through registers (cp.async, 4 or 8 bytes);
+// inside = false writes 0 (zero-fill: nothing is read from src).
+template <typename T>
+__device__ __forceinline__ void stage_elem(T* dst, const T* src, bool inside) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if (sizeof(T) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src),
+                     "r"(inside ? 8 : 0) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src),
+                     "r"(inside ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+constexpr int kTileX = 32, kTileY = 32, kTileH = 4, kTileThreads = 256;
+constexpr int kTRX = kTileX + 2 * kTileH, kTRY = kTileY + 2 * kTileH;           // staged nodes
+constexpr int kTCX = kTileX + 2 * kTileH - 1, kTCY = kTileY + 2 * kTileH - 1;   // staged cells
+constexpr int kTFX = kTileX + 2 * kTileH - 2, kTFY = kTileY + 2 * kTileH - 2;   // right-hand side
+template <typename T>
+constexpr size_t tile_smem() {
+    return sizeof(T) * (3 * kTRX * kTRY + 2 * kTCX * kTCY + kTFX * kTFY);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kTileThreads)
+k_hg_gs_tile(hg::Geo G, hg::LevT<T> L, int sp, int ntx, const T* __restrict__ src,
+             const T* __restrict__ srcnb, T* __restrict__ dst, const T* __restrict__ f) {
+    extern __shared__ __align__(16) unsigned char hg_tile_smem[];
+    T* sphi = reinterpret_cast<T*>(hg_tile_smem);   // [3][kTRY][kTRX], slabs z-1, z, z+1
+    T* ssig = sphi + 3 * kTRX * kTRY;                // [2][kTCY][kTCX], cell layers z-1, z
+    T* sf = ssig + 2 * kTCX * kTCY;                  // [kTFY][kTFX]
+    const int z = 2 * (int)blockIdx.y + sp;
+    const int nzu = G.per[2] ? L.n[2] : L.n[2] + 1;  // slabs with unknown nodes
+    if (z >= nzu) return;
+    const int x0 = kTileX * ((int)blockIdx.x % ntx), y0 = kTileY * ((int)blockIdx.x / ntx);
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    // per staged column / row: folded node and cell coordinates (-1: outside a non-periodic
+    // face), whether the folded node is an unknown along that direction, whether the raw node
+    // is interior (one node or more from both faces) along it
+    __shared__ int sqx[kTRX], sqy[kTRY], scx[kTCX], scy[kTCY];
+    __shared__ unsigned char sux[kTRX], suy[kTRY], six[kTRX], siy[kTRY];
+    if (t < kTRX) {
+        const int raw = x0 - kTileH + t;
+        const int q = hg::node_wrap(G, L, 0, raw);
+        sqx[t] = q;
+        sux[t] = q >= 0 && !(G.per[0] ? q == L.n[0] : ((q == 0 && G.dlo[0]) || (q == L.n[0] && G.dhi[0])));
+        six[t] = raw >= 1 && raw <= L.n[0] - 2;
+        if (t < kTCX) scx[t] = hg::cell_wrap(G, L, 0, raw);
+    } else if (t >= 64 && t < 64 + kTRY) {
+        const int u = t - 64, raw = y0 - kTileH + u;
+        const int q = hg::node_wrap(G, L, 1, raw);
+        sqy[u] = q;
+        suy[u] = q >= 0 && !(G.per[1] ? q == L.n[1] : ((q == 0 && G.dlo[1]) || (q == L.n[1] && G.dhi[1])));
+        siy[u] = raw >= 1 && raw <= L.n[1] - 2;
+        if (u < kTCY) scy[u] = hg::cell_wrap(G, L, 1, raw);
+    }
+    // (scalars, not arrays: a dynamically indexed array would live in local memory)
+    const int qz0 = hg::node_wrap(G, L, 2, z - 1), qz1 = hg::node_wrap(G, L, 2, z),
+              qz2 = hg::node_wrap(G, L, 2, z + 1);
+    const int cz0 = hg::cell_wrap(G, L, 2, z - 1), cz1 = hg::cell_wrap(G, L, 2, z);
+    const bool uz = qz1 >= 0 &&
+                    !(G.per[2] ? qz1 == L.n[2] : ((qz1 == 0 && G.dlo[2]) || (qz1 == L.n[2] && G.dhi[2])));
+    const bool iz = z >= 1 && z <= L.n[2] - 2;
+    __syncthreads();
+    const long m0 = L.nn[0], m01 = (long)L.nn[0] * L.nn[1];
+    const long c0s = L.n[0], c01 = (long)L.n[0] * L.n[1];
+    // stage: nodes x0 - kTileH .. x0 + kTileX + kTileH - 1 (same in y), slabs z - 1 .. z + 1,
+    // the two cell layers and the right-hand side, all copies in flight at once
+    for (int e = t; e < 3 * kTRX * kTRY; e += kTileThreads) {
+        const int lx = e % kTRX, row = e / kTRX, ly = row % kTRY, lz = row / kTRY;
+        const int q0 = sqx[lx], q1 = sqy[ly], q2 = lz == 0 ? qz0 : (lz == 1 ? qz1 : qz2);
+        const bool in = q0 >= 0 && q1 >= 0 && q2 >= 0;
+        const T* from = lz == 1 ? src : srcnb;
+        stage_elem(sphi + e, in ? from + (q0 + q1 * m0 + q2 * m01) : from, in);
+    }
+    for (int e = t; e < 2 * kTCX * kTCY; e += kTileThreads) {
+        const int lx = e % kTCX, row = e / kTCX, ly = row % kTCY, lz = row / kTCY;
+        const int c0 = scx[lx], c1 = scy[ly], c2 = lz == 0 ? cz0 : cz1;
+        const bool in = c0 >= 0 && c1 >= 0 && c2 >= 0;
+        stage_elem(ssig + e, in ? L.sig + (c0 + c1 * c0s + c2 * c01) : L.sig, in);
+    }
+    for (int e = t; e < kTFX * kTFY; e += kTileThreads) {
+        const int lx = e % kTFX, ly = e / kTFX;
+        const int q0 = sqx[lx + 1], q1 = sqy[ly + 1], q2 = qz1;
+        const bool in = q0 >= 0 && q1 >= 0 && q2 >= 0;
+        stage_elem(sf + e, in ? f + (q0 + q1 * m0 + q2 * m01) : f, in);
+    }
+    stage_wait();
+    __syncthreads();
+    // the four in-slab colours, on the tile grown by 3, 2, 1, 0 nodes
+#pragma unroll 1
+    for (int k = 0; k < 4; ++k) {
+        const int h = 3 - k, px = k & 1, py = k >> 1;
+        const int xs = x0 - h + ((px - (x0 - h)) & 1), ys = y0 - h + ((py - (y0 - h)) & 1);
+        const int nx = (x0 + kTileX - 1 + h - xs) / 2 + 1, ny = (y0 + kTileY - 1 + h - ys) / 2 + 1;
+        for (int e = t; e < nx * ny; e += kTileThreads) {
+            const int lx = xs - (x0 - kTileH) + 2 * (e % nx), ly = ys - (y0 - kTileH) + 2 * (e / nx);
+            if (!(sux[lx] && suy[ly] && uz)) continue;
+            T s[2][2][2];
+#pragma unroll
+            for (int zz = 0; zz < 2; ++zz)
+#pragma unroll
+                for (int yy = 0; yy < 2; ++yy)
+#pragma unroll
+                    for (int xx = 0; xx < 2; ++xx)
+                        s[zz][yy][xx] = ssig[(lx - 1 + xx) + kTCX * ((ly - 1 + yy) + kTCY * zz)];
+            T sx[2][2][3];
+#pragma unroll
+            for (int zz = 0; zz < 2; ++zz)
+#pragma unroll
+                for (int yy = 0; yy < 2; ++yy) {
+                    sx[zz][yy][0] = s[zz][yy][0];
+                    sx[zz][yy][1] = s[zz][yy][0] + s[zz][yy][1];
+                    sx[zz][yy][2] = s[zz][yy][1];
+                }
+            T sxy[2][3][3];
+#pragma unroll
+            for (int zz = 0; zz < 2; ++zz)
+#pragma unroll
+                for (int ox = 0; ox < 3; ++ox) {
+                    sxy[zz][0][ox] = sx[zz][0][ox];
+                    sxy[zz][1][ox] = sx[zz][0][ox] + sx[zz][1][ox];
+                    sxy[zz][2][ox] = sx[zz][1][ox];
+                }
+            const T* ph = sphi + (lx - 1) + kTRX * (ly - 1);
+            T dg, off;
+            if (six[lx] && siy[ly] && iz) {
+                // node_op_dense3's order: the neighbours summed per weight class, then kw
+                T am[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                T centre = 0;
+#pragma unroll
+                for (int oz = 0; oz < 3; ++oz)
+#pragma unroll
+                    for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+                        for (int ox = 0; ox < 3; ++ox) {
+                            const T S = oz == 0 ? sxy[0][oy][ox]
+                                                : (oz == 2 ? sxy[1][oy][ox]
+                                                           : sxy[0][oy][ox] + sxy[1][oy][ox]);
+                            const int mask = (ox != 1 ? 1 : 0) | (oy != 1 ? 2 : 0) | (oz != 1 ? 4 : 0);
+                            if (mask == 0)
+                                centre = S;
+                            else
+                                am[mask] = fma(S, ph[ox + kTRX * (oy + kTRY * oz)], am[mask]);
+                        }
+                T acc = 0;
+#pragma unroll
+                for (int m = 1; m < 8; ++m) acc = fma(L.kw[m], am[m], acc);
+                dg = -L.kw[0] * centre;
+                off = acc;
+            } else {
+                // node_op_dense3_face's order: each neighbour weighted, then accumulated (a
+                // missing neighbour carries weight 0 and a staged 0)
+                T acc = 0, centre = 0;
+#pragma unroll
+                for (int oz = 0; oz < 3; ++oz)
+#pragma unroll
+                    for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+                        for (int ox = 0; ox < 3; ++ox) {
+                            const T S = oz == 0 ? sxy[0][oy][ox]
+                                                : (oz == 2 ? sxy[1][oy][ox]
+                                                           : sxy[0][oy][ox] + sxy[1][oy][ox]);
+                            const int mask = (ox != 1 ? 1 : 0) | (oy != 1 ? 2 : 0) | (oz != 1 ? 4 : 0);
+                            if (mask == 0)
+                                centre = S;
+                            else
+                                acc = fma(L.kw[mask] * S, ph[ox + kTRX * (oy + kTRY * oz)], acc);
+                        }
+                dg = -(L.kw[0] * centre + T(0));
+                off = acc;
+            }
+            const int fi = (lx - 1) + kTFX * (ly - 1);
+            sphi[lx + kTRX * (ly + kTRY)] = (sf[fi] + off) / dg;
+        }
+        __syncthreads();
+    }
+    // the tile's own unknown nodes
+    for (int e = t; e < kTileX * kTileY; e += kTileThreads) {
+        const int p[3] = {x0 + e % kTileX, y0 + e / kTileX, z};
+        if (p[0] > L.n[0] - (G.per[0] ? 1 : 0) || p[1] > L.n[1] - (G.per[1] ? 1 : 0)) continue;
+        if (!hg::is_unknown(G, L, p)) continue;
+        dst[hg::nix(L, p[0], p[1], p[2])] =
+            sphi[(p[0] - x0 + kTileH) + kTRX * ((p[1] - y0 + kTileH) + kTRY)];
+    }
+}
+
 constexpr int kSlabThreads = 512;   // most threads of a slab block
 template <typename T, bool DENSE3>
 __global__ void __launch_bounds__(kSlabThreads)
@@ -565,6 +767,10 @@ struct HgState {
         hg::LevT<float> lev32{};          // FP32 copy of the level (mixed precision)
         float* sig32 = nullptr;
         float* buf32[hg::kNumBufs] = {};
+        // the second phi array of the tiled Gauss-Seidel (first use; zero, so that the
+        // outflow nodes it never writes read 0)
+        double* alt = nullptr;
+        float* alt32 = nullptr;
         long nn = 0, nc = 0;
     };
     std::vector<Level> L;
@@ -720,10 +926,12 @@ template <typename T> struct HgAccess;
 template <> struct HgAccess<double> {
     static hg::LevT<double> lev(const HgState::Level& S) { return S.lev; }
     static double* buf(const HgState::Level& S, int w) { return S.buf[w]; }
+    static double*& alt(HgState::Level& S) { return S.alt; }
 };
 template <> struct HgAccess<float> {
     static hg::LevT<float> lev(const HgState::Level& S) { return S.lev32; }
     static float* buf(const HgState::Level& S, int w) { return S.buf32[w]; }
+    static float*& alt(HgState::Level& S) { return S.alt32; }
 };
 
 // The multigrid half of the executor in precision T on the context's stream.
@@ -754,6 +962,7 @@ struct HgMg {
     // stencil) and replayed: the cycle issues one launch per colour, level and kernel kind,
     // most of them small, and needs no host value inside
     void run_cycles(int count, int nu1, int nu2) {
+        prepare_tiles();
         if (err) return;
         HgState::Graph& g = H->graph[std::is_same<T, float>::value ? 1 : 0];
         const int key[4] = {count, nu1, nu2, geo.dense};
@@ -807,6 +1016,10 @@ struct HgMg {
         const hg::LevT<T>& L = lev(l);
         const int ns = L.nn[dm - 1];
         const int per_slab = (L.nn[0] + 1) / 2 * (dm == 3 ? (L.nn[1] + 1) / 2 : 1);
+        if (per_slab > kSlabThreads && dense3()) {
+            gs_tiled(l, phi, f, nu);
+            return;
+        }
         if (per_slab > kSlabThreads) {
             for (int s = 0; s < nu; ++s)
                 for (int colour = 0; colour < (1 << dm); ++colour) {
@@ -831,6 +1044,64 @@ struct HgMg {
                     k_hg_gs_slab<T, false><<<nb, threads, 0, c->stream>>>(geo, L, sp, phi, f);
                 launched();
             }
+    }
+    // nu sweeps of the tiled Gauss-Seidel (fine 3-D dense levels), two launches a sweep,
+    // alternating between phi and the level's second array (a copy back after an odd count)
+    void gs_tiled(int l, T* phi, const T* f, int nu) {
+        const hg::LevT<T>& L = lev(l);
+        T* alt = HgAccess<T>::alt(H->L[l]);
+        if (!alt) {   // prepare_tiles runs before the cycles are captured
+            err = MAC_ERR_CUDA;
+            return;
+        }
+        const int ntx = (L.n[0] + (geo.per[0] ? 0 : 1) + kTileX - 1) / kTileX;
+        const int nty = (L.n[1] + (geo.per[1] ? 0 : 1) + kTileY - 1) / kTileY;
+        const int nzu = L.n[2] + (geo.per[2] ? 0 : 1);
+        const dim3 grid((unsigned)(ntx * nty), (unsigned)((nzu + 1) / 2));
+        T* cur = phi;
+        T* nxt = alt;
+        for (int s = 0; s < nu; ++s) {
+            k_hg_gs_tile<T><<<grid, kTileThreads, tile_smem<T>(), c->stream>>>(geo, L, 0, ntx, cur, cur,
+                                                                                nxt, f);
+            launched();
+            k_hg_gs_tile<T><<<grid, kTileThreads, tile_smem<T>(), c->stream>>>(geo, L, 1, ntx, cur, nxt,
+                                                                                nxt, f);
+            launched();
+            T* tmp = cur;
+            cur = nxt;
+            nxt = tmp;
+        }
+        if (cur != phi &&
+            cudaMemcpyAsync(phi, cur, (size_t)nn(l) * sizeof(T), cudaMemcpyDeviceToDevice, c->stream) !=
+                cudaSuccess)
+            err = MAC_ERR_CUDA;
+    }
+    // Levels that sweep with the tiled kernel: their second phi array (zeroed) and the kernel's
+    // shared-memory limit, set up outside any stream capture.
+    void prepare_tiles() {
+        if (err || !dense3()) return;
+        static bool attr_set = false;
+        if (!attr_set) {
+            if (cudaFuncSetAttribute(k_hg_gs_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)tile_smem<T>()) != cudaSuccess) {
+                set_last_cuda_error(cudaGetLastError(), "cudaFuncSetAttribute", __FILE__, __LINE__);
+                err = MAC_ERR_CUDA;
+                return;
+            }
+            attr_set = true;
+        }
+        for (int l = 0; l < nlev; ++l) {
+            const hg::LevT<T>& L = lev(l);
+            if ((L.nn[0] + 1) / 2 * ((L.nn[1] + 1) / 2) <= kSlabThreads) continue;
+            T*& alt = HgAccess<T>::alt(H->L[l]);
+            if (alt) continue;
+            if (hg_alloc(H, &alt, (size_t)nn(l)) ||
+                cudaMemsetAsync(alt, 0, (size_t)nn(l) * sizeof(T), c->stream) != cudaSuccess) {
+                alt = nullptr;
+                err = MAC_ERR_ALLOC;
+                return;
+            }
+        }
     }
     void bottom_gs(int l, T* phi, const T* f, int nu) {
         if (H->binv && l == (int)H->L.size() - 1) {

@@ -366,6 +366,33 @@ HG_HD inline void restrict_node(const Geo& G, const LevT<T>& F, const LevT<T>& K
     }
     const int dm = G.dm;
     T s = 0;
+    // a coarse node whose fine neighbours 2P-1 .. 2P+1 need no fold: direct offsets, the same
+    // terms in the same order as below
+    bool inner = true;
+    HG_UNROLL
+    for (int d = 0; d < 3; ++d) {
+        if (d >= dm) break;
+        inner = inner && P[d] >= 1 && 2 * P[d] + 1 <= F.n[d] - 1;
+    }
+    if (inner) {
+        const long st1 = F.nn[0], st2 = (long)F.nn[0] * F.nn[1];
+        const T* r = rF + nix(F, 2 * P[0], dm > 1 ? 2 * P[1] : 0, dm > 2 ? 2 * P[2] : 0);
+        HG_UNROLL
+        for (int a2 = -1; a2 <= 1; ++a2)
+            HG_UNROLL
+            for (int a1 = -1; a1 <= 1; ++a1)
+                HG_UNROLL
+                for (int a0 = -1; a0 <= 1; ++a0) {
+                    if ((dm < 3 && a2 != 0) || (dm < 2 && a1 != 0)) continue;
+                    T w = 1;
+                    if (a0) w *= (T)0.5;
+                    if (a1) w *= (T)0.5;
+                    if (a2) w *= (T)0.5;
+                    s += w * r[a0 + a1 * st1 + a2 * st2];
+                }
+        fK[idx] = s / (T)(1 << dm);
+        return;
+    }
     // (static bounds, the same terms in the same order: the small arrays stay in registers)
     HG_UNROLL
     for (int a2 = -1; a2 <= 1; ++a2)
@@ -407,6 +434,35 @@ HG_HD inline void prolong_node(const Geo& G, const LevT<T>& K, const LevT<T>& F,
         odd[d] = p[d] & 1;
     }
     T s = 0;
+    // a fine node whose coarse parents need no fold: direct offsets, the same terms in the same
+    // order as below
+    bool inner = true;
+    HG_UNROLL
+    for (int d = 0; d < 3; ++d) {
+        if (d >= dm) break;
+        inner = inner && p[d] <= F.n[d] - 2;
+    }
+    if (inner) {
+        const long st1 = K.nn[0], st2 = (long)K.nn[0] * K.nn[1];
+        const T* e = eK + nix(K, lo[0], lo[1], lo[2]);
+        T w = 1;
+        HG_UNROLL
+        for (int d = 0; d < 3; ++d) {
+            if (d >= dm) break;
+            if (odd[d]) w *= (T)0.5;
+        }
+        HG_UNROLL
+        for (int a2 = 0; a2 <= 1; ++a2)
+            HG_UNROLL
+            for (int a1 = 0; a1 <= 1; ++a1)
+                HG_UNROLL
+                for (int a0 = 0; a0 <= 1; ++a0) {
+                    if (a2 > odd[2] || a1 > odd[1] || a0 > odd[0]) continue;
+                    s += w * e[a0 + a1 * st1 + a2 * st2];
+                }
+        phiF[idx] += s;
+        return;
+    }
     HG_UNROLL
     for (int a2 = 0; a2 <= 1; ++a2)
         HG_UNROLL
