@@ -808,6 +808,15 @@ struct HgState {
     size_t staging_cap = 0;
     double* fwall = nullptr;   // per-box calls: wall values of the inflow faces (hg::Wall)
     size_t fwall_cap = 0;
+    // kernel-class timing (mac_opts.timing): CUDA events around level-0 launches, read after
+    // the call; the cycles run uncaptured then
+    struct Span {
+        int cls, launches;
+        cudaEvent_t a, b;
+    };
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    std::vector<Span> spans;
 };
 
 void hg_release(mac_ctx* c) {
@@ -820,6 +829,7 @@ void hg_release(mac_ctx* c) {
     if (H->d_tab) cudaFree(H->d_tab);
     if (H->staging) cudaFree(H->staging);
     if (H->fwall) cudaFree(H->fwall);
+    for (cudaEvent_t e : H->ev_pool) cudaEventDestroy(e);
     if (H->h_tab) cudaFreeHost(H->h_tab);
     if (H->h_out) cudaFreeHost(H->h_out);
     if (H->h_flag) cudaFreeHost(H->h_flag);
@@ -964,6 +974,10 @@ struct HgMg {
     void run_cycles(int count, int nu1, int nu2) {
         prepare_tiles();
         if (err) return;
+        if (c->o.timing) {   // events around the level-0 launches: no capture
+            for (int v = 0; v < count; ++v) hg::vcycle(*this, 0, nu1, nu2);
+            return;
+        }
         HgState::Graph& g = H->graph[std::is_same<T, float>::value ? 1 : 0];
         const int key[4] = {count, nu1, nu2, geo.dense};
         if (!g.exec || std::memcmp(g.key, key, sizeof(key)) != 0) {
@@ -998,20 +1012,59 @@ struct HgMg {
         }
         c->issued += g.kernels;
     }
+    // timing spans (level 0 only)
+    cudaEvent_t next_event() {
+        if (H->ev_used < H->ev_pool.size()) return H->ev_pool[H->ev_used++];
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            set_last_cuda_error(cudaGetLastError(), "cudaEventCreate", __FILE__, __LINE__);
+            err = MAC_ERR_CUDA;
+            return nullptr;
+        }
+        H->ev_pool.push_back(e);
+        ++H->ev_used;
+        return e;
+    }
+    bool span_on(int l) const { return c->o.timing && l == 0 && !err; }
+    cudaEvent_t span_begin() {
+        cudaEvent_t a = next_event();
+        if (a) cudaEventRecord(a, c->stream);
+        return a;
+    }
+    void span_end(cudaEvent_t a, int cls, long long issued_before) {
+        cudaEvent_t b = next_event();
+        if (!a || !b) return;
+        cudaEventRecord(b, c->stream);
+        H->spans.push_back(HgState::Span{cls, (int)(c->issued - issued_before), a, b});
+    }
     void defect(int l, const T* phi, const T* f, T* r) {
+        const bool tm = span_on(l) && std::is_same<T, double>::value;
+        const long long before = c->issued;
+        cudaEvent_t a = tm ? span_begin() : nullptr;
+        defect_launch(l, phi, f, r);
+        if (tm) span_end(a, MAC_KT_RESID, before);
+    }
+    void defect_launch(int l, const T* phi, const T* f, T* r) {
         if (dense3())
             k_hg_defect3<T><<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), phi, f, r, nn(l));
         else
             k_hg_defect<T><<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), phi, f, r, nn(l));
         launched();
     }
-    // nu sweeps, each as two slab-parity halves (k_hg_gs_slab: the same update sequence as one
-    // launch per colour)
-    // Levels whose in-slab colours fit one block (one node per thread, at most kSlabThreads)
-    // sweep by slabs, two launches a sweep; finer levels keep one launch per colour: there one
-    // block per slab would leave most of the SMs idle (128 blocks at 256^3, 15.1 against 22.9
-    // projections/s measured).  Both orders are the same update sequence.
+    // nu Gauss-Seidel sweeps in the colour order.  Levels whose in-slab colours fit one block
+    // (one node per thread, at most kSlabThreads) sweep by slabs (k_hg_gs_slab, two launches a
+    // sweep, one block per slab); finer 3-D dense levels by tiles (k_hg_gs_tile, two launches
+    // a sweep: one block per slab would leave most SMs idle there, 128 blocks at 256^3);
+    // others (cross stencil, fine 2-D levels) one launch per colour.  All three are the same
+    // update sequence.
     void gs(int l, T* phi, const T* f, int nu) {
+        const bool tm = span_on(l);
+        const long long before = c->issued;
+        cudaEvent_t a = tm ? span_begin() : nullptr;
+        gs_launch(l, phi, f, nu);
+        if (tm) span_end(a, MAC_KT_SMOOTH, before);
+    }
+    void gs_launch(int l, T* phi, const T* f, int nu) {
         const int dm = geo.dm;
         const hg::LevT<T>& L = lev(l);
         const int ns = L.nn[dm - 1];
@@ -1301,6 +1354,8 @@ int hg_core(mac_ctx* c, int proj_type, double dt, int dense_stencil, double rel_
         if (!rc && *H->h_flag) rc = MAC_ERR_BAD_DENSITY;
     }
     hg::SolveStats S{};
+    H->spans.clear();
+    H->ev_used = 0;
     cudaEventRecord(c->ev[0], c->stream);
     const double eps = rel_eps > 0.0 ? rel_eps : 1e-12;
     const bool mixed = c->o.precision == MAC_PREC_MIXED;
@@ -1329,6 +1384,13 @@ int hg_core(mac_ctx* c, int proj_type, double dt, int dense_stencil, double rel_
     }
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, c->ev[0], c->ev[2]) == cudaSuccess) st->solve_ms = ms;
+    for (const HgState::Span& sp : H->spans) {   // timing: the level-0 launch classes
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, sp.a, sp.b) != cudaSuccess) continue;
+        c->ktime_ms[sp.cls] += t;
+        c->ktime_launches[sp.cls] += sp.launches;
+    }
+    H->spans.clear();
     cudaGetLastError();
     st->vcycles = S.cycles;
     st->nlevels = (int)H->L.size();
