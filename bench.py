@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--workload", default="mac", choices=["mac", "amr", "hg"],
                     help="mac: the MAC projection headline (default); amr: the two-level "
                          "projection; hg: the nodal projection")
+    ap.add_argument("--hg-n", type=int, default=256,
+                    help="--workload hg: cells per direction (default 256, the bench workload; "
+                         "smaller cubes for profiling captures)")
     ap.add_argument("--e2e-steps", type=int, default=24)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
@@ -285,7 +288,6 @@ def run_reference(args, rank, world):
 
 # ---- the other rows: multi-level and nodal projections (run with --workload) -------------------
 AMR_N0, AMR_BOX, AMR_FINE = (128, 128, 128), (64, 64, 64), ((64, 64, 64), (191, 191, 191))
-HG_N, HG_BOX = (256, 256, 256), (128, 128, 128)
 
 
 def _amr_inputs(n0, fine, seed):
@@ -309,6 +311,8 @@ def _hg_inputs(n, seed):
 
 def run_extra(args, rank, world, local):
     """One JSON line for the multi-level (amr) or nodal (hg) projection."""
+    hg_n = (args.hg_n,) * 3
+    hg_box = tuple(max(v // 2, 1) for v in hg_n)
     import numpy as np
     import oracle as O
     if args.workload == "amr":
@@ -319,10 +323,11 @@ def run_extra(args, rank, world, local):
         full_cells = np.prod(AMR_N0) + np.prod([b - a + 1 for a, b in zip(*AMR_FINE)])
         sample_cells = np.prod(sample_n0) + np.prod([b - a + 1 for a, b in zip(*sample_fine)])
     else:
-        metric = "nodal (HG) projections/s at 256^3 (dense stencil, regular time step) to 1e-12"
-        cfg = {"workload": "hg_256", "n": list(HG_N), "box": list(HG_BOX), "rel_eps": O.EPS_HG,
+        metric = (f"nodal (HG) projections/s at {args.hg_n}^3 (dense stencil, regular time step) "
+                  "to 1e-12")
+        cfg = {"workload": f"hg_{args.hg_n}", "n": list(hg_n), "box": list(hg_box), "rel_eps": O.EPS_HG,
                "stencil": "dense"}
-        full_cells = np.prod(HG_N)
+        full_cells = np.prod(hg_n)
         sample_n = (64, 64, 64)
         sample_cells = np.prod(sample_n)
     threads = host_cores()
@@ -398,10 +403,10 @@ def run_extra(args, rank, world, local):
                                          beta0=[b.data_ptr() for b in b0],
                                          beta0_edge=[b.data_ptr() for b in b0e], strict=True)
     else:
-        h = _hg_inputs(HG_N, args.seed + rank)
-        lay = Layout.tiled(HG_N, HG_BOX)
+        h = _hg_inputs(hg_n, args.seed + rank)
+        lay = Layout.tiled(hg_n, hg_box)
         # mixed precision: FP32 V-cycles under FP64 refinement (the FP64 rate is printed too)
-        P = MacProjector(lay, tuple(1.0 / v for v in HG_N),
+        P = MacProjector(lay, tuple(1.0 / v for v in hg_n),
                          BcTower((-1, -1, 2), (-1, -1, 2)), precision="mixed",
                          stream=stream.cuda_stream)
         fields = {k: to_dev(v) for k, v in h.items()}
@@ -448,7 +453,7 @@ def run_extra(args, rank, world, local):
         nl = st["ktime_launches"][0]
         if nl > 0:
             nodes = 1
-            for v in HG_N:
+            for v in hg_n:
                 nodes *= v + 1
             # one launch = one slab parity of a sweep, per level node in FP32: the own slabs'
             # phi, f and new phi (2 + 2 + 2 B), the other slabs' phi once (2 B), every cell's
@@ -475,7 +480,7 @@ def run_extra(args, rank, world, local):
     # the FP64 rate of the same workload (one untimed solve, then at least one timed)
     n64 = max(nsteps, 2)
     if args.workload == "hg":
-        P = MacProjector(lay, tuple(1.0 / v for v in HG_N),
+        P = MacProjector(lay, tuple(1.0 / v for v in hg_n),
                          BcTower((-1, -1, 2), (-1, -1, 2)), precision="fp64",
                          stream=stream.cuda_stream)
         work = [(fields["unew"].clone(), fields["gpi"].clone(), fields["pi"].clone())
