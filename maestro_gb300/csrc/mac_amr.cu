@@ -241,9 +241,6 @@ __global__ void k_to_single(const double* x, float* y, long N) {
 __global__ void k_accumulate(Lev L, double* phi, const float* e, long N) {
     AMR_LOOP(N) amr::accumulate_cell(L, idx, phi, e);
 }
-__global__ void k_to_double(const float* x, double* y, long N) {
-    AMR_LOOP(N) y[idx] = (double)x[idx];
-}
 
 // Caller fabs of one level <-> the level array; blockIdx.y is the fab.
 __global__ void k_fabs_gather(Geo G, Lev L, int dir, const amr::FabDesc* T, int with_ghosts,
@@ -605,20 +602,43 @@ struct GpuMl {
         if (rc && !err) err = rc;
         return err;
     }
+    // One FP32 V-cycle of the level-0 multigrid (the one-level solver's mixed-precision inner
+    // cycle: over-relaxed half-sweeps, its V-cycle shape and exact bottom) on rhs from a zero
+    // guess into e, natural layout; the means as in level0_fp64.
+    int level0_fp32(const float* rhs, float* e) {
+        if (err) return err;
+        Level& F = c->lev[0];
+        float* r0 = A->L[0].buf32[amr::kTmp];
+        const amr::LevT<float> L0 = A->L[0].lev32;
+        if (cudaMemcpyAsync(r0, rhs, sizeof(float) * ncell(0), cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess)
+            err = MAC_ERR_CUDA;
+        if (!err && singular) {
+            int np = 0;
+            reduce_level<float>(0, r0, 0, &np);
+            finish_reduce(np);
+            k_sub_scalar<float><<<blocks(ncell(0)), kThreads, 0, c->stream>>>(L0, r0, A->out + 4, 0, ncell(0));
+            launched();
+        }
+        int rc = err ? err : natural_to_level0(c, r0, F.a32.f);
+        if (!rc && cudaMemsetAsync(F.a32.phi, 0, sizeof(float) * (size_t)F.d.ncell, c->stream) != cudaSuccess)
+            rc = MAC_ERR_CUDA;
+        if (!rc) rc = level0_fp32_vcycle(c);
+        if (!rc) rc = level0_to_natural(c, F.a32.phi, e);
+        if (!rc && singular) {
+            int np = 0;
+            reduce_level<float>(0, e, 0, &np);
+            finish_reduce(np);
+            k_sub_scalar<float><<<blocks(ncell(0)), kThreads, 0, c->stream>>>(L0, e, A->out + 4, 0, ncell(0));
+            launched();
+        }
+        if (rc && !err) err = rc;
+        return err;
+    }
     int level0_correction(const T* rhs, T* e) {
         if constexpr (std::is_same<T, double>::value) {
             return level0_fp64(rhs, e);
         } else {
-            // FP32 cycle: the level-0 correction in FP64 on scratch copies
-            double* r64 = A->L[0].buf[amr::kHold];
-            double* e64 = A->L[0].buf[amr::kDu];
-            k_to_double<<<blocks(ncell(0)), kThreads, 0, c->stream>>>(rhs, r64, ncell(0));
-            launched();
-            const int rc = level0_fp64(r64, e64);
-            if (rc) return rc;
-            k_to_single<<<blocks(ncell(0)), kThreads, 0, c->stream>>>(e64, e, ncell(0));
-            launched();
-            return err;
+            return level0_fp32(rhs, e);
         }
     }
 };
@@ -639,6 +659,8 @@ struct GpuExec : GpuMl<double> {
         if (!rc) rc = set_otf_mode(c, false);
         if (!rc) rc = setup_fine_from_faces(c, A->L[0].beta[0], A->L[0].beta[1],
                                             geo.dm == 3 ? A->L[0].beta[2] : nullptr, nullptr);
+        // mixed precision: the FP32 level-0 operator of the inner cycles' coarse correction
+        if (!rc && c->o.precision == MAC_PREC_MIXED) rc = setup_fp32_copies(c);
         if (!rc) rc = setup_coarse_levels(c);
         singular = c->singular;
         return rc;

@@ -446,6 +446,8 @@ int setup_fine_from_faces(mac_ctx* c, const double* fx, const double* fy, const 
 int setup_rhs_from(mac_ctx* c, const double* rh_nat, const double* phi_nat = nullptr);
 int natural_to_level0(mac_ctx* c, const double* src, double* dst);
 int level0_to_natural(mac_ctx* c, const double* src, double* dst);
+int natural_to_level0(mac_ctx* c, const float* src, float* dst);
+int level0_to_natural(mac_ctx* c, const float* src, float* dst);
 int check_density(mac_ctx* c, bool* ok);
 
 // caller box layout
@@ -476,6 +478,9 @@ int scatter_faces(mac_ctx* c, int ptr_kind, double* const* fabs, int ng, int dir
 int run_solve(mac_ctx* c, mac_stats* st);
 // One FP64 V-cycle of the level-0 multigrid on (lev[0].a64.phi, lev[0].a64.f), in place.
 int level0_fp64_vcycle(mac_ctx* c);
+// One FP32 V-cycle (the mixed-precision inner cycle) on (lev[0].a32.phi, lev[0].a32.f), in
+// place; the FP32 operator copies must be set up (setup_fp32_copies).
+int level0_fp32_vcycle(mac_ctx* c);
 
 // ---- multi-level hierarchy (mac_amr.cu) -------------------------------------------------------
 // Validate and store the finer levels' boxes (levels 1 .. nlev-1) and allocate their arrays.

@@ -446,7 +446,8 @@ k_correct(CorrParams P, Dims d, double* __restrict__ u, const double* __restrict
     if (phi_nat && i < P.n[0]) phi_nat[i + P.n[0] * (j + P.n[1] * k)] = phi[lidx(d, i, j, k)];
 }
 
-__global__ void k_nat_to_l0(Dims d, const double* __restrict__ src, double* __restrict__ dst) {
+template <typename T>
+__global__ void k_nat_to_l0(Dims d, const T* __restrict__ src, T* __restrict__ dst) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
@@ -454,7 +455,8 @@ __global__ void k_nat_to_l0(Dims d, const double* __restrict__ src, double* __re
     dst[lidx(d, i, j, k)] = src[i + d.n0 * (j + d.n1 * k)];
 }
 
-__global__ void k_l0_to_nat(Dims d, const double* __restrict__ src, double* __restrict__ dst) {
+template <typename T>
+__global__ void k_l0_to_nat(Dims d, const T* __restrict__ src, T* __restrict__ dst) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
@@ -804,23 +806,31 @@ int correct_velocity(mac_ctx* c, bool have_beta0, const std::function<int(int)>*
     return MAC_OK;
 }
 
-int natural_to_level0(mac_ctx* c, const double* src, double* dst) {
+namespace {
+template <typename T>
+int nat_to_l0(mac_ctx* c, const T* src, T* dst) {
     const Dims d = level0_dims(c);
     const Grid3 g = grid3(d.n0, d.n1, d.n2);
-    k_nat_to_l0<<<g.grid, g.block, 0, c->stream>>>(d, src, dst);
+    k_nat_to_l0<T><<<g.grid, g.block, 0, c->stream>>>(d, src, dst);
     MAC_CUDA_TRY(cudaGetLastError());
     ++c->issued;
     return MAC_OK;
 }
+template <typename T>
+int l0_to_nat(mac_ctx* c, const T* src, T* dst) {
+    const Dims d = level0_dims(c);
+    const Grid3 g = grid3(d.n0, d.n1, d.n2);
+    k_l0_to_nat<T><<<g.grid, g.block, 0, c->stream>>>(d, src, dst);
+    MAC_CUDA_TRY(cudaGetLastError());
+    ++c->issued;
+    return MAC_OK;
+}
+}  // namespace
 
-int level0_to_natural(mac_ctx* c, const double* src, double* dst) {
-    const Dims d = level0_dims(c);
-    const Grid3 g = grid3(d.n0, d.n1, d.n2);
-    k_l0_to_nat<<<g.grid, g.block, 0, c->stream>>>(d, src, dst);
-    MAC_CUDA_TRY(cudaGetLastError());
-    ++c->issued;
-    return MAC_OK;
-}
+int natural_to_level0(mac_ctx* c, const double* src, double* dst) { return nat_to_l0(c, src, dst); }
+int level0_to_natural(mac_ctx* c, const double* src, double* dst) { return l0_to_nat(c, src, dst); }
+int natural_to_level0(mac_ctx* c, const float* src, float* dst) { return nat_to_l0(c, src, dst); }
+int level0_to_natural(mac_ctx* c, const float* src, float* dst) { return l0_to_nat(c, src, dst); }
 
 // ---- box tables ----------------------------------------------------------------------------
 namespace {

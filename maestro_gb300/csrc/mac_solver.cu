@@ -946,6 +946,11 @@ int level0_fp64_vcycle(mac_ctx* c) {
     MAC_CUDA_TRY(cudaGetLastError());
     return MAC_OK;
 }
+int level0_fp32_vcycle(mac_ctx* c) {
+    vcycle<float>(c, 0);
+    MAC_CUDA_TRY(cudaGetLastError());
+    return MAC_OK;
+}
 int forward_projection(mac_ctx* c, const double* macrhs, bool have_beta0, mac_stats* st) {
     return core_macproject(c, macrhs, have_beta0, st);
 }
