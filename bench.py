@@ -434,6 +434,41 @@ def run_extra(args, rank, world, local):
     ck = clocks.stop()
     ms = e0.elapsed_time(e1)
     roof, by_class = None, None
+    if args.workload == "amr":
+        # the dominant kernel's live launch time, after the timed region: one more projection
+        # with CUDA events around the fine level's sweeps, on a fresh copy of the inputs
+        P.set_opts(timing=1)
+        u = [[x.clone() for x in u0[l]] for l in range(2)]
+        phi = [torch.zeros_like(r) for r in rho]
+        st = P.macproject_ml_dense([[x.data_ptr() for x in u[l]] for l in range(2)],
+                                   [p.data_ptr() for p in phi], [r.data_ptr() for r in rho],
+                                   macrhs=[m.data_ptr() for m in rhs],
+                                   beta0=[b.data_ptr() for b in b0],
+                                   beta0_edge=[b.data_ptr() for b in b0e], strict=True)
+        P.set_opts(timing=0)
+        torch.cuda.synchronize()
+        del u, phi
+        nl = st["ktime_launches"][0]
+        by_class = {"fine_gs_ms": st["ktime_ms"][0], "fine_gs_launches": nl,
+                    "solve_ms": st["solve_ms"]}
+        if nl > 0:
+            # the fine level's array box: its boxes' bounding box grown by one cell, clipped
+            cells = 1
+            for d in range(3):
+                lo = max(AMR_FINE[0][d] - 1, 0)
+                hi = min(AMR_FINE[1][d] + 1, 2 * AMR_N0[d] - 1)
+                cells *= hi - lo + 1
+            # one colour launch, per cell of the box (FP32): every cell's u (neighbours) 4 B, the
+            # own colour's f and new u 2 + 2 B, the face coefficients 3 x 4 B, the mask 1 B
+            alg = 21.0 * cells
+            avg_ms = st["ktime_ms"][0] / nl
+            achieved = alg / (avg_ms * 1e-3) / 1e9
+            hbm_peak, peak_kind = peaks()
+            roof = {"bound": "hbm", "kernel": "k_gsrb<float> (fine level, one colour of a red/black "
+                    "sweep of the composite operator, FP32, natural layout, masked)",
+                    "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": achieved / hbm_peak, "traffic": None, "alg_bytes_per_launch": alg,
+                    "avg_launch_ms": avg_ms, "launches": nl, "peak_kind": peak_kind}
     if args.workload == "hg":
         # the dominant kernel's live launch time, after the timed region: one more projection
         # with CUDA events around the finest level's sweeps and the FP64 defects (launched

@@ -280,6 +280,15 @@ inline int blocks_for(long n, int sms) {
 struct AmrState {
     int nlev = 0;
     Geo geo{};
+    // kernel-class timing (mac_opts.timing): CUDA events around the finest level's sweeps, read
+    // after the call
+    struct Span {
+        int cls, launches;
+        cudaEvent_t a, b;
+    };
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    std::vector<Span> spans;
     std::vector<std::vector<int>> boxes;   // per level: lo[3], hi[3] per box (level indices)
     struct LevelStore {
         Lev lev{};
@@ -327,6 +336,7 @@ void amr_release(mac_ctx* c) {
     if (A->h_tab) cudaFreeHost(A->h_tab);
     if (A->h_out) cudaFreeHost(A->h_out);
     if (A->h_flag) cudaFreeHost(A->h_flag);
+    for (cudaEvent_t e : A->ev_pool) cudaEventDestroy(e);
     delete A;
     c->amr = nullptr;
 }
@@ -476,7 +486,34 @@ struct GpuMl {
         k_defect<T><<<blocks(ncell(l)), kThreads, 0, c->stream>>>(geo, lev(l), C, uu, cu, f, r, ncell(l));
         launched();
     }
+    cudaEvent_t next_event() {
+        if (A->ev_used < A->ev_pool.size()) return A->ev_pool[A->ev_used++];
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            set_last_cuda_error(cudaGetLastError(), "cudaEventCreate", __FILE__, __LINE__);
+            err = MAC_ERR_CUDA;
+            return nullptr;
+        }
+        A->ev_pool.push_back(e);
+        ++A->ev_used;
+        return e;
+    }
     void gsrb(int l, T* uu, const T* f, int nu) {
+        // timing: the finest level's sweeps (one span per call)
+        const bool tm = c->o.timing && l == nlev - 1 && !err;
+        const long long before = c->issued;
+        cudaEvent_t ta = tm ? next_event() : nullptr;
+        if (ta) cudaEventRecord(ta, c->stream);
+        gsrb_launch(l, uu, f, nu);
+        if (ta) {
+            cudaEvent_t tb = next_event();
+            if (tb) {
+                cudaEventRecord(tb, c->stream);
+                A->spans.push_back(AmrState::Span{MAC_KT_SMOOTH, (int)(c->issued - before), ta, tb});
+            }
+        }
+    }
+    void gsrb_launch(int l, T* uu, const T* f, int nu) {
         for (int s = 0; s < nu; ++s)
             for (int colour = 0; colour < 2; ++colour) {
                 const long nt = amr::colour_threads(lev(l));
@@ -847,6 +884,8 @@ int ml_core(mac_ctx* c, double* const* umac, double* const* phi, const double* c
     double rel = c->o.rel_eps;
     if (rel < 1e-8) rel = std::min(rel * std::pow(10.0, nl - 1), 1e-8);
     amr::SolveStats S{};
+    A->spans.clear();
+    A->ev_used = 0;
     cudaEventRecord(c->ev[0], c->stream);
     if (!rc) {
         if (c->o.precision == MAC_PREC_MIXED) {
@@ -876,6 +915,14 @@ int ml_core(mac_ctx* c, double* const* umac, double* const* phi, const double* c
     for (int l = 0; l < nl; ++l) A->L[l].buf[amr::kPhi] = saved_phi[l];
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, c->ev[0], c->ev[2]) == cudaSuccess) st->solve_ms = ms;
+    for (const AmrState::Span& sp : A->spans) {   // timing: the finest level's sweeps
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, sp.a, sp.b) != cudaSuccess) continue;
+        c->ktime_ms[sp.cls] += t;
+        c->ktime_launches[sp.cls] += sp.launches;
+    }
+    A->spans.clear();
+    A->ev_used = 0;
     cudaGetLastError();
     st->vcycles = S.cycles;
     st->fnorm = S.fnorm;

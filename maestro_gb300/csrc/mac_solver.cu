@@ -941,13 +941,21 @@ void report(const mac_ctx* c, const char* what, const mac_stats* st) {
 }  // namespace
 
 namespace mac {
+// (launched outside a stream capture: the V-cycle's own class-timing events, which are
+// recorded as nodes of its captured graph, stay off)
 int level0_fp64_vcycle(mac_ctx* c) {
+    const int tm = c->o.timing;
+    c->o.timing = 0;
     vcycle<double>(c, 0);
+    c->o.timing = tm;
     MAC_CUDA_TRY(cudaGetLastError());
     return MAC_OK;
 }
 int level0_fp32_vcycle(mac_ctx* c) {
+    const int tm = c->o.timing;
+    c->o.timing = 0;
     vcycle<float>(c, 0);
+    c->o.timing = tm;
     MAC_CUDA_TRY(cudaGetLastError());
     return MAC_OK;
 }
