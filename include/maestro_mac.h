@@ -429,8 +429,8 @@ int mac_macproject_adjoint_dense(mac_ctx* ctx,
  * fixed array of 14*MAC_NOALLOC_MAX_CELLS doubles that every GPU loading the library holds until
  * the process exits.  All calls share that array and it keeps the last call's contents; calls
  * that overlap on the GPU (other streams or host threads) race -- serialise them.  The first call
- * on a device looks up the array's address with that device current; make it before any stream
- * capture.  Blocks the host until the solve has finished (it reads the result back).
+ * on a device looks up the array's address with that device current.  Blocks the host until the
+ * solve has finished (it reads the result back).
  */
 int mac_solve_small_noalloc(int dm, const int* n, const double* dx, const int* bc_lo,
                             const int* bc_hi, const double* rh, double* phi,

@@ -19,8 +19,7 @@
 //   * calls that overlap on the GPU (different streams, or different host threads) race on the
 //     array -- serialise them (one stream does that);
 //   * the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress while that device is current; that first call should come before any
-//     stream capture on the device.
+//     cudaGetSymbolAddress while that device is current.
 //   * every max-norm propagates NaN (a NaN input makes the call return MAC_ERR_NONFINITE, never a
 //     converged status).
 #include <cmath>
