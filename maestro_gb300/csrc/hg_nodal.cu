@@ -284,7 +284,7 @@ k_hg_gs_tile(hg::Geo G, hg::LevT<T> L, int sp, int ntx, const T* __restrict__ sr
     const int nzu = G.per[2] ? L.n[2] : L.n[2] + 1;  // slabs with unknown nodes
     if (z >= nzu) return;
     const int x0 = kTileX * ((int)blockIdx.x % ntx), y0 = kTileY * ((int)blockIdx.x / ntx);
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int t = threadIdx.x;
     // per staged column / row: folded node and cell coordinates (-1: outside a non-periodic
     // face), whether the folded node is an unknown along that direction, whether the raw node
     // is interior (one node or more from both faces) along it

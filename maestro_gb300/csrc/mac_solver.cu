@@ -384,7 +384,6 @@ void issue_iteration(mac_ctx* c, int prec) {
 // Accumulate the per-class device times of the iteration that just completed.
 void collect_timing(mac_ctx* c, int prec) {
     if (!c->o.timing) return;
-    const mac_opts& o = c->o;
     const int nv = inner_cycles(c, prec);
     for (int v = 0; v < nv && v < 4; ++v) {
         float t[5];

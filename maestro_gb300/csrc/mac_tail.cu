@@ -21,13 +21,6 @@ struct TailLevel {
     T *e, *f, *bx, *by, *bz, *dg, *idg;   // shared memory, natural layout
 };
 
-__device__ __forceinline__ void decode(int c, int n0, int n1, int& i, int& j, int& k) {
-    i = c % n0;
-    const int row = c / n0;
-    j = row % n1;
-    k = row / n1;
-}
-
 template <typename T>
 __device__ __forceinline__ T arms_nat(T acc, const TailLevel<T>& L, const T* __restrict__ u, int i,
                                       int j, int k, int c) {
