@@ -526,6 +526,32 @@ HG_HD inline void divu_node(const Geo& G, const Lev& L, long idx, const double* 
     const int dm = G.dm;
     const long nc = ncells(L);
     double s = 0.0;
+    // a node with all 2^dm cells inside and unfolded: direct offsets, the same terms in the same
+    // order as the general loop below
+    bool inner = true;
+    HG_UNROLL
+    for (int d = 0; d < 3; ++d) {
+        if (d >= dm) break;
+        inner = inner && p[d] >= 1 && p[d] <= L.n[d] - 1;
+    }
+    if (inner) {
+        HG_UNROLL
+        for (int a = 0; a < 8; ++a) {
+            if (a >= (1 << dm)) break;
+            const long ci = cix(L, p[0] - (a & 1), dm > 1 ? p[1] - ((a >> 1) & 1) : 0,
+                                dm > 2 ? p[2] - ((a >> 2) & 1) : 0);
+            const double bb = b0 ? b0[ci] : 1.0;
+            HG_UNROLL
+            for (int d = 0; d < 3; ++d) {
+                if (d >= dm) break;
+                s += (((a >> d) & 1) ? -1.0 : 1.0) * bb * u[d * nc + ci] * L.ih[d];
+            }
+        }
+        s *= 1.0 / (1 << (dm - 1));
+        if (nodalrhs) s -= nodalrhs[idx];
+        rh[idx] = s;
+        return;
+    }
     HG_UNROLL
     for (int a = 0; a < 8; ++a) {   // (static bounds keep the small arrays in registers)
         if (a >= (1 << dm)) break;
@@ -565,26 +591,6 @@ HG_HD inline void divu_node(const Geo& G, const Lev& L, long idx, const double* 
     rh[idx] = s;
 }
 
-// mkgphi: component d of the cell gradient of phi at cell idx.
-HG_HD inline double grad_cell(const Geo& G, const Lev& L, long idx, int d, const double* phi) {
-    int c[3];
-    cell_coords(L, idx, c);
-    const int dm = G.dm;
-    double s = 0.0;
-    HG_UNROLL
-    for (int b = 0; b < 8; ++b) {   // (static bounds keep the small arrays in registers)
-        if (b >= (1 << dm)) break;
-        int m[3] = {0, 0, 0};
-        HG_UNROLL
-        for (int e = 0; e < 3; ++e) {
-            if (e >= dm) break;
-            m[e] = node_wrap(G, L, e, c[e] + ((b >> e) & 1));
-        }
-        s += (((b >> d) & 1) ? 1.0 : -1.0) * phi[nix(L, m[0], m[1], m[2])];
-    }
-    return s * (1.0 / (1 << (dm - 1))) * L.ih[d];
-}
-
 // create_uvec_for_projection (Source/hgproject.f90:437-513) and the solver coefficient of a
 // cell: sigma = beta0 / rhohalf (beta0^2 / rhohalf with the alt energy fix outside the initial
 // and divu projections).
@@ -611,8 +617,38 @@ HG_HD inline void update_cell(const Geo& G, const Lev& L, long idx, int proj_typ
     // one division per cell (FP64 division being slow on the GPU): 1 / rhohalf and 1 / dt
     const double irho = 1.0 / rhohalf[idx];
     const double idt = proj_type == kRegular ? 1.0 / dt : 0.0;
+    // mkgphi (Source/hgproject.f90:605-636): gphi_d = 2^(1-dm) [phi summed over the cell's nodes
+    // on its + side along d - the same on the - side] / h_d.  The cell's 2^dm nodes are read once
+    // for all directions, by direct offsets where no node folds through the periodic wrap.
+    int c[3];
+    cell_coords(L, idx, c);
+    const int dm = G.dm;
+    bool inner = true;
+    HG_UNROLL
+    for (int e = 0; e < 3; ++e) {
+        if (e >= dm) break;
+        inner = inner && !(G.per[e] && c[e] + 1 >= L.n[e]);
+    }
+    double pv[8];
+    HG_UNROLL
+    for (int b = 0; b < 8; ++b) {
+        if (b >= (1 << dm)) break;
+        int m[3] = {0, 0, 0};
+        HG_UNROLL
+        for (int e = 0; e < 3; ++e) {
+            if (e >= dm) break;
+            m[e] = inner ? c[e] + ((b >> e) & 1) : node_wrap(G, L, e, c[e] + ((b >> e) & 1));
+        }
+        pv[b] = phi[nix(L, m[0], m[1], m[2])];
+    }
     for (int d = 0; d < G.dm; ++d) {
-        double g = grad_cell(G, L, idx, d, phi);
+        double sg = 0.0;
+        HG_UNROLL
+        for (int b = 0; b < 8; ++b) {
+            if (b >= (1 << dm)) break;
+            sg += (((b >> d) & 1) ? 1.0 : -1.0) * pv[b];
+        }
+        double g = sg * (1.0 / (1 << (dm - 1))) * L.ih[d];
         if (alt) g *= b0 ? b0[idx] : 1.0;
         double& u = unew[d * nc + idx];
         u -= g * irho;
