@@ -249,6 +249,7 @@ __global__ void k_hg_gs3(hg::Geo G, hg::LevT<T> L, int colour, T* phi, const T* 
 // fold through the periodic wrap when staged; outside a non-periodic face the staged values are
 // 0.  Each node takes node_op_dense3's arithmetic when interior3, node_op_dense3_face's
 // otherwise, so the results are bitwise those of the colour launches.
+
 // One element global -> shared without passing through registers (cp.async, 4 or 8 bytes);
 // inside = false writes 0 (zero-fill: nothing is read from src).
 template <typename T>
