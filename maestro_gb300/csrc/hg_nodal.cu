@@ -47,19 +47,20 @@ template <typename T>
 __global__ void k_hg_finish(hg::Geo G, hg::LevT<T> L, T* x, long N) {
     HG_LOOP(N) hg::finish_node(G, L, idx, x);
 }
-__global__ void k_hg_uvec(hg::Geo G, long nc, int proj_type, double dt, double* unew,
+__global__ void k_hg_uvec(hg::Geo G, long nc, int proj_type, double dt, double idt, double* unew,
                           const double* uold, const double* gpi, const double* rhohalf,
                           const double* b0, int alt, double* sig) {
-    HG_LOOP(nc) hg::uvec_cell(G, idx, nc, proj_type, dt, unew, uold, gpi, rhohalf, b0, alt, sig);
+    HG_LOOP(nc) hg::uvec_cell(G, idx, nc, proj_type, dt, idt, unew, uold, gpi, rhohalf, b0, alt, sig);
 }
 __global__ void k_hg_divu(hg::Geo G, hg::Lev L, const double* u, const double* b0,
                           const double* nodalrhs, hg::Wall W, double* rh, long N) {
     HG_LOOP(N) hg::divu_node(G, L, idx, u, b0, nodalrhs, W, rh);
 }
-__global__ void k_hg_update(hg::Geo G, hg::Lev L, int proj_type, double dt, const double* phi,
+__global__ void k_hg_update(hg::Geo G, hg::Lev L, int proj_type, double dt, double idt,
+                            const double* phi,
                             double* unew, const double* uold, double* gpi, const double* rhohalf,
                             const double* b0, int alt, long N) {
-    HG_LOOP(N) hg::update_cell(G, L, idx, proj_type, dt, phi, unew, uold, gpi, rhohalf, b0, alt);
+    HG_LOOP(N) hg::update_cell(G, L, idx, proj_type, dt, idt, phi, unew, uold, gpi, rhohalf, b0, alt);
 }
 __global__ void k_hg_update_pi(hg::Lev L, int proj_type, double dt, const double* phi, double* pi,
                                long N) {
@@ -79,7 +80,10 @@ __device__ __forceinline__ bool interior3(const hg::LevT<T>& L, const int p[3]) 
     return p[0] >= 1 && p[0] <= L.n[0] - 2 && p[1] >= 1 && p[1] <= L.n[1] - 2 && p[2] >= 1 &&
            p[2] <= L.n[2] - 2;
 }
-template <typename T>
+// ISO: the level's spacing is isotropic, so the weight of the 6 neighbours along one axis is
+// exactly 0 (kw[1] = kw[2] = kw[4] = 0, checked by the caller) and those terms are left out:
+// fma(0, a, acc) = acc for finite a, so the result is bitwise that of the full stencil.
+template <typename T, bool ISO = false>
 __device__ __forceinline__ void node_op_dense3(const hg::LevT<T>& L, const int p[3],
                                                const T* __restrict__ phi, T& diag, T& off) {
     const int n0 = L.n[0], n1 = L.n[1], m0 = L.nn[0], m1 = L.nn[1];
@@ -127,13 +131,14 @@ __device__ __forceinline__ void node_op_dense3(const hg::LevT<T>& L, const int p
                 const int mask = (ox != 1 ? 1 : 0) | (oy != 1 ? 2 : 0) | (oz != 1 ? 4 : 0);
                 if (mask == 0) {
                     centre = S;
-                } else {
+                } else if (!(ISO && (mask == 1 || mask == 2 || mask == 4))) {
                     am[mask] = fma(S, ph[ox + (long)m0 * (oy + (long)m1 * oz)], am[mask]);
                 }
             }
     T acc = 0;
 #pragma unroll
-    for (int m = 1; m < 8; ++m) acc = fma(L.kw[m], am[m], acc);
+    for (int m = 1; m < 8; ++m)
+        if (!(ISO && (m == 1 || m == 2 || m == 4))) acc = fma(L.kw[m], am[m], acc);
     diag = -L.kw[0] * centre;
     off = acc;
 }
@@ -247,8 +252,10 @@ __global__ void k_hg_gs3(hg::Geo G, hg::LevT<T> L, int colour, T* phi, const T* 
 // neighbour slabs), writes go to dst != src: the caller alternates two arrays (the first launch
 // reads and leaves src, the second reads the new even slabs from dst).  Node and cell indices
 // fold through the periodic wrap when staged; outside a non-periodic face the staged values are
-// 0.  Each node takes node_op_dense3's arithmetic when interior3, node_op_dense3_face's
-// otherwise, so the results are bitwise those of the colour launches.
+// 0, so every node, next to a face or not, takes node_op_dense3's arithmetic on the staged
+// values: the missing neighbours of a face node carry weight 0 (a single formula keeps the
+// warps of the tiles along a face from running two; the colour launches take
+// node_op_dense3_face there, the same terms summed in another order).
 
 // One element global -> shared without passing through registers (cp.async, 4 or 8 bytes);
 // inside = false writes 0 (zero-fill: nothing is read from src).
@@ -264,7 +271,7 @@ __device__ __forceinline__ void stage_elem(T* dst, const T* src, bool inside) {
 }
 __device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-constexpr int kTileX = 32, kTileY = 32, kTileH = 4, kTileThreads = 256;
+constexpr int kTileX = 32, kTileY = 32, kTileH = 4, kTileThreads = 384;
 constexpr int kTRX = kTileX + 2 * kTileH, kTRY = kTileY + 2 * kTileH;           // staged nodes
 constexpr int kTCX = kTileX + 2 * kTileH - 1, kTCY = kTileY + 2 * kTileH - 1;   // staged cells
 constexpr int kTFX = kTileX + 2 * kTileH - 2, kTFY = kTileY + 2 * kTileH - 2;   // right-hand side
@@ -273,7 +280,7 @@ constexpr size_t tile_smem() {
     return sizeof(T) * (3 * kTRX * kTRY + 2 * kTCX * kTCY + kTFX * kTFY);
 }
 
-template <typename T>
+template <typename T, bool ISO>
 __global__ void __launch_bounds__(kTileThreads)
 k_hg_gs_tile(hg::Geo G, hg::LevT<T> L, int sp, int ntx, const T* __restrict__ src,
              const T* __restrict__ srcnb, T* __restrict__ dst, const T* __restrict__ f) {
@@ -287,23 +294,20 @@ k_hg_gs_tile(hg::Geo G, hg::LevT<T> L, int sp, int ntx, const T* __restrict__ sr
     const int x0 = kTileX * ((int)blockIdx.x % ntx), y0 = kTileY * ((int)blockIdx.x / ntx);
     const int t = threadIdx.x;
     // per staged column / row: folded node and cell coordinates (-1: outside a non-periodic
-    // face), whether the folded node is an unknown along that direction, whether the raw node
-    // is interior (one node or more from both faces) along it
+    // face), whether the folded node is an unknown along that direction
     __shared__ int sqx[kTRX], sqy[kTRY], scx[kTCX], scy[kTCY];
-    __shared__ unsigned char sux[kTRX], suy[kTRY], six[kTRX], siy[kTRY];
+    __shared__ unsigned char sux[kTRX], suy[kTRY];
     if (t < kTRX) {
         const int raw = x0 - kTileH + t;
         const int q = hg::node_wrap(G, L, 0, raw);
         sqx[t] = q;
         sux[t] = q >= 0 && !(G.per[0] ? q == L.n[0] : ((q == 0 && G.dlo[0]) || (q == L.n[0] && G.dhi[0])));
-        six[t] = raw >= 1 && raw <= L.n[0] - 2;
         if (t < kTCX) scx[t] = hg::cell_wrap(G, L, 0, raw);
     } else if (t >= 64 && t < 64 + kTRY) {
         const int u = t - 64, raw = y0 - kTileH + u;
         const int q = hg::node_wrap(G, L, 1, raw);
         sqy[u] = q;
         suy[u] = q >= 0 && !(G.per[1] ? q == L.n[1] : ((q == 0 && G.dlo[1]) || (q == L.n[1] && G.dhi[1])));
-        siy[u] = raw >= 1 && raw <= L.n[1] - 2;
         if (u < kTCY) scy[u] = hg::cell_wrap(G, L, 1, raw);
     }
     // (scalars, not arrays: a dynamically indexed array would live in local memory)
@@ -312,30 +316,54 @@ k_hg_gs_tile(hg::Geo G, hg::LevT<T> L, int sp, int ntx, const T* __restrict__ sr
     const int cz0 = hg::cell_wrap(G, L, 2, z - 1), cz1 = hg::cell_wrap(G, L, 2, z);
     const bool uz = qz1 >= 0 &&
                     !(G.per[2] ? qz1 == L.n[2] : ((qz1 == 0 && G.dlo[2]) || (qz1 == L.n[2] && G.dhi[2])));
-    const bool iz = z >= 1 && z <= L.n[2] - 2;
     __syncthreads();
-    const long m0 = L.nn[0], m01 = (long)L.nn[0] * L.nn[1];
-    const long c0s = L.n[0], c01 = (long)L.n[0] * L.n[1];
+    const long m01 = (long)L.nn[0] * L.nn[1], c01 = (long)L.n[0] * L.n[1];
     // stage: nodes x0 - kTileH .. x0 + kTileX + kTileH - 1 (same in y), slabs z - 1 .. z + 1,
-    // the two cell layers and the right-hand side, all copies in flight at once
-    for (int e = t; e < 3 * kTRX * kTRY; e += kTileThreads) {
-        const int lx = e % kTRX, row = e / kTRX, ly = row % kTRY, lz = row / kTRY;
-        const int q0 = sqx[lx], q1 = sqy[ly], q2 = lz == 0 ? qz0 : (lz == 1 ? qz1 : qz2);
-        const bool in = q0 >= 0 && q1 >= 0 && q2 >= 0;
-        const T* from = lz == 1 ? src : srcnb;
-        stage_elem(sphi + e, in ? from + (q0 + q1 * m0 + q2 * m01) : from, in);
-    }
-    for (int e = t; e < 2 * kTCX * kTCY; e += kTileThreads) {
-        const int lx = e % kTCX, row = e / kTCX, ly = row % kTCY, lz = row / kTCY;
-        const int c0 = scx[lx], c1 = scy[ly], c2 = lz == 0 ? cz0 : cz1;
-        const bool in = c0 >= 0 && c1 >= 0 && c2 >= 0;
-        stage_elem(ssig + e, in ? L.sig + (c0 + c1 * c0s + c2 * c01) : L.sig, in);
-    }
-    for (int e = t; e < kTFX * kTFY; e += kTileThreads) {
-        const int lx = e % kTFX, ly = e / kTFX;
-        const int q0 = sqx[lx + 1], q1 = sqy[ly + 1], q2 = qz1;
-        const bool in = q0 >= 0 && q1 >= 0 && q2 >= 0;
-        stage_elem(sf + e, in ? f + (q0 + q1 * m0 + q2 * m01) : f, in);
+    // the two cell layers and the right-hand side, all copies in flight at once.  A thread keeps
+    // one staged column (its folded x in a register) and walks the rows kPR apart.
+    constexpr int kPR = kTileThreads / kTRX;
+    if (t < kPR * kTRX) {
+        const int lx = t % kTRX, r0 = t / kTRX;
+        const int q0 = sqx[lx];
+        const int im0 = L.nn[0], ic0 = L.n[0];
+#pragma unroll 1
+        for (int lz = 0; lz < 3; ++lz) {
+            const int q2 = lz == 0 ? qz0 : (lz == 1 ? qz1 : qz2);
+            const T* from = lz == 1 ? src : srcnb;
+            const bool zin = q0 >= 0 && q2 >= 0;
+            const T* pb = from + (zin ? q0 + q2 * m01 : 0);
+            T* dst_col = sphi + lz * (kTRX * kTRY) + lx;
+            for (int ly = r0; ly < kTRY; ly += kPR) {
+                const int q1 = sqy[ly];
+                const bool in = zin && q1 >= 0;
+                stage_elem(dst_col + ly * kTRX, in ? pb + (long)q1 * im0 : from, in);
+            }
+        }
+        if (lx < kTCX) {
+            const int c0 = scx[lx];
+#pragma unroll 1
+            for (int lz = 0; lz < 2; ++lz) {
+                const int c2 = lz == 0 ? cz0 : cz1;
+                const bool zin = c0 >= 0 && c2 >= 0;
+                const T* pb = L.sig + (zin ? c0 + c2 * c01 : 0);
+                T* dst_col = ssig + lz * (kTCX * kTCY) + lx;
+                for (int ly = r0; ly < kTCY; ly += kPR) {
+                    const int c1 = scy[ly];
+                    const bool in = zin && c1 >= 0;
+                    stage_elem(dst_col + ly * kTCX, in ? pb + (long)c1 * ic0 : L.sig, in);
+                }
+            }
+        }
+        if (lx >= 1 && lx <= kTFX) {
+            const bool zin = q0 >= 0 && qz1 >= 0;
+            const T* pb = f + (zin ? q0 + qz1 * m01 : 0);
+            T* dst_col = sf + (lx - 1);
+            for (int ly = r0; ly < kTFY; ly += kPR) {
+                const int q1 = sqy[ly + 1];
+                const bool in = zin && q1 >= 0;
+                stage_elem(dst_col + ly * kTFX, in ? pb + (long)q1 * im0 : f, in);
+            }
+        }
     }
     stage_wait();
     __syncthreads();
@@ -375,53 +403,30 @@ k_hg_gs_tile(hg::Geo G, hg::LevT<T> L, int sp, int ntx, const T* __restrict__ sr
                     sxy[zz][2][ox] = sx[zz][1][ox];
                 }
             const T* ph = sphi + (lx - 1) + kTRX * (ly - 1);
-            T dg, off;
-            if (six[lx] && siy[ly] && iz) {
-                // node_op_dense3's order: the neighbours summed per weight class, then kw
-                T am[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-                T centre = 0;
+            // node_op_dense3's formula for every node: the staged values are folded through the
+            // periodic wrap and 0 outside a non-periodic face (sigma and phi), so the missing
+            // neighbours of a face node carry weight 0 here as well
+            T am[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            T centre = 0;
 #pragma unroll
-                for (int oz = 0; oz < 3; ++oz)
+            for (int oz = 0; oz < 3; ++oz)
 #pragma unroll
-                    for (int oy = 0; oy < 3; ++oy)
+                for (int oy = 0; oy < 3; ++oy)
 #pragma unroll
-                        for (int ox = 0; ox < 3; ++ox) {
-                            const T S = oz == 0 ? sxy[0][oy][ox]
-                                                : (oz == 2 ? sxy[1][oy][ox]
-                                                           : sxy[0][oy][ox] + sxy[1][oy][ox]);
-                            const int mask = (ox != 1 ? 1 : 0) | (oy != 1 ? 2 : 0) | (oz != 1 ? 4 : 0);
-                            if (mask == 0)
-                                centre = S;
-                            else
-                                am[mask] = fma(S, ph[ox + kTRX * (oy + kTRY * oz)], am[mask]);
-                        }
-                T acc = 0;
+                    for (int ox = 0; ox < 3; ++ox) {
+                        const T S = oz == 0 ? sxy[0][oy][ox]
+                                            : (oz == 2 ? sxy[1][oy][ox] : sxy[0][oy][ox] + sxy[1][oy][ox]);
+                        const int mask = (ox != 1 ? 1 : 0) | (oy != 1 ? 2 : 0) | (oz != 1 ? 4 : 0);
+                        if (mask == 0)
+                            centre = S;
+                        else if (!(ISO && (mask == 1 || mask == 2 || mask == 4)))
+                            am[mask] = fma(S, ph[ox + kTRX * (oy + kTRY * oz)], am[mask]);
+                    }
+            T off = 0;
 #pragma unroll
-                for (int m = 1; m < 8; ++m) acc = fma(L.kw[m], am[m], acc);
-                dg = -L.kw[0] * centre;
-                off = acc;
-            } else {
-                // node_op_dense3_face's order: each neighbour weighted, then accumulated (a
-                // missing neighbour carries weight 0 and a staged 0)
-                T acc = 0, centre = 0;
-#pragma unroll
-                for (int oz = 0; oz < 3; ++oz)
-#pragma unroll
-                    for (int oy = 0; oy < 3; ++oy)
-#pragma unroll
-                        for (int ox = 0; ox < 3; ++ox) {
-                            const T S = oz == 0 ? sxy[0][oy][ox]
-                                                : (oz == 2 ? sxy[1][oy][ox]
-                                                           : sxy[0][oy][ox] + sxy[1][oy][ox]);
-                            const int mask = (ox != 1 ? 1 : 0) | (oy != 1 ? 2 : 0) | (oz != 1 ? 4 : 0);
-                            if (mask == 0)
-                                centre = S;
-                            else
-                                acc = fma(L.kw[mask] * S, ph[ox + kTRX * (oy + kTRY * oz)], acc);
-                        }
-                dg = -(L.kw[0] * centre + T(0));
-                off = acc;
-            }
+            for (int m = 1; m < 8; ++m)
+                if (!(ISO && (m == 1 || m == 2 || m == 4))) off = fma(L.kw[m], am[m], off);
+            const T dg = -L.kw[0] * centre;
             const int fi = (lx - 1) + kTFX * (ly - 1);
             sphi[lx + kTRX * (ly + kTRY)] = (sf[fi] + off) / dg;
         }
@@ -475,7 +480,7 @@ k_hg_gs_slab(hg::Geo G, hg::LevT<T> L, int sp, T* phi, const T* f) {
     }
 }
 
-template <typename T>
+template <typename T, bool ISO>
 __global__ void k_hg_defect3(hg::Geo G, hg::LevT<T> L, const T* phi, const T* f, T* r, long N) {
     HG_LOOP(N) {
         int p[3];
@@ -486,7 +491,7 @@ __global__ void k_hg_defect3(hg::Geo G, hg::LevT<T> L, const T* phi, const T* f,
         }
         T dg, off;
         if (interior3(L, p))
-            node_op_dense3(L, p, phi, dg, off);
+            node_op_dense3<T, ISO>(L, p, phi, dg, off);
         else
             node_op_dense3_face(G, L, p, phi, dg, off);
         r[idx] = f[idx] - (dg * phi[idx] - off);
@@ -598,41 +603,55 @@ __global__ void k_hg_sig_single(const double* s, float* s32, long N) {
 }
 
 // Per-block partials over the unknown nodes: [0] sum, [1] max |x|, [2] NaN count, [3] count.
+// Only the sum is FP64 arithmetic: the NaN test, |x| and its maximum work on the IEEE bit
+// pattern (for non-negative doubles the unsigned order of the bits is the numeric order) and
+// the counts are integers, as GB300's FP64 pipe is the narrow one.
 template <typename T>
 __global__ void k_hg_reduce(hg::Geo G, hg::LevT<T> L, const T* x, double* part, long N) {
-    __shared__ double s[4][kThreads / 32];
-    double a[4] = {0.0, 0.0, 0.0, 0.0};
+    __shared__ double s[kThreads / 32];
+    __shared__ unsigned long long smax[kThreads / 32], snan[kThreads / 32], scnt[kThreads / 32];
+    double sum = 0.0;
+    unsigned long long amax = 0, nnan = 0, cnt = 0;
     HG_LOOP(N) {
         int p[3];
         hg::node_coords(L, idx, p);
         if (!hg::is_unknown(G, L, p)) continue;
         const double v = (double)x[idx];
-        if (v != v) {
-            a[2] += 1.0;
+        const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+        if (b > 0x7ff0000000000000ull) {
+            ++nnan;
             continue;
         }
-        a[0] += v;
-        a[1] = fmax(a[1], fabs(v));
-        a[3] += 1.0;
+        sum += v;
+        amax = b > amax ? b : amax;
+        ++cnt;
     }
     for (int o = 16; o > 0; o >>= 1) {
-        a[0] += __shfl_down_sync(0xffffffffu, a[0], o);
-        a[1] = fmax(a[1], __shfl_down_sync(0xffffffffu, a[1], o));
-        a[2] += __shfl_down_sync(0xffffffffu, a[2], o);
-        a[3] += __shfl_down_sync(0xffffffffu, a[3], o);
+        sum += __shfl_down_sync(0xffffffffu, sum, o);
+        const unsigned long long m = __shfl_down_sync(0xffffffffu, amax, o);
+        amax = m > amax ? m : amax;
+        nnan += __shfl_down_sync(0xffffffffu, nnan, o);
+        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
     }
     const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0)
-        for (int k = 0; k < 4; ++k) s[k][w] = a[k];
+    if ((threadIdx.x & 31) == 0) {
+        s[w] = sum;
+        smax[w] = amax;
+        snan[w] = nnan;
+        scnt[w] = cnt;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int q = 1; q < kThreads / 32; ++q) {
-            a[0] += s[0][q];
-            a[1] = fmax(a[1], s[1][q]);
-            a[2] += s[2][q];
-            a[3] += s[3][q];
+            sum += s[q];
+            amax = smax[q] > amax ? smax[q] : amax;
+            nnan += snan[q];
+            cnt += scnt[q];
         }
-        for (int k = 0; k < 4; ++k) part[4 * blockIdx.x + k] = a[k];
+        part[4 * blockIdx.x] = sum;
+        part[4 * blockIdx.x + 1] = __longlong_as_double((long long)amax);
+        part[4 * blockIdx.x + 2] = (double)nnan;
+        part[4 * blockIdx.x + 3] = (double)cnt;
     }
 }
 
@@ -969,6 +988,11 @@ struct HgMg {
         }
     }
     bool dense3() const { return geo.dense && geo.dm == 3; }
+    // isotropic level spacing: the dense 3-D weights of the axis neighbours are exactly 0
+    bool iso(int l) const {
+        const hg::LevT<T>& L = lev(l);
+        return dense3() && L.kw[1] == T(0) && L.kw[2] == T(0) && L.kw[4] == T(0);
+    }
     // count V-cycles from level 0, captured once into a CUDA graph per (count, nu1, nu2,
     // stencil) and replayed: the cycle issues one launch per colour, level and kernel kind,
     // most of them small, and needs no host value inside
@@ -1046,8 +1070,10 @@ struct HgMg {
         if (tm) span_end(a, MAC_KT_RESID, before);
     }
     void defect_launch(int l, const T* phi, const T* f, T* r) {
-        if (dense3())
-            k_hg_defect3<T><<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), phi, f, r, nn(l));
+        if (dense3() && iso(l))
+            k_hg_defect3<T, true><<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), phi, f, r, nn(l));
+        else if (dense3())
+            k_hg_defect3<T, false><<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), phi, f, r, nn(l));
         else
             k_hg_defect<T><<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), phi, f, r, nn(l));
         launched();
@@ -1114,12 +1140,11 @@ struct HgMg {
         const dim3 grid((unsigned)(ntx * nty), (unsigned)((nzu + 1) / 2));
         T* cur = phi;
         T* nxt = alt;
+        auto kern = iso(l) ? k_hg_gs_tile<T, true> : k_hg_gs_tile<T, false>;
         for (int s = 0; s < nu; ++s) {
-            k_hg_gs_tile<T><<<grid, kTileThreads, tile_smem<T>(), c->stream>>>(geo, L, 0, ntx, cur, cur,
-                                                                                nxt, f);
+            kern<<<grid, kTileThreads, tile_smem<T>(), c->stream>>>(geo, L, 0, ntx, cur, cur, nxt, f);
             launched();
-            k_hg_gs_tile<T><<<grid, kTileThreads, tile_smem<T>(), c->stream>>>(geo, L, 1, ntx, cur, nxt,
-                                                                                nxt, f);
+            kern<<<grid, kTileThreads, tile_smem<T>(), c->stream>>>(geo, L, 1, ntx, cur, nxt, nxt, f);
             launched();
             T* tmp = cur;
             cur = nxt;
@@ -1136,7 +1161,9 @@ struct HgMg {
         if (err || !dense3()) return;
         static bool attr_set = false;
         if (!attr_set) {
-            if (cudaFuncSetAttribute(k_hg_gs_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            if (cudaFuncSetAttribute(k_hg_gs_tile<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)tile_smem<T>()) != cudaSuccess ||
+                cudaFuncSetAttribute(k_hg_gs_tile<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)tile_smem<T>()) != cudaSuccess) {
                 set_last_cuda_error(cudaGetLastError(), "cudaFuncSetAttribute", __FILE__, __LINE__);
                 err = MAC_ERR_CUDA;
@@ -1224,8 +1251,8 @@ struct HgExec : HgMg<double> {
     int alt = 0;
 
     void uvec() {
-        k_hg_uvec<<<blocks(nc(0)), kThreads, 0, c->stream>>>(geo, nc(0), proj_type, dt, unew, uold, gpi,
-                                                            rhohalf, b0, alt, H->L[0].sig);
+        k_hg_uvec<<<blocks(nc(0)), kThreads, 0, c->stream>>>(geo, nc(0), proj_type, dt, 1.0 / dt, unew,
+                                                            uold, gpi, rhohalf, b0, alt, H->L[0].sig);
         launched();
     }
     int build_levels() {
@@ -1262,8 +1289,9 @@ struct HgExec : HgMg<double> {
         launched();
     }
     void update() {
-        k_hg_update<<<blocks(nc(0)), kThreads, 0, c->stream>>>(geo, lev(0), proj_type, dt, buf(0, hg::kPhi),
-                                                              unew, uold, gpi, rhohalf, b0, alt, nc(0));
+        k_hg_update<<<blocks(nc(0)), kThreads, 0, c->stream>>>(geo, lev(0), proj_type, dt, 1.0 / dt,
+                                                              buf(0, hg::kPhi), unew, uold, gpi, rhohalf,
+                                                              b0, alt, nc(0));
         launched();
         k_hg_update_pi<<<blocks(nn(0)), kThreads, 0, c->stream>>>(lev(0), proj_type, dt, buf(0, hg::kPhi),
                                                                  pi, nn(0));

@@ -519,13 +519,15 @@ HG_HD inline void finish_node(const Geo& G, const LevT<T>& L, long idx, T* x) {
 // the nodal source (nullable).  Cells outside a non-periodic face carry U = 0, except that at an
 // inflow face (W) the cell just outside contributes its wall value of beta0 U_d through the face:
 // the boundary flux of the finite-element divergence, with the inflow velocity on the wall.
+// The signed sums of beta0 U_d are formed per direction (one FMA a term) and scaled by 1 / h_d
+// once: 3 FP64 operations a cell instead of 3 a term, the FP64 pipe being GB300's narrow one.
 HG_HD inline void divu_node(const Geo& G, const Lev& L, long idx, const double* u,
                             const double* b0, const double* nodalrhs, const Wall& W, double* rh) {
     int p[3];
     node_coords(L, idx, p);
     const int dm = G.dm;
     const long nc = ncells(L);
-    double s = 0.0;
+    double sd[3] = {0.0, 0.0, 0.0};
     // a node with all 2^dm cells inside and unfolded: direct offsets, the same terms in the same
     // order as the general loop below
     bool inner = true;
@@ -544,47 +546,54 @@ HG_HD inline void divu_node(const Geo& G, const Lev& L, long idx, const double* 
             HG_UNROLL
             for (int d = 0; d < 3; ++d) {
                 if (d >= dm) break;
-                s += (((a >> d) & 1) ? -1.0 : 1.0) * bb * u[d * nc + ci] * L.ih[d];
+                sd[d] = fma(((a >> d) & 1) ? -bb : bb, u[d * nc + ci], sd[d]);
             }
         }
-        s *= 1.0 / (1 << (dm - 1));
-        if (nodalrhs) s -= nodalrhs[idx];
-        rh[idx] = s;
-        return;
-    }
-    HG_UNROLL
-    for (int a = 0; a < 8; ++a) {   // (static bounds keep the small arrays in registers)
-        if (a >= (1 << dm)) break;
-        int c[3] = {0, 0, 0};
-        int nout = 0, dout = 0, side = 0;
+    } else {
         HG_UNROLL
-        for (int d = 0; d < 3; ++d) {
-            if (d >= dm) break;
-            const int raw = p[d] - ((a >> d) & 1);
-            const int cw = cell_wrap(G, L, d, raw);
-            if (cw < 0) {
-                ++nout;
-                dout = d;
-                side = raw < 0 ? 0 : 1;
-            }
-            c[d] = cw;
-        }
-        if (nout == 0) {
-            const long ci = cix(L, c[0], c[1], c[2]);
-            const double bb = b0 ? b0[ci] : 1.0;
+        for (int a = 0; a < 8; ++a) {   // (static bounds keep the small arrays in registers)
+            if (a >= (1 << dm)) break;
+            int c[3] = {0, 0, 0};
+            int nout = 0, dout = 0, side = 0;
             HG_UNROLL
             for (int d = 0; d < 3; ++d) {
                 if (d >= dm) break;
-                s += (((a >> d) & 1) ? -1.0 : 1.0) * bb * u[d * nc + ci] * L.ih[d];
+                const int raw = p[d] - ((a >> d) & 1);
+                const int cw = cell_wrap(G, L, d, raw);
+                if (cw < 0) {
+                    ++nout;
+                    dout = d;
+                    side = raw < 0 ? 0 : 1;
+                }
+                c[d] = cw;
             }
-        } else if (nout == 1 && W.off[2 * dout + side] >= 0) {
-            // the ghost cell just outside an inflow face: its normal velocity is the wall value
-            // (its flux through the face), the tangential ones carry no flux out of the domain
-            const int e1 = dout == 0 ? 1 : 0;
-            const int e2 = dout == 2 ? 1 : 2;
-            const long t = c[e1] + (dm == 3 ? (long)L.n[e1] * c[e2] : 0L);
-            s += (((a >> dout) & 1) ? -1.0 : 1.0) * W.w[W.off[2 * dout + side] + t] * L.ih[dout];
+            if (nout == 0) {
+                const long ci = cix(L, c[0], c[1], c[2]);
+                const double bb = b0 ? b0[ci] : 1.0;
+                HG_UNROLL
+                for (int d = 0; d < 3; ++d) {
+                    if (d >= dm) break;
+                    sd[d] = fma(((a >> d) & 1) ? -bb : bb, u[d * nc + ci], sd[d]);
+                }
+            } else if (nout == 1 && W.off[2 * dout + side] >= 0) {
+                // the ghost cell just outside an inflow face: its normal velocity is the wall
+                // value (its flux through the face), the tangential ones carry no flux out of the
+                // domain
+                const int e1 = dout == 0 ? 1 : 0;
+                const int e2 = dout == 2 ? 1 : 2;
+                const long t = c[e1] + (dm == 3 ? (long)L.n[e1] * c[e2] : 0L);
+                const double w = W.w[W.off[2 * dout + side] + t];
+                HG_UNROLL
+                for (int d = 0; d < 3; ++d)
+                    if (d == dout) sd[d] += ((a >> d) & 1) ? -w : w;
+            }
         }
+    }
+    double s = sd[0] * L.ih[0];
+    HG_UNROLL
+    for (int d = 1; d < 3; ++d) {
+        if (d >= dm) break;
+        s = fma(sd[d], L.ih[d], s);
     }
     s *= 1.0 / (1 << (dm - 1));
     if (nodalrhs) s -= nodalrhs[idx];
@@ -594,12 +603,12 @@ HG_HD inline void divu_node(const Geo& G, const Lev& L, long idx, const double* 
 // create_uvec_for_projection (Source/hgproject.f90:437-513) and the solver coefficient of a
 // cell: sigma = beta0 / rhohalf (beta0^2 / rhohalf with the alt energy fix outside the initial
 // and divu projections).
-HG_HD inline void uvec_cell(const Geo& G, long idx, long nc, int proj_type, double dt,
+// idt = 1 / dt, formed once by the caller.
+HG_HD inline void uvec_cell(const Geo& G, long idx, long nc, int proj_type, double dt, double idt,
                             double* unew, const double* uold, const double* gpi,
                             const double* rhohalf, const double* b0, int alt, double* sig) {
-    // one division per cell (FP64 division being slow on the GPU): 1 / rhohalf and 1 / dt
+    // one division per cell (FP64 division being slow on the GPU): 1 / rhohalf
     const double irho = 1.0 / rhohalf[idx];
-    const double idt = proj_type == kPressureIters ? 1.0 / dt : 0.0;
     for (int d = 0; d < G.dm; ++d) {
         double& u = unew[d * nc + idx];
         if (proj_type == kPressureIters) u = (u - uold[d * nc + idx]) * idt;
@@ -609,14 +618,14 @@ HG_HD inline void uvec_cell(const Geo& G, long idx, long nc, int proj_type, doub
     sig[idx] = (alt ? bb * bb : bb) * irho;
 }
 
-// hg_update (Source/hgproject.f90:867-1009) on one cell; gphi written to gpi per proj_type.
+// hg_update (Source/hgproject.f90:867-1009) on one cell; gphi written to gpi per proj_type;
+// idt = 1 / dt, formed once by the caller.
 HG_HD inline void update_cell(const Geo& G, const Lev& L, long idx, int proj_type, double dt,
-                              const double* phi, double* unew, const double* uold, double* gpi,
-                              const double* rhohalf, const double* b0, int alt) {
+                              double idt, const double* phi, double* unew, const double* uold,
+                              double* gpi, const double* rhohalf, const double* b0, int alt) {
     const long nc = ncells(L);
-    // one division per cell (FP64 division being slow on the GPU): 1 / rhohalf and 1 / dt
+    // one division per cell (FP64 division being slow on the GPU): 1 / rhohalf
     const double irho = 1.0 / rhohalf[idx];
-    const double idt = proj_type == kRegular ? 1.0 / dt : 0.0;
     // mkgphi (Source/hgproject.f90:605-636): gphi_d = 2^(1-dm) [phi summed over the cell's nodes
     // on its + side along d - the same on the - side] / h_d.  The cell's 2^dm nodes are read once
     // for all directions, by direct offsets where no node folds through the periodic wrap.
@@ -648,7 +657,8 @@ HG_HD inline void update_cell(const Geo& G, const Lev& L, long idx, int proj_typ
             if (b >= (1 << dm)) break;
             sg += (((b >> d) & 1) ? 1.0 : -1.0) * pv[b];
         }
-        double g = sg * (1.0 / (1 << (dm - 1))) * L.ih[d];
+        // (2^(1-dm) / h_d as one factor: the power of two scales exactly)
+        double g = sg * ((1.0 / (1 << (dm - 1))) * L.ih[d]);
         if (alt) g *= b0 ? b0[idx] : 1.0;
         double& u = unew[d * nc + idx];
         u -= g * irho;

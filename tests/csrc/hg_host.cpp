@@ -122,7 +122,8 @@ struct HostExec : HostMg<double> {
 
     void uvec() {
         for (long i = 0; i < nc(0); ++i)
-            hg::uvec_cell(geo, i, nc(0), proj_type, dt, unew, uold, gpi, rhohalf, b0, alt, sig[0].data());
+            hg::uvec_cell(geo, i, nc(0), proj_type, dt, 1.0 / dt, unew, uold, gpi, rhohalf, b0, alt,
+                          sig[0].data());
     }
     int build_levels() {
         for (int l = 1; l < nlev; ++l)
@@ -145,8 +146,8 @@ struct HostExec : HostMg<double> {
     }
     void update() {
         for (long i = 0; i < nc(0); ++i)
-            hg::update_cell(geo, L[0], i, proj_type, dt, buf(0, hg::kPhi), unew, uold, gpi,
-                            rhohalf, b0, alt);
+            hg::update_cell(geo, L[0], i, proj_type, dt, 1.0 / dt, buf(0, hg::kPhi), unew, uold,
+                            gpi, rhohalf, b0, alt);
         for (long i = 0; i < nn(0); ++i)
             hg::update_pi_node(L[0], i, proj_type, dt, buf(0, hg::kPhi), pi);
     }
