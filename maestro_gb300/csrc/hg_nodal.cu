@@ -10,8 +10,8 @@
 #include <cstring>
 #include <vector>
 
+#include "mac_internal.cuh"   // (first: hg_nodal.cuh's device code calls recip_nr)
 #include "hg_nodal.cuh"
-#include "mac_internal.cuh"
 
 namespace mac {
 
@@ -280,8 +280,9 @@ constexpr size_t tile_smem() {
     return sizeof(T) * (3 * kTRX * kTRY + 2 * kTCX * kTCY + kTFX * kTFY);
 }
 
+// (FP32: five blocks an SM, registers capped for it; FP64: two, the staged tile being twice as large)
 template <typename T, bool ISO>
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void __launch_bounds__(kTileThreads, sizeof(T) == 4 ? 5 : 2)
 k_hg_gs_tile(hg::Geo G, hg::LevT<T> L, int sp, int ntx, const T* __restrict__ src,
              const T* __restrict__ srcnb, T* __restrict__ dst, const T* __restrict__ f) {
     extern __shared__ __align__(16) unsigned char hg_tile_smem[];
@@ -1161,6 +1162,12 @@ struct HgMg {
         if (err || !dense3()) return;
         static bool attr_set = false;
         if (!attr_set) {
+            // the largest shared-memory carveout (a hint; the kernel runs with any)
+            cudaFuncSetAttribute(k_hg_gs_tile<T, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+            cudaFuncSetAttribute(k_hg_gs_tile<T, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+            (void)cudaGetLastError();   // (a refused hint leaves no error behind)
             if (cudaFuncSetAttribute(k_hg_gs_tile<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)tile_smem<T>()) != cudaSuccess ||
                 cudaFuncSetAttribute(k_hg_gs_tile<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,

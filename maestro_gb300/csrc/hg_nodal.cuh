@@ -603,12 +603,23 @@ HG_HD inline void divu_node(const Geo& G, const Lev& L, long idx, const double* 
 // create_uvec_for_projection (Source/hgproject.f90:437-513) and the solver coefficient of a
 // cell: sigma = beta0 / rhohalf (beta0^2 / rhohalf with the alt energy fix outside the initial
 // and divu projections).
+// 1 / x: on the GPU the FP64 Newton reciprocal of the MAC kernels (recip_nr, within 1 ulp of the
+// division and a fraction of its FP64 instructions; the file that launches these functions
+// includes mac_internal.cuh first), on the host the division.
+HG_HD inline double recip_cell(double x) {
+#if defined(__CUDA_ARCH__)
+    return recip_nr(x);
+#else
+    return 1.0 / x;
+#endif
+}
+
 // idt = 1 / dt, formed once by the caller.
 HG_HD inline void uvec_cell(const Geo& G, long idx, long nc, int proj_type, double dt, double idt,
                             double* unew, const double* uold, const double* gpi,
                             const double* rhohalf, const double* b0, int alt, double* sig) {
-    // one division per cell (FP64 division being slow on the GPU): 1 / rhohalf
-    const double irho = 1.0 / rhohalf[idx];
+    // one reciprocal per cell (FP64 division being slow on the GPU): 1 / rhohalf
+    const double irho = recip_cell(rhohalf[idx]);
     for (int d = 0; d < G.dm; ++d) {
         double& u = unew[d * nc + idx];
         if (proj_type == kPressureIters) u = (u - uold[d * nc + idx]) * idt;
@@ -624,8 +635,8 @@ HG_HD inline void update_cell(const Geo& G, const Lev& L, long idx, int proj_typ
                               double idt, const double* phi, double* unew, const double* uold,
                               double* gpi, const double* rhohalf, const double* b0, int alt) {
     const long nc = ncells(L);
-    // one division per cell (FP64 division being slow on the GPU): 1 / rhohalf
-    const double irho = 1.0 / rhohalf[idx];
+    // one reciprocal per cell (FP64 division being slow on the GPU): 1 / rhohalf
+    const double irho = recip_cell(rhohalf[idx]);
     // mkgphi (Source/hgproject.f90:605-636): gphi_d = 2^(1-dm) [phi summed over the cell's nodes
     // on its + side along d - the same on the - side] / h_d.  The cell's 2^dm nodes are read once
     // for all directions, by direct offsets where no node folds through the periodic wrap.
