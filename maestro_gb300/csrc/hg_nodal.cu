@@ -40,6 +40,59 @@ template <typename T>
 __global__ void k_hg_prolong(hg::Geo G, hg::LevT<T> K, hg::LevT<T> F, const T* eK, T* phiF, long N) {
     HG_LOOP(N) hg::prolong_node(G, K, F, idx, eK, phiF);
 }
+// The same prolongation in 3-D by coarse nodes (N = the coarse level's nodes): the thread of
+// coarse node P loads the 8 coarse values P + c, c in {0,1}^3 (folded through the periodic wrap)
+// once and adds to each fine node 2P + a, a in {0,1}^3, that exists and is an unknown the
+// interpolation prolong_node gives it -- the terms c <= a with weight 2^-(a0+a1+a2), in its
+// order, so the result is bitwise the same -- instead of one thread per fine node gathering its
+// own 1 to 8 parents (27 loads for the 8 fine nodes of a coarse cell instead of 8).
+template <typename T>
+__global__ void k_hg_prolong3(hg::Geo G, hg::LevT<T> K, hg::LevT<T> F, const T* __restrict__ eK,
+                              T* __restrict__ phiF, long N) {
+    HG_LOOP(N) {
+        int P[3];
+        hg::node_coords(K, idx, P);
+        int q1[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) q1[d] = hg::node_wrap(G, K, d, P[d] + 1);
+        // the 8 parents (one beyond a non-periodic face is never used: its children do not exist)
+        T e[2][2][2];
+#pragma unroll
+        for (int c2 = 0; c2 < 2; ++c2)
+#pragma unroll
+            for (int c1 = 0; c1 < 2; ++c1)
+#pragma unroll
+                for (int c0 = 0; c0 < 2; ++c0) {
+                    const int i0 = c0 ? q1[0] : P[0], i1 = c1 ? q1[1] : P[1], i2 = c2 ? q1[2] : P[2];
+                    e[c2][c1][c0] = (i0 >= 0 && i1 >= 0 && i2 >= 0) ? eK[hg::nix(K, i0, i1, i2)] : T(0);
+                }
+#pragma unroll
+        for (int a2 = 0; a2 < 2; ++a2)
+#pragma unroll
+            for (int a1 = 0; a1 < 2; ++a1)
+#pragma unroll
+                for (int a0 = 0; a0 < 2; ++a0) {
+                    const int p[3] = {2 * P[0] + a0, 2 * P[1] + a1, 2 * P[2] + a2};
+                    if (p[0] > F.n[0] || p[1] > F.n[1] || p[2] > F.n[2]) continue;
+                    if (!hg::is_unknown(G, F, p)) continue;
+                    T w = 1;
+                    if (a0) w *= (T)0.5;
+                    if (a1) w *= (T)0.5;
+                    if (a2) w *= (T)0.5;
+                    T s = 0;
+#pragma unroll
+                    for (int b2 = 0; b2 < 2; ++b2)
+#pragma unroll
+                        for (int b1 = 0; b1 < 2; ++b1)
+#pragma unroll
+                            for (int b0 = 0; b0 < 2; ++b0) {
+                                if (b2 > a2 || b1 > a1 || b0 > a0) continue;
+                                s += w * e[b2][b1][b0];
+                            }
+                    phiF[hg::nix(F, p[0], p[1], p[2])] += s;
+                }
+    }
+}
 __global__ void k_hg_coarsen(hg::Geo G, hg::Lev F, hg::Lev K, double* sK, long N) {
     HG_LOOP(N) hg::coarsen_sig_cell(G, F, K, idx, sK);
 }
@@ -271,6 +324,63 @@ __device__ __forceinline__ void stage_elem(T* dst, const T* src, bool inside) {
 }
 __device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
+// node_op_dense3's formula on staged arrays, for every node of a tile: the staged values are
+// folded through the periodic wrap and 0 outside a non-periodic face (sigma and phi), so the
+// missing neighbours of a face node carry weight 0 here as well.  ss: the node's cell (-1,-1,-1)
+// in a cell array of row pitch CX and layer pitch CP; ph: its node (-1,-1,-1) in a node array of
+// row pitch RX and plane pitch RP.
+template <typename T, bool ISO, int RX, int RP, int CX, int CP>
+__device__ __forceinline__ void staged_node_op(const hg::LevT<T>& L, const T* ss, const T* ph, T& dg,
+                                               T& off) {
+    T s[2][2][2];
+#pragma unroll
+    for (int zz = 0; zz < 2; ++zz)
+#pragma unroll
+        for (int yy = 0; yy < 2; ++yy)
+#pragma unroll
+            for (int xx = 0; xx < 2; ++xx) s[zz][yy][xx] = ss[xx + CX * yy + CP * zz];
+    T sx[2][2][3];
+#pragma unroll
+    for (int zz = 0; zz < 2; ++zz)
+#pragma unroll
+        for (int yy = 0; yy < 2; ++yy) {
+            sx[zz][yy][0] = s[zz][yy][0];
+            sx[zz][yy][1] = s[zz][yy][0] + s[zz][yy][1];
+            sx[zz][yy][2] = s[zz][yy][1];
+        }
+    T sxy[2][3][3];
+#pragma unroll
+    for (int zz = 0; zz < 2; ++zz)
+#pragma unroll
+        for (int ox = 0; ox < 3; ++ox) {
+            sxy[zz][0][ox] = sx[zz][0][ox];
+            sxy[zz][1][ox] = sx[zz][0][ox] + sx[zz][1][ox];
+            sxy[zz][2][ox] = sx[zz][1][ox];
+        }
+    T am[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    T centre = 0;
+#pragma unroll
+    for (int oz = 0; oz < 3; ++oz)
+#pragma unroll
+        for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+            for (int ox = 0; ox < 3; ++ox) {
+                const T S = oz == 0 ? sxy[0][oy][ox]
+                                    : (oz == 2 ? sxy[1][oy][ox] : sxy[0][oy][ox] + sxy[1][oy][ox]);
+                const int mask = (ox != 1 ? 1 : 0) | (oy != 1 ? 2 : 0) | (oz != 1 ? 4 : 0);
+                if (mask == 0)
+                    centre = S;
+                else if (!(ISO && (mask == 1 || mask == 2 || mask == 4)))
+                    am[mask] = fma(S, ph[ox + RX * oy + RP * oz], am[mask]);
+            }
+    T acc = 0;
+#pragma unroll
+    for (int m = 1; m < 8; ++m)
+        if (!(ISO && (m == 1 || m == 2 || m == 4))) acc = fma(L.kw[m], am[m], acc);
+    dg = -L.kw[0] * centre;
+    off = acc;
+}
+
 constexpr int kTileX = 32, kTileY = 32, kTileH = 4, kTileThreads = 384;
 constexpr int kTRX = kTileX + 2 * kTileH, kTRY = kTileY + 2 * kTileH;           // staged nodes
 constexpr int kTCX = kTileX + 2 * kTileH - 1, kTCY = kTileY + 2 * kTileH - 1;   // staged cells
@@ -377,57 +487,9 @@ k_hg_gs_tile(hg::Geo G, hg::LevT<T> L, int sp, int ntx, const T* __restrict__ sr
         for (int e = t; e < nx * ny; e += kTileThreads) {
             const int lx = xs - (x0 - kTileH) + 2 * (e % nx), ly = ys - (y0 - kTileH) + 2 * (e / nx);
             if (!(sux[lx] && suy[ly] && uz)) continue;
-            T s[2][2][2];
-#pragma unroll
-            for (int zz = 0; zz < 2; ++zz)
-#pragma unroll
-                for (int yy = 0; yy < 2; ++yy)
-#pragma unroll
-                    for (int xx = 0; xx < 2; ++xx)
-                        s[zz][yy][xx] = ssig[(lx - 1 + xx) + kTCX * ((ly - 1 + yy) + kTCY * zz)];
-            T sx[2][2][3];
-#pragma unroll
-            for (int zz = 0; zz < 2; ++zz)
-#pragma unroll
-                for (int yy = 0; yy < 2; ++yy) {
-                    sx[zz][yy][0] = s[zz][yy][0];
-                    sx[zz][yy][1] = s[zz][yy][0] + s[zz][yy][1];
-                    sx[zz][yy][2] = s[zz][yy][1];
-                }
-            T sxy[2][3][3];
-#pragma unroll
-            for (int zz = 0; zz < 2; ++zz)
-#pragma unroll
-                for (int ox = 0; ox < 3; ++ox) {
-                    sxy[zz][0][ox] = sx[zz][0][ox];
-                    sxy[zz][1][ox] = sx[zz][0][ox] + sx[zz][1][ox];
-                    sxy[zz][2][ox] = sx[zz][1][ox];
-                }
-            const T* ph = sphi + (lx - 1) + kTRX * (ly - 1);
-            // node_op_dense3's formula for every node: the staged values are folded through the
-            // periodic wrap and 0 outside a non-periodic face (sigma and phi), so the missing
-            // neighbours of a face node carry weight 0 here as well
-            T am[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            T centre = 0;
-#pragma unroll
-            for (int oz = 0; oz < 3; ++oz)
-#pragma unroll
-                for (int oy = 0; oy < 3; ++oy)
-#pragma unroll
-                    for (int ox = 0; ox < 3; ++ox) {
-                        const T S = oz == 0 ? sxy[0][oy][ox]
-                                            : (oz == 2 ? sxy[1][oy][ox] : sxy[0][oy][ox] + sxy[1][oy][ox]);
-                        const int mask = (ox != 1 ? 1 : 0) | (oy != 1 ? 2 : 0) | (oz != 1 ? 4 : 0);
-                        if (mask == 0)
-                            centre = S;
-                        else if (!(ISO && (mask == 1 || mask == 2 || mask == 4)))
-                            am[mask] = fma(S, ph[ox + kTRX * (oy + kTRY * oz)], am[mask]);
-                    }
-            T off = 0;
-#pragma unroll
-            for (int m = 1; m < 8; ++m)
-                if (!(ISO && (m == 1 || m == 2 || m == 4))) off = fma(L.kw[m], am[m], off);
-            const T dg = -L.kw[0] * centre;
+            T dg, off;
+            staged_node_op<T, ISO, kTRX, kTRX * kTRY, kTCX, kTCX * kTCY>(
+                L, ssig + (lx - 1) + kTCX * (ly - 1), sphi + (lx - 1) + kTRX * (ly - 1), dg, off);
             const int fi = (lx - 1) + kTFX * (ly - 1);
             sphi[lx + kTRX * (ly + kTRY)] = (sf[fi] + off) / dg;
         }
@@ -440,6 +502,99 @@ k_hg_gs_tile(hg::Geo G, hg::LevT<T> L, int sp, int ntx, const T* __restrict__ sr
         if (!hg::is_unknown(G, L, p)) continue;
         dst[hg::nix(L, p[0], p[1], p[2])] =
             sphi[(p[0] - x0 + kTileH) + kTRX * ((p[1] - y0 + kTileH) + kTRY)];
+    }
+}
+
+// ---- tiled defect of the fine 3-D dense levels ---------------------------------------------
+// r = f - L phi on the unknown nodes, 0 on the other nodes of the domain (periodic images are
+// left as they are: nothing reads them).  A block owns a kDefX x kDefY tile of one slab: it stages
+// the slab and its two neighbour slabs over the tile grown by one node and the two cell layers
+// (folded through the periodic wrap, 0 outside the domain) and forms each node's defect with
+// staged_node_op -- the arithmetic of node_op_dense3 for every node, so interior nodes get
+// k_hg_defect3's result bitwise and nodes next to a face its terms in another order -- instead
+// of one thread per node reading its 35 operands through the cache.
+constexpr int kDefX = 32, kDefY = 32, kDefThreads = 256;
+constexpr int kDRX = kDefX + 2, kDRY = kDefY + 2;   // staged nodes
+constexpr int kDCX = kDefX + 1, kDCY = kDefY + 1;   // staged cells
+template <typename T>
+constexpr size_t deftile_smem() {
+    return sizeof(T) * (3 * kDRX * kDRY + 2 * kDCX * kDCY);
+}
+
+template <typename T, bool ISO>
+__global__ void __launch_bounds__(kDefThreads)
+k_hg_defect_tile(hg::Geo G, hg::LevT<T> L, int ntx, const T* __restrict__ phi,
+                 const T* __restrict__ f, T* __restrict__ r) {
+    extern __shared__ __align__(16) unsigned char hg_deftile_smem[];
+    T* sphi = reinterpret_cast<T*>(hg_deftile_smem);   // [3][kDRY][kDRX], slabs z-1, z, z+1
+    T* ssig = sphi + 3 * kDRX * kDRY;                   // [2][kDCY][kDCX], cell layers z-1, z
+    const int z = (int)blockIdx.y;                      // 0 .. the slabs with unknown nodes - 1
+    const int x0 = kDefX * ((int)blockIdx.x % ntx), y0 = kDefY * ((int)blockIdx.x / ntx);
+    const int t = threadIdx.x;
+    __shared__ int sqx[kDRX], sqy[kDRY], scx[kDCX], scy[kDCY];
+    if (t < kDRX) {
+        const int raw = x0 - 1 + t;
+        sqx[t] = hg::node_wrap(G, L, 0, raw);
+        if (t < kDCX) scx[t] = hg::cell_wrap(G, L, 0, raw);
+    } else if (t >= 64 && t < 64 + kDRY) {
+        const int u = t - 64, raw = y0 - 1 + u;
+        sqy[u] = hg::node_wrap(G, L, 1, raw);
+        if (u < kDCY) scy[u] = hg::cell_wrap(G, L, 1, raw);
+    }
+    const int qz0 = hg::node_wrap(G, L, 2, z - 1), qz1 = hg::node_wrap(G, L, 2, z),
+              qz2 = hg::node_wrap(G, L, 2, z + 1);
+    const int cz0 = hg::cell_wrap(G, L, 2, z - 1), cz1 = hg::cell_wrap(G, L, 2, z);
+    __syncthreads();
+    const long m01 = (long)L.nn[0] * L.nn[1], c01 = (long)L.n[0] * L.n[1];
+    // stage, one column a thread (its folded x in a register), rows kPR apart
+    constexpr int kPR = kDefThreads / kDRX;
+    if (t < kPR * kDRX) {
+        const int lx = t % kDRX, r0 = t / kDRX;
+        const int q0 = sqx[lx];
+        const int im0 = L.nn[0], ic0 = L.n[0];
+#pragma unroll 1
+        for (int lz = 0; lz < 3; ++lz) {
+            const int q2 = lz == 0 ? qz0 : (lz == 1 ? qz1 : qz2);
+            const bool zin = q0 >= 0 && q2 >= 0;
+            const T* pb = phi + (zin ? q0 + q2 * m01 : 0);
+            T* dst_col = sphi + lz * (kDRX * kDRY) + lx;
+            for (int ly = r0; ly < kDRY; ly += kPR) {
+                const int q1 = sqy[ly];
+                const bool in = zin && q1 >= 0;
+                stage_elem(dst_col + ly * kDRX, in ? pb + (long)q1 * im0 : phi, in);
+            }
+        }
+        if (lx < kDCX) {
+            const int c0 = scx[lx];
+#pragma unroll 1
+            for (int lz = 0; lz < 2; ++lz) {
+                const int c2 = lz == 0 ? cz0 : cz1;
+                const bool zin = c0 >= 0 && c2 >= 0;
+                const T* pb = L.sig + (zin ? c0 + c2 * c01 : 0);
+                T* dst_col = ssig + lz * (kDCX * kDCY) + lx;
+                for (int ly = r0; ly < kDCY; ly += kPR) {
+                    const int c1 = scy[ly];
+                    const bool in = zin && c1 >= 0;
+                    stage_elem(dst_col + ly * kDCX, in ? pb + (long)c1 * ic0 : L.sig, in);
+                }
+            }
+        }
+    }
+    stage_wait();
+    __syncthreads();
+    for (int e = t; e < kDefX * kDefY; e += kDefThreads) {
+        const int lx = 1 + e % kDefX, ly = 1 + e / kDefX;
+        const int p[3] = {x0 + lx - 1, y0 + ly - 1, z};
+        if (p[0] > L.n[0] - (G.per[0] ? 1 : 0) || p[1] > L.n[1] - (G.per[1] ? 1 : 0)) continue;
+        const long i = hg::nix(L, p[0], p[1], p[2]);
+        if (!hg::is_unknown(G, L, p)) {
+            r[i] = 0;
+            continue;
+        }
+        T dg, off;
+        staged_node_op<T, ISO, kDRX, kDRX * kDRY, kDCX, kDCX * kDCY>(
+            L, ssig + (lx - 1) + kDCX * (ly - 1), sphi + (lx - 1) + kDRX * (ly - 1), dg, off);
+        r[i] = f[i] - (dg * sphi[lx + kDRX * (ly + kDRY)] - off);
     }
 }
 
@@ -1071,7 +1226,16 @@ struct HgMg {
         if (tm) span_end(a, MAC_KT_RESID, before);
     }
     void defect_launch(int l, const T* phi, const T* f, T* r) {
-        if (dense3() && iso(l))
+        const hg::LevT<T>& L = lev(l);
+        if (dense3() && (L.nn[0] + 1) / 2 * ((L.nn[1] + 1) / 2) > kSlabThreads) {
+            // the fine levels (those the Gauss-Seidel sweeps by tiles): by tiles
+            const int ntx = (L.n[0] + (geo.per[0] ? 0 : 1) + kDefX - 1) / kDefX;
+            const int nty = (L.n[1] + (geo.per[1] ? 0 : 1) + kDefY - 1) / kDefY;
+            const int nzu = L.n[2] + (geo.per[2] ? 0 : 1);
+            const dim3 grid((unsigned)(ntx * nty), (unsigned)nzu);
+            auto kern = iso(l) ? k_hg_defect_tile<T, true> : k_hg_defect_tile<T, false>;
+            kern<<<grid, kDefThreads, deftile_smem<T>(), c->stream>>>(geo, L, ntx, phi, f, r);
+        } else if (dense3() && iso(l))
             k_hg_defect3<T, true><<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), phi, f, r, nn(l));
         else if (dense3())
             k_hg_defect3<T, false><<<blocks(nn(l)), kThreads, 0, c->stream>>>(geo, lev(l), phi, f, r, nn(l));
@@ -1205,7 +1369,11 @@ struct HgMg {
         launched();
     }
     void prolong(int lc, const T* eK, T* phiF) {
-        k_hg_prolong<T><<<blocks(nn(lc - 1)), kThreads, 0, c->stream>>>(geo, lev(lc), lev(lc - 1), eK, phiF, nn(lc - 1));
+        if (geo.dm == 3)
+            k_hg_prolong3<T><<<blocks(nn(lc)), kThreads, 0, c->stream>>>(geo, lev(lc), lev(lc - 1), eK, phiF, nn(lc));
+        else
+            k_hg_prolong<T><<<blocks(nn(lc - 1)), kThreads, 0, c->stream>>>(geo, lev(lc), lev(lc - 1), eK, phiF,
+                                                                              nn(lc - 1));
         launched();
     }
     void zero(int l, T* x) {

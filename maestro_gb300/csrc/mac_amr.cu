@@ -80,24 +80,36 @@ __global__ void k_add_region(amr::LevT<T> L, T* phi, const T* uu, long N) {
 template <typename T>
 __global__ void k_reduce(amr::LevT<T> L, const T* x, double vol, int valid_only, double* part,
                          long N) {
-    __shared__ double s_sum[kThreads / 32], s_max[kThreads / 32], s_nan[kThreads / 32],
-        s_vol[kThreads / 32];
-    double sum = 0.0, mx = 0.0, nan = 0.0, v = 0.0;
+    // Only the volume-weighted sum is FP64 arithmetic: the NaN test and the maximum of |x| work
+    // on the IEEE bits (for non-negative doubles the unsigned order of the bits is the numeric
+    // order), the cells are counted as integers and the volume is vol x count, a float's
+    // widening takes the integer pipe: GB300's FP64 pipe is the narrow one.
+    __shared__ double s_sum[kThreads / 32], s_vol[kThreads / 32];
+    __shared__ unsigned long long s_max[kThreads / 32], s_nan[kThreads / 32];
+    double sum = 0.0;
+    unsigned long long mx = 0, nan = 0, cnt = 0;
     AMR_LOOP(N) {
         const bool take = valid_only ? amr::is_valid(L, idx) : amr::in_region(L, idx);
         if (!take) continue;
-        const double a = (double)x[idx];
-        if (a != a) {
-            nan += 1.0;
+        double a;
+        if (std::is_same<T, float>::value)
+            a = to_double((float)x[idx]);
+        else
+            a = (double)x[idx];
+        const unsigned long long b = (unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull;
+        if (b > 0x7ff0000000000000ull) {
+            ++nan;
             continue;
         }
-        sum += vol * a;
-        mx = fmax(mx, fabs(a));
-        v += vol;
+        sum = fma(vol, a, sum);
+        mx = b > mx ? b : mx;
+        ++cnt;
     }
+    double v = vol * (double)cnt;
     for (int o = 16; o > 0; o >>= 1) {
         sum += __shfl_down_sync(0xffffffffu, sum, o);
-        mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+        const unsigned long long m = __shfl_down_sync(0xffffffffu, mx, o);
+        mx = m > mx ? m : mx;
         nan += __shfl_down_sync(0xffffffffu, nan, o);
         v += __shfl_down_sync(0xffffffffu, v, o);
     }
@@ -112,14 +124,14 @@ __global__ void k_reduce(amr::LevT<T> L, const T* x, double vol, int valid_only,
     if (threadIdx.x == 0) {
         for (int q = 1; q < kThreads / 32; ++q) {
             sum += s_sum[q];
-            mx = fmax(mx, s_max[q]);
+            mx = s_max[q] > mx ? s_max[q] : mx;
             nan += s_nan[q];
             v += s_vol[q];
         }
         double* p = part + 4 * blockIdx.x;
         p[0] = sum;
-        p[1] = mx;
-        p[2] = nan;
+        p[1] = __longlong_as_double((long long)mx);
+        p[2] = (double)nan;
         p[3] = v;
     }
 }
