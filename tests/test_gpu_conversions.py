@@ -28,7 +28,7 @@ def test_conversions_match_hardware(cuda_lib):
 
 def test_recip_nr_within_one_ulp_of_division(cuda_lib):
     """recip_nr (reciprocal estimate + one third-order Newton step, used in place of the FP64
-    division by the coefficient and bottom kernels) is within 1 ulp of the IEEE division 1.0/x
+    division by the coefficient and bottom kernels and the nodal cell kernels' 1/rhohalf) is within 1 ulp of the IEEE division 1.0/x
     on every input it refines (biased exponents 64..1980), and inputs outside that range take the
     division itself (bitwise equal)."""
     import re
