@@ -213,12 +213,16 @@ AMR_HD inline void cell_op(const Geo& G, const LevT<T>& L, const LevT<T>& C, con
     }
 }
 
+// Box coordinates of a cell index.  32-bit unsigned division (several times cheaper than 64-bit
+// on the GPU): a level holds at most 2^31 cells, checked where the hierarchy is built, and its
+// face arrays fewer than 2^32 entries.
 template <typename T>
 AMR_HD inline void cell_coords(const LevT<T>& L, long idx, int c[3]) {
-    c[0] = L.lo[0] + (int)(idx % L.ext[0]);
-    const long r = idx / L.ext[0];
-    c[1] = L.lo[1] + (int)(r % L.ext[1]);
-    c[2] = L.lo[2] + (int)(r / L.ext[1]);
+    const unsigned u = (unsigned)idx, e0 = (unsigned)L.ext[0], e1 = (unsigned)L.ext[1];
+    const unsigned r = u / e0, k = r / e1;
+    c[0] = L.lo[0] + (int)(u - r * e0);
+    c[1] = L.lo[1] + (int)(r - k * e1);
+    c[2] = L.lo[2] + (int)k;
 }
 
 // r = f - L u on a region cell, 0 elsewhere.
@@ -246,11 +250,11 @@ AMR_HD inline long colour_threads(const LevT<T>& L) {
 }
 template <typename T>
 AMR_HD inline long colour_cell(const LevT<T>& L, long t, int colour) {
-    const int hw = (L.ext[0] + 1) / 2;
-    const long row = t / hw;
-    const int j = (int)(row % L.ext[1]), k = (int)(row / L.ext[1]);
+    const unsigned hw = (unsigned)(L.ext[0] + 1) / 2, e1 = (unsigned)L.ext[1];
+    const unsigned ut = (unsigned)t, row = ut / hw, kk = row / e1;
+    const int j = (int)(row - kk * e1), k = (int)kk;
     const int x0 = (colour + L.lo[0] + L.lo[1] + j + L.lo[2] + k) & 1;
-    const int x = 2 * (int)(t % hw) + x0;
+    const int x = 2 * (int)(ut - row * hw) + x0;
     if (x >= L.ext[0]) return -1;
     return (long)x + (long)L.ext[0] * ((long)j + (long)L.ext[1] * k);
 }
@@ -386,11 +390,11 @@ AMR_HD inline bool face_in_level(const Geo& G, const LevT<T>& L, int d, const in
 
 template <typename T>
 AMR_HD inline void face_coords(const LevT<T>& L, int d, long idx, int f[3]) {
-    const int m0 = L.ext[0] + (d == 0), m1 = L.ext[1] + (d == 1);
-    f[0] = L.lo[0] + (int)(idx % m0);
-    const long r = idx / m0;
-    f[1] = L.lo[1] + (int)(r % m1);
-    f[2] = L.lo[2] + (int)(r / m1);
+    const unsigned m0 = (unsigned)(L.ext[0] + (d == 0)), m1 = (unsigned)(L.ext[1] + (d == 1));
+    const unsigned u = (unsigned)idx, r = u / m0, k = r / m1;
+    f[0] = L.lo[0] + (int)(u - r * m0);
+    f[1] = L.lo[1] + (int)(r - k * m1);
+    f[2] = L.lo[2] + (int)k;
 }
 
 // ml_edge_restriction of one coarse face (direction d): the mean of the fine faces tiling it,
