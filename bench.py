@@ -229,8 +229,16 @@ def link_rates(dev, nbytes=1 << 29, reps=3):
 
 
 def mac_config(name, n, box, world):
+    # a timed step's own inputs: the face velocities and phi, a distinct copy per step
+    cells = 1
+    for v in n:
+        cells *= v
+    faces = sum(cells // v * (v + 1) for v in n)
+    mb = 8 * (faces + cells) / 1e6
+    size = f"{mb / 1e3:.2g} GB" if mb >= 100 else f"{mb:.3g} MB"
+    where = "larger than" if mb > 129 else "within"
     return {"workload": name, "n": list(n), "box": list(box), "rel_eps": 1e-10,
-            "l2": "inputs larger than L2 (0.5 GB per step, a distinct copy per step)",
+            "l2": f"inputs {where} L2 ({size} per step, a distinct copy per step)",
             "parallelism": f"replicas x{world}"}
 
 
