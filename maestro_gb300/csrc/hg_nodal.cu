@@ -1324,8 +1324,7 @@ struct HgMg {
     // shared-memory limit, set up outside any stream capture.
     void prepare_tiles() {
         if (err || !dense3()) return;
-        static bool attr_set = false;
-        if (!attr_set) {
+        {   // (per call, a few host calls: a process-wide flag would skip a second device)
             // the largest shared-memory carveout (a hint; the kernel runs with any)
             cudaFuncSetAttribute(k_hg_gs_tile<T, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared);
@@ -1340,7 +1339,6 @@ struct HgMg {
                 err = MAC_ERR_CUDA;
                 return;
             }
-            attr_set = true;
         }
         for (int l = 0; l < nlev; ++l) {
             const hg::LevT<T>& L = lev(l);

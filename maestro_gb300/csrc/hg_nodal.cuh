@@ -390,7 +390,7 @@ HG_HD inline void restrict_node(const Geo& G, const LevT<T>& F, const LevT<T>& K
                     if (a2) w *= (T)0.5;
                     s += w * r[a0 + a1 * st1 + a2 * st2];
                 }
-        fK[idx] = s / (T)(1 << dm);
+        fK[idx] = s * (dm == 3 ? (T)0.125 : (dm == 2 ? (T)0.25 : (T)0.5));   // 2^-dm, exact
         return;
     }
     // (static bounds, the same terms in the same order: the small arrays stay in registers)
@@ -415,7 +415,7 @@ HG_HD inline void restrict_node(const Geo& G, const LevT<T>& F, const LevT<T>& K
                 }
                 if (!out) s += w * rF[nix(F, q[0], q[1], q[2])];
             }
-    fK[idx] = s / (T)(1 << dm);
+    fK[idx] = s * (dm == 3 ? (T)0.125 : (dm == 2 ? (T)0.25 : (T)0.5));   // 2^-dm, exact
 }
 
 // Fine unknowns += multilinear interpolation of the coarse correction.
