@@ -571,7 +571,9 @@ k_resid64_to32(Dims F, const double* __restrict__ u, const double* __restrict__ 
     if (threadIdx.x == 0 && threadIdx.y == 0 && m) atomicMax(maxbits, m);
 }
 
-// phi += e, four cells a thread (n % 4 == 0; the level-0 arrays always qualify), else one.
+// phi += e, four cells a thread (n % 4 == 0; the level-0 arrays always qualify), else one.  The
+// FP32 -> FP64 widening takes the integer pipe (to_double), leaving the add the only FP64
+// instruction of a cell.
 template <int V>
 __global__ void __launch_bounds__(kBlock)
 k_accumulate(int n, double* __restrict__ u, const float* __restrict__ e) {
@@ -583,14 +585,14 @@ k_accumulate(int n, double* __restrict__ u, const float* __restrict__ e) {
         const float4 ev = *reinterpret_cast<const float4*>(e + q);
         double2 a = *reinterpret_cast<const double2*>(u + q);
         double2 b = *reinterpret_cast<const double2*>(u + q + 2);
-        a.x += (double)ev.x;
-        a.y += (double)ev.y;
-        b.x += (double)ev.z;
-        b.y += (double)ev.w;
+        a.x += to_double(ev.x);
+        a.y += to_double(ev.y);
+        b.x += to_double(ev.z);
+        b.y += to_double(ev.w);
         *reinterpret_cast<double2*>(u + q) = a;
         *reinterpret_cast<double2*>(u + q + 2) = b;
     } else {
-        u[q] += (double)e[q];
+        u[q] += to_double(e[q]);
     }
 }
 
