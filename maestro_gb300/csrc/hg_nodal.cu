@@ -268,21 +268,6 @@ __device__ __forceinline__ void node_op_dense3_face(const hg::Geo& G, const hg::
     off = acc;
 }
 
-template <typename T>
-__global__ void k_hg_gs3(hg::Geo G, hg::LevT<T> L, int colour, T* phi, const T* f, long N) {
-    HG_LOOP(N) {
-        int p[3];
-        hg::colour_node(G, L, colour, idx, p);
-        if (!hg::is_unknown(G, L, p)) continue;
-        T dg, off;
-        if (interior3(L, p))
-            node_op_dense3(L, p, phi, dg, off);
-        else
-            node_op_dense3_face(G, L, p, phi, dg, off);
-        const long i = hg::nix(L, p[0], p[1], p[2]);
-        phi[i] = (f[i] + off) / dg;
-    }
-}
 // One half of a colour-ordered Gauss-Seidel sweep, by slabs.  The colours are the node-parity
 // patterns, colour = p_0 + 2 p_1 (+ 4 p_2), updated in that order; the slab direction is the last
 // active one (z in 3-D, y in 2-D).  A node's neighbours along the slab direction have the other
@@ -307,7 +292,7 @@ __global__ void k_hg_gs3(hg::Geo G, hg::LevT<T> L, int colour, T* phi, const T* 
 // fold through the periodic wrap when staged; outside a non-periodic face the staged values are
 // 0, so every node, next to a face or not, takes node_op_dense3's arithmetic on the staged
 // values: the missing neighbours of a face node carry weight 0 (a single formula keeps the
-// warps of the tiles along a face from running two; the colour launches take
+// warps of the tiles along a face from running two; the slab sweeps of the coarser levels take
 // node_op_dense3_face there, the same terms summed in another order).
 
 // One element global -> shared without passing through registers (cp.async, 4 or 8 bytes);
@@ -1269,10 +1254,7 @@ struct HgMg {
             for (int s = 0; s < nu; ++s)
                 for (int colour = 0; colour < (1 << dm); ++colour) {
                     const long m = hg::colour_count(geo, L, colour);
-                    if (dense3())
-                        k_hg_gs3<T><<<blocks(m), kThreads, 0, c->stream>>>(geo, L, colour, phi, f, m);
-                    else
-                        k_hg_gs<T><<<blocks(m), kThreads, 0, c->stream>>>(geo, L, colour, phi, f, m);
+                    k_hg_gs<T><<<blocks(m), kThreads, 0, c->stream>>>(geo, L, colour, phi, f, m);
                     launched();
                 }
             return;
