@@ -160,6 +160,20 @@ hg::Wall g_wall{nullptr, {-1, -1, -1, -1, -1, -1}};
 
 extern "C" {
 
+// The dense stencil's weight table (set_dense_weights) of a level with spacing h, in FP64 and
+// as the FP32 levels hold it: kw64[8], kw32[8].
+void hgh_dense_weights(int dm, const double* h, double* kw64, float* kw32) {
+    hg::LevT<double> L{};
+    hg::LevT<float> L32{};
+    for (int d = 0; d < 3; ++d) L.h[d] = L32.h[d] = h[d];
+    hg::set_dense_weights(dm, L);
+    hg::set_dense_weights(dm, L32);
+    for (int x = 0; x < 8; ++x) {
+        kw64[x] = L.kw[x];
+        kw32[x] = L32.kw[x];
+    }
+}
+
 // Inflow faces for the following hgh_project* calls: off[f] >= 0 marks face f = 2 d + side as an
 // inflow face with its wall values at w + off[f] (hg::Wall); off NULL: none.
 void hgh_set_wall(const long* off, const double* w) {

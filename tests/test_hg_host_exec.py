@@ -201,6 +201,24 @@ def test_node_row_reproduces_node_op(host_lib, dm, n, per, dlo, dhi, dense):
     assert err <= 1e-14, err
 
 
+@pytest.mark.parametrize("n", [2, 7, 16, 100, 128, 256, 384, 512, 1000, 4096])
+def test_isotropic_dense_weights_of_the_axis_neighbours_are_exactly_zero(host_lib, n):
+    """The GPU's dense 3-D kernels leave out the six axis neighbours on a level whose weights
+    kw[1], kw[2], kw[4] are exactly 0 (fma(0, a, acc) = acc: bitwise the full stencil).  On an
+    isotropic level they are, in FP64 and in the FP32 levels' rounding, for spacings that are
+    not powers of two as well; on an anisotropic level they are not, and the kernels keep them."""
+    L = host_lib
+    kw64 = (ctypes.c_double * 8)()
+    kw32 = (ctypes.c_float * 8)()
+    for h in (1.0 / n, 0.7 / n, 3.0 / n):
+        L.hgh_dense_weights(3, (ctypes.c_double * 3)(h, h, h), kw64, kw32)
+        assert [kw64[m] for m in (1, 2, 4)] == [0.0, 0.0, 0.0]
+        assert [kw32[m] for m in (1, 2, 4)] == [0.0, 0.0, 0.0]
+        assert all(kw64[m] != 0.0 for m in (0, 3, 5, 6, 7))
+    L.hgh_dense_weights(3, (ctypes.c_double * 3)(1.0 / n, 1.0 / n, 2.0 / n), kw64, kw32)
+    assert any(kw64[m] != 0.0 for m in (1, 2, 4))
+
+
 @pytest.mark.parametrize("inner", [0, 2])
 @pytest.mark.parametrize("name", sorted(G.HG_INFLOW_CASES))
 def test_library_hg_code_on_host_inflow_matches_golden(host_lib, name, inner):
