@@ -292,6 +292,47 @@ void build(HostExec& E, const orc_opts* o, int nlev, const int* nboxes, const in
 
 extern "C" {
 
+// Cell, colour and face coordinates of a level array box (the 32-bit index arithmetic of
+// mac_amr.cuh) against plain 64-bit arithmetic on every index: the number of mismatches.
+long amrh_coords_check(const int* lo, const int* ext) {
+    amr::Lev L{};
+    for (int d = 0; d < 3; ++d) {
+        L.lo[d] = lo[d];
+        L.ext[d] = ext[d];
+        L.n[d] = lo[d] + ext[d];
+    }
+    long bad = 0;
+    const long nc = (long)ext[0] * ext[1] * ext[2];
+    for (long idx = 0; idx < nc; ++idx) {
+        int c[3];
+        amr::cell_coords(L, idx, c);
+        const long r = idx / ext[0];
+        bad += c[0] != lo[0] + (int)(idx % ext[0]) || c[1] != lo[1] + (int)(r % ext[1]) ||
+               c[2] != lo[2] + (int)(r / ext[1]);
+    }
+    for (int d = 0; d < 3; ++d) {
+        const long m0 = ext[0] + (d == 0), m1 = ext[1] + (d == 1), m2 = ext[2] + (d == 2);
+        for (long idx = 0; idx < m0 * m1 * m2; ++idx) {
+            int f[3];
+            amr::face_coords(L, d, idx, f);
+            const long r = idx / m0;
+            bad += f[0] != lo[0] + (int)(idx % m0) || f[1] != lo[1] + (int)(r % m1) ||
+                   f[2] != lo[2] + (int)(r / m1);
+        }
+    }
+    const long hw = (ext[0] + 1) / 2;
+    for (int colour = 0; colour < 2; ++colour)
+        for (long t = 0; t < amr::colour_threads(L); ++t) {
+            const long row = t / hw;
+            const int j = (int)(row % ext[1]), k = (int)(row / ext[1]);
+            const int x0 = (colour + lo[0] + lo[1] + j + lo[2] + k) & 1;
+            const int x = 2 * (int)(t % hw) + x0;
+            const long want = x >= ext[0] ? -1 : (long)x + (long)ext[0] * ((long)j + (long)ext[1] * k);
+            bad += amr::colour_cell(L, t, colour) != want;
+        }
+    return bad;
+}
+
 // The library's multi-level projection run on the host; arguments as orc_macproject_ml
 // (phi[l] in/out, umac[3 l + d] in/out).  Returns the solve status (0 converged).
 int amrh_macproject_prec(const orc_opts* o, int nlev, const int* nboxes, const int* boxes,

@@ -204,3 +204,16 @@ def test_smoother_colour_map_covers_each_colour_once(host_lib, dm, lo, ext):
     # the compact GS-RB launch: one thread per cell of the colour, odd extents and offset boxes
     ia = lambda v: (ctypes.c_int * 3)(*(list(v) + [0] * (3 - len(v))))  # noqa: E731
     assert host_lib.amrh_check_colour_map(dm, ia(lo), ia(ext)) == 0
+
+
+@pytest.mark.parametrize("lo,ext", [((0, 0, 0), (130, 130, 130)), ((5, 3, 7), (37, 11, 9)),
+                                    ((63, 0, 1), (1, 70, 3)), ((0, 0, 0), (2, 1, 1)),
+                                    ((11, 2, 0), (13, 17, 1))])
+def test_index_coordinates_match_64_bit_arithmetic(host_lib, lo, ext):
+    """The level helpers' 32-bit divisions (cell, face and colour coordinates) give the 64-bit
+    arithmetic's results on every index of the array box, odd extents and 2-D boxes included."""
+    L = host_lib
+    L.amrh_coords_check.restype = ctypes.c_long
+    ia = lambda v: (ctypes.c_int * 3)(*v)  # noqa: E731
+    assert L.amrh_coords_check(ia(lo), ia(ext)) == 0
+
